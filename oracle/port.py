@@ -1,0 +1,135 @@
+"""TEST INFRASTRUCTURE ONLY: ctypes view of the C restatement (sl_oracle.c).
+
+The library is built by `make -C oracle port` (also run by
+__graft_entry__.build()) into oracle/_build/libsloracle.so.  Only tests/,
+__graft_entry__.smoke() and bench.py's CPU-baseline leg use it, as the checker
+or as the timed CPU port; the product path never does.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libsloracle.so")
+
+_lib = None
+
+
+def build() -> str:
+    subprocess.run(["make", "-s", "-C", _HERE, "port"], check=True)
+    return LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        _lib = ctypes.CDLL(LIB_PATH)
+        _lib.slo_fag_likelihood.restype = ctypes.c_double
+        _lib.slo_loglik.restype = ctypes.c_double
+        _lib.slo_philox_uniform.restype = ctypes.c_double
+        _lib.slo_philox_uniform.argtypes = [ctypes.c_uint64] * 3
+    return _lib
+
+
+class _Problem(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int) for n in ("N", "F", "M", "K", "n_lod")] + [
+        (n, ctypes.c_void_p) for n in (
+            "mother", "father", "sex", "geno", "typed", "legal", "prior", "dprob", "theta",
+            "partial", "minor", "op_type", "op_peel", "cut_off", "cut", "prev_off", "prev",
+            "ch_off", "ch")
+    ]
+
+
+def _csr(lists):
+    off = np.zeros(len(lists) + 1, np.int32)
+    for i, x in enumerate(lists):
+        off[i + 1] = off[i] + len(x)
+    flat = np.concatenate([np.asarray(x, np.int32) for x in lists]) if off[-1] else np.zeros(1, np.int32)
+    return off, flat.astype(np.int32)
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+class Port:
+    """Holds the arrays of one problem (a dict of numpy arrays, see tests/golden)."""
+
+    def __init__(self, prob: dict):
+        self.keep = {}
+        g = lambda k, dt: self.keep.setdefault(k, np.ascontiguousarray(prob[k], dt))
+        self.N, self.F, self.M = int(prob["N"]), int(prob["F"]), int(prob["M"])
+        self.K, self.n_lod = int(prob["K"]), int(prob["n_lod"])
+        cut_off, cut = _csr(prob["op_cutset"])
+        prev_off, prev = _csr(prob["op_prev"])
+        ch_off, ch = _csr(prob["op_children"])
+        for k, v in dict(cut_off=cut_off, cut=cut, prev_off=prev_off, prev=prev, ch_off=ch_off,
+                         ch=ch).items():
+            self.keep[k] = v
+        s = _Problem()
+        s.N, s.F, s.M, s.K, s.n_lod = self.N, self.F, self.M, self.K, self.n_lod
+        s.mother = _p(g("mother", np.int32))
+        s.father = _p(g("father", np.int32))
+        s.sex = _p(g("sex", np.int32))
+        s.geno = _p(g("genotypes", np.uint8))
+        s.typed = _p(g("typed", np.uint8))
+        s.legal = _p(g("legal", np.uint8))
+        s.prior = _p(g("trait_prior", np.float64))
+        s.dprob = _p(g("disease_prob", np.float64))
+        s.theta = _p(g("theta", np.float64))
+        s.partial = _p(g("partial", np.float64))
+        s.minor = _p(g("minor", np.float64))
+        s.op_type = _p(g("op_type", np.int32))
+        s.op_peel = _p(g("op_peel", np.int32))
+        s.cut_off, s.cut = _p(cut_off), _p(cut)
+        s.prev_off, s.prev = _p(prev_off), _p(prev)
+        s.ch_off, s.ch = _p(ch_off), _p(ch)
+        self.s = s
+
+    def lstep(self, dg, locus, u):
+        dg = np.ascontiguousarray(dg, np.int32).copy()
+        u = np.ascontiguousarray(u, np.float64)
+        used = ctypes.c_int()
+        rc = lib().slo_lstep(ctypes.byref(self.s), _p(dg), int(locus), _p(u), u.size, ctypes.byref(used))
+        if rc != 0:
+            raise RuntimeError(f"slo_lstep failed ({rc})")
+        return dg, used.value
+
+    def msweep(self, dg, meioses, u):
+        dg = np.ascontiguousarray(dg, np.int32).copy()
+        meioses = np.ascontiguousarray(meioses, np.int32)
+        u = np.ascontiguousarray(u, np.float64)
+        used = np.zeros(meioses.size, np.int32)
+        rc = lib().slo_msweep(ctypes.byref(self.s), _p(dg), _p(meioses), meioses.size, _p(u), _p(used))
+        if rc != 0:
+            raise RuntimeError(f"slo_msweep failed ({rc})")
+        return dg, used
+
+    def lod(self, dgs):
+        dgs = np.ascontiguousarray(dgs, np.int32)
+        raw = np.zeros((self.M - 1) * self.n_lod)
+        cnt = ctypes.c_uint32()
+        tp = ctypes.c_double()
+        rc = lib().slo_lod(ctypes.byref(self.s), _p(dgs), dgs.shape[0], _p(raw), ctypes.byref(cnt),
+                           ctypes.byref(tp))
+        if rc != 0:
+            raise RuntimeError("slo_lod failed")
+        return raw, cnt.value, tp.value
+
+    def fag(self, dg, locus):
+        dg = np.ascontiguousarray(dg, np.int32)
+        return lib().slo_fag_likelihood(ctypes.byref(self.s), _p(dg), int(locus))
+
+    def loglik(self, dg):
+        dg = np.ascontiguousarray(dg, np.int32)
+        return lib().slo_loglik(ctypes.byref(self.s), _p(dg))
+
+
+def philox_uniform(key: int, hi: int, lo: int) -> float:
+    return lib().slo_philox_uniform(key, hi, lo)
