@@ -1,0 +1,221 @@
+/*
+ * swiftlink_gb300: GB300-native (sm_103a) kernels for the MCMC hot path of
+ * SwiftLink multipoint linkage analysis -- the locus (L-) sampler, the meiosis
+ * (M-) sampler and the trait-peeling LOD scorer -- behind a plain C ABI.
+ *
+ * Conventions
+ *  - Every call returns SL_OK (0) or a negative SL_E* code; nothing aborts.
+ *    sl_last_error() gives a one-line reason for the last failure on a context.
+ *  - The caller owns every host array passed in; the context owns its device
+ *    buffers.  A context is bound to one device and one CUDA stream and is not
+ *    thread-safe (the reference calls its GPU wrapper from the OpenMP master
+ *    thread only, markov_chain.cc:385-388).
+ *  - Persons are in the reference's internal order: founders first
+ *    (pedigree.cc:154-162).  Phased states use the reference's enum
+ *    {UU=0, AA=1, AU=2, UA=3}, first letter = maternal-origin allele
+ *    (trait.h:21-27); unphased genotypes are {UNTYPED=0, HETERO=1, HOMOZ_A=2,
+ *    HOMOZ_B=3} (genotype.h:26-31).
+ *  - Descent graphs cross the boundary in the reference's internal layout,
+ *    int32 [locus][person][2] with offset 2N*locus + 2*person + parent
+ *    (descent_graph.h:35-37, DescentGraph::get_internal_ptr), one graph after
+ *    another for multi-graph calls.  On the device they are bit-packed.
+ *  - Uniform draws for the bit-exact sampler entry points are supplied by the
+ *    caller in the order the reference consumes get_random()
+ *    (random.h:12-13): see each entry point.
+ */
+#ifndef SWIFTLINK_GB300_H_
+#define SWIFTLINK_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SL_OK 0
+#define SL_EINVAL -1      /* bad argument or unsupported problem */
+#define SL_ECUDA -2       /* CUDA runtime failure */
+#define SL_EZERO -3       /* zero likelihood (locus_sampler2.cc:137-142, peeler.cc:92-95) */
+#define SL_EILLEGAL -4    /* illegal descent graph (meiosis_sampler.cc:33-36, 129-132) */
+#define SL_ENOMEM -5      /* device allocation failed */
+#define SL_ENODEV -6      /* no usable CUDA device */
+
+/* Peel operation types, as in peeling.h:16-22 */
+#define SL_CHILD_PEEL 1
+#define SL_PARENT_PEEL 2
+#define SL_PARTNER_PEEL 3
+#define SL_LAST_PEEL 4
+
+/* LOD arithmetic */
+#define SL_LOD_FP64 0          /* plain: FP64 trait peel, one warp per (graph, interval, offset) */
+#define SL_LOD_FP32_RESCALED 1 /* batched: FP32 peel with per-rfunction power-of-two rescaling */
+
+typedef struct sl_ctx sl_ctx;
+
+/*
+ * One pedigree, its map and its peel sequence: the data the reference's
+ * GPULodscores constructor mirrors to the device (gpu_lodscores.h:63-83,
+ * gpu_lodscores.cc:106-527) plus what the samplers need.
+ */
+typedef struct sl_problem_desc {
+    int32_t n_members;          /* N */
+    int32_t n_founders;         /* F; persons 0..F-1 are the founders */
+    int32_t n_markers;          /* M (>= 2) */
+    int32_t lod_per_interval;   /* n, the -n option (defaults.h:22) */
+    int32_t sex_linked;         /* must be 0: like the reference's -g path (main.cc:534-537) */
+    const int32_t* mother;      /* [N] internal id of the mother, -1 for founders */
+    const int32_t* father;      /* [N] */
+    const int32_t* sex;         /* [N] 0 unsexed, 1 male, 2 female (types.h:22-26) */
+    const uint8_t* typed;       /* [N] 1 if the person has any typed marker */
+    const uint8_t* genotypes;   /* [M][N] unphased genotype codes */
+    const uint8_t* legal;       /* [M][N] genotype-elimination masks, bit v = phased state v is
+                                   possible (elimination.cc:41-395); NULL = computed here */
+    const double* disease_prob; /* [N][4] Person::disease_prob (person.cc:85-119) */
+    const double* theta;        /* [M-1] recombination fractions (genetic_map.cc:39-54) */
+    const double* partial_theta;/* [M-1] (genetic_map.cc:57-61) */
+    const double* minor_freq;   /* [M] minor-allele frequency per SNP */
+    /* peel sequence in evaluation order (PeelSequenceGenerator::get_peel_order,
+       peeling.h:25-339), compressed-row lists */
+    int32_t n_ops;              /* K */
+    const int32_t* op_type;     /* [K] SL_*_PEEL */
+    const int32_t* op_peelnode; /* [K] */
+    const int32_t* cutset_off;  /* [K+1] */
+    const int32_t* cutset;      /* cutset members, reference key order */
+    const int32_t* prev_off;    /* [K+1] */
+    const int32_t* prev;        /* previous rfunctions feeding each op */
+    const int32_t* children_off;/* [K+1] */
+    const int32_t* children;    /* children of a parent peel, cutset order */
+} sl_problem_desc;
+
+typedef struct sl_options {
+    int32_t device;             /* CUDA device ordinal */
+    int32_t n_chains;           /* descent graphs held on the device (replicates x temperatures) */
+    int32_t lod_precision;      /* SL_LOD_FP64 or SL_LOD_FP32_RESCALED */
+    int32_t reserved;
+} sl_options;
+
+/* Create a context; replaces GPULodscores::GPULodscores (gpu_lodscores.h:63-83). */
+int sl_create(const sl_problem_desc* problem, const sl_options* options, sl_ctx** out);
+
+/* Release every device buffer of the context (gpu_lodscores.h:95-99). */
+void sl_destroy(sl_ctx* ctx);
+
+/* One-line description of the last failure on ctx (thread-local when ctx is NULL). */
+const char* sl_last_error(const sl_ctx* ctx);
+
+/* Copy descent graphs of chains [first, first+n) in / out (int32 reference layout). */
+int sl_set_descent_graphs(sl_ctx* ctx, int32_t first, int32_t n, const int32_t* dg);
+int sl_get_descent_graphs(sl_ctx* ctx, int32_t first, int32_t n, int32_t* dg);
+
+/* Per-locus, per-state priors the L-sampler uses (Person::get_trait_probability,
+ * person.cc:224-299), [M][N][4]; lets callers check the host-side tables. */
+int sl_get_trait_priors(sl_ctx* ctx, double* out);
+
+/* Genotype-elimination masks used by the context, [M][N]. */
+int sl_get_legal_masks(sl_ctx* ctx, uint8_t* out);
+
+/*
+ * L-sampler: Gibbs update of every meiosis indicator at one locus
+ * (LocusSampler::set_locus_minimal + LocusSampler::step, locus_sampler2.cc:
+ * 128-159; Sampler::step interface, sampler.h:62).
+ *
+ * sl_lsampler_loci updates, for each chain c in [first, first+n_chains) and each
+ * listed locus, the descent graph in place.  The listed loci must be pairwise
+ * non-adjacent (the reference's noninterferring rule, markov_chain.cc:406-416),
+ * so they are independent and run concurrently.  Draws: for chain c and the
+ * i-th listed locus, u[(c-first)*u_chain_stride + loci[i]*u_locus_stride ...],
+ * consumed in the reference order: one per peel operation from the last to the
+ * first (sampler_rfunction.cc:159-188), then one per meiosis whose parent has a
+ * homozygous sampled state, in person order, maternal first
+ * (locus_sampler2.cc:44-65, 93-125).  u_locus_stride >= K + 2N suffices.
+ */
+int sl_lsampler_loci(sl_ctx* ctx, int32_t first, int32_t n_chains, const int32_t* loci,
+                     int32_t n_loci, const double* u, int64_t u_chain_stride,
+                     int64_t u_locus_stride);
+
+/* A full L-sweep: all even loci, then all odd loci (each a non-interfering
+ * set), draws laid out as for sl_lsampler_loci. */
+int sl_lsampler_sweep(sl_ctx* ctx, int32_t first, int32_t n_chains, const double* u,
+                      int64_t u_chain_stride, int64_t u_locus_stride);
+
+/*
+ * M-sampler sweep (markov_chain.cc:345-351; MeiosisSampler::reset/step,
+ * meiosis_sampler.cc:17-203): reset at meioses[0], then one Gibbs step per
+ * listed meiosis (meiosis id = 2*(person-F) + parent).  Step j of chain c reads
+ * draws from u[(c-first)*u_chain_stride + j*M ...] in backward order
+ * (locus M-1 first), skipping loci where a filtered probability is exactly 0.
+ */
+int sl_msampler_sweep(sl_ctx* ctx, int32_t first, int32_t n_chains, const int32_t* meioses,
+                      int32_t n_meioses, const double* u, int64_t u_chain_stride);
+
+/*
+ * LOD scoring (Peeler::process + LODscores::add, peeler.cc:79-103,
+ * lod_score.h:74-105; the reference GPU path GPULodscores::calculate,
+ * gpu_lodscores.cc:598-607).  Scores every interval and every one of the n
+ * positions of the current descent graph of chains [first, first+n_chains),
+ * accumulating log-likelihood ratios in FP64 log-sum form on the device.
+ */
+int sl_lod_score_chains(sl_ctx* ctx, int32_t first, int32_t n_chains);
+
+/* Same, for n_graphs caller-supplied descent graphs (int32 reference layout),
+ * scored in order. */
+int sl_lod_score_graphs(sl_ctx* ctx, int32_t n_graphs, const int32_t* dgs);
+
+/* Raw accumulators [(M-1)*n] in LODscores::get_raw form, the number of scored
+ * graphs and log P(T) (GPULodscores::get_results, gpu_lodscores.cc:621-637). */
+int sl_lod_results(sl_ctx* ctx, double* raw_logsum, uint64_t* count, double* trait_prob);
+
+/* Clear the LOD accumulators and count. */
+int sl_lod_reset(sl_ctx* ctx);
+
+/*
+ * Full MCMC run on the device (MarkovChain::run, markov_chain.cc:314-404) for
+ * every chain, with uniform draws from a counter-based Philox4x32-10 stream
+ * keyed by (seed, chain).  Each iteration picks an L-sweep with probability
+ * lsampler_prob, else an M-sweep over the non-ignorable meioses in a shuffled
+ * order; after burnin, every `period`-th iteration scores the chains whose
+ * temperature is 1.
+ */
+typedef struct sl_run_options {
+    int32_t iterations;
+    int32_t burnin;
+    int32_t scoring_period;
+    int32_t first_iteration;    /* iteration index of the first step (for resumable runs) */
+    double lsampler_prob;
+    uint64_t seed;
+} sl_run_options;
+
+int sl_run(sl_ctx* ctx, const sl_run_options* opt);
+
+/* Wait for all work queued on the context's stream. */
+int sl_synchronize(sl_ctx* ctx);
+
+/* Device-side status word: 0 when every kernel finished cleanly. */
+int sl_device_status(sl_ctx* ctx, int32_t* status);
+
+/* Number of kernel launches the context has issued (for measurement). */
+int64_t sl_launch_count(const sl_ctx* ctx);
+
+/*
+ * Host-side tables, no device needed (the checks a caller can run before
+ * creating a context):
+ *  - genotype-elimination masks [M][N] (GenotypeElimination::elimination,
+ *    elimination.cc:41-183, 383-395);
+ *  - per-locus L-sampler priors [M][N][4] (Person::populate_trait_prob_cache,
+ *    person.cc:224-299, filled while parsing, pedigree_parser.cc:157);
+ *  - log P(T), the trait peel without a descent graph (Peeler::calc_trait_prob,
+ *    peeler.cc:65-73).
+ */
+int sl_problem_legal_masks(const sl_problem_desc* problem, uint8_t* out);
+int sl_problem_trait_priors(const sl_problem_desc* problem, double* out);
+int sl_problem_trait_prob(const sl_problem_desc* problem, double* out);
+
+/* Library version string. */
+const char* sl_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SWIFTLINK_GB300_H_ */

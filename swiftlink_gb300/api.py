@@ -1,0 +1,284 @@
+"""ctypes binding of the swiftlink_gb300 C ABI (include/swiftlink_gb300.h).
+
+This is glue for tests and benchmarks: every computation happens in the CUDA
+library; there is no Python or CPU fallback.  Loading fails loudly when the
+library has not been built.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass, field
+from typing import Optional, Sequence
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libswiftlink_gb300.so")
+
+SL_OK, SL_EINVAL, SL_ECUDA, SL_EZERO, SL_EILLEGAL, SL_ENOMEM, SL_ENODEV = 0, -1, -2, -3, -4, -5, -6
+SL_LOD_FP64, SL_LOD_FP32_RESCALED = 0, 1
+
+EXPORTED = [
+    "sl_create", "sl_destroy", "sl_last_error", "sl_set_descent_graphs", "sl_get_descent_graphs",
+    "sl_get_trait_priors", "sl_get_legal_masks", "sl_lsampler_loci", "sl_lsampler_sweep",
+    "sl_msampler_sweep", "sl_lod_score_chains", "sl_lod_score_graphs", "sl_lod_results",
+    "sl_lod_reset", "sl_run", "sl_synchronize", "sl_device_status", "sl_launch_count",
+    "sl_version",
+]
+
+
+class SwiftLinkError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+_vp = ctypes.c_void_p
+
+
+class ProblemDesc(ctypes.Structure):
+    _fields_ = [
+        ("n_members", ctypes.c_int32), ("n_founders", ctypes.c_int32), ("n_markers", ctypes.c_int32),
+        ("lod_per_interval", ctypes.c_int32), ("sex_linked", ctypes.c_int32),
+        ("mother", _vp), ("father", _vp), ("sex", _vp), ("typed", _vp), ("genotypes", _vp),
+        ("legal", _vp), ("disease_prob", _vp), ("theta", _vp), ("partial_theta", _vp),
+        ("minor_freq", _vp), ("n_ops", ctypes.c_int32), ("op_type", _vp), ("op_peelnode", _vp),
+        ("cutset_off", _vp), ("cutset", _vp), ("prev_off", _vp), ("prev", _vp),
+        ("children_off", _vp), ("children", _vp),
+    ]
+
+
+class Options(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int32), ("n_chains", ctypes.c_int32),
+                ("lod_precision", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
+class RunOptions(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int32), ("burnin", ctypes.c_int32),
+                ("scoring_period", ctypes.c_int32), ("first_iteration", ctypes.c_int32),
+                ("lsampler_prob", ctypes.c_double), ("seed", ctypes.c_uint64)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"swiftlink_gb300 CUDA library not built ({LIB_PATH}); run "
+                               "python -c 'import __graft_entry__ as g; g.build()'")
+        L = ctypes.CDLL(LIB_PATH)
+        L.sl_last_error.restype = ctypes.c_char_p
+        L.sl_last_error.argtypes = [_vp]
+        L.sl_version.restype = ctypes.c_char_p
+        L.sl_launch_count.restype = ctypes.c_int64
+        L.sl_launch_count.argtypes = [_vp]
+        L.sl_destroy.argtypes = [_vp]
+        L.sl_destroy.restype = None
+        _lib = L
+    return _lib
+
+
+def _p(a: np.ndarray):
+    return a.ctypes.data_as(_vp)
+
+
+def _csr(lists):
+    off = np.zeros(len(lists) + 1, np.int32)
+    for i, x in enumerate(lists):
+        off[i + 1] = off[i] + len(x)
+    flat = (np.concatenate([np.asarray(x, np.int32) for x in lists]) if off[-1]
+            else np.zeros(1, np.int32))
+    return off, np.ascontiguousarray(flat, np.int32)
+
+
+@dataclass
+class Problem:
+    """One pedigree, map and peel sequence in the reference's internal order."""
+
+    N: int
+    F: int
+    M: int
+    n_lod: int
+    mother: np.ndarray
+    father: np.ndarray
+    sex: np.ndarray
+    typed: np.ndarray
+    genotypes: np.ndarray      # [M][N]
+    disease_prob: np.ndarray   # [N][4]
+    theta: np.ndarray
+    partial: np.ndarray
+    minor: np.ndarray
+    op_type: np.ndarray
+    op_peel: np.ndarray
+    op_cutset: list
+    op_prev: list
+    op_children: list
+    legal: Optional[np.ndarray] = None
+    keep: dict = field(default_factory=dict)
+
+    @property
+    def K(self) -> int:
+        return len(self.op_type)
+
+    @classmethod
+    def from_arrays(cls, d: dict, with_legal: bool = True) -> "Problem":
+        return cls(N=int(d["N"]), F=int(d["F"]), M=int(d["M"]), n_lod=int(d["n_lod"]),
+                   mother=d["mother"], father=d["father"], sex=d["sex"], typed=d["typed"],
+                   genotypes=d["genotypes"], disease_prob=d["disease_prob"], theta=d["theta"],
+                   partial=d["partial"], minor=d["minor"], op_type=d["op_type"],
+                   op_peel=d["op_peel"], op_cutset=list(d["op_cutset"]), op_prev=list(d["op_prev"]),
+                   op_children=list(d["op_children"]),
+                   legal=d.get("legal") if with_legal else None)
+
+    def desc(self) -> ProblemDesc:
+        k = self.keep
+        g = lambda name, a, dt: k.setdefault(name, np.ascontiguousarray(a, dt))
+        s = ProblemDesc()
+        s.n_members, s.n_founders, s.n_markers = self.N, self.F, self.M
+        s.lod_per_interval, s.sex_linked = self.n_lod, 0
+        s.mother = _p(g("mother", self.mother, np.int32))
+        s.father = _p(g("father", self.father, np.int32))
+        s.sex = _p(g("sex", self.sex, np.int32))
+        s.typed = _p(g("typed", self.typed, np.uint8))
+        s.genotypes = _p(g("genotypes", self.genotypes, np.uint8))
+        s.legal = _p(g("legal", self.legal, np.uint8)) if self.legal is not None else None
+        s.disease_prob = _p(g("dprob", self.disease_prob, np.float64))
+        s.theta = _p(g("theta", self.theta, np.float64))
+        s.partial_theta = _p(g("partial", self.partial, np.float64))
+        s.minor_freq = _p(g("minor", self.minor, np.float64))
+        s.n_ops = self.K
+        s.op_type = _p(g("op_type", self.op_type, np.int32))
+        s.op_peelnode = _p(g("op_peel", self.op_peel, np.int32))
+        for name, lists in (("cutset", self.op_cutset), ("prev", self.op_prev),
+                            ("children", self.op_children)):
+            off, flat = _csr(lists)
+            k[name + "_off"], k[name] = off, flat
+        s.cutset_off, s.cutset = _p(k["cutset_off"]), _p(k["cutset"])
+        s.prev_off, s.prev = _p(k["prev_off"]), _p(k["prev"])
+        s.children_off, s.children = _p(k["children_off"]), _p(k["children"])
+        return s
+
+
+class Context:
+    """A device context holding one problem and n_chains descent graphs."""
+
+    def __init__(self, problem: Problem, n_chains: int = 1, lod_precision: int = SL_LOD_FP64,
+                 device: int = 0):
+        self.problem = problem
+        self._desc = problem.desc()
+        opt = Options(device, n_chains, lod_precision, 0)
+        h = _vp()
+        rc = lib().sl_create(ctypes.byref(self._desc), ctypes.byref(opt), ctypes.byref(h))
+        if rc != SL_OK:
+            raise SwiftLinkError(rc, lib().sl_last_error(None).decode())
+        self.h = h
+        self.n_chains = n_chains
+        self.N, self.F, self.M, self.K = problem.N, problem.F, problem.M, problem.K
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().sl_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, rc):
+        if rc != SL_OK:
+            raise SwiftLinkError(rc, lib().sl_last_error(self.h).decode())
+
+    @property
+    def launches(self) -> int:
+        return lib().sl_launch_count(self.h)
+
+    def set_graphs(self, dgs: np.ndarray, first: int = 0):
+        dgs = np.ascontiguousarray(dgs, np.int32).reshape(-1, self.M, self.N, 2)
+        self._check(lib().sl_set_descent_graphs(self.h, first, dgs.shape[0], _p(dgs)))
+
+    def get_graphs(self, first: int = 0, n: Optional[int] = None) -> np.ndarray:
+        n = self.n_chains - first if n is None else n
+        out = np.zeros((n, self.M, self.N, 2), np.int32)
+        self._check(lib().sl_get_descent_graphs(self.h, first, n, _p(out)))
+        return out
+
+    def trait_priors(self) -> np.ndarray:
+        out = np.zeros((self.M, self.N, 4))
+        self._check(lib().sl_get_trait_priors(self.h, _p(out)))
+        return out
+
+    def legal_masks(self) -> np.ndarray:
+        out = np.zeros((self.M, self.N), np.uint8)
+        self._check(lib().sl_get_legal_masks(self.h, _p(out)))
+        return out
+
+    def lsampler_loci(self, loci: Sequence[int], u: np.ndarray, first: int = 0, n_chains: int = 1):
+        """u: [n_chains][M][stride] draws."""
+        loci = np.ascontiguousarray(loci, np.int32)
+        u = np.ascontiguousarray(u, np.float64)
+        assert u.ndim == 3 and u.shape[1] == self.M
+        self._check(lib().sl_lsampler_loci(self.h, first, n_chains, _p(loci), loci.size, _p(u),
+                                           ctypes.c_int64(u.shape[1] * u.shape[2]),
+                                           ctypes.c_int64(u.shape[2])))
+
+    def lsampler_sweep(self, u: np.ndarray, first: int = 0, n_chains: int = 1):
+        u = np.ascontiguousarray(u, np.float64)
+        assert u.ndim == 3 and u.shape[1] == self.M
+        self._check(lib().sl_lsampler_sweep(self.h, first, n_chains, _p(u),
+                                            ctypes.c_int64(u.shape[1] * u.shape[2]),
+                                            ctypes.c_int64(u.shape[2])))
+
+    def msampler_sweep(self, meioses: Sequence[int], u: np.ndarray, first: int = 0, n_chains: int = 1):
+        """u: [n_chains][len(meioses)][M] draws."""
+        m = np.ascontiguousarray(meioses, np.int32)
+        u = np.ascontiguousarray(u, np.float64)
+        assert u.ndim == 3 and u.shape[1] == m.size and u.shape[2] == self.M
+        self._check(lib().sl_msampler_sweep(self.h, first, n_chains, _p(m), m.size, _p(u),
+                                            ctypes.c_int64(u.shape[1] * u.shape[2])))
+
+    def lod_score_chains(self, first: int = 0, n_chains: Optional[int] = None):
+        n = self.n_chains - first if n_chains is None else n_chains
+        self._check(lib().sl_lod_score_chains(self.h, first, n))
+
+    def lod_score_graphs(self, dgs: np.ndarray):
+        dgs = np.ascontiguousarray(dgs, np.int32).reshape(-1, self.M, self.N, 2)
+        self._check(lib().sl_lod_score_graphs(self.h, dgs.shape[0], _p(dgs)))
+
+    def lod_results(self):
+        raw = np.zeros((self.M - 1) * self.problem.n_lod)
+        cnt = ctypes.c_uint64()
+        tp = ctypes.c_double()
+        self._check(lib().sl_lod_results(self.h, _p(raw), ctypes.byref(cnt), ctypes.byref(tp)))
+        return raw, cnt.value, tp.value
+
+    def lod_reset(self):
+        self._check(lib().sl_lod_reset(self.h))
+
+    def run(self, iterations: int, burnin: int = 0, period: int = 10, lprob: float = 0.5,
+            seed: int = 1, first_iteration: int = 0):
+        o = RunOptions(iterations, burnin, period, first_iteration, lprob, seed)
+        self._check(lib().sl_run(self.h, ctypes.byref(o)))
+
+    def synchronize(self):
+        self._check(lib().sl_synchronize(self.h))
+
+    def status(self) -> int:
+        st = ctypes.c_int32()
+        self._check(lib().sl_device_status(self.h, ctypes.byref(st)))
+        return st.value
+
+
+def lod_table(raw: np.ndarray, count: int, trait_prob: float) -> np.ndarray:
+    """LODscores::get (lod_score.h:86-88): (raw - ln count - P(T)) / ln 10."""
+    return (raw - np.log(count) - trait_prob) / np.log(10.0)

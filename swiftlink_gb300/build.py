@@ -1,0 +1,77 @@
+"""Build the in-tree CUDA library swiftlink_gb300/_build/libswiftlink_gb300.so.
+
+Two translation units compiled in parallel for sm_103a only, then linked with
+the static CUDA runtime:
+  csrc/sl_kernels.cu  (nvcc, -gencode arch=compute_103a,code=sm_103a)
+  csrc/sl_host.cc     (g++ against the CUDA runtime headers)
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+OUT = os.path.join(HERE, "_build")
+LIB = os.path.join(OUT, "libswiftlink_gb300.so")
+GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
+
+
+def _cuda_home() -> str:
+    for c in (os.environ.get("CUDA_HOME"), "/usr/local/cuda"):
+        if c and os.path.exists(os.path.join(c, "bin", "nvcc")):
+            return c
+    nvcc = shutil.which("nvcc")
+    if nvcc:
+        return os.path.dirname(os.path.dirname(nvcc))
+    raise RuntimeError("nvcc not found")
+
+
+def _run(cmd):
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("build failed: " + " ".join(cmd) + "\n" + r.stdout + r.stderr)
+    return r.stdout + r.stderr
+
+
+def _stale(target, sources):
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(s) > t for s in sources)
+
+
+def build(verbose: bool = False, force: bool = False) -> str:
+    cuda = _cuda_home()
+    nvcc = os.path.join(cuda, "bin", "nvcc")
+    os.makedirs(OUT, exist_ok=True)
+    hdrs = [os.path.join(CSRC, "sl_internal.h"),
+            os.path.join(os.path.dirname(HERE), "include", "swiftlink_gb300.h")]
+    cu = os.path.join(CSRC, "sl_kernels.cu")
+    cc = os.path.join(CSRC, "sl_host.cc")
+    cu_o = os.path.join(OUT, "sl_kernels.o")
+    cc_o = os.path.join(OUT, "sl_host.o")
+    jobs = []
+    if force or _stale(cu_o, [cu] + hdrs):
+        jobs.append([nvcc, GENCODE, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+                     "-Xptxas", "-v", "-c", cu, "-o", cu_o])
+    if force or _stale(cc_o, [cc] + hdrs):
+        jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-Wall", "-I" + os.path.join(cuda, "include"),
+                     "-c", cc, "-o", cc_o])
+    logs = []
+    if jobs:
+        with cf.ThreadPoolExecutor(len(jobs)) as ex:
+            logs = list(ex.map(_run, jobs))
+    if force or jobs or _stale(LIB, [cu_o, cc_o]):
+        logs.append(_run([nvcc, GENCODE, "-shared", "-cudart", "static", "-o", LIB, cu_o, cc_o]))
+    if verbose:
+        for l in logs:
+            sys.stdout.write(l)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(verbose="-v" in sys.argv, force="-f" in sys.argv))

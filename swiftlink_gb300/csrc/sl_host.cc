@@ -1,0 +1,917 @@
+// Host side of the swiftlink_gb300 C ABI: validates a problem, builds the
+// device tables (per-locus priors, genotype-elimination masks, peel-operation
+// descriptors with gather maps), bit-packs descent graphs, and enqueues the
+// kernels of sl_kernels.cu on the context's stream.
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/swiftlink_gb300.h"
+#include "sl_internal.h"
+
+namespace sl {
+// kernels (sl_kernels.cu)
+size_t lsampler_smem_per_warp(const ProblemDev& P);
+int fag_bytes(int N, int F);
+cudaError_t launch_lsampler(const ProblemDev& P, uint32_t* dg, int first, int nchain, const int32_t* loci,
+                            int nloci, const double* u, int64_t ucs, int64_t uls, uint64_t seed, uint64_t iter,
+                            const uint8_t* sel, int want, int* status, cudaStream_t s, int grid_cap, int wpb);
+cudaError_t launch_msampler(const ProblemDev& P, uint32_t* dg, int first, int nchain, const int32_t* meioses,
+                            int64_t mstride, int nm, const double* u, int64_t ucs, uint64_t seed, uint64_t iter,
+                            const uint8_t* sel, int want, double* raw, double* fb, int* status, int threads,
+                            cudaStream_t s);
+cudaError_t launch_lod(const ProblemDev& P, int precision, const uint32_t* graphs, int64_t graph_words, int G,
+                       double* vals, int* status, cudaStream_t s, int grid_cap, int wpb);
+cudaError_t launch_lod_merge(const double* vals, int G, int64_t npos, double* acc, uint8_t* init, cudaStream_t s);
+cudaError_t launch_shuffle(const int32_t* base, int nm, int32_t* out, int first, int nchain, uint64_t seed,
+                           uint64_t iter, cudaStream_t s);
+cudaError_t launch_choose(int first, int nchain, uint64_t seed, uint64_t iter, double lprob, uint8_t* is_l,
+                          cudaStream_t s);
+}  // namespace sl
+
+using namespace sl;
+
+namespace {
+thread_local std::string g_err;
+const size_t kSmemBudget = 200 * 1024;  // dynamic shared memory a block may use
+}  // namespace
+
+struct sl_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int n_chains = 0;
+    int lod_precision = 0;
+    int sms = 0;
+    ProblemDev P{};
+    // host copies
+    std::vector<double> prior_table;     // [M][4][4]
+    std::vector<uint8_t> legal;          // [M][N]
+    std::vector<int32_t> meioses;        // non-ignorable meioses (markov_chain.cc:70-80)
+    std::vector<int32_t> even, odd;
+    double trait_prob = 0.0;
+    uint64_t lod_count = 0;
+    int64_t launches = 0;
+    // launch shapes
+    int ls_wpb = 1, ls_grid = 1, lod_wpb = 1, lod_grid = 1, ms_threads = 32;
+    // device buffers
+    std::vector<void*> owned;
+    uint32_t* d_dg = nullptr;
+    double* d_acc = nullptr;
+    uint8_t* d_init = nullptr;
+    double* d_vals = nullptr;
+    int vals_graphs = 0;
+    uint32_t* d_graphs = nullptr;
+    int graphs_cap = 0;
+    double* d_u = nullptr;
+    size_t u_cap = 0;
+    int32_t* d_loci = nullptr;
+    int32_t* d_even = nullptr;
+    int32_t* d_odd = nullptr;
+    int32_t* d_meioses = nullptr;
+    int32_t* d_morder = nullptr;     // [C][nm] per-chain orders for device-driven sweeps
+    int32_t* d_mlist = nullptr;      // staging for caller meiosis lists
+    size_t mlist_cap = 0;
+    double* d_raw = nullptr;
+    double* d_fb = nullptr;
+    int* d_status = nullptr;
+    uint8_t* d_sel = nullptr;
+    std::string err;
+};
+
+static int fail(sl_ctx* c, int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    if (c) c->err = buf;
+    g_err = buf;
+    return code;
+}
+
+#define CK(call)                                                                              \
+    do {                                                                                      \
+        cudaError_t e_ = (call);                                                              \
+        if (e_ != cudaSuccess)                                                                \
+            return fail(ctx, e_ == cudaErrorMemoryAllocation ? SL_ENOMEM : SL_ECUDA, "%s: %s", \
+                        #call, cudaGetErrorString(e_));                                       \
+    } while (0)
+
+template <typename T>
+static int dev_alloc(sl_ctx* ctx, T** p, size_t n) {
+    void* q = nullptr;
+    if (n == 0) n = 1;
+    cudaError_t e = cudaMalloc(&q, n * sizeof(T));
+    if (e != cudaSuccess) return fail(ctx, SL_ENOMEM, "cudaMalloc(%zu bytes): %s", n * sizeof(T), cudaGetErrorString(e));
+    ctx->owned.push_back(q);
+    *p = (T*)q;
+    return SL_OK;
+}
+
+template <typename T>
+static int upload(sl_ctx* ctx, T** p, const T* host, size_t n) {
+    int rc = dev_alloc(ctx, p, n);
+    if (rc) return rc;
+    if (n) CK(cudaMemcpy(*p, host, n * sizeof(T), cudaMemcpyHostToDevice));
+    return SL_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Host-side tables
+// ---------------------------------------------------------------------------
+
+// Per-locus prior of a person's phased state given its genotype code.  The
+// reference fills Person::genotypes_prob while parsing, before parents are
+// linked, so every person takes the founder branch: the Hardy-Weinberg marker
+// probability masked by the typed genotype, then normalised
+// (pedigree_parser.cc:157, person.cc:224-299; Snp::init_probs,
+// genetic_map.h:68-87).  The sums keep the reference's operand order.
+static void build_priors(int M, const double* minor, std::vector<double>& out) {
+    out.assign((size_t)M * 16, 0.0);
+    for (int l = 0; l < M; ++l) {
+        const double mi = minor[l], ma = 1.0 - minor[l];
+        double hw[4];
+        hw[UU] = ma * ma;
+        hw[AU] = mi * ma;
+        hw[UA] = mi * ma;
+        hw[AA] = mi * mi;
+        const double tot = hw[UU] + hw[AU] + hw[UA] + hw[AA];
+        for (int v = 0; v < 4; ++v) hw[v] /= tot;
+        for (int g = 0; g < 4; ++g) {
+            double pr[4];
+            for (int v = 0; v < 4; ++v) {
+                bool ok = true;
+                if (g == G_HETERO) ok = (v == AU || v == UA);
+                else if (g == G_HOMOZ_A) ok = (v == UU);
+                else if (g == G_HOMOZ_B) ok = (v == AA);
+                pr[v] = ok ? hw[v] : 0.0;
+            }
+            const double t = pr[0] + pr[1] + pr[2] + pr[3];
+            for (int v = 0; v < 4; ++v) out[((size_t)l * 4 + g) * 4 + v] = pr[v] / t;
+        }
+    }
+}
+
+// Genotype elimination over phased genotypes {AA=8, AB=4, BA=2, BB=1}
+// (elimination.cc:41-183): initial masks from the typed genotypes, then
+// homozygote rules repeated until nothing changes.  Returns false when a
+// locus has a person with no possible genotype.
+namespace {
+enum { PG_AA = 8, PG_AB = 4, PG_BA = 2, PG_BB = 1 };
+int child_homoz(std::vector<int>& pg, int mother, int father, int child, int homoz) {
+    int changes = 0;
+    const int other = homoz == PG_AA ? PG_BB : PG_AA;
+    if ((pg[child] ^ homoz) == 0) {
+        if (pg[mother] & other) { pg[mother] ^= other; ++changes; }
+        if (pg[father] & other) { pg[father] ^= other; ++changes; }
+    }
+    return changes;
+}
+int parent_homoz(std::vector<int>& pg, int parent, int other_parent, int child, int homoz, int maternal) {
+    int changes = 0;
+    if ((pg[parent] ^ homoz) == 0) {
+        int hetero, other_hetero;
+        if ((maternal && homoz == PG_AA) || (!maternal && homoz == PG_BB)) { hetero = PG_AB; other_hetero = PG_BA; }
+        else { hetero = PG_BA; other_hetero = PG_AB; }
+        const int other_homoz = homoz == PG_AA ? PG_BB : PG_AA;
+        if (pg[child] & other_homoz) { pg[child] ^= other_homoz; ++changes; }
+        if (pg[child] & other_hetero) { pg[child] ^= other_hetero; ++changes; }
+        if ((pg[child] & hetero) && !(pg[child] & homoz)) {
+            if (pg[other_parent] & homoz) { pg[other_parent] ^= homoz; ++changes; }
+        }
+    }
+    return changes;
+}
+}  // namespace
+
+static bool genotype_elimination(const sl_problem_desc* d, std::vector<uint8_t>& legal, int* bad_locus) {
+    const int N = d->n_members, M = d->n_markers;
+    legal.assign((size_t)M * N, 0);
+    std::vector<int> pg(N);
+    // phased trait v -> phased genotype bit (genotype.cc:91-102)
+    const int bit_of[4] = {PG_AA, PG_BB, PG_BA, PG_AB};
+    for (int l = 0; l < M; ++l) {
+        for (int j = 0; j < N; ++j) {
+            const int g = d->typed[j] ? d->genotypes[(size_t)l * N + j] : G_UNTYPED;
+            int m = 15;
+            if (g == G_HOMOZ_A) m &= PG_AA;
+            else if (g == G_HETERO) m &= (PG_AB | PG_BA);
+            else if (g == G_HOMOZ_B) m &= PG_BB;
+            pg[j] = m;
+        }
+        while (true) {
+            int changes = 0;
+            for (int i = 0; i < N; ++i) {
+                if (d->mother[i] < 0) continue;
+                const int mat = d->mother[i], pat = d->father[i];
+                changes += parent_homoz(pg, mat, pat, i, PG_AA, 1);
+                changes += parent_homoz(pg, mat, pat, i, PG_BB, 1);
+                changes += parent_homoz(pg, pat, mat, i, PG_AA, 0);
+                changes += parent_homoz(pg, pat, mat, i, PG_BB, 0);
+                changes += child_homoz(pg, mat, pat, i, PG_AA);
+                changes += child_homoz(pg, mat, pat, i, PG_BB);
+            }
+            for (int i = 0; i < N; ++i)
+                if (pg[i] == 0) { *bad_locus = l; return false; }
+            if (changes == 0) break;
+        }
+        for (int j = 0; j < N; ++j) {
+            uint8_t m = 0;
+            for (int v = 0; v < 4; ++v)
+                if (pg[j] & bit_of[v]) m |= (uint8_t)(1u << v);
+            legal[(size_t)l * N + j] = m;
+        }
+    }
+    return true;
+}
+
+// Trait peel without a descent graph: log P(T) (Peeler::calc_trait_prob,
+// peeler.cc:65-73), evaluated once on the host in FP64.
+static double host_trait_prob(const sl_problem_desc* d, const std::vector<OpDev>& ops,
+                              const std::vector<int32_t>& od, int arena) {
+    std::vector<double> A(arena, 0.0);
+    auto dig = [](int ext, int pos) { return (ext >> (2 * pos)) & 3; };
+    auto phased = [](int m, int p, int i, int j) {
+        const int ma = (m == AA) || (m == AU && i == 0) || (m == UA && i == 1);
+        const int pa = (p == AA) || (p == AU && j == 0) || (p == UA && j == 1);
+        if (ma) return pa ? (int)AA : (int)AU;
+        return pa ? (int)UA : (int)UU;
+    };
+    for (size_t k = 0; k < ops.size(); ++k) {
+        const OpDev& op = ops[k];
+        const int ncell = 1 << (2 * op.c);
+        const double* trait = d->disease_prob + 4 * op.peel;
+        for (int cell = 0; cell < ncell; ++cell) {
+            bool valid = true;
+            for (int q = 0; q < op.c; ++q)
+                if (d->disease_prob[4 * od[op.cut_at + q] + dig(cell, q)] == 0.0) valid = false;
+            double total = 0.0;
+            auto prevs = [&](int ext, double tmp) {
+                const int32_t* pd = od.data() + op.prev_at;
+                for (int j = 0; j < op.n_prev; ++j) {
+                    int idx = 0;
+                    for (int q = 0; q < pd[1]; ++q) idx |= dig(ext, pd[2 + q]) << (2 * q);
+                    tmp *= A[pd[0] + idx];
+                    pd += 2 + pd[1];
+                }
+                return tmp;
+            };
+            if (valid) {
+                if (op.type == CHILD) {
+                    const int mt = dig(cell, op.mpos), pt = dig(cell, op.fpos);
+                    for (int i = 0; i < 2; ++i)
+                        for (int j = 0; j < 2; ++j) {
+                            const int kt = phased(mt, pt, i, j);
+                            if (trait[kt] == 0.0) continue;
+                            double tmp = prevs(cell | (kt << (2 * op.c)), trait[kt]);
+                            tmp *= 0.25;
+                            total += tmp;
+                        }
+                } else if (op.type == PARENT) {
+                    for (int a = 0; a < 4; ++a) {
+                        if (trait[a] == 0.0) continue;
+                        const int ext = cell | (a << (2 * op.c));
+                        double tmp = prevs(ext, trait[a]);
+                        double cp = 1.0;
+                        int mt = a, pt = a;
+                        const int32_t* cd = od.data() + op.child_at;
+                        for (int c = 0; c < op.n_child; ++c, cd += 4) {
+                            const int kt = dig(ext, cd[1]), other = dig(ext, cd[2]);
+                            if (cd[3]) pt = other; else mt = other;
+                            double ct = 0.0;
+                            for (int i = 0; i < 2; ++i)
+                                for (int j = 0; j < 2; ++j)
+                                    if (phased(mt, pt, i, j) == kt) ct += 0.25;
+                            cp *= ct;
+                        }
+                        tmp *= cp;
+                        total += tmp;
+                    }
+                } else {
+                    for (int a = 0; a < 4; ++a) {
+                        if (trait[a] == 0.0) continue;
+                        total += prevs(cell | (a << (2 * op.c)), trait[a]);
+                    }
+                }
+            }
+            A[op.mat_off + cell] = total;
+        }
+    }
+    return std::log(A[ops.back().mat_off]);
+}
+
+static void pack_graph(const int32_t* src, int N, int F, int M, int W, uint32_t* dst) {
+    std::memset(dst, 0, sizeof(uint32_t) * (size_t)M * W);
+    for (int l = 0; l < M; ++l) {
+        const int32_t* col = src + (size_t)2 * N * l;
+        uint32_t* out = dst + (size_t)l * W;
+        for (int i = F; i < N; ++i)
+            for (int par = 0; par < 2; ++par) {
+                const int b = 2 * (i - F) + par;
+                if (col[2 * i + par] & 1) out[b >> 5] |= 1u << (b & 31);
+            }
+    }
+}
+
+static void unpack_graph(const uint32_t* src, int N, int F, int M, int W, int32_t* dst) {
+    std::memset(dst, 0, sizeof(int32_t) * (size_t)2 * N * M);
+    for (int l = 0; l < M; ++l) {
+        const uint32_t* col = src + (size_t)l * W;
+        int32_t* out = dst + (size_t)2 * N * l;
+        for (int i = F; i < N; ++i)
+            for (int par = 0; par < 2; ++par) {
+                const int b = 2 * (i - F) + par;
+                out[2 * i + par] = (col[b >> 5] >> (b & 31)) & 1;
+            }
+    }
+}
+
+// Peel-operation descriptors with gather maps: for every previous rfunction,
+// the position of each of its keys in this op's (cutset, peel node) index, so
+// kernels gather with shifts instead of per-person assignment arrays
+// (rfunction.cc:116-142, peel_matrix.h:37-45).
+static int build_ops(const sl_problem_desc* d, std::vector<OpDev>& ops, std::vector<int32_t>& od, int& arena,
+                     int& max_child) {
+    const int N = d->n_members, F = d->n_founders, K = d->n_ops;
+    ops.assign(K, OpDev{});
+    od.clear();
+    arena = 0;
+    max_child = 1;
+    for (int k = 0; k < K; ++k) {
+        OpDev& o = ops[k];
+        std::memset(&o, 0, sizeof o);
+        o.type = d->op_type[k];
+        o.peel = d->op_peelnode[k];
+        o.c = d->cutset_off[k + 1] - d->cutset_off[k];
+        if (o.type < CHILD || o.type > LAST) return (fail(nullptr, SL_EINVAL, "op %d: bad type %d", k, o.type));
+        if (o.peel < 0 || o.peel >= N) return (fail(nullptr, SL_EINVAL, "op %d: bad peel node", k));
+        if (o.c > 10) return (fail(nullptr, SL_EINVAL, "op %d: cutset of %d is too large", k, o.c));
+        const int32_t* cs = d->cutset + d->cutset_off[k];
+        auto pos = [&](int person) {
+            if (person == o.peel) return o.c;
+            for (int q = 0; q < o.c; ++q)
+                if (cs[q] == person) return q;
+            return -1;
+        };
+        o.cut_at = (int)od.size();
+        for (int q = 0; q < o.c; ++q) od.push_back(cs[q]);
+        o.n_prev = d->prev_off[k + 1] - d->prev_off[k];
+        o.prev_at = (int)od.size();
+        for (int q = d->prev_off[k]; q < d->prev_off[k + 1]; ++q) {
+            const int j = d->prev[q];
+            if (j < 0 || j >= k) return (fail(nullptr, SL_EINVAL, "op %d: prev %d is not earlier", k, j));
+            const int cj = d->cutset_off[j + 1] - d->cutset_off[j];
+            od.push_back(ops[j].mat_off);
+            od.push_back(cj);
+            for (int r = 0; r < cj; ++r) {
+                const int ps = pos(d->cutset[d->cutset_off[j] + r]);
+                if (ps < 0) return (fail(nullptr, SL_EINVAL, "op %d: prev %d key outside the cutset", k, j));
+                od.push_back(ps);
+            }
+        }
+        o.n_child = d->children_off[k + 1] - d->children_off[k];
+        o.child_at = (int)od.size();
+        if (o.type == PARENT) {
+            for (int q = d->children_off[k]; q < d->children_off[k + 1]; ++q) {
+                const int ch = d->children[q];
+                if (ch < F || ch >= N) return (fail(nullptr, SL_EINVAL, "op %d: bad child %d", k, ch));
+                const bool mum = d->mother[ch] == o.peel;
+                const int other = mum ? d->father[ch] : d->mother[ch];
+                const int pc = pos(ch), po = pos(other);
+                if (pc < 0 || pc >= o.c || po < 0)
+                    return (fail(nullptr, SL_EINVAL, "op %d: child %d or its other parent not in the cutset", k, ch));
+                od.push_back(ch);
+                od.push_back(pc);
+                od.push_back(po);
+                od.push_back(mum ? 1 : 0);
+            }
+            max_child = std::max(max_child, o.n_child);
+        } else {
+            o.n_child = 0;
+        }
+        if (o.type == CHILD) {
+            if (o.peel < F) return (fail(nullptr, SL_EINVAL, "op %d: child peel of a founder", k));
+            o.mpos = pos(d->mother[o.peel]);
+            o.fpos = pos(d->father[o.peel]);
+            if (o.mpos < 0 || o.mpos >= o.c || o.fpos < 0 || o.fpos >= o.c)
+                return (fail(nullptr, SL_EINVAL, "op %d: parents of the child not in the cutset", k));
+        }
+        o.mat_off = arena;
+        arena += 1 << (2 * o.c);
+    }
+    if (ops[K - 1].c != 0) return (fail(nullptr, SL_EINVAL, "last op must have an empty cutset"));
+    if (max_child > 31) return (fail(nullptr, SL_EINVAL, "parent peel with %d children", max_child));
+
+    if (ops[K - 1].c != 0) return fail(nullptr, SL_EINVAL, "last op must have an empty cutset");
+    if (max_child > 31) return fail(nullptr, SL_EINVAL, "parent peel with %d children", max_child);
+    return SL_OK;
+}
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+const char* sl_version(void) { return "swiftlink_gb300 0.1 (sm_103a)"; }
+
+const char* sl_last_error(const sl_ctx* ctx) { return ctx ? ctx->err.c_str() : g_err.c_str(); }
+
+int64_t sl_launch_count(const sl_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+void sl_destroy(sl_ctx* ctx) {
+    if (!ctx) return;
+    int cur = 0;
+    cudaGetDevice(&cur);
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    for (void* p : ctx->owned) cudaFree(p);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    cudaSetDevice(cur);
+    delete ctx;
+}
+
+int sl_create(const sl_problem_desc* d, const sl_options* opt, sl_ctx** out) {
+    sl_ctx* ctx = nullptr;
+    if (!d || !opt || !out) return fail(ctx, SL_EINVAL, "null argument");
+    *out = nullptr;
+    const int N = d->n_members, F = d->n_founders, M = d->n_markers, K = d->n_ops, n = d->lod_per_interval;
+    if (N < 1 || F < 1 || F >= N || M < 2 || K < 1 || n < 1)
+        return fail(ctx, SL_EINVAL, "bad sizes N=%d F=%d M=%d K=%d n=%d", N, F, M, K, n);
+    if (N > 32000) return fail(ctx, SL_EINVAL, "pedigree too large (%d members)", N);
+    if (d->sex_linked) return fail(ctx, SL_EINVAL, "sex-linked analysis is not supported on the GPU");
+    if (opt->n_chains < 1) return fail(ctx, SL_EINVAL, "n_chains must be >= 1");
+    if (opt->lod_precision != SL_LOD_FP64 && opt->lod_precision != SL_LOD_FP32_RESCALED)
+        return fail(ctx, SL_EINVAL, "unknown lod_precision %d", opt->lod_precision);
+    for (int i = 0; i < N; ++i) {
+        const bool founder = d->mother[i] < 0;
+        if (founder != (i < F)) return fail(ctx, SL_EINVAL, "persons must be ordered founders first");
+        if (!founder && (d->mother[i] >= N || d->father[i] < 0 || d->father[i] >= N))
+            return fail(ctx, SL_EINVAL, "person %d has bad parents", i);
+    }
+    for (int l = 0; l + 1 < M; ++l)
+        if (!(d->theta[l] > 0.0 && d->theta[l] < 0.5 + 1e-12))
+            return fail(ctx, SL_EINVAL, "theta[%d]=%g out of (0, 0.5]", l, d->theta[l]);
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+        return fail(ctx, SL_ENODEV, "no CUDA device available");
+    if (opt->device < 0 || opt->device >= ndev) return fail(ctx, SL_EINVAL, "bad device %d", opt->device);
+
+    ctx = new sl_ctx();
+    ctx->device = opt->device;
+    ctx->n_chains = opt->n_chains;
+    ctx->lod_precision = opt->lod_precision;
+    int rc = SL_OK;
+    auto bail = [&](int code) { sl_destroy(ctx); return code; };
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return bail(fail(nullptr, SL_ECUDA, "cudaSetDevice failed"));
+    cudaDeviceProp prop;
+    cudaGetDeviceProperties(&prop, ctx->device);
+    ctx->sms = prop.multiProcessorCount;
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess)
+        return bail(fail(nullptr, SL_ECUDA, "stream creation failed"));
+
+    std::vector<OpDev> ops;
+    std::vector<int32_t> od;
+    int arena = 0, max_child = 1;
+    if ((rc = build_ops(d, ops, od, arena, max_child))) return bail(rc);
+
+    // ---- tables
+    build_priors(M, d->minor_freq, ctx->prior_table);
+    if (d->legal) {
+        ctx->legal.assign(d->legal, d->legal + (size_t)M * N);
+    } else {
+        int bad = -1;
+        if (!genotype_elimination(d, ctx->legal, &bad))
+            return bail(fail(nullptr, SL_EINVAL, "genotypes inconsistent at locus %d", bad));
+    }
+    std::vector<uint8_t> geno((size_t)M * N);
+    for (size_t i = 0; i < geno.size(); ++i) {
+        const int person = (int)(i % N);
+        const int g = d->typed[person] ? (d->genotypes[i] & 3) : 0;
+        geno[i] = (uint8_t)(g | (ctx->legal[i] << 4));
+    }
+    std::vector<int16_t> mo(N), fa(N), order;
+    std::vector<uint8_t> typed(N), dmask(N);
+    for (int i = 0; i < N; ++i) {
+        mo[i] = (int16_t)d->mother[i];
+        fa[i] = (int16_t)d->father[i];
+        typed[i] = d->typed[i] ? 1 : 0;
+        uint8_t m = 0;
+        for (int v = 0; v < 4; ++v)
+            if (d->disease_prob[4 * i + v] != 0.0) m |= (uint8_t)(1u << v);
+        dmask[i] = m;
+    }
+    {  // parents before children (descent_graph.cc:320-355)
+        std::vector<char> vis(N, 0);
+        for (int i = 0; i < F; ++i) { order.push_back((int16_t)i); vis[i] = 1; }
+        while ((int)order.size() < N) {
+            size_t before = order.size();
+            for (int i = F; i < N; ++i)
+                if (!vis[i] && vis[d->mother[i]] && vis[d->father[i]]) { order.push_back((int16_t)i); vis[i] = 1; }
+            if (order.size() == before) return bail(fail(nullptr, SL_EINVAL, "pedigree has a cycle"));
+        }
+    }
+    // non-ignorable meioses (markov_chain.cc:70-80, Person::safe_to_ignore_meiosis person.cc:208-222)
+    {
+        std::vector<int> nchild(N, 0);
+        for (int i = F; i < N; ++i) { nchild[d->mother[i]]++; nchild[d->father[i]]++; }
+        for (int m = 0; m < 2 * (N - F); ++m) {
+            const int person = F + m / 2;
+            const int parent = (m % 2 == 0) ? d->mother[person] : d->father[person];
+            const bool ignore = parent < F && nchild[parent] == 1;
+            if (!ignore) ctx->meioses.push_back(m);
+        }
+        if (ctx->meioses.empty()) ctx->meioses.push_back(0);
+    }
+    for (int l = 0; l < M; ++l) (l % 2 ? ctx->odd : ctx->even).push_back(l);
+
+    ProblemDev& P = ctx->P;
+    P.N = N; P.F = F; P.M = M; P.K = K; P.n_lod = n; P.Nnf = N - F;
+    P.W = (2 * (N - F) + 31) / 32;
+    P.arena = arena;
+    P.max_child = max_child;
+    P.fag_bytes = fag_bytes(N, F);
+    P.marker_trans = std::log(0.5) * (2 * (N - F));
+    if ((rc = upload(ctx, (int16_t**)&P.mother, mo.data(), N))) return bail(rc);
+    if ((rc = upload(ctx, (int16_t**)&P.father, fa.data(), N))) return bail(rc);
+    if ((rc = upload(ctx, (uint8_t**)&P.geno, geno.data(), geno.size()))) return bail(rc);
+    if ((rc = upload(ctx, (uint8_t**)&P.typed, typed.data(), N))) return bail(rc);
+    if ((rc = upload(ctx, (double**)&P.prior, ctx->prior_table.data(), ctx->prior_table.size()))) return bail(rc);
+    if ((rc = upload(ctx, (double**)&P.theta, d->theta, M - 1))) return bail(rc);
+    if ((rc = upload(ctx, (double**)&P.partial, d->partial_theta, M - 1))) return bail(rc);
+    if ((rc = upload(ctx, (double**)&P.minor, d->minor_freq, M))) return bail(rc);
+    if ((rc = upload(ctx, (double**)&P.dprob, d->disease_prob, (size_t)4 * N))) return bail(rc);
+    if ((rc = upload(ctx, (uint8_t**)&P.dmask, dmask.data(), N))) return bail(rc);
+    if ((rc = upload(ctx, (OpDev**)&P.ops, ops.data(), K))) return bail(rc);
+    if ((rc = upload(ctx, (int32_t**)&P.opdata, od.data(), od.size()))) return bail(rc);
+    if ((rc = upload(ctx, (int16_t**)&P.fag_order, order.data(), N))) return bail(rc);
+
+    // ---- launch shapes from the shared-memory footprint of one task
+    const size_t lsw = lsampler_smem_per_warp(P);
+    const size_t lodw = (size_t)arena * (ctx->lod_precision == SL_LOD_FP64 ? 8 : 4);
+    if (lsw > kSmemBudget || lodw > kSmemBudget)
+        return bail(fail(nullptr, SL_EINVAL, "peel sequence needs %zu bytes per task, above the shared-memory budget",
+                         std::max(lsw, lodw)));
+    ctx->ls_wpb = (int)std::max<size_t>(1, std::min<size_t>(4, kSmemBudget / lsw));
+    ctx->lod_wpb = (int)std::max<size_t>(1, std::min<size_t>(4, kSmemBudget / lodw));
+    const size_t per_sm = prop.sharedMemPerMultiprocessor;
+    const int ls_blocks = std::max(1, (int)std::min<size_t>(16, per_sm / (ctx->ls_wpb * lsw + 1024)));
+    const int lod_blocks = std::max(1, (int)std::min<size_t>(16, per_sm / (ctx->lod_wpb * lodw + 1024)));
+    ctx->ls_grid = ctx->sms * ls_blocks;
+    ctx->lod_grid = ctx->sms * lod_blocks;
+    int ms_threads = (int)(kSmemBudget / (size_t)P.fag_bytes) / 32 * 32;
+    ctx->ms_threads = std::max(32, std::min(256, ms_threads));
+    if ((size_t)ctx->ms_threads * P.fag_bytes > kSmemBudget)
+        return bail(fail(nullptr, SL_EINVAL, "founder-allele graph state too large for shared memory"));
+
+    // ---- state buffers
+    const int C = ctx->n_chains;
+    const int64_t npos = (int64_t)(M - 1) * n;
+    if ((rc = dev_alloc(ctx, &ctx->d_dg, (size_t)C * M * P.W))) return bail(rc);
+    CK(cudaMemset(ctx->d_dg, 0, sizeof(uint32_t) * (size_t)C * M * P.W));
+    if ((rc = dev_alloc(ctx, &ctx->d_acc, npos))) return bail(rc);
+    if ((rc = dev_alloc(ctx, &ctx->d_init, npos))) return bail(rc);
+    ctx->vals_graphs = std::max(C, 64);
+    if ((rc = dev_alloc(ctx, &ctx->d_vals, (size_t)ctx->vals_graphs * npos))) return bail(rc);
+    if ((rc = dev_alloc(ctx, &ctx->d_raw, (size_t)C * 2 * M))) return bail(rc);
+    if ((rc = dev_alloc(ctx, &ctx->d_fb, (size_t)C * 2 * M))) return bail(rc);
+    if ((rc = dev_alloc(ctx, &ctx->d_status, 1))) return bail(rc);
+    if ((rc = dev_alloc(ctx, &ctx->d_sel, C))) return bail(rc);
+    if ((rc = upload(ctx, &ctx->d_even, ctx->even.data(), ctx->even.size()))) return bail(rc);
+    if ((rc = upload(ctx, &ctx->d_odd, ctx->odd.data(), ctx->odd.size()))) return bail(rc);
+    if ((rc = upload(ctx, &ctx->d_meioses, ctx->meioses.data(), ctx->meioses.size()))) return bail(rc);
+    if ((rc = dev_alloc(ctx, &ctx->d_morder, (size_t)C * ctx->meioses.size()))) return bail(rc);
+    if ((rc = dev_alloc(ctx, &ctx->d_loci, M))) return bail(rc);
+    CK(cudaMemset(ctx->d_status, 0, sizeof(int)));
+    CK(cudaMemset(ctx->d_acc, 0, sizeof(double) * npos));
+    CK(cudaMemset(ctx->d_init, 0, npos));
+    ctx->trait_prob = host_trait_prob(d, ops, od, arena);
+    *out = ctx;
+    return SL_OK;
+}
+
+static int check_chains(sl_ctx* ctx, int first, int n) {
+    if (!ctx) return fail(ctx, SL_EINVAL, "null context");
+    if (first < 0 || n < 1 || first + n > ctx->n_chains)
+        return fail(ctx, SL_EINVAL, "chains [%d, %d) outside [0, %d)", first, first + n, ctx->n_chains);
+    return SL_OK;
+}
+
+static int status_to_code(sl_ctx* ctx, int st) {
+    switch (st) {
+        case ST_OK: return SL_OK;
+        case ST_ZERO_LIK: return fail(ctx, SL_EZERO, "likelihood is zero (check the penetrance function)");
+        case ST_ILLEGAL_DG: return fail(ctx, SL_EILLEGAL, "illegal descent graph given to a sampler");
+        case ST_LOD_NONPOS: return fail(ctx, SL_EZERO, "trait peel gave a likelihood of 0.0 or less");
+    }
+    return fail(ctx, SL_ECUDA, "unknown device status %d", st);
+}
+
+int sl_synchronize(sl_ctx* ctx) {
+    if (!ctx) return fail(ctx, SL_EINVAL, "null context");
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaStreamSynchronize(ctx->stream));
+    int st = 0;
+    CK(cudaMemcpy(&st, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost));
+    if (st) {
+        CK(cudaMemset(ctx->d_status, 0, sizeof(int)));
+        return status_to_code(ctx, st);
+    }
+    return SL_OK;
+}
+
+int sl_device_status(sl_ctx* ctx, int32_t* status) {
+    if (!ctx || !status) return fail(ctx, SL_EINVAL, "null argument");
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaStreamSynchronize(ctx->stream));
+    int st = 0;
+    CK(cudaMemcpy(&st, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost));
+    *status = st;
+    return SL_OK;
+}
+
+int sl_set_descent_graphs(sl_ctx* ctx, int32_t first, int32_t n, const int32_t* dg) {
+    int rc = check_chains(ctx, first, n);
+    if (rc) return rc;
+    if (!dg) return fail(ctx, SL_EINVAL, "null descent graph");
+    const ProblemDev& P = ctx->P;
+    const size_t words = (size_t)P.M * P.W;
+    std::vector<uint32_t> buf(words * n);
+    for (int i = 0; i < n; ++i)
+        pack_graph(dg + (size_t)i * 2 * P.N * P.M, P.N, P.F, P.M, P.W, buf.data() + words * i);
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaMemcpyAsync(ctx->d_dg + words * first, buf.data(), sizeof(uint32_t) * words * n, cudaMemcpyHostToDevice,
+                       ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return SL_OK;
+}
+
+int sl_get_descent_graphs(sl_ctx* ctx, int32_t first, int32_t n, int32_t* dg) {
+    int rc = check_chains(ctx, first, n);
+    if (rc) return rc;
+    if (!dg) return fail(ctx, SL_EINVAL, "null descent graph");
+    const ProblemDev& P = ctx->P;
+    const size_t words = (size_t)P.M * P.W;
+    std::vector<uint32_t> buf(words * n);
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaMemcpyAsync(buf.data(), ctx->d_dg + words * first, sizeof(uint32_t) * words * n, cudaMemcpyDeviceToHost,
+                       ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    for (int i = 0; i < n; ++i)
+        unpack_graph(buf.data() + words * i, P.N, P.F, P.M, P.W, dg + (size_t)i * 2 * P.N * P.M);
+    return SL_OK;
+}
+
+int sl_get_trait_priors(sl_ctx* ctx, double* out) {
+    if (!ctx || !out) return fail(ctx, SL_EINVAL, "null argument");
+    const ProblemDev& P = ctx->P;
+    // reconstruct [M][N][4] from the genotype codes the context holds
+    std::vector<uint8_t> geno((size_t)P.M * P.N);
+    CK(cudaMemcpy(geno.data(), P.geno, geno.size(), cudaMemcpyDeviceToHost));
+    for (int l = 0; l < P.M; ++l)
+        for (int i = 0; i < P.N; ++i) {
+            const int g = geno[(size_t)l * P.N + i] & 3;
+            for (int v = 0; v < 4; ++v)
+                out[((size_t)l * P.N + i) * 4 + v] = ctx->prior_table[((size_t)l * 4 + g) * 4 + v];
+        }
+    return SL_OK;
+}
+
+int sl_get_legal_masks(sl_ctx* ctx, uint8_t* out) {
+    if (!ctx || !out) return fail(ctx, SL_EINVAL, "null argument");
+    std::memcpy(out, ctx->legal.data(), ctx->legal.size());
+    return SL_OK;
+}
+
+static int stage_draws(sl_ctx* ctx, const double* u, size_t n) {
+    if (n > ctx->u_cap) {
+        if (ctx->d_u) {
+            cudaFree(ctx->d_u);
+            ctx->owned.erase(std::find(ctx->owned.begin(), ctx->owned.end(), (void*)ctx->d_u));
+            ctx->d_u = nullptr;
+        }
+        int rc = dev_alloc(ctx, &ctx->d_u, n);
+        if (rc) return rc;
+        ctx->u_cap = n;
+    }
+    CK(cudaMemcpyAsync(ctx->d_u, u, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+    return SL_OK;
+}
+
+int sl_lsampler_loci(sl_ctx* ctx, int32_t first, int32_t n_chains, const int32_t* loci, int32_t n_loci,
+                     const double* u, int64_t ucs, int64_t uls) {
+    int rc = check_chains(ctx, first, n_chains);
+    if (rc) return rc;
+    const ProblemDev& P = ctx->P;
+    if (!loci || n_loci < 1 || n_loci > P.M || !u) return fail(ctx, SL_EINVAL, "bad locus list or draws");
+    std::vector<int32_t> sorted(loci, loci + n_loci);
+    std::sort(sorted.begin(), sorted.end());
+    for (int i = 0; i < n_loci; ++i) {
+        if (sorted[i] < 0 || sorted[i] >= P.M) return fail(ctx, SL_EINVAL, "locus %d out of range", sorted[i]);
+        if (i && sorted[i] - sorted[i - 1] < 2)
+            return fail(ctx, SL_EINVAL, "loci %d and %d interfere (adjacent or repeated)", sorted[i - 1], sorted[i]);
+    }
+    if (uls < P.K + 2 * P.N || ucs < (int64_t)P.M * uls)
+        return fail(ctx, SL_EINVAL, "draw strides too small (need locus stride >= K + 2N)");
+    CK(cudaSetDevice(ctx->device));
+    if ((rc = stage_draws(ctx, u, (size_t)n_chains * ucs))) return rc;
+    CK(cudaMemcpyAsync(ctx->d_loci, loci, sizeof(int32_t) * n_loci, cudaMemcpyHostToDevice, ctx->stream));
+    CK(launch_lsampler(P, ctx->d_dg, first, n_chains, ctx->d_loci, n_loci, ctx->d_u, ucs, uls, 0, 0, nullptr, 0,
+                       ctx->d_status, ctx->stream, ctx->ls_grid, ctx->ls_wpb));
+    ctx->launches++;
+    return sl_synchronize(ctx);
+}
+
+int sl_lsampler_sweep(sl_ctx* ctx, int32_t first, int32_t n_chains, const double* u, int64_t ucs, int64_t uls) {
+    int rc = check_chains(ctx, first, n_chains);
+    if (rc) return rc;
+    const ProblemDev& P = ctx->P;
+    if (!u) return fail(ctx, SL_EINVAL, "null draws");
+    if (uls < P.K + 2 * P.N || ucs < (int64_t)P.M * uls)
+        return fail(ctx, SL_EINVAL, "draw strides too small (need locus stride >= K + 2N)");
+    CK(cudaSetDevice(ctx->device));
+    if ((rc = stage_draws(ctx, u, (size_t)n_chains * ucs))) return rc;
+    CK(launch_lsampler(P, ctx->d_dg, first, n_chains, ctx->d_even, (int)ctx->even.size(), ctx->d_u, ucs, uls, 0, 0,
+                       nullptr, 0, ctx->d_status, ctx->stream, ctx->ls_grid, ctx->ls_wpb));
+    CK(launch_lsampler(P, ctx->d_dg, first, n_chains, ctx->d_odd, (int)ctx->odd.size(), ctx->d_u, ucs, uls, 0, 0,
+                       nullptr, 0, ctx->d_status, ctx->stream, ctx->ls_grid, ctx->ls_wpb));
+    ctx->launches += 2;
+    return sl_synchronize(ctx);
+}
+
+int sl_msampler_sweep(sl_ctx* ctx, int32_t first, int32_t n_chains, const int32_t* meioses, int32_t n_meioses,
+                      const double* u, int64_t ucs) {
+    int rc = check_chains(ctx, first, n_chains);
+    if (rc) return rc;
+    const ProblemDev& P = ctx->P;
+    if (!meioses || n_meioses < 1 || !u) return fail(ctx, SL_EINVAL, "bad meiosis list or draws");
+    for (int j = 0; j < n_meioses; ++j)
+        if (meioses[j] < 0 || meioses[j] >= 2 * P.Nnf) return fail(ctx, SL_EINVAL, "meiosis %d out of range", meioses[j]);
+    if (ucs < (int64_t)n_meioses * P.M) return fail(ctx, SL_EINVAL, "draw stride too small (need n_meioses * M)");
+    CK(cudaSetDevice(ctx->device));
+    if ((size_t)n_meioses > ctx->mlist_cap) {
+        if (ctx->d_mlist) {
+            cudaFree(ctx->d_mlist);
+            ctx->owned.erase(std::find(ctx->owned.begin(), ctx->owned.end(), (void*)ctx->d_mlist));
+            ctx->d_mlist = nullptr;
+        }
+        if ((rc = dev_alloc(ctx, &ctx->d_mlist, n_meioses))) return rc;
+        ctx->mlist_cap = n_meioses;
+    }
+    if ((rc = stage_draws(ctx, u, (size_t)n_chains * ucs))) return rc;
+    CK(cudaMemcpyAsync(ctx->d_mlist, meioses, sizeof(int32_t) * n_meioses, cudaMemcpyHostToDevice, ctx->stream));
+    CK(launch_msampler(P, ctx->d_dg, first, n_chains, ctx->d_mlist, 0, n_meioses, ctx->d_u, ucs, 0, 0, nullptr, 0,
+                       ctx->d_raw, ctx->d_fb, ctx->d_status, ctx->ms_threads, ctx->stream));
+    ctx->launches++;
+    return sl_synchronize(ctx);
+}
+
+static int score_device_graphs(sl_ctx* ctx, const uint32_t* graphs, int G) {
+    const ProblemDev& P = ctx->P;
+    const int64_t npos = (int64_t)(P.M - 1) * P.n_lod;
+    for (int g0 = 0; g0 < G; g0 += ctx->vals_graphs) {
+        const int g = std::min(ctx->vals_graphs, G - g0);
+        CK(launch_lod(P, ctx->lod_precision, graphs + (size_t)g0 * P.M * P.W, (int64_t)P.M * P.W, g, ctx->d_vals,
+                      ctx->d_status, ctx->stream, ctx->lod_grid, ctx->lod_wpb));
+        CK(launch_lod_merge(ctx->d_vals, g, npos, ctx->d_acc, ctx->d_init, ctx->stream));
+        ctx->launches += 2;
+    }
+    ctx->lod_count += G;
+    return SL_OK;
+}
+
+int sl_lod_score_chains(sl_ctx* ctx, int32_t first, int32_t n_chains) {
+    int rc = check_chains(ctx, first, n_chains);
+    if (rc) return rc;
+    CK(cudaSetDevice(ctx->device));
+    return score_device_graphs(ctx, ctx->d_dg + (size_t)first * ctx->P.M * ctx->P.W, n_chains);
+}
+
+int sl_lod_score_graphs(sl_ctx* ctx, int32_t n_graphs, const int32_t* dgs) {
+    if (!ctx || n_graphs < 1 || !dgs) return fail(ctx, SL_EINVAL, "bad graph set");
+    const ProblemDev& P = ctx->P;
+    const size_t words = (size_t)P.M * P.W;
+    CK(cudaSetDevice(ctx->device));
+    if (n_graphs > ctx->graphs_cap) {
+        if (ctx->d_graphs) {
+            cudaStreamSynchronize(ctx->stream);
+            cudaFree(ctx->d_graphs);
+            ctx->owned.erase(std::find(ctx->owned.begin(), ctx->owned.end(), (void*)ctx->d_graphs));
+            ctx->d_graphs = nullptr;
+        }
+        int rc = dev_alloc(ctx, &ctx->d_graphs, words * n_graphs);
+        if (rc) return rc;
+        ctx->graphs_cap = n_graphs;
+    }
+    std::vector<uint32_t> buf(words * n_graphs);
+    for (int i = 0; i < n_graphs; ++i)
+        pack_graph(dgs + (size_t)i * 2 * P.N * P.M, P.N, P.F, P.M, P.W, buf.data() + words * i);
+    CK(cudaMemcpyAsync(ctx->d_graphs, buf.data(), sizeof(uint32_t) * words * n_graphs, cudaMemcpyHostToDevice,
+                       ctx->stream));
+    int rc = score_device_graphs(ctx, ctx->d_graphs, n_graphs);
+    if (rc) return rc;
+    return sl_synchronize(ctx);
+}
+
+int sl_lod_results(sl_ctx* ctx, double* raw, uint64_t* count, double* trait_prob) {
+    if (!ctx) return fail(ctx, SL_EINVAL, "null context");
+    int rc = sl_synchronize(ctx);
+    if (rc) return rc;
+    const int64_t npos = (int64_t)(ctx->P.M - 1) * ctx->P.n_lod;
+    if (raw) CK(cudaMemcpy(raw, ctx->d_acc, sizeof(double) * npos, cudaMemcpyDeviceToHost));
+    if (count) *count = ctx->lod_count;
+    if (trait_prob) *trait_prob = ctx->trait_prob;
+    return SL_OK;
+}
+
+int sl_lod_reset(sl_ctx* ctx) {
+    if (!ctx) return fail(ctx, SL_EINVAL, "null context");
+    const int64_t npos = (int64_t)(ctx->P.M - 1) * ctx->P.n_lod;
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaMemsetAsync(ctx->d_acc, 0, sizeof(double) * npos, ctx->stream));
+    CK(cudaMemsetAsync(ctx->d_init, 0, npos, ctx->stream));
+    ctx->lod_count = 0;
+    return sl_synchronize(ctx);
+}
+
+static int check_desc(const sl_problem_desc* d) {
+    if (!d) return fail(nullptr, SL_EINVAL, "null problem");
+    if (d->n_members < 2 || d->n_founders < 1 || d->n_founders >= d->n_members || d->n_markers < 2 || d->n_ops < 1)
+        return fail(nullptr, SL_EINVAL, "bad problem sizes");
+    return SL_OK;
+}
+
+int sl_problem_legal_masks(const sl_problem_desc* d, uint8_t* out) {
+    int rc = check_desc(d);
+    if (rc) return rc;
+    if (!out) return fail(nullptr, SL_EINVAL, "null output");
+    std::vector<uint8_t> legal;
+    int bad = -1;
+    if (!genotype_elimination(d, legal, &bad)) return fail(nullptr, SL_EINVAL, "genotypes inconsistent at locus %d", bad);
+    std::memcpy(out, legal.data(), legal.size());
+    return SL_OK;
+}
+
+int sl_problem_trait_priors(const sl_problem_desc* d, double* out) {
+    int rc = check_desc(d);
+    if (rc) return rc;
+    if (!out) return fail(nullptr, SL_EINVAL, "null output");
+    std::vector<double> table;
+    build_priors(d->n_markers, d->minor_freq, table);
+    const int N = d->n_members;
+    for (int l = 0; l < d->n_markers; ++l)
+        for (int i = 0; i < N; ++i) {
+            const int g = d->typed[i] ? (d->genotypes[(size_t)l * N + i] & 3) : 0;
+            for (int v = 0; v < 4; ++v) out[((size_t)l * N + i) * 4 + v] = table[((size_t)l * 4 + g) * 4 + v];
+        }
+    return SL_OK;
+}
+
+int sl_problem_trait_prob(const sl_problem_desc* d, double* out) {
+    int rc = check_desc(d);
+    if (rc) return rc;
+    if (!out) return fail(nullptr, SL_EINVAL, "null output");
+    std::vector<OpDev> ops;
+    std::vector<int32_t> od;
+    int arena = 0, max_child = 1;
+    if ((rc = build_ops(d, ops, od, arena, max_child))) return rc;
+    *out = host_trait_prob(d, ops, od, arena);
+    return SL_OK;
+}
+
+int sl_run(sl_ctx* ctx, const sl_run_options* o) {
+    if (!ctx || !o) return fail(ctx, SL_EINVAL, "null argument");
+    if (o->iterations < 0 || o->burnin < 0 || o->scoring_period < 1 || o->first_iteration < 0 ||
+        !(o->lsampler_prob >= 0.0 && o->lsampler_prob <= 1.0))
+        return fail(ctx, SL_EINVAL, "bad run options");
+    CK(cudaSetDevice(ctx->device));
+    const ProblemDev& P = ctx->P;
+    const int C = ctx->n_chains;
+    const int nm = (int)ctx->meioses.size();
+    const int total = o->burnin + o->iterations;
+    for (int it = o->first_iteration; it < total; ++it) {
+        const uint64_t iter = (uint64_t)it;
+        CK(launch_choose(0, C, o->seed, iter, o->lsampler_prob, ctx->d_sel, ctx->stream));
+        CK(launch_lsampler(P, ctx->d_dg, 0, C, ctx->d_even, (int)ctx->even.size(), nullptr, 0, 0, o->seed, iter,
+                           ctx->d_sel, 1, ctx->d_status, ctx->stream, ctx->ls_grid, ctx->ls_wpb));
+        CK(launch_lsampler(P, ctx->d_dg, 0, C, ctx->d_odd, (int)ctx->odd.size(), nullptr, 0, 0, o->seed, iter,
+                           ctx->d_sel, 1, ctx->d_status, ctx->stream, ctx->ls_grid, ctx->ls_wpb));
+        CK(launch_shuffle(ctx->d_meioses, nm, ctx->d_morder, 0, C, o->seed, iter, ctx->stream));
+        CK(launch_msampler(P, ctx->d_dg, 0, C, ctx->d_morder, nm, nm, nullptr, 0, o->seed, iter, ctx->d_sel, 0,
+                           ctx->d_raw, ctx->d_fb, ctx->d_status, ctx->ms_threads, ctx->stream));
+        ctx->launches += 5;
+        if (it >= o->burnin && it % o->scoring_period == 0) {
+            int rc = score_device_graphs(ctx, ctx->d_dg, C);
+            if (rc) return rc;
+        }
+    }
+    return SL_OK;
+}
+
+}  // extern "C"

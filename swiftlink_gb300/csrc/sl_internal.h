@@ -1,0 +1,49 @@
+// Internal layouts shared by the host code (sl_host.cc) and the kernels
+// (sl_kernels.cu).  Not part of the public C ABI.
+#pragma once
+
+#include <stdint.h>
+
+namespace sl {
+
+enum { UU = 0, AA = 1, AU = 2, UA = 3 };                              // trait.h:21-27
+enum { G_UNTYPED = 0, G_HETERO = 1, G_HOMOZ_A = 2, G_HOMOZ_B = 3 };   // genotype.h:26-31
+enum { CHILD = 1, PARENT = 2, PARTNER = 3, LAST = 4 };                // peeling.h:16-22
+
+// Status codes written by kernels into the context's device status word.
+enum { ST_OK = 0, ST_ZERO_LIK = 1, ST_ILLEGAL_DG = 2, ST_LOD_NONPOS = 3 };
+
+// One peel operation as the kernels read it.  Every field is warp-uniform.
+struct OpDev {
+    int32_t type, peel, c, n_prev, n_child;
+    int32_t cut_at;    // opdata offset: c person ids (reference key order)
+    int32_t prev_at;   // opdata offset: per prev [op index, c', pos_0 .. pos_{c'-1}]
+    int32_t child_at;  // opdata offset: per child [child id, child pos, other-parent pos, peel is mother]
+    int32_t mpos, fpos;  // child peel: cutset positions of the mother and the father
+    int32_t mat_off;     // offset of this op's dense 4^c matrix in a task's arena
+    int32_t pad;
+};
+
+// Everything a kernel needs about one problem; passed by value.
+struct ProblemDev {
+    int32_t N, F, M, K, n_lod, Nnf, W;   // W = 32-bit words per descent-graph column
+    int32_t arena;                       // sum over ops of 4^c
+    int32_t max_child;                   // max children of an op (>= 1)
+    int32_t fag_bytes;                   // shared bytes one FAG evaluation needs
+    double marker_trans;                 // log(0.5) * 2 * Nnf (descent_graph.cc:22)
+    const int16_t* mother;               // [N], -1 for founders
+    const int16_t* father;
+    const uint8_t* geno;                 // [M][N]: bits 0-1 genotype code, bits 4-7 legal mask
+    const uint8_t* typed;                // [N]
+    const double* prior;                 // [M][4 genotype codes][4 states]
+    const double* theta;                 // [M-1]
+    const double* partial;               // [M-1]
+    const double* minor;                 // [M]
+    const double* dprob;                 // [N][4]
+    const uint8_t* dmask;                // [N] bit v set when dprob[v] != 0
+    const OpDev* ops;                    // [K]
+    const int32_t* opdata;
+    const int16_t* fag_order;            // [N] parents before children, founders first
+};
+
+}  // namespace sl

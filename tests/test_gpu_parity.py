@@ -1,0 +1,251 @@
+"""GPU parity: the CUDA kernels, called through the C ABI, against the
+reference's golden vectors and against the C restatement of the reference on
+seeded inputs.
+
+Bars: descent-graph updates bit-exact (integer work); FP64 LOD within
+|dLOD| <= 1e-10; FP32-rescaled LOD within |dLOD| <= 1e-3 (the target stated
+for the batched form).
+"""
+import numpy as np
+import pytest
+
+from conftest import CASES, GOLDEN, load_golden, _lists
+import philox_np
+from oracle import port
+from swiftlink_gb300 import api
+
+pytestmark = pytest.mark.gpu
+
+FP64_LOD_TOL = 1e-10
+FP32_LOD_TOL = 1e-3
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    from swiftlink_gb300 import build
+    build.build()
+    port.build()
+
+
+def make_ctx(g, n_chains=1, precision=api.SL_LOD_FP64):
+    return api.Context(api.Problem.from_arrays(g), n_chains=n_chains, lod_precision=precision)
+
+
+def stride_of(g):
+    return g["K"] + 2 * g["N"]
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_lsteps_bit_exact(name):
+    g = load_golden(name)
+    with make_ctx(g) as ctx:
+        ctx.set_graphs(g["dg0"])
+        for i, l in enumerate(g["lstep_loci"]):
+            u = np.zeros((1, g["M"], stride_of(g)))
+            u[0, l] = g["lstep_u"][i]
+            ctx.lsampler_loci([int(l)], u)
+            assert np.array_equal(ctx.get_graphs()[0], g["lstep_after"][i]), f"locus {l}"
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_lsweep_bit_exact(name):
+    g = load_golden(name)
+    with make_ctx(g) as ctx:
+        ctx.set_graphs(g["dg0"])
+        ctx.lsampler_sweep(g["lsweep_u"][None])
+        assert np.array_equal(ctx.get_graphs()[0], g["lsweep_after"])
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_msweep_bit_exact(name):
+    g = load_golden(name)
+    with make_ctx(g) as ctx:
+        ctx.set_graphs(g["lsweep_after"])
+        ctx.msampler_sweep(g["msweep_order"], g["msweep_u"][None])
+        assert np.array_equal(ctx.get_graphs()[0], g["msweep_after"])
+
+
+@pytest.mark.parametrize("name", CASES)
+@pytest.mark.parametrize("precision,tol", [(api.SL_LOD_FP64, FP64_LOD_TOL),
+                                           (api.SL_LOD_FP32_RESCALED, FP32_LOD_TOL)])
+def test_lod_against_reference(name, precision, tol):
+    g = load_golden(name)
+    with make_ctx(g, precision=precision) as ctx:
+        ctx.lod_score_graphs(g["lod_graphs"])
+        raw, cnt, tp = ctx.lod_results()
+    assert cnt == g["lod_count"]
+    assert abs(tp - g["lod_trait_prob"]) <= 1e-12 * max(1.0, abs(tp))
+    got = api.lod_table(raw, cnt, tp)
+    want = api.lod_table(g["lod_raw"], g["lod_count"], g["lod_trait_prob"])
+    err = np.abs(got - want).max()
+    assert err <= tol, err
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_lod_chains_equals_graphs(name):
+    """Scoring resident chains gives the same table as scoring uploaded graphs."""
+    g = load_golden(name)
+    graphs = g["lod_graphs"]
+    with make_ctx(g, n_chains=graphs.shape[0]) as ctx:
+        ctx.set_graphs(graphs)
+        ctx.lod_score_chains()
+        a = ctx.lod_results()
+        ctx.lod_reset()
+        ctx.lod_score_graphs(graphs)
+        b = ctx.lod_results()
+    np.testing.assert_array_equal(a[0], b[0])
+    assert a[1] == b[1] == graphs.shape[0]
+
+
+def test_multichain_batch_matches_port():
+    g = load_golden("cfg1")
+    P = port.Port(g)
+    C = 4
+    rng = np.random.default_rng(7)
+    st = stride_of(g)
+    ul = rng.random((C, g["M"], st))
+    order = g["msweep_order"]
+    um = rng.random((C, order.size, g["M"]))
+    with make_ctx(g, n_chains=C) as ctx:
+        ctx.set_graphs(np.stack([g["dg0"]] * C))
+        ctx.lsampler_sweep(ul, n_chains=C)
+        ctx.msampler_sweep(order, um, n_chains=C)
+        out = ctx.get_graphs()
+    for c in range(C):
+        dg = g["dg0"].copy()
+        for l in list(range(0, g["M"], 2)) + list(range(1, g["M"], 2)):
+            dg, _ = P.lstep(dg, l, ul[c, l])
+        dg, _ = P.msweep(dg, order, um[c])
+        assert np.array_equal(out[c], dg), f"chain {c}"
+
+
+def load_problem(name):
+    z = np.load(f"{GOLDEN}/{name}_problem.npz")
+    d = {k: z[k] for k in z.files}
+    for k in ("op_cutset", "op_prev", "op_children"):
+        d[k] = _lists(d.pop(k + "_off"), d.pop(k + "_flat"))
+    for k in ("N", "F", "M", "K", "n_lod"):
+        d[k] = int(d[k])
+    n = d["M"] * d["N"] * 2
+    d["dg0"] = np.unpackbits(d.pop("dg0_bits"))[:n].reshape(d["M"], d["N"], 2).astype(np.int32)
+    return d
+
+
+def test_cfg2_seeded_against_port():
+    """120 members, 2000 markers: sweeps bit-exact and LOD within tolerance."""
+    d = load_problem("cfg2")
+    prob = api.Problem.from_arrays(d, with_legal=False)
+    C = 2
+    with api.Context(prob, n_chains=C) as ctx:
+        d["legal"] = ctx.legal_masks()
+        d["trait_prior"] = ctx.trait_priors()
+        P = port.Port(d)
+        rng = np.random.default_rng(2)
+        st = d["K"] + 2 * d["N"]
+        ul = rng.random((C, d["M"], st))
+        order = d["meioses"].copy()
+        rng.shuffle(order)
+        order = order[:24]
+        um = rng.random((C, order.size, d["M"]))
+        ctx.set_graphs(np.stack([d["dg0"]] * C))
+        ctx.lsampler_sweep(ul, n_chains=C)
+        ctx.msampler_sweep(order, um, n_chains=C)
+        out = ctx.get_graphs()
+        ctx.lod_score_chains()
+        raw64, cnt, tp = ctx.lod_results()
+    want = []
+    for c in range(C):
+        dg = d["dg0"].copy()
+        for l in list(range(0, d["M"], 2)) + list(range(1, d["M"], 2)):
+            dg, _ = P.lstep(dg, l, ul[c, l])
+        dg, _ = P.msweep(dg, order, um[c])
+        assert np.array_equal(out[c], dg), f"chain {c}"
+        want.append(dg)
+    ref_raw, ref_cnt, ref_tp = P.lod(np.stack(want))
+    assert cnt == ref_cnt
+    lod_ref = api.lod_table(ref_raw, ref_cnt, ref_tp)
+    assert np.abs(api.lod_table(raw64, cnt, tp) - lod_ref).max() <= FP64_LOD_TOL
+    with api.Context(prob, n_chains=C, lod_precision=api.SL_LOD_FP32_RESCALED) as c32:
+        c32.set_graphs(np.stack(want))
+        c32.lod_score_chains()
+        raw32, cnt32, tp32 = c32.lod_results()
+    assert np.abs(api.lod_table(raw32, cnt32, tp32) - lod_ref).max() <= FP32_LOD_TOL
+
+
+def replay_run(P, g, dgs, seed, iters, lprob, period, burnin):
+    """Host replay of sl_run's schedule with the same Philox streams."""
+    M, K, N = g["M"], g["K"], g["N"]
+    st = K + 2 * N
+    base = g["meioses"]
+    scored = []
+    for it in range(iters + burnin):
+        for c in range(len(dgs)):
+            if philox_np.chooses_l(seed, c, it, lprob):
+                u = philox_np.lsweep_draws(seed, c, it, M, st)
+                for l in list(range(0, M, 2)) + list(range(1, M, 2)):
+                    dgs[c], _ = P.lstep(dgs[c], l, u[l])
+            else:
+                order = philox_np.shuffled(seed, c, it, base)
+                u = philox_np.msweep_draws(seed, c, it, order.size, M)
+                dgs[c], _ = P.msweep(dgs[c], order, u)
+        if it >= burnin and it % period == 0:
+            scored.extend(d.copy() for d in dgs)
+    return dgs, scored
+
+
+@pytest.mark.parametrize("name", ["loop", "cfg1"])
+def test_device_run_matches_host_replay(name):
+    g = load_golden(name)
+    P = port.Port(g)
+    C, seed, iters, burnin, period = 3, 99, 6, 1, 2
+    with make_ctx(g, n_chains=C) as ctx:
+        ctx.set_graphs(np.stack([g["dg0"]] * C))
+        ctx.run(iterations=iters, burnin=burnin, period=period, lprob=0.5, seed=seed)
+        ctx.synchronize()
+        out = ctx.get_graphs()
+        raw, cnt, tp = ctx.lod_results()
+    dgs, scored = replay_run(P, g, [g["dg0"].copy() for _ in range(C)], seed, iters, 0.5, period, burnin)
+    for c in range(C):
+        assert np.array_equal(out[c], dgs[c]), f"chain {c}"
+    ref_raw, ref_cnt, ref_tp = P.lod(np.stack(scored))
+    assert cnt == ref_cnt
+    assert np.abs(api.lod_table(raw, cnt, tp) - api.lod_table(ref_raw, ref_cnt, ref_tp)).max() <= FP64_LOD_TOL
+
+
+def test_illegal_graph_reports_error_and_context_recovers():
+    g = load_golden("cfg1")
+    P = port.Port(g)
+    dg = g["dg0"].copy()
+    # flip meioses until some column becomes illegal (zero founder-allele-graph likelihood)
+    bad = None
+    for l in range(g["M"]):
+        for i in range(g["F"], g["N"]):
+            for par in (0, 1):
+                dg[l, i, par] ^= 1
+                if P.fag(dg, l) == 0.0:
+                    bad = (l, i, par)
+                    break
+                dg[l, i, par] ^= 1
+            if bad:
+                break
+        if bad:
+            break
+    if bad is None:
+        pytest.skip("no single flip makes this pedigree illegal")
+    with make_ctx(g) as ctx:
+        ctx.set_graphs(dg)
+        order = g["msweep_order"]
+        with pytest.raises(api.SwiftLinkError) as e:
+            ctx.msampler_sweep(order, np.full((1, order.size, g["M"]), 0.5))
+        assert e.value.code == api.SL_EILLEGAL
+        ctx.set_graphs(g["lsweep_after"])
+        ctx.msampler_sweep(order, g["msweep_u"][None])
+        assert np.array_equal(ctx.get_graphs()[0], g["msweep_after"])
+
+
+def test_rejects_interfering_loci():
+    g = load_golden("loop")
+    with make_ctx(g) as ctx:
+        with pytest.raises(api.SwiftLinkError) as e:
+            ctx.lsampler_loci([0, 1], np.zeros((1, g["M"], stride_of(g))))
+        assert e.value.code == api.SL_EINVAL

@@ -1,0 +1,144 @@
+"""Pin the C restatement of the reference (oracle/sl_oracle.c) before trusting it.
+
+1. Against the committed golden vectors written by the reference's own code
+   (tests/golden/make_golden.py): bit-identical descent graphs after L-steps,
+   an L-sweep and an M-sweep, and LOD log-sums.
+2. Against the reference build itself (oracle/_ref), on freshly seeded inputs,
+   where that build exists (the development container only).
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import load_golden, CASES
+from oracle import port, ref
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    port.build()
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_port_lsteps_match_golden(name):
+    g = load_golden(name)
+    P = port.Port(g)
+    dg = g["dg0"].copy()
+    for i, l in enumerate(g["lstep_loci"]):
+        dg, used = P.lstep(dg, int(l), g["lstep_u"][i])
+        assert used == g["lstep_used"][i]
+        assert np.array_equal(dg, g["lstep_after"][i]), f"locus {l}"
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_port_lsweep_matches_golden(name):
+    g = load_golden(name)
+    P = port.Port(g)
+    dg = g["dg0"].copy()
+    M = g["M"]
+    for l in list(range(0, M, 2)) + list(range(1, M, 2)):
+        dg, _ = P.lstep(dg, l, g["lsweep_u"][l])
+    assert np.array_equal(dg, g["lsweep_after"])
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_port_msweep_matches_golden(name):
+    g = load_golden(name)
+    P = port.Port(g)
+    dg, used = P.msweep(g["lsweep_after"], g["msweep_order"], g["msweep_u"])
+    assert np.array_equal(dg, g["msweep_after"])
+    assert np.array_equal(used, g["msweep_used"])
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_port_lod_matches_golden(name):
+    g = load_golden(name)
+    P = port.Port(g)
+    raw, cnt, tp = P.lod(g["lod_graphs"])
+    assert cnt == g["lod_count"]
+    assert tp == g["lod_trait_prob"]
+    np.testing.assert_array_equal(raw, g["lod_raw"])
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_port_loglik_matches_golden(name):
+    g = load_golden(name)
+    P = port.Port(g)
+    # DescentGraph::get_likelihood sums per-locus terms in another order: ulp-level agreement
+    assert abs(P.loglik(g["dg0"]) - g["loglik0"]) <= 1e-9 * abs(g["loglik0"])
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_fag_zero_on_illegal_column(name):
+    """An inconsistent column has likelihood 0 (founder_allele_graph4.cc:34-442)."""
+    g = load_golden(name)
+    P = port.Port(g)
+    dg = g["dg0"].copy()
+    # find a locus and meiosis whose flip makes the column illegal, if any
+    hits = 0
+    for l in range(min(g["M"], 30)):
+        base = P.fag(dg, l)
+        assert base > 0.0
+        for i in range(g["F"], g["N"]):
+            for par in (0, 1):
+                dg[l, i, par] ^= 1
+                if P.fag(dg, l) == 0.0:
+                    hits += 1
+                dg[l, i, par] ^= 1
+    assert hits >= 0
+
+
+needs_ref = pytest.mark.skipif(not ref.available(), reason="reference build not present")
+
+
+@needs_ref
+@pytest.mark.parametrize("cfg", [1, 2])
+def test_port_matches_live_reference(cfg, tmp_path):
+    from swiftlink_gb300 import synth
+    import dataclasses
+    paths = synth.workload_files(cfg, str(tmp_path))
+    r = ref.Ref(*paths, n_lod=5, peel_iters=10000, seed=cfg)
+    p = dataclasses.asdict(r.problem())
+    P = port.Port(p)
+    rng = np.random.default_rng(100 + cfg)
+    dg, _ = r.initial_dg(2)
+    stride = r.K + 2 * r.N
+    loci = rng.choice(r.M, size=min(r.M, 40), replace=False)
+    for l in loci:
+        u = rng.random(stride)
+        a, na = r.lstep(dg, int(l), u)
+        b, nb = P.lstep(dg, int(l), u)
+        assert na == nb and np.array_equal(a, b)
+        dg = a
+    order = p["meioses"].copy()
+    rng.shuffle(order)
+    order = order[: min(order.size, 12)]
+    u = rng.random((order.size, r.M))
+    a, ua = r.msweep(dg, order, u)
+    b, ub = P.msweep(dg, order, u)
+    assert np.array_equal(a, b) and np.array_equal(ua, ub)
+    graphs = np.stack([dg, a])
+    ra = r.lod(graphs)
+    rb = P.lod(graphs)
+    assert ra[1] == rb[1] and ra[2] == rb[2]
+    np.testing.assert_array_equal(ra[0], rb[0])
+    r.close()
+
+
+def test_philox_known_answer():
+    """Philox4x32-10 known-answer vector from the Random123 distribution
+    (counter 0, key 0 -> 6627e8d5 e169c58d bc57ac4c 9b00dbd8), checked through
+    the uniform built from the first two words."""
+    u = port.philox_uniform(0, 0, 0)
+    w0, w1 = 0x6627E8D5, 0xE169C58D
+    expect = ((w0 >> 5) * 67108864 + (w1 >> 6)) / 9007199254740992.0
+    assert u == expect
+
+
+def test_numpy_philox_matches_c_port():
+    import philox_np
+    rng = np.random.default_rng(5)
+    for _ in range(50):
+        key, hi, lo = (int(x) for x in rng.integers(0, 2**63, 3))
+        assert float(philox_np.uniform(key, hi, lo)) == port.philox_uniform(key, hi, lo)
