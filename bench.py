@@ -1,0 +1,445 @@
+#!/usr/bin/env python
+"""Benchmark of the SwiftLink MCMC hot path on GB300.
+
+Workload: the seeded synthetic 120-member, 6-generation pedigree with 3
+consanguinity loops and 35 affected, 2,000 SNPs at 0.2 cM, recessive model,
+10 replicate chains per GPU, scoring every 100th descent graph at 5 positions
+per marker interval (9,995 LOD positions per scored graph).
+
+A step is one MCMC iteration (MarkovChain::run, markov_chain.cc:335-392) of
+every chain: an L-sweep over all 2,000 loci or an M-sweep over all 184
+non-ignorable meioses, chosen per chain with probability 0.5, plus LOD scoring
+on iterations that are multiples of 100.  `value` is descent-graph steps/s
+over all chains and GPUs (batched form: all chains in each launch, FP32
+rescaled LOD); LOD positions/s and the plain single-chain FP64 form are
+reported beside it.
+
+Arms:
+  python bench.py [--gpus N --steps K --warmup W]           this implementation
+  python bench.py --impl reference ...                        the reference's CPU
+      path on the host cores (the C restatement in oracle/, one process per
+      core, the reference's own build being unavailable on this machine)
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "descent-graph steps/s + LOD positions/s, batched vs plain GB300, |ΔLOD|≤1e-3"
+UNIT = "steps/s"
+CHAINS = 10
+PERIOD = 100
+LPROB = 0.5
+SEED = 20261205
+WORKLOAD = "cfg2"
+L2_FLUSH_BYTES = 256 << 20  # larger than the 129 MB L2
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    return ap.parse_args()
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def config(world):
+    return {"workload": "120-member 6-generation pedigree, 3 loops, 35 affected, 2000 SNPs at 0.2 cM, "
+                        "recessive (0,0,1) q=1e-4, 10 replicate chains per GPU, scoring every 100th graph, "
+                        "5 LOD positions per interval",
+            "members": 120, "markers": 2000, "chains_per_gpu": CHAINS, "scoring_period": PERIOD,
+            "lod_positions_per_graph": 9995, "lsampler_prob": LPROB,
+            "parallelism": f"replicas x{world}",
+            "l2": "flushed (256 MB write) before every timed step"}
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class Clocks:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = max(mx, float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the C restatement of the reference (oracle/)
+# ---------------------------------------------------------------------------
+def port_problem():
+    from oracle import port
+    from swiftlink_gb300.workloads import load_problem
+    d = load_problem(WORKLOAD)
+    d["trait_prior"] = port.derive_priors(d["genotypes"], d["typed"], d["minor"])
+    return d
+
+
+def port_iteration(P, d, dg, chain, it):
+    """One MarkovChain::run iteration of one chain on the CPU port with the
+    same Philox draw streams the device driver uses."""
+    from swiftlink_gb300 import philox
+    M, K, N = d["M"], d["K"], d["N"]
+    if philox.chooses_l(SEED, chain, it, LPROB):
+        u = philox.lsweep_draws(SEED, chain, it, M, K + 2 * N)
+        for l in list(range(0, M, 2)) + list(range(1, M, 2)):
+            dg, _ = P.lstep(dg, l, u[l])
+    else:
+        order = philox.shuffled(SEED, chain, it, d["meioses"])
+        u = philox.msweep_draws(SEED, chain, it, order.size, M)
+        dg, _ = P.msweep(dg, order, u)
+    return dg
+
+
+def cpu_baseline_sample():
+    """~10-30 s of single-core CPU work: one L-sweep, one M-sweep and one LOD
+    scoring of one chain, from which steps/s and positions/s follow."""
+    from oracle import port
+    port.build()
+    d = port_problem()
+    P = port.Port(d)
+    M, K, N = d["M"], d["K"], d["N"]
+    rng = np.random.default_rng(1)
+    dg = d["dg0"].copy()
+    t0 = time.perf_counter()
+    u = rng.random((M, K + 2 * N))
+    for l in list(range(0, M, 2)) + list(range(1, M, 2)):
+        dg, _ = P.lstep(dg, l, u[l])
+    tl = time.perf_counter() - t0
+    order = d["meioses"].copy()
+    rng.shuffle(order)
+    t0 = time.perf_counter()
+    dg, _ = P.msweep(dg, order, rng.random((order.size, M)))
+    tm = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    P.lod(dg[None])
+    tlod = time.perf_counter() - t0
+    steps_per_s = 2.0 / (tl + tm)
+    return {"value": steps_per_s, "unit": UNIT, "cores": 1, "kind": "port",
+            "lod_positions_per_s": (M - 1) * d["n_lod"] / tlod,
+            "sample": f"one chain: 1 L-sweep ({tl:.2f} s) + 1 M-sweep over {order.size} meioses ({tm:.2f} s) "
+                      f"+ 1 LOD scoring of 9995 positions ({tlod:.2f} s), single thread"}
+
+
+def _ref_worker(args):
+    chains, steps, warmup, budget_s = args
+    from oracle import port
+    d = port_problem()
+    P = port.Port(d)
+    dgs = {c: d["dg0"].copy() for c in chains}
+    for it in range(warmup):
+        for c in chains:
+            dgs[c] = port_iteration(P, d, dgs[c], c, it)
+    t0 = time.perf_counter()
+    done = 0
+    scored = 0
+    for it in range(warmup, warmup + steps):
+        for c in chains:
+            dgs[c] = port_iteration(P, d, dgs[c], c, it)
+        if it % PERIOD == 0:
+            P.lod(np.stack([dgs[c] for c in chains]))
+            scored += len(chains)
+        done += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    return done * len(chains), time.perf_counter() - t0, scored
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    import multiprocessing as mp
+    from oracle import port
+    port.build()
+    cores = os.cpu_count() or 1
+    workers = max(1, min(cores, CHAINS * args.gpus))
+    total_chains = CHAINS * args.gpus
+    groups = [list(range(w, total_chains, workers)) for w in range(workers)]
+    budget = 60.0
+    ctx = mp.get_context("spawn")
+    t0 = time.perf_counter()
+    with ctx.Pool(workers) as pool:
+        res = pool.map(_ref_worker, [(g, args.steps, args.warmup, budget) for g in groups])
+    wall = time.perf_counter() - t0
+    chain_steps = sum(r[0] for r in res)
+    tmax = max(r[1] for r in res)
+    value = chain_steps / tmax
+    min_steps = min(r[0] // max(1, len(g)) for r, g in zip(res, groups))
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tmax / max(1, min_steps),
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic (seeded generator, swiftlink_gb300/synth.py)", "config": config(args.gpus),
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": workers, "kind": "port",
+                            "sample": f"C restatement of the reference, {workers} processes over "
+                                      f"{total_chains} chains, {min_steps} timed iterations per chain "
+                                      f"(capped at {budget:.0f} s), wall {wall:.1f} s"},
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+# ---------------------------------------------------------------------------
+# this implementation
+# ---------------------------------------------------------------------------
+def run_ours(args):
+    import torch
+    from swiftlink_gb300 import api, philox
+    from swiftlink_gb300.workloads import load_problem, step_bytes, position_bytes
+
+    rank, world, local = dist_env()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    def barrier():
+        if dist:
+            dist.barrier()
+
+    def allmax(x):
+        if not dist:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    d = load_problem(WORKLOAD)
+    prob = api.Problem.from_arrays(d, with_legal=False)
+    N, F, M, n = d["N"], d["F"], d["M"], d["n_lod"]
+    npos = (M - 1) * n
+    C = CHAINS
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
+    seed = SEED + 7919 * rank
+
+    # ---------------- batched form: all chains per launch, FP32-rescaled LOD
+    ctx = api.Context(prob, n_chains=C, lod_precision=api.SL_LOD_FP32_RESCALED, device=local)
+    ctx.set_graphs(np.stack([d["dg0"]] * C))
+    stream = torch.cuda.ExternalStream(ctx.stream_handle())
+    W, K = args.warmup, args.steps
+    ctx.run(iterations=W, burnin=0, period=PERIOD, lprob=LPROB, seed=seed)
+    ctx.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+    clocks = Clocks(local)
+    launches0 = ctx.launches
+    barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    ctx.profile(True)
+    for i in range(K):
+        with torch.cuda.stream(stream):
+            flush.fill_(i & 0xff)
+            ev[i][0].record(stream)
+        ctx.run(iterations=W + i + 1, burnin=0, period=PERIOD, lprob=LPROB, seed=seed, first_iteration=W + i)
+        with torch.cuda.stream(stream):
+            ev[i][1].record(stream)
+    ctx.synchronize()
+    torch.cuda.synchronize()
+    barrier()
+    clk = clocks.stop()
+    kern = {k: ctx.profile_read(k) for k in range(5)}
+    ctx.profile(False)
+    gpu_launches = ctx.launches - launches0
+    t_ms = sum(a.elapsed_time(b) for a, b in ev)
+    t_s = allmax(t_ms / 1e3)
+    value = K * C * world / t_s
+
+    # algorithmic bytes per launch of each kernel class over the timed iterations
+    n_l = [sum(philox.chooses_l(seed, c, W + i, LPROB) for c in range(C)) for i in range(K)]
+    sb = step_bytes(N, F, M)
+    scorings = sum(1 for i in range(K) if (W + i) % PERIOD == 0)
+    alg = {
+        0: sum(nl * sb / 2.0 for nl in n_l for _ in range(2)),      # two half-sweeps per iteration
+        1: sum((C - nl) * sb for nl in n_l),
+        2: scorings * C * npos * position_bytes(N, F, n),
+    }
+    names = {0: "lsampler_kernel", 1: "msampler_kernel", 2: "lod_kernel<float,true>", 3: "lod_merge_kernel",
+             4: "choose/shuffle"}
+    dom = max(kern, key=lambda k: kern[k][0])
+    dom_ms, dom_n = kern[dom]
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {"hbm_gbs": 6800.0}
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    per_launch = alg.get(dom, 0.0) / max(1, dom_n)
+    avg_s = dom_ms / 1e3 / max(1, dom_n)
+    achieved = per_launch / avg_s / 1e9 if avg_s > 0 else 0.0
+    roofline = {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": traffic_from_profiles(names[dom]),
+                "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if "when" in peaks else "fallback",
+                "algorithmic_bytes_per_launch": per_launch, "avg_launch_ms": 1e3 * avg_s,
+                "kernel_share": {names[k]: round(v[0] / max(1e-9, sum(x[0] for x in kern.values())), 4)
+                                 for k, v in kern.items()}}
+
+    # ---------------- LOD positions/s, batched (many graphs per launch, FP32) vs plain (FP64, one graph)
+    graphs = ctx.get_graphs()
+    G = 64
+    gset = np.stack([graphs[i % C] for i in range(G)])
+    lctx = api.Context(prob, n_chains=G, lod_precision=api.SL_LOD_FP32_RESCALED, device=local)
+    lctx.set_graphs(gset)
+    lstream = torch.cuda.ExternalStream(lctx.stream_handle())
+    lod_pos_s = timed_lod(lctx, lstream, flush, G, npos, reps=5)
+    pctx = api.Context(prob, n_chains=1, lod_precision=api.SL_LOD_FP64, device=local)
+    pctx.set_graphs(gset[:1])
+    pstream = torch.cuda.ExternalStream(pctx.stream_handle())
+    plain_lod_pos_s = timed_lod(pctx, pstream, flush, 1, npos, reps=3)
+
+    # ---------------- plain form: one chain, FP64 LOD
+    pctx.run(iterations=W, burnin=0, period=PERIOD, lprob=LPROB, seed=seed)
+    pctx.synchronize()
+    Kp = min(K, 40)
+    evp = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(Kp)]
+    for i in range(Kp):
+        with torch.cuda.stream(pstream):
+            flush.fill_(i & 0xff)
+            evp[i][0].record(pstream)
+        pctx.run(iterations=W + i + 1, burnin=0, period=PERIOD, lprob=LPROB, seed=seed, first_iteration=W + i)
+        with torch.cuda.stream(pstream):
+            evp[i][1].record(pstream)
+    pctx.synchronize()
+    plain_steps_s = Kp / (sum(a.elapsed_time(b) for a, b in evp) / 1e3)
+
+    # ---------------- end to end through the public API with host buffers
+    ectx = api.Context(prob, n_chains=C, lod_precision=api.SL_LOD_FP32_RESCALED, device=local)
+    host_graphs = np.ascontiguousarray(np.stack([d["dg0"]] * C))
+    ectx.set_graphs(host_graphs)
+    ectx.run(iterations=W, burnin=0, period=PERIOD, lprob=LPROB, seed=seed)
+    ectx.synchronize()
+    host_graphs = ectx.get_graphs()
+    Ke = min(K, 50)
+    barrier()
+    t0 = time.perf_counter()
+    for i in range(Ke):
+        ectx.set_graphs(host_graphs)                                   # H2D: the step's state
+        ectx.run(iterations=W + i + 1, burnin=0, period=PERIOD, lprob=LPROB, seed=seed, first_iteration=W + i)
+        host_graphs = ectx.get_graphs()                                # D2H: the step's result
+    e2e_t = allmax(time.perf_counter() - t0)
+    words = M * ((2 * (N - F) + 31) // 32)
+    e2e = {"value": Ke * C * world / e2e_t, "unit": UNIT, "h2d_bytes_per_step": 4 * words * C,
+           "d2h_bytes_per_step": 4 * words * C,
+           "path": "sl_set_descent_graphs (pinned, packed) + sl_run(1 iteration) + sl_get_descent_graphs per step"}
+
+    if rank == 0:
+        out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
+               "ms_per_step": t_s * 1e3 / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+               "dtype": "f64 samplers, f32-rescaled LOD peel with f64 accumulation",
+               "data": "synthetic (seeded generator, swiftlink_gb300/synth.py; no public dataset)",
+               "config": config(world), "impl": "ours",
+               "lod_positions_per_s": lod_pos_s * world,
+               "plain": {"steps_per_s": plain_steps_s * world, "lod_positions_per_s": plain_lod_pos_s * world,
+                         "form": "one chain per launch, FP64 LOD peel"},
+               "batched_vs_plain": {"steps": value / (plain_steps_s * world),
+                                    "lod_positions": lod_pos_s / plain_lod_pos_s},
+               "gpu_launches": int(gpu_launches), "roofline": roofline, "clocks": clk, "e2e": e2e}
+        if world == 1:
+            out["cpu_baseline"] = cpu_baseline_sample()
+        print(json.dumps(out))
+    for c in (ctx, lctx, pctx, ectx):
+        c.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+def timed_lod(ctx, stream, flush, G, npos, reps):
+    import torch
+    ctx.lod_score_chains()
+    ctx.synchronize()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+    for i in range(reps):
+        with torch.cuda.stream(stream):
+            flush.fill_(i)
+            evs[i][0].record(stream)
+        ctx.lod_score_chains()
+        with torch.cuda.stream(stream):
+            evs[i][1].record(stream)
+    ctx.synchronize()
+    t = sum(a.elapsed_time(b) for a, b in evs) / 1e3
+    return reps * G * npos / t
+
+
+def traffic_from_profiles(kernel):
+    """DRAM bytes per launch from the committed ncu summary, if one exists."""
+    path = os.path.join(ROOT, "profiles", "traffic.md")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.startswith("|") and kernel in line:
+            cells = [c.strip() for c in line.strip().strip("|").split("|")]
+            try:
+                return float(cells[-1])
+            except ValueError:
+                return None
+    return None
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -47,6 +47,10 @@ extern "C" {
 #define SL_PARTNER_PEEL 3
 #define SL_LAST_PEEL 4
 
+/* Sampler arithmetic */
+#define SL_SAMPLER_EXACT 0     /* FP64 in the reference's operation order: bit-exact draws */
+#define SL_SAMPLER_FAST 1      /* M-sampler filter in FP32 on normalised likelihood pairs */
+
 /* LOD arithmetic */
 #define SL_LOD_FP64 0          /* plain: FP64 trait peel, one warp per (graph, interval, offset) */
 #define SL_LOD_FP32_RESCALED 1 /* batched: FP32 peel with per-rfunction power-of-two rescaling */
@@ -92,7 +96,7 @@ typedef struct sl_options {
     int32_t device;             /* CUDA device ordinal */
     int32_t n_chains;           /* descent graphs held on the device (replicates x temperatures) */
     int32_t lod_precision;      /* SL_LOD_FP64 or SL_LOD_FP32_RESCALED */
-    int32_t reserved;
+    int32_t sampler_precision;  /* SL_SAMPLER_EXACT or SL_SAMPLER_FAST */
 } sl_options;
 
 /* Create a context; replaces GPULodscores::GPULodscores (gpu_lodscores.h:63-83). */
@@ -196,6 +200,21 @@ int sl_device_status(sl_ctx* ctx, int32_t* status);
 
 /* Number of kernel launches the context has issued (for measurement). */
 int64_t sl_launch_count(const sl_ctx* ctx);
+
+/* The cudaStream_t the context enqueues all its work on. */
+int sl_get_stream(sl_ctx* ctx, void** stream);
+
+/* Per-kernel timing (the reference's *_MICROBENCHMARKING cudaEvent timers,
+ * gpu_markov_chain.cc:1104-1140): while enabled, every launch is bracketed by
+ * CUDA events on the context's stream; sl_profile_read returns the summed
+ * device time and launch count of one kernel class and clears it. */
+#define SL_KERNEL_LSAMPLER 0
+#define SL_KERNEL_MSAMPLER 1
+#define SL_KERNEL_LOD 2
+#define SL_KERNEL_LOD_MERGE 3
+#define SL_KERNEL_OTHER 4
+int sl_profile(sl_ctx* ctx, int32_t enable);
+int sl_profile_read(sl_ctx* ctx, int32_t kernel, double* total_ms, int64_t* launches);
 
 /*
  * Host-side tables, no device needed (the checks a caller can run before

@@ -131,5 +131,31 @@ class Port:
         return lib().slo_loglik(ctypes.byref(self.s), _p(dg))
 
 
+def derive_priors(genotypes, typed, minor):
+    """L-sampler priors [M][N][4] restated from person.cc:224-299 (every person
+    takes the founder branch because the cache is filled while parsing,
+    pedigree_parser.cc:157) and Snp::init_probs (genetic_map.h:68-87), with
+    the reference's operand order: HW total = ((UU + AU) + UA) + AA, person
+    total in state-index order."""
+    UU, AA, AU, UA = 0, 1, 2, 3
+    minor = np.asarray(minor, np.float64)
+    ma = 1.0 - minor
+    hw = np.zeros((minor.size, 4))
+    hw[:, UU] = ma * ma
+    hw[:, AU] = minor * ma
+    hw[:, UA] = minor * ma
+    hw[:, AA] = minor * minor
+    tot = ((hw[:, UU] + hw[:, AU]) + hw[:, UA]) + hw[:, AA]
+    hw = hw / tot[:, None]
+    table = np.zeros((minor.size, 4, 4))
+    masks = {0: [1, 1, 1, 1], 1: [0, 0, 1, 1], 2: [1, 0, 0, 0], 3: [0, 1, 0, 0]}
+    for g, m in masks.items():
+        pr = hw * np.array(m, np.float64)[None, :]
+        t = ((pr[:, 0] + pr[:, 1]) + pr[:, 2]) + pr[:, 3]
+        table[:, g, :] = pr / t[:, None]
+    geno = np.where(np.asarray(typed, bool)[None, :], np.asarray(genotypes) & 3, 0)
+    return table[np.arange(minor.size)[:, None], geno, :]
+
+
 def philox_uniform(key: int, hi: int, lo: int) -> float:
     return lib().slo_philox_uniform(key, hi, lo)

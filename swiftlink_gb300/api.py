@@ -18,13 +18,15 @@ LIB_PATH = os.path.join(_HERE, "_build", "libswiftlink_gb300.so")
 
 SL_OK, SL_EINVAL, SL_ECUDA, SL_EZERO, SL_EILLEGAL, SL_ENOMEM, SL_ENODEV = 0, -1, -2, -3, -4, -5, -6
 SL_LOD_FP64, SL_LOD_FP32_RESCALED = 0, 1
+SL_SAMPLER_EXACT, SL_SAMPLER_FAST = 0, 1
 
 EXPORTED = [
     "sl_create", "sl_destroy", "sl_last_error", "sl_set_descent_graphs", "sl_get_descent_graphs",
     "sl_get_trait_priors", "sl_get_legal_masks", "sl_lsampler_loci", "sl_lsampler_sweep",
     "sl_msampler_sweep", "sl_lod_score_chains", "sl_lod_score_graphs", "sl_lod_results",
     "sl_lod_reset", "sl_run", "sl_synchronize", "sl_device_status", "sl_launch_count",
-    "sl_version",
+    "sl_version", "sl_get_stream", "sl_profile", "sl_profile_read", "sl_problem_legal_masks",
+    "sl_problem_trait_priors", "sl_problem_trait_prob",
 ]
 
 
@@ -51,7 +53,7 @@ class ProblemDesc(ctypes.Structure):
 
 class Options(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int32), ("n_chains", ctypes.c_int32),
-                ("lod_precision", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+                ("lod_precision", ctypes.c_int32), ("sampler_precision", ctypes.c_int32)]
 
 
 class RunOptions(ctypes.Structure):
@@ -166,10 +168,10 @@ class Context:
     """A device context holding one problem and n_chains descent graphs."""
 
     def __init__(self, problem: Problem, n_chains: int = 1, lod_precision: int = SL_LOD_FP64,
-                 device: int = 0):
+                 device: int = 0, sampler_precision: int = SL_SAMPLER_EXACT):
         self.problem = problem
         self._desc = problem.desc()
-        opt = Options(device, n_chains, lod_precision, 0)
+        opt = Options(device, n_chains, lod_precision, sampler_precision)
         h = _vp()
         rc = lib().sl_create(ctypes.byref(self._desc), ctypes.byref(opt), ctypes.byref(h))
         if rc != SL_OK:
@@ -269,6 +271,20 @@ class Context:
             seed: int = 1, first_iteration: int = 0):
         o = RunOptions(iterations, burnin, period, first_iteration, lprob, seed)
         self._check(lib().sl_run(self.h, ctypes.byref(o)))
+
+    def stream_handle(self) -> int:
+        h = _vp()
+        self._check(lib().sl_get_stream(self.h, ctypes.byref(h)))
+        return h.value or 0
+
+    def profile(self, enable: bool):
+        self._check(lib().sl_profile(self.h, 1 if enable else 0))
+
+    def profile_read(self, kernel: int):
+        ms = ctypes.c_double()
+        n = ctypes.c_int64()
+        self._check(lib().sl_profile_read(self.h, kernel, ctypes.byref(ms), ctypes.byref(n)))
+        return ms.value, n.value
 
     def synchronize(self):
         self._check(lib().sl_synchronize(self.h))

@@ -19,14 +19,14 @@
 namespace sl {
 // kernels (sl_kernels.cu)
 size_t lsampler_smem_per_warp(const ProblemDev& P);
-int fag_bytes(int N, int F);
 cudaError_t launch_lsampler(const ProblemDev& P, uint32_t* dg, int first, int nchain, const int32_t* loci,
                             int nloci, const double* u, int64_t ucs, int64_t uls, uint64_t seed, uint64_t iter,
                             const uint8_t* sel, int want, int* status, cudaStream_t s, int grid_cap, int wpb);
 cudaError_t launch_msampler(const ProblemDev& P, uint32_t* dg, int first, int nchain, const int32_t* meioses,
                             int64_t mstride, int nm, const double* u, int64_t ucs, uint64_t seed, uint64_t iter,
-                            const uint8_t* sel, int want, double* raw, double* fb, int* status, int threads,
-                            cudaStream_t s);
+                            const uint8_t* sel, int want, double* raw64, float* raw32, void* fb, uint8_t* badc,
+                            int* status, int fag_threads, int exact, cudaStream_t s);
+size_t fag_smem(int N, int F, int threads);
 cudaError_t launch_lod(const ProblemDev& P, int precision, const uint32_t* graphs, int64_t graph_words, int G,
                        double* vals, int* status, cudaStream_t s, int grid_cap, int wpb);
 cudaError_t launch_lod_merge(const double* vals, int G, int64_t npos, double* acc, uint8_t* init, cudaStream_t s);
@@ -48,6 +48,7 @@ struct sl_ctx {
     cudaStream_t stream = nullptr;
     int n_chains = 0;
     int lod_precision = 0;
+    int sampler_precision = 0;
     int sms = 0;
     ProblemDev P{};
     // host copies
@@ -79,11 +80,67 @@ struct sl_ctx {
     int32_t* d_mlist = nullptr;      // staging for caller meiosis lists
     size_t mlist_cap = 0;
     double* d_raw = nullptr;
+    float* d_raw32 = nullptr;
     double* d_fb = nullptr;
+    uint8_t* d_badc = nullptr;
     int* d_status = nullptr;
     uint8_t* d_sel = nullptr;
+    uint32_t* h_stage = nullptr;     // pinned staging for packed descent graphs
+    size_t h_stage_words = 0;
     std::string err;
+    // per-kernel event timing
+    bool profiling = false;
+    struct Mark { int kernel; cudaEvent_t a, b; };
+    std::vector<Mark> marks;
+    std::vector<cudaEvent_t> event_pool;
+    double prof_ms[5] = {0, 0, 0, 0, 0};
+    int64_t prof_n[5] = {0, 0, 0, 0, 0};
 };
+
+namespace {
+cudaEvent_t take_event(sl_ctx* c) {
+    if (!c->event_pool.empty()) {
+        cudaEvent_t e = c->event_pool.back();
+        c->event_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    return e;
+}
+// Bracket one launch with events when profiling is on.
+struct Prof {
+    sl_ctx* c;
+    int kernel;
+    cudaEvent_t a = nullptr;
+    Prof(sl_ctx* c_, int k) : c(c_), kernel(k) {
+        if (c->profiling) {
+            a = take_event(c);
+            cudaEventRecord(a, c->stream);
+        }
+        c->launches++;
+    }
+    ~Prof() {
+        if (a) {
+            cudaEvent_t b = take_event(c);
+            cudaEventRecord(b, c->stream);
+            c->marks.push_back({kernel, a, b});
+        }
+    }
+};
+void drain_marks(sl_ctx* c) {
+    cudaStreamSynchronize(c->stream);
+    for (auto& m : c->marks) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, m.a, m.b);
+        c->prof_ms[m.kernel] += ms;
+        c->prof_n[m.kernel] += 1;
+        c->event_pool.push_back(m.a);
+        c->event_pool.push_back(m.b);
+    }
+    c->marks.clear();
+}
+}  // namespace
 
 static int fail(sl_ctx* c, int code, const char* fmt, ...) {
     char buf[512];
@@ -431,7 +488,10 @@ void sl_destroy(sl_ctx* ctx) {
     cudaGetDevice(&cur);
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    for (auto& m : ctx->marks) { cudaEventDestroy(m.a); cudaEventDestroy(m.b); }
+    for (auto e : ctx->event_pool) cudaEventDestroy(e);
     for (void* p : ctx->owned) cudaFree(p);
+    if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     cudaSetDevice(cur);
     delete ctx;
@@ -449,6 +509,8 @@ int sl_create(const sl_problem_desc* d, const sl_options* opt, sl_ctx** out) {
     if (opt->n_chains < 1) return fail(ctx, SL_EINVAL, "n_chains must be >= 1");
     if (opt->lod_precision != SL_LOD_FP64 && opt->lod_precision != SL_LOD_FP32_RESCALED)
         return fail(ctx, SL_EINVAL, "unknown lod_precision %d", opt->lod_precision);
+    if (opt->sampler_precision != SL_SAMPLER_EXACT && opt->sampler_precision != SL_SAMPLER_FAST)
+        return fail(ctx, SL_EINVAL, "unknown sampler_precision %d", opt->sampler_precision);
     for (int i = 0; i < N; ++i) {
         const bool founder = d->mother[i] < 0;
         if (founder != (i < F)) return fail(ctx, SL_EINVAL, "persons must be ordered founders first");
@@ -467,6 +529,7 @@ int sl_create(const sl_problem_desc* d, const sl_options* opt, sl_ctx** out) {
     ctx->device = opt->device;
     ctx->n_chains = opt->n_chains;
     ctx->lod_precision = opt->lod_precision;
+    ctx->sampler_precision = opt->sampler_precision;
     int rc = SL_OK;
     auto bail = [&](int code) { sl_destroy(ctx); return code; };
     if (cudaSetDevice(ctx->device) != cudaSuccess) return bail(fail(nullptr, SL_ECUDA, "cudaSetDevice failed"));
@@ -536,7 +599,7 @@ int sl_create(const sl_problem_desc* d, const sl_options* opt, sl_ctx** out) {
     P.W = (2 * (N - F) + 31) / 32;
     P.arena = arena;
     P.max_child = max_child;
-    P.fag_bytes = fag_bytes(N, F);
+    P.fag_bytes = 0;
     P.marker_trans = std::log(0.5) * (2 * (N - F));
     if ((rc = upload(ctx, (int16_t**)&P.mother, mo.data(), N))) return bail(rc);
     if ((rc = upload(ctx, (int16_t**)&P.father, fa.data(), N))) return bail(rc);
@@ -565,9 +628,13 @@ int sl_create(const sl_problem_desc* d, const sl_options* opt, sl_ctx** out) {
     const int lod_blocks = std::max(1, (int)std::min<size_t>(16, per_sm / (ctx->lod_wpb * lodw + 1024)));
     ctx->ls_grid = ctx->sms * ls_blocks;
     ctx->lod_grid = ctx->sms * lod_blocks;
-    int ms_threads = (int)(kSmemBudget / (size_t)P.fag_bytes) / 32 * 32;
-    ctx->ms_threads = std::max(32, std::min(256, ms_threads));
-    if ((size_t)ctx->ms_threads * P.fag_bytes > kSmemBudget)
+    // founder-allele-graph block: the widest of 128/96/64/32 threads whose state
+    // fits two blocks per SM, else one
+    ctx->ms_threads = 0;
+    for (int half = 1; half >= 0 && !ctx->ms_threads; --half)
+        for (int t = 128; t >= 32; t -= 32)
+            if (fag_smem(N, F, t) <= (half ? per_sm / 2 - 2048 : kSmemBudget)) { ctx->ms_threads = t; break; }
+    if (!ctx->ms_threads)
         return bail(fail(nullptr, SL_EINVAL, "founder-allele graph state too large for shared memory"));
 
     // ---- state buffers
@@ -581,6 +648,9 @@ int sl_create(const sl_problem_desc* d, const sl_options* opt, sl_ctx** out) {
     if ((rc = dev_alloc(ctx, &ctx->d_vals, (size_t)ctx->vals_graphs * npos))) return bail(rc);
     if ((rc = dev_alloc(ctx, &ctx->d_raw, (size_t)C * 2 * M))) return bail(rc);
     if ((rc = dev_alloc(ctx, &ctx->d_fb, (size_t)C * 2 * M))) return bail(rc);
+    if ((rc = dev_alloc(ctx, &ctx->d_raw32, (size_t)C * 2 * M))) return bail(rc);
+    if ((rc = dev_alloc(ctx, &ctx->d_badc, C))) return bail(rc);
+    CK(cudaMemset(ctx->d_badc, 0, C));
     if ((rc = dev_alloc(ctx, &ctx->d_status, 1))) return bail(rc);
     if ((rc = dev_alloc(ctx, &ctx->d_sel, C))) return bail(rc);
     if ((rc = upload(ctx, &ctx->d_even, ctx->even.data(), ctx->even.size()))) return bail(rc);
@@ -636,17 +706,28 @@ int sl_device_status(sl_ctx* ctx, int32_t* status) {
     return SL_OK;
 }
 
+static int stage_host(sl_ctx* ctx, size_t words) {
+    if (words <= ctx->h_stage_words) return SL_OK;
+    if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
+    ctx->h_stage = nullptr;
+    ctx->h_stage_words = 0;
+    CK(cudaMallocHost((void**)&ctx->h_stage, sizeof(uint32_t) * words));
+    ctx->h_stage_words = words;
+    return SL_OK;
+}
+
 int sl_set_descent_graphs(sl_ctx* ctx, int32_t first, int32_t n, const int32_t* dg) {
     int rc = check_chains(ctx, first, n);
     if (rc) return rc;
     if (!dg) return fail(ctx, SL_EINVAL, "null descent graph");
     const ProblemDev& P = ctx->P;
     const size_t words = (size_t)P.M * P.W;
-    std::vector<uint32_t> buf(words * n);
-    for (int i = 0; i < n; ++i)
-        pack_graph(dg + (size_t)i * 2 * P.N * P.M, P.N, P.F, P.M, P.W, buf.data() + words * i);
     CK(cudaSetDevice(ctx->device));
-    CK(cudaMemcpyAsync(ctx->d_dg + words * first, buf.data(), sizeof(uint32_t) * words * n, cudaMemcpyHostToDevice,
+    CK(cudaStreamSynchronize(ctx->stream));
+    if ((rc = stage_host(ctx, words * n))) return rc;
+    for (int i = 0; i < n; ++i)
+        pack_graph(dg + (size_t)i * 2 * P.N * P.M, P.N, P.F, P.M, P.W, ctx->h_stage + words * i);
+    CK(cudaMemcpyAsync(ctx->d_dg + words * first, ctx->h_stage, sizeof(uint32_t) * words * n, cudaMemcpyHostToDevice,
                        ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     return SL_OK;
@@ -658,13 +739,14 @@ int sl_get_descent_graphs(sl_ctx* ctx, int32_t first, int32_t n, int32_t* dg) {
     if (!dg) return fail(ctx, SL_EINVAL, "null descent graph");
     const ProblemDev& P = ctx->P;
     const size_t words = (size_t)P.M * P.W;
-    std::vector<uint32_t> buf(words * n);
     CK(cudaSetDevice(ctx->device));
-    CK(cudaMemcpyAsync(buf.data(), ctx->d_dg + words * first, sizeof(uint32_t) * words * n, cudaMemcpyDeviceToHost,
+    CK(cudaStreamSynchronize(ctx->stream));
+    if ((rc = stage_host(ctx, words * n))) return rc;
+    CK(cudaMemcpyAsync(ctx->h_stage, ctx->d_dg + words * first, sizeof(uint32_t) * words * n, cudaMemcpyDeviceToHost,
                        ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     for (int i = 0; i < n; ++i)
-        unpack_graph(buf.data() + words * i, P.N, P.F, P.M, P.W, dg + (size_t)i * 2 * P.N * P.M);
+        unpack_graph(ctx->h_stage + words * i, P.N, P.F, P.M, P.W, dg + (size_t)i * 2 * P.N * P.M);
     return SL_OK;
 }
 
@@ -722,9 +804,10 @@ int sl_lsampler_loci(sl_ctx* ctx, int32_t first, int32_t n_chains, const int32_t
     CK(cudaSetDevice(ctx->device));
     if ((rc = stage_draws(ctx, u, (size_t)n_chains * ucs))) return rc;
     CK(cudaMemcpyAsync(ctx->d_loci, loci, sizeof(int32_t) * n_loci, cudaMemcpyHostToDevice, ctx->stream));
-    CK(launch_lsampler(P, ctx->d_dg, first, n_chains, ctx->d_loci, n_loci, ctx->d_u, ucs, uls, 0, 0, nullptr, 0,
+    { Prof pf_(ctx, SL_KERNEL_LSAMPLER);
+      CK(launch_lsampler(P, ctx->d_dg, first, n_chains, ctx->d_loci, n_loci, ctx->d_u, ucs, uls, 0, 0, nullptr, 0,
                        ctx->d_status, ctx->stream, ctx->ls_grid, ctx->ls_wpb));
-    ctx->launches++;
+    }
     return sl_synchronize(ctx);
 }
 
@@ -737,11 +820,14 @@ int sl_lsampler_sweep(sl_ctx* ctx, int32_t first, int32_t n_chains, const double
         return fail(ctx, SL_EINVAL, "draw strides too small (need locus stride >= K + 2N)");
     CK(cudaSetDevice(ctx->device));
     if ((rc = stage_draws(ctx, u, (size_t)n_chains * ucs))) return rc;
-    CK(launch_lsampler(P, ctx->d_dg, first, n_chains, ctx->d_even, (int)ctx->even.size(), ctx->d_u, ucs, uls, 0, 0,
+    { Prof pf_(ctx, SL_KERNEL_LSAMPLER);
+      CK(launch_lsampler(P, ctx->d_dg, first, n_chains, ctx->d_even, (int)ctx->even.size(), ctx->d_u, ucs, uls, 0, 0,
                        nullptr, 0, ctx->d_status, ctx->stream, ctx->ls_grid, ctx->ls_wpb));
-    CK(launch_lsampler(P, ctx->d_dg, first, n_chains, ctx->d_odd, (int)ctx->odd.size(), ctx->d_u, ucs, uls, 0, 0,
+    }
+    { Prof pf_(ctx, SL_KERNEL_LSAMPLER);
+      CK(launch_lsampler(P, ctx->d_dg, first, n_chains, ctx->d_odd, (int)ctx->odd.size(), ctx->d_u, ucs, uls, 0, 0,
                        nullptr, 0, ctx->d_status, ctx->stream, ctx->ls_grid, ctx->ls_wpb));
-    ctx->launches += 2;
+    }
     return sl_synchronize(ctx);
 }
 
@@ -766,9 +852,12 @@ int sl_msampler_sweep(sl_ctx* ctx, int32_t first, int32_t n_chains, const int32_
     }
     if ((rc = stage_draws(ctx, u, (size_t)n_chains * ucs))) return rc;
     CK(cudaMemcpyAsync(ctx->d_mlist, meioses, sizeof(int32_t) * n_meioses, cudaMemcpyHostToDevice, ctx->stream));
-    CK(launch_msampler(P, ctx->d_dg, first, n_chains, ctx->d_mlist, 0, n_meioses, ctx->d_u, ucs, 0, 0, nullptr, 0,
-                       ctx->d_raw, ctx->d_fb, ctx->d_status, ctx->ms_threads, ctx->stream));
-    ctx->launches++;
+    { Prof pf_(ctx, SL_KERNEL_MSAMPLER);
+      ctx->launches += 2 * n_meioses;
+      CK(launch_msampler(P, ctx->d_dg, first, n_chains, ctx->d_mlist, 0, n_meioses, ctx->d_u, ucs, 0, 0, nullptr, 0,
+                       ctx->d_raw, ctx->d_raw32, ctx->d_fb, ctx->d_badc, ctx->d_status, ctx->ms_threads,
+                       ctx->sampler_precision == SL_SAMPLER_EXACT, ctx->stream));
+    }
     return sl_synchronize(ctx);
 }
 
@@ -777,10 +866,12 @@ static int score_device_graphs(sl_ctx* ctx, const uint32_t* graphs, int G) {
     const int64_t npos = (int64_t)(P.M - 1) * P.n_lod;
     for (int g0 = 0; g0 < G; g0 += ctx->vals_graphs) {
         const int g = std::min(ctx->vals_graphs, G - g0);
+        { Prof pf_(ctx, SL_KERNEL_LOD);
         CK(launch_lod(P, ctx->lod_precision, graphs + (size_t)g0 * P.M * P.W, (int64_t)P.M * P.W, g, ctx->d_vals,
-                      ctx->d_status, ctx->stream, ctx->lod_grid, ctx->lod_wpb));
-        CK(launch_lod_merge(ctx->d_vals, g, npos, ctx->d_acc, ctx->d_init, ctx->stream));
-        ctx->launches += 2;
+                      ctx->d_status, ctx->stream, ctx->lod_grid, ctx->lod_wpb)); }
+        { Prof pf_(ctx, SL_KERNEL_LOD_MERGE);
+      CK(launch_lod_merge(ctx->d_vals, g, npos, ctx->d_acc, ctx->d_init, ctx->stream));
+    }
     }
     ctx->lod_count += G;
     return SL_OK;
@@ -885,6 +976,29 @@ int sl_problem_trait_prob(const sl_problem_desc* d, double* out) {
     return SL_OK;
 }
 
+int sl_get_stream(sl_ctx* ctx, void** stream) {
+    if (!ctx || !stream) return fail(ctx, SL_EINVAL, "null argument");
+    *stream = (void*)ctx->stream;
+    return SL_OK;
+}
+
+int sl_profile(sl_ctx* ctx, int32_t enable) {
+    if (!ctx) return fail(ctx, SL_EINVAL, "null context");
+    drain_marks(ctx);
+    ctx->profiling = enable != 0;
+    return SL_OK;
+}
+
+int sl_profile_read(sl_ctx* ctx, int32_t kernel, double* total_ms, int64_t* launches) {
+    if (!ctx || kernel < 0 || kernel > 4) return fail(ctx, SL_EINVAL, "bad kernel id");
+    drain_marks(ctx);
+    if (total_ms) *total_ms = ctx->prof_ms[kernel];
+    if (launches) *launches = ctx->prof_n[kernel];
+    ctx->prof_ms[kernel] = 0.0;
+    ctx->prof_n[kernel] = 0;
+    return SL_OK;
+}
+
 int sl_run(sl_ctx* ctx, const sl_run_options* o) {
     if (!ctx || !o) return fail(ctx, SL_EINVAL, "null argument");
     if (o->iterations < 0 || o->burnin < 0 || o->scoring_period < 1 || o->first_iteration < 0 ||
@@ -897,15 +1011,26 @@ int sl_run(sl_ctx* ctx, const sl_run_options* o) {
     const int total = o->burnin + o->iterations;
     for (int it = o->first_iteration; it < total; ++it) {
         const uint64_t iter = (uint64_t)it;
-        CK(launch_choose(0, C, o->seed, iter, o->lsampler_prob, ctx->d_sel, ctx->stream));
-        CK(launch_lsampler(P, ctx->d_dg, 0, C, ctx->d_even, (int)ctx->even.size(), nullptr, 0, 0, o->seed, iter,
+        { Prof pf_(ctx, SL_KERNEL_OTHER);
+      CK(launch_choose(0, C, o->seed, iter, o->lsampler_prob, ctx->d_sel, ctx->stream));
+    }
+        { Prof pf_(ctx, SL_KERNEL_LSAMPLER);
+      CK(launch_lsampler(P, ctx->d_dg, 0, C, ctx->d_even, (int)ctx->even.size(), nullptr, 0, 0, o->seed, iter,
                            ctx->d_sel, 1, ctx->d_status, ctx->stream, ctx->ls_grid, ctx->ls_wpb));
-        CK(launch_lsampler(P, ctx->d_dg, 0, C, ctx->d_odd, (int)ctx->odd.size(), nullptr, 0, 0, o->seed, iter,
+    }
+        { Prof pf_(ctx, SL_KERNEL_LSAMPLER);
+      CK(launch_lsampler(P, ctx->d_dg, 0, C, ctx->d_odd, (int)ctx->odd.size(), nullptr, 0, 0, o->seed, iter,
                            ctx->d_sel, 1, ctx->d_status, ctx->stream, ctx->ls_grid, ctx->ls_wpb));
-        CK(launch_shuffle(ctx->d_meioses, nm, ctx->d_morder, 0, C, o->seed, iter, ctx->stream));
-        CK(launch_msampler(P, ctx->d_dg, 0, C, ctx->d_morder, nm, nm, nullptr, 0, o->seed, iter, ctx->d_sel, 0,
-                           ctx->d_raw, ctx->d_fb, ctx->d_status, ctx->ms_threads, ctx->stream));
-        ctx->launches += 5;
+    }
+        { Prof pf_(ctx, SL_KERNEL_OTHER);
+      CK(launch_shuffle(ctx->d_meioses, nm, ctx->d_morder, 0, C, o->seed, iter, ctx->stream));
+    }
+        { Prof pf_(ctx, SL_KERNEL_MSAMPLER);
+      ctx->launches += 2 * nm;
+      CK(launch_msampler(P, ctx->d_dg, 0, C, ctx->d_morder, nm, nm, nullptr, 0, o->seed, iter, ctx->d_sel, 0,
+                           ctx->d_raw, ctx->d_raw32, ctx->d_fb, ctx->d_badc, ctx->d_status, ctx->ms_threads,
+                           ctx->sampler_precision == SL_SAMPLER_EXACT, ctx->stream));
+    }
         if (it >= o->burnin && it % o->scoring_period == 0) {
             int rc = score_device_graphs(ctx, ctx->d_dg, C);
             if (rc) return rc;

@@ -2,9 +2,10 @@
 //
 //  * lsampler_kernel   -- L-sampler, one warp per (chain, locus), FP64 with the
 //                         reference's operation order (bit-exact decisions).
-//  * msampler_kernel   -- M-sampler sweep, one block per chain: founder-allele
-//                         graph likelihoods in parallel over loci, then a
-//                         warp-wide serial forward-filter / backward-sample.
+//  * fag_kernel        -- M-sampler likelihoods: founder-allele graph of every
+//                         (chain, locus) column with one meiosis toggled.
+//  * ffbs_kernel<T>    -- M-sampler forward filter / backward sample, one warp
+//                         per chain (T=double exact, T=float fast).
 //  * lod_kernel<T,R>   -- trait peel at every (graph, interval, position), one
 //                         warp per task; T=double is the plain FP64 form,
 //                         T=float with R=true rescales every rfunction by a
@@ -297,34 +298,53 @@ __global__ void __launch_bounds__(128) lsampler_kernel(ProblemDev P, uint32_t* d
 
 // ---------------------------------------------------------------------------
 // Founder allele graph likelihood (FounderAlleleGraph4::likelihood,
-// founder_allele_graph4.cc:34-442), one thread, state in shared memory.
+// founder_allele_graph4.cc:34-442), one thread per (chain, locus).  The
+// per-thread state lives in shared memory as structure-of-arrays over the
+// block's threads (element i of thread t at [i * S + t]) so a warp's accesses
+// to the same field hit 32 consecutive banks.
 // ---------------------------------------------------------------------------
-struct FagState {
-    double* pr0;      // [2F] prob[0][group]
-    double* pr1;      // [2F]
-    int16_t* edge;    // [2N]
-    int16_t* member;  // [2F]
-    int8_t* fixed;    // [2F]
-    uint8_t* active;  // [2F]
-    uint8_t* a0;      // [2F] allele_assignment[0][founder allele]
-    uint8_t* a1;      // [2F]
+struct Fag {
+    double* pr0;      // [2F][S] prob[0][group]
+    double* pr1;      // [2F][S]
+    uint16_t* edge;   // [2N][S] founder allele of each person's maternal/paternal allele
+    uint16_t* member; // [2F][S] group of a founder allele, 0xffff = none
+    int8_t* fixed;    // [2F][S] -1 unfixed, 0/1 fixed assignment
+    uint8_t* active;  // [2F][S]
+    uint8_t* a0;      // [2F][S] allele_assignment[0][founder allele]
+    uint8_t* a1;      // [2F][S]
+    int S, t;
+    __device__ __forceinline__ double& p0(int g) { return pr0[g * S + t]; }
+    __device__ __forceinline__ double& p1(int g) { return pr1[g * S + t]; }
+    __device__ __forceinline__ double& pw(int w, int g) { return w == 0 ? p0(g) : p1(g); }
+    __device__ __forceinline__ uint16_t& e(int i) { return edge[i * S + t]; }
+    __device__ __forceinline__ uint16_t& mem(int i) { return member[i * S + t]; }
+    __device__ __forceinline__ int8_t& fx(int g) { return fixed[g * S + t]; }
+    __device__ __forceinline__ uint8_t& act(int g) { return active[g * S + t]; }
+    __device__ __forceinline__ uint8_t& as0(int i) { return a0[i * S + t]; }
+    __device__ __forceinline__ uint8_t& as1(int i) { return a1[i * S + t]; }
+    __device__ __forceinline__ uint8_t& asw(int w, int i) { return w == 0 ? as0(i) : as1(i); }
 };
 
-__host__ __device__ inline int fag_state_bytes(int N, int F) {
-    int b = 2 * F * 16 + 2 * N * 2 + 2 * F * 2 + 2 * F * 4;
-    return (b + 15) & ~15;
+// Shared bytes of a block of S threads: the FAG arrays plus the staged
+// person tables (order, mother, father as int16 and typed as uint8).
+__host__ __device__ inline size_t fag_block_bytes(int N, int F, int S) {
+    size_t per = (size_t)2 * F * 16 + (size_t)2 * N * 2 + (size_t)2 * F * 2 + (size_t)2 * F * 4;
+    size_t tables = ((size_t)N * 7 + 15) & ~(size_t)15;
+    return per * S + tables;
 }
 
-__device__ __forceinline__ FagState fag_bind(unsigned char* p, int N, int F) {
-    FagState s;
+__device__ __forceinline__ Fag fag_bind(unsigned char* p, int N, int F, int S, int t) {
+    Fag s;
+    s.S = S;
+    s.t = t;
     s.pr0 = (double*)p;
-    s.pr1 = s.pr0 + 2 * F;
-    s.edge = (int16_t*)(s.pr1 + 2 * F);
-    s.member = s.edge + 2 * N;
-    s.fixed = (int8_t*)(s.member + 2 * F);
-    s.active = (uint8_t*)(s.fixed + 2 * F);
-    s.a0 = s.active + 2 * F;
-    s.a1 = s.a0 + 2 * F;
+    s.pr1 = s.pr0 + (size_t)2 * F * S;
+    s.edge = (uint16_t*)(s.pr1 + (size_t)2 * F * S);
+    s.member = s.edge + (size_t)2 * N * S;
+    s.fixed = (int8_t*)(s.member + (size_t)2 * F * S);
+    s.active = (uint8_t*)(s.fixed + (size_t)2 * F * S);
+    s.a0 = s.active + (size_t)2 * F * S;
+    s.a1 = s.a0 + (size_t)2 * F * S;
     return s;
 }
 
@@ -340,115 +360,113 @@ __device__ __forceinline__ int fag_other(int obs, int x) {
     return x == G_HOMOZ_B ? G_HOMOZ_B : G_UNTYPED;
 }
 
-__device__ void fag_combine(FagState& s, int nfa, int c1, int c2, bool flip) {
+__device__ void fag_combine(Fag& s, int nfa, int c1, int c2, bool flip) {
     for (int i = 0; i < nfa; ++i) {
-        if (s.member[i] == c2) {
-            s.member[i] = (int16_t)c1;
-            if (flip) { uint8_t t = s.a0[i]; s.a0[i] = s.a1[i]; s.a1[i] = t; }
+        if (s.mem(i) == c2) {
+            s.mem(i) = (uint16_t)c1;
+            if (flip) { uint8_t t = s.as0(i); s.as0(i) = s.as1(i); s.as1(i) = t; }
         }
     }
     if (flip) {
-        s.pr0[c1] = DMUL(s.pr0[c1], s.pr1[c2]);
-        s.pr1[c1] = DMUL(s.pr1[c1], s.pr0[c2]);
+        s.p0(c1) = DMUL(s.p0(c1), s.p1(c2));
+        s.p1(c1) = DMUL(s.p1(c1), s.p0(c2));
     } else {
-        s.pr0[c1] = DMUL(s.pr0[c1], s.pr0[c2]);
-        s.pr1[c1] = DMUL(s.pr1[c1], s.pr1[c2]);
+        s.p0(c1) = DMUL(s.p0(c1), s.p0(c2));
+        s.p1(c1) = DMUL(s.p1(c1), s.p1(c2));
     }
-    s.active[c2] = 0;
+    s.act(c2) = 0;
 }
 
 // Edges of the column (FounderAlleleGraph4::reset, founder_allele_graph4.cc:
 // 543-569) with one meiosis optionally toggled, which equals flip() and its
 // propagation (founder_allele_graph4.cc:571-597).
-__device__ void fag_edges(const ProblemDev& P, const uint32_t* col, FagState& s, int flip_b) {
-    for (int n = 0; n < P.N; ++n) {
-        const int pid = P.fag_order[n];
-        if (pid < P.F) {
-            s.edge[2 * pid] = (int16_t)(2 * pid);
-            s.edge[2 * pid + 1] = (int16_t)(2 * pid + 1);
+__device__ void fag_edges(int N, int F, const int16_t* order, const int16_t* mo, const int16_t* fa,
+                          const uint32_t* col, Fag& s, int flip_b) {
+    for (int n = 0; n < N; ++n) {
+        const int pid = order[n];
+        if (pid < F) {
+            s.e(2 * pid) = (uint16_t)(2 * pid);
+            s.e(2 * pid + 1) = (uint16_t)(2 * pid + 1);
         } else {
-            const int b = 2 * (pid - P.F);
+            const int b = 2 * (pid - F);
             const int vm = dgbit(col, b) ^ (flip_b == b);
             const int vp = dgbit(col, b + 1) ^ (flip_b == b + 1);
-            s.edge[2 * pid] = s.edge[2 * P.mother[pid] + vm];
-            s.edge[2 * pid + 1] = s.edge[2 * P.father[pid] + vp];
+            s.e(2 * pid) = s.e(2 * mo[pid] + vm);
+            s.e(2 * pid + 1) = s.e(2 * fa[pid] + vp);
         }
     }
 }
 
-#define ASG(s, w, fa) ((w) == 0 ? (s).a0[fa] : (s).a1[fa])
-#define PRB(s, w, g) (*((w) == 0 ? &(s).pr0[g] : &(s).pr1[g]))
+#define NONE_GROUP 0xffff
 
-__device__ double fag_like(const ProblemDev& P, int locus, FagState& s) {
-    const int nfa = 2 * P.F;
-    const double minor = P.minor[locus];
+__device__ double fag_like(int N, int F, const uint8_t* typed, const uint8_t* gcol, double minor, Fag& s) {
+    const int nfa = 2 * F;
     const double major = DSUB(1.0, minor);
     for (int i = 0; i < nfa; ++i) {
-        s.member[i] = -1; s.fixed[i] = -1; s.active[i] = 0; s.a0[i] = 0; s.a1[i] = 0;
+        s.mem(i) = NONE_GROUP; s.fx(i) = -1; s.act(i) = 0; s.as0(i) = 0; s.as1(i) = 0;
     }
     int gi = 0;
-    const uint8_t* gcol = P.geno + (size_t)locus * P.N;
 #define FREQ(g) ((g) == G_HOMOZ_A ? major : minor)
-    for (int i = 0; i < P.N; ++i) {
-        if (!P.typed[i]) continue;
+    for (int i = 0; i < N; ++i) {
+        if (!typed[i]) continue;
         const int g = gcol[i] & 3;
         if (g == G_UNTYPED) continue;
-        const int mfa = s.edge[2 * i], pfa = s.edge[2 * i + 1];
+        const int mfa = s.e(2 * i), pfa = s.e(2 * i + 1);
         if (mfa == pfa) {
             if (g == G_HETERO) return 0.0;
-            const int g1 = s.member[mfa];
-            if (g1 != -1) {
-                const int f1 = s.fixed[g1];
+            const int g1 = s.mem(mfa);
+            if (g1 != NONE_GROUP) {
+                const int f1 = s.fx(g1);
                 if (f1 != -1) {
-                    if (g != ASG(s, f1, mfa)) return 0.0;
+                    if (g != s.asw(f1, mfa)) return 0.0;
                 } else {
-                    if (s.a0[mfa] == g) { s.fixed[g1] = 0; s.pr1[g1] = 0.0; }
-                    else if (s.a1[mfa] == g) { s.fixed[g1] = 1; s.pr0[g1] = 0.0; }
+                    if (s.as0(mfa) == g) { s.fx(g1) = 0; s.p1(g1) = 0.0; }
+                    else if (s.as1(mfa) == g) { s.fx(g1) = 1; s.p0(g1) = 0.0; }
                     else return 0.0;
                 }
             } else {
-                s.member[mfa] = (int16_t)gi; s.fixed[gi] = 0; s.active[gi] = 1;
-                s.a0[mfa] = (uint8_t)g; s.pr0[gi] = FREQ(g); s.pr1[gi] = 0.0;
+                s.mem(mfa) = (uint16_t)gi; s.fx(gi) = 0; s.act(gi) = 1;
+                s.as0(mfa) = (uint8_t)g; s.p0(gi) = FREQ(g); s.p1(gi) = 0.0;
                 ++gi;
             }
             continue;
         }
-        const int g1 = s.member[mfa], g2 = s.member[pfa];
-        if (g1 != -1) {
-            int f1 = s.fixed[g1];
-            if (g2 != -1) {
+        const int g1 = s.mem(mfa), g2 = s.mem(pfa);
+        if (g1 != NONE_GROUP) {
+            int f1 = s.fx(g1);
+            if (g2 != NONE_GROUP) {
                 if (g1 == g2) {
                     if (f1 != -1) {
-                        if (!fag_legal(g, ASG(s, f1, mfa), ASG(s, f1, pfa))) return 0.0;
+                        if (!fag_legal(g, s.asw(f1, mfa), s.asw(f1, pfa))) return 0.0;
                     } else {
-                        const int l0 = fag_legal(g, s.a0[mfa], s.a0[pfa]);
-                        const int l1 = fag_legal(g, s.a1[mfa], s.a1[pfa]);
+                        const int l0 = fag_legal(g, s.as0(mfa), s.as0(pfa));
+                        const int l1 = fag_legal(g, s.as1(mfa), s.as1(pfa));
                         if (l0) {
-                            if (!l1) { s.fixed[g1] = 0; s.pr1[g1] = 0.0; }
+                            if (!l1) { s.fx(g1) = 0; s.p1(g1) = 0.0; }
                         } else {
-                            if (l1) { s.fixed[g1] = 1; s.pr0[g1] = 0.0; }
+                            if (l1) { s.fx(g1) = 1; s.p0(g1) = 0.0; }
                             else return 0.0;
                         }
                     }
                 } else {
-                    int f2 = s.fixed[g2];
+                    int f2 = s.fx(g2);
                     if (f1 != -1) {
                         if (f2 != -1) {
-                            if (!fag_legal(g, ASG(s, f1, mfa), ASG(s, f2, pfa))) return 0.0;
+                            if (!fag_legal(g, s.asw(f1, mfa), s.asw(f2, pfa))) return 0.0;
                         } else {
-                            const int l0 = fag_legal(g, ASG(s, f1, mfa), s.a0[pfa]);
-                            const int l1 = fag_legal(g, ASG(s, f1, mfa), s.a1[pfa]);
+                            const int l0 = fag_legal(g, s.asw(f1, mfa), s.as0(pfa));
+                            const int l1 = fag_legal(g, s.asw(f1, mfa), s.as1(pfa));
                             if (l0) f2 = 0; else if (l1) f2 = 1; else return 0.0;
                         }
                     } else if (f2 != -1) {
-                        const int l0 = fag_legal(g, s.a0[mfa], ASG(s, f2, pfa));
-                        const int l1 = fag_legal(g, s.a1[mfa], ASG(s, f2, pfa));
+                        const int l0 = fag_legal(g, s.as0(mfa), s.asw(f2, pfa));
+                        const int l1 = fag_legal(g, s.as1(mfa), s.asw(f2, pfa));
                         if (l0) f1 = 0; else if (l1) f1 = 1; else return 0.0;
                     } else {
-                        const int l0 = fag_legal(g, s.a0[mfa], s.a0[pfa]);
-                        const int l1 = fag_legal(g, s.a1[mfa], s.a0[pfa]);
-                        const int l2 = fag_legal(g, s.a0[mfa], s.a1[pfa]);
-                        const int l3 = fag_legal(g, s.a1[mfa], s.a1[pfa]);
+                        const int l0 = fag_legal(g, s.as0(mfa), s.as0(pfa));
+                        const int l1 = fag_legal(g, s.as1(mfa), s.as0(pfa));
+                        const int l2 = fag_legal(g, s.as0(mfa), s.as1(pfa));
+                        const int l3 = fag_legal(g, s.as1(mfa), s.as1(pfa));
                         if (!(l0 || l1 || l2 || l3)) return 0.0;
                         if (l0 && !(l1 || l2 || l3)) { f1 = 0; f2 = 0; }
                         else if (l1 && !(l0 || l2 || l3)) { f1 = 1; f2 = 0; }
@@ -459,242 +477,300 @@ __device__ double fag_like(const ProblemDev& P, int locus, FagState& s) {
                         else { f1 = -1; f2 = -1; }
                     }
                     if (f1 != f2) {
-                        s.fixed[g1] = (int8_t)f1;
-                        PRB(s, 1 - f1, g1) = 0.0;
-                        PRB(s, 1 - f2, g2) = 0.0;
+                        s.fx(g1) = (int8_t)f1;
+                        s.pw(1 - f1, g1) = 0.0;
+                        s.pw(1 - f2, g2) = 0.0;
                         fag_combine(s, nfa, g1, g2, true);
                     } else if (f1 == -2) {
-                        s.fixed[g1] = -1;
+                        s.fx(g1) = -1;
                         fag_combine(s, nfa, g1, g2, true);
                     } else {
-                        s.fixed[g1] = (int8_t)f1;
+                        s.fx(g1) = (int8_t)f1;
                         if (f1 != -1) {
-                            PRB(s, 1 - f1, g1) = 0.0;
-                            PRB(s, 1 - f2, g2) = 0.0;
+                            s.pw(1 - f1, g1) = 0.0;
+                            s.pw(1 - f2, g2) = 0.0;
                         }
                         fag_combine(s, nfa, g1, g2, false);
                     }
                 }
             } else {
                 if (f1 != -1) {
-                    const int t0 = fag_other(g, ASG(s, f1, mfa));
+                    const int t0 = fag_other(g, s.asw(f1, mfa));
                     if (t0 == G_UNTYPED) return 0.0;
-                    if (f1 == 0) s.a0[pfa] = (uint8_t)t0; else s.a1[pfa] = (uint8_t)t0;
-                    PRB(s, f1, g1) = DMUL(PRB(s, f1, g1), FREQ(t0));
+                    s.asw(f1, pfa) = (uint8_t)t0;
+                    s.pw(f1, g1) = DMUL(s.pw(f1, g1), FREQ(t0));
                 } else {
-                    const int t0 = fag_other(g, s.a0[mfa]);
-                    const int t1 = fag_other(g, s.a1[mfa]);
+                    const int t0 = fag_other(g, s.as0(mfa));
+                    const int t1 = fag_other(g, s.as1(mfa));
                     if (t0 != G_UNTYPED) {
                         if (t1 != G_UNTYPED) {
-                            s.a0[pfa] = (uint8_t)t0; s.a1[pfa] = (uint8_t)t1;
-                            s.pr0[g1] = DMUL(s.pr0[g1], FREQ(t0));
-                            s.pr1[g1] = DMUL(s.pr1[g1], FREQ(t1));
+                            s.as0(pfa) = (uint8_t)t0; s.as1(pfa) = (uint8_t)t1;
+                            s.p0(g1) = DMUL(s.p0(g1), FREQ(t0));
+                            s.p1(g1) = DMUL(s.p1(g1), FREQ(t1));
                         } else {
-                            s.a0[pfa] = (uint8_t)t0;
-                            s.pr0[g1] = DMUL(s.pr0[g1], FREQ(t0));
-                            s.pr1[g1] = 0.0;
-                            s.fixed[g1] = 0;
+                            s.as0(pfa) = (uint8_t)t0;
+                            s.p0(g1) = DMUL(s.p0(g1), FREQ(t0));
+                            s.p1(g1) = 0.0;
+                            s.fx(g1) = 0;
                         }
                     } else {
                         if (t1 != G_UNTYPED) {
-                            s.a1[pfa] = (uint8_t)t1;
-                            s.pr1[g1] = DMUL(s.pr1[g1], FREQ(t1));
-                            s.pr0[g1] = 0.0;
-                            s.fixed[g1] = 1;
+                            s.as1(pfa) = (uint8_t)t1;
+                            s.p1(g1) = DMUL(s.p1(g1), FREQ(t1));
+                            s.p0(g1) = 0.0;
+                            s.fx(g1) = 1;
                         } else return 0.0;
                     }
                 }
-                s.member[pfa] = (int16_t)g1;
+                s.mem(pfa) = (uint16_t)g1;
             }
-        } else if (g2 != -1) {
-            const int f2 = s.fixed[g2];
+        } else if (g2 != NONE_GROUP) {
+            const int f2 = s.fx(g2);
             if (f2 != -1) {
-                const int t0 = fag_other(g, ASG(s, f2, pfa));
+                const int t0 = fag_other(g, s.asw(f2, pfa));
                 if (t0 == G_UNTYPED) return 0.0;
-                if (f2 == 0) s.a0[mfa] = (uint8_t)t0; else s.a1[mfa] = (uint8_t)t0;
-                PRB(s, f2, g2) = DMUL(PRB(s, f2, g2), FREQ(t0));
+                s.asw(f2, mfa) = (uint8_t)t0;
+                s.pw(f2, g2) = DMUL(s.pw(f2, g2), FREQ(t0));
             } else {
-                const int t0 = fag_other(g, s.a0[pfa]);
-                const int t1 = fag_other(g, s.a1[pfa]);
+                const int t0 = fag_other(g, s.as0(pfa));
+                const int t1 = fag_other(g, s.as1(pfa));
                 if (t0 != G_UNTYPED) {
                     if (t1 != G_UNTYPED) {
-                        s.a0[mfa] = (uint8_t)t0; s.a1[mfa] = (uint8_t)t1;
-                        s.pr0[g2] = DMUL(s.pr0[g2], FREQ(t0));
-                        s.pr1[g2] = DMUL(s.pr1[g2], FREQ(t1));
+                        s.as0(mfa) = (uint8_t)t0; s.as1(mfa) = (uint8_t)t1;
+                        s.p0(g2) = DMUL(s.p0(g2), FREQ(t0));
+                        s.p1(g2) = DMUL(s.p1(g2), FREQ(t1));
                     } else {
-                        s.a0[mfa] = (uint8_t)t0;
-                        s.pr0[g2] = DMUL(s.pr0[g2], FREQ(t0));
-                        s.pr1[g2] = 0.0;
-                        s.fixed[g2] = 0;
+                        s.as0(mfa) = (uint8_t)t0;
+                        s.p0(g2) = DMUL(s.p0(g2), FREQ(t0));
+                        s.p1(g2) = 0.0;
+                        s.fx(g2) = 0;
                     }
                 } else {
                     if (t1 != G_UNTYPED) {
-                        s.a1[mfa] = (uint8_t)t1;
-                        s.pr1[g2] = DMUL(s.pr1[g2], FREQ(t1));
-                        s.pr0[g2] = 0.0;
-                        s.fixed[g2] = 1;
+                        s.as1(mfa) = (uint8_t)t1;
+                        s.p1(g2) = DMUL(s.p1(g2), FREQ(t1));
+                        s.p0(g2) = 0.0;
+                        s.fx(g2) = 1;
                     } else return 0.0;
                 }
             }
-            s.member[mfa] = (int16_t)g2;
+            s.mem(mfa) = (uint16_t)g2;
         } else {
             if (g == G_HETERO) {
-                s.a0[mfa] = G_HOMOZ_A; s.a1[pfa] = G_HOMOZ_A;
-                s.a1[mfa] = G_HOMOZ_B; s.a0[pfa] = G_HOMOZ_B;
-                s.pr0[gi] = DMUL(major, minor);
-                s.pr1[gi] = DMUL(major, minor);
-                s.fixed[gi] = -1;
+                s.as0(mfa) = G_HOMOZ_A; s.as1(pfa) = G_HOMOZ_A;
+                s.as1(mfa) = G_HOMOZ_B; s.as0(pfa) = G_HOMOZ_B;
+                s.p0(gi) = DMUL(major, minor);
+                s.p1(gi) = DMUL(major, minor);
+                s.fx(gi) = -1;
             } else {
-                s.a0[mfa] = (uint8_t)g; s.a0[pfa] = (uint8_t)g;
-                s.pr0[gi] = DMUL(FREQ(g), FREQ(g));
-                s.pr1[gi] = 0.0;
-                s.fixed[gi] = 0;
+                s.as0(mfa) = (uint8_t)g; s.as0(pfa) = (uint8_t)g;
+                s.p0(gi) = DMUL(FREQ(g), FREQ(g));
+                s.p1(gi) = 0.0;
+                s.fx(gi) = 0;
             }
-            s.member[mfa] = (int16_t)gi;
-            s.member[pfa] = (int16_t)gi;
-            s.active[gi] = 1;
+            s.mem(mfa) = (uint16_t)gi;
+            s.mem(pfa) = (uint16_t)gi;
+            s.act(gi) = 1;
             ++gi;
         }
     }
 #undef FREQ
     double ret = 1.0;
     for (int i = 0; i < gi; ++i) {
-        if (!s.active[i]) continue;
-        const int fx = s.fixed[i];
-        if (fx != -1) ret = DMUL(ret, PRB(s, fx, i));
-        else ret = DMUL(ret, DADD(s.pr0[i], s.pr1[i]));
+        if (!s.act(i)) continue;
+        const int f = s.fx(i);
+        if (f != -1) ret = DMUL(ret, s.pw(f, i));
+        else ret = DMUL(ret, DADD(s.p0(i), s.p1(i)));
     }
     return ret;
 }
 
 // ---------------------------------------------------------------------------
-// M-sampler sweep: one block per chain.  Warp 0 runs the forward filter and
-// backward sampling (serial along the map) with all 32 lanes computing the
-// same recursion on values broadcast by shuffles from coalesced chunks.
+// M-sampler, split per meiosis step into a grid-wide likelihood kernel and a
+// per-chain forward-filter / backward-sample kernel (meiosis_sampler.cc:
+// 17-203).  raw64[cr][locus][2] holds the exact likelihoods; raw32 holds the
+// same pair divided by its larger member, for the FP32 filter.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) msampler_kernel(ProblemDev P, uint32_t* dg, int first, const int32_t* meioses,
-                                                       int64_t meioses_chain_stride, int nm, Draws draws,
-                                                       const uint8_t* sel, int want, double* rawbuf,
-                                                       double* fbbuf, int* status) {
+__device__ __forceinline__ void put_raw32(float* r32, int l, double v0, double v1) {
+    const double mx = v0 > v1 ? v0 : v1;
+    float a = 0.f, b = 0.f;
+    if (mx > 0.0) {
+        a = (float)(v0 / mx);
+        b = (float)(v1 / mx);
+    }
+    r32[2 * l] = a;
+    r32[2 * l + 1] = b;
+}
+
+// step < 0: reset at order[0] (raw64[l][cur] = likelihood of the column);
+// step >= 0: likelihoods of meiosis order[step] at both values.
+__global__ void __launch_bounds__(128) fag_kernel(ProblemDev P, uint32_t* dg, int first, int nchain,
+                                                  const int32_t* order, int64_t ostride, int step,
+                                                  const uint8_t* sel, int want, double* raw64, float* raw32,
+                                                  uint8_t* badc, int* status) {
     extern __shared__ __align__(16) unsigned char smem[];
-    const int cr = blockIdx.x;
+    const int S = blockDim.x;
+    const size_t per = fag_block_bytes(P.N, P.F, S) - (((size_t)P.N * 7 + 15) & ~(size_t)15);
+    int16_t* s_order = (int16_t*)(smem + per);
+    int16_t* s_mo = s_order + P.N;
+    int16_t* s_fa = s_mo + P.N;
+    uint8_t* s_typed = (uint8_t*)(s_fa + P.N);
+    for (int i = threadIdx.x; i < P.N; i += S) {
+        s_order[i] = P.fag_order[i];
+        s_mo[i] = P.mother[i];
+        s_fa[i] = P.father[i];
+        s_typed[i] = P.typed[i];
+    }
+    __syncthreads();
+    Fag fs = fag_bind(smem, P.N, P.F, S, threadIdx.x);
+    const int64_t ntask = (int64_t)nchain * P.M;
+    const int64_t t = (int64_t)blockIdx.x * S + threadIdx.x;
+    if (t >= ntask) return;
+    const int cr = (int)(t / P.M);
+    const int l = (int)(t % P.M);
     if (sel && sel[cr] != want) return;
     const int chain = first + cr;
-    const int tid = threadIdx.x, lane = tid & 31;
-    FagState fs = fag_bind(smem + (size_t)tid * P.fag_bytes, P.N, P.F);
-    uint32_t* G = dg + (size_t)chain * P.M * P.W;
-    double* raw = rawbuf + (size_t)cr * 2 * P.M;
-    double* fb = fbbuf + (size_t)cr * 2 * P.M;
-    const int32_t* order = meioses + cr * meioses_chain_stride;
-    __shared__ int bad;
-    if (tid == 0) bad = 0;
-    __syncthreads();
-    // reset (meiosis_sampler.cc:17-40)
-    const int m0 = order[0];
-    for (int l = tid; l < P.M; l += blockDim.x) {
-        const uint32_t* col = G + (size_t)l * P.W;
-        fag_edges(P, col, fs, -1);
-        const double lk = fag_like(P, l, fs);
-        raw[2 * l + dgbit(col, m0)] = lk;
-        if (lk == 0.0) bad = 1;
-    }
-    __syncthreads();
-    if (bad) {
-        if (tid == 0) set_status(status, ST_ILLEGAL_DG);
+    const uint32_t* col = dg + ((size_t)chain * P.M + l) * P.W;
+    const int32_t* ord = order + cr * ostride;
+    double* raw = raw64 + (size_t)cr * 2 * P.M;
+    const uint8_t* gcol = P.geno + (size_t)l * P.N;
+    if (step < 0) {
+        fag_edges(P.N, P.F, s_order, s_mo, s_fa, col, fs, -1);
+        const double lk = fag_like(P.N, P.F, s_typed, gcol, P.minor[l], fs);
+        raw[2 * l + dgbit(col, ord[0])] = lk;
+        if (lk == 0.0) {
+            badc[cr] = 1;
+            set_status(status, ST_ILLEGAL_DG);
+        }
         return;
     }
-    int last = m0;
-    for (int j = 0; j < nm; ++j) {
-        const int m = order[j];
-        // likelihoods with meiosis m at both values (meiosis_sampler.cc:116-133)
-        for (int l = tid; l < P.M; l += blockDim.x) {
-            const uint32_t* col = G + (size_t)l * P.W;
-            const int t = dgbit(col, m), t2 = dgbit(col, last);
-            const double keep = raw[2 * l + t2];
-            fag_edges(P, col, fs, m);
-            const double lk = fag_like(P, l, fs);
-            raw[2 * l + t] = keep;
-            raw[2 * l + 1 - t] = lk;
-            if (keep == 0.0 && lk == 0.0) bad = 1;
+    const int m = ord[step];
+    const int last = ord[step > 0 ? step - 1 : 0];
+    const int tb = dgbit(col, m), t2 = dgbit(col, last);
+    const double keep = raw[2 * l + t2];
+    fag_edges(P.N, P.F, s_order, s_mo, s_fa, col, fs, m);
+    const double lk = fag_like(P.N, P.F, s_typed, gcol, P.minor[l], fs);
+    raw[2 * l + tb] = keep;
+    raw[2 * l + 1 - tb] = lk;
+    if (raw32) {
+        float* r32 = raw32 + (size_t)cr * 2 * P.M;
+        if (tb == 0) put_raw32(r32, l, keep, lk); else put_raw32(r32, l, lk, keep);
+    }
+    if (keep == 0.0 && lk == 0.0) {
+        badc[cr] = 1;
+        set_status(status, ST_ILLEGAL_DG);
+    }
+}
+
+template <typename T>
+struct Flt;
+template <>
+struct Flt<double> {
+    static __device__ __forceinline__ double mul(double a, double b) { return DMUL(a, b); }
+    static __device__ __forceinline__ double add(double a, double b) { return DADD(a, b); }
+    static __device__ __forceinline__ double sub(double a, double b) { return DSUB(a, b); }
+    static __device__ __forceinline__ double div(double a, double b) { return DDIV(a, b); }
+};
+template <>
+struct Flt<float> {
+    static __device__ __forceinline__ float mul(float a, float b) { return a * b; }
+    static __device__ __forceinline__ float add(float a, float b) { return a + b; }
+    static __device__ __forceinline__ float sub(float a, float b) { return a - b; }
+    static __device__ __forceinline__ float div(float a, float b) { return __fdividef(a, b); }
+};
+
+// One warp per chain.  All 32 lanes run the same serial recursion on values
+// broadcast by shuffles from coalesced 32-locus chunks (the FP64 pipe costs
+// the same per warp instruction whatever the active mask).  T=double is the
+// reference's arithmetic; T=float is the fast filter on normalised pairs.
+template <typename T>
+__global__ void __launch_bounds__(32) ffbs_kernel(ProblemDev P, uint32_t* dg, int first, int nchain,
+                                                  const int32_t* order, int64_t ostride, int step, Draws draws,
+                                                  const uint8_t* sel, int want, const uint8_t* badc,
+                                                  const double* raw64, const float* raw32, T* fbbuf) {
+    using Fl = Flt<T>;
+    const int cr = blockIdx.x;
+    if (cr >= nchain) return;
+    if (sel && sel[cr] != want) return;
+    if (badc[cr]) return;
+    const int lane = threadIdx.x;
+    const int chain = first + cr;
+    const int m = order[cr * ostride + step];
+    uint32_t* G = dg + (size_t)chain * P.M * P.W;
+    T* fb = fbbuf + (size_t)cr * 2 * P.M;
+    const double* r64 = raw64 + (size_t)cr * 2 * P.M;
+    const float* r32 = raw32 ? raw32 + (size_t)cr * 2 * P.M : nullptr;
+    // forward filter (meiosis_sampler.cc:136-155)
+    T prev0 = (T)0, prev1 = (T)0;
+    for (int base = 0; base < P.M; base += 32) {
+        const int i = base + lane;
+        T q0 = (T)0, q1 = (T)0, th = (T)0;
+        if (i < P.M) {
+            if (sizeof(T) == 8) { q0 = (T)r64[2 * i]; q1 = (T)r64[2 * i + 1]; }
+            else { q0 = (T)r32[2 * i]; q1 = (T)r32[2 * i + 1]; }
+            if (i >= 1) th = (T)P.theta[i - 1];
         }
-        __syncthreads();
-        if (bad) {
-            if (tid == 0) set_status(status, ST_ILLEGAL_DG);
-            return;
-        }
-        if (tid < 32) {
-            // forward filter (meiosis_sampler.cc:136-155)
-            double prev0 = 0.0, prev1 = 0.0;
-            for (int base = 0; base < P.M; base += 32) {
-                const int i = base + lane;
-                const double r0 = i < P.M ? raw[2 * i] : 0.0;
-                const double r1 = i < P.M ? raw[2 * i + 1] : 0.0;
-                const double th = (i >= 1 && i < P.M) ? P.theta[i - 1] : 0.0;
-                const int n = min(32, P.M - base);
-                double k0 = 0.0, k1 = 0.0;
-                for (int x = 0; x < n; ++x) {
-                    const double a0 = __shfl_sync(FULLMASK, r0, x), a1 = __shfl_sync(FULLMASK, r1, x);
-                    const double tx = __shfl_sync(FULLMASK, th, x);
-                    double f0, f1;
-                    if (base + x == 0) {
-                        const double tot = DADD(a0, a1);
-                        f0 = DDIV(a0, tot);
-                        f1 = DDIV(a1, tot);
-                    } else {
-                        const double ax = DSUB(1.0, tx);
-                        f0 = DMUL(a0, DADD(DMUL(prev1, tx), DMUL(prev0, ax)));
-                        f1 = DMUL(a1, DADD(DMUL(prev0, tx), DMUL(prev1, ax)));
-                        const double tt = DADD(f0, f1);
-                        f0 = DDIV(f0, tt);
-                        f1 = DDIV(f1, tt);
-                    }
-                    prev0 = f0;
-                    prev1 = f1;
-                    if (lane == x) { k0 = f0; k1 = f1; }
-                }
-                if (i < P.M) { fb[2 * i] = k0; fb[2 * i + 1] = k1; }
+        const int n = min(32, P.M - base);
+        T k0 = (T)0, k1 = (T)0;
+        for (int x = 0; x < n; ++x) {
+            const T a0 = __shfl_sync(FULLMASK, q0, x), a1 = __shfl_sync(FULLMASK, q1, x);
+            const T tx = __shfl_sync(FULLMASK, th, x);
+            T f0, f1;
+            if (base + x == 0) {
+                const T tot = Fl::add(a0, a1);
+                f0 = Fl::div(a0, tot);
+                f1 = Fl::div(a1, tot);
+            } else {
+                const T ax = Fl::sub((T)1, tx);
+                f0 = Fl::mul(a0, Fl::add(Fl::mul(prev1, tx), Fl::mul(prev0, ax)));
+                f1 = Fl::mul(a1, Fl::add(Fl::mul(prev0, tx), Fl::mul(prev1, ax)));
+                const T tt = Fl::add(f0, f1);
+                f0 = Fl::div(f0, tt);
+                f1 = Fl::div(f1, tt);
             }
-            __syncwarp();
-            // backward sampling (meiosis_sampler.cc:157-203)
-            int64_t cursor = 0;
-            int nxt = 0;
-            for (int top = P.M - 1; top >= 0; top -= 32) {
-                const int lo = max(0, top - 31);
-                const int n = top - lo + 1;
-                const int i = top - lane;
-                const bool in = i >= lo;
-                const double f0 = in ? fb[2 * i] : 0.0, f1 = in ? fb[2 * i + 1] : 0.0;
-                const double th = (in && i < P.M - 1) ? P.theta[i] : 0.0;
-                uint32_t* wp = in ? (G + (size_t)i * P.W + (m >> 5)) : nullptr;
-                const int cur = in ? (int)((*wp >> (m & 31)) & 1u) : 0;
-                const int64_t c0 = cursor;
-                const double dr = (c0 + lane < P.M) ? draws.get(cr, chain, j, c0 + lane) : 0.0;
-                int mine = cur;
-                for (int x = 0; x < n; ++x) {
-                    const int ii = top - x;
-                    double a0 = __shfl_sync(FULLMASK, f0, x), a1 = __shfl_sync(FULLMASK, f1, x);
-                    const double tx = __shfl_sync(FULLMASK, th, x);
-                    if (ii < P.M - 1) {
-                        const double ax = DSUB(1.0, tx);
-                        a0 = DMUL(a0, nxt != 0 ? tx : ax);
-                        a1 = DMUL(a1, nxt != 1 ? tx : ax);
-                    }
-                    int samp;
-                    if (a0 == 0.0) samp = 1;
-                    else if (a1 == 0.0) samp = 0;
-                    else {
-                        const double r = __shfl_sync(FULLMASK, dr, (int)(cursor - c0));
-                        ++cursor;
-                        samp = (r < DDIV(a0, DADD(a0, a1))) ? 0 : 1;
-                    }
-                    nxt = samp;
-                    if (lane == x) mine = samp;
-                }
-                if (in && mine != cur) *wp ^= (1u << (m & 31));
-            }
+            prev0 = f0;
+            prev1 = f1;
+            if (lane == x) { k0 = f0; k1 = f1; }
         }
-        __syncthreads();
-        last = m;
+        if (i < P.M) { fb[2 * i] = k0; fb[2 * i + 1] = k1; }
+    }
+    __syncwarp();
+    // backward sampling (meiosis_sampler.cc:157-203)
+    int64_t cursor = 0;
+    int nxt = 0;
+    for (int top = P.M - 1; top >= 0; top -= 32) {
+        const int lo = max(0, top - 31);
+        const int n = top - lo + 1;
+        const int i = top - lane;
+        const bool in = i >= lo;
+        const T f0 = in ? fb[2 * i] : (T)0, f1 = in ? fb[2 * i + 1] : (T)0;
+        const T th = (in && i < P.M - 1) ? (T)P.theta[i] : (T)0;
+        uint32_t* wp = in ? (G + (size_t)i * P.W + (m >> 5)) : nullptr;
+        const int cur = in ? (int)((*wp >> (m & 31)) & 1u) : 0;
+        const int64_t c0 = cursor;
+        const double dr = (c0 + lane < P.M) ? draws.get(cr, chain, step, c0 + lane) : 0.0;
+        int mine = cur;
+        for (int x = 0; x < n; ++x) {
+            const int ii = top - x;
+            T a0 = __shfl_sync(FULLMASK, f0, x), a1 = __shfl_sync(FULLMASK, f1, x);
+            const T tx = __shfl_sync(FULLMASK, th, x);
+            if (ii < P.M - 1) {
+                const T ax = Fl::sub((T)1, tx);
+                a0 = Fl::mul(a0, nxt != 0 ? tx : ax);
+                a1 = Fl::mul(a1, nxt != 1 ? tx : ax);
+            }
+            int samp;
+            if (a0 == (T)0) samp = 1;
+            else if (a1 == (T)0) samp = 0;
+            else {
+                const double r = __shfl_sync(FULLMASK, dr, (int)(cursor - c0));
+                ++cursor;
+                samp = (r < (double)Fl::div(a0, Fl::add(a0, a1))) ? 0 : 1;
+            }
+            nxt = samp;
+            if (lane == x) mine = samp;
+        }
+        if (in && mine != cur) *wp ^= (1u << (m & 31));
     }
 }
 
@@ -936,7 +1012,6 @@ size_t lsampler_smem_per_warp(const ProblemDev& P) {
     return (size_t)P.arena * 8 + (size_t)P.max_child * 128 + (((size_t)P.N + 15) & ~(size_t)15);
 }
 
-int fag_bytes(int N, int F) { return fag_state_bytes(N, F); }
 
 cudaError_t launch_lsampler(const ProblemDev& P, uint32_t* dg, int first, int nchain, const int32_t* loci, int nloci,
                             const double* u, int64_t ucs, int64_t uls, uint64_t seed, uint64_t iter,
@@ -959,19 +1034,36 @@ cudaError_t launch_lsampler(const ProblemDev& P, uint32_t* dg, int first, int nc
 
 cudaError_t launch_msampler(const ProblemDev& P, uint32_t* dg, int first, int nchain, const int32_t* meioses,
                             int64_t mstride, int nm, const double* u, int64_t ucs, uint64_t seed, uint64_t iter,
-                            const uint8_t* sel, int want, double* raw, double* fb, int* status, int threads,
-                            cudaStream_t s) {
-    const size_t smem = (size_t)threads * P.fag_bytes;
+                            const uint8_t* sel, int want, double* raw64, float* raw32, void* fb, uint8_t* badc,
+                            int* status, int fag_threads, int exact, cudaStream_t s) {
+    const size_t smem = fag_block_bytes(P.N, P.F, fag_threads);
     static size_t configured = 0;
     if (smem > configured) {
-        cudaError_t e = cudaFuncSetAttribute(msampler_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaError_t e = cudaFuncSetAttribute(fag_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         configured = smem;
     }
     Draws d{u, ucs, P.M, seed, iter, 2};
-    msampler_kernel<<<nchain, threads, smem, s>>>(P, dg, first, meioses, mstride, nm, d, sel, want, raw, fb, status);
+    cudaError_t e0 = cudaMemsetAsync(badc, 0, (size_t)nchain, s);
+    if (e0 != cudaSuccess) return e0;
+    const int64_t ntask = (int64_t)nchain * P.M;
+    const int grid = (int)((ntask + fag_threads - 1) / fag_threads);
+    fag_kernel<<<grid, fag_threads, smem, s>>>(P, dg, first, nchain, meioses, mstride, -1, sel, want, raw64,
+                                               nullptr, badc, status);
+    for (int j = 0; j < nm; ++j) {
+        fag_kernel<<<grid, fag_threads, smem, s>>>(P, dg, first, nchain, meioses, mstride, j, sel, want, raw64,
+                                                   exact ? nullptr : raw32, badc, status);
+        if (exact)
+            ffbs_kernel<double><<<nchain, 32, 0, s>>>(P, dg, first, nchain, meioses, mstride, j, d, sel, want, badc,
+                                                      raw64, nullptr, (double*)fb);
+        else
+            ffbs_kernel<float><<<nchain, 32, 0, s>>>(P, dg, first, nchain, meioses, mstride, j, d, sel, want, badc,
+                                                     raw64, raw32, (float*)fb);
+    }
     return cudaGetLastError();
 }
+
+size_t fag_smem(int N, int F, int threads) { return fag_block_bytes(N, F, threads); }
 
 cudaError_t launch_lod(const ProblemDev& P, int precision, const uint32_t* graphs, int64_t graph_words, int G,
                        double* vals, int* status, cudaStream_t s, int grid_cap, int wpb) {

@@ -1,5 +1,5 @@
 """Vectorised numpy Philox4x32-10 (Salmon et al., SC'11) for replaying the
-device driver's draw streams on the host in tests.  Same construction as the
+device driver's draw streams on the host (replays and accounting).  Same construction as the
 device code: uniform = ((w0 >> 5) * 2^26 + (w1 >> 6)) * 2^-53."""
 import numpy as np
 

@@ -104,7 +104,7 @@ def make_problem_only(name, seed):
     r = ref.Ref(*case_paths(name), n_lod=5, peel_iters=10000, seed=seed)
     p = r.problem()
     d = dataclasses.asdict(p)
-    out = {k: v for k, v in d.items() if isinstance(v, np.ndarray) and k not in ("trait_prior", "legal")}
+    out = {k: v for k, v in d.items() if isinstance(v, np.ndarray) and k != "trait_prior"}
     for k in ("N", "F", "M", "K", "n_lod"):
         out[k] = np.int64(d[k])
     for k in ("op_cutset", "op_prev", "op_children"):

@@ -9,8 +9,8 @@ for the batched form).
 import numpy as np
 import pytest
 
-from conftest import CASES, GOLDEN, load_golden, _lists
-import philox_np
+from conftest import CASES, load_golden
+from swiftlink_gb300 import philox as philox_np
 from oracle import port
 from swiftlink_gb300 import api
 
@@ -119,16 +119,7 @@ def test_multichain_batch_matches_port():
         assert np.array_equal(out[c], dg), f"chain {c}"
 
 
-def load_problem(name):
-    z = np.load(f"{GOLDEN}/{name}_problem.npz")
-    d = {k: z[k] for k in z.files}
-    for k in ("op_cutset", "op_prev", "op_children"):
-        d[k] = _lists(d.pop(k + "_off"), d.pop(k + "_flat"))
-    for k in ("N", "F", "M", "K", "n_lod"):
-        d[k] = int(d[k])
-    n = d["M"] * d["N"] * 2
-    d["dg0"] = np.unpackbits(d.pop("dg0_bits"))[:n].reshape(d["M"], d["N"], 2).astype(np.int32)
-    return d
+from swiftlink_gb300.workloads import load_problem  # noqa: E402
 
 
 def test_cfg2_seeded_against_port():

@@ -137,8 +137,15 @@ def test_philox_known_answer():
 
 
 def test_numpy_philox_matches_c_port():
-    import philox_np
+    from swiftlink_gb300 import philox as philox_np
     rng = np.random.default_rng(5)
     for _ in range(50):
         key, hi, lo = (int(x) for x in rng.integers(0, 2**63, 3))
         assert float(philox_np.uniform(key, hi, lo)) == port.philox_uniform(key, hi, lo)
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_port_priors_match_reference_bitwise(name):
+    g = load_golden(name)
+    pri = port.derive_priors(g["genotypes"], g["typed"], g["minor"])
+    np.testing.assert_array_equal(pri, g["trait_prior"])
