@@ -240,3 +240,21 @@ def test_rejects_interfering_loci():
         with pytest.raises(api.SwiftLinkError) as e:
             ctx.lsampler_loci([0, 1], np.zeros((1, g["M"], stride_of(g))))
         assert e.value.code == api.SL_EINVAL
+
+
+def test_fast_msampler_agrees_with_exact():
+    """The FP32 filter draws the same meiosis indicators as the exact FP64
+    filter except at near-ties; over a full cfg1 sweep the graphs agree in
+    at least 99.9% of bits (usually all)."""
+    g = load_golden("cfg1")
+    order = g["msweep_order"]
+    out = {}
+    for prec in (api.SL_SAMPLER_EXACT, api.SL_SAMPLER_FAST):
+        with api.Context(api.Problem.from_arrays(g), n_chains=1, sampler_precision=prec) as ctx:
+            ctx.set_graphs(g["lsweep_after"])
+            ctx.msampler_sweep(order, g["msweep_u"][None])
+            out[prec] = ctx.get_graphs()[0]
+    assert np.array_equal(out[api.SL_SAMPLER_EXACT], g["msweep_after"])
+    agree = float((out[api.SL_SAMPLER_FAST] == out[api.SL_SAMPLER_EXACT]).mean())
+    print(f"fast/exact M-sweep bit agreement {agree:.6f}")
+    assert agree >= 0.999
