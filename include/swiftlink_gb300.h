@@ -230,6 +230,34 @@ int sl_problem_legal_masks(const sl_problem_desc* problem, uint8_t* out);
 int sl_problem_trait_priors(const sl_problem_desc* problem, double* out);
 int sl_problem_trait_prob(const sl_problem_desc* problem, double* out);
 
+/*
+ * LOD scoring that allocates nothing.  This entry point has no counterpart in
+ * the reference.  It is for callers that cannot allocate device memory at the
+ * point where they score: hosts whose own allocator reserves the device's
+ * memory up front and forbids further driver allocations, and latency-bound
+ * loops where a cudaMalloc/cudaFree, which can synchronise the whole device,
+ * would stall other streams.  It does what sl_lod_score_graphs does, but the
+ * per-graph, per-position values live in a file-scope device array of
+ * SL_NOALLOC_SCRATCH_BYTES (8 MiB) that every GPU loading the library holds
+ * until exit, and the caller passes device buffers:
+ *   d_graphs  n_graphs packed descent graphs, uint32 [n_graphs][M][W] with
+ *             W = ceil(2 (N - F) / 32) and bit b = 2 (person - F) + parent of
+ *             word b >> 5 in each locus column (padding bits zero);
+ *   d_logsum  (M-1)*n doubles of LOD log-sum accumulators, set by the caller to
+ *             -DBL_MAX before the first call (the empty LODscores state); each
+ *             call adds the graphs' log-likelihood ratios in graph order.
+ * n_graphs * (M-1) * n must not exceed SL_NOALLOC_SCRATCH_BYTES / 8; larger
+ * requests return SL_EINVAL.  The work is queued on the context's stream;
+ * sl_synchronize reports device errors.  The first call on a device looks up
+ * the array's device address (cudaGetSymbolAddress) once for that device.
+ * All calls share the one array: calls that overlap on the GPU (several
+ * contexts or streams at once) race on it.  The context's own accumulators
+ * and count are not touched.
+ */
+#define SL_NOALLOC_SCRATCH_BYTES (8u << 20)
+int sl_lod_score_device_graphs_noalloc(sl_ctx* ctx, int32_t n_graphs, const uint32_t* d_graphs,
+                                       double* d_logsum);
+
 /* Library version string. */
 const char* sl_version(void);
 

@@ -1,8 +1,9 @@
 """Build the in-tree CUDA library swiftlink_gb300/_build/libswiftlink_gb300.so.
 
-Two translation units compiled in parallel for sm_103a only, then linked with
-the static CUDA runtime:
+Three translation units compiled in parallel for sm_103a only, then linked
+with the static CUDA runtime:
   csrc/sl_kernels.cu  (nvcc, -gencode arch=compute_103a,code=sm_103a)
+  csrc/sl_noalloc.cu  (nvcc, same flags)
   csrc/sl_host.cc     (g++ against the CUDA runtime headers)
 """
 from __future__ import annotations
@@ -51,13 +52,16 @@ def build(verbose: bool = False, force: bool = False) -> str:
     hdrs = [os.path.join(CSRC, "sl_internal.h"),
             os.path.join(os.path.dirname(HERE), "include", "swiftlink_gb300.h")]
     cu = os.path.join(CSRC, "sl_kernels.cu")
+    cu2 = os.path.join(CSRC, "sl_noalloc.cu")
     cc = os.path.join(CSRC, "sl_host.cc")
     cu_o = os.path.join(OUT, "sl_kernels.o")
+    cu2_o = os.path.join(OUT, "sl_noalloc.o")
     cc_o = os.path.join(OUT, "sl_host.o")
     jobs = []
-    if force or _stale(cu_o, [cu] + hdrs):
-        jobs.append([nvcc, GENCODE, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
-                     "-Xptxas", "-v", "-c", cu, "-o", cu_o])
+    for src, obj in ((cu, cu_o), (cu2, cu2_o)):
+        if force or _stale(obj, [src] + hdrs):
+            jobs.append([nvcc, GENCODE, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+                         "-Xptxas", "-v", "-c", src, "-o", obj])
     if force or _stale(cc_o, [cc] + hdrs):
         jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-Wall", "-I" + os.path.join(cuda, "include"),
                      "-c", cc, "-o", cc_o])
@@ -65,8 +69,8 @@ def build(verbose: bool = False, force: bool = False) -> str:
     if jobs:
         with cf.ThreadPoolExecutor(len(jobs)) as ex:
             logs = list(ex.map(_run, jobs))
-    if force or jobs or _stale(LIB, [cu_o, cc_o]):
-        logs.append(_run([nvcc, GENCODE, "-shared", "-cudart", "static", "-o", LIB, cu_o, cc_o]))
+    if force or jobs or _stale(LIB, [cu_o, cu2_o, cc_o]):
+        logs.append(_run([nvcc, GENCODE, "-shared", "-cudart", "static", "-o", LIB, cu_o, cu2_o, cc_o]))
     if verbose:
         for l in logs:
             sys.stdout.write(l)

@@ -976,6 +976,25 @@ int sl_problem_trait_prob(const sl_problem_desc* d, double* out) {
     return SL_OK;
 }
 
+}  // extern "C"
+
+namespace sl {
+int ctx_view(sl_ctx* ctx, CtxView* v) {
+    if (!ctx || !v) return SL_EINVAL;
+    v->P = ctx->P;
+    v->stream = (void*)ctx->stream;
+    v->d_status = ctx->d_status;
+    v->device = ctx->device;
+    v->lod_precision = ctx->lod_precision;
+    v->lod_grid = ctx->lod_grid;
+    v->lod_wpb = ctx->lod_wpb;
+    return SL_OK;
+}
+void ctx_fail(sl_ctx* ctx, int code, const char* msg) { fail(ctx, code, "%s", msg); }
+}  // namespace sl
+
+extern "C" {
+
 int sl_get_stream(sl_ctx* ctx, void** stream) {
     if (!ctx || !stream) return fail(ctx, SL_EINVAL, "null argument");
     *stream = (void*)ctx->stream;

@@ -46,4 +46,14 @@ struct ProblemDev {
     const int16_t* fag_order;            // [N] parents before children, founders first
 };
 
+// What code outside sl_host.cc may read of a context.
+struct CtxView {
+    ProblemDev P;
+    void* stream;        // cudaStream_t
+    int* d_status;
+    int device;
+    int lod_precision;
+    int lod_grid, lod_wpb;
+};
+
 }  // namespace sl

@@ -965,14 +965,14 @@ __device__ __forceinline__ double log_sum(double a, double b) {
 __global__ void lod_merge_kernel(const double* vals, int G, int64_t npos, double* acc, uint8_t* init) {
     for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < npos; p += (int64_t)gridDim.x * blockDim.x) {
         double a = acc[p];
-        uint8_t ini = init[p];
+        uint8_t ini = init ? init[p] : 1;   // without flags, acc starts at -DBL_MAX
         for (int b = 0; b < G; ++b) {
             const double v = vals[(size_t)b * npos + p];
             a = ini ? log_sum(v, a) : v;
             ini = 1;
         }
         acc[p] = a;
-        init[p] = ini;
+        if (init) init[p] = ini;
     }
 }
 
