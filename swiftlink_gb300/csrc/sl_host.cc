@@ -25,7 +25,7 @@ cudaError_t launch_lsampler(const ProblemDev& P, uint32_t* dg, int first, int nc
 cudaError_t launch_msampler(const ProblemDev& P, uint32_t* dg, int first, int nchain, const int32_t* meioses,
                             int64_t mstride, int nm, const double* u, int64_t ucs, uint64_t seed, uint64_t iter,
                             const uint8_t* sel, int want, double* raw64, float* raw32, void* fb, uint8_t* badc,
-                            int* status, int fag_threads, int exact, cudaStream_t s);
+                            uint8_t* maps, int* status, int fag_threads, int exact, cudaStream_t s);
 size_t fag_smem(int N, int F, int threads);
 cudaError_t launch_lod(const ProblemDev& P, int precision, const uint32_t* graphs, int64_t graph_words, int G,
                        double* vals, int* status, cudaStream_t s, int grid_cap, int wpb);
@@ -46,6 +46,8 @@ const size_t kSmemBudget = 200 * 1024;  // dynamic shared memory a block may use
 struct sl_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t lstream = nullptr;   // L-sweeps of device-driven runs, concurrent with M-sweeps
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     int n_chains = 0;
     int lod_precision = 0;
     int sampler_precision = 0;
@@ -83,6 +85,7 @@ struct sl_ctx {
     float* d_raw32 = nullptr;
     double* d_fb = nullptr;
     uint8_t* d_badc = nullptr;
+    uint8_t* d_maps = nullptr;       // [C][M] backward decision maps of the fast filter
     int* d_status = nullptr;
     uint8_t* d_sel = nullptr;
     uint32_t* h_stage = nullptr;     // pinned staging for packed descent graphs
@@ -112,24 +115,26 @@ cudaEvent_t take_event(sl_ctx* c) {
 struct Prof {
     sl_ctx* c;
     int kernel;
+    cudaStream_t s;
     cudaEvent_t a = nullptr;
-    Prof(sl_ctx* c_, int k) : c(c_), kernel(k) {
+    Prof(sl_ctx* c_, int k, cudaStream_t s_ = nullptr) : c(c_), kernel(k), s(s_ ? s_ : c_->stream) {
         if (c->profiling) {
             a = take_event(c);
-            cudaEventRecord(a, c->stream);
+            cudaEventRecord(a, s);
         }
         c->launches++;
     }
     ~Prof() {
         if (a) {
             cudaEvent_t b = take_event(c);
-            cudaEventRecord(b, c->stream);
+            cudaEventRecord(b, s);
             c->marks.push_back({kernel, a, b});
         }
     }
 };
 void drain_marks(sl_ctx* c) {
     cudaStreamSynchronize(c->stream);
+    if (c->lstream) cudaStreamSynchronize(c->lstream);
     for (auto& m : c->marks) {
         float ms = 0.f;
         cudaEventElapsedTime(&ms, m.a, m.b);
@@ -488,10 +493,14 @@ void sl_destroy(sl_ctx* ctx) {
     cudaGetDevice(&cur);
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->lstream) cudaStreamSynchronize(ctx->lstream);
     for (auto& m : ctx->marks) { cudaEventDestroy(m.a); cudaEventDestroy(m.b); }
     for (auto e : ctx->event_pool) cudaEventDestroy(e);
     for (void* p : ctx->owned) cudaFree(p);
     if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
+    if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+    if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
+    if (ctx->lstream) cudaStreamDestroy(ctx->lstream);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     cudaSetDevice(cur);
     delete ctx;
@@ -536,7 +545,10 @@ int sl_create(const sl_problem_desc* d, const sl_options* opt, sl_ctx** out) {
     cudaDeviceProp prop;
     cudaGetDeviceProperties(&prop, ctx->device);
     ctx->sms = prop.multiProcessorCount;
-    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess)
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ctx->lstream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming) != cudaSuccess)
         return bail(fail(nullptr, SL_ECUDA, "stream creation failed"));
 
     std::vector<OpDev> ops;
@@ -650,6 +662,7 @@ int sl_create(const sl_problem_desc* d, const sl_options* opt, sl_ctx** out) {
     if ((rc = dev_alloc(ctx, &ctx->d_fb, (size_t)C * 2 * M))) return bail(rc);
     if ((rc = dev_alloc(ctx, &ctx->d_raw32, (size_t)C * 2 * M))) return bail(rc);
     if ((rc = dev_alloc(ctx, &ctx->d_badc, C))) return bail(rc);
+    if ((rc = dev_alloc(ctx, &ctx->d_maps, (size_t)C * M))) return bail(rc);
     CK(cudaMemset(ctx->d_badc, 0, C));
     if ((rc = dev_alloc(ctx, &ctx->d_status, 1))) return bail(rc);
     if ((rc = dev_alloc(ctx, &ctx->d_sel, C))) return bail(rc);
@@ -686,6 +699,7 @@ static int status_to_code(sl_ctx* ctx, int st) {
 int sl_synchronize(sl_ctx* ctx) {
     if (!ctx) return fail(ctx, SL_EINVAL, "null context");
     CK(cudaSetDevice(ctx->device));
+    CK(cudaStreamSynchronize(ctx->lstream));
     CK(cudaStreamSynchronize(ctx->stream));
     int st = 0;
     CK(cudaMemcpy(&st, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost));
@@ -855,7 +869,7 @@ int sl_msampler_sweep(sl_ctx* ctx, int32_t first, int32_t n_chains, const int32_
     { Prof pf_(ctx, SL_KERNEL_MSAMPLER);
       ctx->launches += 2 * n_meioses;
       CK(launch_msampler(P, ctx->d_dg, first, n_chains, ctx->d_mlist, 0, n_meioses, ctx->d_u, ucs, 0, 0, nullptr, 0,
-                       ctx->d_raw, ctx->d_raw32, ctx->d_fb, ctx->d_badc, ctx->d_status, ctx->ms_threads,
+                       ctx->d_raw, ctx->d_raw32, ctx->d_fb, ctx->d_badc, ctx->d_maps, ctx->d_status, ctx->ms_threads,
                        ctx->sampler_precision == SL_SAMPLER_EXACT, ctx->stream));
     }
     return sl_synchronize(ctx);
@@ -1031,25 +1045,26 @@ int sl_run(sl_ctx* ctx, const sl_run_options* o) {
     for (int it = o->first_iteration; it < total; ++it) {
         const uint64_t iter = (uint64_t)it;
         { Prof pf_(ctx, SL_KERNEL_OTHER);
-      CK(launch_choose(0, C, o->seed, iter, o->lsampler_prob, ctx->d_sel, ctx->stream));
-    }
-        { Prof pf_(ctx, SL_KERNEL_LSAMPLER);
-      CK(launch_lsampler(P, ctx->d_dg, 0, C, ctx->d_even, (int)ctx->even.size(), nullptr, 0, 0, o->seed, iter,
-                           ctx->d_sel, 1, ctx->d_status, ctx->stream, ctx->ls_grid, ctx->ls_wpb));
-    }
-        { Prof pf_(ctx, SL_KERNEL_LSAMPLER);
-      CK(launch_lsampler(P, ctx->d_dg, 0, C, ctx->d_odd, (int)ctx->odd.size(), nullptr, 0, 0, o->seed, iter,
-                           ctx->d_sel, 1, ctx->d_status, ctx->stream, ctx->ls_grid, ctx->ls_wpb));
-    }
+            CK(launch_choose(0, C, o->seed, iter, o->lsampler_prob, ctx->d_sel, ctx->stream)); }
         { Prof pf_(ctx, SL_KERNEL_OTHER);
-      CK(launch_shuffle(ctx->d_meioses, nm, ctx->d_morder, 0, C, o->seed, iter, ctx->stream));
-    }
+            CK(launch_shuffle(ctx->d_meioses, nm, ctx->d_morder, 0, C, o->seed, iter, ctx->stream)); }
+        // L-sweeps of the chains that chose L run on the second stream while the
+        // M-sweeps of the others run here: the two sets of chains are disjoint
+        CK(cudaEventRecord(ctx->ev_fork, ctx->stream));
+        CK(cudaStreamWaitEvent(ctx->lstream, ctx->ev_fork, 0));
+        { Prof pf_(ctx, SL_KERNEL_LSAMPLER, ctx->lstream);
+            CK(launch_lsampler(P, ctx->d_dg, 0, C, ctx->d_even, (int)ctx->even.size(), nullptr, 0, 0, o->seed, iter,
+                               ctx->d_sel, 1, ctx->d_status, ctx->lstream, ctx->ls_grid, ctx->ls_wpb)); }
+        { Prof pf_(ctx, SL_KERNEL_LSAMPLER, ctx->lstream);
+            CK(launch_lsampler(P, ctx->d_dg, 0, C, ctx->d_odd, (int)ctx->odd.size(), nullptr, 0, 0, o->seed, iter,
+                               ctx->d_sel, 1, ctx->d_status, ctx->lstream, ctx->ls_grid, ctx->ls_wpb)); }
         { Prof pf_(ctx, SL_KERNEL_MSAMPLER);
-      ctx->launches += 2 * nm;
-      CK(launch_msampler(P, ctx->d_dg, 0, C, ctx->d_morder, nm, nm, nullptr, 0, o->seed, iter, ctx->d_sel, 0,
-                           ctx->d_raw, ctx->d_raw32, ctx->d_fb, ctx->d_badc, ctx->d_status, ctx->ms_threads,
-                           ctx->sampler_precision == SL_SAMPLER_EXACT, ctx->stream));
-    }
+            ctx->launches += 2 * nm;
+            CK(launch_msampler(P, ctx->d_dg, 0, C, ctx->d_morder, nm, nm, nullptr, 0, o->seed, iter, ctx->d_sel, 0,
+                               ctx->d_raw, ctx->d_raw32, ctx->d_fb, ctx->d_badc, ctx->d_maps, ctx->d_status,
+                               ctx->ms_threads, ctx->sampler_precision == SL_SAMPLER_EXACT, ctx->stream)); }
+        CK(cudaEventRecord(ctx->ev_join, ctx->lstream));
+        CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0));
         if (it >= o->burnin && it % o->scoring_period == 0) {
             int rc = score_device_graphs(ctx, ctx->d_dg, C);
             if (rc) return rc;

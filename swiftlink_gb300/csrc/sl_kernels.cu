@@ -303,48 +303,58 @@ __global__ void __launch_bounds__(128) lsampler_kernel(ProblemDev P, uint32_t* d
 // block's threads (element i of thread t at [i * S + t]) so a warp's accesses
 // to the same field hit 32 consecutive banks.
 // ---------------------------------------------------------------------------
+// Founder-allele groups are kept in a union-find whose links carry a swap
+// parity: the reference relabels every member of the absorbed component and
+// swaps its two allele assignments when merging (combine_components,
+// founder_allele_graph4.cc:491-541); here the absorbed component's root is
+// linked under the survivor's root with parity = swap, and a member's
+// assignment in its group's frame is its stored pair read through the
+// accumulated parity.  Group ids, the fixed/active flags and every FP64
+// product follow the reference's order exactly, so the likelihood is the
+// same double.  IX is uint8_t when 2F <= 255 (founder-allele and group ids
+// fit a byte), else uint16_t.
+template <typename IX>
 struct Fag {
     double* pr0;      // [2F][S] prob[0][group]
     double* pr1;      // [2F][S]
-    uint16_t* edge;   // [2N][S] founder allele of each person's maternal/paternal allele
-    uint16_t* member; // [2F][S] group of a founder allele, 0xffff = none
-    int8_t* fixed;    // [2F][S] -1 unfixed, 0/1 fixed assignment
-    uint8_t* active;  // [2F][S]
-    uint8_t* a0;      // [2F][S] allele_assignment[0][founder allele]
-    uint8_t* a1;      // [2F][S]
+    IX* edge;         // [2N][S] founder allele of each person's maternal/paternal allele
+    IX* up;           // [2F][S] union-find parent of a founder allele
+    uint8_t* fl;      // [2F][S] bit0 parity to parent, bit1 in a group, bits 2-3 a0, bits 4-5 a1
+    int8_t* fx;       // [2F][S] group fixed: -1 unfixed, 0/1 fixed, 2 inactive
+    IX* root;         // [2F][S] root founder allele of a group id
+    IX* gid;          // [2F][S] group id of a root founder allele
     int S, t;
     __device__ __forceinline__ double& p0(int g) { return pr0[g * S + t]; }
     __device__ __forceinline__ double& p1(int g) { return pr1[g * S + t]; }
     __device__ __forceinline__ double& pw(int w, int g) { return w == 0 ? p0(g) : p1(g); }
-    __device__ __forceinline__ uint16_t& e(int i) { return edge[i * S + t]; }
-    __device__ __forceinline__ uint16_t& mem(int i) { return member[i * S + t]; }
-    __device__ __forceinline__ int8_t& fx(int g) { return fixed[g * S + t]; }
-    __device__ __forceinline__ uint8_t& act(int g) { return active[g * S + t]; }
-    __device__ __forceinline__ uint8_t& as0(int i) { return a0[i * S + t]; }
-    __device__ __forceinline__ uint8_t& as1(int i) { return a1[i * S + t]; }
-    __device__ __forceinline__ uint8_t& asw(int w, int i) { return w == 0 ? as0(i) : as1(i); }
+    __device__ __forceinline__ IX& e(int i) { return edge[i * S + t]; }
 };
+
+__host__ __device__ inline size_t fag_per_thread(int N, int F) {
+    const size_t ix = (2 * F <= 255) ? 1 : 2;
+    return (size_t)2 * F * 16 + (size_t)2 * N * ix + (size_t)2 * F * (3 * ix + 2);
+}
 
 // Shared bytes of a block of S threads: the FAG arrays plus the staged
 // person tables (order, mother, father as int16 and typed as uint8).
 __host__ __device__ inline size_t fag_block_bytes(int N, int F, int S) {
-    size_t per = (size_t)2 * F * 16 + (size_t)2 * N * 2 + (size_t)2 * F * 2 + (size_t)2 * F * 4;
     size_t tables = ((size_t)N * 7 + 15) & ~(size_t)15;
-    return per * S + tables;
+    return ((fag_per_thread(N, F) * S + 15) & ~(size_t)15) + tables;
 }
 
-__device__ __forceinline__ Fag fag_bind(unsigned char* p, int N, int F, int S, int t) {
-    Fag s;
+template <typename IX>
+__device__ __forceinline__ Fag<IX> fag_bind(unsigned char* p, int N, int F, int S, int t) {
+    Fag<IX> s;
     s.S = S;
     s.t = t;
     s.pr0 = (double*)p;
     s.pr1 = s.pr0 + (size_t)2 * F * S;
-    s.edge = (uint16_t*)(s.pr1 + (size_t)2 * F * S);
-    s.member = s.edge + (size_t)2 * N * S;
-    s.fixed = (int8_t*)(s.member + (size_t)2 * F * S);
-    s.active = (uint8_t*)(s.fixed + (size_t)2 * F * S);
-    s.a0 = s.active + (size_t)2 * F * S;
-    s.a1 = s.a0 + (size_t)2 * F * S;
+    s.edge = (IX*)(s.pr1 + (size_t)2 * F * S);
+    s.up = s.edge + (size_t)2 * N * S;
+    s.root = s.up + (size_t)2 * F * S;
+    s.gid = s.root + (size_t)2 * F * S;
+    s.fl = (uint8_t*)(s.gid + (size_t)2 * F * S);
+    s.fx = (int8_t*)(s.fl + (size_t)2 * F * S);
     return s;
 }
 
@@ -360,13 +370,81 @@ __device__ __forceinline__ int fag_other(int obs, int x) {
     return x == G_HOMOZ_B ? G_HOMOZ_B : G_UNTYPED;
 }
 
-__device__ void fag_combine(Fag& s, int nfa, int c1, int c2, bool flip) {
-    for (int i = 0; i < nfa; ++i) {
-        if (s.mem(i) == c2) {
-            s.mem(i) = (uint16_t)c1;
-            if (flip) { uint8_t t = s.as0(i); s.as0(i) = s.as1(i); s.as1(i) = t; }
-        }
+// Root of a founder allele's component and the parity from the allele to it,
+// compressing the path.
+template <typename IX>
+__device__ __forceinline__ int fag_find(Fag<IX>& s, int fa, int& parity) {
+    int r = fa, p = 0;
+    while (true) {
+        const int u = s.up[r * s.S + s.t];
+        if (u == r) break;
+        p ^= s.fl[r * s.S + s.t] & 1;
+        r = u;
     }
+    int x = fa, px = p;
+    while (x != r) {
+        const int u = s.up[x * s.S + s.t];
+        const uint8_t f = s.fl[x * s.S + s.t];
+        s.up[x * s.S + s.t] = (IX)r;
+        s.fl[x * s.S + s.t] = (uint8_t)((f & ~1) | px);
+        px ^= f & 1;
+        x = u;
+    }
+    parity = p;
+    return r;
+}
+
+// A founder allele as the reference sees it: its group id (-1 = none) and its
+// two allele assignments in its group's frame.
+struct FaView {
+    int group, a[2];
+};
+
+template <typename IX>
+__device__ __forceinline__ FaView fag_view(Fag<IX>& s, int fa) {
+    FaView v;
+    const uint8_t f = s.fl[fa * s.S + s.t];
+    if (!(f & 2)) { v.group = -1; v.a[0] = v.a[1] = 0; return v; }
+    int par;
+    const int r = fag_find(s, fa, par);
+    const uint8_t g = s.fl[fa * s.S + s.t];
+    const int s0 = (g >> 2) & 3, s1 = (g >> 4) & 3;
+    v.group = s.gid[r * s.S + s.t];
+    v.a[0] = par ? s1 : s0;
+    v.a[1] = par ? s0 : s1;
+    return v;
+}
+
+// Put founder allele fa in group g with assignment value `val` in slot w (the
+// other slot unset, as in the reference), linked straight to the group's root.
+template <typename IX>
+__device__ __forceinline__ void fag_join(Fag<IX>& s, int fa, int g, int w, int val) {
+    const int r = s.root[g * s.S + s.t];
+    s.up[fa * s.S + s.t] = (IX)r;
+    s.fl[fa * s.S + s.t] = (uint8_t)(2 | (val << (w == 0 ? 2 : 4)));
+}
+
+template <typename IX>
+__device__ __forceinline__ void fag_join2(Fag<IX>& s, int fa, int g, int v0, int v1) {
+    const int r = s.root[g * s.S + s.t];
+    s.up[fa * s.S + s.t] = (IX)r;
+    s.fl[fa * s.S + s.t] = (uint8_t)(2 | (v0 << 2) | (v1 << 4));
+}
+
+template <typename IX>
+__device__ __forceinline__ void fag_new_root(Fag<IX>& s, int fa, int g, int v0, int v1) {
+    s.up[fa * s.S + s.t] = (IX)fa;
+    s.fl[fa * s.S + s.t] = (uint8_t)(2 | (v0 << 2) | (v1 << 4));
+    s.root[g * s.S + s.t] = (IX)fa;
+    s.gid[fa * s.S + s.t] = (IX)g;
+}
+
+// combine_components(c1, c2, flip) (founder_allele_graph4.cc:491-541)
+template <typename IX>
+__device__ __forceinline__ void fag_combine(Fag<IX>& s, int c1, int c2, bool flip) {
+    const int r1 = s.root[c1 * s.S + s.t], r2 = s.root[c2 * s.S + s.t];
+    s.up[r2 * s.S + s.t] = (IX)r1;
+    s.fl[r2 * s.S + s.t] = (uint8_t)((s.fl[r2 * s.S + s.t] & ~1) | (flip ? 1 : 0));
     if (flip) {
         s.p0(c1) = DMUL(s.p0(c1), s.p1(c2));
         s.p1(c1) = DMUL(s.p1(c1), s.p0(c2));
@@ -374,19 +452,20 @@ __device__ void fag_combine(Fag& s, int nfa, int c1, int c2, bool flip) {
         s.p0(c1) = DMUL(s.p0(c1), s.p0(c2));
         s.p1(c1) = DMUL(s.p1(c1), s.p1(c2));
     }
-    s.act(c2) = 0;
+    s.fx[c2 * s.S + s.t] = 2;
 }
 
 // Edges of the column (FounderAlleleGraph4::reset, founder_allele_graph4.cc:
 // 543-569) with one meiosis optionally toggled, which equals flip() and its
 // propagation (founder_allele_graph4.cc:571-597).
+template <typename IX>
 __device__ void fag_edges(int N, int F, const int16_t* order, const int16_t* mo, const int16_t* fa,
-                          const uint32_t* col, Fag& s, int flip_b) {
+                          const uint32_t* col, Fag<IX>& s, int flip_b) {
     for (int n = 0; n < N; ++n) {
         const int pid = order[n];
         if (pid < F) {
-            s.e(2 * pid) = (uint16_t)(2 * pid);
-            s.e(2 * pid + 1) = (uint16_t)(2 * pid + 1);
+            s.e(2 * pid) = (IX)(2 * pid);
+            s.e(2 * pid + 1) = (IX)(2 * pid + 1);
         } else {
             const int b = 2 * (pid - F);
             const int vm = dgbit(col, b) ^ (flip_b == b);
@@ -397,16 +476,14 @@ __device__ void fag_edges(int N, int F, const int16_t* order, const int16_t* mo,
     }
 }
 
-#define NONE_GROUP 0xffff
-
-__device__ double fag_like(int N, int F, const uint8_t* typed, const uint8_t* gcol, double minor, Fag& s) {
+template <typename IX>
+__device__ double fag_like(int N, int F, const uint8_t* typed, const uint8_t* gcol, double minor, Fag<IX>& s) {
     const int nfa = 2 * F;
     const double major = DSUB(1.0, minor);
-    for (int i = 0; i < nfa; ++i) {
-        s.mem(i) = NONE_GROUP; s.fx(i) = -1; s.act(i) = 0; s.as0(i) = 0; s.as1(i) = 0;
-    }
+    for (int i = 0; i < nfa; ++i) s.fl[i * s.S + s.t] = 0;
     int gi = 0;
 #define FREQ(g) ((g) == G_HOMOZ_A ? major : minor)
+#define FX(g) s.fx[(g) * s.S + s.t]
     for (int i = 0; i < N; ++i) {
         if (!typed[i]) continue;
         const int g = gcol[i] & 3;
@@ -414,59 +491,64 @@ __device__ double fag_like(int N, int F, const uint8_t* typed, const uint8_t* gc
         const int mfa = s.e(2 * i), pfa = s.e(2 * i + 1);
         if (mfa == pfa) {
             if (g == G_HETERO) return 0.0;
-            const int g1 = s.mem(mfa);
-            if (g1 != NONE_GROUP) {
-                const int f1 = s.fx(g1);
+            const FaView m = fag_view(s, mfa);
+            if (m.group != -1) {
+                const int g1 = m.group;
+                const int f1 = FX(g1);
                 if (f1 != -1) {
-                    if (g != s.asw(f1, mfa)) return 0.0;
+                    if (g != m.a[f1]) return 0.0;
                 } else {
-                    if (s.as0(mfa) == g) { s.fx(g1) = 0; s.p1(g1) = 0.0; }
-                    else if (s.as1(mfa) == g) { s.fx(g1) = 1; s.p0(g1) = 0.0; }
+                    if (m.a[0] == g) { FX(g1) = 0; s.p1(g1) = 0.0; }
+                    else if (m.a[1] == g) { FX(g1) = 1; s.p0(g1) = 0.0; }
                     else return 0.0;
                 }
             } else {
-                s.mem(mfa) = (uint16_t)gi; s.fx(gi) = 0; s.act(gi) = 1;
-                s.as0(mfa) = (uint8_t)g; s.p0(gi) = FREQ(g); s.p1(gi) = 0.0;
+                fag_new_root(s, mfa, gi, g, 0);
+                FX(gi) = 0;
+                s.p0(gi) = FREQ(g);
+                s.p1(gi) = 0.0;
                 ++gi;
             }
             continue;
         }
-        const int g1 = s.mem(mfa), g2 = s.mem(pfa);
-        if (g1 != NONE_GROUP) {
-            int f1 = s.fx(g1);
-            if (g2 != NONE_GROUP) {
+        const FaView m = fag_view(s, mfa);
+        const FaView p = fag_view(s, pfa);
+        const int g1 = m.group, g2 = p.group;
+        if (g1 != -1) {
+            int f1 = FX(g1);
+            if (g2 != -1) {
                 if (g1 == g2) {
                     if (f1 != -1) {
-                        if (!fag_legal(g, s.asw(f1, mfa), s.asw(f1, pfa))) return 0.0;
+                        if (!fag_legal(g, m.a[f1], p.a[f1])) return 0.0;
                     } else {
-                        const int l0 = fag_legal(g, s.as0(mfa), s.as0(pfa));
-                        const int l1 = fag_legal(g, s.as1(mfa), s.as1(pfa));
+                        const int l0 = fag_legal(g, m.a[0], p.a[0]);
+                        const int l1 = fag_legal(g, m.a[1], p.a[1]);
                         if (l0) {
-                            if (!l1) { s.fx(g1) = 0; s.p1(g1) = 0.0; }
+                            if (!l1) { FX(g1) = 0; s.p1(g1) = 0.0; }
                         } else {
-                            if (l1) { s.fx(g1) = 1; s.p0(g1) = 0.0; }
+                            if (l1) { FX(g1) = 1; s.p0(g1) = 0.0; }
                             else return 0.0;
                         }
                     }
                 } else {
-                    int f2 = s.fx(g2);
+                    int f2 = FX(g2);
                     if (f1 != -1) {
                         if (f2 != -1) {
-                            if (!fag_legal(g, s.asw(f1, mfa), s.asw(f2, pfa))) return 0.0;
+                            if (!fag_legal(g, m.a[f1], p.a[f2])) return 0.0;
                         } else {
-                            const int l0 = fag_legal(g, s.asw(f1, mfa), s.as0(pfa));
-                            const int l1 = fag_legal(g, s.asw(f1, mfa), s.as1(pfa));
+                            const int l0 = fag_legal(g, m.a[f1], p.a[0]);
+                            const int l1 = fag_legal(g, m.a[f1], p.a[1]);
                             if (l0) f2 = 0; else if (l1) f2 = 1; else return 0.0;
                         }
                     } else if (f2 != -1) {
-                        const int l0 = fag_legal(g, s.as0(mfa), s.asw(f2, pfa));
-                        const int l1 = fag_legal(g, s.as1(mfa), s.asw(f2, pfa));
+                        const int l0 = fag_legal(g, m.a[0], p.a[f2]);
+                        const int l1 = fag_legal(g, m.a[1], p.a[f2]);
                         if (l0) f1 = 0; else if (l1) f1 = 1; else return 0.0;
                     } else {
-                        const int l0 = fag_legal(g, s.as0(mfa), s.as0(pfa));
-                        const int l1 = fag_legal(g, s.as1(mfa), s.as0(pfa));
-                        const int l2 = fag_legal(g, s.as0(mfa), s.as1(pfa));
-                        const int l3 = fag_legal(g, s.as1(mfa), s.as1(pfa));
+                        const int l0 = fag_legal(g, m.a[0], p.a[0]);
+                        const int l1 = fag_legal(g, m.a[1], p.a[0]);
+                        const int l2 = fag_legal(g, m.a[0], p.a[1]);
+                        const int l3 = fag_legal(g, m.a[1], p.a[1]);
                         if (!(l0 || l1 || l2 || l3)) return 0.0;
                         if (l0 && !(l1 || l2 || l3)) { f1 = 0; f2 = 0; }
                         else if (l1 && !(l0 || l2 || l3)) { f1 = 1; f2 = 0; }
@@ -477,111 +559,108 @@ __device__ double fag_like(int N, int F, const uint8_t* typed, const uint8_t* gc
                         else { f1 = -1; f2 = -1; }
                     }
                     if (f1 != f2) {
-                        s.fx(g1) = (int8_t)f1;
+                        FX(g1) = (int8_t)f1;
                         s.pw(1 - f1, g1) = 0.0;
                         s.pw(1 - f2, g2) = 0.0;
-                        fag_combine(s, nfa, g1, g2, true);
+                        fag_combine(s, g1, g2, true);
                     } else if (f1 == -2) {
-                        s.fx(g1) = -1;
-                        fag_combine(s, nfa, g1, g2, true);
+                        FX(g1) = -1;
+                        fag_combine(s, g1, g2, true);
                     } else {
-                        s.fx(g1) = (int8_t)f1;
+                        FX(g1) = (int8_t)f1;
                         if (f1 != -1) {
                             s.pw(1 - f1, g1) = 0.0;
                             s.pw(1 - f2, g2) = 0.0;
                         }
-                        fag_combine(s, nfa, g1, g2, false);
+                        fag_combine(s, g1, g2, false);
                     }
                 }
             } else {
                 if (f1 != -1) {
-                    const int t0 = fag_other(g, s.asw(f1, mfa));
+                    const int t0 = fag_other(g, m.a[f1]);
                     if (t0 == G_UNTYPED) return 0.0;
-                    s.asw(f1, pfa) = (uint8_t)t0;
+                    fag_join(s, pfa, g1, f1, t0);
                     s.pw(f1, g1) = DMUL(s.pw(f1, g1), FREQ(t0));
                 } else {
-                    const int t0 = fag_other(g, s.as0(mfa));
-                    const int t1 = fag_other(g, s.as1(mfa));
+                    const int t0 = fag_other(g, m.a[0]);
+                    const int t1 = fag_other(g, m.a[1]);
                     if (t0 != G_UNTYPED) {
                         if (t1 != G_UNTYPED) {
-                            s.as0(pfa) = (uint8_t)t0; s.as1(pfa) = (uint8_t)t1;
+                            fag_join2(s, pfa, g1, t0, t1);
                             s.p0(g1) = DMUL(s.p0(g1), FREQ(t0));
                             s.p1(g1) = DMUL(s.p1(g1), FREQ(t1));
                         } else {
-                            s.as0(pfa) = (uint8_t)t0;
+                            fag_join(s, pfa, g1, 0, t0);
                             s.p0(g1) = DMUL(s.p0(g1), FREQ(t0));
                             s.p1(g1) = 0.0;
-                            s.fx(g1) = 0;
+                            FX(g1) = 0;
                         }
                     } else {
                         if (t1 != G_UNTYPED) {
-                            s.as1(pfa) = (uint8_t)t1;
+                            fag_join(s, pfa, g1, 1, t1);
                             s.p1(g1) = DMUL(s.p1(g1), FREQ(t1));
                             s.p0(g1) = 0.0;
-                            s.fx(g1) = 1;
+                            FX(g1) = 1;
                         } else return 0.0;
                     }
                 }
-                s.mem(pfa) = (uint16_t)g1;
             }
-        } else if (g2 != NONE_GROUP) {
-            const int f2 = s.fx(g2);
+        } else if (g2 != -1) {
+            const int f2 = FX(g2);
             if (f2 != -1) {
-                const int t0 = fag_other(g, s.asw(f2, pfa));
+                const int t0 = fag_other(g, p.a[f2]);
                 if (t0 == G_UNTYPED) return 0.0;
-                s.asw(f2, mfa) = (uint8_t)t0;
+                fag_join(s, mfa, g2, f2, t0);
                 s.pw(f2, g2) = DMUL(s.pw(f2, g2), FREQ(t0));
             } else {
-                const int t0 = fag_other(g, s.as0(pfa));
-                const int t1 = fag_other(g, s.as1(pfa));
+                const int t0 = fag_other(g, p.a[0]);
+                const int t1 = fag_other(g, p.a[1]);
                 if (t0 != G_UNTYPED) {
                     if (t1 != G_UNTYPED) {
-                        s.as0(mfa) = (uint8_t)t0; s.as1(mfa) = (uint8_t)t1;
+                        fag_join2(s, mfa, g2, t0, t1);
                         s.p0(g2) = DMUL(s.p0(g2), FREQ(t0));
                         s.p1(g2) = DMUL(s.p1(g2), FREQ(t1));
                     } else {
-                        s.as0(mfa) = (uint8_t)t0;
+                        fag_join(s, mfa, g2, 0, t0);
                         s.p0(g2) = DMUL(s.p0(g2), FREQ(t0));
                         s.p1(g2) = 0.0;
-                        s.fx(g2) = 0;
+                        FX(g2) = 0;
                     }
                 } else {
                     if (t1 != G_UNTYPED) {
-                        s.as1(mfa) = (uint8_t)t1;
+                        fag_join(s, mfa, g2, 1, t1);
                         s.p1(g2) = DMUL(s.p1(g2), FREQ(t1));
                         s.p0(g2) = 0.0;
-                        s.fx(g2) = 1;
+                        FX(g2) = 1;
                     } else return 0.0;
                 }
             }
-            s.mem(mfa) = (uint16_t)g2;
         } else {
             if (g == G_HETERO) {
-                s.as0(mfa) = G_HOMOZ_A; s.as1(pfa) = G_HOMOZ_A;
-                s.as1(mfa) = G_HOMOZ_B; s.as0(pfa) = G_HOMOZ_B;
+                fag_new_root(s, mfa, gi, G_HOMOZ_A, G_HOMOZ_B);
+                fag_join2(s, pfa, gi, G_HOMOZ_B, G_HOMOZ_A);
                 s.p0(gi) = DMUL(major, minor);
                 s.p1(gi) = DMUL(major, minor);
-                s.fx(gi) = -1;
+                FX(gi) = -1;
             } else {
-                s.as0(mfa) = (uint8_t)g; s.as0(pfa) = (uint8_t)g;
+                fag_new_root(s, mfa, gi, g, 0);
+                fag_join(s, pfa, gi, 0, g);
                 s.p0(gi) = DMUL(FREQ(g), FREQ(g));
                 s.p1(gi) = 0.0;
-                s.fx(gi) = 0;
+                FX(gi) = 0;
             }
-            s.mem(mfa) = (uint16_t)gi;
-            s.mem(pfa) = (uint16_t)gi;
-            s.act(gi) = 1;
             ++gi;
         }
     }
 #undef FREQ
     double ret = 1.0;
     for (int i = 0; i < gi; ++i) {
-        if (!s.act(i)) continue;
-        const int f = s.fx(i);
+        const int f = FX(i);
+        if (f == 2) continue;
         if (f != -1) ret = DMUL(ret, s.pw(f, i));
         else ret = DMUL(ret, DADD(s.p0(i), s.p1(i)));
     }
+#undef FX
     return ret;
 }
 
@@ -604,6 +683,7 @@ __device__ __forceinline__ void put_raw32(float* r32, int l, double v0, double v
 
 // step < 0: reset at order[0] (raw64[l][cur] = likelihood of the column);
 // step >= 0: likelihoods of meiosis order[step] at both values.
+template <typename IX>
 __global__ void __launch_bounds__(128) fag_kernel(ProblemDev P, uint32_t* dg, int first, int nchain,
                                                   const int32_t* order, int64_t ostride, int step,
                                                   const uint8_t* sel, int want, double* raw64, float* raw32,
@@ -622,7 +702,7 @@ __global__ void __launch_bounds__(128) fag_kernel(ProblemDev P, uint32_t* dg, in
         s_typed[i] = P.typed[i];
     }
     __syncthreads();
-    Fag fs = fag_bind(smem, P.N, P.F, S, threadIdx.x);
+    Fag<IX> fs = fag_bind<IX>(smem, P.N, P.F, S, threadIdx.x);
     const int64_t ntask = (int64_t)nchain * P.M;
     const int64_t t = (int64_t)blockIdx.x * S + threadIdx.x;
     if (t >= ntask) return;
@@ -771,6 +851,141 @@ __global__ void __launch_bounds__(32) ffbs_kernel(ProblemDev P, uint32_t* dg, in
             if (lane == x) mine = samp;
         }
         if (in && mine != cur) *wp ^= (1u << (m & 31));
+    }
+}
+
+// Fast M-sampler filter and sampling in O(M/32 + log 32) depth per chain.
+// The forward filter f_i = normalise(diag(r_i) T_i f_{i-1}) is a product of
+// 2x2 matrices: each lane multiplies its chunk's matrices, a warp scan
+// combines the chunk products, and each lane then replays its chunk from the
+// vector entering it.  Backward sampling s_i = d_i(s_{i+1}) is a composition
+// of maps {0,1} -> {0,1} (2 bits each: the decision when s_{i+1} = 0 and when
+// it is 1), scanned the same way from the top locus down.  A locus consumes a
+// draw only when neither filtered probability is zero (meiosis_sampler.cc:
+// 193-203), so draw indices come from a suffix count of such loci.
+__device__ __forceinline__ void mat_norm(float& a, float& b, float& c, float& d) {
+    const float mx = fmaxf(fmaxf(fabsf(a), fabsf(b)), fmaxf(fabsf(c), fabsf(d)));
+    if (mx > 0.f) {
+        const float inv = 1.f / mx;
+        a *= inv; b *= inv; c *= inv; d *= inv;
+    }
+}
+
+// (x o y)(v) = x(y(v)) for 2-bit maps
+__device__ __forceinline__ int map_compose(int x, int y) {
+    const int y0 = y & 1, y1 = (y >> 1) & 1;
+    return ((x >> y0) & 1) | (((x >> y1) & 1) << 1);
+}
+
+__global__ void __launch_bounds__(32) ffbs_scan_kernel(ProblemDev P, uint32_t* dg, int first, int nchain,
+                                                       const int32_t* order, int64_t ostride, int step,
+                                                       Draws draws, const uint8_t* sel, int want,
+                                                       const uint8_t* badc, const float* raw32, float* fbbuf,
+                                                       uint8_t* mapbuf) {
+    const int cr = blockIdx.x;
+    if (cr >= nchain) return;
+    if (sel && sel[cr] != want) return;
+    if (badc[cr]) return;
+    const int lane = threadIdx.x;
+    const int chain = first + cr;
+    const int m = order[cr * ostride + step];
+    const int M = P.M;
+    uint32_t* G = dg + (size_t)chain * M * P.W;
+    const float* r = raw32 + (size_t)cr * 2 * M;
+    float* fb = fbbuf + (size_t)cr * 2 * M;
+    uint8_t* maps = mapbuf + (size_t)cr * M;
+    const int L = (M + 31) / 32;
+    const int s0 = min(M, lane * L), s1 = min(M, s0 + L);
+    // chunk product P = A_{s1-1} ... A_{s0}, A_i = diag(r_i) [[1-t, t], [t, 1-t]] (A_0 = diag(r_0))
+    float p00 = 1.f, p01 = 0.f, p10 = 0.f, p11 = 1.f;
+    for (int i = s0; i < s1; ++i) {
+        const float q0 = r[2 * i], q1 = r[2 * i + 1];
+        const float t = i > 0 ? (float)P.theta[i - 1] : 0.f, a = 1.f - t;
+        const float n00 = q0 * (a * p00 + t * p10), n01 = q0 * (a * p01 + t * p11);
+        const float n10 = q1 * (t * p00 + a * p10), n11 = q1 * (t * p01 + a * p11);
+        p00 = n00; p01 = n01; p10 = n10; p11 = n11;
+        mat_norm(p00, p01, p10, p11);
+    }
+    // inclusive scan S_k = P_k ... P_0 (later chunks multiply on the left)
+    for (int d = 1; d < 32; d <<= 1) {
+        const float o00 = __shfl_up_sync(FULLMASK, p00, d), o01 = __shfl_up_sync(FULLMASK, p01, d);
+        const float o10 = __shfl_up_sync(FULLMASK, p10, d), o11 = __shfl_up_sync(FULLMASK, p11, d);
+        if (lane >= d) {
+            const float n00 = p00 * o00 + p01 * o10, n01 = p00 * o01 + p01 * o11;
+            const float n10 = p10 * o00 + p11 * o10, n11 = p10 * o01 + p11 * o11;
+            p00 = n00; p01 = n01; p10 = n10; p11 = n11;
+            mat_norm(p00, p01, p10, p11);
+        }
+    }
+    // vector entering the chunk: S_{k-1} (1, 1)
+    const float e00 = __shfl_up_sync(FULLMASK, p00, 1), e01 = __shfl_up_sync(FULLMASK, p01, 1);
+    const float e10 = __shfl_up_sync(FULLMASK, p10, 1), e11 = __shfl_up_sync(FULLMASK, p11, 1);
+    float v0 = 1.f, v1 = 1.f;
+    if (lane > 0) { v0 = e00 + e01; v1 = e10 + e11; }
+    for (int i = s0; i < s1; ++i) {
+        const float q0 = r[2 * i], q1 = r[2 * i + 1];
+        const float t = i > 0 ? (float)P.theta[i - 1] : 0.f, a = 1.f - t;
+        float f0 = q0 * (a * v0 + t * v1), f1 = q1 * (t * v0 + a * v1);
+        const float tot = f0 + f1;
+        if (tot > 0.f) { const float inv = 1.f / tot; f0 *= inv; f1 *= inv; }
+        // keep the reference's exact zeros: a zero likelihood stays zero
+        if (q0 == 0.f) f0 = 0.f;
+        if (q1 == 0.f) f1 = 0.f;
+        fb[2 * i] = f0;
+        fb[2 * i + 1] = f1;
+        v0 = f0;
+        v1 = f1;
+    }
+    // draws: loci are visited from M-1 down; a locus draws when both entries are non-zero
+    int cnt = 0;
+    for (int i = s0; i < s1; ++i) cnt += (fb[2 * i] != 0.f && fb[2 * i + 1] != 0.f);
+    int above = 0;  // draws consumed by loci in higher chunks
+    {
+        int x = cnt;
+        for (int d = 1; d < 32; d <<= 1) {
+            const int y = __shfl_down_sync(FULLMASK, x, d);
+            if (lane + d < 32) x += y;
+        }
+        above = x - cnt;
+    }
+    // per-locus decision maps and the chunk's composed map
+    int gmap = 2;  // identity: bit0 = 0, bit1 = 1
+    int idx = above;
+    for (int i = s1 - 1; i >= s0; --i) {
+        const float f0 = fb[2 * i], f1 = fb[2 * i + 1];
+        int dmap;
+        if (f0 == 0.f) dmap = 3;
+        else if (f1 == 0.f) dmap = 0;
+        else {
+            const double u = draws.get(cr, chain, step, idx++);
+            if (i == M - 1) {
+                const int v = (u < (double)(f0 / (f0 + f1))) ? 0 : 1;
+                dmap = v | (v << 1);
+            } else {
+                const float t = (float)P.theta[i], a = 1.f - t;
+                const float x0 = f0 * a, y0 = f1 * t;   // next = 0
+                const float x1 = f0 * t, y1 = f1 * a;   // next = 1
+                const int d0 = (u < (double)(x0 / (x0 + y0))) ? 0 : 1;
+                const int d1 = (u < (double)(x1 / (x1 + y1))) ? 0 : 1;
+                dmap = d0 | (d1 << 1);
+            }
+        }
+        maps[i] = (uint8_t)dmap;
+        gmap = map_compose(dmap, gmap);
+    }
+    // suffix composition over chunks: x_k = G_k o G_{k+1} o ... o G_31
+    int x = gmap;
+    for (int d = 1; d < 32; d <<= 1) {
+        const int y = __shfl_down_sync(FULLMASK, x, d);
+        if (lane + d < 32) x = map_compose(x, y);
+    }
+    const int above_map = __shfl_down_sync(FULLMASK, x, 1);
+    int sv = lane < 31 ? (above_map & 1) : 0;  // constant: the top chunk holds locus M-1
+    for (int i = s1 - 1; i >= s0; --i) {
+        sv = (maps[i] >> sv) & 1;
+        uint32_t* wp = G + (size_t)i * P.W + (m >> 5);
+        const int cur = (int)((*wp >> (m & 31)) & 1u);
+        if (sv != cur) *wp ^= (1u << (m & 31));
     }
 }
 
@@ -1032,14 +1247,16 @@ cudaError_t launch_lsampler(const ProblemDev& P, uint32_t* dg, int first, int nc
     return cudaGetLastError();
 }
 
-cudaError_t launch_msampler(const ProblemDev& P, uint32_t* dg, int first, int nchain, const int32_t* meioses,
-                            int64_t mstride, int nm, const double* u, int64_t ucs, uint64_t seed, uint64_t iter,
-                            const uint8_t* sel, int want, double* raw64, float* raw32, void* fb, uint8_t* badc,
-                            int* status, int fag_threads, int exact, cudaStream_t s) {
+template <typename IX>
+static cudaError_t launch_msampler_t(const ProblemDev& P, uint32_t* dg, int first, int nchain, const int32_t* meioses,
+                                     int64_t mstride, int nm, const double* u, int64_t ucs, uint64_t seed,
+                                     uint64_t iter, const uint8_t* sel, int want, double* raw64, float* raw32, void* fb,
+                                     uint8_t* badc, uint8_t* maps, int* status, int fag_threads, int exact,
+                                     cudaStream_t s) {
     const size_t smem = fag_block_bytes(P.N, P.F, fag_threads);
     static size_t configured = 0;
     if (smem > configured) {
-        cudaError_t e = cudaFuncSetAttribute(fag_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaError_t e = cudaFuncSetAttribute(fag_kernel<IX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         configured = smem;
     }
@@ -1048,19 +1265,30 @@ cudaError_t launch_msampler(const ProblemDev& P, uint32_t* dg, int first, int nc
     if (e0 != cudaSuccess) return e0;
     const int64_t ntask = (int64_t)nchain * P.M;
     const int grid = (int)((ntask + fag_threads - 1) / fag_threads);
-    fag_kernel<<<grid, fag_threads, smem, s>>>(P, dg, first, nchain, meioses, mstride, -1, sel, want, raw64,
-                                               nullptr, badc, status);
+    fag_kernel<IX><<<grid, fag_threads, smem, s>>>(P, dg, first, nchain, meioses, mstride, -1, sel, want, raw64,
+                                                   nullptr, badc, status);
     for (int j = 0; j < nm; ++j) {
-        fag_kernel<<<grid, fag_threads, smem, s>>>(P, dg, first, nchain, meioses, mstride, j, sel, want, raw64,
-                                                   exact ? nullptr : raw32, badc, status);
+        fag_kernel<IX><<<grid, fag_threads, smem, s>>>(P, dg, first, nchain, meioses, mstride, j, sel, want, raw64,
+                                                       exact ? nullptr : raw32, badc, status);
         if (exact)
             ffbs_kernel<double><<<nchain, 32, 0, s>>>(P, dg, first, nchain, meioses, mstride, j, d, sel, want, badc,
                                                       raw64, nullptr, (double*)fb);
         else
-            ffbs_kernel<float><<<nchain, 32, 0, s>>>(P, dg, first, nchain, meioses, mstride, j, d, sel, want, badc,
-                                                     raw64, raw32, (float*)fb);
+            ffbs_scan_kernel<<<nchain, 32, 0, s>>>(P, dg, first, nchain, meioses, mstride, j, d, sel, want, badc,
+                                                   raw32, (float*)fb, maps);
     }
     return cudaGetLastError();
+}
+
+cudaError_t launch_msampler(const ProblemDev& P, uint32_t* dg, int first, int nchain, const int32_t* meioses,
+                            int64_t mstride, int nm, const double* u, int64_t ucs, uint64_t seed, uint64_t iter,
+                            const uint8_t* sel, int want, double* raw64, float* raw32, void* fb, uint8_t* badc,
+                            uint8_t* maps, int* status, int fag_threads, int exact, cudaStream_t s) {
+    if (2 * P.F <= 255)
+        return launch_msampler_t<uint8_t>(P, dg, first, nchain, meioses, mstride, nm, u, ucs, seed, iter, sel, want,
+                                          raw64, raw32, fb, badc, maps, status, fag_threads, exact, s);
+    return launch_msampler_t<uint16_t>(P, dg, first, nchain, meioses, mstride, nm, u, ucs, seed, iter, sel, want,
+                                       raw64, raw32, fb, badc, maps, status, fag_threads, exact, s);
 }
 
 size_t fag_smem(int N, int F, int threads) { return fag_block_bytes(N, F, threads); }
