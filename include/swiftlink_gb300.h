@@ -230,6 +230,14 @@ int sl_problem_legal_masks(const sl_problem_desc* problem, uint8_t* out);
 int sl_problem_trait_priors(const sl_problem_desc* problem, double* out);
 int sl_problem_trait_prob(const sl_problem_desc* problem, double* out);
 
+/* The batched LOD form's compiled trait-peel program (its construction is host
+ * work), evaluated on the host in FP64 for one descent graph (int32 reference
+ * layout), interval and position: the log-likelihood ratio the kernels add,
+ * log r - recombination log-probability - marker transmission
+ * (peeler.cc:79-103). */
+int sl_problem_lod_program_eval(const sl_problem_desc* problem, const int32_t* dg, int32_t locus,
+                                int32_t offset, double* out);
+
 /*
  * LOD scoring that allocates nothing.  This entry point has no counterpart in
  * the reference.  It is for callers that cannot allocate device memory at the

@@ -10,6 +10,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -477,6 +478,218 @@ static int build_ops(const sl_problem_desc* d, std::vector<OpDev>& ops, std::vec
 }
 
 // ---------------------------------------------------------------------------
+// Trait-peel compiler for the batched LOD scorer
+// ---------------------------------------------------------------------------
+// The trait peel (TraitRfunction::evaluate_*_peel, trait_rfunction.cc:28-137)
+// is the same sum-product at every graph, interval and position; only the
+// recombination terms differ.  It is compiled once per problem into the
+// LI_* program (sl_internal.h): only LOD-valid cells get a slot
+// (peel_sequence_generator.cc:155-179), terms whose trait probability is zero
+// or that gather an invalid cell are dropped (they add exactly zero in the
+// reference), gathers become slot indices, and slots are reused once the op
+// that consumes a matrix has run.
+namespace {
+struct SlotAlloc {
+    std::vector<char> used;
+    int high = 0;
+    int alloc(int n) {
+        if (n <= 0) return 0;
+        int run = 0;
+        for (int i = 0; i < (int)used.size(); ++i) {
+            run = used[i] ? 0 : run + 1;
+            if (run == n) {
+                for (int j = i - n + 1; j <= i; ++j) used[j] = 1;
+                return i - n + 1;
+            }
+        }
+        const int first = (int)used.size() - run;
+        used.resize(first + n, 0);
+        for (int j = first; j < first + n; ++j) used[j] = 1;
+        high = std::max(high, (int)used.size());
+        return first;
+    }
+    void release(int first, int n) {
+        for (int j = first; j < first + n; ++j) used[j] = 0;
+    }
+};
+
+int phased_trait_host(int m, int p, int i, int j) {
+    const int ma = (m == AA) || (m == AU && i == 0) || (m == UA && i == 1);
+    const int pa = (p == AA) || (p == AU && j == 0) || (p == UA && j == 1);
+    if (ma) return pa ? (int)AA : (int)AU;
+    return pa ? (int)UA : (int)UU;
+}
+}  // namespace
+
+struct LodProgram {
+    std::vector<int32_t> words;
+    std::vector<float> consts;
+    std::vector<double> consts64;   // the same constants unrounded, for host evaluation
+    int slots = 0;
+};
+
+static void compile_lod_program(const sl_problem_desc* d, const std::vector<OpDev>& ops, const std::vector<int32_t>& od,
+                                LodProgram& out) {
+    const int K = (int)ops.size();
+    SlotAlloc sa;
+    std::vector<std::vector<int>> slot_of(K);   // cell -> slot, -1 when not LOD-valid
+    std::vector<int> first(K, 0), count(K, 0);
+    auto dig = [](int ext, int pos) { return (ext >> (2 * pos)) & 3; };
+    auto cnst = [&](double v) {
+        out.consts.push_back((float)v);
+        out.consts64.push_back(v);
+        return (int)out.consts.size() - 1;
+    };
+    auto& W = out.words;
+    for (int k = 0; k < K; ++k) {
+        const OpDev& op = ops[k];
+        const int ncell = 1 << (2 * op.c);
+        const int32_t* cut = od.data() + op.cut_at;
+        const double* trait = d->disease_prob + 4 * op.peel;
+        std::vector<int> valid;
+        for (int cell = 0; cell < ncell; ++cell) {
+            bool ok = true;
+            for (int q = 0; q < op.c; ++q)
+                if (d->disease_prob[4 * cut[q] + dig(cell, q)] == 0.0) ok = false;
+            if (ok) valid.push_back(cell);
+        }
+        // recombination terms of the children this op transmits to
+        std::vector<int> kids;
+        if (op.type == CHILD) kids.push_back(op.peel);
+        if (op.type == PARENT)
+            for (int c = 0; c < op.n_child; ++c) kids.push_back(od[op.child_at + 4 * c]);
+        std::vector<int> rec_slot(kids.size());
+        for (size_t c = 0; c < kids.size(); ++c) rec_slot[c] = sa.alloc(4);
+        struct Term { int ci; std::vector<int> f; };
+        std::vector<std::vector<Term>> terms(valid.size());
+        std::map<std::pair<int, int>, int> sum_slot;   // (child index, mask) -> slot
+        std::vector<std::pair<int, int>> sum_order;
+        auto gather = [&](int ext, std::vector<int>& f) {
+            const int32_t* pd = od.data() + op.prev_at;
+            for (int j = 0; j < op.n_prev; ++j) {
+                // pd[0] is the previous op's matrix offset; find that op
+                int pk = -1;
+                for (int q = 0; q < k; ++q)
+                    if (ops[q].mat_off == pd[0]) { pk = q; break; }
+                int idx = 0;
+                for (int q = 0; q < pd[1]; ++q) idx |= dig(ext, pd[2 + q]) << (2 * q);
+                const int sl = slot_of[pk][idx];
+                if (sl < 0) return false;
+                f.push_back(sl);
+                pd += 2 + pd[1];
+            }
+            return true;
+        };
+        for (size_t vi = 0; vi < valid.size(); ++vi) {
+            const int cell = valid[vi];
+            if (op.type == CHILD) {
+                const int mt = dig(cell, op.mpos), pt = dig(cell, op.fpos);
+                for (int i = 0; i < 2; ++i)
+                    for (int j = 0; j < 2; ++j) {
+                        const int kt = phased_trait_host(mt, pt, i, j);
+                        if (trait[kt] == 0.0) continue;
+                        Term t;
+                        if (!gather(cell | (kt << (2 * op.c)), t.f)) continue;
+                        t.f.push_back(rec_slot[0] + 2 * i + j);
+                        t.ci = cnst(trait[kt]);
+                        terms[vi].push_back(t);
+                    }
+            } else if (op.type == PARENT) {
+                for (int a = 0; a < 4; ++a) {
+                    if (trait[a] == 0.0) continue;
+                    const int ext = cell | (a << (2 * op.c));
+                    Term t;
+                    if (!gather(ext, t.f)) continue;
+                    int mt = a, pt = a;
+                    bool zero = false;
+                    for (int c = 0; c < op.n_child; ++c) {
+                        const int32_t* cd = od.data() + op.child_at + 4 * c;
+                        const int kt = dig(ext, cd[1]), other = dig(ext, cd[2]);
+                        if (cd[3]) pt = other; else mt = other;
+                        int mask = 0;
+                        for (int i = 0; i < 2; ++i)
+                            for (int j = 0; j < 2; ++j)
+                                if (phased_trait_host(mt, pt, i, j) == kt) mask |= 1 << (2 * i + j);
+                        if (mask == 0) { zero = true; break; }
+                        if ((mask & (mask - 1)) == 0) {
+                            t.f.push_back(rec_slot[c] + __builtin_ctz(mask));
+                        } else {
+                            auto key = std::make_pair(c, mask);
+                            auto it = sum_slot.find(key);
+                            if (it == sum_slot.end()) {
+                                const int sl = sa.alloc(1);
+                                sum_slot[key] = sl;
+                                sum_order.push_back(key);
+                                t.f.push_back(sl);
+                            } else {
+                                t.f.push_back(it->second);
+                            }
+                        }
+                    }
+                    if (zero) continue;
+                    t.ci = cnst(trait[a]);
+                    terms[vi].push_back(t);
+                }
+            } else {
+                for (int a = 0; a < 4; ++a) {
+                    if (trait[a] == 0.0) continue;
+                    Term t;
+                    if (!gather(cell | (a << (2 * op.c)), t.f)) continue;
+                    t.ci = cnst(trait[a]);
+                    terms[vi].push_back(t);
+                }
+            }
+        }
+        // outputs
+        count[k] = (int)valid.size();
+        first[k] = sa.alloc(count[k]);
+        slot_of[k].assign(ncell, -1);
+        for (size_t vi = 0; vi < valid.size(); ++vi) slot_of[k][valid[vi]] = first[k] + (int)vi;
+        // emit
+        for (size_t c = 0; c < kids.size(); ++c) {
+            W.push_back(LI_REC);
+            W.push_back(kids[c]);
+            W.push_back(rec_slot[c]);
+        }
+        for (auto& key : sum_order) {
+            const int c = key.first, mask = key.second;
+            W.push_back(LI_SUM);
+            W.push_back(sum_slot[key]);
+            W.push_back(__builtin_popcount(mask));
+            for (int b = 0; b < 4; ++b)
+                if (mask & (1 << b)) W.push_back(rec_slot[c] + b);
+        }
+        for (size_t vi = 0; vi < valid.size(); ++vi) {
+            W.push_back(LI_CELL);
+            W.push_back(first[k] + (int)vi);
+            W.push_back((int)terms[vi].size());
+            for (auto& t : terms[vi]) {
+                W.push_back((int)t.f.size());
+                W.push_back(t.ci);
+                for (int f : t.f) W.push_back(f);
+            }
+        }
+        if (count[k] > 0) {
+            W.push_back(LI_SCALE);
+            W.push_back(first[k]);
+            W.push_back(count[k]);
+        }
+        // temporaries and consumed matrices are dead now
+        for (size_t c = 0; c < kids.size(); ++c) sa.release(rec_slot[c], 4);
+        for (auto& kv : sum_slot) sa.release(kv.second, 1);
+        const int32_t* pd = od.data() + op.prev_at;
+        for (int j = 0; j < op.n_prev; ++j) {
+            for (int q = 0; q < k; ++q)
+                if (ops[q].mat_off == pd[0]) { sa.release(first[q], count[q]); break; }
+            pd += 2 + pd[1];
+        }
+    }
+    W.push_back(LI_END);
+    W.push_back(count[K - 1] > 0 ? first[K - 1] : -1);
+    out.slots = std::max(1, sa.high);
+}
+
+// ---------------------------------------------------------------------------
 // C ABI
 // ---------------------------------------------------------------------------
 extern "C" {
@@ -675,6 +888,26 @@ int sl_create(const sl_problem_desc* d, const sl_options* opt, sl_ctx** out) {
     CK(cudaMemset(ctx->d_acc, 0, sizeof(double) * npos));
     CK(cudaMemset(ctx->d_init, 0, npos));
     ctx->trait_prob = host_trait_prob(d, ops, od, arena);
+    // compiled trait peel for the batched LOD form
+    P.prog = nullptr;
+    P.pconst = nullptr;
+    P.prog_slots = 0;
+    P.prog_threads = 0;
+    if (ctx->lod_precision == SL_LOD_FP32_RESCALED) {
+        LodProgram prog;
+        compile_lod_program(d, ops, od, prog);
+        int S = 0;
+        for (int t = 128; t >= 32; t /= 2)
+            if ((size_t)t * prog.slots * sizeof(float) <= kSmemBudget / 2) { S = t; break; }
+        if (!S && (size_t)32 * prog.slots * sizeof(float) <= kSmemBudget) S = 32;
+        if (S) {
+            if ((rc = upload(ctx, (int32_t**)&P.prog, prog.words.data(), prog.words.size()))) return bail(rc);
+            if ((rc = upload(ctx, (float**)&P.pconst, prog.consts.data(), std::max<size_t>(1, prog.consts.size()))))
+                return bail(rc);
+            P.prog_slots = prog.slots;
+            P.prog_threads = S;
+        }
+    }
     *out = ctx;
     return SL_OK;
 }
@@ -1029,6 +1262,73 @@ int sl_profile_read(sl_ctx* ctx, int32_t kernel, double* total_ms, int64_t* laun
     if (launches) *launches = ctx->prof_n[kernel];
     ctx->prof_ms[kernel] = 0.0;
     ctx->prof_n[kernel] = 0;
+    return SL_OK;
+}
+
+int sl_problem_lod_program_eval(const sl_problem_desc* d, const int32_t* dg, int32_t locus, int32_t offset,
+                                double* out) {
+    int rc = check_desc(d);
+    if (rc) return rc;
+    if (!dg || !out || locus < 0 || locus >= d->n_markers - 1 || offset < 0 || offset >= d->lod_per_interval)
+        return fail(nullptr, SL_EINVAL, "bad arguments");
+    std::vector<OpDev> ops;
+    std::vector<int32_t> od;
+    int arena = 0, max_child = 1;
+    if ((rc = build_ops(d, ops, od, arena, max_child))) return rc;
+    LodProgram prog;
+    compile_lod_program(d, ops, od, prog);
+    const int N = d->n_members, F = d->n_founders, n = d->lod_per_interval;
+    const double th = d->partial_theta[locus] * (offset + 1), an = 1.0 - th;
+    const double th2 = d->partial_theta[locus] * (n - offset), an2 = 1.0 - th2;
+    auto bit = [&](int person, int l, int par) { return dg[(size_t)2 * N * l + 2 * person + par] & 1; };
+    std::vector<double> A(prog.slots, 0.0);
+    const int32_t* pc = prog.words.data();
+    double result = 0.0;
+    while (true) {
+        const int op = pc[0];
+        if (op == LI_CELL) {
+            const int dst = pc[1], nt = pc[2];
+            pc += 3;
+            double total = 0.0;
+            for (int q = 0; q < nt; ++q) {
+                const int nf = pc[0];
+                double v = prog.consts64[pc[1]];
+                pc += 2;
+                for (int f = 0; f < nf; ++f) v *= A[pc[f]];
+                pc += nf;
+                total += v;
+            }
+            A[dst] = total;
+        } else if (op == LI_REC) {
+            const int c = pc[1], dst = pc[2];
+            pc += 3;
+            for (int i = 0; i < 2; ++i)
+                for (int j = 0; j < 2; ++j) {
+                    double r = (bit(c, locus, 0) == i) ? an : th;
+                    r *= (bit(c, locus + 1, 0) == i) ? an2 : th2;
+                    r *= (bit(c, locus, 1) == j) ? an : th;
+                    r *= (bit(c, locus + 1, 1) == j) ? an2 : th2;
+                    A[dst + 2 * i + j] = 0.25 * r;
+                }
+        } else if (op == LI_SUM) {
+            const int dst = pc[1], ns = pc[2];
+            double v = 0.0;
+            for (int q = 0; q < ns; ++q) v += A[pc[3 + q]];
+            A[dst] = v;
+            pc += 3 + ns;
+        } else if (op == LI_SCALE) {
+            pc += 3;
+        } else {
+            result = pc[1] >= 0 ? A[pc[1]] : 0.0;
+            break;
+        }
+    }
+    if (!(result > 0.0)) return fail(nullptr, SL_EZERO, "trait peel gave a likelihood of 0.0 or less");
+    int cross = 0;
+    for (int i = F; i < N; ++i)
+        for (int par = 0; par < 2; ++par) cross += bit(i, locus, par) != bit(i, locus + 1, par);
+    const double rec = cross * std::log(d->theta[locus]) + (2 * (N - F) - cross) * std::log(1.0 - d->theta[locus]);
+    *out = std::log(result) - rec - std::log(0.5) * (2 * (N - F));
     return SL_OK;
 }
 

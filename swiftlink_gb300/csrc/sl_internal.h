@@ -44,7 +44,20 @@ struct ProblemDev {
     const OpDev* ops;                    // [K]
     const int32_t* opdata;
     const int16_t* fag_order;            // [N] parents before children, founders first
+    const int32_t* prog;                 // compiled trait peel (LI_* words), or null
+    const float* pconst;                 // its constants
+    int32_t prog_slots;                  // FP32 slots one task of the program needs
+    int32_t prog_threads;                // threads per block of the program kernel
 };
+
+// Instructions of a compiled trait-peel program (the batched LOD scorer).
+//   LI_REC  child dst            A[dst + 2i + j] = 0.25 * recombination term of child (i, j)
+//   LI_SUM  dst n src...         A[dst] = sum of A[src]
+//   LI_CELL dst nterm, then per term: nf const_index slot x nf
+//                                A[dst] = sum over terms of const * product of A[slot]
+//   LI_SCALE first count         divide A[first .. first+count) by 2^e, e from their max
+//   LI_END  slot                 the likelihood
+enum { LI_REC = 1, LI_SUM = 2, LI_CELL = 3, LI_SCALE = 4, LI_END = 5 };
 
 // What code outside sl_host.cc may read of a context.
 struct CtxView {

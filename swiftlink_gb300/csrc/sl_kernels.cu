@@ -1169,6 +1169,94 @@ __global__ void __launch_bounds__(128) lod_kernel(ProblemDev P, const uint32_t* 
     }
 }
 
+// Batched trait peel: one thread per (graph, interval, position) runs the
+// compiled LI_* program; every lane of a warp executes the same instruction
+// stream (uniform loads of the program) on its own recombination terms, with
+// its FP32 slots in shared memory at [slot][thread].  Each rfunction's cells
+// are rescaled by a power of two after they are computed; the exponents are
+// summed and restored in FP64 at the end.
+__global__ void __launch_bounds__(128) lod_prog_kernel(ProblemDev P, const uint32_t* graphs, int64_t graph_words,
+                                                       int G, double* vals, int* status) {
+    extern __shared__ float sh[];
+    const int S = blockDim.x;
+    float* A = sh + threadIdx.x;
+    const int n = P.n_lod;
+    const int64_t npos = (int64_t)(P.M - 1) * n;
+    const int64_t ntask = (int64_t)G * npos;
+    for (int64_t t = (int64_t)blockIdx.x * S + threadIdx.x; t < ntask; t += (int64_t)gridDim.x * S) {
+        const int b = (int)(t / npos);
+        const int64_t pidx = t % npos;
+        const int l = (int)(pidx / n), o = (int)(pidx % n);
+        const uint32_t* colL = graphs + (size_t)b * graph_words + (size_t)l * P.W;
+        const uint32_t* colR = colL + P.W;
+        const double thd = P.partial[l] * (double)(o + 1);
+        const double th2d = P.partial[l] * (double)(n - o);
+        const float th = (float)thd, an = (float)(1.0 - thd), th2 = (float)th2d, an2 = (float)(1.0 - th2d);
+        int scale = 0;
+        float result = 0.f;
+        const int32_t* pc = P.prog;
+        while (true) {
+            const int op = __ldg(pc);
+            if (op == LI_CELL) {
+                const int dst = __ldg(pc + 1), nt = __ldg(pc + 2);
+                pc += 3;
+                float total = 0.f;
+                for (int q = 0; q < nt; ++q) {
+                    const int nf = __ldg(pc);
+                    float v = __ldg(P.pconst + __ldg(pc + 1));
+                    pc += 2;
+                    for (int f = 0; f < nf; ++f) v *= A[__ldg(pc + f) * S];
+                    pc += nf;
+                    total += v;
+                }
+                A[dst * S] = total;
+            } else if (op == LI_REC) {
+                const int child = __ldg(pc + 1), dst = __ldg(pc + 2);
+                pc += 3;
+                const int bits = person_bits(P, colL, colR, child);
+                A[(dst + 0) * S] = 0.25f * trait_rec<float>(bits, 0, 0, th, an, th2, an2);
+                A[(dst + 1) * S] = 0.25f * trait_rec<float>(bits, 0, 1, th, an, th2, an2);
+                A[(dst + 2) * S] = 0.25f * trait_rec<float>(bits, 1, 0, th, an, th2, an2);
+                A[(dst + 3) * S] = 0.25f * trait_rec<float>(bits, 1, 1, th, an, th2, an2);
+            } else if (op == LI_SUM) {
+                const int dst = __ldg(pc + 1), ns = __ldg(pc + 2);
+                float v = 0.f;
+                for (int q = 0; q < ns; ++q) v += A[__ldg(pc + 3 + q) * S];
+                A[dst * S] = v;
+                pc += 3 + ns;
+            } else if (op == LI_SCALE) {
+                const int first = __ldg(pc + 1), cnt = __ldg(pc + 2);
+                pc += 3;
+                float mx = 0.f;
+                for (int q = 0; q < cnt; ++q) mx = fmaxf(mx, A[(first + q) * S]);
+                if (mx > 0.f) {
+                    const int e = ilogbf(mx);
+                    const float f = scalbnf(1.0f, -e);
+                    for (int q = 0; q < cnt; ++q) A[(first + q) * S] *= f;
+                    scale += e;
+                }
+            } else {
+                const int rs = __ldg(pc + 1);
+                result = rs >= 0 ? A[rs * S] : 0.f;
+                break;
+            }
+        }
+        // DescentGraph::get_recombination_prob (descent_graph.cc:212-242) by crossover count
+        int cross = 0;
+        for (int w = 0; w < P.W; ++w) cross += __popc(colL[w] ^ colR[w]);
+        const double lt = log(P.theta[l]), la = log(1.0 - P.theta[l]);
+        const double rec = cross * lt + (2 * P.Nnf - cross) * la;
+        double v;
+        if (!(result > 0.f)) {
+            set_status(status, ST_LOD_NONPOS);
+            v = -DBL_MAX;
+        } else {
+            v = log((double)result) + (double)scale * 0.69314718055994530942 - rec - P.marker_trans;
+        }
+        vals[t] = v;
+    }
+}
+
 // log_sum (logarithms.cc:14-25)
 __device__ __forceinline__ double log_sum(double a, double b) {
     if (a == -DBL_MAX) return b;
@@ -1308,6 +1396,18 @@ cudaError_t launch_lod(const ProblemDev& P, int precision, const uint32_t* graph
             configured = smem;
         }
         lod_kernel<double, false><<<(int)grid, wpb * 32, smem, s>>>(P, graphs, graph_words, G, vals, status);
+    } else if (P.prog) {
+        const int S = P.prog_threads;
+        const size_t smem = (size_t)S * P.prog_slots * sizeof(float);
+        static size_t configured_prog = 0;
+        if (smem > configured_prog) {
+            cudaError_t e = cudaFuncSetAttribute(lod_prog_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess) return e;
+            configured_prog = smem;
+        }
+        int64_t pgrid = (ntask + S - 1) / S;
+        if (pgrid > grid_cap * 4) pgrid = grid_cap * 4;
+        lod_prog_kernel<<<(int)pgrid, S, smem, s>>>(P, graphs, graph_words, G, vals, status);
     } else {
         const size_t smem = (size_t)wpb * P.arena * sizeof(float);
         static size_t configured = 0;

@@ -97,3 +97,26 @@ def test_create_without_gpu_fails_cleanly():
     with pytest.raises(api.SwiftLinkError) as e:
         api.Context(api.Problem.from_arrays(g))
     assert e.value.code == api.SL_ENODEV
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_compiled_lod_program_matches_reference(name):
+    """The host compiler of the batched trait peel, evaluated in FP64, gives the
+    reference's per-position log-likelihood ratios."""
+    g = load_golden(name)
+    prob = api.Problem.from_arrays(g)
+    desc = prob.desc()
+    dg = np.ascontiguousarray(g["lod_graphs"][0], np.int32)
+    n = g["n_lod"]
+    raw_one = None
+    from oracle import port
+    raw_one, _, _ = port.Port(g).lod(dg[None])
+    rng = np.random.default_rng(3)
+    loci = sorted(set([0, g["M"] - 2] + list(rng.integers(0, g["M"] - 1, 12))))
+    fn = api.lib().sl_problem_lod_program_eval
+    for l in loci:
+        for o in range(n):
+            v = ctypes.c_double()
+            rc = fn(ctypes.byref(desc), dg.ctypes.data_as(ctypes.c_void_p), int(l), o, ctypes.byref(v))
+            assert rc == 0
+            assert abs(v.value - raw_one[l * n + o]) <= 1e-9 * max(1.0, abs(raw_one[l * n + o])), (l, o)
