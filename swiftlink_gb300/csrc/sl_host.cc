@@ -27,7 +27,7 @@ cudaError_t launch_msampler(const ProblemDev& P, uint32_t* dg, int first, int nc
                             int64_t mstride, int nm, const double* u, int64_t ucs, uint64_t seed, uint64_t iter,
                             const uint8_t* sel, int want, double* raw64, float* raw32, void* fb, uint8_t* badc,
                             uint8_t* maps, int* status, int fag_threads, int exact, cudaStream_t s);
-size_t fag_smem(int N, int F, int threads);
+size_t fag_smem(int N, int F, int threads, int fast);
 cudaError_t launch_lod(const ProblemDev& P, int precision, const uint32_t* graphs, int64_t graph_words, int G,
                        double* vals, int* status, cudaStream_t s, int grid_cap, int wpb);
 cudaError_t launch_lod_merge(const double* vals, int G, int64_t npos, double* acc, uint8_t* init, cudaStream_t s);
@@ -853,12 +853,18 @@ int sl_create(const sl_problem_desc* d, const sl_options* opt, sl_ctx** out) {
     const int lod_blocks = std::max(1, (int)std::min<size_t>(16, per_sm / (ctx->lod_wpb * lodw + 1024)));
     ctx->ls_grid = ctx->sms * ls_blocks;
     ctx->lod_grid = ctx->sms * lod_blocks;
-    // founder-allele-graph block: the widest of 128/96/64/32 threads whose state
-    // fits two blocks per SM, else one
+    // founder-allele-graph block: the size that keeps the most threads resident
+    // per SM (a chain-by-locus grid then fits in as few waves as possible)
     ctx->ms_threads = 0;
-    for (int half = 1; half >= 0 && !ctx->ms_threads; --half)
-        for (int t = 128; t >= 32; t -= 32)
-            if (fag_smem(N, F, t) <= (half ? per_sm / 2 - 2048 : kSmemBudget)) { ctx->ms_threads = t; break; }
+    {
+        int best = 0;
+        for (int t = 32; t <= 128; t += 32) {
+            const size_t b = fag_smem(N, F, t, ctx->sampler_precision == SL_SAMPLER_FAST) + 1024;
+            if (b > kSmemBudget) break;
+            const int resident = t * (int)std::min<size_t>(32, per_sm / b);
+            if (resident > best) { best = resident; ctx->ms_threads = t; }
+        }
+    }
     if (!ctx->ms_threads)
         return bail(fail(nullptr, SL_EINVAL, "founder-allele graph state too large for shared memory"));
 

@@ -303,6 +303,34 @@ __global__ void __launch_bounds__(128) lsampler_kernel(ProblemDev P, uint32_t* d
 // block's threads (element i of thread t at [i * S + t]) so a warp's accesses
 // to the same field hit 32 consecutive banks.
 // ---------------------------------------------------------------------------
+// Probability arithmetic of the founder-allele graph.  ProbExact is the
+// reference's FP64 (bit-exact); ProbLog2 works on log2 values in FP32 for the
+// fast sampler mode, where only the normalised pair of likelihoods is used:
+// products become sums and a zero likelihood is -inf.
+struct ProbExact {
+    using T = double;
+    static __device__ __forceinline__ T zero() { return 0.0; }
+    static __device__ __forceinline__ T one() { return 1.0; }
+    static __device__ __forceinline__ T mul(T a, T b) { return DMUL(a, b); }
+    static __device__ __forceinline__ T add(T a, T b) { return DADD(a, b); }
+    static __device__ __forceinline__ T from(double x) { return x; }
+    static __device__ __forceinline__ bool is_zero(T a) { return a == 0.0; }
+};
+struct ProbLog2 {
+    using T = float;
+    static __device__ __forceinline__ T zero() { return -INFINITY; }
+    static __device__ __forceinline__ T one() { return 0.f; }
+    static __device__ __forceinline__ T mul(T a, T b) { return a + b; }
+    static __device__ __forceinline__ T add(T a, T b) {
+        if (a == -INFINITY) return b;
+        if (b == -INFINITY) return a;
+        const T m = fmaxf(a, b), d = fminf(a, b) - m;
+        return m + log2f(1.f + exp2f(d));
+    }
+    static __device__ __forceinline__ T from(double x) { return x > 0.0 ? log2f((float)x) : -INFINITY; }
+    static __device__ __forceinline__ bool is_zero(T a) { return a == -INFINITY; }
+};
+
 // Founder-allele groups are kept in a union-find whose links carry a swap
 // parity: the reference relabels every member of the absorbed component and
 // swaps its two allele assignments when merging (combine_components,
@@ -313,10 +341,10 @@ __global__ void __launch_bounds__(128) lsampler_kernel(ProblemDev P, uint32_t* d
 // product follow the reference's order exactly, so the likelihood is the
 // same double.  IX is uint8_t when 2F <= 255 (founder-allele and group ids
 // fit a byte), else uint16_t.
-template <typename IX>
+template <typename IX, typename PT>
 struct Fag {
-    double* pr0;      // [2F][S] prob[0][group]
-    double* pr1;      // [2F][S]
+    PT* pr0;          // [2F][S] prob[0][group]
+    PT* pr1;          // [2F][S]
     IX* edge;         // [2N][S] founder allele of each person's maternal/paternal allele
     IX* up;           // [2F][S] union-find parent of a founder allele
     uint8_t* fl;      // [2F][S] bit0 parity to parent, bit1 in a group, bits 2-3 a0, bits 4-5 a1
@@ -324,30 +352,31 @@ struct Fag {
     IX* root;         // [2F][S] root founder allele of a group id
     IX* gid;          // [2F][S] group id of a root founder allele
     int S, t;
-    __device__ __forceinline__ double& p0(int g) { return pr0[g * S + t]; }
-    __device__ __forceinline__ double& p1(int g) { return pr1[g * S + t]; }
-    __device__ __forceinline__ double& pw(int w, int g) { return w == 0 ? p0(g) : p1(g); }
+    __device__ __forceinline__ PT& p0(int g) { return pr0[g * S + t]; }
+    __device__ __forceinline__ PT& p1(int g) { return pr1[g * S + t]; }
+    __device__ __forceinline__ PT& pw(int w, int g) { return w == 0 ? p0(g) : p1(g); }
     __device__ __forceinline__ IX& e(int i) { return edge[i * S + t]; }
 };
 
-__host__ __device__ inline size_t fag_per_thread(int N, int F) {
+__host__ __device__ inline size_t fag_per_thread(int N, int F, int fast) {
     const size_t ix = (2 * F <= 255) ? 1 : 2;
-    return (size_t)2 * F * 16 + (size_t)2 * N * ix + (size_t)2 * F * (3 * ix + 2);
+    const size_t pb = fast ? 4 : 8;
+    return (size_t)2 * F * 2 * pb + (size_t)2 * N * ix + (size_t)2 * F * (3 * ix + 2);
 }
 
 // Shared bytes of a block of S threads: the FAG arrays plus the staged
 // person tables (order, mother, father as int16 and typed as uint8).
-__host__ __device__ inline size_t fag_block_bytes(int N, int F, int S) {
+__host__ __device__ inline size_t fag_block_bytes(int N, int F, int S, int fast) {
     size_t tables = ((size_t)N * 7 + 15) & ~(size_t)15;
-    return ((fag_per_thread(N, F) * S + 15) & ~(size_t)15) + tables;
+    return ((fag_per_thread(N, F, fast) * S + 15) & ~(size_t)15) + tables;
 }
 
-template <typename IX>
-__device__ __forceinline__ Fag<IX> fag_bind(unsigned char* p, int N, int F, int S, int t) {
-    Fag<IX> s;
+template <typename IX, typename PT>
+__device__ __forceinline__ Fag<IX, PT> fag_bind(unsigned char* p, int N, int F, int S, int t) {
+    Fag<IX, PT> s;
     s.S = S;
     s.t = t;
-    s.pr0 = (double*)p;
+    s.pr0 = (PT*)p;
     s.pr1 = s.pr0 + (size_t)2 * F * S;
     s.edge = (IX*)(s.pr1 + (size_t)2 * F * S);
     s.up = s.edge + (size_t)2 * N * S;
@@ -372,8 +401,8 @@ __device__ __forceinline__ int fag_other(int obs, int x) {
 
 // Root of a founder allele's component and the parity from the allele to it,
 // compressing the path.
-template <typename IX>
-__device__ __forceinline__ int fag_find(Fag<IX>& s, int fa, int& parity) {
+template <typename FS>
+__device__ __forceinline__ int fag_find(FS& s, int fa, int& parity) {
     int r = fa, p = 0;
     while (true) {
         const int u = s.up[r * s.S + s.t];
@@ -385,7 +414,7 @@ __device__ __forceinline__ int fag_find(Fag<IX>& s, int fa, int& parity) {
     while (x != r) {
         const int u = s.up[x * s.S + s.t];
         const uint8_t f = s.fl[x * s.S + s.t];
-        s.up[x * s.S + s.t] = (IX)r;
+        s.up[x * s.S + s.t] = r;
         s.fl[x * s.S + s.t] = (uint8_t)((f & ~1) | px);
         px ^= f & 1;
         x = u;
@@ -397,60 +426,61 @@ __device__ __forceinline__ int fag_find(Fag<IX>& s, int fa, int& parity) {
 // A founder allele as the reference sees it: its group id (-1 = none) and its
 // two allele assignments in its group's frame.
 struct FaView {
-    int group, a[2];
+    int group, a0, a1;
+    __device__ __forceinline__ int a(int w) const { return w ? a1 : a0; }
 };
 
-template <typename IX>
-__device__ __forceinline__ FaView fag_view(Fag<IX>& s, int fa) {
+template <typename FS>
+__device__ __forceinline__ FaView fag_view(FS& s, int fa) {
     FaView v;
     const uint8_t f = s.fl[fa * s.S + s.t];
-    if (!(f & 2)) { v.group = -1; v.a[0] = v.a[1] = 0; return v; }
+    if (!(f & 2)) { v.group = -1; v.a0 = v.a1 = 0; return v; }
     int par;
     const int r = fag_find(s, fa, par);
     const uint8_t g = s.fl[fa * s.S + s.t];
     const int s0 = (g >> 2) & 3, s1 = (g >> 4) & 3;
     v.group = s.gid[r * s.S + s.t];
-    v.a[0] = par ? s1 : s0;
-    v.a[1] = par ? s0 : s1;
+    v.a0 = par ? s1 : s0;
+    v.a1 = par ? s0 : s1;
     return v;
 }
 
 // Put founder allele fa in group g with assignment value `val` in slot w (the
 // other slot unset, as in the reference), linked straight to the group's root.
-template <typename IX>
-__device__ __forceinline__ void fag_join(Fag<IX>& s, int fa, int g, int w, int val) {
+template <typename FS>
+__device__ __forceinline__ void fag_join(FS& s, int fa, int g, int w, int val) {
     const int r = s.root[g * s.S + s.t];
-    s.up[fa * s.S + s.t] = (IX)r;
+    s.up[fa * s.S + s.t] = r;
     s.fl[fa * s.S + s.t] = (uint8_t)(2 | (val << (w == 0 ? 2 : 4)));
 }
 
-template <typename IX>
-__device__ __forceinline__ void fag_join2(Fag<IX>& s, int fa, int g, int v0, int v1) {
+template <typename FS>
+__device__ __forceinline__ void fag_join2(FS& s, int fa, int g, int v0, int v1) {
     const int r = s.root[g * s.S + s.t];
-    s.up[fa * s.S + s.t] = (IX)r;
+    s.up[fa * s.S + s.t] = r;
     s.fl[fa * s.S + s.t] = (uint8_t)(2 | (v0 << 2) | (v1 << 4));
 }
 
-template <typename IX>
-__device__ __forceinline__ void fag_new_root(Fag<IX>& s, int fa, int g, int v0, int v1) {
-    s.up[fa * s.S + s.t] = (IX)fa;
+template <typename FS>
+__device__ __forceinline__ void fag_new_root(FS& s, int fa, int g, int v0, int v1) {
+    s.up[fa * s.S + s.t] = fa;
     s.fl[fa * s.S + s.t] = (uint8_t)(2 | (v0 << 2) | (v1 << 4));
-    s.root[g * s.S + s.t] = (IX)fa;
-    s.gid[fa * s.S + s.t] = (IX)g;
+    s.root[g * s.S + s.t] = fa;
+    s.gid[fa * s.S + s.t] = g;
 }
 
 // combine_components(c1, c2, flip) (founder_allele_graph4.cc:491-541)
-template <typename IX>
-__device__ __forceinline__ void fag_combine(Fag<IX>& s, int c1, int c2, bool flip) {
+template <typename PP, typename FS>
+__device__ __forceinline__ void fag_combine(FS& s, int c1, int c2, bool flip) {
     const int r1 = s.root[c1 * s.S + s.t], r2 = s.root[c2 * s.S + s.t];
-    s.up[r2 * s.S + s.t] = (IX)r1;
+    s.up[r2 * s.S + s.t] = r1;
     s.fl[r2 * s.S + s.t] = (uint8_t)((s.fl[r2 * s.S + s.t] & ~1) | (flip ? 1 : 0));
     if (flip) {
-        s.p0(c1) = DMUL(s.p0(c1), s.p1(c2));
-        s.p1(c1) = DMUL(s.p1(c1), s.p0(c2));
+        s.p0(c1) = PP::mul(s.p0(c1), s.p1(c2));
+        s.p1(c1) = PP::mul(s.p1(c1), s.p0(c2));
     } else {
-        s.p0(c1) = DMUL(s.p0(c1), s.p0(c2));
-        s.p1(c1) = DMUL(s.p1(c1), s.p1(c2));
+        s.p0(c1) = PP::mul(s.p0(c1), s.p0(c2));
+        s.p1(c1) = PP::mul(s.p1(c1), s.p1(c2));
     }
     s.fx[c2 * s.S + s.t] = 2;
 }
@@ -458,14 +488,14 @@ __device__ __forceinline__ void fag_combine(Fag<IX>& s, int c1, int c2, bool fli
 // Edges of the column (FounderAlleleGraph4::reset, founder_allele_graph4.cc:
 // 543-569) with one meiosis optionally toggled, which equals flip() and its
 // propagation (founder_allele_graph4.cc:571-597).
-template <typename IX>
+template <typename FS>
 __device__ void fag_edges(int N, int F, const int16_t* order, const int16_t* mo, const int16_t* fa,
-                          const uint32_t* col, Fag<IX>& s, int flip_b) {
+                          const uint32_t* col, FS& s, int flip_b) {
     for (int n = 0; n < N; ++n) {
         const int pid = order[n];
         if (pid < F) {
-            s.e(2 * pid) = (IX)(2 * pid);
-            s.e(2 * pid + 1) = (IX)(2 * pid + 1);
+            s.e(2 * pid) = 2 * pid;
+            s.e(2 * pid + 1) = 2 * pid + 1;
         } else {
             const int b = 2 * (pid - F);
             const int vm = dgbit(col, b) ^ (flip_b == b);
@@ -476,37 +506,39 @@ __device__ void fag_edges(int N, int F, const int16_t* order, const int16_t* mo,
     }
 }
 
-template <typename IX>
-__device__ double fag_like(int N, int F, const uint8_t* typed, const uint8_t* gcol, double minor, Fag<IX>& s) {
+template <typename PP, typename FS>
+__device__ typename PP::T fag_like(int N, int F, const uint8_t* typed, const uint8_t* gcol, double minor_d, FS& s) {
+    using T = typename PP::T;
     const int nfa = 2 * F;
-    const double major = DSUB(1.0, minor);
+    const T major = PP::from(DSUB(1.0, minor_d)), minor = PP::from(minor_d);
     for (int i = 0; i < nfa; ++i) s.fl[i * s.S + s.t] = 0;
     int gi = 0;
 #define FREQ(g) ((g) == G_HOMOZ_A ? major : minor)
 #define FX(g) s.fx[(g) * s.S + s.t]
+#define ZERO PP::zero()
     for (int i = 0; i < N; ++i) {
         if (!typed[i]) continue;
         const int g = gcol[i] & 3;
         if (g == G_UNTYPED) continue;
         const int mfa = s.e(2 * i), pfa = s.e(2 * i + 1);
         if (mfa == pfa) {
-            if (g == G_HETERO) return 0.0;
+            if (g == G_HETERO) return ZERO;
             const FaView m = fag_view(s, mfa);
             if (m.group != -1) {
                 const int g1 = m.group;
                 const int f1 = FX(g1);
                 if (f1 != -1) {
-                    if (g != m.a[f1]) return 0.0;
+                    if (g != m.a(f1)) return ZERO;
                 } else {
-                    if (m.a[0] == g) { FX(g1) = 0; s.p1(g1) = 0.0; }
-                    else if (m.a[1] == g) { FX(g1) = 1; s.p0(g1) = 0.0; }
-                    else return 0.0;
+                    if (m.a(0) == g) { FX(g1) = 0; s.p1(g1) = ZERO; }
+                    else if (m.a(1) == g) { FX(g1) = 1; s.p0(g1) = ZERO; }
+                    else return ZERO;
                 }
             } else {
                 fag_new_root(s, mfa, gi, g, 0);
                 FX(gi) = 0;
                 s.p0(gi) = FREQ(g);
-                s.p1(gi) = 0.0;
+                s.p1(gi) = ZERO;
                 ++gi;
             }
             continue;
@@ -519,37 +551,37 @@ __device__ double fag_like(int N, int F, const uint8_t* typed, const uint8_t* gc
             if (g2 != -1) {
                 if (g1 == g2) {
                     if (f1 != -1) {
-                        if (!fag_legal(g, m.a[f1], p.a[f1])) return 0.0;
+                        if (!fag_legal(g, m.a(f1), p.a(f1))) return ZERO;
                     } else {
-                        const int l0 = fag_legal(g, m.a[0], p.a[0]);
-                        const int l1 = fag_legal(g, m.a[1], p.a[1]);
+                        const int l0 = fag_legal(g, m.a(0), p.a(0));
+                        const int l1 = fag_legal(g, m.a(1), p.a(1));
                         if (l0) {
-                            if (!l1) { FX(g1) = 0; s.p1(g1) = 0.0; }
+                            if (!l1) { FX(g1) = 0; s.p1(g1) = ZERO; }
                         } else {
-                            if (l1) { FX(g1) = 1; s.p0(g1) = 0.0; }
-                            else return 0.0;
+                            if (l1) { FX(g1) = 1; s.p0(g1) = ZERO; }
+                            else return ZERO;
                         }
                     }
                 } else {
                     int f2 = FX(g2);
                     if (f1 != -1) {
                         if (f2 != -1) {
-                            if (!fag_legal(g, m.a[f1], p.a[f2])) return 0.0;
+                            if (!fag_legal(g, m.a(f1), p.a(f2))) return ZERO;
                         } else {
-                            const int l0 = fag_legal(g, m.a[f1], p.a[0]);
-                            const int l1 = fag_legal(g, m.a[f1], p.a[1]);
-                            if (l0) f2 = 0; else if (l1) f2 = 1; else return 0.0;
+                            const int l0 = fag_legal(g, m.a(f1), p.a(0));
+                            const int l1 = fag_legal(g, m.a(f1), p.a(1));
+                            if (l0) f2 = 0; else if (l1) f2 = 1; else return ZERO;
                         }
                     } else if (f2 != -1) {
-                        const int l0 = fag_legal(g, m.a[0], p.a[f2]);
-                        const int l1 = fag_legal(g, m.a[1], p.a[f2]);
-                        if (l0) f1 = 0; else if (l1) f1 = 1; else return 0.0;
+                        const int l0 = fag_legal(g, m.a(0), p.a(f2));
+                        const int l1 = fag_legal(g, m.a(1), p.a(f2));
+                        if (l0) f1 = 0; else if (l1) f1 = 1; else return ZERO;
                     } else {
-                        const int l0 = fag_legal(g, m.a[0], p.a[0]);
-                        const int l1 = fag_legal(g, m.a[1], p.a[0]);
-                        const int l2 = fag_legal(g, m.a[0], p.a[1]);
-                        const int l3 = fag_legal(g, m.a[1], p.a[1]);
-                        if (!(l0 || l1 || l2 || l3)) return 0.0;
+                        const int l0 = fag_legal(g, m.a(0), p.a(0));
+                        const int l1 = fag_legal(g, m.a(1), p.a(0));
+                        const int l2 = fag_legal(g, m.a(0), p.a(1));
+                        const int l3 = fag_legal(g, m.a(1), p.a(1));
+                        if (!(l0 || l1 || l2 || l3)) return ZERO;
                         if (l0 && !(l1 || l2 || l3)) { f1 = 0; f2 = 0; }
                         else if (l1 && !(l0 || l2 || l3)) { f1 = 1; f2 = 0; }
                         else if (l2 && !(l0 || l1 || l3)) { f1 = 0; f2 = 1; }
@@ -560,107 +592,108 @@ __device__ double fag_like(int N, int F, const uint8_t* typed, const uint8_t* gc
                     }
                     if (f1 != f2) {
                         FX(g1) = (int8_t)f1;
-                        s.pw(1 - f1, g1) = 0.0;
-                        s.pw(1 - f2, g2) = 0.0;
-                        fag_combine(s, g1, g2, true);
+                        s.pw(1 - f1, g1) = ZERO;
+                        s.pw(1 - f2, g2) = ZERO;
+                        fag_combine<PP>(s, g1, g2, true);
                     } else if (f1 == -2) {
                         FX(g1) = -1;
-                        fag_combine(s, g1, g2, true);
+                        fag_combine<PP>(s, g1, g2, true);
                     } else {
                         FX(g1) = (int8_t)f1;
                         if (f1 != -1) {
-                            s.pw(1 - f1, g1) = 0.0;
-                            s.pw(1 - f2, g2) = 0.0;
+                            s.pw(1 - f1, g1) = ZERO;
+                            s.pw(1 - f2, g2) = ZERO;
                         }
-                        fag_combine(s, g1, g2, false);
+                        fag_combine<PP>(s, g1, g2, false);
                     }
                 }
             } else {
                 if (f1 != -1) {
-                    const int t0 = fag_other(g, m.a[f1]);
-                    if (t0 == G_UNTYPED) return 0.0;
+                    const int t0 = fag_other(g, m.a(f1));
+                    if (t0 == G_UNTYPED) return ZERO;
                     fag_join(s, pfa, g1, f1, t0);
-                    s.pw(f1, g1) = DMUL(s.pw(f1, g1), FREQ(t0));
+                    s.pw(f1, g1) = PP::mul(s.pw(f1, g1), FREQ(t0));
                 } else {
-                    const int t0 = fag_other(g, m.a[0]);
-                    const int t1 = fag_other(g, m.a[1]);
+                    const int t0 = fag_other(g, m.a(0));
+                    const int t1 = fag_other(g, m.a(1));
                     if (t0 != G_UNTYPED) {
                         if (t1 != G_UNTYPED) {
                             fag_join2(s, pfa, g1, t0, t1);
-                            s.p0(g1) = DMUL(s.p0(g1), FREQ(t0));
-                            s.p1(g1) = DMUL(s.p1(g1), FREQ(t1));
+                            s.p0(g1) = PP::mul(s.p0(g1), FREQ(t0));
+                            s.p1(g1) = PP::mul(s.p1(g1), FREQ(t1));
                         } else {
                             fag_join(s, pfa, g1, 0, t0);
-                            s.p0(g1) = DMUL(s.p0(g1), FREQ(t0));
-                            s.p1(g1) = 0.0;
+                            s.p0(g1) = PP::mul(s.p0(g1), FREQ(t0));
+                            s.p1(g1) = ZERO;
                             FX(g1) = 0;
                         }
                     } else {
                         if (t1 != G_UNTYPED) {
                             fag_join(s, pfa, g1, 1, t1);
-                            s.p1(g1) = DMUL(s.p1(g1), FREQ(t1));
-                            s.p0(g1) = 0.0;
+                            s.p1(g1) = PP::mul(s.p1(g1), FREQ(t1));
+                            s.p0(g1) = ZERO;
                             FX(g1) = 1;
-                        } else return 0.0;
+                        } else return ZERO;
                     }
                 }
             }
         } else if (g2 != -1) {
             const int f2 = FX(g2);
             if (f2 != -1) {
-                const int t0 = fag_other(g, p.a[f2]);
-                if (t0 == G_UNTYPED) return 0.0;
+                const int t0 = fag_other(g, p.a(f2));
+                if (t0 == G_UNTYPED) return ZERO;
                 fag_join(s, mfa, g2, f2, t0);
-                s.pw(f2, g2) = DMUL(s.pw(f2, g2), FREQ(t0));
+                s.pw(f2, g2) = PP::mul(s.pw(f2, g2), FREQ(t0));
             } else {
-                const int t0 = fag_other(g, p.a[0]);
-                const int t1 = fag_other(g, p.a[1]);
+                const int t0 = fag_other(g, p.a(0));
+                const int t1 = fag_other(g, p.a(1));
                 if (t0 != G_UNTYPED) {
                     if (t1 != G_UNTYPED) {
                         fag_join2(s, mfa, g2, t0, t1);
-                        s.p0(g2) = DMUL(s.p0(g2), FREQ(t0));
-                        s.p1(g2) = DMUL(s.p1(g2), FREQ(t1));
+                        s.p0(g2) = PP::mul(s.p0(g2), FREQ(t0));
+                        s.p1(g2) = PP::mul(s.p1(g2), FREQ(t1));
                     } else {
                         fag_join(s, mfa, g2, 0, t0);
-                        s.p0(g2) = DMUL(s.p0(g2), FREQ(t0));
-                        s.p1(g2) = 0.0;
+                        s.p0(g2) = PP::mul(s.p0(g2), FREQ(t0));
+                        s.p1(g2) = ZERO;
                         FX(g2) = 0;
                     }
                 } else {
                     if (t1 != G_UNTYPED) {
                         fag_join(s, mfa, g2, 1, t1);
-                        s.p1(g2) = DMUL(s.p1(g2), FREQ(t1));
-                        s.p0(g2) = 0.0;
+                        s.p1(g2) = PP::mul(s.p1(g2), FREQ(t1));
+                        s.p0(g2) = ZERO;
                         FX(g2) = 1;
-                    } else return 0.0;
+                    } else return ZERO;
                 }
             }
         } else {
             if (g == G_HETERO) {
                 fag_new_root(s, mfa, gi, G_HOMOZ_A, G_HOMOZ_B);
                 fag_join2(s, pfa, gi, G_HOMOZ_B, G_HOMOZ_A);
-                s.p0(gi) = DMUL(major, minor);
-                s.p1(gi) = DMUL(major, minor);
+                s.p0(gi) = PP::mul(major, minor);
+                s.p1(gi) = PP::mul(major, minor);
                 FX(gi) = -1;
             } else {
                 fag_new_root(s, mfa, gi, g, 0);
                 fag_join(s, pfa, gi, 0, g);
-                s.p0(gi) = DMUL(FREQ(g), FREQ(g));
-                s.p1(gi) = 0.0;
+                s.p0(gi) = PP::mul(FREQ(g), FREQ(g));
+                s.p1(gi) = ZERO;
                 FX(gi) = 0;
             }
             ++gi;
         }
     }
 #undef FREQ
-    double ret = 1.0;
+    T ret = PP::one();
     for (int i = 0; i < gi; ++i) {
         const int f = FX(i);
         if (f == 2) continue;
-        if (f != -1) ret = DMUL(ret, s.pw(f, i));
-        else ret = DMUL(ret, DADD(s.p0(i), s.p1(i)));
+        if (f != -1) ret = PP::mul(ret, s.pw(f, i));
+        else ret = PP::mul(ret, PP::add(s.p0(i), s.p1(i)));
     }
 #undef FX
+#undef ZERO
     return ret;
 }
 
@@ -681,16 +714,30 @@ __device__ __forceinline__ void put_raw32(float* r32, int l, double v0, double v
     r32[2 * l + 1] = b;
 }
 
-// step < 0: reset at order[0] (raw64[l][cur] = likelihood of the column);
-// step >= 0: likelihoods of meiosis order[step] at both values.
-template <typename IX>
+__device__ __forceinline__ void put_raw32_log2(float* r32, int l, float l0, float l1) {
+    const float mx = fmaxf(l0, l1);
+    float a = 0.f, b = 0.f;
+    if (mx != -INFINITY) {
+        a = l0 == -INFINITY ? 0.f : exp2f(l0 - mx);
+        b = l1 == -INFINITY ? 0.f : exp2f(l1 - mx);
+    }
+    r32[2 * l] = a;
+    r32[2 * l + 1] = b;
+}
+
+// step < 0: reset at order[0] (raw[l][cur] = likelihood of the column);
+// step >= 0: likelihoods of meiosis order[step] at both values.  With
+// ProbExact, raw holds the reference's doubles; with ProbLog2 it holds log2
+// likelihoods and raw32 receives each pair divided by its larger member.
+template <typename IX, typename PP>
 __global__ void __launch_bounds__(128) fag_kernel(ProblemDev P, uint32_t* dg, int first, int nchain,
                                                   const int32_t* order, int64_t ostride, int step,
-                                                  const uint8_t* sel, int want, double* raw64, float* raw32,
-                                                  uint8_t* badc, int* status) {
+                                                  const uint8_t* sel, int want, typename PP::T* rawbuf,
+                                                  float* raw32, uint8_t* badc, int* status, int fast) {
+    using T = typename PP::T;
     extern __shared__ __align__(16) unsigned char smem[];
     const int S = blockDim.x;
-    const size_t per = fag_block_bytes(P.N, P.F, S) - (((size_t)P.N * 7 + 15) & ~(size_t)15);
+    const size_t per = fag_block_bytes(P.N, P.F, S, fast) - (((size_t)P.N * 7 + 15) & ~(size_t)15);
     int16_t* s_order = (int16_t*)(smem + per);
     int16_t* s_mo = s_order + P.N;
     int16_t* s_fa = s_mo + P.N;
@@ -702,7 +749,7 @@ __global__ void __launch_bounds__(128) fag_kernel(ProblemDev P, uint32_t* dg, in
         s_typed[i] = P.typed[i];
     }
     __syncthreads();
-    Fag<IX> fs = fag_bind<IX>(smem, P.N, P.F, S, threadIdx.x);
+    Fag<IX, T> fs = fag_bind<IX, T>(smem, P.N, P.F, S, threadIdx.x);
     const int64_t ntask = (int64_t)nchain * P.M;
     const int64_t t = (int64_t)blockIdx.x * S + threadIdx.x;
     if (t >= ntask) return;
@@ -712,13 +759,13 @@ __global__ void __launch_bounds__(128) fag_kernel(ProblemDev P, uint32_t* dg, in
     const int chain = first + cr;
     const uint32_t* col = dg + ((size_t)chain * P.M + l) * P.W;
     const int32_t* ord = order + cr * ostride;
-    double* raw = raw64 + (size_t)cr * 2 * P.M;
+    T* raw = rawbuf + (size_t)cr * 2 * P.M;
     const uint8_t* gcol = P.geno + (size_t)l * P.N;
     if (step < 0) {
         fag_edges(P.N, P.F, s_order, s_mo, s_fa, col, fs, -1);
-        const double lk = fag_like(P.N, P.F, s_typed, gcol, P.minor[l], fs);
+        const T lk = fag_like<PP>(P.N, P.F, s_typed, gcol, P.minor[l], fs);
         raw[2 * l + dgbit(col, ord[0])] = lk;
-        if (lk == 0.0) {
+        if (PP::is_zero(lk)) {
             badc[cr] = 1;
             set_status(status, ST_ILLEGAL_DG);
         }
@@ -727,16 +774,21 @@ __global__ void __launch_bounds__(128) fag_kernel(ProblemDev P, uint32_t* dg, in
     const int m = ord[step];
     const int last = ord[step > 0 ? step - 1 : 0];
     const int tb = dgbit(col, m), t2 = dgbit(col, last);
-    const double keep = raw[2 * l + t2];
+    const T keep = raw[2 * l + t2];
     fag_edges(P.N, P.F, s_order, s_mo, s_fa, col, fs, m);
-    const double lk = fag_like(P.N, P.F, s_typed, gcol, P.minor[l], fs);
+    const T lk = fag_like<PP>(P.N, P.F, s_typed, gcol, P.minor[l], fs);
     raw[2 * l + tb] = keep;
     raw[2 * l + 1 - tb] = lk;
     if (raw32) {
         float* r32 = raw32 + (size_t)cr * 2 * P.M;
-        if (tb == 0) put_raw32(r32, l, keep, lk); else put_raw32(r32, l, lk, keep);
+        if (sizeof(T) == 8) {
+            if (tb == 0) put_raw32(r32, l, (double)keep, (double)lk); else put_raw32(r32, l, (double)lk, (double)keep);
+        } else {
+            if (tb == 0) put_raw32_log2(r32, l, (float)keep, (float)lk);
+            else put_raw32_log2(r32, l, (float)lk, (float)keep);
+        }
     }
-    if (keep == 0.0 && lk == 0.0) {
+    if (PP::is_zero(keep) && PP::is_zero(lk)) {
         badc[cr] = 1;
         set_status(status, ST_ILLEGAL_DG);
     }
@@ -881,7 +933,8 @@ __global__ void __launch_bounds__(32) ffbs_scan_kernel(ProblemDev P, uint32_t* d
                                                        const int32_t* order, int64_t ostride, int step,
                                                        Draws draws, const uint8_t* sel, int want,
                                                        const uint8_t* badc, const float* raw32, float* fbbuf,
-                                                       uint8_t* mapbuf) {
+                                                       uint8_t* mapbuf, int staged) {
+    extern __shared__ __align__(16) unsigned char fsm[];
     const int cr = blockIdx.x;
     if (cr >= nchain) return;
     if (sel && sel[cr] != want) return;
@@ -894,13 +947,29 @@ __global__ void __launch_bounds__(32) ffbs_scan_kernel(ProblemDev P, uint32_t* d
     const float* r = raw32 + (size_t)cr * 2 * M;
     float* fb = fbbuf + (size_t)cr * 2 * M;
     uint8_t* maps = mapbuf + (size_t)cr * M;
+    float* th = nullptr;  // theta as floats, [M]
+    if (staged) {
+        // stage the chain's pairs and the map in shared memory with coalesced loads:
+        // [r: 2M floats][fb: 2M floats][theta: M floats][maps: M bytes]
+        float* sr = (float*)fsm;
+        float* sfb = sr + 2 * M;
+        th = sfb + 2 * M;
+        uint8_t* smaps = (uint8_t*)(th + M);
+        for (int i = lane; i < 2 * M; i += 32) sr[i] = r[i];
+        for (int i = lane; i < M; i += 32) th[i] = i > 0 ? (float)P.theta[i - 1] : 0.f;
+        __syncwarp();
+        r = sr;
+        fb = sfb;
+        maps = smaps;
+    }
+    auto tof = [&](int i) { return th ? th[i] : (i > 0 ? (float)P.theta[i - 1] : 0.f); };
     const int L = (M + 31) / 32;
     const int s0 = min(M, lane * L), s1 = min(M, s0 + L);
     // chunk product P = A_{s1-1} ... A_{s0}, A_i = diag(r_i) [[1-t, t], [t, 1-t]] (A_0 = diag(r_0))
     float p00 = 1.f, p01 = 0.f, p10 = 0.f, p11 = 1.f;
     for (int i = s0; i < s1; ++i) {
         const float q0 = r[2 * i], q1 = r[2 * i + 1];
-        const float t = i > 0 ? (float)P.theta[i - 1] : 0.f, a = 1.f - t;
+        const float t = tof(i), a = 1.f - t;
         const float n00 = q0 * (a * p00 + t * p10), n01 = q0 * (a * p01 + t * p11);
         const float n10 = q1 * (t * p00 + a * p10), n11 = q1 * (t * p01 + a * p11);
         p00 = n00; p01 = n01; p10 = n10; p11 = n11;
@@ -922,9 +991,10 @@ __global__ void __launch_bounds__(32) ffbs_scan_kernel(ProblemDev P, uint32_t* d
     const float e10 = __shfl_up_sync(FULLMASK, p10, 1), e11 = __shfl_up_sync(FULLMASK, p11, 1);
     float v0 = 1.f, v1 = 1.f;
     if (lane > 0) { v0 = e00 + e01; v1 = e10 + e11; }
+    int cnt = 0;
     for (int i = s0; i < s1; ++i) {
         const float q0 = r[2 * i], q1 = r[2 * i + 1];
-        const float t = i > 0 ? (float)P.theta[i - 1] : 0.f, a = 1.f - t;
+        const float t = tof(i), a = 1.f - t;
         float f0 = q0 * (a * v0 + t * v1), f1 = q1 * (t * v0 + a * v1);
         const float tot = f0 + f1;
         if (tot > 0.f) { const float inv = 1.f / tot; f0 *= inv; f1 *= inv; }
@@ -933,12 +1003,11 @@ __global__ void __launch_bounds__(32) ffbs_scan_kernel(ProblemDev P, uint32_t* d
         if (q1 == 0.f) f1 = 0.f;
         fb[2 * i] = f0;
         fb[2 * i + 1] = f1;
+        cnt += (f0 != 0.f && f1 != 0.f);
         v0 = f0;
         v1 = f1;
     }
     // draws: loci are visited from M-1 down; a locus draws when both entries are non-zero
-    int cnt = 0;
-    for (int i = s0; i < s1; ++i) cnt += (fb[2 * i] != 0.f && fb[2 * i + 1] != 0.f);
     int above = 0;  // draws consumed by loci in higher chunks
     {
         int x = cnt;
@@ -962,7 +1031,7 @@ __global__ void __launch_bounds__(32) ffbs_scan_kernel(ProblemDev P, uint32_t* d
                 const int v = (u < (double)(f0 / (f0 + f1))) ? 0 : 1;
                 dmap = v | (v << 1);
             } else {
-                const float t = (float)P.theta[i], a = 1.f - t;
+                const float t = tof(i + 1), a = 1.f - t;
                 const float x0 = f0 * a, y0 = f1 * t;   // next = 0
                 const float x1 = f0 * t, y1 = f1 * a;   // next = 1
                 const int d0 = (u < (double)(x0 / (x0 + y0))) ? 0 : 1;
@@ -988,6 +1057,8 @@ __global__ void __launch_bounds__(32) ffbs_scan_kernel(ProblemDev P, uint32_t* d
         if (sv != cur) *wp ^= (1u << (m & 31));
     }
 }
+
+size_t ffbs_scan_smem(int M) { return (size_t)5 * 4 * M + (size_t)M + 16; }
 
 // ---------------------------------------------------------------------------
 // Trait peel LOD scorer: one warp per (graph, interval, position).
@@ -1335,35 +1406,44 @@ cudaError_t launch_lsampler(const ProblemDev& P, uint32_t* dg, int first, int nc
     return cudaGetLastError();
 }
 
-template <typename IX>
+template <typename IX, typename PP>
 static cudaError_t launch_msampler_t(const ProblemDev& P, uint32_t* dg, int first, int nchain, const int32_t* meioses,
                                      int64_t mstride, int nm, const double* u, int64_t ucs, uint64_t seed,
-                                     uint64_t iter, const uint8_t* sel, int want, double* raw64, float* raw32, void* fb,
-                                     uint8_t* badc, uint8_t* maps, int* status, int fag_threads, int exact,
+                                     uint64_t iter, const uint8_t* sel, int want, typename PP::T* raw, float* raw32,
+                                     void* fb, uint8_t* badc, uint8_t* maps, int* status, int fag_threads, int exact,
                                      cudaStream_t s) {
-    const size_t smem = fag_block_bytes(P.N, P.F, fag_threads);
+    const int fast = exact ? 0 : 1;
+    const size_t smem = fag_block_bytes(P.N, P.F, fag_threads, fast);
     static size_t configured = 0;
     if (smem > configured) {
-        cudaError_t e = cudaFuncSetAttribute(fag_kernel<IX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaError_t e = cudaFuncSetAttribute(fag_kernel<IX, PP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         configured = smem;
     }
     Draws d{u, ucs, P.M, seed, iter, 2};
+    size_t scan_smem = ffbs_scan_smem(P.M);
+    if (scan_smem > 200 * 1024) scan_smem = 0;  // long maps: read the chain's arrays from global memory
+    static size_t scan_configured = 0;
+    if (scan_smem > scan_configured) {
+        cudaError_t e = cudaFuncSetAttribute(ffbs_scan_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)scan_smem);
+        if (e != cudaSuccess) return e;
+        scan_configured = scan_smem;
+    }
     cudaError_t e0 = cudaMemsetAsync(badc, 0, (size_t)nchain, s);
     if (e0 != cudaSuccess) return e0;
     const int64_t ntask = (int64_t)nchain * P.M;
     const int grid = (int)((ntask + fag_threads - 1) / fag_threads);
-    fag_kernel<IX><<<grid, fag_threads, smem, s>>>(P, dg, first, nchain, meioses, mstride, -1, sel, want, raw64,
-                                                   nullptr, badc, status);
+    fag_kernel<IX, PP><<<grid, fag_threads, smem, s>>>(P, dg, first, nchain, meioses, mstride, -1, sel, want, raw,
+                                                       nullptr, badc, status, fast);
     for (int j = 0; j < nm; ++j) {
-        fag_kernel<IX><<<grid, fag_threads, smem, s>>>(P, dg, first, nchain, meioses, mstride, j, sel, want, raw64,
-                                                       exact ? nullptr : raw32, badc, status);
+        fag_kernel<IX, PP><<<grid, fag_threads, smem, s>>>(P, dg, first, nchain, meioses, mstride, j, sel, want, raw,
+                                                           exact ? nullptr : raw32, badc, status, fast);
         if (exact)
             ffbs_kernel<double><<<nchain, 32, 0, s>>>(P, dg, first, nchain, meioses, mstride, j, d, sel, want, badc,
-                                                      raw64, nullptr, (double*)fb);
+                                                      (const double*)raw, nullptr, (double*)fb);
         else
-            ffbs_scan_kernel<<<nchain, 32, 0, s>>>(P, dg, first, nchain, meioses, mstride, j, d, sel, want, badc,
-                                                   raw32, (float*)fb, maps);
+            ffbs_scan_kernel<<<nchain, 32, scan_smem, s>>>(P, dg, first, nchain, meioses, mstride, j, d, sel, want,
+                                                           badc, raw32, (float*)fb, maps, scan_smem > 0);
     }
     return cudaGetLastError();
 }
@@ -1372,14 +1452,26 @@ cudaError_t launch_msampler(const ProblemDev& P, uint32_t* dg, int first, int nc
                             int64_t mstride, int nm, const double* u, int64_t ucs, uint64_t seed, uint64_t iter,
                             const uint8_t* sel, int want, double* raw64, float* raw32, void* fb, uint8_t* badc,
                             uint8_t* maps, int* status, int fag_threads, int exact, cudaStream_t s) {
-    if (2 * P.F <= 255)
-        return launch_msampler_t<uint8_t>(P, dg, first, nchain, meioses, mstride, nm, u, ucs, seed, iter, sel, want,
-                                          raw64, raw32, fb, badc, maps, status, fag_threads, exact, s);
-    return launch_msampler_t<uint16_t>(P, dg, first, nchain, meioses, mstride, nm, u, ucs, seed, iter, sel, want,
-                                       raw64, raw32, fb, badc, maps, status, fag_threads, exact, s);
+    // the fast mode keeps log2 likelihoods as floats in the first half of the raw buffer
+    float* rawl = (float*)raw64;
+    if (2 * P.F <= 255) {
+        if (exact)
+            return launch_msampler_t<uint8_t, ProbExact>(P, dg, first, nchain, meioses, mstride, nm, u, ucs, seed,
+                                                         iter, sel, want, raw64, raw32, fb, badc, maps, status,
+                                                         fag_threads, exact, s);
+        return launch_msampler_t<uint8_t, ProbLog2>(P, dg, first, nchain, meioses, mstride, nm, u, ucs, seed, iter,
+                                                    sel, want, rawl, raw32, fb, badc, maps, status, fag_threads,
+                                                    exact, s);
+    }
+    if (exact)
+        return launch_msampler_t<uint16_t, ProbExact>(P, dg, first, nchain, meioses, mstride, nm, u, ucs, seed, iter,
+                                                      sel, want, raw64, raw32, fb, badc, maps, status, fag_threads,
+                                                      exact, s);
+    return launch_msampler_t<uint16_t, ProbLog2>(P, dg, first, nchain, meioses, mstride, nm, u, ucs, seed, iter, sel,
+                                                 want, rawl, raw32, fb, badc, maps, status, fag_threads, exact, s);
 }
 
-size_t fag_smem(int N, int F, int threads) { return fag_block_bytes(N, F, threads); }
+size_t fag_smem(int N, int F, int threads, int fast) { return fag_block_bytes(N, F, threads, fast); }
 
 cudaError_t launch_lod(const ProblemDev& P, int precision, const uint32_t* graphs, int64_t graph_words, int G,
                        double* vals, int* status, cudaStream_t s, int grid_cap, int wpb) {
