@@ -90,6 +90,11 @@ typedef struct sl_problem_desc {
     const int32_t* prev;        /* previous rfunctions feeding each op */
     const int32_t* children_off;/* [K+1] */
     const int32_t* children;    /* children of a parent peel, cutset order */
+    /* disease model, needed only by the trait-peel adjoint (affection NULL = absent):
+       Person::disease_prob follows from these (person.cc:85-119, disease_model.cc:139-187) */
+    const int32_t* affection;   /* [N] 0 unknown, 1 unaffected, 2 affected (types.h:28-32) */
+    double disease_freq;        /* disease-allele frequency */
+    double penetrance[3];       /* penetrance of the HOMO_U, HETERO, HOMO_A traits (trait.h:13-17) */
 } sl_problem_desc;
 
 typedef struct sl_options {
@@ -265,6 +270,29 @@ int sl_problem_lod_program_eval(const sl_problem_desc* problem, const int32_t* d
 #define SL_NOALLOC_SCRATCH_BYTES (8u << 20)
 int sl_lod_score_device_graphs_noalloc(sl_ctx* ctx, int32_t n_graphs, const uint32_t* d_graphs,
                                        double* d_logsum);
+
+/*
+ * Adjoint of the trait peel (the reverse sum-product of TraitRfunction's
+ * peel, trait_rfunction.cc:28-137; no counterpart kernel in the reference).
+ * For each of n_graphs descent graphs (int32 reference layout) and each LOD
+ * position (interval l, position o), grad[((g*(M-1) + l)*n + o)*6 + k] is the
+ * derivative of log L, L the trait-peel likelihood at that position
+ * (peeler.cc:79-91), with respect to
+ *   k = 0, 1: theta_L and theta_R of the position (trait_rfunction.h:50-56);
+ *   k = 2, 3, 4: the penetrances of HOMO_U, HETERO, HOMO_A;
+ *   k = 5: the disease-allele frequency.
+ * ptrait_grad[4] (may be NULL) receives d log P(T) / d (penetrances, frequency)
+ * (Peeler::calc_trait_prob, peeler.cc:65-73).  Needs the disease-model fields
+ * of the problem.  The peel is recomputed on the device in FP32 with
+ * power-of-two rescaling; every forward value is kept for the reverse pass.
+ */
+int sl_trait_backward(sl_ctx* ctx, int32_t n_graphs, const int32_t* dgs, double* grad, double* ptrait_grad);
+
+/* The same adjoint for one graph and position evaluated on the host in FP64
+ * (the reference gradient the device result is checked against); dg NULL
+ * gives the gradient of log P(T) in grad[2..5]. */
+int sl_problem_trait_backward_eval(const sl_problem_desc* problem, const int32_t* dg, int32_t locus,
+                                   int32_t offset, double* grad);
 
 /* Library version string. */
 const char* sl_version(void);

@@ -26,7 +26,8 @@ EXPORTED = [
     "sl_msampler_sweep", "sl_lod_score_chains", "sl_lod_score_graphs", "sl_lod_results",
     "sl_lod_reset", "sl_run", "sl_synchronize", "sl_device_status", "sl_launch_count",
     "sl_version", "sl_get_stream", "sl_profile", "sl_profile_read", "sl_problem_legal_masks",
-    "sl_problem_trait_priors", "sl_problem_trait_prob",
+    "sl_problem_trait_priors", "sl_problem_trait_prob", "sl_trait_backward",
+    "sl_problem_trait_backward_eval",
 ]
 
 
@@ -48,6 +49,7 @@ class ProblemDesc(ctypes.Structure):
         ("minor_freq", _vp), ("n_ops", ctypes.c_int32), ("op_type", _vp), ("op_peelnode", _vp),
         ("cutset_off", _vp), ("cutset", _vp), ("prev_off", _vp), ("prev", _vp),
         ("children_off", _vp), ("children", _vp),
+        ("affection", _vp), ("disease_freq", ctypes.c_double), ("penetrance", ctypes.c_double * 3),
     ]
 
 
@@ -119,6 +121,9 @@ class Problem:
     op_prev: list
     op_children: list
     legal: Optional[np.ndarray] = None
+    affection: Optional[np.ndarray] = None   # [N] 0 unknown, 1 unaffected, 2 affected
+    freq: float = 0.0                        # disease-allele frequency
+    penetrance: tuple = (0.0, 0.0, 0.0)      # HOMO_U, HETERO, HOMO_A
     keep: dict = field(default_factory=dict)
 
     @property
@@ -133,7 +138,9 @@ class Problem:
                    partial=d["partial"], minor=d["minor"], op_type=d["op_type"],
                    op_peel=d["op_peel"], op_cutset=list(d["op_cutset"]), op_prev=list(d["op_prev"]),
                    op_children=list(d["op_children"]),
-                   legal=d.get("legal") if with_legal else None)
+                   legal=d.get("legal") if with_legal else None,
+                   affection=d.get("affection"), freq=float(d.get("freq", 0.0)),
+                   penetrance=tuple(float(x) for x in d.get("penetrance", (0.0, 0.0, 0.0))))
 
     def desc(self) -> ProblemDesc:
         k = self.keep
@@ -161,6 +168,11 @@ class Problem:
         s.cutset_off, s.cutset = _p(k["cutset_off"]), _p(k["cutset"])
         s.prev_off, s.prev = _p(k["prev_off"]), _p(k["prev"])
         s.children_off, s.children = _p(k["children_off"]), _p(k["children"])
+        if self.affection is not None:
+            s.affection = _p(g("affection", self.affection, np.int32))
+            s.disease_freq = self.freq
+            for i in range(3):
+                s.penetrance[i] = self.penetrance[i]
         return s
 
 
@@ -266,6 +278,20 @@ class Context:
 
     def lod_reset(self):
         self._check(lib().sl_lod_reset(self.h))
+
+    def trait_backward(self, dgs: Optional[np.ndarray] = None):
+        """d log L / d (theta_L, theta_R, pen x3, frequency) at every LOD
+        position of every graph: [G][M-1][n][6], and d log P(T) / d (pen x3,
+        frequency): [4]."""
+        n = self.problem.n_lod
+        pt = np.zeros(4)
+        if dgs is None:
+            self._check(lib().sl_trait_backward(self.h, 0, None, None, _p(pt)))
+            return None, pt
+        dgs = np.ascontiguousarray(dgs, np.int32).reshape(-1, self.M, self.N, 2)
+        grad = np.zeros((dgs.shape[0], self.M - 1, n, 6))
+        self._check(lib().sl_trait_backward(self.h, dgs.shape[0], _p(dgs), _p(grad), _p(pt)))
+        return grad, pt
 
     def run(self, iterations: int, burnin: int = 0, period: int = 10, lprob: float = 0.5,
             seed: int = 1, first_iteration: int = 0):

@@ -31,6 +31,9 @@ size_t fag_smem(int N, int F, int threads, int fast);
 cudaError_t launch_lod(const ProblemDev& P, int precision, const uint32_t* graphs, int64_t graph_words, int G,
                        double* vals, int* status, cudaStream_t s, int grid_cap, int wpb);
 cudaError_t launch_lod_merge(const double* vals, int G, int64_t npos, double* acc, uint8_t* init, cudaStream_t s);
+cudaError_t launch_trait_adjoint(const ProblemDev& P, const AdjDev& D, const uint32_t* graphs, int64_t graph_words,
+                                 int64_t task0, int64_t ntask, int64_t stride, float* A, float* B, int* E,
+                                 double* grad, int* status, cudaStream_t s);
 cudaError_t launch_shuffle(const int32_t* base, int nm, int32_t* out, int first, int nchain, uint64_t seed,
                            uint64_t iter, cudaStream_t s);
 cudaError_t launch_choose(int first, int nchain, uint64_t seed, uint64_t iter, double lprob, uint8_t* is_l,
@@ -91,6 +94,14 @@ struct sl_ctx {
     uint8_t* d_sel = nullptr;
     uint32_t* h_stage = nullptr;     // pinned staging for packed descent graphs
     size_t h_stage_words = 0;
+    // trait-peel adjoint (present when the problem carries the disease model)
+    bool has_adjoint = false;
+    AdjDev adj{};
+    float* d_adjA = nullptr;         // [slots][chunk] forward values
+    float* d_adjB = nullptr;         // [slots][chunk] adjoints
+    int* d_adjE = nullptr;           // [nscale][chunk] rescaling exponents
+    double* d_adjG = nullptr;        // [chunk][6] gradients
+    int64_t adj_chunk = 0;
     std::string err;
     // per-kernel event timing
     bool profiling = false;
@@ -492,6 +503,7 @@ namespace {
 struct SlotAlloc {
     std::vector<char> used;
     int high = 0;
+    bool keep = false;   // never reuse a slot (every forward value stays for an adjoint)
     int alloc(int n) {
         if (n <= 0) return 0;
         int run = 0;
@@ -509,6 +521,7 @@ struct SlotAlloc {
         return first;
     }
     void release(int first, int n) {
+        if (keep) return;
         for (int j = first; j < first + n; ++j) used[j] = 0;
     }
 };
@@ -525,19 +538,29 @@ struct LodProgram {
     std::vector<int32_t> words;
     std::vector<float> consts;
     std::vector<double> consts64;   // the same constants unrounded, for host evaluation
+    std::vector<int> cperson, cstate;  // the disease probability each constant is
+    std::vector<int> starts;        // word offset of every instruction
     int slots = 0;
+    int nscale = 0;                 // LI_SCALE instructions
 };
 
+// full = true compiles the peel without dropping zero-probability cells or
+// terms and without reusing slots: the form the adjoint needs (a zero
+// disease probability still has a derivative with respect to the model).
 static void compile_lod_program(const sl_problem_desc* d, const std::vector<OpDev>& ops, const std::vector<int32_t>& od,
-                                LodProgram& out) {
+                                LodProgram& out, bool full = false) {
     const int K = (int)ops.size();
     SlotAlloc sa;
+    sa.keep = full;
     std::vector<std::vector<int>> slot_of(K);   // cell -> slot, -1 when not LOD-valid
     std::vector<int> first(K, 0), count(K, 0);
     auto dig = [](int ext, int pos) { return (ext >> (2 * pos)) & 3; };
-    auto cnst = [&](double v) {
+    auto cnst_ps = [&](int person, int state) {
+        const double v = d->disease_prob[4 * person + state];
         out.consts.push_back((float)v);
         out.consts64.push_back(v);
+        out.cperson.push_back(person);
+        out.cstate.push_back(state);
         return (int)out.consts.size() - 1;
     };
     auto& W = out.words;
@@ -549,8 +572,9 @@ static void compile_lod_program(const sl_problem_desc* d, const std::vector<OpDe
         std::vector<int> valid;
         for (int cell = 0; cell < ncell; ++cell) {
             bool ok = true;
-            for (int q = 0; q < op.c; ++q)
-                if (d->disease_prob[4 * cut[q] + dig(cell, q)] == 0.0) ok = false;
+            if (!full)
+                for (int q = 0; q < op.c; ++q)
+                    if (d->disease_prob[4 * cut[q] + dig(cell, q)] == 0.0) ok = false;
             if (ok) valid.push_back(cell);
         }
         // recombination terms of the children this op transmits to
@@ -587,16 +611,16 @@ static void compile_lod_program(const sl_problem_desc* d, const std::vector<OpDe
                 for (int i = 0; i < 2; ++i)
                     for (int j = 0; j < 2; ++j) {
                         const int kt = phased_trait_host(mt, pt, i, j);
-                        if (trait[kt] == 0.0) continue;
+                        if (trait[kt] == 0.0 && !full) continue;
                         Term t;
                         if (!gather(cell | (kt << (2 * op.c)), t.f)) continue;
                         t.f.push_back(rec_slot[0] + 2 * i + j);
-                        t.ci = cnst(trait[kt]);
+                        t.ci = cnst_ps(op.peel, kt);
                         terms[vi].push_back(t);
                     }
             } else if (op.type == PARENT) {
                 for (int a = 0; a < 4; ++a) {
-                    if (trait[a] == 0.0) continue;
+                    if (trait[a] == 0.0 && !full) continue;
                     const int ext = cell | (a << (2 * op.c));
                     Term t;
                     if (!gather(ext, t.f)) continue;
@@ -627,15 +651,15 @@ static void compile_lod_program(const sl_problem_desc* d, const std::vector<OpDe
                         }
                     }
                     if (zero) continue;
-                    t.ci = cnst(trait[a]);
+                    t.ci = cnst_ps(op.peel, a);
                     terms[vi].push_back(t);
                 }
             } else {
                 for (int a = 0; a < 4; ++a) {
-                    if (trait[a] == 0.0) continue;
+                    if (trait[a] == 0.0 && !full) continue;
                     Term t;
                     if (!gather(cell | (a << (2 * op.c)), t.f)) continue;
-                    t.ci = cnst(trait[a]);
+                    t.ci = cnst_ps(op.peel, a);
                     terms[vi].push_back(t);
                 }
             }
@@ -647,12 +671,14 @@ static void compile_lod_program(const sl_problem_desc* d, const std::vector<OpDe
         for (size_t vi = 0; vi < valid.size(); ++vi) slot_of[k][valid[vi]] = first[k] + (int)vi;
         // emit
         for (size_t c = 0; c < kids.size(); ++c) {
+            out.starts.push_back((int)W.size());
             W.push_back(LI_REC);
             W.push_back(kids[c]);
             W.push_back(rec_slot[c]);
         }
         for (auto& key : sum_order) {
             const int c = key.first, mask = key.second;
+            out.starts.push_back((int)W.size());
             W.push_back(LI_SUM);
             W.push_back(sum_slot[key]);
             W.push_back(__builtin_popcount(mask));
@@ -660,6 +686,7 @@ static void compile_lod_program(const sl_problem_desc* d, const std::vector<OpDe
                 if (mask & (1 << b)) W.push_back(rec_slot[c] + b);
         }
         for (size_t vi = 0; vi < valid.size(); ++vi) {
+            out.starts.push_back((int)W.size());
             W.push_back(LI_CELL);
             W.push_back(first[k] + (int)vi);
             W.push_back((int)terms[vi].size());
@@ -670,6 +697,8 @@ static void compile_lod_program(const sl_problem_desc* d, const std::vector<OpDe
             }
         }
         if (count[k] > 0) {
+            out.starts.push_back((int)W.size());
+            out.nscale++;
             W.push_back(LI_SCALE);
             W.push_back(first[k]);
             W.push_back(count[k]);
@@ -684,9 +713,154 @@ static void compile_lod_program(const sl_problem_desc* d, const std::vector<OpDe
             pd += 2 + pd[1];
         }
     }
+    out.starts.push_back((int)W.size());
     W.push_back(LI_END);
     W.push_back(count[K - 1] > 0 ? first[K - 1] : -1);
     out.slots = std::max(1, sa.high);
+}
+
+// Derivatives of Person::disease_prob[person][state] with respect to the
+// penetrances of HOMO_U, HETERO, HOMO_A and the disease-allele frequency
+// (person.cc:85-119; DiseaseModel::get_apriori_prob2 / get_penetrance_prob2,
+// disease_model.cc:139-187; autosomal).
+static void disease_prob_grad(const sl_problem_desc* d, int person, int state, double* g4) {
+    static const int unph[4] = {0, 2, 1, 1};   // UU, AA, AU, UA -> HOMO_U, HOMO_A, HETERO
+    const int t = unph[state];
+    const double q = d->disease_freq, pen = d->penetrance[t];
+    const int a = d->affection[person];
+    g4[0] = g4[1] = g4[2] = g4[3] = 0.0;
+    if (d->mother[person] < 0) {
+        const double prior[3] = {(1.0 - q) * (1.0 - q), q * (1.0 - q), q * q};
+        const double dprior[3] = {-2.0 * (1.0 - q), 1.0 - 2.0 * q, 2.0 * q};
+        if (a == 2) { g4[t] = prior[t]; g4[3] = dprior[t] * pen; }
+        else if (a == 1) { g4[t] = -prior[t]; g4[3] = dprior[t] * (1.0 - pen); }
+        else { g4[3] = dprior[t]; }
+    } else {
+        if (a == 2) g4[t] = 1.0;
+        else if (a == 1) g4[t] = -1.0;
+    }
+}
+
+// Forward and reverse evaluation of a full program in FP64, with each op's
+// cells scaled by a power of two (the same scaling the device uses), for one
+// graph / interval / position, or for the peel without a graph (dg NULL,
+// every recombination term 0.25).  grad: [theta_L, theta_R, pen x3, freq].
+static int host_backward(const sl_problem_desc* d, const LodProgram& prog, const int32_t* dg, int locus, int offset,
+                         double* grad, double* loglik) {
+    const int N = d->n_members, n = d->lod_per_interval;
+    double th = 0, an = 0, th2 = 0, an2 = 0;
+    if (dg) {
+        th = d->partial_theta[locus] * (offset + 1);
+        an = 1.0 - th;
+        th2 = d->partial_theta[locus] * (n - offset);
+        an2 = 1.0 - th2;
+    }
+    auto bit = [&](int person, int l, int par) { return dg[(size_t)2 * N * l + 2 * person + par] & 1; };
+    std::vector<double> A(prog.slots, 0.0), B(prog.slots, 0.0);
+    std::vector<int> exps;
+    const int32_t* W = prog.words.data();
+    int scale = 0, res = -1;
+    for (int s : prog.starts) {
+        const int32_t* pc = W + s;
+        const int op = pc[0];
+        if (op == LI_CELL) {
+            const int dst = pc[1], nt = pc[2];
+            pc += 3;
+            double total = 0.0;
+            for (int q = 0; q < nt; ++q) {
+                const int nf = pc[0];
+                double v = prog.consts64[pc[1]];
+                pc += 2;
+                for (int f = 0; f < nf; ++f) v *= A[pc[f]];
+                pc += nf;
+                total += v;
+            }
+            A[dst] = total;
+        } else if (op == LI_REC) {
+            const int c = pc[1], dst = pc[2];
+            for (int i = 0; i < 2; ++i)
+                for (int j = 0; j < 2; ++j) {
+                    double r = 1.0;
+                    if (dg) {
+                        r = (bit(c, locus, 0) == i) ? an : th;
+                        r *= (bit(c, locus + 1, 0) == i) ? an2 : th2;
+                        r *= (bit(c, locus, 1) == j) ? an : th;
+                        r *= (bit(c, locus + 1, 1) == j) ? an2 : th2;
+                    }
+                    A[dst + 2 * i + j] = 0.25 * r;
+                }
+        } else if (op == LI_SUM) {
+            double v = 0.0;
+            for (int q = 0; q < pc[2]; ++q) v += A[pc[3 + q]];
+            A[pc[1]] = v;
+        } else if (op == LI_SCALE) {
+            double mx = 0.0;
+            for (int q = 0; q < pc[2]; ++q) mx = std::max(mx, A[pc[1] + q]);
+            int e = 0;
+            if (mx > 0.0) {
+                e = std::ilogb(mx);
+                const double f = std::ldexp(1.0, -e);
+                for (int q = 0; q < pc[2]; ++q) A[pc[1] + q] *= f;
+            }
+            exps.push_back(e);
+            scale += e;
+        } else {
+            res = pc[1];
+        }
+    }
+    if (res < 0 || !(A[res] > 0.0)) return fail(nullptr, SL_EZERO, "trait peel gave a likelihood of 0.0 or less");
+    if (loglik) *loglik = std::log(A[res]) + scale * std::log(2.0);
+    for (int k = 0; k < 6; ++k) grad[k] = 0.0;
+    B[res] = 1.0 / A[res];
+    int si = (int)exps.size();
+    for (int ii = (int)prog.starts.size() - 1; ii >= 0; --ii) {
+        const int32_t* pc = W + prog.starts[ii];
+        const int op = pc[0];
+        if (op == LI_SCALE) {
+            const double f = std::ldexp(1.0, -exps[--si]);
+            for (int q = 0; q < pc[2]; ++q) B[pc[1] + q] *= f;
+        } else if (op == LI_CELL) {
+            const int dst = pc[1], nt = pc[2];
+            const double g = B[dst];
+            pc += 3;
+            for (int q = 0; q < nt; ++q) {
+                const int nf = pc[0], ci = pc[1];
+                const int32_t* fs = pc + 2;
+                double prod = 1.0;
+                for (int f = 0; f < nf; ++f) prod *= A[fs[f]];
+                if (g != 0.0) {
+                    double g4[4];
+                    if (d->affection) {
+                        disease_prob_grad(d, prog.cperson[ci], prog.cstate[ci], g4);
+                        for (int k = 0; k < 4; ++k) grad[2 + k] += g * prod * g4[k];
+                    }
+                    const double c = prog.consts64[ci];
+                    for (int f = 0; f < nf; ++f) {
+                        double others = c;
+                        for (int f2 = 0; f2 < nf; ++f2)
+                            if (f2 != f) others *= A[fs[f2]];
+                        B[fs[f]] += g * others;
+                    }
+                }
+                pc += 2 + nf;
+            }
+        } else if (op == LI_SUM) {
+            for (int q = 0; q < pc[2]; ++q) B[pc[3 + q]] += B[pc[1]];
+        } else if (op == LI_REC && dg) {
+            const int c = pc[1], dst = pc[2];
+            for (int i = 0; i < 2; ++i)
+                for (int j = 0; j < 2; ++j) {
+                    const double gb = B[dst + 2 * i + j];
+                    const bool ml = bit(c, locus, 0) == i, mr = bit(c, locus + 1, 0) == i;
+                    const bool pl = bit(c, locus, 1) == j, pr = bit(c, locus + 1, 1) == j;
+                    const double a = ml ? an : th, b = mr ? an2 : th2, cc = pl ? an : th, dd = pr ? an2 : th2;
+                    const double da = ml ? -1.0 : 1.0, db = mr ? -1.0 : 1.0, dc = pl ? -1.0 : 1.0, ddd = pr ? -1.0 : 1.0;
+                    grad[0] += gb * 0.25 * (da * b * cc * dd + a * b * dc * dd);
+                    grad[1] += gb * 0.25 * (a * db * cc * dd + a * b * cc * ddd);
+                }
+        }
+    }
+    return SL_OK;
 }
 
 // ---------------------------------------------------------------------------
@@ -913,6 +1087,26 @@ int sl_create(const sl_problem_desc* d, const sl_options* opt, sl_ctx** out) {
             P.prog_slots = prog.slots;
             P.prog_threads = S;
         }
+    }
+    if (d->affection) {
+        LodProgram full;
+        compile_lod_program(d, ops, od, full, true);
+        std::vector<float> dc(4 * std::max<size_t>(1, full.consts.size()), 0.f);
+        for (size_t i = 0; i < full.consts.size(); ++i) {
+            double g4[4];
+            disease_prob_grad(d, full.cperson[i], full.cstate[i], g4);
+            for (int k = 0; k < 4; ++k) dc[4 * i + k] = (float)g4[k];
+        }
+        AdjDev& D = ctx->adj;
+        if ((rc = upload(ctx, (int32_t**)&D.prog, full.words.data(), full.words.size()))) return bail(rc);
+        if ((rc = upload(ctx, (int32_t**)&D.starts, full.starts.data(), full.starts.size()))) return bail(rc);
+        if ((rc = upload(ctx, (float**)&D.pconst, full.consts.data(), std::max<size_t>(1, full.consts.size()))))
+            return bail(rc);
+        if ((rc = upload(ctx, (float**)&D.dconst, dc.data(), dc.size()))) return bail(rc);
+        D.n_instr = (int32_t)full.starts.size();
+        D.slots = full.slots;
+        D.nscale = full.nscale;
+        ctx->has_adjoint = true;
     }
     *out = ctx;
     return SL_OK;
@@ -1336,6 +1530,100 @@ int sl_problem_lod_program_eval(const sl_problem_desc* d, const int32_t* dg, int
     const double rec = cross * std::log(d->theta[locus]) + (2 * (N - F) - cross) * std::log(1.0 - d->theta[locus]);
     *out = std::log(result) - rec - std::log(0.5) * (2 * (N - F));
     return SL_OK;
+}
+
+// Scratch of the adjoint: per task 2 x slots floats and nscale exponents,
+// processed in chunks of at most kAdjScratchBytes.
+static constexpr size_t kAdjScratchBytes = size_t(4) << 30;
+
+static int adjoint_chunk(sl_ctx* ctx, int64_t ntask) {
+    const AdjDev& D = ctx->adj;
+    const size_t per = (size_t)(2 * D.slots + D.nscale) * 4 + 6 * sizeof(double);
+    int64_t want = (int64_t)std::min<size_t>((size_t)ntask, kAdjScratchBytes / per);
+    want = std::max<int64_t>(1, want);
+    if (want <= ctx->adj_chunk) return SL_OK;
+    cudaStreamSynchronize(ctx->stream);
+    for (void* p : {(void*)ctx->d_adjA, (void*)ctx->d_adjB, (void*)ctx->d_adjE, (void*)ctx->d_adjG}) {
+        if (!p) continue;
+        cudaFree(p);
+        ctx->owned.erase(std::find(ctx->owned.begin(), ctx->owned.end(), p));
+    }
+    ctx->d_adjA = ctx->d_adjB = nullptr;
+    ctx->d_adjE = nullptr;
+    ctx->d_adjG = nullptr;
+    ctx->adj_chunk = 0;
+    int rc;
+    if ((rc = dev_alloc(ctx, &ctx->d_adjA, (size_t)D.slots * want))) return rc;
+    if ((rc = dev_alloc(ctx, &ctx->d_adjB, (size_t)D.slots * want))) return rc;
+    if ((rc = dev_alloc(ctx, &ctx->d_adjE, (size_t)std::max(1, D.nscale) * want))) return rc;
+    if ((rc = dev_alloc(ctx, &ctx->d_adjG, (size_t)6 * want))) return rc;
+    ctx->adj_chunk = want;
+    return SL_OK;
+}
+
+int sl_trait_backward(sl_ctx* ctx, int32_t n_graphs, const int32_t* dgs, double* grad, double* ptrait_grad) {
+    if (!ctx) return fail(ctx, SL_EINVAL, "null context");
+    if (!ctx->has_adjoint) return fail(ctx, SL_EINVAL, "the problem carries no disease model (affection is NULL)");
+    if (n_graphs < 0 || (n_graphs > 0 && (!dgs || !grad))) return fail(ctx, SL_EINVAL, "bad graph set");
+    const ProblemDev& P = ctx->P;
+    const size_t words = (size_t)P.M * P.W;
+    const int64_t npos = (int64_t)(P.M - 1) * P.n_lod;
+    CK(cudaSetDevice(ctx->device));
+    int rc;
+    if (ptrait_grad) {
+        if ((rc = adjoint_chunk(ctx, 1))) return rc;
+        Prof pr(ctx, SL_KERNEL_LOD);
+        CK(launch_trait_adjoint(P, ctx->adj, nullptr, 0, 0, 1, ctx->adj_chunk, ctx->d_adjA, ctx->d_adjB, ctx->d_adjE,
+                                ctx->d_adjG, ctx->d_status, ctx->stream));
+        double g6[6];
+        CK(cudaMemcpyAsync(g6, ctx->d_adjG, sizeof(g6), cudaMemcpyDeviceToHost, ctx->stream));
+        if ((rc = sl_synchronize(ctx))) return rc;
+        for (int k = 0; k < 4; ++k) ptrait_grad[k] = g6[2 + k];
+    }
+    if (n_graphs == 0) return SL_OK;
+    if (n_graphs > ctx->graphs_cap) {
+        if (ctx->d_graphs) {
+            cudaStreamSynchronize(ctx->stream);
+            cudaFree(ctx->d_graphs);
+            ctx->owned.erase(std::find(ctx->owned.begin(), ctx->owned.end(), (void*)ctx->d_graphs));
+            ctx->d_graphs = nullptr;
+        }
+        if ((rc = dev_alloc(ctx, &ctx->d_graphs, words * n_graphs))) return rc;
+        ctx->graphs_cap = n_graphs;
+    }
+    std::vector<uint32_t> buf(words * n_graphs);
+    for (int i = 0; i < n_graphs; ++i)
+        pack_graph(dgs + (size_t)i * 2 * P.N * P.M, P.N, P.F, P.M, P.W, buf.data() + words * i);
+    CK(cudaMemcpyAsync(ctx->d_graphs, buf.data(), sizeof(uint32_t) * words * n_graphs, cudaMemcpyHostToDevice,
+                       ctx->stream));
+    const int64_t ntask = npos * n_graphs;
+    if ((rc = adjoint_chunk(ctx, ntask))) return rc;
+    for (int64_t t0 = 0; t0 < ntask; t0 += ctx->adj_chunk) {
+        const int64_t nt = std::min(ctx->adj_chunk, ntask - t0);
+        {
+            Prof pr(ctx, SL_KERNEL_LOD);
+            CK(launch_trait_adjoint(P, ctx->adj, ctx->d_graphs, (int64_t)words, t0, nt, ctx->adj_chunk, ctx->d_adjA,
+                                    ctx->d_adjB, ctx->d_adjE, ctx->d_adjG, ctx->d_status, ctx->stream));
+        }
+        CK(cudaMemcpyAsync(grad + t0 * 6, ctx->d_adjG, sizeof(double) * 6 * nt, cudaMemcpyDeviceToHost,
+                           ctx->stream));
+    }
+    return sl_synchronize(ctx);
+}
+
+int sl_problem_trait_backward_eval(const sl_problem_desc* d, const int32_t* dg, int32_t locus, int32_t offset,
+                                   double* grad) {
+    int rc = check_desc(d);
+    if (rc) return rc;
+    if (!grad || (dg && (locus < 0 || locus >= d->n_markers - 1 || offset < 0 || offset >= d->lod_per_interval)))
+        return fail(nullptr, SL_EINVAL, "bad arguments");
+    std::vector<OpDev> ops;
+    std::vector<int32_t> od;
+    int arena = 0, max_child = 1;
+    if ((rc = build_ops(d, ops, od, arena, max_child))) return rc;
+    LodProgram prog;
+    compile_lod_program(d, ops, od, prog, true);
+    return host_backward(d, prog, dg, locus, offset, grad, nullptr);
 }
 
 int sl_run(sl_ctx* ctx, const sl_run_options* o) {

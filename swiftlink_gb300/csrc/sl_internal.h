@@ -59,6 +59,19 @@ struct ProblemDev {
 //   LI_END  slot                 the likelihood
 enum { LI_REC = 1, LI_SUM = 2, LI_CELL = 3, LI_SCALE = 4, LI_END = 5 };
 
+// The trait peel compiled for the adjoint: every cell and term kept (a zero
+// disease probability still has a derivative), no slot reused (the reverse
+// pass reads every forward value).
+struct AdjDev {
+    const int32_t* prog;     // LI_* words
+    const int32_t* starts;   // word offset of every instruction, in order
+    const float* pconst;     // constants (disease probabilities)
+    const float4* dconst;    // d constant / d (pen HOMO_U, pen HETERO, pen HOMO_A, frequency)
+    int32_t n_instr;
+    int32_t slots;
+    int32_t nscale;          // LI_SCALE instructions
+};
+
 // What code outside sl_host.cc may read of a context.
 struct CtxView {
     ProblemDev P;

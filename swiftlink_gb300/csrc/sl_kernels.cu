@@ -948,13 +948,16 @@ __global__ void __launch_bounds__(32) ffbs_scan_kernel(ProblemDev P, uint32_t* d
     float* fb = fbbuf + (size_t)cr * 2 * M;
     uint8_t* maps = mapbuf + (size_t)cr * M;
     float* th = nullptr;  // theta as floats, [M]
+    uint32_t* words = nullptr;  // the meiosis's descent-graph word at each locus, [M]
     if (staged) {
-        // stage the chain's pairs and the map in shared memory with coalesced loads:
-        // [r: 2M floats][fb: 2M floats][theta: M floats][maps: M bytes]
+        // stage the chain's pairs, theta and the meiosis's words in shared memory with
+        // coalesced / independent loads: [r: 2M][fb: 2M][theta: M] floats, [words: M], [maps: M bytes]
         float* sr = (float*)fsm;
         float* sfb = sr + 2 * M;
         th = sfb + 2 * M;
-        uint8_t* smaps = (uint8_t*)(th + M);
+        words = (uint32_t*)(th + M);
+        uint8_t* smaps = (uint8_t*)(words + M);
+        for (int i = lane; i < M; i += 32) words[i] = G[(size_t)i * P.W + (m >> 5)];
         for (int i = lane; i < 2 * M; i += 32) sr[i] = r[i];
         for (int i = lane; i < M; i += 32) th[i] = i > 0 ? (float)P.theta[i - 1] : 0.f;
         __syncwarp();
@@ -973,8 +976,10 @@ __global__ void __launch_bounds__(32) ffbs_scan_kernel(ProblemDev P, uint32_t* d
         const float n00 = q0 * (a * p00 + t * p10), n01 = q0 * (a * p01 + t * p11);
         const float n10 = q1 * (t * p00 + a * p10), n11 = q1 * (t * p01 + a * p11);
         p00 = n00; p01 = n01; p10 = n10; p11 = n11;
-        mat_norm(p00, p01, p10, p11);
+        // each pair is scaled to a maximum of 1, so 8 steps cannot underflow
+        if (((i - s0) & 7) == 7) mat_norm(p00, p01, p10, p11);
     }
+    mat_norm(p00, p01, p10, p11);
     // inclusive scan S_k = P_k ... P_0 (later chunks multiply on the left)
     for (int d = 1; d < 32; d <<= 1) {
         const float o00 = __shfl_up_sync(FULLMASK, p00, d), o01 = __shfl_up_sync(FULLMASK, p01, d);
@@ -1017,16 +1022,25 @@ __global__ void __launch_bounds__(32) ffbs_scan_kernel(ProblemDev P, uint32_t* d
         }
         above = x - cnt;
     }
-    // per-locus decision maps and the chunk's composed map
+    // per-locus decision maps and the chunk's composed map; the chunk's draws are
+    // independent of one another, so they are generated four at a time
     int gmap = 2;  // identity: bit0 = 0, bit1 = 1
     int idx = above;
+    double ubuf[4];
+    int ub = 4;
     for (int i = s1 - 1; i >= s0; --i) {
         const float f0 = fb[2 * i], f1 = fb[2 * i + 1];
         int dmap;
         if (f0 == 0.f) dmap = 3;
         else if (f1 == 0.f) dmap = 0;
         else {
-            const double u = draws.get(cr, chain, step, idx++);
+            if (ub == 4) {
+#pragma unroll
+                for (int q = 0; q < 4; ++q) ubuf[q] = idx + q < M ? draws.get(cr, chain, step, idx + q) : 0.0;
+                ub = 0;
+            }
+            const double u = ubuf[ub++];
+            ++idx;
             if (i == M - 1) {
                 const int v = (u < (double)(f0 / (f0 + f1))) ? 0 : 1;
                 dmap = v | (v << 1);
@@ -1053,12 +1067,13 @@ __global__ void __launch_bounds__(32) ffbs_scan_kernel(ProblemDev P, uint32_t* d
     for (int i = s1 - 1; i >= s0; --i) {
         sv = (maps[i] >> sv) & 1;
         uint32_t* wp = G + (size_t)i * P.W + (m >> 5);
-        const int cur = (int)((*wp >> (m & 31)) & 1u);
-        if (sv != cur) *wp ^= (1u << (m & 31));
+        const uint32_t w = words ? words[i] : *wp;
+        const int cur = (int)((w >> (m & 31)) & 1u);
+        if (sv != cur) *wp = w ^ (1u << (m & 31));
     }
 }
 
-size_t ffbs_scan_smem(int M) { return (size_t)5 * 4 * M + (size_t)M + 16; }
+size_t ffbs_scan_smem(int M) { return (size_t)6 * 4 * M + (size_t)M + 16; }
 
 // ---------------------------------------------------------------------------
 // Trait peel LOD scorer: one warp per (graph, interval, position).
@@ -1328,6 +1343,180 @@ __global__ void __launch_bounds__(128) lod_prog_kernel(ProblemDev P, const uint3
     }
 }
 
+// Adjoint of the trait peel, one thread per (graph, interval, position) task:
+// the program of AdjDev run forward in FP32 with per-rfunction power-of-two
+// rescaling, every value kept in A[slot][task] (global scratch, coalesced
+// across the warp), then run backward over the same instructions.  The
+// rescaling factors are constants of the forward pass, so the reverse pass on
+// scaled values gives d log L exactly as on unscaled ones: B[root] = 1/A[root],
+// and a LI_SCALE that multiplied its values by f multiplies their adjoints by f.
+// graphs == nullptr peels without a graph (every recombination term 1/4,
+// Peeler::calc_trait_prob): one task, no theta derivatives.
+// grad[task - task0][6] = d log L / d (theta_L, theta_R, pen x3, frequency), FP64.
+constexpr int kAdjMaxFactors = 32;
+
+__global__ void __launch_bounds__(128) trait_adjoint_kernel(ProblemDev P, AdjDev D, const uint32_t* graphs,
+                                                            int64_t graph_words, int64_t task0, int64_t ntask,
+                                                            int64_t stride, float* A, float* B, int* E,
+                                                            double* grad, int* status) {
+    const int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= ntask) return;
+    const int64_t t = task0 + u;
+    const int n = P.n_lod;
+    const int64_t npos = (int64_t)(P.M - 1) * n;
+    const uint32_t* colL = nullptr;
+    const uint32_t* colR = nullptr;
+    float th = 0.f, an = 0.f, th2 = 0.f, an2 = 0.f;
+    if (graphs) {
+        const int b = (int)(t / npos);
+        const int64_t pidx = t % npos;
+        const int l = (int)(pidx / n), o = (int)(pidx % n);
+        colL = graphs + (size_t)b * graph_words + (size_t)l * P.W;
+        colR = colL + P.W;
+        const double thd = P.partial[l] * (double)(o + 1);
+        const double th2d = P.partial[l] * (double)(n - o);
+        th = (float)thd;
+        an = (float)(1.0 - thd);
+        th2 = (float)th2d;
+        an2 = (float)(1.0 - th2d);
+    }
+    float* a = A + u;
+    float* g = B + u;
+    int* e = E + u;
+    // forward
+    int si = 0, res = -1;
+    for (int ii = 0; ii < D.n_instr; ++ii) {
+        const int32_t* pc = D.prog + __ldg(D.starts + ii);
+        const int op = __ldg(pc);
+        if (op == LI_CELL) {
+            const int dst = __ldg(pc + 1), nt = __ldg(pc + 2);
+            pc += 3;
+            float total = 0.f;
+            for (int q = 0; q < nt; ++q) {
+                const int nf = __ldg(pc);
+                float v = __ldg(D.pconst + __ldg(pc + 1));
+                pc += 2;
+                for (int f = 0; f < nf; ++f) v *= a[__ldg(pc + f) * stride];
+                pc += nf;
+                total += v;
+            }
+            a[dst * stride] = total;
+            g[dst * stride] = 0.f;
+        } else if (op == LI_REC) {
+            const int child = __ldg(pc + 1), dst = __ldg(pc + 2);
+            const int bits = graphs ? person_bits(P, colL, colR, child) : 0;
+            for (int k = 0; k < 4; ++k) {
+                a[(dst + k) * stride] = graphs ? 0.25f * trait_rec<float>(bits, k >> 1, k & 1, th, an, th2, an2) : 0.25f;
+                g[(dst + k) * stride] = 0.f;
+            }
+        } else if (op == LI_SUM) {
+            const int dst = __ldg(pc + 1), ns = __ldg(pc + 2);
+            float v = 0.f;
+            for (int q = 0; q < ns; ++q) v += a[__ldg(pc + 3 + q) * stride];
+            a[dst * stride] = v;
+            g[dst * stride] = 0.f;
+        } else if (op == LI_SCALE) {
+            const int first = __ldg(pc + 1), cnt = __ldg(pc + 2);
+            float mx = 0.f;
+            for (int q = 0; q < cnt; ++q) mx = fmaxf(mx, a[(first + q) * stride]);
+            int ex = 0;
+            if (mx > 0.f) {
+                ex = ilogbf(mx);
+                const float f = scalbnf(1.0f, -ex);
+                for (int q = 0; q < cnt; ++q) a[(first + q) * stride] *= f;
+            }
+            e[(si++) * stride] = ex;
+        } else {
+            res = __ldg(pc + 1);
+        }
+    }
+    double acc[6] = {0, 0, 0, 0, 0, 0};
+    const float root = res >= 0 ? a[res * stride] : 0.f;
+    if (!(root > 0.f)) {
+        set_status(status, ST_LOD_NONPOS);
+        for (int k = 0; k < 6; ++k) grad[u * 6 + k] = 0.0;
+        return;
+    }
+    g[res * stride] = 1.0f / root;
+    // reverse
+    for (int ii = D.n_instr - 1; ii >= 0; --ii) {
+        const int32_t* pc = D.prog + __ldg(D.starts + ii);
+        const int op = __ldg(pc);
+        if (op == LI_SCALE) {
+            const int first = __ldg(pc + 1), cnt = __ldg(pc + 2);
+            const float f = scalbnf(1.0f, -e[(--si) * stride]);
+            for (int q = 0; q < cnt; ++q) g[(first + q) * stride] *= f;
+        } else if (op == LI_CELL) {
+            const int dst = __ldg(pc + 1), nt = __ldg(pc + 2);
+            const float gd = g[dst * stride];
+            pc += 3;
+            if (gd == 0.f) {
+                for (int q = 0; q < nt; ++q) pc += 2 + __ldg(pc);
+                continue;
+            }
+            float m0 = 0.f, m1 = 0.f, m2 = 0.f, m3 = 0.f;
+            for (int q = 0; q < nt; ++q) {
+                const int nf = __ldg(pc), ci = __ldg(pc + 1);
+                const int32_t* fs = pc + 2;
+                pc += 2 + nf;
+                const float c = __ldg(D.pconst + ci);
+                float prod = 1.f;
+                if (nf <= kAdjMaxFactors) {
+                    float pre[kAdjMaxFactors];
+                    for (int f = 0; f < nf; ++f) {
+                        pre[f] = prod;
+                        prod *= a[__ldg(fs + f) * stride];
+                    }
+                    float suf = gd * c;
+                    for (int f = nf - 1; f >= 0; --f) {
+                        const int sl = __ldg(fs + f);
+                        g[sl * stride] += suf * pre[f];
+                        suf *= a[sl * stride];
+                    }
+                } else {
+                    for (int f = 0; f < nf; ++f) prod *= a[__ldg(fs + f) * stride];
+                    for (int f = 0; f < nf; ++f) {
+                        float others = gd * c;
+                        for (int f2 = 0; f2 < nf; ++f2)
+                            if (f2 != f) others *= a[__ldg(fs + f2) * stride];
+                        g[__ldg(fs + f) * stride] += others;
+                    }
+                }
+                const float4 dc = __ldg(D.dconst + ci);
+                m0 += prod * dc.x;
+                m1 += prod * dc.y;
+                m2 += prod * dc.z;
+                m3 += prod * dc.w;
+            }
+            acc[2] += (double)(gd * m0);
+            acc[3] += (double)(gd * m1);
+            acc[4] += (double)(gd * m2);
+            acc[5] += (double)(gd * m3);
+        } else if (op == LI_SUM) {
+            const int dst = __ldg(pc + 1), ns = __ldg(pc + 2);
+            const float gd = g[dst * stride];
+            for (int q = 0; q < ns; ++q) g[__ldg(pc + 3 + q) * stride] += gd;
+        } else if (op == LI_REC && graphs) {
+            const int child = __ldg(pc + 1), dst = __ldg(pc + 2);
+            const int bits = person_bits(P, colL, colR, child);
+            float dl = 0.f, dr = 0.f;
+            for (int k = 0; k < 4; ++k) {
+                const int i = k >> 1, j = k & 1;
+                const float gb = 0.25f * g[(dst + k) * stride];
+                const bool ml = (bits & 1) == i, mr = ((bits >> 2) & 1) == i;
+                const bool pl = ((bits >> 1) & 1) == j, pr = ((bits >> 3) & 1) == j;
+                const float x0 = ml ? an : th, x1 = mr ? an2 : th2, x2 = pl ? an : th, x3 = pr ? an2 : th2;
+                const float s0 = ml ? -1.f : 1.f, s1 = mr ? -1.f : 1.f, s2 = pl ? -1.f : 1.f, s3 = pr ? -1.f : 1.f;
+                dl += gb * (s0 * x1 * x2 * x3 + x0 * x1 * s2 * x3);
+                dr += gb * (x0 * s1 * x2 * x3 + x0 * x1 * x2 * s3);
+            }
+            acc[0] += (double)dl;
+            acc[1] += (double)dr;
+        }
+    }
+    for (int k = 0; k < 6; ++k) grad[u * 6 + k] = acc[k];
+}
+
 // log_sum (logarithms.cc:14-25)
 __device__ __forceinline__ double log_sum(double a, double b) {
     if (a == -DBL_MAX) return b;
@@ -1510,6 +1699,16 @@ cudaError_t launch_lod(const ProblemDev& P, int precision, const uint32_t* graph
         }
         lod_kernel<float, true><<<(int)grid, wpb * 32, smem, s>>>(P, graphs, graph_words, G, vals, status);
     }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_trait_adjoint(const ProblemDev& P, const AdjDev& D, const uint32_t* graphs, int64_t graph_words,
+                                 int64_t task0, int64_t ntask, int64_t stride, float* A, float* B, int* E,
+                                 double* grad, int* status, cudaStream_t s) {
+    const int threads = 128;
+    const int64_t grid = (ntask + threads - 1) / threads;
+    trait_adjoint_kernel<<<(int)grid, threads, 0, s>>>(P, D, graphs, graph_words, task0, ntask, stride, A, B, E,
+                                                       grad, status);
     return cudaGetLastError();
 }
 

@@ -45,3 +45,35 @@ def position_bytes(N: int, F: int, n: int) -> float:
     the FP64 accumulator read-modify-write: (2*ceil(Nnf/4) + 4)/n + 16."""
     nnf = N - F
     return (2 * (-(-nnf // 4)) + 4) / n + 16
+
+
+def disease_probs(affection, founder, freq, penetrance):
+    """Person::disease_prob (person.cc:85-119) from the disease model
+    (DiseaseModel::get_apriori_prob2 / get_penetrance_prob2,
+    disease_model.cc:139-187), autosomal, phased order UU, AA, AU, UA.
+    affection: 0 unknown, 1 unaffected, 2 affected; founder: bool per person."""
+    affection = np.asarray(affection)
+    founder = np.asarray(founder, bool)
+    q = float(freq)
+    pen = [float(x) for x in penetrance]
+    prior = [(1.0 - q) * (1.0 - q), q * (1.0 - q), q * q]   # HOMO_U, HETERO, HOMO_A
+    unph = [0, 2, 1, 1]                                     # UU, AA, AU, UA -> unphased trait
+    out = np.zeros((affection.size, 4))
+    for i, (a, f) in enumerate(zip(affection, founder)):
+        for v in range(4):
+            t = unph[v]
+            if f:
+                if a == 2:
+                    out[i, v] = prior[t] * pen[t]
+                elif a == 1:
+                    out[i, v] = prior[t] * (1.0 - pen[t])
+                else:
+                    out[i, v] = (prior[t] * pen[t]) + (prior[t] * (1.0 - pen[t]))
+            else:
+                if a == 2:
+                    out[i, v] = pen[t]
+                elif a == 1:
+                    out[i, v] = 1.0 - pen[t]
+                else:
+                    out[i, v] = 0.25
+    return out

@@ -107,6 +107,7 @@ def make_problem_only(name, seed):
     out = {k: v for k, v in d.items() if isinstance(v, np.ndarray) and k != "trait_prior"}
     for k in ("N", "F", "M", "K", "n_lod"):
         out[k] = np.int64(d[k])
+    out["freq"] = np.float64(p.freq)
     for k in ("op_cutset", "op_prev", "op_children"):
         out[k + "_off"], out[k + "_flat"] = csr(d[k])
     dg0, ll0 = r.initial_dg(si_iters=2)

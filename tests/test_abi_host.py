@@ -120,3 +120,11 @@ def test_compiled_lod_program_matches_reference(name):
             rc = fn(ctypes.byref(desc), dg.ctypes.data_as(ctypes.c_void_p), int(l), o, ctypes.byref(v))
             assert rc == 0
             assert abs(v.value - raw_one[l * n + o]) <= 1e-9 * max(1.0, abs(raw_one[l * n + o])), (l, o)
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_disease_probs_restatement_matches_reference(name):
+    from swiftlink_gb300.workloads import disease_probs
+    g = load_golden(name)
+    dp = disease_probs(g["affection"], g["mother"] < 0, g["freq"], g["penetrance"])
+    np.testing.assert_array_equal(dp, g["disease_prob"])
