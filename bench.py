@@ -316,7 +316,10 @@ def run_ours(args):
         1: sum((C - nl) * sb for nl in n_l),
         2: scorings * C * npos * position_bytes(N, F, n),
     }
-    names = {0: "lsampler_kernel", 1: "fag_kernel+ffbs_kernel<float>", 2: "lod_kernel<float,true>",
+    lod_kernel_names = {api.SL_LOD_KERNEL_INTERP: "lod_prog_kernel", api.SL_LOD_KERNEL_JIT_REG: "sl_lod_jit (registers)",
+                        api.SL_LOD_KERNEL_JIT_SMEM: "sl_lod_jit (shared memory)"}
+    sel, jit_ms = ctx.lod_kernel_info()
+    names = {0: "lsampler_kernel", 1: "fag_kernel+ffbs_scan_kernel", 2: lod_kernel_names.get(sel, "lod_kernel"),
              3: "lod_merge_kernel", 4: "choose/shuffle"}
     dom = max(kern, key=lambda k: kern[k][0])
     dom_ms, dom_n = kern[dom]
@@ -341,6 +344,7 @@ def run_ours(args):
     lctx.set_graphs(gset)
     lstream = torch.cuda.ExternalStream(lctx.stream_handle())
     lod_pos_s = timed_lod(lctx, lstream, flush, G, npos, reps=5)
+    lsel, ljit_ms = lctx.lod_kernel_info()
     pctx = api.Context(prob, n_chains=1, lod_precision=api.SL_LOD_FP64, device=local)
     pctx.set_graphs(gset[:1])
     pstream = torch.cuda.ExternalStream(pctx.stream_handle())
@@ -390,6 +394,9 @@ def run_ours(args):
                "data": "synthetic (seeded generator, swiftlink_gb300/synth.py; no public dataset)",
                "config": config(world), "impl": "ours",
                "lod_positions_per_s": lod_pos_s * world,
+               "lod_kernel": {"selected": lod_kernel_names.get(lsel, str(lsel)),
+                              "specialised_compile_ms": round(ljit_ms, 1),
+                              "selection": "timed at the first scoring (SL_LOD_KERNEL_AUTO)"},
                "plain": {"steps_per_s": plain_steps_s * world, "lod_positions_per_s": plain_lod_pos_s * world,
                          "form": "one chain per launch, exact FP64 samplers, FP64 LOD peel"},
                "batched_vs_plain": {"steps": value / (plain_steps_s * world),

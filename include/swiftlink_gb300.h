@@ -102,7 +102,18 @@ typedef struct sl_options {
     int32_t n_chains;           /* descent graphs held on the device (replicates x temperatures) */
     int32_t lod_precision;      /* SL_LOD_FP64 or SL_LOD_FP32_RESCALED */
     int32_t sampler_precision;  /* SL_SAMPLER_EXACT or SL_SAMPLER_FAST */
+    int32_t lod_kernel;         /* SL_LOD_KERNEL_*: the batched scorer's kernel (0 = timed choice) */
 } sl_options;
+
+/* Kernels of the batched (FP32-rescaled) LOD scorer.  AUTO compiles the
+ * problem-specialised forms at sl_create and, at the first scoring, times each
+ * candidate on that batch and keeps the fastest (the reference autotunes its
+ * launch shape in GPULodscores, gpu_lodscores.cc:529-596).  The others force
+ * one kernel; a forced specialised form that cannot be built fails sl_create. */
+#define SL_LOD_KERNEL_AUTO 0
+#define SL_LOD_KERNEL_INTERP 1      /* slot-program interpreter */
+#define SL_LOD_KERNEL_JIT_REG 2     /* specialised straight-line code, values in registers */
+#define SL_LOD_KERNEL_JIT_SMEM 3    /* specialised straight-line code, values in shared memory */
 
 /* Create a context; replaces GPULodscores::GPULodscores (gpu_lodscores.h:63-83). */
 int sl_create(const sl_problem_desc* problem, const sl_options* options, sl_ctx** out);
@@ -293,6 +304,11 @@ int sl_trait_backward(sl_ctx* ctx, int32_t n_graphs, const int32_t* dgs, double*
  * gives the gradient of log P(T) in grad[2..5]. */
 int sl_problem_trait_backward_eval(const sl_problem_desc* problem, const int32_t* dg, int32_t locus,
                                    int32_t offset, double* grad);
+
+/* The batched LOD kernel in use (SL_LOD_KERNEL_*; AUTO until the first
+ * scoring has timed the candidates) and the milliseconds spent compiling the
+ * specialised forms at sl_create. */
+int sl_lod_kernel_info(sl_ctx* ctx, int32_t* kernel, double* compile_ms);
 
 /* Library version string. */
 const char* sl_version(void);

@@ -19,6 +19,7 @@ LIB_PATH = os.path.join(_HERE, "_build", "libswiftlink_gb300.so")
 SL_OK, SL_EINVAL, SL_ECUDA, SL_EZERO, SL_EILLEGAL, SL_ENOMEM, SL_ENODEV = 0, -1, -2, -3, -4, -5, -6
 SL_LOD_FP64, SL_LOD_FP32_RESCALED = 0, 1
 SL_SAMPLER_EXACT, SL_SAMPLER_FAST = 0, 1
+SL_LOD_KERNEL_AUTO, SL_LOD_KERNEL_INTERP, SL_LOD_KERNEL_JIT_REG, SL_LOD_KERNEL_JIT_SMEM = 0, 1, 2, 3
 
 EXPORTED = [
     "sl_create", "sl_destroy", "sl_last_error", "sl_set_descent_graphs", "sl_get_descent_graphs",
@@ -27,7 +28,7 @@ EXPORTED = [
     "sl_lod_reset", "sl_run", "sl_synchronize", "sl_device_status", "sl_launch_count",
     "sl_version", "sl_get_stream", "sl_profile", "sl_profile_read", "sl_problem_legal_masks",
     "sl_problem_trait_priors", "sl_problem_trait_prob", "sl_trait_backward",
-    "sl_problem_trait_backward_eval",
+    "sl_problem_trait_backward_eval", "sl_lod_kernel_info",
 ]
 
 
@@ -55,7 +56,8 @@ class ProblemDesc(ctypes.Structure):
 
 class Options(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int32), ("n_chains", ctypes.c_int32),
-                ("lod_precision", ctypes.c_int32), ("sampler_precision", ctypes.c_int32)]
+                ("lod_precision", ctypes.c_int32), ("sampler_precision", ctypes.c_int32),
+                ("lod_kernel", ctypes.c_int32)]
 
 
 class RunOptions(ctypes.Structure):
@@ -180,10 +182,10 @@ class Context:
     """A device context holding one problem and n_chains descent graphs."""
 
     def __init__(self, problem: Problem, n_chains: int = 1, lod_precision: int = SL_LOD_FP64,
-                 device: int = 0, sampler_precision: int = SL_SAMPLER_EXACT):
+                 device: int = 0, sampler_precision: int = SL_SAMPLER_EXACT, lod_kernel: int = SL_LOD_KERNEL_AUTO):
         self.problem = problem
         self._desc = problem.desc()
-        opt = Options(device, n_chains, lod_precision, sampler_precision)
+        opt = Options(device, n_chains, lod_precision, sampler_precision, lod_kernel)
         h = _vp()
         rc = lib().sl_create(ctypes.byref(self._desc), ctypes.byref(opt), ctypes.byref(h))
         if rc != SL_OK:
@@ -278,6 +280,13 @@ class Context:
 
     def lod_reset(self):
         self._check(lib().sl_lod_reset(self.h))
+
+    def lod_kernel_info(self):
+        """(SL_LOD_KERNEL_* in use, milliseconds spent compiling specialised forms)."""
+        k = ctypes.c_int32()
+        ms = ctypes.c_double()
+        self._check(lib().sl_lod_kernel_info(self.h, ctypes.byref(k), ctypes.byref(ms)))
+        return k.value, ms.value
 
     def trait_backward(self, dgs: Optional[np.ndarray] = None):
         """d log L / d (theta_L, theta_R, pen x3, frequency) at every LOD

@@ -1,10 +1,12 @@
 """Build the in-tree CUDA library swiftlink_gb300/_build/libswiftlink_gb300.so.
 
-Three translation units compiled in parallel for sm_103a only, then linked
-with the static CUDA runtime:
+Four translation units compiled in parallel for sm_103a only, then linked
+with the static CUDA runtime and NVRTC (which compiles the problem-specialised
+LOD kernels when a context is created):
   csrc/sl_kernels.cu  (nvcc, -gencode arch=compute_103a,code=sm_103a)
   csrc/sl_noalloc.cu  (nvcc, same flags)
   csrc/sl_host.cc     (g++ against the CUDA runtime headers)
+  csrc/sl_jit.cc      (g++, NVRTC source generator and loader)
 """
 from __future__ import annotations
 
@@ -49,11 +51,13 @@ def build(verbose: bool = False, force: bool = False) -> str:
     cuda = _cuda_home()
     nvcc = os.path.join(cuda, "bin", "nvcc")
     os.makedirs(OUT, exist_ok=True)
-    hdrs = [os.path.join(CSRC, "sl_internal.h"),
+    hdrs = [os.path.join(CSRC, "sl_internal.h"), os.path.join(CSRC, "sl_jit.h"),
             os.path.join(os.path.dirname(HERE), "include", "swiftlink_gb300.h")]
     cu = os.path.join(CSRC, "sl_kernels.cu")
     cu2 = os.path.join(CSRC, "sl_noalloc.cu")
     cc = os.path.join(CSRC, "sl_host.cc")
+    jc = os.path.join(CSRC, "sl_jit.cc")
+    jc_o = os.path.join(OUT, "sl_jit.o")
     cu_o = os.path.join(OUT, "sl_kernels.o")
     cu2_o = os.path.join(OUT, "sl_noalloc.o")
     cc_o = os.path.join(OUT, "sl_host.o")
@@ -62,15 +66,18 @@ def build(verbose: bool = False, force: bool = False) -> str:
         if force or _stale(obj, [src] + hdrs):
             jobs.append([nvcc, GENCODE, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                          "-Xptxas", "-v", "-c", src, "-o", obj])
-    if force or _stale(cc_o, [cc] + hdrs):
-        jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-Wall", "-I" + os.path.join(cuda, "include"),
-                     "-c", cc, "-o", cc_o])
+    for src, obj in ((cc, cc_o), (jc, jc_o)):
+        if force or _stale(obj, [src] + hdrs):
+            jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-Wall", "-I" + os.path.join(cuda, "include"),
+                         "-c", src, "-o", obj])
     logs = []
     if jobs:
         with cf.ThreadPoolExecutor(len(jobs)) as ex:
             logs = list(ex.map(_run, jobs))
-    if force or jobs or _stale(LIB, [cu_o, cu2_o, cc_o]):
-        logs.append(_run([nvcc, GENCODE, "-shared", "-cudart", "static", "-o", LIB, cu_o, cu2_o, cc_o]))
+    if force or jobs or _stale(LIB, [cu_o, cu2_o, cc_o, jc_o]):
+        lib64 = os.path.join(cuda, "lib64")
+        logs.append(_run([nvcc, GENCODE, "-shared", "-cudart", "static", "-o", LIB, cu_o, cu2_o, cc_o, jc_o,
+                          "-L" + lib64, "-lnvrtc", "-Xlinker", "-rpath=" + lib64]))
     if verbose:
         for l in logs:
             sys.stdout.write(l)

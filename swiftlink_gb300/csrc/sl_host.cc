@@ -12,10 +12,13 @@
 #include <cstring>
 #include <map>
 #include <string>
+#include <chrono>
+#include <thread>
 #include <vector>
 
 #include "../../include/swiftlink_gb300.h"
 #include "sl_internal.h"
+#include "sl_jit.h"
 
 namespace sl {
 // kernels (sl_kernels.cu)
@@ -102,6 +105,11 @@ struct sl_ctx {
     int* d_adjE = nullptr;           // [nscale][chunk] rescaling exponents
     double* d_adjG = nullptr;        // [chunk][6] gradients
     int64_t adj_chunk = 0;
+    // batched LOD kernel: the interpreter, or a problem-specialised form
+    int lod_kernel_req = SL_LOD_KERNEL_AUTO;
+    int lod_kernel_sel = SL_LOD_KERNEL_INTERP;   // AUTO while the first scoring has not timed them
+    JitLod jit_reg, jit_smem;
+    double jit_ms = 0.0;
     std::string err;
     // per-kernel event timing
     bool profiling = false;
@@ -889,6 +897,8 @@ void sl_destroy(sl_ctx* ctx) {
     if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
     if (ctx->lstream) cudaStreamDestroy(ctx->lstream);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    jit_lod_release(&ctx->jit_reg);
+    jit_lod_release(&ctx->jit_smem);
     cudaSetDevice(cur);
     delete ctx;
 }
@@ -1087,6 +1097,33 @@ int sl_create(const sl_problem_desc* d, const sl_options* opt, sl_ctx** out) {
             P.prog_slots = prog.slots;
             P.prog_threads = S;
         }
+        const int req = opt->lod_kernel;
+        if (req < SL_LOD_KERNEL_AUTO || req > SL_LOD_KERNEL_JIT_SMEM)
+            return bail(fail(nullptr, SL_EINVAL, "unknown lod_kernel %d", req));
+        ctx->lod_kernel_req = req;
+        if (req != SL_LOD_KERNEL_INTERP) {
+            const JitProgramIn in{prog.words.data(), prog.words.size(), prog.consts.data(), F, M, n,
+                                  P.W, N - F, prog.slots, P.marker_trans};
+            const auto t0 = std::chrono::steady_clock::now();
+            std::string log_reg, log_smem;
+            int rc_reg = -1, rc_smem = -1;
+            // the two forms compile concurrently (NVRTC programs are independent)
+            std::thread th([&] {
+                cudaSetDevice(ctx->device);
+                if (req != SL_LOD_KERNEL_JIT_SMEM) rc_reg = jit_lod_compile(in, 128, false, &ctx->jit_reg, &log_reg);
+            });
+            if (req != SL_LOD_KERNEL_JIT_REG && S)
+                rc_smem = jit_lod_compile(in, S, true, &ctx->jit_smem, &log_smem);
+            th.join();
+            ctx->jit_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+            if (req == SL_LOD_KERNEL_JIT_REG && rc_reg)
+                return bail(fail(nullptr, SL_EINVAL, "specialised LOD kernel (registers) failed: %.300s", log_reg.c_str()));
+            if (req == SL_LOD_KERNEL_JIT_SMEM && rc_smem)
+                return bail(fail(nullptr, SL_EINVAL, "specialised LOD kernel (shared) failed: %.300s", log_smem.c_str()));
+        }
+        if (!S && !ctx->jit_reg.kern && !ctx->jit_smem.kern) ctx->lod_kernel_sel = SL_LOD_KERNEL_INTERP;
+        else if (req == SL_LOD_KERNEL_AUTO) ctx->lod_kernel_sel = SL_LOD_KERNEL_AUTO;
+        else ctx->lod_kernel_sel = req;
     }
     if (d->affection) {
         LodProgram full;
@@ -1308,14 +1345,63 @@ int sl_msampler_sweep(sl_ctx* ctx, int32_t first, int32_t n_chains, const int32_
     return sl_synchronize(ctx);
 }
 
+// One launch of the batched scorer's kernel `which` over G graphs.
+static cudaError_t launch_lod_kernel(sl_ctx* ctx, int which, const uint32_t* graphs, int G) {
+    const ProblemDev& P = ctx->P;
+    const int64_t npos = (int64_t)(P.M - 1) * P.n_lod;
+    if (which == SL_LOD_KERNEL_JIT_REG || which == SL_LOD_KERNEL_JIT_SMEM) {
+        const JitLod& j = which == SL_LOD_KERNEL_JIT_REG ? ctx->jit_reg : ctx->jit_smem;
+        return jit_lod_launch(j, graphs, (int64_t)P.M * P.W, G, ctx->d_vals, ctx->d_status, P.partial, P.theta,
+                              npos * G, ctx->sms, ctx->stream);
+    }
+    return launch_lod(P, ctx->lod_precision, graphs, (int64_t)P.M * P.W, G, ctx->d_vals, ctx->d_status, ctx->stream,
+                      ctx->lod_grid, ctx->lod_wpb);
+}
+
+// The timed choice of the batched scorer's kernel, on the first batch scored:
+// each candidate runs twice on it (the second run timed), the fastest is kept.
+static int autotune_lod(sl_ctx* ctx, const uint32_t* graphs, int G) {
+    std::vector<int> cand;
+    if (ctx->P.prog) cand.push_back(SL_LOD_KERNEL_INTERP);
+    if (ctx->jit_reg.kern) cand.push_back(SL_LOD_KERNEL_JIT_REG);
+    if (ctx->jit_smem.kern) cand.push_back(SL_LOD_KERNEL_JIT_SMEM);
+    if (cand.empty()) cand.push_back(SL_LOD_KERNEL_INTERP);
+    int best = cand[0];
+    float best_ms = 0.f;
+    cudaEvent_t a = take_event(ctx), b = take_event(ctx);
+    for (int k : cand) {
+        CK(launch_lod_kernel(ctx, k, graphs, G));
+        CK(cudaEventRecord(a, ctx->stream));
+        CK(launch_lod_kernel(ctx, k, graphs, G));
+        CK(cudaEventRecord(b, ctx->stream));
+        CK(cudaEventSynchronize(b));
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, a, b));
+        if (k == cand[0] || ms < best_ms) {
+            best = k;
+            best_ms = ms;
+        }
+    }
+    ctx->event_pool.push_back(a);
+    ctx->event_pool.push_back(b);
+    ctx->lod_kernel_sel = best;
+    return SL_OK;
+}
+
 static int score_device_graphs(sl_ctx* ctx, const uint32_t* graphs, int G) {
     const ProblemDev& P = ctx->P;
     const int64_t npos = (int64_t)(P.M - 1) * P.n_lod;
     for (int g0 = 0; g0 < G; g0 += ctx->vals_graphs) {
         const int g = std::min(ctx->vals_graphs, G - g0);
+        const uint32_t* gr = graphs + (size_t)g0 * P.M * P.W;
+        if (ctx->lod_precision == SL_LOD_FP32_RESCALED && ctx->lod_kernel_sel == SL_LOD_KERNEL_AUTO) {
+            int rc = autotune_lod(ctx, gr, g);
+            if (rc) return rc;
+        }
         { Prof pf_(ctx, SL_KERNEL_LOD);
-        CK(launch_lod(P, ctx->lod_precision, graphs + (size_t)g0 * P.M * P.W, (int64_t)P.M * P.W, g, ctx->d_vals,
-                      ctx->d_status, ctx->stream, ctx->lod_grid, ctx->lod_wpb)); }
+        CK(launch_lod_kernel(ctx, ctx->lod_precision == SL_LOD_FP32_RESCALED ? ctx->lod_kernel_sel
+                                                                              : SL_LOD_KERNEL_INTERP,
+                             gr, g)); }
         { Prof pf_(ctx, SL_KERNEL_LOD_MERGE);
       CK(launch_lod_merge(ctx->d_vals, g, npos, ctx->d_acc, ctx->d_init, ctx->stream));
     }
@@ -1558,6 +1644,13 @@ static int adjoint_chunk(sl_ctx* ctx, int64_t ntask) {
     if ((rc = dev_alloc(ctx, &ctx->d_adjE, (size_t)std::max(1, D.nscale) * want))) return rc;
     if ((rc = dev_alloc(ctx, &ctx->d_adjG, (size_t)6 * want))) return rc;
     ctx->adj_chunk = want;
+    return SL_OK;
+}
+
+int sl_lod_kernel_info(sl_ctx* ctx, int32_t* kernel, double* compile_ms) {
+    if (!ctx) return fail(ctx, SL_EINVAL, "null context");
+    if (kernel) *kernel = ctx->lod_precision == SL_LOD_FP32_RESCALED ? ctx->lod_kernel_sel : SL_LOD_KERNEL_INTERP;
+    if (compile_ms) *compile_ms = ctx->jit_ms;
     return SL_OK;
 }
 

@@ -1,0 +1,40 @@
+// The batched trait peel specialised to one problem at context creation
+// (straight-line CUDA C++ compiled with NVRTC); see sl_jit.cc.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+
+namespace sl {
+
+// One compiled slot program and the sizes its source needs.
+struct JitProgramIn {
+    const int32_t* words;
+    size_t n_words;
+    const float* consts;
+    int F, M, n, W, Nnf, slots;
+    double marker_trans;
+};
+
+struct JitLod {
+    void* lib = nullptr;     // cudaLibrary_t
+    void* kern = nullptr;    // cudaKernel_t
+    int threads = 0;
+    bool shared = false;     // values in a shared-memory arena (else registers)
+    size_t smem = 0;
+    int regs = 0;
+    int local_bytes = 0;     // spill space per thread
+    int blocks_per_sm = 0;
+    double compile_ms = 0.0;
+};
+
+std::string jit_lod_source(const JitProgramIn& in, int threads, bool shared);
+int jit_lod_compile(const JitProgramIn& in, int threads, bool shared, JitLod* out, std::string* log);
+void jit_lod_release(JitLod* j);
+cudaError_t jit_lod_launch(const JitLod& j, const uint32_t* graphs, int64_t graph_words, int G, double* vals,
+                           int* status, const double* partial, const double* theta, int64_t ntask, int sms,
+                           cudaStream_t s);
+
+}  // namespace sl

@@ -258,3 +258,57 @@ def test_fast_msampler_agrees_with_exact():
     agree = float((out[api.SL_SAMPLER_FAST] == out[api.SL_SAMPLER_EXACT]).mean())
     print(f"fast/exact M-sweep bit agreement {agree:.6f}")
     assert agree >= 0.999
+
+
+LOD_KERNELS = [api.SL_LOD_KERNEL_INTERP, api.SL_LOD_KERNEL_JIT_REG, api.SL_LOD_KERNEL_JIT_SMEM,
+               api.SL_LOD_KERNEL_AUTO]
+
+
+@pytest.mark.parametrize("kernel", LOD_KERNELS)
+@pytest.mark.parametrize("name", CASES)
+def test_batched_lod_kernels_against_reference(name, kernel):
+    """Every kernel of the FP32-rescaled scorer (the slot-program interpreter,
+    the problem-specialised forms with values in registers or in shared
+    memory, and the timed choice) within |dLOD| <= 1e-3 of the reference."""
+    g = load_golden(name)
+    with api.Context(api.Problem.from_arrays(g), n_chains=1, lod_precision=api.SL_LOD_FP32_RESCALED,
+                     lod_kernel=kernel) as ctx:
+        ctx.lod_score_graphs(g["lod_graphs"][:1])
+        ctx.lod_score_graphs(g["lod_graphs"][1:])
+        raw, cnt, tp = ctx.lod_results()
+        used, _ = ctx.lod_kernel_info()
+    assert used != api.SL_LOD_KERNEL_AUTO
+    if kernel != api.SL_LOD_KERNEL_AUTO:
+        assert used == kernel
+    assert cnt == g["lod_count"]
+    got = api.lod_table(raw, cnt, tp)
+    want = api.lod_table(g["lod_raw"], g["lod_count"], g["lod_trait_prob"])
+    assert np.abs(got - want).max() <= FP32_LOD_TOL
+
+
+@pytest.mark.parametrize("kernel", LOD_KERNELS)
+def test_batched_lod_kernels_large_pedigree(kernel):
+    """The 120-member, 2000-SNP pedigree: four seeded graphs (the starting
+    graph after 0-3 L-sweeps from the oracle) scored by each kernel, against
+    the oracle's FP64 LOD."""
+    from swiftlink_gb300.workloads import load_problem
+    d = load_problem("cfg2")
+    P = port.Port(d)
+    rng = np.random.default_rng(31)
+    st = d["K"] + 2 * d["N"]
+    graphs = [d["dg0"].copy()]
+    for _ in range(3):
+        dg = graphs[-1].copy()
+        u = rng.random((d["M"], st))
+        for l in list(range(0, d["M"], 2)) + list(range(1, d["M"], 2)):
+            dg, _ = P.lstep(dg, l, u[l])
+        graphs.append(dg)
+    graphs = np.stack(graphs)
+    ref_raw, ref_cnt, ref_tp = P.lod(graphs)
+    with api.Context(api.Problem.from_arrays(d), n_chains=1, lod_precision=api.SL_LOD_FP32_RESCALED,
+                     lod_kernel=kernel) as ctx:
+        ctx.lod_score_graphs(graphs)
+        raw, cnt, tp = ctx.lod_results()
+    assert cnt == ref_cnt
+    err = np.abs(api.lod_table(raw, cnt, tp) - api.lod_table(ref_raw, ref_cnt, ref_tp)).max()
+    assert err <= FP32_LOD_TOL, err
