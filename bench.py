@@ -68,7 +68,9 @@ def config(world):
             "members": 120, "markers": 2000, "chains_per_gpu": CHAINS, "scoring_period": PERIOD,
             "lod_positions_per_graph": 9995, "lsampler_prob": LPROB,
             "parallelism": f"replicas x{world}",
-            "l2": "flushed (256 MB write) before every timed step"}
+            "l2": "flushed (256 MB write) before every timed step",
+            "zero_likelihood_positions": "counted as zero terms of the log-sum (SL_LOD_ZERO_OK); the "
+                                         "reference exits at the first one (peeler.cc:89-92)"}
 
 
 # ---------------------------------------------------------------------------
@@ -173,7 +175,7 @@ def cpu_baseline_sample():
     dg, _ = P.msweep(dg, order, rng.random((order.size, M)))
     tm = time.perf_counter() - t0
     t0 = time.perf_counter()
-    P.lod(dg[None])
+    P.lod(dg[None], zero_ok=True)
     tlod = time.perf_counter() - t0
     steps_per_s = 2.0 / (tl + tm)
     return {"value": steps_per_s, "unit": UNIT, "cores": 1, "kind": "port",
@@ -198,7 +200,7 @@ def _ref_worker(args):
         for c in chains:
             dgs[c] = port_iteration(P, d, dgs[c], c, it)
         if it % PERIOD == 0:
-            P.lod(np.stack([dgs[c] for c in chains]))
+            P.lod(np.stack([dgs[c] for c in chains]), zero_ok=True)
             scored += len(chains)
         done += 1
         if time.perf_counter() - t0 > budget_s:
@@ -276,7 +278,7 @@ def run_ours(args):
 
     # ---------------- batched form: all chains per launch, FP32-rescaled LOD
     ctx = api.Context(prob, n_chains=C, lod_precision=api.SL_LOD_FP32_RESCALED, device=local,
-                      sampler_precision=api.SL_SAMPLER_FAST)
+                      sampler_precision=api.SL_SAMPLER_FAST, lod_flags=api.SL_LOD_ZERO_OK)
     ctx.set_graphs(np.stack([d["dg0"]] * C))
     stream = torch.cuda.ExternalStream(ctx.stream_handle())
     W, K = args.warmup, args.steps
@@ -340,12 +342,12 @@ def run_ours(args):
     graphs = ctx.get_graphs()
     G = 64
     gset = np.stack([graphs[i % C] for i in range(G)])
-    lctx = api.Context(prob, n_chains=G, lod_precision=api.SL_LOD_FP32_RESCALED, device=local)
+    lctx = api.Context(prob, n_chains=G, lod_precision=api.SL_LOD_FP32_RESCALED, device=local, lod_flags=api.SL_LOD_ZERO_OK)
     lctx.set_graphs(gset)
     lstream = torch.cuda.ExternalStream(lctx.stream_handle())
     lod_pos_s = timed_lod(lctx, lstream, flush, G, npos, reps=5)
     lsel, ljit_ms = lctx.lod_kernel_info()
-    pctx = api.Context(prob, n_chains=1, lod_precision=api.SL_LOD_FP64, device=local)
+    pctx = api.Context(prob, n_chains=1, lod_precision=api.SL_LOD_FP64, device=local, lod_flags=api.SL_LOD_ZERO_OK)
     pctx.set_graphs(gset[:1])
     pstream = torch.cuda.ExternalStream(pctx.stream_handle())
     plain_lod_pos_s = timed_lod(pctx, pstream, flush, 1, npos, reps=3)
@@ -367,7 +369,7 @@ def run_ours(args):
 
     # ---------------- end to end through the public API with host buffers
     ectx = api.Context(prob, n_chains=C, lod_precision=api.SL_LOD_FP32_RESCALED, device=local,
-                       sampler_precision=api.SL_SAMPLER_FAST)
+                       sampler_precision=api.SL_SAMPLER_FAST, lod_flags=api.SL_LOD_ZERO_OK)
     host_graphs = np.ascontiguousarray(np.stack([d["dg0"]] * C))
     ectx.set_graphs(host_graphs)
     ectx.run(iterations=W, burnin=0, period=PERIOD, lprob=LPROB, seed=seed)

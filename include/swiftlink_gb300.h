@@ -103,7 +103,17 @@ typedef struct sl_options {
     int32_t lod_precision;      /* SL_LOD_FP64 or SL_LOD_FP32_RESCALED */
     int32_t sampler_precision;  /* SL_SAMPLER_EXACT or SL_SAMPLER_FAST */
     int32_t lod_kernel;         /* SL_LOD_KERNEL_*: the batched scorer's kernel (0 = timed choice) */
+    int32_t lod_flags;          /* SL_LOD_ZERO_OK or 0 */
 } sl_options;
+
+/* A LOD position whose trait likelihood is 0 (an affected and an unaffected
+ * member IBD 2 under a fully penetrant model, for instance) stops the
+ * reference (Peeler::process, peeler.cc:89-92: exit(1)).  By default the
+ * library reports it as SL_EZERO from the next synchronising call, after
+ * counting the position as a zero term of the log-sum.  With SL_LOD_ZERO_OK
+ * the zero term is counted and no error is raised (the adjoint then writes
+ * NaN for that position). */
+#define SL_LOD_ZERO_OK 1
 
 /* Kernels of the batched (FP32-rescaled) LOD scorer.  AUTO compiles the
  * problem-specialised forms at sl_create and, at the first scoring, times each

@@ -111,13 +111,13 @@ class Port:
             raise RuntimeError(f"slo_msweep failed ({rc})")
         return dg, used
 
-    def lod(self, dgs):
+    def lod(self, dgs, zero_ok=False):
         dgs = np.ascontiguousarray(dgs, np.int32)
         raw = np.zeros((self.M - 1) * self.n_lod)
         cnt = ctypes.c_uint32()
         tp = ctypes.c_double()
-        rc = lib().slo_lod(ctypes.byref(self.s), _p(dgs), dgs.shape[0], _p(raw), ctypes.byref(cnt),
-                           ctypes.byref(tp))
+        rc = lib().slo_lod_ex(ctypes.byref(self.s), _p(dgs), dgs.shape[0], _p(raw), ctypes.byref(cnt),
+                              ctypes.byref(tp), int(zero_ok))
         if rc != 0:
             raise RuntimeError("slo_lod failed")
         return raw, cnt.value, tp.value

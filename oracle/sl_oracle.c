@@ -740,6 +740,14 @@ static double log_sum(double a, double b) {  /* logarithms.cc:14-25 */
 
 int slo_lod(const slo_problem* p, const int32_t* dgs, int n_dgs, double* raw, uint32_t* count,
             double* trait_prob) {
+    return slo_lod_ex(p, dgs, n_dgs, raw, count, trait_prob, 0);
+}
+
+/* zero_ok = 0: stop at a zero trait likelihood as Peeler::process does
+ * (peeler.cc:89-92).  zero_ok = 1: count it as a zero term of the log-sum
+ * (the value -DBL_MAX, which log_sum skips). */
+int slo_lod_ex(const slo_problem* p, const int32_t* dgs, int n_dgs, double* raw, uint32_t* count,
+               double* trait_prob, int zero_ok) {
     int K = p->K, M = p->M, n = p->n_lod, N = p->N;
     double** mat = (double**)calloc(K, sizeof(double*));
     for (int k = 0; k < K; ++k) mat[k] = (double*)calloc(ipow4(cut_len(p, k)), sizeof(double));
@@ -773,8 +781,8 @@ int slo_lod(const slo_problem* p, const int32_t* dgs, int n_dgs, double* raw, ui
                 t.th2 = p->partial[l] * (n + 1 - (o + 1));
                 t.an2 = 1.0 - t.th2;
                 double r = trait_peel(p, &t, mat, assign);
-                if (r <= 0.0) { rc = -1; goto out; }
-                double prob = log(r) - rec - marker_trans;
+                if (r <= 0.0 && !zero_ok) { rc = -1; goto out; }
+                double prob = r > 0.0 ? log(r) - rec - marker_trans : -DBL_MAX;
                 int idx = l * n + o;
                 raw[idx] = init[idx] ? log_sum(prob, raw[idx]) : prob;
                 init[idx] = 1;

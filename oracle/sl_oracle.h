@@ -61,6 +61,8 @@ int slo_msweep(const slo_problem* p, int32_t* dg, const int32_t* meioses, int n,
  * raw[(M-1)*n_lod] log-sum accumulators, the scored count and log P(T). */
 int slo_lod(const slo_problem* p, const int32_t* dgs, int n_dgs, double* raw, uint32_t* count,
             double* trait_prob);
+int slo_lod_ex(const slo_problem* p, const int32_t* dgs, int n_dgs, double* raw, uint32_t* count,
+               double* trait_prob, int zero_ok);
 
 /* Founder-allele-graph likelihood of one descent-graph column
  * (founder_allele_graph4.cc:34-442); 0.0 when the column is illegal. */

@@ -20,6 +20,7 @@ SL_OK, SL_EINVAL, SL_ECUDA, SL_EZERO, SL_EILLEGAL, SL_ENOMEM, SL_ENODEV = 0, -1,
 SL_LOD_FP64, SL_LOD_FP32_RESCALED = 0, 1
 SL_SAMPLER_EXACT, SL_SAMPLER_FAST = 0, 1
 SL_LOD_KERNEL_AUTO, SL_LOD_KERNEL_INTERP, SL_LOD_KERNEL_JIT_REG, SL_LOD_KERNEL_JIT_SMEM = 0, 1, 2, 3
+SL_LOD_ZERO_OK = 1
 
 EXPORTED = [
     "sl_create", "sl_destroy", "sl_last_error", "sl_set_descent_graphs", "sl_get_descent_graphs",
@@ -57,7 +58,7 @@ class ProblemDesc(ctypes.Structure):
 class Options(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int32), ("n_chains", ctypes.c_int32),
                 ("lod_precision", ctypes.c_int32), ("sampler_precision", ctypes.c_int32),
-                ("lod_kernel", ctypes.c_int32)]
+                ("lod_kernel", ctypes.c_int32), ("lod_flags", ctypes.c_int32)]
 
 
 class RunOptions(ctypes.Structure):
@@ -182,10 +183,11 @@ class Context:
     """A device context holding one problem and n_chains descent graphs."""
 
     def __init__(self, problem: Problem, n_chains: int = 1, lod_precision: int = SL_LOD_FP64,
-                 device: int = 0, sampler_precision: int = SL_SAMPLER_EXACT, lod_kernel: int = SL_LOD_KERNEL_AUTO):
+                 device: int = 0, sampler_precision: int = SL_SAMPLER_EXACT, lod_kernel: int = SL_LOD_KERNEL_AUTO,
+                 lod_flags: int = 0):
         self.problem = problem
         self._desc = problem.desc()
-        opt = Options(device, n_chains, lod_precision, sampler_precision, lod_kernel)
+        opt = Options(device, n_chains, lod_precision, sampler_precision, lod_kernel, lod_flags)
         h = _vp()
         rc = lib().sl_create(ctypes.byref(self._desc), ctypes.byref(opt), ctypes.byref(h))
         if rc != SL_OK:

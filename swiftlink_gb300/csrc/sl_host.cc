@@ -913,6 +913,7 @@ int sl_create(const sl_problem_desc* d, const sl_options* opt, sl_ctx** out) {
     if (N > 32000) return fail(ctx, SL_EINVAL, "pedigree too large (%d members)", N);
     if (d->sex_linked) return fail(ctx, SL_EINVAL, "sex-linked analysis is not supported on the GPU");
     if (opt->n_chains < 1) return fail(ctx, SL_EINVAL, "n_chains must be >= 1");
+    if (opt->lod_flags & ~SL_LOD_ZERO_OK) return fail(ctx, SL_EINVAL, "unknown lod_flags %#x", opt->lod_flags);
     if (opt->lod_precision != SL_LOD_FP64 && opt->lod_precision != SL_LOD_FP32_RESCALED)
         return fail(ctx, SL_EINVAL, "unknown lod_precision %d", opt->lod_precision);
     if (opt->sampler_precision != SL_SAMPLER_EXACT && opt->sampler_precision != SL_SAMPLER_FAST)
@@ -1010,6 +1011,7 @@ int sl_create(const sl_problem_desc* d, const sl_options* opt, sl_ctx** out) {
     P.max_child = max_child;
     P.fag_bytes = 0;
     P.marker_trans = std::log(0.5) * (2 * (N - F));
+    P.lod_zero_ok = (opt->lod_flags & SL_LOD_ZERO_OK) ? 1 : 0;
     if ((rc = upload(ctx, (int16_t**)&P.mother, mo.data(), N))) return bail(rc);
     if ((rc = upload(ctx, (int16_t**)&P.father, fa.data(), N))) return bail(rc);
     if ((rc = upload(ctx, (uint8_t**)&P.geno, geno.data(), geno.size()))) return bail(rc);
@@ -1103,7 +1105,7 @@ int sl_create(const sl_problem_desc* d, const sl_options* opt, sl_ctx** out) {
         ctx->lod_kernel_req = req;
         if (req != SL_LOD_KERNEL_INTERP) {
             const JitProgramIn in{prog.words.data(), prog.words.size(), prog.consts.data(), F, M, n,
-                                  P.W, N - F, prog.slots, P.marker_trans};
+                                  P.W, N - F, prog.slots, P.marker_trans, P.lod_zero_ok};
             const auto t0 = std::chrono::steady_clock::now();
             std::string log_reg, log_smem;
             int rc_reg = -1, rc_smem = -1;

@@ -48,6 +48,7 @@ struct ProblemDev {
     const float* pconst;                 // its constants
     int32_t prog_slots;                  // FP32 slots one task of the program needs
     int32_t prog_threads;                // threads per block of the program kernel
+    int32_t lod_zero_ok;                 // a zero trait likelihood is a zero term, not an error
 };
 
 // Instructions of a compiled trait-peel program (the batched LOD scorer).

@@ -178,9 +178,10 @@ std::string jit_source(const JitProgramIn& in, int threads, bool shared) {
     emitf(s, "    const double rec = cross * lt + (%d - cross) * la;\n", 2 * in.Nnf);
     s += "    double v;\n";
     emitf(s,
-          "    if (!(result > 0.0f)) { atomicCAS(status, 0, %d); v = -1.7976931348623157e308; }\n"
+          "    if (!(result > 0.0f)) { %s v = -1.7976931348623157e308; }\n"
           "    else v = log((double)result) + (double)scale * 0.69314718055994530942 - rec - (%.17g);\n",
-          (int)ST_LOD_NONPOS, in.marker_trans);
+          in.zero_ok ? "" : ("atomicCAS(status, 0, " + std::to_string((int)ST_LOD_NONPOS) + ");").c_str(),
+          in.marker_trans);
     s += "    vals[t] = v;\n  }\n}\n";
     return s;
 }

@@ -16,6 +16,7 @@ struct JitProgramIn {
     const float* consts;
     int F, M, n, W, Nnf, slots;
     double marker_trans;
+    int zero_ok;             // a zero trait likelihood is a zero term, not an error
 };
 
 struct JitLod {

@@ -1244,7 +1244,7 @@ __global__ void __launch_bounds__(128) lod_kernel(ProblemDev P, const uint32_t* 
             for (int bb = 0; bb < 2 * P.Nnf; ++bb) rec = DADD(rec, dgbit(colL, bb) != dgbit(colR, bb) ? lt : la);
             double v;
             if (r <= 0.0) {
-                set_status(status, ST_LOD_NONPOS);
+                if (!P.lod_zero_ok) set_status(status, ST_LOD_NONPOS);
                 v = -DBL_MAX;
             } else {
                 v = log(r) + (double)scale * 0.69314718055994530942 - rec - P.marker_trans;
@@ -1334,7 +1334,7 @@ __global__ void __launch_bounds__(128) lod_prog_kernel(ProblemDev P, const uint3
         const double rec = cross * lt + (2 * P.Nnf - cross) * la;
         double v;
         if (!(result > 0.f)) {
-            set_status(status, ST_LOD_NONPOS);
+            if (!P.lod_zero_ok) set_status(status, ST_LOD_NONPOS);
             v = -DBL_MAX;
         } else {
             v = log((double)result) + (double)scale * 0.69314718055994530942 - rec - P.marker_trans;
@@ -1433,8 +1433,8 @@ __global__ void __launch_bounds__(128) trait_adjoint_kernel(ProblemDev P, AdjDev
     double acc[6] = {0, 0, 0, 0, 0, 0};
     const float root = res >= 0 ? a[res * stride] : 0.f;
     if (!(root > 0.f)) {
-        set_status(status, ST_LOD_NONPOS);
-        for (int k = 0; k < 6; ++k) grad[u * 6 + k] = 0.0;
+        if (!P.lod_zero_ok) set_status(status, ST_LOD_NONPOS);
+        for (int k = 0; k < 6; ++k) grad[u * 6 + k] = __longlong_as_double(0x7ff8000000000000LL);   // NaN
         return;
     }
     g[res * stride] = 1.0f / root;

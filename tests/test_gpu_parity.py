@@ -286,29 +286,72 @@ def test_batched_lod_kernels_against_reference(name, kernel):
     assert np.abs(got - want).max() <= FP32_LOD_TOL
 
 
+_LARGE = {}
+
+
+def large_pedigree_graphs():
+    """The 120-member, 2000-SNP pedigree and four seeded graphs (the starting
+    graph after 0-3 oracle L-sweeps) with the oracle's FP64 LOD of the set.
+    Under the fully penetrant recessive model the second sweep's graph has
+    positions of zero trait likelihood; the LOD counts them as zero terms."""
+    if not _LARGE:
+        from swiftlink_gb300.workloads import load_problem
+        d = load_problem("cfg2")
+        d["trait_prior"] = port.derive_priors(d["genotypes"], d["typed"], d["minor"])
+        P = port.Port(d)
+        rng = np.random.default_rng(31)
+        st = d["K"] + 2 * d["N"]
+        graphs = [d["dg0"].copy()]
+        for _ in range(3):
+            dg = graphs[-1].copy()
+            u = rng.random((d["M"], st))
+            for l in list(range(0, d["M"], 2)) + list(range(1, d["M"], 2)):
+                dg, _ = P.lstep(dg, l, u[l])
+            graphs.append(dg)
+        graphs = np.stack(graphs)
+        _LARGE.update(d=d, graphs=graphs, ref=P.lod(graphs, zero_ok=True))
+    return _LARGE["d"], _LARGE["graphs"], _LARGE["ref"]
+
+
 @pytest.mark.parametrize("kernel", LOD_KERNELS)
 def test_batched_lod_kernels_large_pedigree(kernel):
-    """The 120-member, 2000-SNP pedigree: four seeded graphs (the starting
-    graph after 0-3 L-sweeps from the oracle) scored by each kernel, against
-    the oracle's FP64 LOD."""
-    from swiftlink_gb300.workloads import load_problem
-    d = load_problem("cfg2")
-    P = port.Port(d)
-    rng = np.random.default_rng(31)
-    st = d["K"] + 2 * d["N"]
-    graphs = [d["dg0"].copy()]
-    for _ in range(3):
-        dg = graphs[-1].copy()
-        u = rng.random((d["M"], st))
-        for l in list(range(0, d["M"], 2)) + list(range(1, d["M"], 2)):
-            dg, _ = P.lstep(dg, l, u[l])
-        graphs.append(dg)
-    graphs = np.stack(graphs)
-    ref_raw, ref_cnt, ref_tp = P.lod(graphs)
+    """Each batched kernel on the 120-member, 2000-SNP pedigree against the
+    oracle's FP64 LOD, |dLOD| <= 1e-3, zero-likelihood positions counted as
+    zero terms (SL_LOD_ZERO_OK)."""
+    d, graphs, (ref_raw, ref_cnt, ref_tp) = large_pedigree_graphs()
     with api.Context(api.Problem.from_arrays(d), n_chains=1, lod_precision=api.SL_LOD_FP32_RESCALED,
-                     lod_kernel=kernel) as ctx:
+                     lod_kernel=kernel, lod_flags=api.SL_LOD_ZERO_OK) as ctx:
         ctx.lod_score_graphs(graphs)
         raw, cnt, tp = ctx.lod_results()
     assert cnt == ref_cnt
     err = np.abs(api.lod_table(raw, cnt, tp) - api.lod_table(ref_raw, ref_cnt, ref_tp)).max()
     assert err <= FP32_LOD_TOL, err
+
+
+@pytest.mark.parametrize("precision", [api.SL_LOD_FP64, api.SL_LOD_FP32_RESCALED])
+def test_zero_trait_likelihood_policy(precision):
+    """A graph with zero-likelihood positions: by default the scoring reports
+    SL_EZERO (the reference exits there, peeler.cc:89-92) and the context stays
+    usable; with SL_LOD_ZERO_OK the FP64 table equals the oracle's with those
+    positions counted as zero terms."""
+    d, graphs, (ref_raw, ref_cnt, ref_tp) = large_pedigree_graphs()
+    P = port.Port(d)
+    bad = graphs[2:3]
+    with pytest.raises(RuntimeError):
+        P.lod(bad)
+    prob = api.Problem.from_arrays(d)
+    with api.Context(prob, n_chains=1, lod_precision=precision) as ctx:
+        with pytest.raises(api.SwiftLinkError) as e:
+            ctx.lod_score_graphs(bad)
+        assert e.value.code == api.SL_EZERO
+        ctx.lod_reset()
+        ctx.lod_score_graphs(graphs[:1])
+        raw, cnt, tp = ctx.lod_results()
+    want_raw, want_cnt, want_tp = P.lod(graphs[:1])
+    tol = FP64_LOD_TOL if precision == api.SL_LOD_FP64 else FP32_LOD_TOL
+    assert np.abs(api.lod_table(raw, cnt, tp) - api.lod_table(want_raw, want_cnt, want_tp)).max() <= tol
+    with api.Context(prob, n_chains=1, lod_precision=precision, lod_flags=api.SL_LOD_ZERO_OK) as ctx:
+        ctx.lod_score_graphs(graphs)
+        raw, cnt, tp = ctx.lod_results()
+    assert cnt == ref_cnt
+    assert np.abs(api.lod_table(raw, cnt, tp) - api.lod_table(ref_raw, ref_cnt, ref_tp)).max() <= tol
