@@ -328,19 +328,21 @@ def test_batched_lod_kernels_large_pedigree(kernel):
     assert err <= FP32_LOD_TOL, err
 
 
-@pytest.mark.parametrize("precision", [api.SL_LOD_FP64, api.SL_LOD_FP32_RESCALED])
-def test_zero_trait_likelihood_policy(precision):
-    """A graph with zero-likelihood positions: by default the scoring reports
-    SL_EZERO (the reference exits there, peeler.cc:89-92) and the context stays
-    usable; with SL_LOD_ZERO_OK the FP64 table equals the oracle's with those
-    positions counted as zero terms."""
+def test_zero_trait_likelihood_policy():
+    """The third graph of the set has two positions whose FP64 trait
+    likelihood, peeled without rescaling as the reference does, underflows to
+    0.  The plain FP64 scorer reports SL_EZERO by default (the reference exits
+    there, peeler.cc:89-92) and the context stays usable; with SL_LOD_ZERO_OK
+    its table equals the oracle's with those positions counted as zero terms.
+    The FP32 scorer rescales every rfunction, does not underflow, and scores
+    the graph without error."""
     d, graphs, (ref_raw, ref_cnt, ref_tp) = large_pedigree_graphs()
     P = port.Port(d)
     bad = graphs[2:3]
     with pytest.raises(RuntimeError):
         P.lod(bad)
     prob = api.Problem.from_arrays(d)
-    with api.Context(prob, n_chains=1, lod_precision=precision) as ctx:
+    with api.Context(prob, n_chains=1, lod_precision=api.SL_LOD_FP64) as ctx:
         with pytest.raises(api.SwiftLinkError) as e:
             ctx.lod_score_graphs(bad)
         assert e.value.code == api.SL_EZERO
@@ -348,10 +350,13 @@ def test_zero_trait_likelihood_policy(precision):
         ctx.lod_score_graphs(graphs[:1])
         raw, cnt, tp = ctx.lod_results()
     want_raw, want_cnt, want_tp = P.lod(graphs[:1])
-    tol = FP64_LOD_TOL if precision == api.SL_LOD_FP64 else FP32_LOD_TOL
-    assert np.abs(api.lod_table(raw, cnt, tp) - api.lod_table(want_raw, want_cnt, want_tp)).max() <= tol
-    with api.Context(prob, n_chains=1, lod_precision=precision, lod_flags=api.SL_LOD_ZERO_OK) as ctx:
+    assert np.abs(api.lod_table(raw, cnt, tp) - api.lod_table(want_raw, want_cnt, want_tp)).max() <= FP64_LOD_TOL
+    with api.Context(prob, n_chains=1, lod_precision=api.SL_LOD_FP64, lod_flags=api.SL_LOD_ZERO_OK) as ctx:
         ctx.lod_score_graphs(graphs)
         raw, cnt, tp = ctx.lod_results()
     assert cnt == ref_cnt
-    assert np.abs(api.lod_table(raw, cnt, tp) - api.lod_table(ref_raw, ref_cnt, ref_tp)).max() <= tol
+    assert np.abs(api.lod_table(raw, cnt, tp) - api.lod_table(ref_raw, ref_cnt, ref_tp)).max() <= FP64_LOD_TOL
+    with api.Context(prob, n_chains=1, lod_precision=api.SL_LOD_FP32_RESCALED) as ctx:
+        ctx.lod_score_graphs(bad)
+        raw32, _, _ = ctx.lod_results()
+    assert np.all(np.isfinite(raw32)) and raw32.min() > -1e300
