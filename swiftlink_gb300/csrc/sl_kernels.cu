@@ -929,17 +929,46 @@ __device__ __forceinline__ int map_compose(int x, int y) {
     return ((x >> y0) & 1) | (((x >> y1) & 1) << 1);
 }
 
-__global__ void __launch_bounds__(32) ffbs_scan_kernel(ProblemDev P, uint32_t* dg, int first, int nchain,
-                                                       const int32_t* order, int64_t ostride, int step,
-                                                       Draws draws, const uint8_t* sel, int want,
-                                                       const uint8_t* badc, const float* raw32, float* fbbuf,
-                                                       uint8_t* mapbuf, int staged) {
+// Block-wide scan scratch of ffbs_scan_kernel (blockDim.x = T, a multiple of 32, <= 1024).
+struct ScanScratch {
+    float4* incl;   // [T] each thread's inclusive filter product
+    float4* wmat;   // [32] warp products, then their inclusive scan
+    int* wcnt;      // [32] draws per warp
+    int* wmap;      // [33] warp decision maps, then their suffix compositions
+};
+
+__device__ __forceinline__ void mat_mul_left(float& p00, float& p01, float& p10, float& p11, float o00, float o01,
+                                             float o10, float o11) {
+    // p <- p * o (o is the earlier product, applied first)
+    const float n00 = p00 * o00 + p01 * o10, n01 = p00 * o01 + p01 * o11;
+    const float n10 = p10 * o00 + p11 * o10, n11 = p10 * o01 + p11 * o11;
+    p00 = n00; p01 = n01; p10 = n10; p11 = n11;
+}
+
+// Fast-mode forward filter and backward sampling of one meiosis over all loci,
+// one block per chain (meiosis_sampler.cc:123-203 restated as scans): each
+// thread owns a run of L = ceil(M / T) loci.
+//   forward:  the filter is a product of 2x2 matrices A_i = diag(r_i) R(theta_i);
+//             chunk products are scanned across the block (later chunks on the
+//             left, normalised to a maximum of 1), and each chunk then filters
+//             its loci from the vector entering it;
+//   backward: loci draw from M-1 down, a locus drawing when both filtered
+//             entries are non-zero; a suffix sum of the chunks' draw counts
+//             gives each chunk its first draw, so all draws are generated in
+//             parallel; each locus's choice given the locus above is a 2-bit
+//             map, and a suffix composition of the chunks' maps gives each
+//             chunk the state entering it from above.
+__global__ void __launch_bounds__(1024) ffbs_scan_kernel(ProblemDev P, uint32_t* dg, int first, int nchain,
+                                                         const int32_t* order, int64_t ostride, int step,
+                                                         Draws draws, const uint8_t* sel, int want,
+                                                         const uint8_t* badc, const float* raw32, float* fbbuf,
+                                                         uint8_t* mapbuf, int staged) {
     extern __shared__ __align__(16) unsigned char fsm[];
     const int cr = blockIdx.x;
     if (cr >= nchain) return;
     if (sel && sel[cr] != want) return;
     if (badc[cr]) return;
-    const int lane = threadIdx.x;
+    const int T = blockDim.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = T >> 5;
     const int chain = first + cr;
     const int m = order[cr * ostride + step];
     const int M = P.M;
@@ -947,28 +976,33 @@ __global__ void __launch_bounds__(32) ffbs_scan_kernel(ProblemDev P, uint32_t* d
     const float* r = raw32 + (size_t)cr * 2 * M;
     float* fb = fbbuf + (size_t)cr * 2 * M;
     uint8_t* maps = mapbuf + (size_t)cr * M;
-    float* th = nullptr;  // theta as floats, [M]
+    float* th = nullptr;        // theta as floats, [M]
     uint32_t* words = nullptr;  // the meiosis's descent-graph word at each locus, [M]
+    ScanScratch sc;
+    sc.incl = (float4*)fsm;
+    sc.wmat = sc.incl + T;
+    sc.wcnt = (int*)(sc.wmat + 32);
+    sc.wmap = sc.wcnt + 32;
+    unsigned char* stage = (unsigned char*)(sc.wmap + 36);
     if (staged) {
-        // stage the chain's pairs, theta and the meiosis's words in shared memory with
-        // coalesced / independent loads: [r: 2M][fb: 2M][theta: M] floats, [words: M], [maps: M bytes]
-        float* sr = (float*)fsm;
+        // [r: 2M][fb: 2M][theta: M] floats, [words: M], [maps: M bytes]
+        float* sr = (float*)stage;
         float* sfb = sr + 2 * M;
         th = sfb + 2 * M;
         words = (uint32_t*)(th + M);
         uint8_t* smaps = (uint8_t*)(words + M);
-        for (int i = lane; i < M; i += 32) words[i] = G[(size_t)i * P.W + (m >> 5)];
-        for (int i = lane; i < 2 * M; i += 32) sr[i] = r[i];
-        for (int i = lane; i < M; i += 32) th[i] = i > 0 ? (float)P.theta[i - 1] : 0.f;
-        __syncwarp();
+        for (int i = tid; i < M; i += T) words[i] = G[(size_t)i * P.W + (m >> 5)];
+        for (int i = tid; i < 2 * M; i += T) sr[i] = r[i];
+        for (int i = tid; i < M; i += T) th[i] = i > 0 ? (float)P.theta[i - 1] : 0.f;
         r = sr;
         fb = sfb;
         maps = smaps;
     }
+    __syncthreads();
     auto tof = [&](int i) { return th ? th[i] : (i > 0 ? (float)P.theta[i - 1] : 0.f); };
-    const int L = (M + 31) / 32;
-    const int s0 = min(M, lane * L), s1 = min(M, s0 + L);
-    // chunk product P = A_{s1-1} ... A_{s0}, A_i = diag(r_i) [[1-t, t], [t, 1-t]] (A_0 = diag(r_0))
+    const int L = (M + T - 1) / T;
+    const int s0 = min(M, tid * L), s1 = min(M, s0 + L);
+    // chunk product P = A_{s1-1} ... A_{s0} (A_0 = diag(r_0)); an empty chunk is the identity
     float p00 = 1.f, p01 = 0.f, p10 = 0.f, p11 = 1.f;
     for (int i = s0; i < s1; ++i) {
         const float q0 = r[2 * i], q1 = r[2 * i + 1];
@@ -980,22 +1014,46 @@ __global__ void __launch_bounds__(32) ffbs_scan_kernel(ProblemDev P, uint32_t* d
         if (((i - s0) & 7) == 7) mat_norm(p00, p01, p10, p11);
     }
     mat_norm(p00, p01, p10, p11);
-    // inclusive scan S_k = P_k ... P_0 (later chunks multiply on the left)
+    // inclusive scan within the warp: S_k = P_k ... P_first
     for (int d = 1; d < 32; d <<= 1) {
         const float o00 = __shfl_up_sync(FULLMASK, p00, d), o01 = __shfl_up_sync(FULLMASK, p01, d);
         const float o10 = __shfl_up_sync(FULLMASK, p10, d), o11 = __shfl_up_sync(FULLMASK, p11, d);
         if (lane >= d) {
-            const float n00 = p00 * o00 + p01 * o10, n01 = p00 * o01 + p01 * o11;
-            const float n10 = p10 * o00 + p11 * o10, n11 = p10 * o01 + p11 * o11;
-            p00 = n00; p01 = n01; p10 = n10; p11 = n11;
+            mat_mul_left(p00, p01, p10, p11, o00, o01, o10, o11);
             mat_norm(p00, p01, p10, p11);
         }
     }
+    if (lane == 31) sc.wmat[warp] = make_float4(p00, p01, p10, p11);
+    __syncthreads();
+    if (warp == 0) {
+        // inclusive scan of the warp products (nw <= 32)
+        float4 w = lane < nw ? sc.wmat[lane] : make_float4(1.f, 0.f, 0.f, 1.f);
+        for (int d = 1; d < 32; d <<= 1) {
+            const float o00 = __shfl_up_sync(FULLMASK, w.x, d), o01 = __shfl_up_sync(FULLMASK, w.y, d);
+            const float o10 = __shfl_up_sync(FULLMASK, w.z, d), o11 = __shfl_up_sync(FULLMASK, w.w, d);
+            if (lane >= d) {
+                mat_mul_left(w.x, w.y, w.z, w.w, o00, o01, o10, o11);
+                mat_norm(w.x, w.y, w.z, w.w);
+            }
+        }
+        __syncwarp();
+        if (lane < nw) sc.wmat[lane] = w;
+    }
+    __syncthreads();
+    if (warp > 0) {
+        const float4 o = sc.wmat[warp - 1];
+        mat_mul_left(p00, p01, p10, p11, o.x, o.y, o.z, o.w);
+        mat_norm(p00, p01, p10, p11);
+    }
+    sc.incl[tid] = make_float4(p00, p01, p10, p11);
+    __syncthreads();
     // vector entering the chunk: S_{k-1} (1, 1)
-    const float e00 = __shfl_up_sync(FULLMASK, p00, 1), e01 = __shfl_up_sync(FULLMASK, p01, 1);
-    const float e10 = __shfl_up_sync(FULLMASK, p10, 1), e11 = __shfl_up_sync(FULLMASK, p11, 1);
     float v0 = 1.f, v1 = 1.f;
-    if (lane > 0) { v0 = e00 + e01; v1 = e10 + e11; }
+    if (tid > 0) {
+        const float4 e = sc.incl[tid - 1];
+        v0 = e.x + e.y;
+        v1 = e.z + e.w;
+    }
     int cnt = 0;
     for (int i = s0; i < s1; ++i) {
         const float q0 = r[2 * i], q1 = r[2 * i + 1];
@@ -1012,16 +1070,16 @@ __global__ void __launch_bounds__(32) ffbs_scan_kernel(ProblemDev P, uint32_t* d
         v0 = f0;
         v1 = f1;
     }
-    // draws: loci are visited from M-1 down; a locus draws when both entries are non-zero
-    int above = 0;  // draws consumed by loci in higher chunks
-    {
-        int x = cnt;
-        for (int d = 1; d < 32; d <<= 1) {
-            const int y = __shfl_down_sync(FULLMASK, x, d);
-            if (lane + d < 32) x += y;
-        }
-        above = x - cnt;
+    // draws consumed by loci in higher chunks: a suffix sum over the block
+    int x = cnt;
+    for (int d = 1; d < 32; d <<= 1) {
+        const int y = __shfl_down_sync(FULLMASK, x, d);
+        if (lane + d < 32) x += y;
     }
+    if (lane == 0) sc.wcnt[warp] = x;
+    __syncthreads();
+    int above = x - cnt;
+    for (int w = warp + 1; w < nw; ++w) above += sc.wcnt[w];
     // per-locus decision maps and the chunk's composed map; the chunk's draws are
     // independent of one another, so they are generated four at a time
     int gmap = 2;  // identity: bit0 = 0, bit1 = 1
@@ -1056,14 +1114,31 @@ __global__ void __launch_bounds__(32) ffbs_scan_kernel(ProblemDev P, uint32_t* d
         maps[i] = (uint8_t)dmap;
         gmap = map_compose(dmap, gmap);
     }
-    // suffix composition over chunks: x_k = G_k o G_{k+1} o ... o G_31
-    int x = gmap;
+    // suffix composition x_k = G_k o G_{k+1} o ... o G_{T-1}: within the warp,
+    // then across warps
+    int xm = gmap;
     for (int d = 1; d < 32; d <<= 1) {
-        const int y = __shfl_down_sync(FULLMASK, x, d);
-        if (lane + d < 32) x = map_compose(x, y);
+        const int y = __shfl_down_sync(FULLMASK, xm, d);
+        if (lane + d < 32) xm = map_compose(xm, y);
     }
-    const int above_map = __shfl_down_sync(FULLMASK, x, 1);
-    int sv = lane < 31 ? (above_map & 1) : 0;  // constant: the top chunk holds locus M-1
+    if (lane == 0) sc.wmap[warp] = xm;
+    __syncthreads();
+    if (tid == 0) {
+        int acc = 2;
+        sc.wmap[nw] = 2;
+        for (int w = nw - 1; w >= 0; --w) {
+            acc = map_compose(sc.wmap[w], acc);
+            sc.wmap[w] = acc;     // warp w's maps composed with every warp above it
+        }
+    }
+    __syncthreads();
+    // the state entering this chunk from above: x_{k+1} applied to anything
+    // (the chunk holding locus M-1 ends in a constant map)
+    const int tail = sc.wmap[warp + 1];
+    const int full = map_compose(xm, tail);
+    int above_map = __shfl_down_sync(FULLMASK, full, 1);
+    if (lane == 31) above_map = tail;
+    int sv = above_map & 1;
     for (int i = s1 - 1; i >= s0; --i) {
         sv = (maps[i] >> sv) & 1;
         uint32_t* wp = G + (size_t)i * P.W + (m >> 5);
@@ -1073,7 +1148,15 @@ __global__ void __launch_bounds__(32) ffbs_scan_kernel(ProblemDev P, uint32_t* d
     }
 }
 
-size_t ffbs_scan_smem(int M) { return (size_t)6 * 4 * M + (size_t)M + 16; }
+// Threads per chain of ffbs_scan_kernel: runs of about 8 loci.
+int ffbs_scan_threads(int M) {
+    int t = ((M + 7) / 8 + 31) / 32 * 32;
+    return t < 32 ? 32 : (t > 1024 ? 1024 : t);
+}
+
+// Shared bytes: the scan scratch, then (when staged) the chain's arrays.
+size_t ffbs_scan_scratch(int T) { return (size_t)16 * T + 16 * 32 + 4 * 32 + 4 * 36; }
+size_t ffbs_scan_smem(int M) { return ffbs_scan_scratch(ffbs_scan_threads(M)) + (size_t)6 * 4 * M + (size_t)M + 16; }
 
 // ---------------------------------------------------------------------------
 // Trait peel LOD scorer: one warp per (graph, interval, position).
@@ -1610,8 +1693,13 @@ static cudaError_t launch_msampler_t(const ProblemDev& P, uint32_t* dg, int firs
         configured = smem;
     }
     Draws d{u, ucs, P.M, seed, iter, 2};
+    const int scan_threads = ffbs_scan_threads(P.M);
     size_t scan_smem = ffbs_scan_smem(P.M);
-    if (scan_smem > 200 * 1024) scan_smem = 0;  // long maps: read the chain's arrays from global memory
+    int staged = 1;
+    if (scan_smem > 200 * 1024) {   // long maps: read the chain's arrays from global memory
+        scan_smem = ffbs_scan_scratch(scan_threads);
+        staged = 0;
+    }
     static size_t scan_configured = 0;
     if (scan_smem > scan_configured) {
         cudaError_t e = cudaFuncSetAttribute(ffbs_scan_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)scan_smem);
@@ -1631,8 +1719,8 @@ static cudaError_t launch_msampler_t(const ProblemDev& P, uint32_t* dg, int firs
             ffbs_kernel<double><<<nchain, 32, 0, s>>>(P, dg, first, nchain, meioses, mstride, j, d, sel, want, badc,
                                                       (const double*)raw, nullptr, (double*)fb);
         else
-            ffbs_scan_kernel<<<nchain, 32, scan_smem, s>>>(P, dg, first, nchain, meioses, mstride, j, d, sel, want,
-                                                           badc, raw32, (float*)fb, maps, scan_smem > 0);
+            ffbs_scan_kernel<<<nchain, scan_threads, scan_smem, s>>>(P, dg, first, nchain, meioses, mstride, j, d, sel,
+                                                                     want, badc, raw32, (float*)fb, maps, staged);
     }
     return cudaGetLastError();
 }
