@@ -990,6 +990,24 @@ int sl_create(const sl_problem_desc* d, const sl_options* opt, sl_ctx** out) {
             if (order.size() == before) return bail(fail(nullptr, SL_EINVAL, "pedigree has a cycle"));
         }
     }
+    // generation levels: a person one level below its deeper parent
+    std::vector<int16_t> lvl_order;
+    std::vector<int32_t> lvl_off;
+    {
+        std::vector<int> lvl(N, 0);
+        int top = 0;
+        for (int16_t i : order)
+            if (i >= F) {
+                lvl[i] = 1 + std::max(lvl[d->mother[i]], lvl[d->father[i]]);
+                top = std::max(top, lvl[i]);
+            }
+        for (int k = 0; k <= top; ++k) {
+            lvl_off.push_back((int32_t)lvl_order.size());
+            for (int i = 0; i < N; ++i)
+                if (lvl[i] == k) lvl_order.push_back((int16_t)i);
+        }
+        lvl_off.push_back((int32_t)lvl_order.size());
+    }
     // non-ignorable meioses (markov_chain.cc:70-80, Person::safe_to_ignore_meiosis person.cc:208-222)
     {
         std::vector<int> nchild(N, 0);
@@ -1025,6 +1043,9 @@ int sl_create(const sl_problem_desc* d, const sl_options* opt, sl_ctx** out) {
     if ((rc = upload(ctx, (OpDev**)&P.ops, ops.data(), K))) return bail(rc);
     if ((rc = upload(ctx, (int32_t**)&P.opdata, od.data(), od.size()))) return bail(rc);
     if ((rc = upload(ctx, (int16_t**)&P.fag_order, order.data(), N))) return bail(rc);
+    if ((rc = upload(ctx, (int16_t**)&P.lvl_order, lvl_order.data(), N))) return bail(rc);
+    if ((rc = upload(ctx, (int32_t**)&P.lvl_off, lvl_off.data(), lvl_off.size()))) return bail(rc);
+    P.n_lvl = (int32_t)lvl_off.size() - 1;
 
     // ---- launch shapes from the shared-memory footprint of one task
     const size_t lsw = lsampler_smem_per_warp(P);

@@ -44,6 +44,9 @@ struct ProblemDev {
     const OpDev* ops;                    // [K]
     const int32_t* opdata;
     const int16_t* fag_order;            // [N] parents before children, founders first
+    const int16_t* lvl_order;            // [N] persons by generation level (founders = level 0)
+    const int32_t* lvl_off;              // [n_lvl + 1] start of each level in lvl_order
+    int32_t n_lvl;
     const int32_t* prog;                 // compiled trait peel (LI_* words), or null
     const float* pconst;                 // its constants
     int32_t prog_slots;                  // FP32 slots one task of the program needs

@@ -794,6 +794,202 @@ __global__ void __launch_bounds__(128) fag_kernel(ProblemDev P, uint32_t* dg, in
     }
 }
 
+// ---------------------------------------------------------------------------
+// Fast-mode founder-allele-graph likelihood, one warp per (chain, locus).
+// The likelihood of the genotypes given the column's founder-allele graph
+// (FounderAlleleGraph4::likelihood, founder_allele_graph4.cc:34-442) is the
+// product over the connected components of the heterozygote edges of the sum,
+// over the component's two colourings (allele A = major, B = minor) that
+// satisfy every homozygote's fixed alleles, of the product of the founder
+// alleles' frequencies.  Here:
+//   1. the founder allele of every person's two alleles is propagated one
+//      generation level at a time, the lanes splitting a level's persons;
+//   2. typed persons mark their founder alleles used / fixed A / fixed B
+//      (shared-memory atomicOr) and a heterozygote on one founder allele is a
+//      zero likelihood;
+//   3. components with the parity of each allele to the component's smallest
+//      allele come from min-label propagation over the heterozygote edges plus
+//      pointer jumping (labels packed as 2 * label + parity, only ever
+//      lowered, so the result is the same whatever the interleaving); an edge
+//      whose endpoints end with equal parity closes an odd cycle: zero;
+//   4. each lane sums its components' colourings in log2 in a fixed order and
+//      a butterfly sum over the warp gives log2 of the likelihood.
+// ---------------------------------------------------------------------------
+constexpr int kFagWarpsPerBlock = 8;
+
+__host__ __device__ inline size_t fagw_tables(int N) { return ((size_t)N * 7 + 15) & ~(size_t)15; }
+__host__ __device__ inline size_t fagw_warp_bytes(int N, int F) {
+    return (((size_t)4 * N + 15) & ~(size_t)15) + (size_t)2 * F * 8;
+}
+size_t fagw_block_bytes(int N, int F) { return fagw_tables(N) + kFagWarpsPerBlock * fagw_warp_bytes(N, F); }
+
+__global__ void __launch_bounds__(kFagWarpsPerBlock * 32) fag_warp_kernel(ProblemDev P, uint32_t* dg, int first,
+                                                                         int nchain, const int32_t* order,
+                                                                         int64_t ostride, int step, const uint8_t* sel,
+                                                                         int want, float* rawbuf, float* raw32,
+                                                                         uint8_t* badc, int* status) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int N = P.N, F = P.F, nfa = 2 * F, M = P.M;
+    int16_t* s_lvl = (int16_t*)smem;
+    int16_t* s_mo = s_lvl + N;
+    int16_t* s_fa = s_mo + N;
+    uint8_t* s_typed = (uint8_t*)(s_fa + N);
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+        s_lvl[i] = P.lvl_order[i];
+        s_mo[i] = P.mother[i];
+        s_fa[i] = P.father[i];
+        s_typed[i] = P.typed[i];
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+    unsigned char* wbase = smem + fagw_tables(N) + (size_t)warp * fagw_warp_bytes(N, F);
+    uint16_t* e = (uint16_t*)wbase;                                   // [2N] founder allele of each allele
+    volatile int* Lb = (volatile int*)(wbase + (((size_t)4 * N + 15) & ~(size_t)15));   // [2F] 2 * label + parity
+    int* fl = (int*)(Lb + nfa);                                       // [2F] bit0 used, bit1 fixed A, bit2 fixed B
+    const int64_t ntask = (int64_t)nchain * M;
+    for (int64_t t = (int64_t)blockIdx.x * wpb + warp; t < ntask; t += (int64_t)gridDim.x * wpb) {
+        const int cr = (int)(t / M);
+        const int l = (int)(t % M);
+        if (sel && sel[cr] != want) continue;
+        const int chain = first + cr;
+        const uint32_t* col = dg + ((size_t)chain * M + l) * P.W;
+        const int32_t* ord = order + cr * ostride;
+        float* raw = rawbuf + (size_t)cr * 2 * M;
+        const uint8_t* gcol = P.geno + (size_t)l * N;
+        int flip = -1, tb = 0;
+        float keep = 0.f;
+        if (step >= 0) {
+            const int m = ord[step];
+            const int last = ord[step > 0 ? step - 1 : 0];
+            tb = dgbit(col, m);
+            keep = raw[2 * l + dgbit(col, last)];
+            flip = m;
+        }
+        // 1. founder alleles, one generation level at a time
+        for (int q = lane; q < P.lvl_off[1]; q += 32) {
+            const int pid = s_lvl[q];
+            e[2 * pid] = (uint16_t)(2 * pid);
+            e[2 * pid + 1] = (uint16_t)(2 * pid + 1);
+        }
+        __syncwarp();
+        for (int k = 1; k < P.n_lvl; ++k) {
+            for (int q = P.lvl_off[k] + lane; q < P.lvl_off[k + 1]; q += 32) {
+                const int pid = s_lvl[q];
+                const int b = 2 * (pid - F);
+                const int vm = dgbit(col, b) ^ (flip == b);
+                const int vp = dgbit(col, b + 1) ^ (flip == b + 1);
+                e[2 * pid] = e[2 * s_mo[pid] + vm];
+                e[2 * pid + 1] = e[2 * s_fa[pid] + vp];
+            }
+            __syncwarp();
+        }
+        // 2. used / fixed founder alleles
+        for (int x = lane; x < nfa; x += 32) {
+            Lb[x] = x << 1;
+            fl[x] = 0;
+        }
+        __syncwarp();
+        int bad = 0, nab = 0;
+        for (int i = lane; i < N; i += 32) {
+            if (!s_typed[i]) continue;
+            const int g = gcol[i] & 3;
+            if (g == G_UNTYPED) continue;
+            const int u = e[2 * i], v = e[2 * i + 1];
+            if (g == G_HETERO) {
+                if (u == v) bad = 1;
+                atomicOr(&fl[u], 1);
+                atomicOr(&fl[v], 1);
+                ++nab;
+            } else {
+                const int bits = 1 | (g == G_HOMOZ_A ? 2 : 4);
+                atomicOr(&fl[u], bits);
+                atomicOr(&fl[v], bits);
+            }
+        }
+        bad = __any_sync(FULLMASK, bad);
+        // 3. components of the heterozygote edges with parities
+        if (!bad && __any_sync(FULLMASK, nab)) {
+            while (true) {
+                int ch = 0;
+                for (int i = lane; i < N; i += 32) {
+                    if (!s_typed[i] || (gcol[i] & 3) != G_HETERO) continue;
+                    const int u = e[2 * i], v = e[2 * i + 1];
+                    const int a = Lb[u], b = Lb[v];
+                    if ((a ^ 1) < b) { atomicMin((int*)&Lb[v], a ^ 1); ch = 1; }
+                    if ((b ^ 1) < a) { atomicMin((int*)&Lb[u], b ^ 1); ch = 1; }
+                }
+                __syncwarp();
+                for (int x = lane; x < nfa; x += 32) {
+                    const int a = Lb[x], r = a >> 1;
+                    if (r != x) {
+                        const int b = Lb[r];
+                        const int nv = (b & ~1) | ((a ^ b) & 1);
+                        if (nv < a) { atomicMin((int*)&Lb[x], nv); ch = 1; }
+                    }
+                }
+                __syncwarp();
+                if (!__any_sync(FULLMASK, ch)) break;
+            }
+            for (int i = lane; i < N; i += 32) {
+                if (!s_typed[i] || (gcol[i] & 3) != G_HETERO) continue;
+                if ((Lb[e[2 * i]] ^ Lb[e[2 * i + 1]]) != 1) bad = 1;   // same label, parities must differ
+            }
+            bad = __any_sync(FULLMASK, bad);
+        }
+        // 4. sum over each component's colourings, log2
+        float lk = -INFINITY;
+        if (!bad) {
+            const double minor_d = P.minor[l];
+            const float lmaj = log2f((float)(1.0 - minor_d)), lmin = log2f((float)minor_d);
+            float sum = 0.f;
+            int zero = 0;
+            for (int x = lane; x < nfa; x += 32) {
+                if (!(fl[x] & 1) || Lb[x] != (x << 1)) continue;
+                float w0 = 0.f, w1 = 0.f;
+                int ok0 = 1, ok1 = 1;
+                for (int y = x; y < nfa; ++y) {
+                    const int ly = Lb[y], f = fl[y];
+                    if ((ly >> 1) != x || !(f & 1)) continue;
+                    const int p = ly & 1;
+                    w0 += p ? lmin : lmaj;   // root coloured A: this allele is A unless its parity is odd
+                    w1 += p ? lmaj : lmin;
+                    if (f & 2) { if (p) ok0 = 0; else ok1 = 0; }
+                    if (f & 4) { if (p) ok1 = 0; else ok0 = 0; }
+                }
+                if (ok0 && ok1) {
+                    const float mx = fmaxf(w0, w1);
+                    sum += mx + log2f(1.f + exp2f(fminf(w0, w1) - mx));
+                } else if (ok0) sum += w0;
+                else if (ok1) sum += w1;
+                else zero = 1;
+            }
+            zero = __any_sync(FULLMASK, zero);
+            for (int dd = 16; dd >= 1; dd >>= 1) sum += __shfl_xor_sync(FULLMASK, sum, dd);
+            lk = zero ? -INFINITY : sum;
+        }
+        if (lane == 0) {
+            if (step < 0) {
+                raw[2 * l + dgbit(col, ord[0])] = lk;
+                if (lk == -INFINITY) {
+                    badc[cr] = 1;
+                    set_status(status, ST_ILLEGAL_DG);
+                }
+            } else {
+                raw[2 * l + tb] = keep;
+                raw[2 * l + 1 - tb] = lk;
+                float* r32 = raw32 + (size_t)cr * 2 * M;
+                if (tb == 0) put_raw32_log2(r32, l, keep, lk);
+                else put_raw32_log2(r32, l, lk, keep);
+                if (keep == -INFINITY && lk == -INFINITY) {
+                    badc[cr] = 1;
+                    set_status(status, ST_ILLEGAL_DG);
+                }
+            }
+        }
+        __syncwarp();
+    }
+}
+
 template <typename T>
 struct Flt;
 template <>
@@ -1710,11 +1906,27 @@ static cudaError_t launch_msampler_t(const ProblemDev& P, uint32_t* dg, int firs
     if (e0 != cudaSuccess) return e0;
     const int64_t ntask = (int64_t)nchain * P.M;
     const int grid = (int)((ntask + fag_threads - 1) / fag_threads);
-    fag_kernel<IX, PP><<<grid, fag_threads, smem, s>>>(P, dg, first, nchain, meioses, mstride, -1, sel, want, raw,
-                                                       nullptr, badc, status, fast);
+    // fast mode: one warp per (chain, locus)
+    const size_t wsm = fagw_block_bytes(P.N, P.F);
+    const bool warp_like = !exact && wsm <= 200 * 1024;   // else the thread-per-locus kernel in log2
+    static size_t wconfigured = 0;
+    if (warp_like && wsm > wconfigured) {
+        cudaError_t e = cudaFuncSetAttribute(fag_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wsm);
+        if (e != cudaSuccess) return e;
+        wconfigured = wsm;
+    }
+    const int wgrid = (int)((ntask + kFagWarpsPerBlock - 1) / kFagWarpsPerBlock);
+    auto like = [&](int j) {
+        if (!warp_like)
+            fag_kernel<IX, PP><<<grid, fag_threads, smem, s>>>(P, dg, first, nchain, meioses, mstride, j, sel, want,
+                                                               raw, exact ? nullptr : raw32, badc, status, fast);
+        else
+            fag_warp_kernel<<<wgrid, kFagWarpsPerBlock * 32, wsm, s>>>(P, dg, first, nchain, meioses, mstride, j, sel,
+                                                                       want, (float*)raw, raw32, badc, status);
+    };
+    like(-1);
     for (int j = 0; j < nm; ++j) {
-        fag_kernel<IX, PP><<<grid, fag_threads, smem, s>>>(P, dg, first, nchain, meioses, mstride, j, sel, want, raw,
-                                                           exact ? nullptr : raw32, badc, status, fast);
+        like(j);
         if (exact)
             ffbs_kernel<double><<<nchain, 32, 0, s>>>(P, dg, first, nchain, meioses, mstride, j, d, sel, want, badc,
                                                       (const double*)raw, nullptr, (double*)fb);
