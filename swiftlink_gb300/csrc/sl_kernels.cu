@@ -909,7 +909,14 @@ __global__ void __launch_bounds__(kFagWarpsPerBlock * 32) fag_warp_kernel(Proble
         bad = __any_sync(FULLMASK, bad);
         // 3. components of the heterozygote edges with parities
         if (!bad && __any_sync(FULLMASK, nab)) {
-            while (true) {
+            // labels only decrease and a path of k edges settles within k rounds:
+            // 2F + 2 rounds always suffice (the bound only guards the loop)
+            for (int round = 0;; ++round) {
+                if (round > nfa + 2) {
+                    bad = 1;
+                    if (lane == 0) set_status(status, ST_ILLEGAL_DG);
+                    break;
+                }
                 int ch = 0;
                 for (int i = lane; i < N; i += 32) {
                     if (!s_typed[i] || (gcol[i] & 3) != G_HETERO) continue;
