@@ -1030,6 +1030,7 @@ int sl_create(const sl_problem_desc* d, const sl_options* opt, sl_ctx** out) {
     P.fag_bytes = 0;
     P.marker_trans = std::log(0.5) * (2 * (N - F));
     P.lod_zero_ok = (opt->lod_flags & SL_LOD_ZERO_OK) ? 1 : 0;
+    P.ls_fast = opt->sampler_precision == SL_SAMPLER_FAST ? 1 : 0;
     if ((rc = upload(ctx, (int16_t**)&P.mother, mo.data(), N))) return bail(rc);
     if ((rc = upload(ctx, (int16_t**)&P.father, fa.data(), N))) return bail(rc);
     if ((rc = upload(ctx, (uint8_t**)&P.geno, geno.data(), geno.size()))) return bail(rc);

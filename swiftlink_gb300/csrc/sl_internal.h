@@ -52,6 +52,7 @@ struct ProblemDev {
     int32_t prog_slots;                  // FP32 slots one task of the program needs
     int32_t prog_threads;                // threads per block of the program kernel
     int32_t lod_zero_ok;                 // a zero trait likelihood is a zero term, not an error
+    int32_t ls_fast;                     // L-sampler in FP32 with per-rfunction rescaling
 };
 
 // Instructions of a compiled trait-peel program (the batched LOD scorer).

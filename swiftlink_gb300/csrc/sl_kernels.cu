@@ -76,6 +76,25 @@ struct Draws {
     }
 };
 
+// Arithmetic of the L-sampler: FP64 without contraction (the reference's
+// doubles) or plain FP32 for the fast sampler mode.
+template <typename T>
+struct Ls;
+template <>
+struct Ls<double> {
+    static __device__ __forceinline__ double mul(double a, double b) { return DMUL(a, b); }
+    static __device__ __forceinline__ double add(double a, double b) { return DADD(a, b); }
+    static __device__ __forceinline__ double sub(double a, double b) { return DSUB(a, b); }
+    static __device__ __forceinline__ double div(double a, double b) { return DDIV(a, b); }
+};
+template <>
+struct Ls<float> {
+    static __device__ __forceinline__ float mul(float a, float b) { return a * b; }
+    static __device__ __forceinline__ float add(float a, float b) { return a + b; }
+    static __device__ __forceinline__ float sub(float a, float b) { return a - b; }
+    static __device__ __forceinline__ float div(float a, float b) { return a / b; }
+};
+
 // ---------------------------------------------------------------------------
 // L-sampler
 // ---------------------------------------------------------------------------
@@ -83,41 +102,43 @@ struct Draws {
 // Recombination distributions of one child's two meioses for every parental
 // state (SamplerRfunction::get_recombination_distribution,
 // sampler_rfunction.cc:102-157): d[side*8 + state*2 + allele].
+template <typename T>
 __device__ void ls_dist_one(const ProblemDev& P, int person, const uint32_t* colL, const uint32_t* colR,
-                            int l, double th, double an, double th2, double an2, double* d) {
+                            int l, T th, T an, T th2, T an2, T* d) {
+    using A = Ls<T>;
     for (int side = 0; side < 2; ++side) {
         const int b = 2 * (person - P.F) + side;
-        double* s = d + side * 8;
-        s[UU * 2 + 0] = 1.0; s[UU * 2 + 1] = 0.0;
-        s[AA * 2 + 0] = 0.0; s[AA * 2 + 1] = 1.0;
-        double tmp0 = 0.5, tmp1 = 0.5;
+        T* s = d + side * 8;
+        s[UU * 2 + 0] = T(1); s[UU * 2 + 1] = T(0);
+        s[AA * 2 + 0] = T(0); s[AA * 2 + 1] = T(1);
+        T tmp0 = T(0.5), tmp1 = T(0.5);
         if (l != 0) {
             const bool cross = dgbit(colL, b) != 0;
-            tmp0 = DMUL(tmp0, cross ? th2 : an2);
-            tmp1 = DMUL(tmp1, cross ? an2 : th2);
+            tmp0 = A::mul(tmp0, cross ? th2 : an2);
+            tmp1 = A::mul(tmp1, cross ? an2 : th2);
         }
         if (l != P.M - 1) {
             const bool cross = dgbit(colR, b) != 0;
-            tmp0 = DMUL(tmp0, cross ? th : an);
-            tmp1 = DMUL(tmp1, cross ? an : th);
+            tmp0 = A::mul(tmp0, cross ? th : an);
+            tmp1 = A::mul(tmp1, cross ? an : th);
         }
-        const double total = DADD(tmp0, tmp1);
-        const double uau = DDIV(tmp1, total);
+        const T total = A::add(tmp0, tmp1);
+        const T uau = A::div(tmp1, total);
         s[AU * 2 + 0] = uau;
-        s[AU * 2 + 1] = DSUB(1.0, uau);
-        const double uua = DDIV(tmp0, total);
+        s[AU * 2 + 1] = A::sub(T(1), uau);
+        const T uua = A::div(tmp0, total);
         s[UA * 2 + 0] = uua;
-        s[UA * 2 + 1] = DSUB(1.0, uua);
+        s[UA * 2 + 1] = A::sub(T(1), uua);
     }
 }
 
+template <typename T>
 __device__ __forceinline__ void ls_dists(const ProblemDev& P, const OpDev& op, const uint32_t* colL,
-                                         const uint32_t* colR, int l, double th, double an, double th2,
-                                         double an2, double* dist, int lane) {
+                                         const uint32_t* colR, int l, T th, T an, T th2, T an2, T* dist, int lane) {
     const int nch = op.type == CHILD ? 1 : (op.type == PARENT ? op.n_child : 0);
     if (lane < nch) {
         const int person = op.type == CHILD ? op.peel : P.opdata[op.child_at + 4 * lane];
-        ls_dist_one(P, person, colL, colR, l, th, an, th2, an2, dist + 16 * lane);
+        ls_dist_one<T>(P, person, colL, colR, l, th, an, th2, an2, dist + 16 * lane);
     }
 }
 
@@ -129,52 +150,56 @@ __device__ __forceinline__ bool ls_valid(const int32_t* cut, int c, const uint8_
 
 // One presum entry (cell, peel state v) in the reference's product order
 // (sampler_rfunction.cc:190-287, rfunction.cc:116-142).
-__device__ double ls_term(const ProblemDev& P, const OpDev& op, const double* A, const double* dist,
-                          int cell, int v, double tv) {
+template <typename T>
+__device__ T ls_term(const ProblemDev& P, const OpDev& op, const T* Am, const T* dist, int cell, int v, T tv) {
+    using A = Ls<T>;
     const int ext = cell | (v << (2 * op.c));
-    double tmp = tv;
+    T tmp = tv;
     if (op.type == CHILD) {
         const int mt = digit(ext, op.mpos), pt = digit(ext, op.fpos);
-        const double T = DMUL(dist[mt * 2 + mat_allele(v)], dist[8 + pt * 2 + pat_allele(v)]);
-        tmp = DMUL(tmp, T);
+        const T tr = A::mul(dist[mt * 2 + mat_allele(v)], dist[8 + pt * 2 + pat_allele(v)]);
+        tmp = A::mul(tmp, tr);
     }
     const int32_t* pd = P.opdata + op.prev_at;
     for (int j = 0; j < op.n_prev; ++j) {
         const int moff = pd[0], pc = pd[1];
         int idx = 0;
         for (int q = 0; q < pc; ++q) idx |= digit(ext, pd[2 + q]) << (2 * q);
-        tmp = DMUL(tmp, A[moff + idx]);
+        tmp = A::mul(tmp, Am[moff + idx]);
         pd += 2 + pc;
     }
     if (op.type == PARENT) {
-        double cp = 1.0;
+        T cp = T(1);
         const int32_t* cd = P.opdata + op.child_at;
         for (int c = 0; c < op.n_child; ++c, cd += 4) {
             const int kt = digit(ext, cd[1]), other = digit(ext, cd[2]);
             const int mt = cd[3] ? v : other, pt = cd[3] ? other : v;
-            const double T = DMUL(dist[c * 16 + mt * 2 + mat_allele(kt)],
-                                  dist[c * 16 + 8 + pt * 2 + pat_allele(kt)]);
-            cp = DMUL(cp, T);
+            const T tr = A::mul(dist[c * 16 + mt * 2 + mat_allele(kt)], dist[c * 16 + 8 + pt * 2 + pat_allele(kt)]);
+            cp = A::mul(cp, tr);
         }
-        tmp = DMUL(tmp, cp);
+        tmp = A::mul(tmp, cp);
     }
     return tmp;
 }
 
-__device__ __forceinline__ size_t ls_warp_bytes(const ProblemDev& P) {
-    return (size_t)P.arena * 8 + (size_t)P.max_child * 128 + (((size_t)P.N + 15) & ~(size_t)15);
+template <typename T>
+__host__ __device__ __forceinline__ size_t ls_warp_bytes(const ProblemDev& P) {
+    return (size_t)P.arena * sizeof(T) + (size_t)P.max_child * 16 * sizeof(T) + (((size_t)P.N + 15) & ~(size_t)15);
 }
 
 // One warp per (chain, locus) task; the listed loci must be pairwise
 // non-adjacent so each task owns its descent-graph column.
+template <typename T>
 __global__ void __launch_bounds__(128) lsampler_kernel(ProblemDev P, uint32_t* dg, int first, int nchain,
                                                        const int32_t* loci, int nloci, Draws draws,
                                                        const uint8_t* sel, int want, int* status) {
+    using Ar = Ls<T>;
+    constexpr bool kRescale = sizeof(T) == 4;   // FP32: each rfunction scaled to a maximum of about 1
     extern __shared__ __align__(16) unsigned char smem[];
     const int wpb = blockDim.x >> 5, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    unsigned char* base = smem + (size_t)warp * ls_warp_bytes(P);
-    double* A = (double*)base;
-    double* dist = A + P.arena;
+    unsigned char* base = smem + (size_t)warp * ls_warp_bytes<T>(P);
+    T* A = (T*)base;
+    T* dist = A + P.arena;
     int8_t* assign = (int8_t*)(dist + 16 * P.max_child);
     const int64_t ntask = (int64_t)nchain * nloci;
     for (int64_t t = (int64_t)blockIdx.x * wpb + warp; t < ntask; t += (int64_t)gridDim.x * wpb) {
@@ -185,35 +210,49 @@ __global__ void __launch_bounds__(128) lsampler_kernel(ProblemDev P, uint32_t* d
         uint32_t* colC = dg + ((size_t)chain * P.M + l) * P.W;
         const uint32_t* colL = l > 0 ? colC - P.W : nullptr;
         const uint32_t* colR = l < P.M - 1 ? colC + P.W : nullptr;
-        double th = 1.0, an = 1.0, th2 = 1.0, an2 = 1.0;
-        if (l > 0) { th2 = P.theta[l - 1]; an2 = DSUB(1.0, th2); }
-        if (l < P.M - 1) { th = P.theta[l]; an = DSUB(1.0, th); }
+        T th = T(1), an = T(1), th2 = T(1), an2 = T(1);
+        if (l > 0) { th2 = (T)P.theta[l - 1]; an2 = (T)DSUB(1.0, P.theta[l - 1]); }
+        if (l < P.M - 1) { th = (T)P.theta[l]; an = (T)DSUB(1.0, P.theta[l]); }
         const uint8_t* gcol = P.geno + (size_t)l * P.N;
         const double* pri = P.prior + (size_t)l * 16;
         // forward peel over the valid cells of every rfunction
         for (int k = 0; k < P.K; ++k) {
             const OpDev op = P.ops[k];
-            ls_dists(P, op, colL, colR, l, th, an, th2, an2, dist, lane);
+            ls_dists<T>(P, op, colL, colR, l, th, an, th2, an2, dist, lane);
             __syncwarp();
             const int ncell = 1 << (2 * op.c);
             const int32_t* cut = P.opdata + op.cut_at;
             const double* trait = pri + 4 * (gcol[op.peel] & 3);
-            double* out = A + op.mat_off;
+            T* out = A + op.mat_off;
+            T mx = T(0);
             for (int cell = lane; cell < ncell; cell += 32) {
-                double total = 0.0;
+                T total = T(0);
                 if (ls_valid(cut, op.c, gcol, cell)) {
                     for (int v = 0; v < 4; ++v) {
-                        const double tv = trait[v];
-                        if (tv == 0.0) continue;
-                        total = DADD(total, ls_term(P, op, A, dist, cell, v, tv));
+                        const T tv = (T)trait[v];
+                        if (tv == T(0)) continue;
+                        total = Ar::add(total, ls_term<T>(P, op, A, dist, cell, v, tv));
                     }
                 }
                 out[cell] = total;
+                mx = total > mx ? total : mx;
+            }
+            if (kRescale) {
+                // the sampling draws from ratios within one rfunction, so a
+                // power-of-two factor per rfunction changes no decision
+                for (int dd = 16; dd >= 1; dd >>= 1) {
+                    const T o = __shfl_xor_sync(FULLMASK, mx, dd);
+                    mx = o > mx ? o : mx;
+                }
+                if (mx > T(0)) {
+                    const float f = scalbnf(1.0f, -ilogbf((float)mx));
+                    for (int cell = lane; cell < ncell; cell += 32) out[cell] = (T)((float)out[cell] * f);
+                }
             }
             __syncwarp();
         }
-        const double root = A[P.ops[P.K - 1].mat_off];
-        if (root == 0.0) {
+        const T root = A[P.ops[P.K - 1].mat_off];
+        if (root == T(0)) {
             if (lane == 0) set_status(status, ST_ZERO_LIK);
             __syncwarp();
             continue;
@@ -223,7 +262,7 @@ __global__ void __launch_bounds__(128) lsampler_kernel(ProblemDev P, uint32_t* d
         // backward sampling of ordered genotypes (SamplerRfunction::sample)
         for (int k = P.K - 1; k >= 0; --k) {
             const OpDev op = P.ops[k];
-            ls_dists(P, op, colL, colR, l, th, an, th2, an2, dist, lane);
+            ls_dists<T>(P, op, colL, colR, l, th, an, th2, an2, dist, lane);
             __syncwarp();
             const int32_t* cut = P.opdata + op.cut_at;
             const double* trait = pri + 4 * (gcol[op.peel] & 3);
@@ -234,26 +273,26 @@ __global__ void __launch_bounds__(128) lsampler_kernel(ProblemDev P, uint32_t* d
                 known &= a >= 0;
                 cellidx |= (a & 3) << (2 * q);
             }
-            double pv = 0.0;
+            T pv = T(0);
             if (lane < 4 && known) {
-                const double tv = trait[lane];
-                if (tv != 0.0 && ls_valid(cut, op.c, gcol, cellidx)) pv = ls_term(P, op, A, dist, cellidx, lane, tv);
+                const T tv = (T)trait[lane];
+                if (tv != T(0) && ls_valid(cut, op.c, gcol, cellidx)) pv = ls_term<T>(P, op, A, dist, cellidx, lane, tv);
             }
-            const double p0 = __shfl_sync(FULLMASK, pv, 0), p1 = __shfl_sync(FULLMASK, pv, 1);
-            const double p2 = __shfl_sync(FULLMASK, pv, 2), p3 = __shfl_sync(FULLMASK, pv, 3);
+            const T p0 = __shfl_sync(FULLMASK, pv, 0), p1 = __shfl_sync(FULLMASK, pv, 1);
+            const T p2 = __shfl_sync(FULLMASK, pv, 2), p3 = __shfl_sync(FULLMASK, pv, 3);
             if (lane == 0) {
                 if (!known) set_status(status, ST_ILLEGAL_DG);
-                double pd[4] = {p0, p1, p2, p3};
-                const double tot = DADD(DADD(DADD(p0, p1), p2), p3);
-                if (tot != 0.0)
-                    for (int v = 0; v < 4; ++v) pd[v] = DDIV(pd[v], tot);
+                T pd[4] = {p0, p1, p2, p3};
+                const T tot = Ar::add(Ar::add(Ar::add(p0, p1), p2), p3);
+                if (tot != T(0))
+                    for (int v = 0; v < 4; ++v) pd[v] = Ar::div(pd[v], tot);
                 const double r = draws.get(cr, chain, l, P.K - 1 - k);
-                double acc = 0.0;
+                T acc = T(0);
                 int lastv = 0, pick = -1;
                 for (int v = 0; v < 4; ++v) {
-                    acc = DADD(acc, pd[v]);
-                    if (r < acc) { pick = v; break; }
-                    if (pd[v] != 0.0) lastv = v;
+                    acc = Ar::add(acc, pd[v]);
+                    if (r < (double)acc) { pick = v; break; }
+                    if (pd[v] != T(0)) lastv = v;
                 }
                 assign[op.peel] = (int8_t)(pick >= 0 ? pick : lastv);
             }
@@ -272,19 +311,19 @@ __global__ void __launch_bounds__(128) lsampler_kernel(ProblemDev P, uint32_t* d
                     if (ptr == UA || ptr == AU) {
                         mi = allele == 0 ? (ptr == UA ? 0 : 1) : (ptr == UA ? 1 : 0);
                     } else {
-                        double p0 = 1.0, p1 = 1.0;
+                        T p0 = T(1), p1 = T(1);
                         if (l != 0) {
                             const int d = dgbit(colL, b);
-                            p0 = DMUL(p0, d == 0 ? an2 : th2);
-                            p1 = DMUL(p1, d == 1 ? an2 : th2);
+                            p0 = Ar::mul(p0, d == 0 ? an2 : th2);
+                            p1 = Ar::mul(p1, d == 1 ? an2 : th2);
                         }
                         if (l != P.M - 1) {
                             const int d = dgbit(colR, b);
-                            p0 = DMUL(p0, d == 0 ? an : th);
-                            p1 = DMUL(p1, d == 1 ? an : th);
+                            p0 = Ar::mul(p0, d == 0 ? an : th);
+                            p1 = Ar::mul(p1, d == 1 ? an : th);
                         }
                         const double r = draws.get(cr, chain, l, cursor++);
-                        mi = (r < DDIV(p0, DADD(p0, p1))) ? 0 : 1;
+                        mi = (r < (double)Ar::div(p0, Ar::add(p0, p1))) ? 0 : 1;
                     }
                     uint32_t w = colC[b >> 5];
                     w = (w & ~(1u << (b & 31))) | ((uint32_t)mi << (b & 31));
@@ -1858,7 +1897,7 @@ __global__ void choose_kernel(int first, int nchain, uint64_t seed, uint64_t ite
 // Host-side launchers
 // ---------------------------------------------------------------------------
 size_t lsampler_smem_per_warp(const ProblemDev& P) {
-    return (size_t)P.arena * 8 + (size_t)P.max_child * 128 + (((size_t)P.N + 15) & ~(size_t)15);
+    return P.ls_fast ? ls_warp_bytes<float>(P) : ls_warp_bytes<double>(P);
 }
 
 
@@ -1866,18 +1905,27 @@ cudaError_t launch_lsampler(const ProblemDev& P, uint32_t* dg, int first, int nc
                             const double* u, int64_t ucs, int64_t uls, uint64_t seed, uint64_t iter,
                             const uint8_t* sel, int want, int* status, cudaStream_t s, int grid_cap, int wpb) {
     const size_t smem = wpb * lsampler_smem_per_warp(P);
-    static size_t configured = 0;
-    if (smem > configured) {
-        cudaError_t e = cudaFuncSetAttribute(lsampler_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    static size_t configured[2] = {0, 0};
+    const int f = P.ls_fast ? 1 : 0;
+    if (smem > configured[f]) {
+        cudaError_t e = f ? cudaFuncSetAttribute(lsampler_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 (int)smem)
+                          : cudaFuncSetAttribute(lsampler_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 (int)smem);
         if (e != cudaSuccess) return e;
-        configured = smem;
+        configured[f] = smem;
     }
     Draws d{u, ucs, uls, seed, iter, 1};
     const int64_t ntask = (int64_t)nchain * nloci;
     int64_t grid = (ntask + wpb - 1) / wpb;
     if (grid > grid_cap) grid = grid_cap;
     if (grid < 1) grid = 1;
-    lsampler_kernel<<<(int)grid, wpb * 32, smem, s>>>(P, dg, first, nchain, loci, nloci, d, sel, want, status);
+    if (f)
+        lsampler_kernel<float><<<(int)grid, wpb * 32, smem, s>>>(P, dg, first, nchain, loci, nloci, d, sel, want,
+                                                                 status);
+    else
+        lsampler_kernel<double><<<(int)grid, wpb * 32, smem, s>>>(P, dg, first, nchain, loci, nloci, d, sel, want,
+                                                                  status);
     return cudaGetLastError();
 }
 

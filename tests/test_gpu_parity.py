@@ -260,6 +260,33 @@ def test_fast_msampler_agrees_with_exact():
     assert agree >= 0.999
 
 
+@pytest.mark.parametrize("name", ["cfg1", "cfg2"])
+def test_fast_lsampler_agrees_with_exact(name):
+    """The FP32 L-sampler (every rfunction rescaled by a power of two) samples
+    the same ordered genotypes and meiosis indicators as the exact FP64 one
+    except at near-ties: one even-then-odd sweep with the same uniforms
+    leaves at least 99.9% of the indicator bits equal."""
+    if name == "cfg1":
+        g = load_golden("cfg1")
+        start, u = g["lsweep_after"], g["lsweep_u"]
+    else:
+        from swiftlink_gb300.workloads import load_problem
+        g = load_problem("cfg2")
+        start = g["dg0"]
+        u = np.random.default_rng(17).random((g["M"], g["K"] + 2 * g["N"]))
+    out = {}
+    for prec in (api.SL_SAMPLER_EXACT, api.SL_SAMPLER_FAST):
+        with api.Context(api.Problem.from_arrays(g), n_chains=1, sampler_precision=prec) as ctx:
+            ctx.set_graphs(start)
+            ctx.lsampler_sweep(u[None])
+            out[prec] = ctx.get_graphs()[0]
+    F = g["F"]
+    a, b = out[api.SL_SAMPLER_FAST][:, F:], out[api.SL_SAMPLER_EXACT][:, F:]
+    agree = float((a == b).mean())
+    print(f"fast/exact L-sweep bit agreement on {name}: {agree:.6f}")
+    assert agree >= 0.999
+
+
 LOD_KERNELS = [api.SL_LOD_KERNEL_INTERP, api.SL_LOD_KERNEL_JIT_REG, api.SL_LOD_KERNEL_JIT_SMEM,
                api.SL_LOD_KERNEL_AUTO]
 
