@@ -851,14 +851,16 @@ __global__ void __launch_bounds__(128) fag_kernel(ProblemDev P, uint32_t* dg, in
 //      pointer jumping (labels packed as 2 * label + parity, only ever
 //      lowered, so the result is the same whatever the interleaving); an edge
 //      whose endpoints end with equal parity closes an odd cycle: zero;
-//   4. each lane sums its components' colourings in log2 in a fixed order and
-//      a butterfly sum over the warp gives log2 of the likelihood.
+//   4. a component's two colourings weigh (even members) x log2 f(A) + (odd
+//      members) x log2 f(B) and the reverse, so each component needs only
+//      integer counts; a butterfly sum over the warp gives log2 of the
+//      likelihood.
 // ---------------------------------------------------------------------------
 constexpr int kFagWarpsPerBlock = 8;
 
 __host__ __device__ inline size_t fagw_tables(int N) { return ((size_t)N * 7 + 15) & ~(size_t)15; }
 __host__ __device__ inline size_t fagw_warp_bytes(int N, int F) {
-    return (((size_t)4 * N + 15) & ~(size_t)15) + (size_t)2 * F * 8;
+    return (((size_t)4 * N + 15) & ~(size_t)15) + (size_t)2 * F * 12;
 }
 size_t fagw_block_bytes(int N, int F) { return fagw_tables(N) + kFagWarpsPerBlock * fagw_warp_bytes(N, F); }
 
@@ -885,6 +887,7 @@ __global__ void __launch_bounds__(kFagWarpsPerBlock * 32) fag_warp_kernel(Proble
     uint16_t* e = (uint16_t*)wbase;                                   // [2N] founder allele of each allele
     volatile int* Lb = (volatile int*)(wbase + (((size_t)4 * N + 15) & ~(size_t)15));   // [2F] 2 * label + parity
     int* fl = (int*)(Lb + nfa);                                       // [2F] bit0 used, bit1 fixed A, bit2 fixed B
+    int* cnt = fl + nfa;                                              // [2F] per component: counts, forbidden colourings
     const int64_t ntask = (int64_t)nchain * M;
     for (int64_t t = (int64_t)blockIdx.x * wpb + warp; t < ntask; t += (int64_t)gridDim.x * wpb) {
         const int cr = (int)(t / M);
@@ -982,26 +985,39 @@ __global__ void __launch_bounds__(kFagWarpsPerBlock * 32) fag_warp_kernel(Proble
             }
             bad = __any_sync(FULLMASK, bad);
         }
-        // 4. sum over each component's colourings, log2
+        // 4. sum over each component's colourings, log2: every member allele
+        // contributes log2 of the major or the minor frequency, so a component
+        // needs only its member count, how many members have even parity and
+        // which colourings its fixed members forbid (integer shared-memory
+        // atomics, the same result in any order)
         float lk = -INFINITY;
         if (!bad) {
+            for (int x = lane; x < nfa; x += 32) cnt[x] = 0;
+            __syncwarp();
+            for (int x = lane; x < nfa; x += 32) {
+                const int f = fl[x];
+                if (!(f & 1)) continue;
+                const int lx = Lb[x], r = lx >> 1, p = lx & 1;
+                // bit 16 + n: member count; bits 0-15: even-parity members; bits 29/30: colouring 0/1 forbidden
+                int add = (1 << 16) + (p ? 0 : 1);
+                int forbid = 0;
+                if (f & 2) forbid |= p ? (1 << 29) : (1 << 30);   // fixed A
+                if (f & 4) forbid |= p ? (1 << 30) : (1 << 29);   // fixed B
+                atomicAdd(&cnt[r], add);
+                if (forbid) atomicOr(&cnt[r], forbid);
+            }
+            __syncwarp();
             const double minor_d = P.minor[l];
             const float lmaj = log2f((float)(1.0 - minor_d)), lmin = log2f((float)minor_d);
             float sum = 0.f;
             int zero = 0;
             for (int x = lane; x < nfa; x += 32) {
-                if (!(fl[x] & 1) || Lb[x] != (x << 1)) continue;
-                float w0 = 0.f, w1 = 0.f;
-                int ok0 = 1, ok1 = 1;
-                for (int y = x; y < nfa; ++y) {
-                    const int ly = Lb[y], f = fl[y];
-                    if ((ly >> 1) != x || !(f & 1)) continue;
-                    const int p = ly & 1;
-                    w0 += p ? lmin : lmaj;   // root coloured A: this allele is A unless its parity is odd
-                    w1 += p ? lmaj : lmin;
-                    if (f & 2) { if (p) ok0 = 0; else ok1 = 0; }
-                    if (f & 4) { if (p) ok1 = 0; else ok0 = 0; }
-                }
+                const int c = cnt[x];
+                const int n = (c >> 16) & 0x1fff, even = c & 0xffff;
+                if (n == 0) continue;
+                const float w0 = (float)even * lmaj + (float)(n - even) * lmin;   // root coloured A
+                const float w1 = (float)even * lmin + (float)(n - even) * lmaj;   // root coloured B
+                const int ok0 = !(c & (1 << 29)), ok1 = !(c & (1 << 30));
                 if (ok0 && ok1) {
                     const float mx = fmaxf(w0, w1);
                     sum += mx + log2f(1.f + exp2f(fminf(w0, w1) - mx));
@@ -1963,7 +1979,8 @@ static cudaError_t launch_msampler_t(const ProblemDev& P, uint32_t* dg, int firs
     const int grid = (int)((ntask + fag_threads - 1) / fag_threads);
     // fast mode: one warp per (chain, locus)
     const size_t wsm = fagw_block_bytes(P.N, P.F);
-    const bool warp_like = !exact && wsm <= 200 * 1024;   // else the thread-per-locus kernel in log2
+    // else the thread-per-locus kernel in log2 (component counts are 13-bit fields)
+    const bool warp_like = !exact && wsm <= 200 * 1024 && 2 * P.F < 8192;
     static size_t wconfigured = 0;
     if (warp_like && wsm > wconfigured) {
         cudaError_t e = cudaFuncSetAttribute(fag_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wsm);
