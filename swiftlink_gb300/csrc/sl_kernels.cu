@@ -860,7 +860,7 @@ constexpr int kFagWarpsPerBlock = 8;
 
 __host__ __device__ inline size_t fagw_tables(int N) { return ((size_t)N * 7 + 15) & ~(size_t)15; }
 __host__ __device__ inline size_t fagw_warp_bytes(int N, int F) {
-    return (((size_t)4 * N + 15) & ~(size_t)15) + (size_t)2 * F * 12;
+    return (((size_t)4 * N + 15) & ~(size_t)15) + (size_t)2 * F * 12 + (size_t)4 * N;
 }
 size_t fagw_block_bytes(int N, int F) { return fagw_tables(N) + kFagWarpsPerBlock * fagw_warp_bytes(N, F); }
 
@@ -888,6 +888,7 @@ __global__ void __launch_bounds__(kFagWarpsPerBlock * 32) fag_warp_kernel(Proble
     volatile int* Lb = (volatile int*)(wbase + (((size_t)4 * N + 15) & ~(size_t)15));   // [2F] 2 * label + parity
     int* fl = (int*)(Lb + nfa);                                       // [2F] bit0 used, bit1 fixed A, bit2 fixed B
     int* cnt = fl + nfa;                                              // [2F] per component: counts, forbidden colourings
+    uint32_t* hed = (uint32_t*)(cnt + nfa);                           // [N] heterozygote edges, u | v << 16
     const int64_t ntask = (int64_t)nchain * M;
     for (int64_t t = (int64_t)blockIdx.x * wpb + warp; t < ntask; t += (int64_t)gridDim.x * wpb) {
         const int cr = (int)(t / M);
@@ -931,26 +932,34 @@ __global__ void __launch_bounds__(kFagWarpsPerBlock * 32) fag_warp_kernel(Proble
             fl[x] = 0;
         }
         __syncwarp();
-        int bad = 0, nab = 0;
-        for (int i = lane; i < N; i += 32) {
-            if (!s_typed[i]) continue;
-            const int g = gcol[i] & 3;
-            if (g == G_UNTYPED) continue;
-            const int u = e[2 * i], v = e[2 * i + 1];
-            if (g == G_HETERO) {
+        // heterozygote edges are also listed, compacted, for the labelling rounds
+        int bad = 0, nhet = 0;
+        for (int base = 0; base < N; base += 32) {
+            const int i = base + lane;
+            int g = G_UNTYPED, u = 0, v = 0;
+            if (i < N && s_typed[i]) {
+                g = gcol[i] & 3;
+                u = e[2 * i];
+                v = e[2 * i + 1];
+            }
+            const bool het = g == G_HETERO;
+            const unsigned hm = __ballot_sync(FULLMASK, het);
+            if (het) {
                 if (u == v) bad = 1;
                 atomicOr(&fl[u], 1);
                 atomicOr(&fl[v], 1);
-                ++nab;
-            } else {
+                hed[nhet + __popc(hm & ((1u << lane) - 1u))] = (uint32_t)u | ((uint32_t)v << 16);
+            } else if (g != G_UNTYPED) {
                 const int bits = 1 | (g == G_HOMOZ_A ? 2 : 4);
                 atomicOr(&fl[u], bits);
                 atomicOr(&fl[v], bits);
             }
+            nhet += __popc(hm);
         }
         bad = __any_sync(FULLMASK, bad);
+        __syncwarp();
         // 3. components of the heterozygote edges with parities
-        if (!bad && __any_sync(FULLMASK, nab)) {
+        if (!bad && nhet > 0) {
             // labels only decrease and a path of k edges settles within k rounds:
             // 2F + 2 rounds always suffice (the bound only guards the loop)
             for (int round = 0;; ++round) {
@@ -960,9 +969,9 @@ __global__ void __launch_bounds__(kFagWarpsPerBlock * 32) fag_warp_kernel(Proble
                     break;
                 }
                 int ch = 0;
-                for (int i = lane; i < N; i += 32) {
-                    if (!s_typed[i] || (gcol[i] & 3) != G_HETERO) continue;
-                    const int u = e[2 * i], v = e[2 * i + 1];
+                for (int q = lane; q < nhet; q += 32) {
+                    const uint32_t h = hed[q];
+                    const int u = (int)(h & 0xffffu), v = (int)(h >> 16);
                     const int a = Lb[u], b = Lb[v];
                     if ((a ^ 1) < b) { atomicMin((int*)&Lb[v], a ^ 1); ch = 1; }
                     if ((b ^ 1) < a) { atomicMin((int*)&Lb[u], b ^ 1); ch = 1; }
@@ -979,9 +988,9 @@ __global__ void __launch_bounds__(kFagWarpsPerBlock * 32) fag_warp_kernel(Proble
                 __syncwarp();
                 if (!__any_sync(FULLMASK, ch)) break;
             }
-            for (int i = lane; i < N; i += 32) {
-                if (!s_typed[i] || (gcol[i] & 3) != G_HETERO) continue;
-                if ((Lb[e[2 * i]] ^ Lb[e[2 * i + 1]]) != 1) bad = 1;   // same label, parities must differ
+            for (int q = lane; q < nhet; q += 32) {
+                const uint32_t h = hed[q];
+                if ((Lb[h & 0xffffu] ^ Lb[h >> 16]) != 1) bad = 1;   // same label, parities must differ
             }
             bad = __any_sync(FULLMASK, bad);
         }
@@ -1406,9 +1415,9 @@ __global__ void __launch_bounds__(1024) ffbs_scan_kernel(ProblemDev P, uint32_t*
     }
 }
 
-// Threads per chain of ffbs_scan_kernel: runs of about 8 loci.
+// Threads per chain of ffbs_scan_kernel: runs of about 4 loci.
 int ffbs_scan_threads(int M) {
-    int t = ((M + 7) / 8 + 31) / 32 * 32;
+    int t = ((M + 3) / 4 + 31) / 32 * 32;
     return t < 32 ? 32 : (t > 1024 ? 1024 : t);
 }
 
