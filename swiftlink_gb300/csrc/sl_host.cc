@@ -29,7 +29,9 @@ cudaError_t launch_lsampler(const ProblemDev& P, uint32_t* dg, int first, int nc
 cudaError_t launch_msampler(const ProblemDev& P, uint32_t* dg, int first, int nchain, const int32_t* meioses,
                             int64_t mstride, int nm, const double* u, int64_t ucs, uint64_t seed, uint64_t iter,
                             const uint8_t* sel, int want, double* raw64, float* raw32, void* fb, uint8_t* badc,
-                            uint8_t* maps, int* status, int fag_threads, int exact, cudaStream_t s);
+                            uint8_t* maps, int* status, int fag_threads, int exact, cudaStream_t s,
+                            const uint64_t* key = nullptr);
+cudaError_t launch_set_key(uint64_t* key, uint64_t seed, uint64_t iter, cudaStream_t s);
 size_t fag_smem(int N, int F, int threads, int fast);
 cudaError_t launch_lod(const ProblemDev& P, int precision, const uint32_t* graphs, int64_t graph_words, int G,
                        double* vals, int* status, cudaStream_t s, int grid_cap, int wpb);
@@ -97,6 +99,13 @@ struct sl_ctx {
     uint8_t* d_sel = nullptr;
     uint32_t* h_stage = nullptr;     // pinned staging for packed descent graphs
     size_t h_stage_words = 0;
+    // the M-sweep of device-driven runs as a graph: one branch per chain, so a
+    // chain's filter overlaps other chains' founder-allele graphs
+    cudaGraphExec_t ms_graph = nullptr;
+    int64_t ms_graph_kernels = 0;
+    uint64_t* d_key = nullptr;        // [2] seed and iteration read by the graph's kernels
+    std::vector<cudaStream_t> cap_streams;
+    std::vector<cudaEvent_t> cap_events;
     // trait-peel adjoint (present when the problem carries the disease model)
     bool has_adjoint = false;
     AdjDev adj{};
@@ -899,6 +908,9 @@ void sl_destroy(sl_ctx* ctx) {
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     jit_lod_release(&ctx->jit_reg);
     jit_lod_release(&ctx->jit_smem);
+    if (ctx->ms_graph) cudaGraphExecDestroy(ctx->ms_graph);
+    for (auto st : ctx->cap_streams) cudaStreamDestroy(st);
+    for (auto ev : ctx->cap_events) cudaEventDestroy(ev);
     cudaSetDevice(cur);
     delete ctx;
 }
@@ -1743,6 +1755,63 @@ int sl_problem_trait_backward_eval(const sl_problem_desc* d, const int32_t* dg, 
     return host_backward(d, prog, dg, locus, offset, grad, nullptr);
 }
 
+// Capture the device-driven M-sweep once: for every chain c a branch
+// memset -> founder-allele graphs (reset) -> [graphs, filter] x nm over that
+// chain alone (first = c, one chain); kernels of chains that chose the
+// L-sampler return at once.  Seed and iteration come from d_key.
+static int build_ms_graph(sl_ctx* ctx) {
+    const ProblemDev& P = ctx->P;
+    const int C = ctx->n_chains, nm = (int)ctx->meioses.size(), M = P.M;
+    const bool exact = ctx->sampler_precision == SL_SAMPLER_EXACT;
+    int rc;
+    if (!ctx->d_key && (rc = dev_alloc(ctx, &ctx->d_key, 2))) return rc;
+    // a first direct launch configures the kernels' shared-memory limits outside the
+    // capture; with every chain's selector 0 and want = 2 its kernels do nothing
+    CK(cudaMemsetAsync(ctx->d_sel, 0, (size_t)C, ctx->stream));
+    CK(launch_set_key(ctx->d_key, 0, 0, ctx->stream));
+    CK(launch_msampler(P, ctx->d_dg, 0, C, ctx->d_morder, nm, 0, nullptr, 0, 0, 0, ctx->d_sel, 2, ctx->d_raw,
+                       ctx->d_raw32, ctx->d_fb, ctx->d_badc, ctx->d_maps, ctx->d_status, ctx->ms_threads, exact ? 1 : 0,
+                       ctx->stream, ctx->d_key));
+    CK(cudaStreamSynchronize(ctx->stream));
+    while ((int)ctx->cap_streams.size() < C + 1) {
+        cudaStream_t st;
+        CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        ctx->cap_streams.push_back(st);
+        cudaEvent_t ev;
+        CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        ctx->cap_events.push_back(ev);
+    }
+    cudaStream_t s0 = ctx->cap_streams[C];
+    CK(cudaStreamBeginCapture(s0, cudaStreamCaptureModeThreadLocal));
+    cudaError_t err = cudaEventRecord(ctx->cap_events[C], s0);
+    for (int c = 0; c < C && err == cudaSuccess; ++c) {
+        cudaStream_t sc = ctx->cap_streams[c];
+        err = cudaStreamWaitEvent(sc, ctx->cap_events[C], 0);
+        if (err != cudaSuccess) break;
+        double* raw = exact ? ctx->d_raw + (size_t)c * 2 * M : ctx->d_raw + (size_t)c * M;   // fast: 2M floats
+        void* fb = exact ? (void*)((double*)ctx->d_fb + (size_t)c * 2 * M) : (void*)((float*)ctx->d_fb + (size_t)c * 2 * M);
+        err = launch_msampler(P, ctx->d_dg, c, 1, ctx->d_morder + (size_t)c * nm, nm, nm, nullptr, 0, 0, 0,
+                              ctx->d_sel + c, 0, raw, ctx->d_raw32 + (size_t)c * 2 * M, fb, ctx->d_badc + c,
+                              ctx->d_maps + (size_t)c * M, ctx->d_status, ctx->ms_threads, exact ? 1 : 0, sc,
+                              ctx->d_key);
+        if (err != cudaSuccess) break;
+        err = cudaEventRecord(ctx->cap_events[c], sc);
+        if (err != cudaSuccess) break;
+        err = cudaStreamWaitEvent(s0, ctx->cap_events[c], 0);
+    }
+    cudaGraph_t graph = nullptr;
+    cudaError_t err2 = cudaStreamEndCapture(s0, &graph);
+    if (err == cudaSuccess) err = err2;
+    if (err == cudaSuccess) err = cudaGraphInstantiate(&ctx->ms_graph, graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    if (err != cudaSuccess) {
+        ctx->ms_graph = nullptr;
+        return fail(ctx, SL_ECUDA, "capturing the M-sweep graph: %s", cudaGetErrorString(err));
+    }
+    ctx->ms_graph_kernels = (int64_t)C * (2 * nm + 1);
+    return SL_OK;
+}
+
 int sl_run(sl_ctx* ctx, const sl_run_options* o) {
     if (!ctx || !o) return fail(ctx, SL_EINVAL, "null argument");
     if (o->iterations < 0 || o->burnin < 0 || o->scoring_period < 1 || o->first_iteration < 0 ||
@@ -1753,6 +1822,10 @@ int sl_run(sl_ctx* ctx, const sl_run_options* o) {
     const int C = ctx->n_chains;
     const int nm = (int)ctx->meioses.size();
     const int total = o->burnin + o->iterations;
+    if (!ctx->ms_graph && o->first_iteration < total) {
+        int rc = build_ms_graph(ctx);
+        if (rc) return rc;
+    }
     for (int it = o->first_iteration; it < total; ++it) {
         const uint64_t iter = (uint64_t)it;
         { Prof pf_(ctx, SL_KERNEL_OTHER);
@@ -1770,10 +1843,9 @@ int sl_run(sl_ctx* ctx, const sl_run_options* o) {
             CK(launch_lsampler(P, ctx->d_dg, 0, C, ctx->d_odd, (int)ctx->odd.size(), nullptr, 0, 0, o->seed, iter,
                                ctx->d_sel, 1, ctx->d_status, ctx->lstream, ctx->ls_grid, ctx->ls_wpb)); }
         { Prof pf_(ctx, SL_KERNEL_MSAMPLER);
-            ctx->launches += 2 * nm;
-            CK(launch_msampler(P, ctx->d_dg, 0, C, ctx->d_morder, nm, nm, nullptr, 0, o->seed, iter, ctx->d_sel, 0,
-                               ctx->d_raw, ctx->d_raw32, ctx->d_fb, ctx->d_badc, ctx->d_maps, ctx->d_status,
-                               ctx->ms_threads, ctx->sampler_precision == SL_SAMPLER_EXACT, ctx->stream)); }
+            CK(launch_set_key(ctx->d_key, o->seed, iter, ctx->stream));
+            CK(cudaGraphLaunch(ctx->ms_graph, ctx->stream));
+            ctx->launches += ctx->ms_graph_kernels; }
         CK(cudaEventRecord(ctx->ev_join, ctx->lstream));
         CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0));
         if (it >= o->burnin && it % o->scoring_period == 0) {

@@ -64,17 +64,26 @@ __device__ __forceinline__ double philox_u01(uint64_t key, uint64_t c_hi, uint64
 // Where uniform draws come from: a caller-supplied array (bit-exact replay of
 // the reference) or the Philox stream (device-driven runs).  `unit` is the
 // locus (L-sampler) or the meiosis step (M-sampler) within the sweep.
+// `key` (device memory, may be null) overrides seed and iteration: a
+// captured graph replayed every iteration reads them there.
 struct Draws {
     const double* u;
     int64_t chain_stride, unit_stride;
     uint64_t seed, iter;
     int stage;
+    const uint64_t* key;
     __device__ __forceinline__ double get(int chain_rel, int chain, int64_t unit, int64_t k) const {
         if (u) return u[chain_rel * chain_stride + unit * unit_stride + k];
-        uint64_t hi = ((uint64_t)chain << 40) ^ (iter << 4) ^ (uint64_t)stage;
-        return philox_u01(seed, hi, ((uint64_t)unit << 24) ^ (uint64_t)k);
+        const uint64_t sd = key ? key[0] : seed, it = key ? key[1] : iter;
+        uint64_t hi = ((uint64_t)chain << 40) ^ (it << 4) ^ (uint64_t)stage;
+        return philox_u01(sd, hi, ((uint64_t)unit << 24) ^ (uint64_t)k);
     }
 };
+
+__global__ void set_key_kernel(uint64_t* key, uint64_t seed, uint64_t iter) {
+    key[0] = seed;
+    key[1] = iter;
+}
 
 // Arithmetic of the L-sampler: FP64 without contraction (the reference's
 // doubles) or plain FP32 for the fast sampler mode.
@@ -1940,7 +1949,7 @@ cudaError_t launch_lsampler(const ProblemDev& P, uint32_t* dg, int first, int nc
         if (e != cudaSuccess) return e;
         configured[f] = smem;
     }
-    Draws d{u, ucs, uls, seed, iter, 1};
+    Draws d{u, ucs, uls, seed, iter, 1, nullptr};
     const int64_t ntask = (int64_t)nchain * nloci;
     int64_t grid = (ntask + wpb - 1) / wpb;
     if (grid > grid_cap) grid = grid_cap;
@@ -1959,7 +1968,7 @@ static cudaError_t launch_msampler_t(const ProblemDev& P, uint32_t* dg, int firs
                                      int64_t mstride, int nm, const double* u, int64_t ucs, uint64_t seed,
                                      uint64_t iter, const uint8_t* sel, int want, typename PP::T* raw, float* raw32,
                                      void* fb, uint8_t* badc, uint8_t* maps, int* status, int fag_threads, int exact,
-                                     cudaStream_t s) {
+                                     cudaStream_t s, const uint64_t* key) {
     const int fast = exact ? 0 : 1;
     const size_t smem = fag_block_bytes(P.N, P.F, fag_threads, fast);
     static size_t configured = 0;
@@ -1968,7 +1977,7 @@ static cudaError_t launch_msampler_t(const ProblemDev& P, uint32_t* dg, int firs
         if (e != cudaSuccess) return e;
         configured = smem;
     }
-    Draws d{u, ucs, P.M, seed, iter, 2};
+    Draws d{u, ucs, P.M, seed, iter, 2, key};
     const int scan_threads = ffbs_scan_threads(P.M);
     size_t scan_smem = ffbs_scan_smem(P.M);
     int staged = 1;
@@ -2018,27 +2027,34 @@ static cudaError_t launch_msampler_t(const ProblemDev& P, uint32_t* dg, int firs
     return cudaGetLastError();
 }
 
+cudaError_t launch_set_key(uint64_t* key, uint64_t seed, uint64_t iter, cudaStream_t s) {
+    set_key_kernel<<<1, 1, 0, s>>>(key, seed, iter);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_msampler(const ProblemDev& P, uint32_t* dg, int first, int nchain, const int32_t* meioses,
                             int64_t mstride, int nm, const double* u, int64_t ucs, uint64_t seed, uint64_t iter,
                             const uint8_t* sel, int want, double* raw64, float* raw32, void* fb, uint8_t* badc,
-                            uint8_t* maps, int* status, int fag_threads, int exact, cudaStream_t s) {
+                            uint8_t* maps, int* status, int fag_threads, int exact, cudaStream_t s,
+                            const uint64_t* key) {
     // the fast mode keeps log2 likelihoods as floats in the first half of the raw buffer
     float* rawl = (float*)raw64;
     if (2 * P.F <= 255) {
         if (exact)
             return launch_msampler_t<uint8_t, ProbExact>(P, dg, first, nchain, meioses, mstride, nm, u, ucs, seed,
                                                          iter, sel, want, raw64, raw32, fb, badc, maps, status,
-                                                         fag_threads, exact, s);
+                                                         fag_threads, exact, s, key);
         return launch_msampler_t<uint8_t, ProbLog2>(P, dg, first, nchain, meioses, mstride, nm, u, ucs, seed, iter,
                                                     sel, want, rawl, raw32, fb, badc, maps, status, fag_threads,
-                                                    exact, s);
+                                                    exact, s, key);
     }
     if (exact)
         return launch_msampler_t<uint16_t, ProbExact>(P, dg, first, nchain, meioses, mstride, nm, u, ucs, seed, iter,
                                                       sel, want, raw64, raw32, fb, badc, maps, status, fag_threads,
-                                                      exact, s);
+                                                      exact, s, key);
     return launch_msampler_t<uint16_t, ProbLog2>(P, dg, first, nchain, meioses, mstride, nm, u, ucs, seed, iter, sel,
-                                                 want, rawl, raw32, fb, badc, maps, status, fag_threads, exact, s);
+                                                 want, rawl, raw32, fb, badc, maps, status, fag_threads, exact, s,
+                                                 key);
 }
 
 size_t fag_smem(int N, int F, int threads, int fast) { return fag_block_bytes(N, F, threads, fast); }
