@@ -307,20 +307,26 @@ __global__ void __launch_bounds__(128) lsampler_kernel(ProblemDev P, uint32_t* d
             }
             __syncwarp();
         }
-        // meiosis indicators (locus_sampler2.cc:32-125), person order, maternal first
-        if (lane == 0) {
+        // meiosis indicators (locus_sampler2.cc:32-125) in person order, maternal
+        // first: bit b = 2 (person - F) + parent, so 32 consecutive meioses are one
+        // descent-graph word.  A lane takes one meiosis; a draw is consumed only
+        // below a homozygous parent, and a ballot prefix gives each draw its index.
+        {
             int64_t cursor = P.K;
-            for (int i = P.F; i < P.N; ++i) {
-                const int tr = assign[i];
-                for (int par = 0; par < 2; ++par) {
+            const int nb = 2 * P.Nnf;
+            for (int w = 0; w < P.W; ++w) {
+                const int b = 32 * w + lane;
+                int mi = 0, need = 0;
+                T p0 = T(1), p1 = T(1);
+                if (b < nb) {
+                    const int i = P.F + (b >> 1), par = b & 1;
+                    const int tr = assign[i];
                     const int ptr = assign[par == 0 ? P.mother[i] : P.father[i]];
                     const int allele = par == 0 ? ((tr == UU || tr == UA) ? 0 : 1) : ((tr == UU || tr == AU) ? 0 : 1);
-                    int mi;
-                    const int b = 2 * (i - P.F) + par;
                     if (ptr == UA || ptr == AU) {
                         mi = allele == 0 ? (ptr == UA ? 0 : 1) : (ptr == UA ? 1 : 0);
                     } else {
-                        T p0 = T(1), p1 = T(1);
+                        need = 1;
                         if (l != 0) {
                             const int d = dgbit(colL, b);
                             p0 = Ar::mul(p0, d == 0 ? an2 : th2);
@@ -331,13 +337,16 @@ __global__ void __launch_bounds__(128) lsampler_kernel(ProblemDev P, uint32_t* d
                             p0 = Ar::mul(p0, d == 0 ? an : th);
                             p1 = Ar::mul(p1, d == 1 ? an : th);
                         }
-                        const double r = draws.get(cr, chain, l, cursor++);
-                        mi = (r < (double)Ar::div(p0, Ar::add(p0, p1))) ? 0 : 1;
                     }
-                    uint32_t w = colC[b >> 5];
-                    w = (w & ~(1u << (b & 31))) | ((uint32_t)mi << (b & 31));
-                    colC[b >> 5] = w;
                 }
+                const unsigned nmask = __ballot_sync(FULLMASK, need);
+                if (need) {
+                    const double r = draws.get(cr, chain, l, cursor + __popc(nmask & ((1u << lane) - 1u)));
+                    mi = (r < (double)Ar::div(p0, Ar::add(p0, p1))) ? 0 : 1;
+                }
+                cursor += __popc(nmask);
+                const unsigned word = __ballot_sync(FULLMASK, mi != 0);
+                if (lane == 0) colC[w] = word;   // bits past 2 Nnf stay zero
             }
         }
         __syncwarp();
