@@ -1,0 +1,61 @@
+"""A short, fixed workload for ncu captures of the library's kernels.
+
+    python -m swiftlink_gb300.profile_workload [--iterations 2] [--chains 10]
+        [--lprob 0.5] [--adjoint 0]
+
+On the 120-member, 2000-SNP pedigree it runs `iterations` device-driven MCMC
+iterations of `chains` chains in the fast sampler mode (L-sweeps and the
+M-sweep graph), then one batched FP32 LOD scoring of every chain (the first
+scoring also times the LOD kernel candidates), and, with --adjoint G, the
+trait-peel adjoint of G graphs under the dominant model (0.01, 0.8, 0.9),
+q = 1e-3.  It prints the per-kernel-class event times of the sampling part.
+"""
+from __future__ import annotations
+
+import argparse
+
+import numpy as np
+
+from swiftlink_gb300 import api
+from swiftlink_gb300.workloads import disease_probs, load_problem
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--iterations", type=int, default=2)
+    ap.add_argument("--chains", type=int, default=10)
+    ap.add_argument("--lprob", type=float, default=0.5)
+    ap.add_argument("--adjoint", type=int, default=0)
+    ap.add_argument("--seed", type=int, default=5)
+    a = ap.parse_args(argv)
+    d = load_problem("cfg2")
+    C = a.chains
+    prob = api.Problem.from_arrays(d, with_legal=False)
+    with api.Context(prob, n_chains=C, lod_precision=api.SL_LOD_FP32_RESCALED,
+                     sampler_precision=api.SL_SAMPLER_FAST, lod_flags=api.SL_LOD_ZERO_OK) as ctx:
+        ctx.set_graphs(np.stack([d["dg0"]] * C))
+        ctx.profile(True)
+        ctx.run(iterations=a.iterations, burnin=0, period=1 << 30, lprob=a.lprob, seed=a.seed)
+        ctx.synchronize()
+        names = ["L-sampler", "M-sampler", "LOD", "LOD merge", "other"]
+        for k in range(5):
+            ms, n = ctx.profile_read(k)
+            print(f"{names[k]:10s} {ms:9.3f} ms over {n} marks")
+        ctx.profile(False)
+        ctx.lod_score_chains()
+        ctx.synchronize()
+        graphs = ctx.get_graphs()
+        print("lod kernel", ctx.lod_kernel_info())
+    if a.adjoint > 0:
+        pen, q = (0.01, 0.8, 0.9), 1e-3
+        dd = dict(d, penetrance=np.array(pen), freq=np.float64(q),
+                  disease_prob=disease_probs(d["affection"], d["mother"] < 0, q, pen))
+        with api.Context(api.Problem.from_arrays(dd, with_legal=False), n_chains=1,
+                         lod_precision=api.SL_LOD_FP32_RESCALED, lod_flags=api.SL_LOD_ZERO_OK) as actx:
+            gset = np.stack([graphs[i % C] for i in range(a.adjoint)])
+            grad, pt = actx.trait_backward(gset)
+            print("adjoint", grad.shape, float(np.abs(grad).max()), pt)
+
+
+if __name__ == "__main__":
+    main()
