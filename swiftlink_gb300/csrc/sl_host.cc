@@ -25,13 +25,22 @@ namespace sl {
 size_t lsampler_smem_per_warp(const ProblemDev& P);
 cudaError_t launch_lsampler(const ProblemDev& P, uint32_t* dg, int first, int nchain, const int32_t* loci,
                             int nloci, const double* u, int64_t ucs, int64_t uls, uint64_t seed, uint64_t iter,
-                            const uint8_t* sel, int want, int* status, cudaStream_t s, int grid_cap, int wpb);
+                            const uint8_t* sel, int want, int* status, cudaStream_t s, int grid_cap, int wpb,
+                            const uint64_t* key = nullptr);
 cudaError_t launch_msampler(const ProblemDev& P, uint32_t* dg, int first, int nchain, const int32_t* meioses,
                             int64_t mstride, int nm, const double* u, int64_t ucs, uint64_t seed, uint64_t iter,
                             const uint8_t* sel, int want, double* raw64, float* raw32, void* fb, uint8_t* badc,
                             uint8_t* maps, int* status, int fag_threads, int exact, cudaStream_t s,
                             const uint64_t* key = nullptr);
 cudaError_t launch_set_key(uint64_t* key, uint64_t seed, uint64_t iter, cudaStream_t s);
+cudaError_t launch_run_init(const RunParams* rp, int64_t* it, int C, cudaStream_t s);
+cudaError_t launch_chain_iter(const RunParams* rp, const int64_t* it, int c, uint64_t* key, const int32_t* base,
+                              int nm, int32_t* order, cudaGraphConditionalHandle hsw,
+                              cudaGraphConditionalHandle hscore, cudaStream_t s);
+cudaError_t launch_chain_advance(const RunParams* rp, int64_t* it, int c, cudaGraphConditionalHandle hwhile,
+                                 cudaStream_t s);
+cudaError_t launch_chain_merge(double* acc_c, uint8_t* init_c, int C, int64_t npos, double* acc, uint8_t* init,
+                               cudaStream_t s);
 size_t fag_smem(int N, int F, int threads, int fast);
 cudaError_t launch_lod(const ProblemDev& P, int precision, const uint32_t* graphs, int64_t graph_words, int G,
                        double* vals, int* status, cudaStream_t s, int grid_cap, int wpb);
@@ -106,6 +115,13 @@ struct sl_ctx {
     uint64_t* d_key = nullptr;        // [2] seed and iteration read by the graph's kernels
     std::vector<cudaStream_t> cap_streams;
     std::vector<cudaEvent_t> cap_events;
+    // the whole device-driven run as one graph: a WHILE node per chain
+    cudaGraphExec_t run_graph = nullptr;
+    RunParams* d_run = nullptr;
+    int64_t* d_chain_it = nullptr;    // [C] each chain's next iteration
+    uint64_t* d_keys = nullptr;       // [C][2] each chain's Philox seed and iteration
+    double* d_acc_c = nullptr;        // [C][npos] each chain's LOD log-sums of the run
+    uint8_t* d_init_c = nullptr;      // [C][npos]
     // trait-peel adjoint (present when the problem carries the disease model)
     bool has_adjoint = false;
     AdjDev adj{};
@@ -909,6 +925,7 @@ void sl_destroy(sl_ctx* ctx) {
     jit_lod_release(&ctx->jit_reg);
     jit_lod_release(&ctx->jit_smem);
     if (ctx->ms_graph) cudaGraphExecDestroy(ctx->ms_graph);
+    if (ctx->run_graph) cudaGraphExecDestroy(ctx->run_graph);
     for (auto st : ctx->cap_streams) cudaStreamDestroy(st);
     for (auto ev : ctx->cap_events) cudaEventDestroy(ev);
     cudaSetDevice(cur);
@@ -1755,6 +1772,213 @@ int sl_problem_trait_backward_eval(const sl_problem_desc* d, const int32_t* dg, 
     return host_backward(d, prog, dg, locus, offset, grad, nullptr);
 }
 
+// Philox4x32-10 uniform, the device stream's host twin (the L/M choice of a
+// chain's iteration, for counting the run graph's launches).
+static double host_philox_u01(uint64_t key, uint64_t c_hi, uint64_t c_lo) {
+    uint32_t c0 = (uint32_t)c_lo, c1 = (uint32_t)(c_lo >> 32), c2 = (uint32_t)c_hi, c3 = (uint32_t)(c_hi >> 32);
+    uint32_t k0 = (uint32_t)key, k1 = (uint32_t)(key >> 32);
+    for (int r = 0; r < 10; ++r) {
+        const uint64_t p0 = (uint64_t)0xD2511F53u * c0, p1 = (uint64_t)0xCD9E8D57u * c2;
+        const uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0, hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+        const uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+        c1 = lo1;
+        c3 = lo0;
+        c0 = n0;
+        c2 = n2;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    const uint64_t hi = c0 >> 5, lo = c1 >> 6;
+    return (double)(hi * 67108864ull + lo) * (1.0 / 9007199254740992.0);
+}
+
+// Add a conditional node at the current point of a stream capture and make it
+// the capture's dependency; its body graphs are returned.
+static cudaError_t capture_conditional(cudaStream_t s, cudaGraphConditionalHandle h, cudaGraphConditionalNodeType type,
+                                       unsigned size, cudaGraph_t* bodies) {
+    cudaStreamCaptureStatus st;
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    const cudaGraphEdgeData* ed = nullptr;
+    size_t nd = 0;
+    cudaError_t e = cudaStreamGetCaptureInfo(s, &st, nullptr, &g, &deps, &ed, &nd);
+    if (e != cudaSuccess) return e;
+    cudaGraphNodeParams p = {};
+    p.type = cudaGraphNodeTypeConditional;
+    p.conditional.handle = h;
+    p.conditional.type = type;
+    p.conditional.size = size;
+    cudaGraphNode_t node;
+    e = cudaGraphAddNode(&node, g, deps, ed, nd, &p);
+    if (e != cudaSuccess) return e;
+    for (unsigned i = 0; i < size; ++i) bodies[i] = p.conditional.phGraph_out[i];
+    return cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+}
+
+// The body of chain c's WHILE node: choose / shuffle / key, then a SWITCH of
+// the L-sweep (0) and the M-sweep (1), an IF that scores the chain into its
+// own LOD table, and the step to the next iteration.
+static cudaError_t capture_chain_body(sl_ctx* ctx, int c, cudaGraph_t body, cudaGraphConditionalHandle hwhile,
+                                      cudaStream_t s1, cudaStream_t s2) {
+    const ProblemDev& P = ctx->P;
+    const int M = P.M, nm = (int)ctx->meioses.size();
+    const int64_t npos = (int64_t)(M - 1) * P.n_lod;
+    const bool exact = ctx->sampler_precision == SL_SAMPLER_EXACT;
+    const cudaStreamCaptureMode mode = cudaStreamCaptureModeThreadLocal;
+    uint64_t* key = ctx->d_keys + 2 * c;
+    uint32_t* graph_c = ctx->d_dg + (size_t)c * M * P.W;
+    cudaError_t e = cudaStreamBeginCaptureToGraph(s1, body, nullptr, nullptr, 0, mode);
+    if (e != cudaSuccess) return e;
+    cudaGraph_t g = body;
+    cudaGraphConditionalHandle hsw, hscore;
+    if ((e = cudaGraphConditionalHandleCreate(&hsw, g, 2, 0)) != cudaSuccess) return e;
+    if ((e = cudaGraphConditionalHandleCreate(&hscore, g, 0, 0)) != cudaSuccess) return e;
+    if ((e = launch_chain_iter(ctx->d_run, ctx->d_chain_it, c, key, ctx->d_meioses, nm, ctx->d_morder + (size_t)c * nm,
+                               hsw, hscore, s1)) != cudaSuccess)
+        return e;
+    cudaGraph_t sw[2];
+    if ((e = capture_conditional(s1, hsw, cudaGraphCondTypeSwitch, 2, sw)) != cudaSuccess) return e;
+    // L-sweep of chain c
+    if ((e = cudaStreamBeginCaptureToGraph(s2, sw[0], nullptr, nullptr, 0, mode)) != cudaSuccess) return e;
+    e = launch_lsampler(P, ctx->d_dg, c, 1, ctx->d_even, (int)ctx->even.size(), nullptr, 0, 0, 0, 0, nullptr, 1,
+                        ctx->d_status, s2, ctx->ls_grid, ctx->ls_wpb, key);
+    if (e == cudaSuccess)
+        e = launch_lsampler(P, ctx->d_dg, c, 1, ctx->d_odd, (int)ctx->odd.size(), nullptr, 0, 0, 0, 0, nullptr, 1,
+                            ctx->d_status, s2, ctx->ls_grid, ctx->ls_wpb, key);
+    cudaError_t e2 = cudaStreamEndCapture(s2, &sw[0]);
+    if (e != cudaSuccess || (e = e2) != cudaSuccess) return e;
+    // M-sweep of chain c
+    if ((e = cudaStreamBeginCaptureToGraph(s2, sw[1], nullptr, nullptr, 0, mode)) != cudaSuccess) return e;
+    double* raw = exact ? ctx->d_raw + (size_t)c * 2 * M : ctx->d_raw + (size_t)c * M;   // fast: 2M floats
+    void* fb = exact ? (void*)((double*)ctx->d_fb + (size_t)c * 2 * M) : (void*)((float*)ctx->d_fb + (size_t)c * 2 * M);
+    e = launch_msampler(P, ctx->d_dg, c, 1, ctx->d_morder + (size_t)c * nm, nm, nm, nullptr, 0, 0, 0, nullptr, 0, raw,
+                        ctx->d_raw32 + (size_t)c * 2 * M, fb, ctx->d_badc + c, ctx->d_maps + (size_t)c * M,
+                        ctx->d_status, ctx->ms_threads, exact ? 1 : 0, s2, key);
+    e2 = cudaStreamEndCapture(s2, &sw[1]);
+    if (e != cudaSuccess || (e = e2) != cudaSuccess) return e;
+    // scoring of chain c into its own table
+    cudaGraph_t sc;
+    if ((e = capture_conditional(s1, hscore, cudaGraphCondTypeIf, 1, &sc)) != cudaSuccess) return e;
+    if ((e = cudaStreamBeginCaptureToGraph(s2, sc, nullptr, nullptr, 0, mode)) != cudaSuccess) return e;
+    double* vals = ctx->d_vals + (size_t)c * npos;
+    const int which = ctx->lod_precision == SL_LOD_FP32_RESCALED ? ctx->lod_kernel_sel : SL_LOD_KERNEL_INTERP;
+    if (which == SL_LOD_KERNEL_JIT_REG || which == SL_LOD_KERNEL_JIT_SMEM) {
+        const JitLod& j = which == SL_LOD_KERNEL_JIT_REG ? ctx->jit_reg : ctx->jit_smem;
+        e = jit_lod_launch(j, graph_c, (int64_t)M * P.W, 1, vals, ctx->d_status, P.partial, P.theta, npos, ctx->sms, s2);
+    } else {
+        e = launch_lod(P, ctx->lod_precision, graph_c, (int64_t)M * P.W, 1, vals, ctx->d_status, s2, ctx->lod_grid,
+                       ctx->lod_wpb);
+    }
+    if (e == cudaSuccess)
+        e = launch_lod_merge(vals, 1, npos, ctx->d_acc_c + (size_t)c * npos, ctx->d_init_c + (size_t)c * npos, s2);
+    e2 = cudaStreamEndCapture(s2, &sc);
+    if (e != cudaSuccess || (e = e2) != cudaSuccess) return e;
+    if ((e = launch_chain_advance(ctx->d_run, ctx->d_chain_it, c, hwhile, s1)) != cudaSuccess) return e;
+    return cudaStreamEndCapture(s1, &body);
+}
+
+// The run graph: init -> one WHILE node per chain (in parallel) -> merge of
+// the chains' LOD tables into the context's.
+static int build_run_graph(sl_ctx* ctx) {
+    const ProblemDev& P = ctx->P;
+    const int C = ctx->n_chains, M = P.M, nm = (int)ctx->meioses.size();
+    const int64_t npos = (int64_t)(M - 1) * P.n_lod;
+    const bool exact = ctx->sampler_precision == SL_SAMPLER_EXACT;
+    int rc;
+    if (!ctx->d_run && (rc = dev_alloc(ctx, (uint8_t**)&ctx->d_run, sizeof(RunParams)))) return rc;
+    if (!ctx->d_chain_it && (rc = dev_alloc(ctx, &ctx->d_chain_it, C))) return rc;
+    if (!ctx->d_keys && (rc = dev_alloc(ctx, &ctx->d_keys, 2 * (size_t)C))) return rc;
+    if (!ctx->d_acc_c && (rc = dev_alloc(ctx, &ctx->d_acc_c, (size_t)C * npos))) return rc;
+    if (!ctx->d_init_c && (rc = dev_alloc(ctx, &ctx->d_init_c, (size_t)C * npos))) return rc;
+    CK(cudaMemsetAsync(ctx->d_init_c, 0, (size_t)C * npos, ctx->stream));
+    CK(cudaMemsetAsync(ctx->d_keys, 0, sizeof(uint64_t) * 2 * C, ctx->stream));
+    // direct launches configure the kernels' shared-memory limits outside the
+    // capture (every chain's selector 0 and want = 2: they do nothing)
+    CK(cudaMemsetAsync(ctx->d_sel, 0, (size_t)C, ctx->stream));
+    CK(launch_msampler(P, ctx->d_dg, 0, C, ctx->d_morder, nm, 0, nullptr, 0, 0, 0, ctx->d_sel, 2, ctx->d_raw,
+                       ctx->d_raw32, ctx->d_fb, ctx->d_badc, ctx->d_maps, ctx->d_status, ctx->ms_threads, exact ? 1 : 0,
+                       ctx->stream, ctx->d_keys));
+    CK(launch_lsampler(P, ctx->d_dg, 0, C, ctx->d_even, (int)ctx->even.size(), nullptr, 0, 0, 0, 0, ctx->d_sel, 2,
+                       ctx->d_status, ctx->stream, ctx->ls_grid, ctx->ls_wpb, ctx->d_keys));
+    // the scoring kernel is fixed in the graph: time the candidates now if needed
+    if (ctx->lod_precision == SL_LOD_FP32_RESCALED && ctx->lod_kernel_sel == SL_LOD_KERNEL_AUTO) {
+        int st = 0;
+        CK(cudaStreamSynchronize(ctx->stream));
+        CK(cudaMemcpy(&st, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost));
+        if ((rc = autotune_lod(ctx, ctx->d_dg, std::min(C, ctx->vals_graphs)))) return rc;
+        CK(cudaStreamSynchronize(ctx->stream));
+        CK(cudaMemcpy(ctx->d_status, &st, sizeof(int), cudaMemcpyHostToDevice));   // the timing runs report nothing
+    }
+    {   // one direct scoring launch configures the scoring kernel outside the capture
+        int st = 0;
+        CK(cudaStreamSynchronize(ctx->stream));
+        CK(cudaMemcpy(&st, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost));
+        CK(launch_lod_kernel(ctx, ctx->lod_precision == SL_LOD_FP32_RESCALED ? ctx->lod_kernel_sel
+                                                                             : SL_LOD_KERNEL_INTERP,
+                             ctx->d_dg, 1));
+        CK(cudaStreamSynchronize(ctx->stream));
+        CK(cudaMemcpy(ctx->d_status, &st, sizeof(int), cudaMemcpyHostToDevice));
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
+    while ((int)ctx->cap_streams.size() < C + 1) {
+        cudaStream_t st;
+        CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        ctx->cap_streams.push_back(st);
+        cudaEvent_t ev;
+        CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        ctx->cap_events.push_back(ev);
+    }
+    cudaStream_t s0 = ctx->cap_streams[0], s1 = ctx->cap_streams[1], s2 = ctx->cap_streams[std::min(2, C)];
+    if (s2 == s1) {
+        cudaStream_t st;
+        CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        ctx->cap_streams.push_back(st);
+        s2 = st;
+    }
+    cudaGraph_t top = nullptr;
+    CK(cudaGraphCreate(&top, 0));
+    cudaError_t e = cudaStreamBeginCaptureToGraph(s0, top, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    std::vector<cudaGraphNode_t> whiles;
+    if (e == cudaSuccess) e = launch_run_init(ctx->d_run, ctx->d_chain_it, C, s0);
+    std::vector<cudaGraphNode_t> init_deps;
+    if (e == cudaSuccess) {
+        cudaStreamCaptureStatus st;
+        const cudaGraphNode_t* deps = nullptr;
+        size_t nd = 0;
+        e = cudaStreamGetCaptureInfo(s0, &st, nullptr, nullptr, &deps, nullptr, &nd);
+        if (e == cudaSuccess) init_deps.assign(deps, deps + nd);
+    }
+    for (int c = 0; c < C && e == cudaSuccess; ++c) {
+        cudaGraphConditionalHandle hw;
+        e = cudaGraphConditionalHandleCreate(&hw, top, 1, cudaGraphCondAssignDefault);
+        if (e != cudaSuccess) break;
+        cudaGraphNodeParams p = {};
+        p.type = cudaGraphNodeTypeConditional;
+        p.conditional.handle = hw;
+        p.conditional.type = cudaGraphCondTypeWhile;
+        p.conditional.size = 1;
+        cudaGraphNode_t wn;
+        e = cudaGraphAddNode(&wn, top, init_deps.data(), nullptr, init_deps.size(), &p);
+        if (e != cudaSuccess) break;
+        whiles.push_back(wn);
+        e = capture_chain_body(ctx, c, p.conditional.phGraph_out[0], hw, s1, s2);
+    }
+    if (e == cudaSuccess)
+        e = cudaStreamUpdateCaptureDependencies(s0, whiles.data(), nullptr, whiles.size(),
+                                                cudaStreamSetCaptureDependencies);
+    if (e == cudaSuccess) e = launch_chain_merge(ctx->d_acc_c, ctx->d_init_c, C, npos, ctx->d_acc, ctx->d_init, s0);
+    cudaError_t e2 = cudaStreamEndCapture(s0, &top);
+    if (e == cudaSuccess) e = e2;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&ctx->run_graph, top, 0);
+    cudaGraphDestroy(top);
+    if (e != cudaSuccess) {
+        ctx->run_graph = nullptr;
+        cudaGetLastError();
+        return fail(ctx, SL_ECUDA, "capturing the run graph: %s", cudaGetErrorString(e));
+    }
+    return SL_OK;
+}
+
 // Capture the device-driven M-sweep once: for every chain c a branch
 // memset -> founder-allele graphs (reset) -> [graphs, filter] x nm over that
 // chain alone (first = c, one chain); kernels of chains that chose the
@@ -1822,6 +2046,29 @@ int sl_run(sl_ctx* ctx, const sl_run_options* o) {
     const int C = ctx->n_chains;
     const int nm = (int)ctx->meioses.size();
     const int total = o->burnin + o->iterations;
+    if (o->first_iteration >= total) return SL_OK;
+    if (!ctx->profiling) {
+        // the whole run is one launch of the run graph
+        if (!ctx->run_graph) {
+            int rc = build_run_graph(ctx);
+            if (rc) return rc;
+        }
+        const RunParams rp{o->first_iteration, total, o->burnin, o->scoring_period, o->lsampler_prob, o->seed};
+        CK(cudaMemcpyAsync(ctx->d_run, &rp, sizeof(rp), cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaGraphLaunch(ctx->run_graph, ctx->stream));
+        int64_t kernels = 2;   // init, merge
+        for (int it = o->first_iteration; it < total; ++it) {
+            const bool score = it >= o->burnin && it % o->scoring_period == 0;
+            if (score) ctx->lod_count += (uint64_t)C;
+            for (int c = 0; c < C; ++c) {
+                const uint64_t hi = ((uint64_t)c << 40) ^ ((uint64_t)it << 4) ^ 7u;
+                const bool is_l = host_philox_u01(o->seed, hi, 0) < o->lsampler_prob;
+                kernels += 2 + (is_l ? 2 : 2 * (int64_t)nm + 1) + (score ? 2 : 0);
+            }
+        }
+        ctx->launches += kernels;
+        return SL_OK;
+    }
     if (!ctx->ms_graph && o->first_iteration < total) {
         int rc = build_ms_graph(ctx);
         if (rc) return rc;

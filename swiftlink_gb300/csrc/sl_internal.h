@@ -77,6 +77,13 @@ struct AdjDev {
     int32_t nscale;          // LI_SCALE instructions
 };
 
+// Options of a device-driven run, read by the run graph's kernels.
+struct RunParams {
+    int64_t first, end, burnin, period;
+    double lprob;
+    uint64_t seed;
+};
+
 // What code outside sl_host.cc may read of a context.
 struct CtxView {
     ProblemDev P;

@@ -1937,6 +1937,107 @@ __global__ void choose_kernel(int first, int nchain, uint64_t seed, uint64_t ite
 }
 
 // ---------------------------------------------------------------------------
+// Kernels of the run graph: every chain iterates on its own inside a WHILE
+// node (MarkovChain::run, markov_chain.cc:335-392, per replicate chain).
+// ---------------------------------------------------------------------------
+__global__ void run_init_kernel(const RunParams* rp, int64_t* it, int C) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < C) it[c] = rp->first;
+}
+
+// Start of an iteration of chain c: the L/M choice (the same draw as
+// choose_kernel), the meiosis order of an M-sweep (the same draws and swaps as
+// shuffle_kernel, the uniforms generated by the warp), the chain's Philox key
+// and whether the iteration scores.  One warp.
+__global__ void chain_iter_kernel(const RunParams* rp, const int64_t* it_arr, int c, uint64_t* key,
+                                  const int32_t* base, int nm, int32_t* order, cudaGraphConditionalHandle hsw,
+                                  cudaGraphConditionalHandle hscore) {
+    extern __shared__ double su[];
+    const int lane = threadIdx.x;
+    const int64_t it = it_arr[c];
+    if (it >= rp->end) {
+        if (lane == 0) {
+            cudaGraphSetConditional(hsw, 2);   // neither sweep
+            cudaGraphSetConditional(hscore, 0);
+        }
+        return;
+    }
+    const uint64_t seed = rp->seed, iter = (uint64_t)it;
+    const uint64_t hic = ((uint64_t)c << 40) ^ (iter << 4) ^ 7u;
+    const bool is_l = philox_u01(seed, hic, 0) < rp->lprob;
+    if (!is_l) {
+        const uint64_t hi = ((uint64_t)c << 40) ^ (iter << 4) ^ 3u;
+        for (int i = 1 + lane; i < nm; i += 32) su[i] = philox_u01(seed, hi, (uint64_t)i);
+        for (int i = lane; i < nm; i += 32) order[i] = base[i];
+        __syncwarp();
+        if (lane == 0)
+            for (int i = nm - 1; i > 0; --i) {
+                int j = (int)(su[i] * (double)(i + 1));
+                if (j > i) j = i;
+                const int32_t t = order[i];
+                order[i] = order[j];
+                order[j] = t;
+            }
+    }
+    if (lane == 0) {
+        key[0] = seed;
+        key[1] = iter;
+        cudaGraphSetConditional(hsw, is_l ? 0 : 1);
+        cudaGraphSetConditional(hscore, (it >= rp->burnin && it % rp->period == 0) ? 1 : 0);
+    }
+}
+
+__global__ void chain_advance_kernel(const RunParams* rp, int64_t* it_arr, int c, cudaGraphConditionalHandle hwhile) {
+    const int64_t next = it_arr[c] + 1;
+    it_arr[c] = next;
+    cudaGraphSetConditional(hwhile, next < rp->end ? 1 : 0);
+}
+
+// Fold the chains' LOD tables into the context's, chain by chain
+// (LODscores::merge_results, lod_score.h:98-105), and clear them.
+__global__ void chain_merge_kernel(double* acc_c, uint8_t* init_c, int C, int64_t npos, double* acc, uint8_t* init) {
+    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < npos; p += (int64_t)gridDim.x * blockDim.x) {
+        double a = acc[p];
+        uint8_t ini = init[p];
+        for (int c = 0; c < C; ++c) {
+            const size_t q = (size_t)c * npos + p;
+            if (!init_c[q]) continue;
+            a = ini ? log_sum(a, acc_c[q]) : acc_c[q];
+            ini = 1;
+            init_c[q] = 0;
+        }
+        acc[p] = a;
+        init[p] = ini;
+    }
+}
+
+cudaError_t launch_run_init(const RunParams* rp, int64_t* it, int C, cudaStream_t s) {
+    run_init_kernel<<<(C + 127) / 128, 128, 0, s>>>(rp, it, C);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_chain_iter(const RunParams* rp, const int64_t* it, int c, uint64_t* key, const int32_t* base,
+                              int nm, int32_t* order, cudaGraphConditionalHandle hsw,
+                              cudaGraphConditionalHandle hscore, cudaStream_t s) {
+    chain_iter_kernel<<<1, 32, sizeof(double) * (nm > 0 ? nm : 1), s>>>(rp, it, c, key, base, nm, order, hsw, hscore);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_chain_advance(const RunParams* rp, int64_t* it, int c, cudaGraphConditionalHandle hwhile,
+                                 cudaStream_t s) {
+    chain_advance_kernel<<<1, 1, 0, s>>>(rp, it, c, hwhile);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_chain_merge(double* acc_c, uint8_t* init_c, int C, int64_t npos, double* acc, uint8_t* init,
+                               cudaStream_t s) {
+    int64_t grid = (npos + 255) / 256;
+    if (grid > 4096) grid = 4096;
+    chain_merge_kernel<<<(int)grid, 256, 0, s>>>(acc_c, init_c, C, npos, acc, init);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
 // Host-side launchers
 // ---------------------------------------------------------------------------
 size_t lsampler_smem_per_warp(const ProblemDev& P) {
@@ -1946,7 +2047,8 @@ size_t lsampler_smem_per_warp(const ProblemDev& P) {
 
 cudaError_t launch_lsampler(const ProblemDev& P, uint32_t* dg, int first, int nchain, const int32_t* loci, int nloci,
                             const double* u, int64_t ucs, int64_t uls, uint64_t seed, uint64_t iter,
-                            const uint8_t* sel, int want, int* status, cudaStream_t s, int grid_cap, int wpb) {
+                            const uint8_t* sel, int want, int* status, cudaStream_t s, int grid_cap, int wpb,
+                            const uint64_t* key) {
     const size_t smem = wpb * lsampler_smem_per_warp(P);
     static size_t configured[2] = {0, 0};
     const int f = P.ls_fast ? 1 : 0;
@@ -1958,7 +2060,7 @@ cudaError_t launch_lsampler(const ProblemDev& P, uint32_t* dg, int first, int nc
         if (e != cudaSuccess) return e;
         configured[f] = smem;
     }
-    Draws d{u, ucs, uls, seed, iter, 1, nullptr};
+    Draws d{u, ucs, uls, seed, iter, 1, key};
     const int64_t ntask = (int64_t)nchain * nloci;
     int64_t grid = (ntask + wpb - 1) / wpb;
     if (grid > grid_cap) grid = grid_cap;
