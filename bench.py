@@ -290,7 +290,7 @@ def run_ours(args):
     barrier()
     torch.cuda.synchronize()
     clocks.start()
-    ctx.profile(True)
+    # each step is one launch of the run graph: one MCMC iteration of every chain
     for i in range(K):
         with torch.cuda.stream(stream):
             flush.fill_(i & 0xff)
@@ -302,41 +302,46 @@ def run_ours(args):
     torch.cuda.synchronize()
     barrier()
     clk = clocks.stop()
-    kern = {k: ctx.profile_read(k) for k in range(5)}
-    ctx.profile(False)
     gpu_launches = ctx.launches - launches0
-    t_ms = sum(a.elapsed_time(b) for a, b in ev)
-    t_s = allmax(t_ms / 1e3)
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    t_s = allmax(sum(step_ms) / 1e3)
     value = K * C * world / t_s
 
-    # algorithmic bytes per launch of each kernel class over the timed iterations
+    # algorithmic bytes of the timed run-graph launches: every chain-step moves
+    # step_bytes, every scored graph position_bytes per position
     n_l = [sum(philox.chooses_l(seed, c, W + i, LPROB) for c in range(C)) for i in range(K)]
     sb = step_bytes(N, F, M)
     scorings = sum(1 for i in range(K) if (W + i) % PERIOD == 0)
-    alg = {
-        0: sum(nl * sb / 2.0 for nl in n_l for _ in range(2)),      # two half-sweeps per iteration
-        1: sum((C - nl) * sb for nl in n_l),
-        2: scorings * C * npos * position_bytes(N, F, n),
-    }
-    lod_kernel_names = {api.SL_LOD_KERNEL_INTERP: "lod_prog_kernel", api.SL_LOD_KERNEL_JIT_REG: "sl_lod_jit (registers)",
-                        api.SL_LOD_KERNEL_JIT_SMEM: "sl_lod_jit (shared memory)"}
-    sel, jit_ms = ctx.lod_kernel_info()
-    names = {0: "lsampler_kernel", 1: "fag_kernel+ffbs_scan_kernel", 2: lod_kernel_names.get(sel, "lod_kernel"),
-             3: "lod_merge_kernel", 4: "choose/shuffle"}
-    dom = max(kern, key=lambda k: kern[k][0])
-    dom_ms, dom_n = kern[dom]
+    alg_total = K * C * sb + scorings * C * npos * position_bytes(N, F, n)
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
         os.path.join(ROOT, "MEASURED_PEAKS.json")) else {"hbm_gbs": 6800.0}
     peak = float(peaks.get("hbm_gbs", 6800.0))
-    per_launch = alg.get(dom, 0.0) / max(1, dom_n)
-    avg_s = dom_ms / 1e3 / max(1, dom_n)
-    achieved = per_launch / avg_s / 1e9 if avg_s > 0 else 0.0
-    roofline = {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": traffic_from_profiles(names[dom]),
+    per_launch = alg_total / K
+    avg_s = sum(step_ms) / 1e3 / K
+    achieved = per_launch / avg_s / 1e9
+    run_graph_name = "run graph (one MCMC iteration of every chain)"
+
+    # kernel shares from a separate profiled pass: the same iterations with
+    # per-kernel-class events (the host-driven path, kernels launched one by one)
+    lod_kernel_names = {api.SL_LOD_KERNEL_INTERP: "lod_prog_kernel", api.SL_LOD_KERNEL_JIT_REG: "sl_lod_jit (registers)",
+                        api.SL_LOD_KERNEL_JIT_SMEM: "sl_lod_jit (shared memory)"}
+    sel, jit_ms = ctx.lod_kernel_info()
+    names = {0: "lsampler_kernel<float>", 1: "fag_warp_kernel+ffbs_scan_kernel", 2: lod_kernel_names.get(sel, "lod_kernel"),
+             3: "lod_merge_kernel", 4: "choose/shuffle"}
+    Kp = min(K, 10)
+    ctx.profile(True)
+    ctx.run(iterations=W + K + Kp, burnin=0, period=PERIOD, lprob=LPROB, seed=seed, first_iteration=W + K)
+    ctx.synchronize()
+    kern = {k: ctx.profile_read(k) for k in range(5)}
+    ctx.profile(False)
+    tot = max(1e-9, sum(x[0] for x in kern.values()))
+    roofline = {"bound": "hbm", "kernel": run_graph_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": traffic_from_profiles(run_graph_name),
                 "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if "when" in peaks else "fallback",
                 "algorithmic_bytes_per_launch": per_launch, "avg_launch_ms": 1e3 * avg_s,
-                "kernel_share": {names[k]: round(v[0] / max(1e-9, sum(x[0] for x in kern.values())), 4)
-                                 for k, v in kern.items()}}
+                "note": "latency-bound integer and FP32 work on small rfunctions: the HBM fraction is small by "
+                        "construction; SM issue utilisation per kernel is in profiles/",
+                "kernel_share_profiled_pass": {names[k]: round(v[0] / tot, 4) for k, v in kern.items()}}
 
     # ---------------- LOD positions/s, batched (many graphs per launch, FP32) vs plain (FP64, one graph)
     graphs = ctx.get_graphs()
@@ -351,6 +356,23 @@ def run_ours(args):
     pctx.set_graphs(gset[:1])
     pstream = torch.cuda.ExternalStream(pctx.stream_handle())
     plain_lod_pos_s = timed_lod(pctx, pstream, flush, 1, npos, reps=3)
+
+    # ---------------- the error of the batched form: one scoring of the 64-graph set in
+    # FP32 with rescaling against FP64, per-position |dLOD|
+    lctx.lod_reset()
+    lctx.lod_score_chains()
+    raw32, c32, tp32 = lctx.lod_results()
+    with api.Context(prob, n_chains=G, lod_precision=api.SL_LOD_FP64, device=local,
+                     lod_flags=api.SL_LOD_ZERO_OK) as p64:
+        p64.set_graphs(gset)
+        p64.lod_score_chains()
+        raw64, c64, tp64 = p64.lod_results()
+    fin = raw64 > -1e300
+    dlod = float(np.abs(api.lod_table(raw32, c32, tp32) - api.lod_table(raw64, c64, tp64))[fin].max())
+
+    # ---------------- adjoint of the trait peel (dominant model 0.01/0.8/0.9, q = 1e-3) over
+    # 16 stored graphs, through sl_trait_backward with host graphs and gradients
+    adj = adjoint_rate(d, gset[:16], local)
 
     # ---------------- plain form: one chain, FP64 LOD
     pctx.run(iterations=W, burnin=0, period=PERIOD, lprob=LPROB, seed=seed)
@@ -403,6 +425,8 @@ def run_ours(args):
                          "form": "one chain per launch, exact FP64 samplers, FP64 LOD peel"},
                "batched_vs_plain": {"steps": value / (plain_steps_s * world),
                                     "lod_positions": lod_pos_s / plain_lod_pos_s},
+               "max_abs_dlod_fp32_vs_fp64": dlod,
+               "adjoint": adj,
                "gpu_launches": int(gpu_launches), "roofline": roofline, "clocks": clk, "e2e": e2e}
         if world == 1:
             out["cpu_baseline"] = cpu_baseline_sample()
@@ -411,6 +435,25 @@ def run_ours(args):
         c.close()
     if dist:
         dist.destroy_process_group()
+
+
+def adjoint_rate(d, graphs, device):
+    from swiftlink_gb300.workloads import disease_probs
+    pen, q = (0.01, 0.8, 0.9), 1e-3
+    dd = dict(d, penetrance=np.array(pen), freq=np.float64(q),
+              disease_prob=disease_probs(d["affection"], d["mother"] < 0, q, pen))
+    npos = (d["M"] - 1) * d["n_lod"]
+    with api.Context(api.Problem.from_arrays(dd, with_legal=False), n_chains=1, device=device,
+                     lod_precision=api.SL_LOD_FP32_RESCALED, lod_flags=api.SL_LOD_ZERO_OK) as ctx:
+        ctx.trait_backward(graphs[:1])
+        reps = 3
+        t = time.perf_counter()
+        for _ in range(reps):
+            grad, pt = ctx.trait_backward(graphs)
+        dt = (time.perf_counter() - t) / reps
+    return {"value": graphs.shape[0] * npos / dt, "unit": "positions/s", "graphs": int(graphs.shape[0]),
+            "model": "dominant (0.01, 0.8, 0.9), q = 1e-3",
+            "path": "sl_trait_backward: host graphs in, d log L / d (theta_L, theta_R, penetrances, q) out"}
 
 
 def timed_lod(ctx, stream, flush, G, npos, reps):
