@@ -438,6 +438,7 @@ def run_ours(args):
 
 
 def adjoint_rate(d, graphs, device):
+    from swiftlink_gb300 import api
     from swiftlink_gb300.workloads import disease_probs
     pen, q = (0.01, 0.8, 0.9), 1e-3
     dd = dict(d, penetrance=np.array(pen), freq=np.float64(q),
