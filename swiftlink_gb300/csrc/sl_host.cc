@@ -1068,6 +1068,22 @@ int sl_create(const sl_problem_desc* d, const sl_options* opt, sl_ctx** out) {
     if ((rc = upload(ctx, (double**)&P.theta, d->theta, M - 1))) return bail(rc);
     if ((rc = upload(ctx, (double**)&P.partial, d->partial_theta, M - 1))) return bail(rc);
     if ((rc = upload(ctx, (double**)&P.minor, d->minor_freq, M))) return bail(rc);
+    {   // FP32 and logarithm tables of the fast kernels
+        std::vector<float> thf(M - 1), pf(M - 1), prf(ctx->prior_table.size());
+        std::vector<double> lt(M - 1), la(M - 1);
+        for (int i = 0; i < M - 1; ++i) {
+            thf[i] = (float)d->theta[i];
+            pf[i] = (float)d->partial_theta[i];
+            lt[i] = std::log(d->theta[i]);
+            la[i] = std::log(1.0 - d->theta[i]);
+        }
+        for (size_t i = 0; i < prf.size(); ++i) prf[i] = (float)ctx->prior_table[i];
+        if ((rc = upload(ctx, (float**)&P.theta_f, thf.data(), M - 1))) return bail(rc);
+        if ((rc = upload(ctx, (float**)&P.partial_f, pf.data(), M - 1))) return bail(rc);
+        if ((rc = upload(ctx, (double**)&P.log_theta, lt.data(), M - 1))) return bail(rc);
+        if ((rc = upload(ctx, (double**)&P.log_itheta, la.data(), M - 1))) return bail(rc);
+        if ((rc = upload(ctx, (float**)&P.prior_f, prf.data(), prf.size()))) return bail(rc);
+    }
     if ((rc = upload(ctx, (double**)&P.dprob, d->disease_prob, (size_t)4 * N))) return bail(rc);
     if ((rc = upload(ctx, (uint8_t**)&P.dmask, dmask.data(), N))) return bail(rc);
     if ((rc = upload(ctx, (OpDev**)&P.ops, ops.data(), K))) return bail(rc);
@@ -1404,7 +1420,7 @@ static cudaError_t launch_lod_kernel(sl_ctx* ctx, int which, const uint32_t* gra
     const int64_t npos = (int64_t)(P.M - 1) * P.n_lod;
     if (which == SL_LOD_KERNEL_JIT_REG || which == SL_LOD_KERNEL_JIT_SMEM) {
         const JitLod& j = which == SL_LOD_KERNEL_JIT_REG ? ctx->jit_reg : ctx->jit_smem;
-        return jit_lod_launch(j, graphs, (int64_t)P.M * P.W, G, ctx->d_vals, ctx->d_status, P.partial, P.theta,
+        return jit_lod_launch(j, graphs, (int64_t)P.M * P.W, G, ctx->d_vals, ctx->d_status, P.partial_f, P.log_theta, P.log_itheta,
                               npos * G, ctx->sms, ctx->stream);
     }
     return launch_lod(P, ctx->lod_precision, graphs, (int64_t)P.M * P.W, G, ctx->d_vals, ctx->d_status, ctx->stream,
@@ -1864,7 +1880,7 @@ static cudaError_t capture_chain_body(sl_ctx* ctx, int c, cudaGraph_t body, cuda
     const int which = ctx->lod_precision == SL_LOD_FP32_RESCALED ? ctx->lod_kernel_sel : SL_LOD_KERNEL_INTERP;
     if (which == SL_LOD_KERNEL_JIT_REG || which == SL_LOD_KERNEL_JIT_SMEM) {
         const JitLod& j = which == SL_LOD_KERNEL_JIT_REG ? ctx->jit_reg : ctx->jit_smem;
-        e = jit_lod_launch(j, graph_c, (int64_t)M * P.W, 1, vals, ctx->d_status, P.partial, P.theta, npos, ctx->sms, s2);
+        e = jit_lod_launch(j, graph_c, (int64_t)M * P.W, 1, vals, ctx->d_status, P.partial_f, P.log_theta, P.log_itheta, npos, ctx->sms, s2);
     } else {
         e = launch_lod(P, ctx->lod_precision, graph_c, (int64_t)M * P.W, 1, vals, ctx->d_status, s2, ctx->lod_grid,
                        ctx->lod_wpb);

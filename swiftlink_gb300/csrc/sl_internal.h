@@ -53,6 +53,12 @@ struct ProblemDev {
     int32_t prog_threads;                // threads per block of the program kernel
     int32_t lod_zero_ok;                 // a zero trait likelihood is a zero term, not an error
     int32_t ls_fast;                     // L-sampler in FP32 with per-rfunction rescaling
+    // FP32 / precomputed copies for the fast kernels
+    const float* theta_f;                // [M-1]
+    const float* partial_f;              // [M-1]
+    const double* log_theta;             // [M-1] log(theta)
+    const double* log_itheta;            // [M-1] log(1 - theta)
+    const float* prior_f;                // [M][4][4]
 };
 
 // Instructions of a compiled trait-peel program (the batched LOD scorer).

@@ -67,8 +67,8 @@ std::string jit_source(const JitProgramIn& in, int threads, bool shared) {
     s += "typedef unsigned int u32;\n";
     emitf(s,
           "extern \"C\" __global__ void __launch_bounds__(S) sl_lod_jit(const u32* __restrict__ graphs, long long gw,\n"
-          "    int G, double* __restrict__ vals, int* status, const double* __restrict__ partial,\n"
-          "    const double* __restrict__ theta) {\n");
+          "    int G, double* __restrict__ vals, int* status, const float* __restrict__ partial,\n"
+          "    const double* __restrict__ lt_tab, const double* __restrict__ la_tab) {\n");
     if (shared) s += "  extern __shared__ float sh[];\n  float* A = sh + threadIdx.x;\n";
     emitf(s, "  const long long npos = %lldLL;\n", (long long)npos);
     s += "  const long long ntask = (long long)G * npos;\n";
@@ -78,8 +78,8 @@ std::string jit_source(const JitProgramIn& in, int threads, bool shared) {
     emitf(s, "    const u32* cL = graphs + (long long)b * gw + (long long)l * %d;\n    const u32* cR = cL + %d;\n", in.W,
           in.W);
     for (int w = 0; w < in.W; ++w) emitf(s, "    const u32 wL%d = cL[%d], wR%d = cR[%d];\n", w, w, w, w);
-    emitf(s, "    const double thd = partial[l] * (double)(o + 1), th2d = partial[l] * (double)(%d - o);\n", in.n);
-    s += "    const float th = (float)thd, an = (float)(1.0 - thd), th2 = (float)th2d, an2 = (float)(1.0 - th2d);\n";
+    emitf(s, "    const float th = partial[l] * (float)(o + 1), th2 = partial[l] * (float)(%d - o);\n", in.n);
+    s += "    const float an = 1.0f - th, an2 = 1.0f - th2;\n";
     s += "    int scale = 0;\n";
     // slot -> current value name
     std::vector<int> cur;
@@ -174,12 +174,11 @@ std::string jit_source(const JitProgramIn& in, int threads, bool shared) {
     emitf(s, "    const float result = %s;\n", result.c_str());
     s += "    int cross = 0;\n";
     for (int w = 0; w < in.W; ++w) emitf(s, "    cross += __popc(wL%d ^ wR%d);\n", w, w);
-    s += "    const double lt = log(theta[l]), la = log(1.0 - theta[l]);\n";
-    emitf(s, "    const double rec = cross * lt + (%d - cross) * la;\n", 2 * in.Nnf);
+    emitf(s, "    const double rec = cross * lt_tab[l] + (%d - cross) * la_tab[l];\n", 2 * in.Nnf);
     s += "    double v;\n";
     emitf(s,
           "    if (!(result > 0.0f)) { %s v = -1.7976931348623157e308; }\n"
-          "    else v = log((double)result) + (double)scale * 0.69314718055994530942 - rec - (%.17g);\n",
+          "    else v = (double)logf(result) + (double)scale * 0.69314718055994530942 - rec - (%.17g);\n",
           in.zero_ok ? "" : ("atomicCAS(status, 0, " + std::to_string((int)ST_LOD_NONPOS) + ");").c_str(),
           in.marker_trans);
     s += "    vals[t] = v;\n  }\n}\n";
@@ -274,14 +273,14 @@ void jit_lod_release(JitLod* j) {
 }
 
 cudaError_t jit_lod_launch(const JitLod& j, const uint32_t* graphs, int64_t graph_words, int G, double* vals,
-                           int* status, const double* partial, const double* theta, int64_t ntask, int sms,
-                           cudaStream_t s) {
+                           int* status, const float* partial, const double* lt, const double* la, int64_t ntask,
+                           int sms, cudaStream_t s) {
     int64_t grid = (ntask + j.threads - 1) / j.threads;
     const int64_t cap = (int64_t)sms * j.blocks_per_sm * 4;
     if (grid > cap) grid = cap;
     long long gw = graph_words;
     void* args[] = {(void*)&graphs, (void*)&gw, (void*)&G, (void*)&vals, (void*)&status, (void*)&partial,
-                    (void*)&theta};
+                    (void*)&lt, (void*)&la};
     return cudaLaunchKernel((const void*)j.kern, dim3((unsigned)grid), dim3(j.threads), args, j.smem, s);
 }
 

@@ -35,7 +35,7 @@ std::string jit_lod_source(const JitProgramIn& in, int threads, bool shared);
 int jit_lod_compile(const JitProgramIn& in, int threads, bool shared, JitLod* out, std::string* log);
 void jit_lod_release(JitLod* j);
 cudaError_t jit_lod_launch(const JitLod& j, const uint32_t* graphs, int64_t graph_words, int G, double* vals,
-                           int* status, const double* partial, const double* theta, int64_t ntask, int sms,
-                           cudaStream_t s);
+                           int* status, const float* partial, const double* lt, const double* la, int64_t ntask,
+                           int sms, cudaStream_t s);
 
 }  // namespace sl

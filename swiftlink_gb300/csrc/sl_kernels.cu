@@ -220,10 +220,17 @@ __global__ void __launch_bounds__(128) lsampler_kernel(ProblemDev P, uint32_t* d
         const uint32_t* colL = l > 0 ? colC - P.W : nullptr;
         const uint32_t* colR = l < P.M - 1 ? colC + P.W : nullptr;
         T th = T(1), an = T(1), th2 = T(1), an2 = T(1);
-        if (l > 0) { th2 = (T)P.theta[l - 1]; an2 = (T)DSUB(1.0, P.theta[l - 1]); }
-        if (l < P.M - 1) { th = (T)P.theta[l]; an = (T)DSUB(1.0, P.theta[l]); }
+        if constexpr (sizeof(T) == 4) {
+            if (l > 0) { th2 = P.theta_f[l - 1]; an2 = 1.f - th2; }
+            if (l < P.M - 1) { th = P.theta_f[l]; an = 1.f - th; }
+        } else {
+            if (l > 0) { th2 = P.theta[l - 1]; an2 = DSUB(1.0, P.theta[l - 1]); }
+            if (l < P.M - 1) { th = P.theta[l]; an = DSUB(1.0, P.theta[l]); }
+        }
         const uint8_t* gcol = P.geno + (size_t)l * P.N;
-        const double* pri = P.prior + (size_t)l * 16;
+        const T* pri;
+        if constexpr (sizeof(T) == 4) pri = (const T*)(P.prior_f + (size_t)l * 16);
+        else pri = (const T*)(P.prior + (size_t)l * 16);
         // forward peel over the valid cells of every rfunction
         for (int k = 0; k < P.K; ++k) {
             const OpDev op = P.ops[k];
@@ -231,14 +238,14 @@ __global__ void __launch_bounds__(128) lsampler_kernel(ProblemDev P, uint32_t* d
             __syncwarp();
             const int ncell = 1 << (2 * op.c);
             const int32_t* cut = P.opdata + op.cut_at;
-            const double* trait = pri + 4 * (gcol[op.peel] & 3);
+            const T* trait = pri + 4 * (gcol[op.peel] & 3);
             T* out = A + op.mat_off;
             T mx = T(0);
             for (int cell = lane; cell < ncell; cell += 32) {
                 T total = T(0);
                 if (ls_valid(cut, op.c, gcol, cell)) {
                     for (int v = 0; v < 4; ++v) {
-                        const T tv = (T)trait[v];
+                        const T tv = trait[v];
                         if (tv == T(0)) continue;
                         total = Ar::add(total, ls_term<T>(P, op, A, dist, cell, v, tv));
                     }
@@ -274,7 +281,7 @@ __global__ void __launch_bounds__(128) lsampler_kernel(ProblemDev P, uint32_t* d
             ls_dists<T>(P, op, colL, colR, l, th, an, th2, an2, dist, lane);
             __syncwarp();
             const int32_t* cut = P.opdata + op.cut_at;
-            const double* trait = pri + 4 * (gcol[op.peel] & 3);
+            const T* trait = pri + 4 * (gcol[op.peel] & 3);
             int cellidx = 0;
             bool known = true;
             for (int q = 0; q < op.c; ++q) {
@@ -284,7 +291,7 @@ __global__ void __launch_bounds__(128) lsampler_kernel(ProblemDev P, uint32_t* d
             }
             T pv = T(0);
             if (lane < 4 && known) {
-                const T tv = (T)trait[lane];
+                const T tv = trait[lane];
                 if (tv != T(0) && ls_valid(cut, op.c, gcol, cellidx)) pv = ls_term<T>(P, op, A, dist, cellidx, lane, tv);
             }
             const T p0 = __shfl_sync(FULLMASK, pv, 0), p1 = __shfl_sync(FULLMASK, pv, 1);
@@ -1278,13 +1285,13 @@ __global__ void __launch_bounds__(1024) ffbs_scan_kernel(ProblemDev P, uint32_t*
         uint8_t* smaps = (uint8_t*)(words + M);
         for (int i = tid; i < M; i += T) words[i] = G[(size_t)i * P.W + (m >> 5)];
         for (int i = tid; i < 2 * M; i += T) sr[i] = r[i];
-        for (int i = tid; i < M; i += T) th[i] = i > 0 ? (float)P.theta[i - 1] : 0.f;
+        for (int i = tid; i < M; i += T) th[i] = i > 0 ? P.theta_f[i - 1] : 0.f;
         r = sr;
         fb = sfb;
         maps = smaps;
     }
     __syncthreads();
-    auto tof = [&](int i) { return th ? th[i] : (i > 0 ? (float)P.theta[i - 1] : 0.f); };
+    auto tof = [&](int i) { return th ? th[i] : (i > 0 ? P.theta_f[i - 1] : 0.f); };
     const int L = (M + T - 1) / T;
     const int s0 = min(M, tid * L), s1 = min(M, s0 + L);
     // chunk product P = A_{s1-1} ... A_{s0} (A_0 = diag(r_0)); an empty chunk is the identity
@@ -1643,9 +1650,8 @@ __global__ void __launch_bounds__(128) lod_prog_kernel(ProblemDev P, const uint3
         const int l = (int)(pidx / n), o = (int)(pidx % n);
         const uint32_t* colL = graphs + (size_t)b * graph_words + (size_t)l * P.W;
         const uint32_t* colR = colL + P.W;
-        const double thd = P.partial[l] * (double)(o + 1);
-        const double th2d = P.partial[l] * (double)(n - o);
-        const float th = (float)thd, an = (float)(1.0 - thd), th2 = (float)th2d, an2 = (float)(1.0 - th2d);
+        const float th = P.partial_f[l] * (float)(o + 1), an = 1.f - th;
+        const float th2 = P.partial_f[l] * (float)(n - o), an2 = 1.f - th2;
         int scale = 0;
         float result = 0.f;
         const int32_t* pc = P.prog;
@@ -1698,14 +1704,14 @@ __global__ void __launch_bounds__(128) lod_prog_kernel(ProblemDev P, const uint3
         // DescentGraph::get_recombination_prob (descent_graph.cc:212-242) by crossover count
         int cross = 0;
         for (int w = 0; w < P.W; ++w) cross += __popc(colL[w] ^ colR[w]);
-        const double lt = log(P.theta[l]), la = log(1.0 - P.theta[l]);
-        const double rec = cross * lt + (2 * P.Nnf - cross) * la;
+        const double rec = cross * P.log_theta[l] + (2 * P.Nnf - cross) * P.log_itheta[l];
         double v;
         if (!(result > 0.f)) {
             if (!P.lod_zero_ok) set_status(status, ST_LOD_NONPOS);
             v = -DBL_MAX;
         } else {
-            v = log((double)result) + (double)scale * 0.69314718055994530942 - rec - P.marker_trans;
+            // log of an FP32 value in FP32 (error ~1e-7, far inside the LOD tolerance)
+            v = (double)logf(result) + (double)scale * 0.69314718055994530942 - rec - P.marker_trans;
         }
         vals[t] = v;
     }
@@ -1741,12 +1747,10 @@ __global__ void __launch_bounds__(128) trait_adjoint_kernel(ProblemDev P, AdjDev
         const int l = (int)(pidx / n), o = (int)(pidx % n);
         colL = graphs + (size_t)b * graph_words + (size_t)l * P.W;
         colR = colL + P.W;
-        const double thd = P.partial[l] * (double)(o + 1);
-        const double th2d = P.partial[l] * (double)(n - o);
-        th = (float)thd;
-        an = (float)(1.0 - thd);
-        th2 = (float)th2d;
-        an2 = (float)(1.0 - th2d);
+        th = P.partial_f[l] * (float)(o + 1);
+        an = 1.f - th;
+        th2 = P.partial_f[l] * (float)(n - o);
+        an2 = 1.f - th2;
     }
     float* a = A + u;
     float* g = B + u;
