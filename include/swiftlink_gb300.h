@@ -214,7 +214,25 @@ typedef struct sl_run_options {
     int32_t first_iteration;    /* iteration index of the first step (for resumable runs) */
     double lsampler_prob;
     uint64_t seed;
+    int32_t exchange_period;    /* MC3: iterations between exchanges of adjacent chains' graphs, 0 = none
+                                   (Mc3::run, mc3.cc:83-162) */
 } sl_run_options;
+
+/* MC3 temperatures, one per chain in exchange order (chain 0 the coldest; the
+ * reference's default is t_i = 1 / (1 + 0.001 2^i) for i > 0, mc3.cc:38-46).
+ * A chain at temperature t samples with theta_t = t theta + (1 - t) / 2 and
+ * maf_t = t maf + (1 - t) / 2 (GeneticMap::set_temperature, genetic_map.cc:
+ * 95-117); only chains at t = 1 are scored (markov_chain.cc:173-174). */
+int sl_set_temperatures(sl_ctx* ctx, const double* temps);
+
+/* Exchange statistics of adjacent pairs (c, c+1), c < n_chains - 1: proposals
+ * and acceptances so far (mc3.cc:166-176). */
+int sl_mc3_stats(sl_ctx* ctx, int64_t* accepted, int64_t* proposed);
+
+/* log P(G, graph) of chain g's descent graph under chain t's map
+ * (DescentGraph::get_likelihood2, descent_graph.h:78-84): the value the
+ * exchange step compares.  LOG_ZERO (-DBL_MAX) for an illegal graph. */
+int sl_chain_loglik(sl_ctx* ctx, int32_t graph_chain, int32_t map_chain, double* loglik);
 
 int sl_run(sl_ctx* ctx, const sl_run_options* opt);
 

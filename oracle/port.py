@@ -159,3 +159,15 @@ def derive_priors(genotypes, typed, minor):
 
 def philox_uniform(key: int, hi: int, lo: int) -> float:
     return lib().slo_philox_uniform(key, hi, lo)
+
+
+def tempered(prob: dict, t: float) -> dict:
+    """The problem as a chain at MC3 temperature t sees it
+    (GeneticMap::set_temperature, genetic_map.cc:95-117): theta_t = (t theta) +
+    ((1 - t) 0.5) and maf_t likewise, in that operation order; the L-sampler
+    priors keep temperature 1 (they are cached while parsing,
+    pedigree_parser.cc:157)."""
+    d = dict(prob)
+    d["theta"] = (t * np.asarray(prob["theta"], np.float64)) + ((1 - t) * 0.5)
+    d["minor"] = (t * np.asarray(prob["minor"], np.float64)) + ((1 - t) * 0.5)
+    return d

@@ -155,6 +155,15 @@ class Ref:
         lib().ref_loglik(_p(self.h), _ptr(dg), ctypes.byref(ll))
         return ll.value
 
+    def set_temperature(self, t: float):
+        lib().ref_set_temperature(_p(self.h), ctypes.c_double(t))
+
+    def loglik_tempered(self, dg: np.ndarray, t: float) -> float:
+        dg = np.ascontiguousarray(dg, np.int32)
+        ll = ctypes.c_double()
+        lib().ref_loglik_tempered(_p(self.h), _ptr(dg), ctypes.c_double(t), ctypes.byref(ll))
+        return ll.value
+
     def lstep(self, dg: np.ndarray, locus: int, u: np.ndarray):
         dg = np.ascontiguousarray(dg, np.int32).copy()
         u = np.ascontiguousarray(u, np.float64)

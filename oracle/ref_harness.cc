@@ -201,6 +201,30 @@ extern "C" int ref_loglik(void* h, const int* dg_in_buf, double* loglik) {
     return 0;
 }
 
+// Temper the map in place (GeneticMap::set_temperature, once per map) and
+// rebuild the samplers on it, as a tempered MarkovChain holds them.
+extern "C" int ref_set_temperature(void* h, double t) {
+    RefState* s = (RefState*)h;
+    s->map.set_temperature(t);
+    delete s->ls;
+    delete s->ms;
+    s->ls = new LocusSampler(s->ped, &s->map, s->psg, 0, s->sex_linked);
+    s->ms = new MeiosisSampler(s->ped, &s->map, s->sex_linked);
+    return 0;
+}
+
+// get_likelihood2 under a copy of the map at MC3 temperature t, as
+// MarkovChain::get_likelihood does for a tempered chain (markov_chain.h:122-124).
+extern "C" int ref_loglik_tempered(void* h, const int* dg_in_buf, double t, double* loglik) {
+    RefState* s = (RefState*)h;
+    GeneticMap m(s->map);
+    if (t != 1.0) m.set_temperature(t);
+    DescentGraph dg(s->ped, &s->map, s->sex_linked);
+    dg_in(s, dg, dg_in_buf);
+    *loglik = dg.get_likelihood2(&m);
+    return 0;
+}
+
 // One L-sampler step at `locus` (locus_sampler2.cc:128-159 after set_locus_minimal).
 extern "C" int ref_lstep(void* h, int* dg_io, int locus, const double* u, int n_u, int* n_used) {
     RefState* s = (RefState*)h;

@@ -803,12 +803,16 @@ out:
 double slo_loglik(const slo_problem* p, const int32_t* dg) {
     int M = p->M, N = p->N;
     double marker_trans = log(0.5) * (2 * (N - p->F));
+    /* DescentGraph::_recombination_prob (descent_graph.cc:200-210): a sum of the
+       per-interval sums of get_recombination_prob (descent_graph.cc:212-242) */
     double rec = 0.0;
     for (int l = 0; l < M - 1; ++l) {
         double lt = log(p->theta[l]), la = log(1.0 - p->theta[l]);
+        double r = 0.0;
         for (int i = p->F; i < N; ++i)
             for (int j = 0; j < 2; ++j)
-                rec += (dgget(p, dg, i, l, j) != dgget(p, dg, i, l + 1, j)) ? lt : la;
+                r += (dgget(p, dg, i, l, j) != dgget(p, dg, i, l + 1, j)) ? lt : la;
+        rec += r;
     }
     fws f;
     fws_init(p, &f);

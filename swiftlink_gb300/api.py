@@ -29,7 +29,8 @@ EXPORTED = [
     "sl_lod_reset", "sl_run", "sl_synchronize", "sl_device_status", "sl_launch_count",
     "sl_version", "sl_get_stream", "sl_profile", "sl_profile_read", "sl_problem_legal_masks",
     "sl_problem_trait_priors", "sl_problem_trait_prob", "sl_trait_backward",
-    "sl_problem_trait_backward_eval", "sl_lod_kernel_info",
+    "sl_problem_trait_backward_eval", "sl_lod_kernel_info", "sl_set_temperatures", "sl_mc3_stats",
+    "sl_chain_loglik",
 ]
 
 
@@ -64,7 +65,8 @@ class Options(ctypes.Structure):
 class RunOptions(ctypes.Structure):
     _fields_ = [("iterations", ctypes.c_int32), ("burnin", ctypes.c_int32),
                 ("scoring_period", ctypes.c_int32), ("first_iteration", ctypes.c_int32),
-                ("lsampler_prob", ctypes.c_double), ("seed", ctypes.c_uint64)]
+                ("lsampler_prob", ctypes.c_double), ("seed", ctypes.c_uint64),
+                ("exchange_period", ctypes.c_int32)]
 
 
 _lib = None
@@ -305,9 +307,26 @@ class Context:
         return grad, pt
 
     def run(self, iterations: int, burnin: int = 0, period: int = 10, lprob: float = 0.5,
-            seed: int = 1, first_iteration: int = 0):
-        o = RunOptions(iterations, burnin, period, first_iteration, lprob, seed)
+            seed: int = 1, first_iteration: int = 0, exchange_period: int = 0):
+        o = RunOptions(iterations, burnin, period, first_iteration, lprob, seed, exchange_period)
         self._check(lib().sl_run(self.h, ctypes.byref(o)))
+
+    def set_temperatures(self, temps):
+        t = np.ascontiguousarray(temps, np.float64)
+        assert t.shape == (self.n_chains,)
+        self._check(lib().sl_set_temperatures(self.h, _p(t)))
+
+    def mc3_stats(self):
+        n = max(1, self.n_chains - 1)
+        acc = np.zeros(n, np.int64)
+        prop = np.zeros(n, np.int64)
+        self._check(lib().sl_mc3_stats(self.h, _p(acc), _p(prop)))
+        return acc[: self.n_chains - 1], prop[: self.n_chains - 1]
+
+    def chain_loglik(self, graph_chain: int, map_chain: int) -> float:
+        v = ctypes.c_double()
+        self._check(lib().sl_chain_loglik(self.h, int(graph_chain), int(map_chain), ctypes.byref(v)))
+        return v.value
 
     def stream_handle(self) -> int:
         h = _vp()

@@ -68,7 +68,10 @@ def build(verbose: bool = False, force: bool = False) -> str:
                          "-Xptxas", "-v", "-c", src, "-o", obj])
     for src, obj in ((cc, cc_o), (jc, jc_o)):
         if force or _stale(obj, [src] + hdrs):
-            jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-Wall", "-I" + os.path.join(cuda, "include"),
+            # no contraction of a * b + c into FMA: host FP64 (priors, tempered maps,
+            # likelihood sums) must round as the reference's x86-64 build does, on aarch64 too
+            jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-Wall", "-ffp-contract=off",
+                         "-I" + os.path.join(cuda, "include"),
                          "-c", src, "-o", obj])
     logs = []
     if jobs:

@@ -12,8 +12,10 @@
 #include <cstring>
 #include <map>
 #include <string>
+#include <cfloat>
 #include <chrono>
 #include <thread>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/swiftlink_gb300.h"
@@ -35,8 +37,11 @@ cudaError_t launch_msampler(const ProblemDev& P, uint32_t* dg, int first, int nc
 cudaError_t launch_set_key(uint64_t* key, uint64_t seed, uint64_t iter, cudaStream_t s);
 cudaError_t launch_run_init(const RunParams* rp, int64_t* it, int C, cudaStream_t s);
 cudaError_t launch_chain_iter(const RunParams* rp, const int64_t* it, int c, uint64_t* key, const int32_t* base,
-                              int nm, int32_t* order, cudaGraphConditionalHandle hsw,
+                              int nm, int32_t* order, const double* temp, cudaGraphConditionalHandle hsw,
                               cudaGraphConditionalHandle hscore, cudaStream_t s);
+cudaError_t launch_loglik_parts(const ProblemDev& P, const uint32_t* dg, const int* gch, const int* tch, int npair,
+                                double* fag_out, double* rec_out, cudaStream_t s);
+cudaError_t launch_swap_graphs(uint32_t* dg, size_t words, int a, int b, cudaStream_t s);
 cudaError_t launch_chain_advance(const RunParams* rp, int64_t* it, int c, cudaGraphConditionalHandle hwhile,
                                  cudaStream_t s);
 cudaError_t launch_chain_merge(double* acc_c, uint8_t* init_c, int C, int64_t npos, double* acc, uint8_t* init,
@@ -73,6 +78,12 @@ struct sl_ctx {
     ProblemDev P{};
     // host copies
     std::vector<double> prior_table;     // [M][4][4]
+    std::vector<double> theta_h, minor_h;   // the map at temperature 1
+    std::vector<double> temps;           // [C] MC3 temperatures
+    // MC3 exchange statistics per adjacent pair (mc3.cc:138-157)
+    std::vector<int64_t> swap_accept, swap_propose;
+    double* d_llfag = nullptr;        // [4][M] founder-allele-graph likelihoods of the exchange step
+    double* d_llrec = nullptr;        // [4][M-1] recombination log-probabilities
     std::vector<uint8_t> legal;          // [M][N]
     std::vector<int32_t> meioses;        // non-ignorable meioses (markov_chain.cc:70-80)
     std::vector<int32_t> even, odd;
@@ -907,6 +918,51 @@ const char* sl_last_error(const sl_ctx* ctx) { return ctx ? ctx->err.c_str() : g
 
 int64_t sl_launch_count(const sl_ctx* ctx) { return ctx ? ctx->launches : 0; }
 
+// Each chain's map at its temperature (GeneticMap::set_temperature,
+// genetic_map.cc:95-117, the same operations in the same order):
+// theta_t = (t theta) + ((1 - t) 0.5), 1 - theta_t, maf_t = (t maf) + ((1 - t) 0.5).
+// The L-sampler's priors stay those of temperature 1: the reference caches
+// them while parsing (pedigree_parser.cc:157) and set_minor_freq does not
+// rebuild them.
+static int upload_chain_maps(sl_ctx* ctx) {
+    ProblemDev& P = ctx->P;
+    const int C = ctx->n_chains, M = P.M;
+    std::vector<double> th((size_t)C * (M - 1)), mi((size_t)C * M), lt((size_t)C * (M - 1)), la((size_t)C * (M - 1));
+    std::vector<float> thf((size_t)C * (M - 1));
+    for (int c = 0; c < C; ++c) {
+        const double t = ctx->temps[c];
+        for (int i = 0; i < M - 1; ++i) {
+            const double v = (t * ctx->theta_h[i]) + ((1 - t) * 0.5);
+            th[(size_t)c * (M - 1) + i] = v;
+            thf[(size_t)c * (M - 1) + i] = (float)v;
+            lt[(size_t)c * (M - 1) + i] = std::log(v);
+            la[(size_t)c * (M - 1) + i] = std::log(1.0 - v);
+        }
+        for (int i = 0; i < M; ++i) mi[(size_t)c * M + i] = (t * ctx->minor_h[i]) + ((1 - t) * 0.5);
+    }
+    int rc;
+    auto put = [&](auto** dst, const auto* src, size_t n) -> int {
+        using E = std::remove_const_t<std::remove_reference_t<decltype(*src)>>;
+        if (!*dst) {
+            E* p = nullptr;
+            if ((rc = dev_alloc(ctx, &p, n))) return rc;
+            *dst = p;
+        }
+        if (cudaMemcpy((void*)*dst, src, sizeof(E) * n, cudaMemcpyHostToDevice) != cudaSuccess)
+            return fail(ctx, SL_ECUDA, "uploading the chains' maps");
+        return SL_OK;
+    };
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (ctx->lstream) CK(cudaStreamSynchronize(ctx->lstream));
+    if ((rc = put((double**)&P.c_theta, th.data(), th.size()))) return rc;
+    if ((rc = put((float**)&P.c_theta_f, thf.data(), thf.size()))) return rc;
+    if ((rc = put((double**)&P.c_minor, mi.data(), mi.size()))) return rc;
+    if ((rc = put((double**)&P.c_log_theta, lt.data(), lt.size()))) return rc;
+    if ((rc = put((double**)&P.c_log_itheta, la.data(), la.size()))) return rc;
+    if ((rc = put((double**)&P.temp, ctx->temps.data(), ctx->temps.size()))) return rc;
+    return SL_OK;
+}
+
 void sl_destroy(sl_ctx* ctx) {
     if (!ctx) return;
     int cur = 0;
@@ -1146,6 +1202,12 @@ int sl_create(const sl_problem_desc* d, const sl_options* opt, sl_ctx** out) {
     CK(cudaMemset(ctx->d_status, 0, sizeof(int)));
     CK(cudaMemset(ctx->d_acc, 0, sizeof(double) * npos));
     CK(cudaMemset(ctx->d_init, 0, npos));
+    ctx->theta_h.assign(d->theta, d->theta + M - 1);
+    ctx->minor_h.assign(d->minor_freq, d->minor_freq + M);
+    ctx->temps.assign(C, 1.0);
+    ctx->swap_accept.assign(std::max(1, C - 1), 0);
+    ctx->swap_propose.assign(std::max(1, C - 1), 0);
+    if ((rc = upload_chain_maps(ctx))) return bail(rc);
     ctx->trait_prob = host_trait_prob(d, ops, od, arena);
     // compiled trait peel for the batched LOD form
     P.prog = nullptr;
@@ -1716,6 +1778,16 @@ static int adjoint_chunk(sl_ctx* ctx, int64_t ntask) {
     return SL_OK;
 }
 
+int sl_set_temperatures(sl_ctx* ctx, const double* temps) {
+    if (!ctx || !temps) return fail(ctx, SL_EINVAL, "null argument");
+    for (int c = 0; c < ctx->n_chains; ++c)
+        if (!(temps[c] > 0.0 && temps[c] <= 1.0))
+            return fail(ctx, SL_EINVAL, "temperature %g of chain %d outside (0, 1]", temps[c], c);
+    CK(cudaSetDevice(ctx->device));
+    ctx->temps.assign(temps, temps + ctx->n_chains);
+    return upload_chain_maps(ctx);
+}
+
 int sl_lod_kernel_info(sl_ctx* ctx, int32_t* kernel, double* compile_ms) {
     if (!ctx) return fail(ctx, SL_EINVAL, "null context");
     if (kernel) *kernel = ctx->lod_precision == SL_LOD_FP32_RESCALED ? ctx->lod_kernel_sel : SL_LOD_KERNEL_INTERP;
@@ -1850,7 +1922,7 @@ static cudaError_t capture_chain_body(sl_ctx* ctx, int c, cudaGraph_t body, cuda
     if ((e = cudaGraphConditionalHandleCreate(&hsw, g, 2, 0)) != cudaSuccess) return e;
     if ((e = cudaGraphConditionalHandleCreate(&hscore, g, 0, 0)) != cudaSuccess) return e;
     if ((e = launch_chain_iter(ctx->d_run, ctx->d_chain_it, c, key, ctx->d_meioses, nm, ctx->d_morder + (size_t)c * nm,
-                               hsw, hscore, s1)) != cudaSuccess)
+                               P.temp, hsw, hscore, s1)) != cudaSuccess)
         return e;
     cudaGraph_t sw[2];
     if ((e = capture_conditional(s1, hsw, cudaGraphCondTypeSwitch, 2, sw)) != cudaSuccess) return e;
@@ -1995,6 +2067,88 @@ static int build_run_graph(sl_ctx* ctx) {
     return SL_OK;
 }
 
+// log P(G, graph) from its parts in the reference's order: the interval sums
+// added from 0.0 (_recombination_prob), marker transmission first
+// (_transmission_prob), then the log of every locus's founder-allele-graph
+// likelihood (_sum_prior_prob), joined by log_product (descent_graph.cc:184-269,
+// logarithms.cc:27-29).
+static double loglik_from_parts(const double* fag, const double* rec, int M, double marker_trans) {
+    const double LOG_ZERO = -DBL_MAX;
+    double r = 0.0;
+    for (int l = 0; l < M - 1; ++l) r += rec[l];
+    const double trans = marker_trans + r;
+    double prior = 0.0;
+    for (int l = 0; l < M; ++l) {
+        if (fag[l] == 0.0) { prior = LOG_ZERO; break; }
+        prior += std::log(fag[l]);
+    }
+    return (trans == LOG_ZERO || prior == LOG_ZERO) ? LOG_ZERO : trans + prior;
+}
+
+static int loglik_pairs(sl_ctx* ctx, const int* g, const int* t, int npair, double* out) {
+    const ProblemDev& P = ctx->P;
+    const int M = P.M;
+    int rc;
+    if (!ctx->d_llfag && (rc = dev_alloc(ctx, &ctx->d_llfag, (size_t)4 * M))) return rc;
+    if (!ctx->d_llrec && (rc = dev_alloc(ctx, &ctx->d_llrec, (size_t)4 * (M - 1)))) return rc;
+    int g4[4] = {0, 0, 0, 0}, t4[4] = {0, 0, 0, 0};
+    for (int k = 0; k < npair; ++k) { g4[k] = g[k]; t4[k] = t[k]; }
+    { Prof pf_(ctx, SL_KERNEL_OTHER);
+    CK(launch_loglik_parts(P, ctx->d_dg, g4, t4, npair, ctx->d_llfag, ctx->d_llrec, ctx->stream)); }
+    ctx->launches += 1;
+    std::vector<double> fag((size_t)npair * M), rec((size_t)npair * (M - 1));
+    CK(cudaMemcpyAsync(fag.data(), ctx->d_llfag, sizeof(double) * fag.size(), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(rec.data(), ctx->d_llrec, sizeof(double) * rec.size(), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    for (int k = 0; k < npair; ++k)
+        out[k] = loglik_from_parts(fag.data() + (size_t)k * M, rec.data() + (size_t)k * (M - 1), M, P.marker_trans);
+    return SL_OK;
+}
+
+// The MC3 exchange after a spurt ending at iteration `it_end` (mc3.cc:138-157):
+// a uniformly chosen adjacent pair (r, r+1) swaps graphs with probability
+// min(1, exp((xy + yx) - (xx + yy))).  Both uniforms come from the Philox
+// stream (stage 9, the spurt's end iteration, draws 0 and 1).
+static int mc3_exchange(sl_ctx* ctx, uint64_t seed, int it_end) {
+    const int C = ctx->n_chains;
+    const uint64_t hi = (0x3ffull << 40) ^ ((uint64_t)it_end << 4) ^ 9u;
+    int r = (int)((C - 1) * host_philox_u01(seed, hi, 0));
+    if (r > C - 2) r = C - 2;
+    const int g[4] = {r, r + 1, r + 1, r}, t[4] = {r, r + 1, r, r + 1};   // xx, yy, xy, yx
+    double ll[4];
+    int rc = loglik_pairs(ctx, g, t, 4, ll);
+    if (rc) return rc;
+    const double ratio = (ll[2] + ll[3]) - (ll[0] + ll[1]);
+    const double u = host_philox_u01(seed, hi, 1);
+    ctx->swap_propose[r] += 1;
+    if (u == 0.0 || std::log(u) < std::min(0.0, ratio)) {
+        { Prof pf_(ctx, SL_KERNEL_OTHER);
+        CK(launch_swap_graphs(ctx->d_dg, (size_t)ctx->P.M * ctx->P.W, r, r + 1, ctx->stream)); }
+        ctx->swap_accept[r] += 1;
+    }
+    return SL_OK;
+}
+
+static int scored_chains(const sl_ctx* ctx) {
+    int n = 0;
+    for (double t : ctx->temps) n += t == 1.0;
+    return n;
+}
+
+// Score the chains at temperature 1 (runs of consecutive chains per call).
+static int score_cold_chains(sl_ctx* ctx) {
+    const int C = ctx->n_chains;
+    for (int c = 0; c < C;) {
+        if (ctx->temps[c] != 1.0) { ++c; continue; }
+        int e = c;
+        while (e < C && ctx->temps[e] == 1.0) ++e;
+        int rc = score_device_graphs(ctx, ctx->d_dg + (size_t)c * ctx->P.M * ctx->P.W, e - c);
+        if (rc) return rc;
+        c = e;
+    }
+    return SL_OK;
+}
+
 // Capture the device-driven M-sweep once: for every chain c a branch
 // memset -> founder-allele graphs (reset) -> [graphs, filter] x nm over that
 // chain alone (first = c, one chain); kernels of chains that chose the
@@ -2052,44 +2206,39 @@ static int build_ms_graph(sl_ctx* ctx) {
     return SL_OK;
 }
 
-int sl_run(sl_ctx* ctx, const sl_run_options* o) {
-    if (!ctx || !o) return fail(ctx, SL_EINVAL, "null argument");
-    if (o->iterations < 0 || o->burnin < 0 || o->scoring_period < 1 || o->first_iteration < 0 ||
-        !(o->lsampler_prob >= 0.0 && o->lsampler_prob <= 1.0))
-        return fail(ctx, SL_EINVAL, "bad run options");
-    CK(cudaSetDevice(ctx->device));
+// Iterations [first, end) of a run: one launch of the run graph, or with
+// profiling on the same kernels launched one by one with per-class marks.
+static int run_span(sl_ctx* ctx, const sl_run_options* o, int first, int end) {
     const ProblemDev& P = ctx->P;
     const int C = ctx->n_chains;
     const int nm = (int)ctx->meioses.size();
-    const int total = o->burnin + o->iterations;
-    if (o->first_iteration >= total) return SL_OK;
+    const int cold = scored_chains(ctx);
     if (!ctx->profiling) {
-        // the whole run is one launch of the run graph
         if (!ctx->run_graph) {
             int rc = build_run_graph(ctx);
             if (rc) return rc;
         }
-        const RunParams rp{o->first_iteration, total, o->burnin, o->scoring_period, o->lsampler_prob, o->seed};
+        const RunParams rp{first, end, o->burnin, o->scoring_period, o->lsampler_prob, o->seed};
         CK(cudaMemcpyAsync(ctx->d_run, &rp, sizeof(rp), cudaMemcpyHostToDevice, ctx->stream));
         CK(cudaGraphLaunch(ctx->run_graph, ctx->stream));
         int64_t kernels = 2;   // init, merge
-        for (int it = o->first_iteration; it < total; ++it) {
+        for (int it = first; it < end; ++it) {
             const bool score = it >= o->burnin && it % o->scoring_period == 0;
-            if (score) ctx->lod_count += (uint64_t)C;
+            if (score) ctx->lod_count += (uint64_t)cold;
             for (int c = 0; c < C; ++c) {
                 const uint64_t hi = ((uint64_t)c << 40) ^ ((uint64_t)it << 4) ^ 7u;
                 const bool is_l = host_philox_u01(o->seed, hi, 0) < o->lsampler_prob;
-                kernels += 2 + (is_l ? 2 : 2 * (int64_t)nm + 1) + (score ? 2 : 0);
+                kernels += 2 + (is_l ? 2 : 2 * (int64_t)nm + 1) + (score && ctx->temps[c] == 1.0 ? 2 : 0);
             }
         }
         ctx->launches += kernels;
         return SL_OK;
     }
-    if (!ctx->ms_graph && o->first_iteration < total) {
+    if (!ctx->ms_graph) {
         int rc = build_ms_graph(ctx);
         if (rc) return rc;
     }
-    for (int it = o->first_iteration; it < total; ++it) {
+    for (int it = first; it < end; ++it) {
         const uint64_t iter = (uint64_t)it;
         { Prof pf_(ctx, SL_KERNEL_OTHER);
             CK(launch_choose(0, C, o->seed, iter, o->lsampler_prob, ctx->d_sel, ctx->stream)); }
@@ -2112,11 +2261,49 @@ int sl_run(sl_ctx* ctx, const sl_run_options* o) {
         CK(cudaEventRecord(ctx->ev_join, ctx->lstream));
         CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0));
         if (it >= o->burnin && it % o->scoring_period == 0) {
-            int rc = score_device_graphs(ctx, ctx->d_dg, C);
+            int rc = score_cold_chains(ctx);
             if (rc) return rc;
         }
     }
     return SL_OK;
+}
+
+int sl_run(sl_ctx* ctx, const sl_run_options* o) {
+    if (!ctx || !o) return fail(ctx, SL_EINVAL, "null argument");
+    if (o->iterations < 0 || o->burnin < 0 || o->scoring_period < 1 || o->first_iteration < 0 ||
+        o->exchange_period < 0 || !(o->lsampler_prob >= 0.0 && o->lsampler_prob <= 1.0))
+        return fail(ctx, SL_EINVAL, "bad run options");
+    CK(cudaSetDevice(ctx->device));
+    const int C = ctx->n_chains;
+    const int total = o->burnin + o->iterations;
+    if (o->first_iteration >= total) return SL_OK;
+    if (o->exchange_period == 0 || C < 2) return run_span(ctx, o, o->first_iteration, total);
+    // MC3: spurts of exchange_period iterations, each followed by an exchange
+    // (Mc3::run, mc3.cc:117-158; iterations are numbered consecutively)
+    for (int it0 = o->first_iteration; it0 < total; it0 += o->exchange_period) {
+        const int it1 = std::min(total, it0 + o->exchange_period);
+        int rc = run_span(ctx, o, it0, it1);
+        if (rc) return rc;
+        if (it1 - it0 == o->exchange_period && (rc = mc3_exchange(ctx, o->seed, it1))) return rc;
+    }
+    return SL_OK;
+}
+
+int sl_mc3_stats(sl_ctx* ctx, int64_t* accepted, int64_t* proposed) {
+    if (!ctx) return fail(ctx, SL_EINVAL, "null context");
+    for (int c = 0; c + 1 < ctx->n_chains; ++c) {
+        if (accepted) accepted[c] = ctx->swap_accept[c];
+        if (proposed) proposed[c] = ctx->swap_propose[c];
+    }
+    return SL_OK;
+}
+
+int sl_chain_loglik(sl_ctx* ctx, int32_t graph_chain, int32_t map_chain, double* loglik) {
+    if (!ctx || !loglik) return fail(ctx, SL_EINVAL, "null argument");
+    if (graph_chain < 0 || graph_chain >= ctx->n_chains || map_chain < 0 || map_chain >= ctx->n_chains)
+        return fail(ctx, SL_EINVAL, "chain outside [0, %d)", ctx->n_chains);
+    CK(cudaSetDevice(ctx->device));
+    return loglik_pairs(ctx, &graph_chain, &map_chain, 1, loglik);
 }
 
 }  // extern "C"

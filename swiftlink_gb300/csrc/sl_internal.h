@@ -59,6 +59,14 @@ struct ProblemDev {
     const double* log_theta;             // [M-1] log(theta)
     const double* log_itheta;            // [M-1] log(1 - theta)
     const float* prior_f;                // [M][4][4]
+    // each chain's map at its MC3 temperature t (GeneticMap::set_temperature,
+    // genetic_map.cc:95-117): theta_t = t theta + (1 - t) / 2, maf_t likewise
+    const double* c_theta;               // [C][M-1]
+    const float* c_theta_f;              // [C][M-1]
+    const double* c_minor;               // [C][M]
+    const double* c_log_theta;           // [C][M-1] log(theta_t)
+    const double* c_log_itheta;          // [C][M-1] log(1 - theta_t)
+    const double* temp;                  // [C] temperatures
 };
 
 // Instructions of a compiled trait-peel program (the batched LOD scorer).

@@ -221,11 +221,13 @@ __global__ void __launch_bounds__(128) lsampler_kernel(ProblemDev P, uint32_t* d
         const uint32_t* colR = l < P.M - 1 ? colC + P.W : nullptr;
         T th = T(1), an = T(1), th2 = T(1), an2 = T(1);
         if constexpr (sizeof(T) == 4) {
-            if (l > 0) { th2 = P.theta_f[l - 1]; an2 = 1.f - th2; }
-            if (l < P.M - 1) { th = P.theta_f[l]; an = 1.f - th; }
+            const float* tf = P.c_theta_f + (size_t)chain * (P.M - 1);
+            if (l > 0) { th2 = tf[l - 1]; an2 = 1.f - th2; }
+            if (l < P.M - 1) { th = tf[l]; an = 1.f - th; }
         } else {
-            if (l > 0) { th2 = P.theta[l - 1]; an2 = DSUB(1.0, P.theta[l - 1]); }
-            if (l < P.M - 1) { th = P.theta[l]; an = DSUB(1.0, P.theta[l]); }
+            const double* td = P.c_theta + (size_t)chain * (P.M - 1);
+            if (l > 0) { th2 = td[l - 1]; an2 = DSUB(1.0, td[l - 1]); }
+            if (l < P.M - 1) { th = td[l]; an = DSUB(1.0, td[l]); }
         }
         const uint8_t* gcol = P.geno + (size_t)l * P.N;
         const T* pri;
@@ -827,7 +829,7 @@ __global__ void __launch_bounds__(128) fag_kernel(ProblemDev P, uint32_t* dg, in
     const uint8_t* gcol = P.geno + (size_t)l * P.N;
     if (step < 0) {
         fag_edges(P.N, P.F, s_order, s_mo, s_fa, col, fs, -1);
-        const T lk = fag_like<PP>(P.N, P.F, s_typed, gcol, P.minor[l], fs);
+        const T lk = fag_like<PP>(P.N, P.F, s_typed, gcol, P.c_minor[(size_t)chain * P.M + l], fs);
         raw[2 * l + dgbit(col, ord[0])] = lk;
         if (PP::is_zero(lk)) {
             badc[cr] = 1;
@@ -840,7 +842,7 @@ __global__ void __launch_bounds__(128) fag_kernel(ProblemDev P, uint32_t* dg, in
     const int tb = dgbit(col, m), t2 = dgbit(col, last);
     const T keep = raw[2 * l + t2];
     fag_edges(P.N, P.F, s_order, s_mo, s_fa, col, fs, m);
-    const T lk = fag_like<PP>(P.N, P.F, s_typed, gcol, P.minor[l], fs);
+    const T lk = fag_like<PP>(P.N, P.F, s_typed, gcol, P.c_minor[(size_t)chain * P.M + l], fs);
     raw[2 * l + tb] = keep;
     raw[2 * l + 1 - tb] = lk;
     if (raw32) {
@@ -1041,7 +1043,7 @@ __global__ void __launch_bounds__(kFagWarpsPerBlock * 32) fag_warp_kernel(Proble
                 if (forbid) atomicOr(&cnt[r], forbid);
             }
             __syncwarp();
-            const double minor_d = P.minor[l];
+            const double minor_d = P.c_minor[(size_t)chain * M + l];
             const float lmaj = log2f((float)(1.0 - minor_d)), lmin = log2f((float)minor_d);
             float sum = 0.f;
             int zero = 0;
@@ -1132,7 +1134,7 @@ __global__ void __launch_bounds__(32) ffbs_kernel(ProblemDev P, uint32_t* dg, in
         if (i < P.M) {
             if (sizeof(T) == 8) { q0 = (T)r64[2 * i]; q1 = (T)r64[2 * i + 1]; }
             else { q0 = (T)r32[2 * i]; q1 = (T)r32[2 * i + 1]; }
-            if (i >= 1) th = (T)P.theta[i - 1];
+            if (i >= 1) th = (T)P.c_theta[(size_t)chain * (P.M - 1) + i - 1];
         }
         const int n = min(32, P.M - base);
         T k0 = (T)0, k1 = (T)0;
@@ -1168,7 +1170,7 @@ __global__ void __launch_bounds__(32) ffbs_kernel(ProblemDev P, uint32_t* dg, in
         const int i = top - lane;
         const bool in = i >= lo;
         const T f0 = in ? fb[2 * i] : (T)0, f1 = in ? fb[2 * i + 1] : (T)0;
-        const T th = (in && i < P.M - 1) ? (T)P.theta[i] : (T)0;
+        const T th = (in && i < P.M - 1) ? (T)P.c_theta[(size_t)chain * (P.M - 1) + i] : (T)0;
         uint32_t* wp = in ? (G + (size_t)i * P.W + (m >> 5)) : nullptr;
         const int cur = in ? (int)((*wp >> (m & 31)) & 1u) : 0;
         const int64_t c0 = cursor;
@@ -1285,13 +1287,13 @@ __global__ void __launch_bounds__(1024) ffbs_scan_kernel(ProblemDev P, uint32_t*
         uint8_t* smaps = (uint8_t*)(words + M);
         for (int i = tid; i < M; i += T) words[i] = G[(size_t)i * P.W + (m >> 5)];
         for (int i = tid; i < 2 * M; i += T) sr[i] = r[i];
-        for (int i = tid; i < M; i += T) th[i] = i > 0 ? P.theta_f[i - 1] : 0.f;
+        for (int i = tid; i < M; i += T) th[i] = i > 0 ? P.c_theta_f[(size_t)chain * (M - 1) + i - 1] : 0.f;
         r = sr;
         fb = sfb;
         maps = smaps;
     }
     __syncthreads();
-    auto tof = [&](int i) { return th ? th[i] : (i > 0 ? P.theta_f[i - 1] : 0.f); };
+    auto tof = [&](int i) { return th ? th[i] : (i > 0 ? P.c_theta_f[(size_t)chain * (M - 1) + i - 1] : 0.f); };
     const int L = (M + T - 1) / T;
     const int s0 = min(M, tid * L), s1 = min(M, s0 + L);
     // chunk product P = A_{s1-1} ... A_{s0} (A_0 = diag(r_0)); an empty chunk is the identity
@@ -1941,6 +1943,97 @@ __global__ void choose_kernel(int first, int nchain, uint64_t seed, uint64_t ite
 }
 
 // ---------------------------------------------------------------------------
+// Parts of log P(G, graph) under a chain's map (DescentGraph::get_likelihood,
+// descent_graph.cc:184-269), for up to four (graph chain, map chain) pairs:
+// the founder-allele-graph likelihood of every locus (exact FP64, as the
+// M-sampler's) and the recombination log-probability of every interval, each
+// a sum in the reference's order; the host adds them up in order.
+// ---------------------------------------------------------------------------
+template <typename IX>
+__global__ void __launch_bounds__(128) loglik_fag_kernel(ProblemDev P, const uint32_t* dg, int4 gch, int4 tch,
+                                                         int npair, double* out) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int S = blockDim.x;
+    const size_t per = fag_block_bytes(P.N, P.F, S, 0) - (((size_t)P.N * 7 + 15) & ~(size_t)15);
+    int16_t* s_order = (int16_t*)(smem + per);
+    int16_t* s_mo = s_order + P.N;
+    int16_t* s_fa = s_mo + P.N;
+    uint8_t* s_typed = (uint8_t*)(s_fa + P.N);
+    for (int i = threadIdx.x; i < P.N; i += S) {
+        s_order[i] = P.fag_order[i];
+        s_mo[i] = P.mother[i];
+        s_fa[i] = P.father[i];
+        s_typed[i] = P.typed[i];
+    }
+    __syncthreads();
+    Fag<IX, double> fs = fag_bind<IX, double>(smem, P.N, P.F, S, threadIdx.x);
+    const int64_t t = (int64_t)blockIdx.x * S + threadIdx.x;
+    if (t >= (int64_t)npair * P.M) return;
+    const int k = (int)(t / P.M), l = (int)(t % P.M);
+    const int g = k == 0 ? gch.x : k == 1 ? gch.y : k == 2 ? gch.z : gch.w;
+    const int tc = k == 0 ? tch.x : k == 1 ? tch.y : k == 2 ? tch.z : tch.w;
+    const uint32_t* col = dg + ((size_t)g * P.M + l) * P.W;
+    fag_edges(P.N, P.F, s_order, s_mo, s_fa, col, fs, -1);
+    out[t] = fag_like<ProbExact>(P.N, P.F, s_typed, P.geno + (size_t)l * P.N, P.c_minor[(size_t)tc * P.M + l], fs);
+}
+
+__global__ void loglik_rec_kernel(ProblemDev P, const uint32_t* dg, int4 gch, int4 tch, int npair, double* out) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int I = P.M - 1;
+    if (t >= (int64_t)npair * I) return;
+    const int k = (int)(t / I), l = (int)(t % I);
+    const int g = k == 0 ? gch.x : k == 1 ? gch.y : k == 2 ? gch.z : gch.w;
+    const int tc = k == 0 ? tch.x : k == 1 ? tch.y : k == 2 ? tch.z : tch.w;
+    const uint32_t* colL = dg + ((size_t)g * P.M + l) * P.W;
+    const uint32_t* colR = colL + P.W;
+    const double lt = P.c_log_theta[(size_t)tc * I + l], la = P.c_log_itheta[(size_t)tc * I + l];
+    double r = 0.0;
+    for (int b = 0; b < 2 * P.Nnf; ++b) r = DADD(r, dgbit(colL, b) != dgbit(colR, b) ? lt : la);
+    out[t] = r;
+}
+
+// Exchange two chains' descent graphs.
+__global__ void swap_graphs_kernel(uint32_t* dg, size_t words, int a, int b) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < words; i += (size_t)gridDim.x * blockDim.x) {
+        const uint32_t x = dg[(size_t)a * words + i];
+        dg[(size_t)a * words + i] = dg[(size_t)b * words + i];
+        dg[(size_t)b * words + i] = x;
+    }
+}
+
+cudaError_t launch_loglik_parts(const ProblemDev& P, const uint32_t* dg, const int* gch, const int* tch, int npair,
+                                double* fag_out, double* rec_out, cudaStream_t s) {
+    const int S = 64;
+    const size_t smem = fag_block_bytes(P.N, P.F, S, 0);
+    static size_t configured[2] = {0, 0};
+    const int wide = 2 * P.F > 255 ? 1 : 0;
+    if (smem > configured[wide]) {
+        cudaError_t e = wide ? cudaFuncSetAttribute(loglik_fag_kernel<uint16_t>,
+                                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
+                             : cudaFuncSetAttribute(loglik_fag_kernel<uint8_t>,
+                                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        configured[wide] = smem;
+    }
+    const int4 g4 = make_int4(gch[0], gch[1], gch[2], gch[3]), t4 = make_int4(tch[0], tch[1], tch[2], tch[3]);
+    const int64_t nf = (int64_t)npair * P.M;
+    if (wide)
+        loglik_fag_kernel<uint16_t><<<(int)((nf + S - 1) / S), S, smem, s>>>(P, dg, g4, t4, npair, fag_out);
+    else
+        loglik_fag_kernel<uint8_t><<<(int)((nf + S - 1) / S), S, smem, s>>>(P, dg, g4, t4, npair, fag_out);
+    const int64_t nr = (int64_t)npair * (P.M - 1);
+    loglik_rec_kernel<<<(int)((nr + 127) / 128), 128, 0, s>>>(P, dg, g4, t4, npair, rec_out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_swap_graphs(uint32_t* dg, size_t words, int a, int b, cudaStream_t s) {
+    int64_t grid = (int64_t)((words + 255) / 256);
+    if (grid > 1024) grid = 1024;
+    swap_graphs_kernel<<<(int)grid, 256, 0, s>>>(dg, words, a, b);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
 // Kernels of the run graph: every chain iterates on its own inside a WHILE
 // node (MarkovChain::run, markov_chain.cc:335-392, per replicate chain).
 // ---------------------------------------------------------------------------
@@ -1954,8 +2047,8 @@ __global__ void run_init_kernel(const RunParams* rp, int64_t* it, int C) {
 // shuffle_kernel, the uniforms generated by the warp), the chain's Philox key
 // and whether the iteration scores.  One warp.
 __global__ void chain_iter_kernel(const RunParams* rp, const int64_t* it_arr, int c, uint64_t* key,
-                                  const int32_t* base, int nm, int32_t* order, cudaGraphConditionalHandle hsw,
-                                  cudaGraphConditionalHandle hscore) {
+                                  const int32_t* base, int nm, int32_t* order, const double* temp,
+                                  cudaGraphConditionalHandle hsw, cudaGraphConditionalHandle hscore) {
     extern __shared__ double su[];
     const int lane = threadIdx.x;
     const int64_t it = it_arr[c];
@@ -1987,7 +2080,8 @@ __global__ void chain_iter_kernel(const RunParams* rp, const int64_t* it_arr, in
         key[0] = seed;
         key[1] = iter;
         cudaGraphSetConditional(hsw, is_l ? 0 : 1);
-        cudaGraphSetConditional(hscore, (it >= rp->burnin && it % rp->period == 0) ? 1 : 0);
+        // only the chains at temperature 1 are scored (markov_chain.cc:173-174)
+        cudaGraphSetConditional(hscore, (it >= rp->burnin && it % rp->period == 0 && temp[c] == 1.0) ? 1 : 0);
     }
 }
 
@@ -2021,9 +2115,10 @@ cudaError_t launch_run_init(const RunParams* rp, int64_t* it, int C, cudaStream_
 }
 
 cudaError_t launch_chain_iter(const RunParams* rp, const int64_t* it, int c, uint64_t* key, const int32_t* base,
-                              int nm, int32_t* order, cudaGraphConditionalHandle hsw,
+                              int nm, int32_t* order, const double* temp, cudaGraphConditionalHandle hsw,
                               cudaGraphConditionalHandle hscore, cudaStream_t s) {
-    chain_iter_kernel<<<1, 32, sizeof(double) * (nm > 0 ? nm : 1), s>>>(rp, it, c, key, base, nm, order, hsw, hscore);
+    chain_iter_kernel<<<1, 32, sizeof(double) * (nm > 0 ? nm : 1), s>>>(rp, it, c, key, base, nm, order, temp, hsw,
+                                                                        hscore);
     return cudaGetLastError();
 }
 

@@ -64,3 +64,10 @@ def shuffled(seed, chain, it, base):
         j = min(int(u * (i + 1)), i)
         o[i], o[j] = o[j], o[i]
     return np.array(o, np.int32)
+
+
+def exchange_draws(seed, it_end):
+    """The two uniforms of the MC3 exchange after the spurt ending at `it_end`
+    (stage 9): the adjacent pair, then the acceptance."""
+    hi = (0x3FF << 40) ^ (it_end << 4) ^ 9
+    return float(uniform(seed, hi, 0)), float(uniform(seed, hi, 1))
