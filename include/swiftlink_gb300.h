@@ -338,6 +338,21 @@ int sl_problem_trait_backward_eval(const sl_problem_desc* problem, const int32_t
  * specialised forms at sl_create. */
 int sl_lod_kernel_info(sl_ctx* ctx, int32_t* kernel, double* compile_ms);
 
+/*
+ * A peel sequence for a pedigree (members founders first, mother/father -1 for
+ * founders), in the form sl_problem_desc takes (replaces PeelSequenceGenerator::
+ * build_peel_sequence, peel_sequence_generator.cc:273-310, and its op
+ * construction, :57-250).  The order is a greedy minimum-cutset elimination
+ * refined by exchanges of neighbours (the reference's is a randomised downhill
+ * search); the operations' types, cutsets, previous functions and children
+ * follow the reference's rules.  op_type/op_peelnode hold n entries, the
+ * offsets n + 1, and cutset/prev/children at most `capacity` each (SL_ENOMEM
+ * when that is too small).  Host only; needs no device.
+ */
+int sl_peel_sequence(int32_t n, const int32_t* mother, const int32_t* father, int32_t capacity, int32_t* op_type,
+                     int32_t* op_peelnode, int32_t* cutset_off, int32_t* cutset, int32_t* prev_off, int32_t* prev,
+                     int32_t* children_off, int32_t* children);
+
 /* Library version string. */
 const char* sl_version(void);
 

@@ -30,7 +30,7 @@ EXPORTED = [
     "sl_version", "sl_get_stream", "sl_profile", "sl_profile_read", "sl_problem_legal_masks",
     "sl_problem_trait_priors", "sl_problem_trait_prob", "sl_trait_backward",
     "sl_problem_trait_backward_eval", "sl_lod_kernel_info", "sl_set_temperatures", "sl_mc3_stats",
-    "sl_chain_loglik",
+    "sl_chain_loglik", "sl_peel_sequence",
 ]
 
 
@@ -88,6 +88,25 @@ def lib():
         L.sl_destroy.restype = None
         _lib = L
     return _lib
+
+
+def peel_sequence(mother, father):
+    """sl_peel_sequence: (op_type, op_peel, cutsets, prevs, children) of a
+    pedigree given in founders-first order (mother/father -1 for founders)."""
+    mo = np.ascontiguousarray(mother, np.int32)
+    fa = np.ascontiguousarray(father, np.int32)
+    n = mo.size
+    cap = n * n + 16
+    ot = np.zeros(n, np.int32)
+    op = np.zeros(n, np.int32)
+    offs = [np.zeros(n + 1, np.int32) for _ in range(3)]
+    flats = [np.zeros(cap, np.int32) for _ in range(3)]
+    rc = lib().sl_peel_sequence(ctypes.c_int32(n), _p(mo), _p(fa), ctypes.c_int32(cap), _p(ot), _p(op),
+                                _p(offs[0]), _p(flats[0]), _p(offs[1]), _p(flats[1]), _p(offs[2]), _p(flats[2]))
+    if rc != SL_OK:
+        raise SwiftLinkError(rc, "peel sequence")
+    lists = [[flats[j][offs[j][k]:offs[j][k + 1]].copy() for k in range(n)] for j in range(3)]
+    return ot, op, lists[0], lists[1], lists[2]
 
 
 def _p(a: np.ndarray):

@@ -1,12 +1,13 @@
 """Build the in-tree CUDA library swiftlink_gb300/_build/libswiftlink_gb300.so.
 
-Four translation units compiled in parallel for sm_103a only, then linked
+Five translation units compiled in parallel for sm_103a only, then linked
 with the static CUDA runtime and NVRTC (which compiles the problem-specialised
 LOD kernels when a context is created):
   csrc/sl_kernels.cu  (nvcc, -gencode arch=compute_103a,code=sm_103a)
   csrc/sl_noalloc.cu  (nvcc, same flags)
   csrc/sl_host.cc     (g++ against the CUDA runtime headers)
   csrc/sl_jit.cc      (g++, NVRTC source generator and loader)
+  csrc/sl_peel.cc     (g++, peel-sequence generator)
 """
 from __future__ import annotations
 
@@ -58,6 +59,8 @@ def build(verbose: bool = False, force: bool = False) -> str:
     cc = os.path.join(CSRC, "sl_host.cc")
     jc = os.path.join(CSRC, "sl_jit.cc")
     jc_o = os.path.join(OUT, "sl_jit.o")
+    pc = os.path.join(CSRC, "sl_peel.cc")
+    pc_o = os.path.join(OUT, "sl_peel.o")
     cu_o = os.path.join(OUT, "sl_kernels.o")
     cu2_o = os.path.join(OUT, "sl_noalloc.o")
     cc_o = os.path.join(OUT, "sl_host.o")
@@ -66,7 +69,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
         if force or _stale(obj, [src] + hdrs):
             jobs.append([nvcc, GENCODE, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                          "-Xptxas", "-v", "-c", src, "-o", obj])
-    for src, obj in ((cc, cc_o), (jc, jc_o)):
+    for src, obj in ((cc, cc_o), (jc, jc_o), (pc, pc_o)):
         if force or _stale(obj, [src] + hdrs):
             # no contraction of a * b + c into FMA: host FP64 (priors, tempered maps,
             # likelihood sums) must round as the reference's x86-64 build does, on aarch64 too
@@ -77,9 +80,9 @@ def build(verbose: bool = False, force: bool = False) -> str:
     if jobs:
         with cf.ThreadPoolExecutor(len(jobs)) as ex:
             logs = list(ex.map(_run, jobs))
-    if force or jobs or _stale(LIB, [cu_o, cu2_o, cc_o, jc_o]):
+    if force or jobs or _stale(LIB, [cu_o, cu2_o, cc_o, jc_o, pc_o]):
         lib64 = os.path.join(cuda, "lib64")
-        logs.append(_run([nvcc, GENCODE, "-shared", "-cudart", "static", "-o", LIB, cu_o, cu2_o, cc_o, jc_o,
+        logs.append(_run([nvcc, GENCODE, "-shared", "-cudart", "static", "-o", LIB, cu_o, cu2_o, cc_o, jc_o, pc_o,
                           "-L" + lib64, "-lnvrtc", "-Xlinker", "-rpath=" + lib64]))
     if verbose:
         for l in logs:

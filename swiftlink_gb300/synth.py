@@ -85,6 +85,7 @@ class Workload:
     marker_cm: np.ndarray        # [M] genetic positions in cM
     maf: np.ndarray              # [M] minor ("2") allele frequency
     genotypes: np.ndarray        # [N][M][2] alleles in {0,1,2} (0 = missing)
+    truth: Optional[np.ndarray] = None   # [N][M][2] the meiosis indicators of the gene drop
     famid: str = "1"
 
 
@@ -256,11 +257,13 @@ def _gene_drop(rng, persons: List[Person], pos_cm: np.ndarray, founder_alleles):
     """
     theta = haldane(np.diff(pos_cm) / 100.0)
     hap = {}
+    inherit = {}
     for p in persons:
         if p.founder:
             hap[p.pid] = founder_alleles(p.pid)
             continue
         kid = np.empty((2, pos_cm.size), dtype=np.int8)
+        src_of = np.empty((2, pos_cm.size), dtype=np.int8)
         for slot, parent in ((0, p.mother), (1, p.father)):
             src = hap[parent]
             cross = rng.random(theta.size) < theta
@@ -268,7 +271,10 @@ def _gene_drop(rng, persons: List[Person], pos_cm: np.ndarray, founder_alleles):
             which[0] = rng.integers(0, 2)
             which[1:] = (which[0] + np.cumsum(cross)) % 2
             kid[slot] = src[which, np.arange(pos_cm.size)]
+            src_of[slot] = which
         hap[p.pid] = kid
+        inherit[p.pid] = src_of
+    _gene_drop.inherit = inherit   # the true meiosis indicators of the last drop
     return hap
 
 
@@ -336,7 +342,13 @@ def make_workload(cfg: int = 1, seed: Optional[int] = None,
         if miss_rate > 0:
             miss = rng.random(M) < miss_rate
             geno[i, miss, :] = 0
-    return Workload(spec=spec, persons=persons, marker_cm=marker_cm, maf=maf, genotypes=geno)
+    # the true descent graph at the markers: indicator 0 = the parent's maternal haplotype
+    inherit = _gene_drop.inherit
+    truth = np.zeros((N, M, 2), dtype=np.int8)
+    for i, p in enumerate(persons):
+        if not p.founder:
+            truth[i] = inherit[p.pid][:, keep].T
+    return Workload(spec=spec, persons=persons, marker_cm=marker_cm, maf=maf, genotypes=geno, truth=truth)
 
 
 def write_linkage(w: Workload, prefix: str) -> Tuple[str, str, str]:
