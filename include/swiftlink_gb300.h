@@ -353,6 +353,21 @@ int sl_peel_sequence(int32_t n, const int32_t* mother, const int32_t* father, in
                      int32_t* op_peelnode, int32_t* cutset_off, int32_t* cutset, int32_t* prev_off, int32_t* prev,
                      int32_t* children_off, int32_t* children);
 
+/*
+ * Batches: contexts of different pedigrees (uneven sizes, each with its own
+ * chains and temperatures) run together, one graph launch per spurt holding
+ * every context's per-chain WHILE nodes (no reference counterpart: the
+ * reference runs pedigrees one after another, linkage_program.cc:96-108).
+ * sl_batch_run takes one set of run options for all; with exchange_period > 0
+ * each context then makes its own MC3 exchange.  Results are read per context
+ * (sl_lod_results, sl_get_descent_graphs), ordered after the batch.  The
+ * contexts must outlive the batch and run without profiling.
+ */
+typedef struct sl_batch sl_batch;
+int sl_batch_create(sl_ctx* const* ctxs, int32_t n, sl_batch** out);
+int sl_batch_run(sl_batch* batch, const sl_run_options* opt);
+void sl_batch_destroy(sl_batch* batch);
+
 /* Library version string. */
 const char* sl_version(void);
 

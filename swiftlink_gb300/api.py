@@ -30,7 +30,7 @@ EXPORTED = [
     "sl_version", "sl_get_stream", "sl_profile", "sl_profile_read", "sl_problem_legal_masks",
     "sl_problem_trait_priors", "sl_problem_trait_prob", "sl_trait_backward",
     "sl_problem_trait_backward_eval", "sl_lod_kernel_info", "sl_set_temperatures", "sl_mc3_stats",
-    "sl_chain_loglik", "sl_peel_sequence",
+    "sl_chain_loglik", "sl_peel_sequence", "sl_batch_create", "sl_batch_run", "sl_batch_destroy",
 ]
 
 
@@ -373,3 +373,42 @@ class Context:
 def lod_table(raw: np.ndarray, count: int, trait_prob: float) -> np.ndarray:
     """LODscores::get (lod_score.h:86-88): (raw - ln count - P(T)) / ln 10."""
     return (raw - np.log(count) - trait_prob) / np.log(10.0)
+
+
+class Batch:
+    """Several contexts run by one graph launch per spurt (sl_batch_*)."""
+
+    def __init__(self, contexts):
+        self.contexts = list(contexts)
+        arr = (_vp * len(self.contexts))(*[c.h for c in self.contexts])
+        h = _vp()
+        rc = lib().sl_batch_create(arr, len(self.contexts), ctypes.byref(h))
+        if rc != SL_OK:
+            raise SwiftLinkError(rc, lib().sl_last_error(None).decode())
+        self.h = h
+
+    def run(self, iterations: int, burnin: int = 0, period: int = 10, lprob: float = 0.5, seed: int = 1,
+            first_iteration: int = 0, exchange_period: int = 0):
+        o = RunOptions(iterations, burnin, period, first_iteration, lprob, seed, exchange_period)
+        rc = lib().sl_batch_run(self.h, ctypes.byref(o))
+        if rc != SL_OK:
+            raise SwiftLinkError(rc, lib().sl_last_error(None).decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().sl_batch_destroy.argtypes = [_vp]
+            lib().sl_batch_destroy.restype = None
+            lib().sl_batch_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1967,7 +1967,10 @@ static cudaError_t capture_chain_body(sl_ctx* ctx, int c, cudaGraph_t body, cuda
 
 // The run graph: init -> one WHILE node per chain (in parallel) -> merge of
 // the chains' LOD tables into the context's.
-static int build_run_graph(sl_ctx* ctx) {
+// Everything the run graph needs that cannot happen inside a capture:
+// buffers, the kernels' shared-memory limits (set by direct launches that do
+// nothing), the timed choice of the scoring kernel, capture streams.
+static int prepare_run_graph(sl_ctx* ctx) {
     const ProblemDev& P = ctx->P;
     const int C = ctx->n_chains, M = P.M, nm = (int)ctx->meioses.size();
     const int64_t npos = (int64_t)(M - 1) * P.n_lod;
@@ -1980,8 +1983,7 @@ static int build_run_graph(sl_ctx* ctx) {
     if (!ctx->d_init_c && (rc = dev_alloc(ctx, &ctx->d_init_c, (size_t)C * npos))) return rc;
     CK(cudaMemsetAsync(ctx->d_init_c, 0, (size_t)C * npos, ctx->stream));
     CK(cudaMemsetAsync(ctx->d_keys, 0, sizeof(uint64_t) * 2 * C, ctx->stream));
-    // direct launches configure the kernels' shared-memory limits outside the
-    // capture (every chain's selector 0 and want = 2: they do nothing)
+    // every chain's selector 0 and want = 2: these launches do nothing
     CK(cudaMemsetAsync(ctx->d_sel, 0, (size_t)C, ctx->stream));
     CK(launch_msampler(P, ctx->d_dg, 0, C, ctx->d_morder, nm, 0, nullptr, 0, 0, 0, ctx->d_sel, 2, ctx->d_raw,
                        ctx->d_raw32, ctx->d_fb, ctx->d_badc, ctx->d_maps, ctx->d_status, ctx->ms_threads, exact ? 1 : 0,
@@ -2008,7 +2010,7 @@ static int build_run_graph(sl_ctx* ctx) {
         CK(cudaMemcpy(ctx->d_status, &st, sizeof(int), cudaMemcpyHostToDevice));
     }
     CK(cudaStreamSynchronize(ctx->stream));
-    while ((int)ctx->cap_streams.size() < C + 1) {
+    while ((int)ctx->cap_streams.size() < 3) {
         cudaStream_t st;
         CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
         ctx->cap_streams.push_back(st);
@@ -2016,45 +2018,50 @@ static int build_run_graph(sl_ctx* ctx) {
         CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
         ctx->cap_events.push_back(ev);
     }
-    cudaStream_t s0 = ctx->cap_streams[0], s1 = ctx->cap_streams[1], s2 = ctx->cap_streams[std::min(2, C)];
-    if (s2 == s1) {
-        cudaStream_t st;
-        CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
-        ctx->cap_streams.push_back(st);
-        s2 = st;
-    }
-    cudaGraph_t top = nullptr;
-    CK(cudaGraphCreate(&top, 0));
-    cudaError_t e = cudaStreamBeginCaptureToGraph(s0, top, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    return SL_OK;
+}
+
+// Capture one context's run nodes at the current point of stream s (which
+// is capturing): init -> one WHILE node per chain (in parallel) -> merge of the
+// chains' LOD tables into the context's.  s1 and s2 capture the bodies.
+static cudaError_t capture_run_nodes(sl_ctx* ctx, cudaStream_t s, cudaStream_t s1, cudaStream_t s2) {
+    const int C = ctx->n_chains;
+    const int64_t npos = (int64_t)(ctx->P.M - 1) * ctx->P.n_lod;
+    cudaError_t e = launch_run_init(ctx->d_run, ctx->d_chain_it, C, s);
+    if (e != cudaSuccess) return e;
+    cudaStreamCaptureStatus st;
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t nd = 0;
+    if ((e = cudaStreamGetCaptureInfo(s, &st, nullptr, &g, &deps, nullptr, &nd)) != cudaSuccess) return e;
+    const std::vector<cudaGraphNode_t> init_deps(deps, deps + nd);
     std::vector<cudaGraphNode_t> whiles;
-    if (e == cudaSuccess) e = launch_run_init(ctx->d_run, ctx->d_chain_it, C, s0);
-    std::vector<cudaGraphNode_t> init_deps;
-    if (e == cudaSuccess) {
-        cudaStreamCaptureStatus st;
-        const cudaGraphNode_t* deps = nullptr;
-        size_t nd = 0;
-        e = cudaStreamGetCaptureInfo(s0, &st, nullptr, nullptr, &deps, nullptr, &nd);
-        if (e == cudaSuccess) init_deps.assign(deps, deps + nd);
-    }
-    for (int c = 0; c < C && e == cudaSuccess; ++c) {
+    for (int c = 0; c < C; ++c) {
         cudaGraphConditionalHandle hw;
-        e = cudaGraphConditionalHandleCreate(&hw, top, 1, cudaGraphCondAssignDefault);
-        if (e != cudaSuccess) break;
+        if ((e = cudaGraphConditionalHandleCreate(&hw, g, 1, cudaGraphCondAssignDefault)) != cudaSuccess) return e;
         cudaGraphNodeParams p = {};
         p.type = cudaGraphNodeTypeConditional;
         p.conditional.handle = hw;
         p.conditional.type = cudaGraphCondTypeWhile;
         p.conditional.size = 1;
         cudaGraphNode_t wn;
-        e = cudaGraphAddNode(&wn, top, init_deps.data(), nullptr, init_deps.size(), &p);
-        if (e != cudaSuccess) break;
+        if ((e = cudaGraphAddNode(&wn, g, init_deps.data(), nullptr, init_deps.size(), &p)) != cudaSuccess) return e;
         whiles.push_back(wn);
-        e = capture_chain_body(ctx, c, p.conditional.phGraph_out[0], hw, s1, s2);
+        if ((e = capture_chain_body(ctx, c, p.conditional.phGraph_out[0], hw, s1, s2)) != cudaSuccess) return e;
     }
-    if (e == cudaSuccess)
-        e = cudaStreamUpdateCaptureDependencies(s0, whiles.data(), nullptr, whiles.size(),
-                                                cudaStreamSetCaptureDependencies);
-    if (e == cudaSuccess) e = launch_chain_merge(ctx->d_acc_c, ctx->d_init_c, C, npos, ctx->d_acc, ctx->d_init, s0);
+    e = cudaStreamUpdateCaptureDependencies(s, whiles.data(), nullptr, whiles.size(), cudaStreamSetCaptureDependencies);
+    if (e != cudaSuccess) return e;
+    return launch_chain_merge(ctx->d_acc_c, ctx->d_init_c, C, npos, ctx->d_acc, ctx->d_init, s);
+}
+
+static int build_run_graph(sl_ctx* ctx) {
+    int rc = prepare_run_graph(ctx);
+    if (rc) return rc;
+    cudaStream_t s0 = ctx->cap_streams[0], s1 = ctx->cap_streams[1], s2 = ctx->cap_streams[2];
+    cudaGraph_t top = nullptr;
+    CK(cudaGraphCreate(&top, 0));
+    cudaError_t e = cudaStreamBeginCaptureToGraph(s0, top, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) e = capture_run_nodes(ctx, s0, s1, s2);
     cudaError_t e2 = cudaStreamEndCapture(s0, &top);
     if (e == cudaSuccess) e = e2;
     if (e == cudaSuccess) e = cudaGraphInstantiate(&ctx->run_graph, top, 0);
@@ -2206,13 +2213,30 @@ static int build_ms_graph(sl_ctx* ctx) {
     return SL_OK;
 }
 
+// The host's tally of a run-graph span: scored graphs and kernel launches
+// (the L/M choices replayed with the same Philox draws).
+static void account_span(sl_ctx* ctx, const sl_run_options* o, int first, int end) {
+    const int C = ctx->n_chains, nm = (int)ctx->meioses.size();
+    const int cold = scored_chains(ctx);
+    int64_t kernels = 2;   // init, merge
+    for (int it = first; it < end; ++it) {
+        const bool score = it >= o->burnin && it % o->scoring_period == 0;
+        if (score) ctx->lod_count += (uint64_t)cold;
+        for (int c = 0; c < C; ++c) {
+            const uint64_t hi = ((uint64_t)c << 40) ^ ((uint64_t)it << 4) ^ 7u;
+            const bool is_l = host_philox_u01(o->seed, hi, 0) < o->lsampler_prob;
+            kernels += 2 + (is_l ? 2 : 2 * (int64_t)nm + 1) + (score && ctx->temps[c] == 1.0 ? 2 : 0);
+        }
+    }
+    ctx->launches += kernels;
+}
+
 // Iterations [first, end) of a run: one launch of the run graph, or with
 // profiling on the same kernels launched one by one with per-class marks.
 static int run_span(sl_ctx* ctx, const sl_run_options* o, int first, int end) {
     const ProblemDev& P = ctx->P;
     const int C = ctx->n_chains;
     const int nm = (int)ctx->meioses.size();
-    const int cold = scored_chains(ctx);
     if (!ctx->profiling) {
         if (!ctx->run_graph) {
             int rc = build_run_graph(ctx);
@@ -2221,17 +2245,7 @@ static int run_span(sl_ctx* ctx, const sl_run_options* o, int first, int end) {
         const RunParams rp{first, end, o->burnin, o->scoring_period, o->lsampler_prob, o->seed};
         CK(cudaMemcpyAsync(ctx->d_run, &rp, sizeof(rp), cudaMemcpyHostToDevice, ctx->stream));
         CK(cudaGraphLaunch(ctx->run_graph, ctx->stream));
-        int64_t kernels = 2;   // init, merge
-        for (int it = first; it < end; ++it) {
-            const bool score = it >= o->burnin && it % o->scoring_period == 0;
-            if (score) ctx->lod_count += (uint64_t)cold;
-            for (int c = 0; c < C; ++c) {
-                const uint64_t hi = ((uint64_t)c << 40) ^ ((uint64_t)it << 4) ^ 7u;
-                const bool is_l = host_philox_u01(o->seed, hi, 0) < o->lsampler_prob;
-                kernels += 2 + (is_l ? 2 : 2 * (int64_t)nm + 1) + (score && ctx->temps[c] == 1.0 ? 2 : 0);
-            }
-        }
-        ctx->launches += kernels;
+        account_span(ctx, o, first, end);
         return SL_OK;
     }
     if (!ctx->ms_graph) {
@@ -2285,6 +2299,136 @@ int sl_run(sl_ctx* ctx, const sl_run_options* o) {
         int rc = run_span(ctx, o, it0, it1);
         if (rc) return rc;
         if (it1 - it0 == o->exchange_period && (rc = mc3_exchange(ctx, o->seed, it1))) return rc;
+    }
+    return SL_OK;
+}
+
+
+// ---------------------------------------------------------------------------
+// Batches: several contexts (pedigrees of any sizes, each with its chains)
+// run by one graph launch per spurt.
+// ---------------------------------------------------------------------------
+struct sl_batch {
+    std::vector<sl_ctx*> ctxs;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::vector<cudaStream_t> fork;
+    std::vector<cudaEvent_t> evs;
+    cudaEvent_t ev_root = nullptr, ev_done = nullptr;
+    cudaGraphExec_t graph = nullptr;
+};
+
+void sl_batch_destroy(sl_batch* b) {
+    if (!b) return;
+    cudaSetDevice(b->device);
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    for (auto st : b->fork) cudaStreamDestroy(st);
+    for (auto ev : b->evs) cudaEventDestroy(ev);
+    if (b->ev_root) cudaEventDestroy(b->ev_root);
+    if (b->ev_done) cudaEventDestroy(b->ev_done);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+}
+
+int sl_batch_create(sl_ctx* const* ctxs, int32_t n, sl_batch** out) {
+    if (!ctxs || n < 1 || !out) return fail(nullptr, SL_EINVAL, "bad batch");
+    *out = nullptr;
+    for (int j = 0; j < n; ++j) {
+        if (!ctxs[j]) return fail(nullptr, SL_EINVAL, "null context %d in batch", j);
+        if (ctxs[j]->device != ctxs[0]->device) return fail(nullptr, SL_EINVAL, "batch contexts on different devices");
+        for (int k = 0; k < j; ++k)
+            if (ctxs[k] == ctxs[j]) return fail(nullptr, SL_EINVAL, "context %d appears twice in the batch", j);
+    }
+    sl_batch* b = new sl_batch();
+    b->ctxs.assign(ctxs, ctxs + n);
+    b->device = ctxs[0]->device;
+    if (cudaSetDevice(b->device) != cudaSuccess || cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) ||
+        cudaEventCreateWithFlags(&b->ev_root, cudaEventDisableTiming) ||
+        cudaEventCreateWithFlags(&b->ev_done, cudaEventDisableTiming)) {
+        sl_batch_destroy(b);
+        return fail(nullptr, SL_ECUDA, "creating the batch's stream");
+    }
+    for (int j = 0; j < n; ++j) {
+        cudaStream_t st;
+        cudaEvent_t ev;
+        if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) ||
+            cudaEventCreateWithFlags(&ev, cudaEventDisableTiming)) {
+            sl_batch_destroy(b);
+            return fail(nullptr, SL_ECUDA, "creating the batch's streams");
+        }
+        b->fork.push_back(st);
+        b->evs.push_back(ev);
+    }
+    *out = b;
+    return SL_OK;
+}
+
+static int build_batch_graph(sl_batch* b) {
+    for (sl_ctx* c : b->ctxs) {
+        int rc = prepare_run_graph(c);
+        if (rc) return rc;
+    }
+    cudaGraph_t top = nullptr;
+    if (cudaGraphCreate(&top, 0) != cudaSuccess) return fail(nullptr, SL_ECUDA, "creating the batch graph");
+    cudaError_t e = cudaStreamBeginCaptureToGraph(b->stream, top, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) e = cudaEventRecord(b->ev_root, b->stream);
+    for (size_t j = 0; j < b->ctxs.size() && e == cudaSuccess; ++j) {
+        sl_ctx* c = b->ctxs[j];
+        if ((e = cudaStreamWaitEvent(b->fork[j], b->ev_root, 0)) != cudaSuccess) break;
+        if ((e = capture_run_nodes(c, b->fork[j], c->cap_streams[1], c->cap_streams[2])) != cudaSuccess) break;
+        if ((e = cudaEventRecord(b->evs[j], b->fork[j])) != cudaSuccess) break;
+        e = cudaStreamWaitEvent(b->stream, b->evs[j], 0);
+    }
+    cudaError_t e2 = cudaStreamEndCapture(b->stream, &top);
+    if (e == cudaSuccess) e = e2;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&b->graph, top, 0);
+    cudaGraphDestroy(top);
+    if (e != cudaSuccess) {
+        b->graph = nullptr;
+        cudaGetLastError();
+        return fail(nullptr, SL_ECUDA, "capturing the batch graph: %s", cudaGetErrorString(e));
+    }
+    return SL_OK;
+}
+
+int sl_batch_run(sl_batch* b, const sl_run_options* o) {
+    if (!b || !o) return fail(nullptr, SL_EINVAL, "null argument");
+    if (o->iterations < 0 || o->burnin < 0 || o->scoring_period < 1 || o->first_iteration < 0 ||
+        o->exchange_period < 0 || !(o->lsampler_prob >= 0.0 && o->lsampler_prob <= 1.0))
+        return fail(nullptr, SL_EINVAL, "bad run options");
+    if (cudaSetDevice(b->device) != cudaSuccess) return fail(nullptr, SL_ECUDA, "cudaSetDevice");
+    for (sl_ctx* c : b->ctxs)
+        if (c->profiling) return fail(c, SL_EINVAL, "a batch runs without per-kernel profiling");
+    if (!b->graph) {
+        int rc = build_batch_graph(b);
+        if (rc) return rc;
+    }
+    const int total = o->burnin + o->iterations;
+    const int period = o->exchange_period > 0 ? o->exchange_period : std::max(1, total - o->first_iteration);
+    for (int it0 = o->first_iteration; it0 < total; it0 += period) {
+        const int it1 = std::min(total, it0 + period);
+        for (size_t j = 0; j < b->ctxs.size(); ++j) {
+            sl_ctx* c = b->ctxs[j];
+            const RunParams rp{it0, it1, o->burnin, o->scoring_period, o->lsampler_prob, o->seed};
+            if (cudaMemcpyAsync(c->d_run, &rp, sizeof(rp), cudaMemcpyHostToDevice, c->stream) != cudaSuccess ||
+                cudaEventRecord(b->evs[j], c->stream) != cudaSuccess ||
+                cudaStreamWaitEvent(b->stream, b->evs[j], 0) != cudaSuccess)
+                return fail(c, SL_ECUDA, "ordering the batch after the context's work");
+        }
+        if (cudaGraphLaunch(b->graph, b->stream) != cudaSuccess || cudaEventRecord(b->ev_done, b->stream) != cudaSuccess)
+            return fail(nullptr, SL_ECUDA, "launching the batch graph");
+        for (sl_ctx* c : b->ctxs) {
+            if (cudaStreamWaitEvent(c->stream, b->ev_done, 0) != cudaSuccess)
+                return fail(c, SL_ECUDA, "ordering the context after the batch");
+            account_span(c, o, it0, it1);
+        }
+        if (o->exchange_period > 0 && it1 - it0 == o->exchange_period)
+            for (sl_ctx* c : b->ctxs)
+                if (c->n_chains > 1) {
+                    int rc = mc3_exchange(c, o->seed, it1);
+                    if (rc) return rc;
+                }
     }
     return SL_OK;
 }

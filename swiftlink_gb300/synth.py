@@ -64,6 +64,27 @@ CONFIGS: Dict[int, WorkloadSpec] = {
 }
 
 
+def uneven_batch(n_pedigrees: int = 64, seed: int = SEED_BASE + 3, markers: int = 1000):
+    """The uneven batch: `n_pedigrees` independent pedigrees with sizes drawn
+    uniformly from 20-150 members and 0-4 loops, `markers` SNPs at 0.5 cM with
+    MAF ~U(0.05, 0.5), the recessive model; each is a seeded workload (its own
+    seed), built with the first shape that the topology builder accepts."""
+    rng = np.random.default_rng(seed)
+    out = []
+    while len(out) < n_pedigrees:
+        n = int(rng.integers(20, 151))
+        loops = int(rng.integers(0, 5))
+        gens = 3 + (n >= 40) + (n >= 90)
+        loops = min(loops, max(0, gens - 3) * 2 + 1) if gens > 3 else min(loops, 1)
+        spec = WorkloadSpec(n_members=n, generations=gens, loops=loops, affected=max(2, n // 10),
+                            markers=markers, spacing_cm=0.5, maf=(0.05, 0.5), missing_all=0.02)
+        try:
+            out.append(make_workload(3, seed=int(rng.integers(1, 2**31)), spec=spec))
+        except RuntimeError:
+            continue
+    return out
+
+
 @dataclasses.dataclass
 class Person:
     pid: int          # 1-based id written to the pedfile
