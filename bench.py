@@ -50,6 +50,7 @@ def parse():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--skip-uneven", action="store_true", help="leave out the uneven multi-pedigree batch")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     return ap.parse_args()
 
@@ -371,8 +372,11 @@ def run_ours(args):
     dlod = float(np.abs(api.lod_table(raw32, c32, tp32) - api.lod_table(raw64, c64, tp64))[fin].max())
 
     # ---------------- adjoint of the trait peel (dominant model 0.01/0.8/0.9, q = 1e-3) over
-    # 16 stored graphs, through sl_trait_backward with host graphs and gradients
-    adj = adjoint_rate(d, gset[:16], local)
+    # the 64 stored graphs, through sl_trait_backward with host graphs and gradients
+    adj = adjoint_rate(d, gset, local)
+
+    # ---------------- the uneven batch: 64 pedigrees of 20-150 members, 8 MC3 chains each
+    uneven = uneven_batch_rate(local) if not args.skip_uneven else None
 
     # ---------------- plain form: one chain, FP64 LOD
     pctx.run(iterations=W, burnin=0, period=PERIOD, lprob=LPROB, seed=seed)
@@ -427,6 +431,7 @@ def run_ours(args):
                                     "lod_positions": lod_pos_s / plain_lod_pos_s},
                "max_abs_dlod_fp32_vs_fp64": dlod,
                "adjoint": adj,
+               "uneven_batch": uneven,
                "gpu_launches": int(gpu_launches), "roofline": roofline, "clocks": clk, "e2e": e2e}
         if world == 1:
             out["cpu_baseline"] = cpu_baseline_sample()
@@ -435,6 +440,46 @@ def run_ours(args):
         c.close()
     if dist:
         dist.destroy_process_group()
+
+
+def uneven_batch_rate(device, n_ped=64, chains=8, K=20):
+    """Chain-steps/s of the uneven batch: 64 seeded pedigrees of 20-150
+    members (0-4 loops, 1,000 SNPs at 0.5 cM), 8 MC3 chains each at
+    temperatures 0.3^(j/7), fast samplers, FP32 LOD (the slot-program
+    interpreter: no per-pedigree compilation), exchange and scoring every 10
+    iterations, all pedigrees in one graph launch per spurt."""
+    from swiftlink_gb300 import api, pedigree, synth
+    t0 = time.perf_counter()
+    probs = [pedigree.problem_from_workload(w) for w in synth.uneven_batch(n_ped)]
+    temps = [0.3 ** (j / 7) for j in range(chains)]
+    ctxs = []
+    for pd in probs:
+        ctx = api.Context(api.Problem.from_arrays(pd, with_legal=False), n_chains=chains, device=device,
+                          lod_precision=api.SL_LOD_FP32_RESCALED, sampler_precision=api.SL_SAMPLER_FAST,
+                          lod_flags=api.SL_LOD_ZERO_OK, lod_kernel=api.SL_LOD_KERNEL_INTERP)
+        ctx.set_temperatures(temps)
+        ctx.set_graphs(np.stack([pd["dg0"]] * chains))
+        ctxs.append(ctx)
+    setup_s = time.perf_counter() - t0
+    opts = dict(burnin=0, period=10, lprob=LPROB, seed=SEED, exchange_period=10)
+    with api.Batch(ctxs) as b:
+        b.run(iterations=10, **opts)                      # builds the graph, warms up
+        for c in ctxs:
+            c.synchronize()
+        t = time.perf_counter()
+        b.run(iterations=10 + K, first_iteration=10, **opts)
+        for c in ctxs:
+            c.synchronize()
+        dt = time.perf_counter() - t
+    acc = sum(int(c.mc3_stats()[0].sum()) for c in ctxs)
+    prop = sum(int(c.mc3_stats()[1].sum()) for c in ctxs)
+    sizes = [pd["N"] for pd in probs]
+    for c in ctxs:
+        c.close()
+    return {"value": K * chains * n_ped / dt, "unit": "chain-steps/s", "pedigrees": n_ped, "chains_per_pedigree": chains,
+            "members": [min(sizes), max(sizes)], "markers": 1000, "iterations_timed": K,
+            "exchanges_accepted": acc, "exchanges_proposed": prop, "setup_s": round(setup_s, 1),
+            "timing": "wall clock around sl_batch_run + synchronize (host-side MC3 exchanges included)"}
 
 
 def adjoint_rate(d, graphs, device):

@@ -16,13 +16,14 @@
 //     (find_prev_functions);
 //   * an order is legal if no member is peeled while it could be both a CHILD
 //     and a PARENT operation (is_legit).
-// The order itself is found differently: the reference runs a randomised
-// downhill search over permutations (10^6 swaps by default); here a greedy
-// minimum-cutset order (ties to the lowest member index) among the members that
-// are legal to peel next, then a deterministic downhill pass of adjacent
-// exchanges that keeps an order only when it is legal and its cost (the sum of
-// cutset sizes, get_cost) does not grow.  Any legal order peels to the same
-// likelihoods; the order changes only the work and the samplers' draw order.
+// The order itself is found differently: the reference starts its randomised
+// downhill search (exchanges of two random positions, get_cost = sum of cutset
+// sizes) from a random permutation; here the search starts from a greedy
+// minimum-cutset order (ties to the least fill-in, then the lowest index)
+// among the members legal to peel next, its exchanges come from a fixed
+// xorshift stream, and the cost is the rfunctions' work, sum of 4^|cutset|.
+// Any legal order peels to the same likelihoods; the order changes only the
+// work and the samplers' draw order.
 #include <algorithm>
 #include <cstdint>
 #include <vector>
@@ -92,29 +93,47 @@ bool ambiguous(const Ped& p, int i, const std::vector<char>& peeled) {
            !all_peeled(p.mates[i], peeled) && !all_peeled(p.children[i], peeled);
 }
 
-// cost (sum of cutset sizes) of an order, or -1 if it is not legal
-long order_cost(const Ped& p, const std::vector<int>& order) {
+// cost of an order: the work of its rfunctions, sum of 4^|cutset| (get_proper_cost,
+// peel_sequence_generator.cc:460-470), or -1 if the order is not legal
+double order_cost(const Ped& p, const std::vector<int>& order) {
     auto g = simple_graph(p);
     std::vector<char> peeled(p.n, 0);
-    long cost = 0;
+    double cost = 0.0;
     for (int node : order) {
-        if (ambiguous(p, node, peeled)) return -1;
-        cost += (long)g[node].size();
+        if (ambiguous(p, node, peeled)) return -1.0;
+        cost += (double)(1ull << (2 * std::min<size_t>(g[node].size(), 30)));
         eliminate(g, node);
         peeled[node] = 1;
     }
     return cost;
 }
 
+// edges that eliminating `i` would add between its neighbours
+int fill_in(const std::vector<std::vector<int>>& g, int i) {
+    const std::vector<int>& c = g[i];
+    int f = 0;
+    for (size_t a = 0; a < c.size(); ++a)
+        for (size_t b = a + 1; b < c.size(); ++b)
+            if (std::find(g[c[a]].begin(), g[c[a]].end(), c[b]) == g[c[a]].end()) ++f;
+    return f;
+}
+
+// greedy: the legal member with the smallest cutset, ties to the least fill-in,
+// then to the lowest index
 std::vector<int> greedy_order(const Ped& p) {
     auto g = simple_graph(p);
     std::vector<char> peeled(p.n, 0);
     std::vector<int> order;
     for (int step = 0; step < p.n; ++step) {
-        int best = -1;
+        int best = -1, best_fill = 0;
         for (int i = 0; i < p.n; ++i) {
             if (peeled[i] || ambiguous(p, i, peeled)) continue;
-            if (best < 0 || g[i].size() < g[best].size()) best = i;
+            if (best >= 0 && g[i].size() > g[best].size()) continue;
+            const int f = fill_in(g, i);
+            if (best < 0 || g[i].size() < g[best].size() || f < best_fill) {
+                best = i;
+                best_fill = f;
+            }
         }
         if (best < 0)   // cannot happen: founders and leaves are never ambiguous
             for (int i = 0; i < p.n; ++i)
@@ -126,21 +145,29 @@ std::vector<int> greedy_order(const Ped& p) {
     return order;
 }
 
-void downhill(const Ped& p, std::vector<int>& order, int passes) {
-    long cost = order_cost(p, order);
-    for (int pass = 0; pass < passes; ++pass) {
-        bool improved = false;
-        for (size_t k = 0; k + 1 < order.size(); ++k) {
-            std::swap(order[k], order[k + 1]);
-            const long c = order_cost(p, order);
-            if (c >= 0 && c < cost) {
-                cost = c;
-                improved = true;
-            } else {
-                std::swap(order[k], order[k + 1]);
-            }
-        }
-        if (!improved) break;
+// downhill search in the reference's manner (random_downhill_search,
+// peel_sequence_generator.cc:350-409): exchange two random positions, keep the
+// exchange when the order stays legal and its cost does not grow; a fixed
+// xorshift stream makes the result reproducible
+void downhill(const Ped& p, std::vector<int>& order, int iterations) {
+    double cost = order_cost(p, order);
+    uint64_t x = 0x9E3779B97F4A7C15ull;
+    auto next = [&]() {
+        x ^= x << 13;
+        x ^= x >> 7;
+        x ^= x << 17;
+        return x;
+    };
+    const int n = (int)order.size();
+    if (n < 2) return;
+    for (int it = 0; it < iterations; ++it) {
+        const int a = (int)(next() % (uint64_t)n);
+        int b = (int)(next() % (uint64_t)n);
+        if (a == b) continue;
+        std::swap(order[a], order[b]);
+        const double c = order_cost(p, order);
+        if (c >= 0.0 && c <= cost) cost = c;
+        else std::swap(order[a], order[b]);
     }
 }
 
@@ -215,8 +242,9 @@ extern "C" int sl_peel_sequence(int32_t n, const int32_t* mother, const int32_t*
         add_node(p.mates[p.fa[i]], p.mo[i]);
     }
     std::vector<int> order = greedy_order(p);
-    downhill(p, order, 4);
-    if (order_cost(p, order) < 0) return SL_EINVAL;
+    // the search costs O(n) per step: keep it to about 2 10^7 node visits
+    downhill(p, order, std::max(200, std::min(20000, 20000000 / (n * n + 1))));
+    if (order_cost(p, order) < 0.0) return SL_EINVAL;
     const std::vector<Op> ops = finalise(p, order);
     int32_t nc = 0, np = 0, nk = 0;
     cutset_off[0] = prev_off[0] = children_off[0] = 0;
