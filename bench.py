@@ -51,6 +51,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--skip-uneven", action="store_true", help="leave out the uneven multi-pedigree batch")
+    ap.add_argument("--skip-large", action="store_true", help="leave out the 400-member, 10,000-SNP workload")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     return ap.parse_args()
 
@@ -377,6 +378,8 @@ def run_ours(args):
 
     # ---------------- the uneven batch: 64 pedigrees of 20-150 members, 8 MC3 chains each
     uneven = uneven_batch_rate(local) if not args.skip_uneven else None
+    # ---------------- large scale: 400 members, 10,000 SNPs, 32 chains
+    large = large_scale(local) if not args.skip_large else None
 
     # ---------------- plain form: one chain, FP64 LOD
     pctx.run(iterations=W, burnin=0, period=PERIOD, lprob=LPROB, seed=seed)
@@ -432,6 +435,7 @@ def run_ours(args):
                "max_abs_dlod_fp32_vs_fp64": dlod,
                "adjoint": adj,
                "uneven_batch": uneven,
+               "large_scale": large,
                "gpu_launches": int(gpu_launches), "roofline": roofline, "clocks": clk, "e2e": e2e}
         if world == 1:
             out["cpu_baseline"] = cpu_baseline_sample()
@@ -440,6 +444,66 @@ def run_ours(args):
         c.close()
     if dist:
         dist.destroy_process_group()
+
+
+def large_scale(device, C=32, K=4):
+    """The 400-member, 8-generation, 10-loop pedigree with 10,000 SNPs at 0.1 cM
+    (seeded, host-built peel sequence, the gene drop's graph as the start), 32
+    chains: steps/s of the batched form (wall clock around sl_run of K
+    iterations, one run-graph launch), LOD positions/s of the batched FP32 form
+    against the plain FP64 form on the chains' 32 graphs, and the FP32 form's
+    max |dLOD| against the FP64 peel with rescaling.  The plain FP64 peel (the
+    reference's arithmetic) underflows to 0 at every position of this
+    pedigree, so the rescaled FP64 peel is the accuracy yardstick."""
+    from swiftlink_gb300 import api, pedigree, synth
+    t0 = time.perf_counter()
+    d = pedigree.problem_from_workload(synth.make_workload(5))
+    prob = api.Problem.from_arrays(d, with_legal=False)
+    ctx = api.Context(prob, n_chains=C, device=device, lod_precision=api.SL_LOD_FP32_RESCALED,
+                      sampler_precision=api.SL_SAMPLER_FAST, lod_flags=api.SL_LOD_ZERO_OK)
+    ctx.set_graphs(np.stack([d["dg0"]] * C))
+    ctx.run(iterations=2, burnin=0, period=1, lprob=LPROB, seed=SEED)
+    ctx.synchronize()
+    setup_s = time.perf_counter() - t0
+    t = time.perf_counter()
+    ctx.run(iterations=2 + K, burnin=0, period=1 << 30, lprob=LPROB, seed=SEED, first_iteration=2)
+    ctx.synchronize()
+    steps_s = K * C / (time.perf_counter() - t)
+    npos = (d["M"] - 1) * d["n_lod"]
+
+    def lod_rate(c, reps):
+        c.lod_score_chains()
+        c.synchronize()
+        c.lod_reset()
+        t = time.perf_counter()
+        for _ in range(reps):
+            c.lod_score_chains()
+        c.synchronize()
+        return reps * C * npos / (time.perf_counter() - t)
+
+    graphs = ctx.get_graphs()
+    fp32 = lod_rate(ctx, 3)
+    ctx.lod_reset()
+    ctx.lod_score_chains()
+    raw32, c32, tp32 = ctx.lod_results()
+    out = {"members": d["N"], "founders": d["F"], "markers": d["M"], "chains": C, "steps_per_s": steps_s,
+           "lod_positions_per_s": fp32, "setup_s": round(setup_s, 1),
+           "max_cutset": int(max(len(c) for c in d["op_cutset"]))}
+    for name, prec in (("plain_fp64", api.SL_LOD_FP64), ("fp64_rescaled", api.SL_LOD_FP64_RESCALED)):
+        with api.Context(prob, n_chains=C, device=device, lod_precision=prec, lod_flags=api.SL_LOD_ZERO_OK) as c64:
+            c64.set_graphs(graphs)
+            rate = lod_rate(c64, 1)
+            c64.lod_reset()
+            c64.lod_score_chains()
+            raw64, c_64, tp64 = c64.lod_results()
+        fin = raw64 > -1e300
+        out[name] = {"lod_positions_per_s": rate, "positions_underflowed": int((~fin).sum()),
+                     "max_abs_dlod_fp32": float(np.abs(api.lod_table(raw32, c32, tp32)
+                                                       - api.lod_table(raw64, c_64, tp64))[fin].max())
+                     if fin.any() else None}
+    out["batched_vs_plain_lod"] = fp32 / out["plain_fp64"]["lod_positions_per_s"]
+    ctx.close()
+    return out
 
 
 def uneven_batch_rate(device, n_ped=64, chains=8, K=20):

@@ -54,6 +54,8 @@ extern "C" {
 /* LOD arithmetic */
 #define SL_LOD_FP64 0          /* plain: FP64 trait peel, one warp per (graph, interval, offset) */
 #define SL_LOD_FP32_RESCALED 1 /* batched: FP32 peel with per-rfunction power-of-two rescaling */
+#define SL_LOD_FP64_RESCALED 2 /* FP64 peel with per-rfunction rescaling: the plain form for pedigrees whose
+                                  unscaled likelihood underflows FP64 (no counterpart in the reference) */
 
 typedef struct sl_ctx sl_ctx;
 

@@ -17,7 +17,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_build", "libswiftlink_gb300.so")
 
 SL_OK, SL_EINVAL, SL_ECUDA, SL_EZERO, SL_EILLEGAL, SL_ENOMEM, SL_ENODEV = 0, -1, -2, -3, -4, -5, -6
-SL_LOD_FP64, SL_LOD_FP32_RESCALED = 0, 1
+SL_LOD_FP64, SL_LOD_FP32_RESCALED, SL_LOD_FP64_RESCALED = 0, 1, 2
 SL_SAMPLER_EXACT, SL_SAMPLER_FAST = 0, 1
 SL_LOD_KERNEL_AUTO, SL_LOD_KERNEL_INTERP, SL_LOD_KERNEL_JIT_REG, SL_LOD_KERNEL_JIT_SMEM = 0, 1, 2, 3
 SL_LOD_ZERO_OK = 1

@@ -999,7 +999,8 @@ int sl_create(const sl_problem_desc* d, const sl_options* opt, sl_ctx** out) {
     if (d->sex_linked) return fail(ctx, SL_EINVAL, "sex-linked analysis is not supported on the GPU");
     if (opt->n_chains < 1) return fail(ctx, SL_EINVAL, "n_chains must be >= 1");
     if (opt->lod_flags & ~SL_LOD_ZERO_OK) return fail(ctx, SL_EINVAL, "unknown lod_flags %#x", opt->lod_flags);
-    if (opt->lod_precision != SL_LOD_FP64 && opt->lod_precision != SL_LOD_FP32_RESCALED)
+    if (opt->lod_precision != SL_LOD_FP64 && opt->lod_precision != SL_LOD_FP32_RESCALED &&
+        opt->lod_precision != SL_LOD_FP64_RESCALED)
         return fail(ctx, SL_EINVAL, "unknown lod_precision %d", opt->lod_precision);
     if (opt->sampler_precision != SL_SAMPLER_EXACT && opt->sampler_precision != SL_SAMPLER_FAST)
         return fail(ctx, SL_EINVAL, "unknown sampler_precision %d", opt->sampler_precision);
@@ -1151,7 +1152,7 @@ int sl_create(const sl_problem_desc* d, const sl_options* opt, sl_ctx** out) {
 
     // ---- launch shapes from the shared-memory footprint of one task
     const size_t lsw = lsampler_smem_per_warp(P);
-    const size_t lodw = (size_t)arena * (ctx->lod_precision == SL_LOD_FP64 ? 8 : 4);
+    const size_t lodw = (size_t)arena * (ctx->lod_precision == SL_LOD_FP32_RESCALED ? 4 : 8);
     if (lsw > kSmemBudget || lodw > kSmemBudget)
         return bail(fail(nullptr, SL_EINVAL, "peel sequence needs %zu bytes per task, above the shared-memory budget",
                          std::max(lsw, lodw)));

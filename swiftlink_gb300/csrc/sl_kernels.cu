@@ -1605,8 +1605,15 @@ __global__ void __launch_bounds__(128) lod_kernel(ProblemDev P, const uint32_t* 
                     mx = o2 > mx ? o2 : mx;
                 }
                 if (mx > (T)0) {
-                    const int e = ilogbf((float)mx);
-                    const T f = (T)scalbnf(1.0f, -e);
+                    int e;
+                    T f;
+                    if constexpr (sizeof(T) == 8) {
+                        e = ilogb(mx);
+                        f = scalbn(1.0, -e);
+                    } else {
+                        e = ilogbf(mx);
+                        f = scalbnf(1.0f, -e);
+                    }
                     for (int cell = lane; cell < ncell; cell += 32) out[cell] *= f;
                     scale += e;
                 }
@@ -2284,6 +2291,15 @@ cudaError_t launch_lod(const ProblemDev& P, int precision, const uint32_t* graph
             configured = smem;
         }
         lod_kernel<double, false><<<(int)grid, wpb * 32, smem, s>>>(P, graphs, graph_words, G, vals, status);
+    } else if (precision == 2) {   // FP64 with per-rfunction power-of-two rescaling
+        const size_t smem = (size_t)wpb * P.arena * sizeof(double);
+        static size_t configured = 0;
+        if (smem > configured) {
+            cudaError_t e = cudaFuncSetAttribute(lod_kernel<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess) return e;
+            configured = smem;
+        }
+        lod_kernel<double, true><<<(int)grid, wpb * 32, smem, s>>>(P, graphs, graph_words, G, vals, status);
     } else if (P.prog) {
         const int S = P.prog_threads;
         const size_t smem = (size_t)S * P.prog_slots * sizeof(float);

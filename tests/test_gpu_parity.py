@@ -387,3 +387,16 @@ def test_zero_trait_likelihood_policy():
         ctx.lod_score_graphs(bad)
         raw32, _, _ = ctx.lod_results()
     assert np.all(np.isfinite(raw32)) and raw32.min() > -1e300
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_fp64_rescaled_lod_equals_plain(name):
+    """The FP64 peel with per-rfunction rescaling (for pedigrees whose unscaled
+    likelihood underflows) equals the plain FP64 peel where that does not
+    underflow."""
+    g = load_golden(name)
+    with make_ctx(g, precision=api.SL_LOD_FP64_RESCALED) as ctx:
+        ctx.lod_score_graphs(g["lod_graphs"])
+        raw, cnt, tp = ctx.lod_results()
+    want = api.lod_table(g["lod_raw"], g["lod_count"], g["lod_trait_prob"])
+    assert np.abs(api.lod_table(raw, cnt, tp) - want).max() <= FP64_LOD_TOL
