@@ -370,6 +370,21 @@ int sl_batch_create(sl_ctx* const* ctxs, int32_t n, sl_batch** out);
 int sl_batch_run(sl_batch* batch, const sl_run_options* opt);
 void sl_batch_destroy(sl_batch* batch);
 
+/*
+ * Sequential imputation (SequentialImputation::run / LocusSampler::start_from,
+ * sequential_imputation.cc:14-43, locus_sampler2.cc:214-241): legal starting
+ * graphs.  sl_sequential_imputation runs one pass per listed chain from the
+ * given start locus with the given draws (chain c's at draws + c *
+ * chain_stride, consumed in order as get_random() would return them) and
+ * writes each pass's weight (the sum of log peel results; -DBL_MAX if a locus
+ * has likelihood 0).  sl_sequential_imputation_run runs `iterations` passes
+ * per chain from the Philox stream and keeps each chain's best graph;
+ * best_weights (may be NULL) receives the best weights.
+ */
+int sl_sequential_imputation(sl_ctx* ctx, int32_t first, int32_t n_chains, const int32_t* start_loci,
+                             const double* draws, int64_t chain_stride, double* weights);
+int sl_sequential_imputation_run(sl_ctx* ctx, int32_t iterations, uint64_t seed, double* best_weights);
+
 /* Library version string. */
 const char* sl_version(void);
 

@@ -101,6 +101,19 @@ class Port:
             raise RuntimeError(f"slo_lstep failed ({rc})")
         return dg, used.value
 
+    def si(self, dg, start, u):
+        """One sequential-imputation pass from locus `start`, draws consumed in
+        order: (graph, draws used, weight)."""
+        dg = np.ascontiguousarray(dg, np.int32).copy()
+        u = np.ascontiguousarray(u, np.float64)
+        used = ctypes.c_int()
+        w = ctypes.c_double()
+        rc = lib().slo_si(ctypes.byref(self.s), _p(dg), int(start), _p(u), u.size, ctypes.byref(used),
+                          ctypes.byref(w))
+        if rc != 0:
+            raise RuntimeError(f"slo_si failed ({rc})")
+        return dg, used.value, w.value
+
     def msweep(self, dg, meioses, u):
         dg = np.ascontiguousarray(dg, np.int32).copy()
         meioses = np.ascontiguousarray(meioses, np.int32)

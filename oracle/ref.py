@@ -173,6 +173,16 @@ class Ref:
             raise RuntimeError("uniform buffer overrun in lstep")
         return dg, used.value
 
+    def si(self, dg: np.ndarray, start: int, u: np.ndarray):
+        dg = np.ascontiguousarray(dg, np.int32).copy()
+        u = np.ascontiguousarray(u, np.float64)
+        used = ctypes.c_int()
+        w = ctypes.c_double()
+        rc = lib().ref_si(_p(self.h), _ptr(dg), int(start), _ptr(u), u.size, ctypes.byref(used), ctypes.byref(w))
+        if rc != 0:
+            raise RuntimeError("uniform buffer overrun in sequential imputation")
+        return dg, used.value, w.value
+
     def msweep(self, dg: np.ndarray, meioses: np.ndarray, u: np.ndarray):
         dg = np.ascontiguousarray(dg, np.int32).copy()
         meioses = np.ascontiguousarray(meioses, np.int32)

@@ -201,6 +201,19 @@ extern "C" int ref_loglik(void* h, const int* dg_in_buf, double* loglik) {
     return 0;
 }
 
+// One sequential-imputation pass from `start` (LocusSampler::start_from,
+// locus_sampler2.cc:214-241) with the injected draws; returns its weight.
+extern "C" int ref_si(void* h, int* dg_io, int start, const double* u, int n_u, int* n_used, double* weight) {
+    RefState* s = (RefState*)h;
+    DescentGraph dg(s->ped, &s->map, s->sex_linked);
+    dg_in(s, dg, dg_io);
+    stub_arm(u, n_u);
+    *weight = s->ls->start_from(dg, (unsigned)start);
+    *n_used = stub_disarm();
+    dg_out(s, dg, dg_io);
+    return *n_used < 0 ? -1 : 0;
+}
+
 // Temper the map in place (GeneticMap::set_temperature, once per map) and
 // rebuild the samplers on it, as a tempered MarkovChain holds them.
 extern "C" int ref_set_temperature(void* h, double t) {

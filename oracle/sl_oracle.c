@@ -33,18 +33,26 @@ static inline int ipow4(int c) { return 1 << (2 * c); }
  * ------------------------------------------------------------------------- */
 
 /* get_recombination_distribution (sampler_rfunction.cc:102-157) */
+/* has_left / has_right: the neighbouring loci the step may use; false at the
+   ends of the map and where sequential imputation ignores a side
+   (set_locus(l, ignore_left, ignore_right), sampler_rfunction.h:84-101) */
+static int g_has_left = -1, g_has_right = -1;   /* -1: decided by the locus */
+
+static int use_left(const slo_problem* p, int locus) { return g_has_left < 0 ? locus != 0 : g_has_left; }
+static int use_right(const slo_problem* p, int locus) { return g_has_right < 0 ? locus != p->M - 1 : g_has_right; }
+
 static void recomb_dist(const slo_problem* p, const int32_t* dg, int locus, int person, int parent_trait,
                         int parent, double* dist) {
     if (parent_trait == UU) { dist[T_U] = 1.0; dist[T_A] = 0.0; return; }
     if (parent_trait == AA) { dist[T_U] = 0.0; dist[T_A] = 1.0; return; }
     double tmp0 = 0.5, tmp1 = 0.5;
-    if (locus != 0) {
+    if (use_left(p, locus)) {
         int cross = dgget(p, dg, person, locus - 1, parent) != 0;
         double th2 = p->theta[locus - 1], an2 = 1.0 - p->theta[locus - 1];
         tmp0 *= (cross ? th2 : an2);
         tmp1 *= (cross ? an2 : th2);
     }
-    if (locus != p->M - 1) {
+    if (use_right(p, locus)) {
         int cross = dgget(p, dg, person, locus + 1, parent) != 0;
         double th = p->theta[locus], an = 1.0 - p->theta[locus];
         tmp0 *= (cross ? th : an);
@@ -92,6 +100,8 @@ static inline int prev_index(const slo_problem* p, int j, const int* assign) {
         idx += assign[p->cut[q]] << (2 * (q - p->cut_off[j]));
     return idx;
 }
+
+static double g_last_root = 0.0;
 
 int slo_lstep(const slo_problem* p, int32_t* dg, int locus, const double* u, int n_u, int* n_used) {
     int N = p->N, K = p->K;
@@ -181,6 +191,7 @@ int slo_lstep(const slo_problem* p, int32_t* dg, int locus, const double* u, int
         }
     }
     if (w.mat[K - 1][0] == 0.0) { rc = -1; goto done; }  /* locus_sampler2.cc:137-142 */
+    g_last_root = w.mat[K - 1][0];
     /* backward sampling (locus_sampler2.cc:146-148, sampler_rfunction.cc:159-188) */
     for (int i = 0; i < N; ++i) w.assign[i] = -1;
     for (int k = K - 1; k >= 0; --k) {
@@ -219,13 +230,13 @@ int slo_lstep(const slo_problem* p, int32_t* dg, int locus, const double* u, int
                 else mi = (ptr == UA) ? 1 : 0;
             } else {  /* sample_homo_mi (locus_sampler2.cc:44-65) */
                 double p0 = 1.0, p1 = 1.0;
-                if (locus != 0) {
+                if (use_left(p, locus)) {
                     int d = dgget(p, dg, i, locus - 1, par);
                     double th = p->theta[locus - 1], an = 1.0 - p->theta[locus - 1];
                     p0 *= (d == 0) ? an : th;
                     p1 *= (d == 1) ? an : th;
                 }
-                if (locus != p->M - 1) {
+                if (use_right(p, locus)) {
                     int d = dgget(p, dg, i, locus + 1, par);
                     double th = p->theta[locus], an = 1.0 - p->theta[locus];
                     p0 *= (d == 0) ? an : th;
@@ -851,4 +862,31 @@ double slo_philox_uniform(uint64_t key, uint64_t c_hi, uint64_t c_lo) {
     }
     uint64_t hi = c0 >> 5, lo = c1 >> 6;
     return (double)(hi * 67108864ull + lo) * (1.0 / 9007199254740992.0);
+}
+
+
+/* ---------------------------------------------------------------------------
+ * Sequential imputation (LocusSampler::start_from, locus_sampler2.cc:214-241):
+ * the starting locus with no neighbours, then leftwards using the right
+ * neighbour only, then rightwards using the left neighbour only; the weight is
+ * the sum of log(root) over the steps.  Draws are consumed in one sequence.
+ * ------------------------------------------------------------------------- */
+int slo_si(const slo_problem* p, int32_t* dg, int start, const double* u, int n_u, int* n_used, double* weight) {
+    int used = 0, rc = 0, M = p->M;
+    double wsum = 0.0;
+    for (int v = 0; v < M; ++v) {
+        int l = v == 0 ? start : (v <= start ? start - v : v);
+        if (v == 0) { g_has_left = 0; g_has_right = 0; }
+        else if (v <= start) { g_has_left = 0; g_has_right = l != M - 1; }
+        else { g_has_left = l != 0; g_has_right = 0; }
+        int n = 0;
+        rc = slo_lstep(p, dg, l, u + used, n_u - used, &n);
+        used += n;
+        if (rc) break;
+        wsum += log(g_last_root);
+    }
+    g_has_left = g_has_right = -1;
+    *n_used = used;
+    *weight = wsum;
+    return rc;
 }

@@ -49,6 +49,7 @@ typedef struct {
  * the first, then one per homozygous-parent meiosis in person order, maternal
  * before paternal.  Returns 0, or -1 on zero likelihood, -2 on draw overrun. */
 int slo_lstep(const slo_problem* p, int32_t* dg, int locus, const double* u, int n_u, int* n_used);
+int slo_si(const slo_problem* p, int32_t* dg, int start, const double* u, int n_u, int* n_used, double* weight);
 
 /* One M-sweep: reset at meioses[0] then one step per listed meiosis
  * (markov_chain.cc:345-351, meiosis_sampler.cc:17-203).  Step j reads its

@@ -31,6 +31,7 @@ EXPORTED = [
     "sl_problem_trait_priors", "sl_problem_trait_prob", "sl_trait_backward",
     "sl_problem_trait_backward_eval", "sl_lod_kernel_info", "sl_set_temperatures", "sl_mc3_stats",
     "sl_chain_loglik", "sl_peel_sequence", "sl_batch_create", "sl_batch_run", "sl_batch_destroy",
+    "sl_sequential_imputation", "sl_sequential_imputation_run",
 ]
 
 
@@ -341,6 +342,23 @@ class Context:
         prop = np.zeros(n, np.int64)
         self._check(lib().sl_mc3_stats(self.h, _p(acc), _p(prop)))
         return acc[: self.n_chains - 1], prop[: self.n_chains - 1]
+
+    def sequential_imputation(self, starts, draws, first: int = 0):
+        """One imputation pass per chain from the given start loci, draws [n][L]
+        consumed in order; returns the passes' weights."""
+        st = np.ascontiguousarray(starts, np.int32)
+        u = np.ascontiguousarray(draws, np.float64)
+        n = st.size
+        assert u.ndim == 2 and u.shape[0] == n
+        w = np.zeros(n)
+        self._check(lib().sl_sequential_imputation(self.h, first, n, _p(st), _p(u), ctypes.c_int64(u.shape[1]),
+                                                   _p(w)))
+        return w
+
+    def sequential_imputation_run(self, iterations: int, seed: int = 1):
+        w = np.zeros(self.n_chains)
+        self._check(lib().sl_sequential_imputation_run(self.h, int(iterations), ctypes.c_uint64(seed), _p(w)))
+        return w
 
     def chain_loglik(self, graph_chain: int, map_chain: int) -> float:
         v = ctypes.c_double()

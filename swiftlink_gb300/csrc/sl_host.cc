@@ -35,6 +35,11 @@ cudaError_t launch_msampler(const ProblemDev& P, uint32_t* dg, int first, int nc
                             uint8_t* maps, int* status, int fag_threads, int exact, cudaStream_t s,
                             const uint64_t* key = nullptr);
 cudaError_t launch_set_key(uint64_t* key, uint64_t seed, uint64_t iter, cudaStream_t s);
+cudaError_t launch_si(const ProblemDev& P, uint32_t* dg, int first, int nchain, const int32_t* starts,
+                      const double* u, int64_t ucs, uint64_t seed, uint64_t pass, double* weights, int* status,
+                      cudaStream_t s, int wpb);
+cudaError_t launch_si_select(const uint32_t* scratch, uint32_t* dg, int first, int nchain, size_t words,
+                             const double* w, double* best, cudaStream_t s);
 cudaError_t launch_run_init(const RunParams* rp, int64_t* it, int C, cudaStream_t s);
 cudaError_t launch_chain_iter(const RunParams* rp, const int64_t* it, int c, uint64_t* key, const int32_t* base,
                               int nm, int32_t* order, const double* temp, cudaGraphConditionalHandle hsw,
@@ -2432,6 +2437,96 @@ int sl_batch_run(sl_batch* b, const sl_run_options* o) {
                 }
     }
     return SL_OK;
+}
+
+
+// ---------------------------------------------------------------------------
+// Sequential imputation: legal starting graphs (SequentialImputation,
+// sequential_imputation.cc:14-125; LocusSampler::start_from,
+// locus_sampler2.cc:214-241).
+// ---------------------------------------------------------------------------
+int sl_sequential_imputation(sl_ctx* ctx, int32_t first, int32_t n_chains, const int32_t* start_loci,
+                             const double* draws, int64_t chain_stride, double* weights) {
+    int rc = check_chains(ctx, first, n_chains);
+    if (rc) return rc;
+    if (!start_loci || !draws || chain_stride < 1 || !weights) return fail(ctx, SL_EINVAL, "bad arguments");
+    for (int c = 0; c < n_chains; ++c)
+        if (start_loci[c] < 0 || start_loci[c] >= ctx->P.M) return fail(ctx, SL_EINVAL, "start locus out of range");
+    CK(cudaSetDevice(ctx->device));
+    const size_t nu = (size_t)n_chains * chain_stride;
+    if (nu > ctx->u_cap) {
+        if (ctx->d_u) {
+            cudaStreamSynchronize(ctx->stream);
+            cudaFree(ctx->d_u);
+            ctx->owned.erase(std::find(ctx->owned.begin(), ctx->owned.end(), (void*)ctx->d_u));
+            ctx->d_u = nullptr;
+        }
+        if ((rc = dev_alloc(ctx, &ctx->d_u, nu))) return rc;
+        ctx->u_cap = nu;
+    }
+    int32_t* d_starts = nullptr;
+    double* d_w = nullptr;
+    if ((rc = dev_alloc(ctx, &d_starts, (size_t)n_chains))) return rc;
+    if ((rc = dev_alloc(ctx, &d_w, (size_t)n_chains))) return rc;
+    CK(cudaMemcpyAsync(ctx->d_u, draws, sizeof(double) * nu, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(d_starts, start_loci, sizeof(int32_t) * n_chains, cudaMemcpyHostToDevice, ctx->stream));
+    { Prof pf_(ctx, SL_KERNEL_LSAMPLER);
+    CK(launch_si(ctx->P, ctx->d_dg, first, n_chains, d_starts, ctx->d_u, chain_stride, 0, 0, d_w, ctx->d_status,
+                 ctx->stream, ctx->ls_wpb)); }
+    CK(cudaMemcpyAsync(weights, d_w, sizeof(double) * n_chains, cudaMemcpyDeviceToHost, ctx->stream));
+    rc = sl_synchronize(ctx);
+    for (void* p : {(void*)d_starts, (void*)d_w}) {
+        cudaFree(p);
+        ctx->owned.erase(std::find(ctx->owned.begin(), ctx->owned.end(), p));
+    }
+    return rc;
+}
+
+int sl_sequential_imputation_run(sl_ctx* ctx, int32_t iterations, uint64_t seed, double* best_weights) {
+    if (!ctx || iterations < 1) return fail(ctx, SL_EINVAL, "bad arguments");
+    CK(cudaSetDevice(ctx->device));
+    const ProblemDev& P = ctx->P;
+    const int C = ctx->n_chains, M = P.M;
+    const size_t words = (size_t)M * P.W;
+    uint32_t* scratch = nullptr;
+    int32_t* d_starts = nullptr;
+    double *d_w = nullptr, *d_best = nullptr;
+    int rc;
+    if ((rc = dev_alloc(ctx, &scratch, words * C))) return rc;
+    if ((rc = dev_alloc(ctx, &d_starts, (size_t)C))) return rc;
+    if ((rc = dev_alloc(ctx, &d_w, (size_t)C))) return rc;
+    if ((rc = dev_alloc(ctx, &d_best, (size_t)C))) return rc;
+    std::vector<double> lowest(C, -DBL_MAX);
+    CK(cudaMemcpyAsync(d_best, lowest.data(), sizeof(double) * C, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemsetAsync(scratch, 0, sizeof(uint32_t) * words * C, ctx->stream));
+    std::vector<int32_t> starts(C);
+    for (int pass = 0; pass < iterations; ++pass) {
+        // the start locus (get_random_locus) from its own Philox stage
+        for (int c = 0; c < C; ++c) {
+            const uint64_t hi = ((uint64_t)c << 40) ^ ((uint64_t)pass << 4) ^ 6u;
+            starts[c] = std::min(M - 1, (int)(host_philox_u01(seed, hi, 0) * M));
+        }
+        CK(cudaMemcpyAsync(d_starts, starts.data(), sizeof(int32_t) * C, cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));   // the host vector is reused next pass
+        // the pass writes chain c's graph into scratch slot c (first = 0 on the scratch array)
+        { Prof pf_(ctx, SL_KERNEL_LSAMPLER);
+        CK(launch_si(P, scratch, 0, C, d_starts, nullptr, 0, seed, (uint64_t)pass, d_w, ctx->d_status, ctx->stream,
+                     ctx->ls_wpb)); }
+        { Prof pf_(ctx, SL_KERNEL_OTHER);
+        CK(launch_si_select(scratch, ctx->d_dg, 0, C, words, d_w, d_best, ctx->stream)); }
+    }
+    if (best_weights)
+        CK(cudaMemcpyAsync(best_weights, d_best, sizeof(double) * C, cudaMemcpyDeviceToHost, ctx->stream));
+    rc = sl_synchronize(ctx);
+    for (void* p : {(void*)scratch, (void*)d_starts, (void*)d_w, (void*)d_best}) {
+        cudaFree(p);
+        ctx->owned.erase(std::find(ctx->owned.begin(), ctx->owned.end(), p));
+    }
+    if (!rc && best_weights)
+        for (int c = 0; c < C; ++c)
+            if (best_weights[c] == -DBL_MAX)
+                return fail(ctx, SL_EZERO, "sequential imputation produced no legal graph for chain %d", c);
+    return rc;
 }
 
 int sl_mc3_stats(sl_ctx* ctx, int64_t* accepted, int64_t* proposed) {

@@ -121,12 +121,12 @@ __device__ void ls_dist_one(const ProblemDev& P, int person, const uint32_t* col
         s[UU * 2 + 0] = T(1); s[UU * 2 + 1] = T(0);
         s[AA * 2 + 0] = T(0); s[AA * 2 + 1] = T(1);
         T tmp0 = T(0.5), tmp1 = T(0.5);
-        if (l != 0) {
+        if (colL) {   // a left neighbour (absent at locus 0 and when imputation ignores it)
             const bool cross = dgbit(colL, b) != 0;
             tmp0 = A::mul(tmp0, cross ? th2 : an2);
             tmp1 = A::mul(tmp1, cross ? an2 : th2);
         }
-        if (l != P.M - 1) {
+        if (colR) {
             const bool cross = dgbit(colR, b) != 0;
             tmp0 = A::mul(tmp0, cross ? th : an);
             tmp1 = A::mul(tmp1, cross ? an : th);
@@ -198,166 +198,218 @@ __host__ __device__ __forceinline__ size_t ls_warp_bytes(const ProblemDev& P) {
 
 // One warp per (chain, locus) task; the listed loci must be pairwise
 // non-adjacent so each task owns its descent-graph column.
+// One L-sampler step at locus l of one chain, by one warp
+// (LocusSampler::step, locus_sampler2.cc:128-159): hasL / hasR say whether the
+// neighbouring columns take part (set_locus(l, ignore_left, ignore_right),
+// sampler_rfunction.h:84-101).  Draws are taken at indices base, base + 1, ...
+// of the unit's stream.  Returns the number of draws used, or -1 when the
+// locus has likelihood 0; *logroot (lane 0) receives log of the peel's result.
+template <typename T>
+__device__ int ls_locus(const ProblemDev& P, uint32_t* dg, int cr, int chain, int l, bool hasL, bool hasR,
+                        const Draws& draws, int64_t unit, int64_t base, unsigned char* wsmem, int lane, int* status,
+                        double* logroot) {
+    using Ar = Ls<T>;
+    constexpr bool kRescale = sizeof(T) == 4;   // FP32: each rfunction scaled to a maximum of about 1
+    T* A = (T*)wsmem;
+    T* dist = A + P.arena;
+    int8_t* assign = (int8_t*)(dist + 16 * P.max_child);
+    uint32_t* colC = dg + ((size_t)chain * P.M + l) * P.W;
+    const uint32_t* colL = hasL ? colC - P.W : nullptr;
+    const uint32_t* colR = hasR ? colC + P.W : nullptr;
+    T th = T(1), an = T(1), th2 = T(1), an2 = T(1);
+    if constexpr (sizeof(T) == 4) {
+        const float* tf = P.c_theta_f + (size_t)chain * (P.M - 1);
+        if (hasL) { th2 = tf[l - 1]; an2 = 1.f - th2; }
+        if (hasR) { th = tf[l]; an = 1.f - th; }
+    } else {
+        const double* td = P.c_theta + (size_t)chain * (P.M - 1);
+        if (hasL) { th2 = td[l - 1]; an2 = DSUB(1.0, td[l - 1]); }
+        if (hasR) { th = td[l]; an = DSUB(1.0, td[l]); }
+    }
+    const uint8_t* gcol = P.geno + (size_t)l * P.N;
+    const T* pri;
+    if constexpr (sizeof(T) == 4) pri = (const T*)(P.prior_f + (size_t)l * 16);
+    else pri = (const T*)(P.prior + (size_t)l * 16);
+    int scale = 0;
+    // forward peel over the valid cells of every rfunction
+    for (int k = 0; k < P.K; ++k) {
+        const OpDev op = P.ops[k];
+        ls_dists<T>(P, op, colL, colR, l, th, an, th2, an2, dist, lane);
+        __syncwarp();
+        const int ncell = 1 << (2 * op.c);
+        const int32_t* cut = P.opdata + op.cut_at;
+        const T* trait = pri + 4 * (gcol[op.peel] & 3);
+        T* out = A + op.mat_off;
+        T mx = T(0);
+        for (int cell = lane; cell < ncell; cell += 32) {
+            T total = T(0);
+            if (ls_valid(cut, op.c, gcol, cell)) {
+                for (int v = 0; v < 4; ++v) {
+                    const T tv = trait[v];
+                    if (tv == T(0)) continue;
+                    total = Ar::add(total, ls_term<T>(P, op, A, dist, cell, v, tv));
+                }
+            }
+            out[cell] = total;
+            mx = total > mx ? total : mx;
+        }
+        if (kRescale) {
+            // the sampling draws from ratios within one rfunction, so a
+            // power-of-two factor per rfunction changes no decision
+            for (int dd = 16; dd >= 1; dd >>= 1) {
+                const T o = __shfl_xor_sync(FULLMASK, mx, dd);
+                mx = o > mx ? o : mx;
+            }
+            if (mx > T(0)) {
+                const float f = scalbnf(1.0f, -ilogbf((float)mx));
+                for (int cell = lane; cell < ncell; cell += 32) out[cell] = (T)((float)out[cell] * f);
+            }
+        }
+        __syncwarp();
+    }
+    const T root = A[P.ops[P.K - 1].mat_off];
+    if (root == T(0)) {
+        if (lane == 0) set_status(status, ST_ZERO_LIK);
+        __syncwarp();
+        return -1;
+    }
+    if (lane == 0 && logroot) *logroot = log((double)root) + (double)scale * 0.69314718055994530942;
+    for (int i = lane; i < P.N; i += 32) assign[i] = -1;
+    __syncwarp();
+    // backward sampling of ordered genotypes (SamplerRfunction::sample)
+    for (int k = P.K - 1; k >= 0; --k) {
+        const OpDev op = P.ops[k];
+        ls_dists<T>(P, op, colL, colR, l, th, an, th2, an2, dist, lane);
+        __syncwarp();
+        const int32_t* cut = P.opdata + op.cut_at;
+        const T* trait = pri + 4 * (gcol[op.peel] & 3);
+        int cellidx = 0;
+        bool known = true;
+        for (int q = 0; q < op.c; ++q) {
+            const int a = assign[cut[q]];
+            known &= a >= 0;
+            cellidx |= (a & 3) << (2 * q);
+        }
+        T pv = T(0);
+        if (lane < 4 && known) {
+            const T tv = trait[lane];
+            if (tv != T(0) && ls_valid(cut, op.c, gcol, cellidx)) pv = ls_term<T>(P, op, A, dist, cellidx, lane, tv);
+        }
+        const T p0 = __shfl_sync(FULLMASK, pv, 0), p1 = __shfl_sync(FULLMASK, pv, 1);
+        const T p2 = __shfl_sync(FULLMASK, pv, 2), p3 = __shfl_sync(FULLMASK, pv, 3);
+        if (lane == 0) {
+            if (!known) set_status(status, ST_ILLEGAL_DG);
+            T pd[4] = {p0, p1, p2, p3};
+            const T tot = Ar::add(Ar::add(Ar::add(p0, p1), p2), p3);
+            if (tot != T(0))
+                for (int v = 0; v < 4; ++v) pd[v] = Ar::div(pd[v], tot);
+            const double r = draws.get(cr, chain, unit, base + P.K - 1 - k);
+            T acc = T(0);
+            int lastv = 0, pick = -1;
+            for (int v = 0; v < 4; ++v) {
+                acc = Ar::add(acc, pd[v]);
+                if (r < (double)acc) { pick = v; break; }
+                if (pd[v] != T(0)) lastv = v;
+            }
+            assign[op.peel] = (int8_t)(pick >= 0 ? pick : lastv);
+        }
+        __syncwarp();
+    }
+    // meiosis indicators (locus_sampler2.cc:32-125) in person order, maternal
+    // first: bit b = 2 (person - F) + parent, so 32 consecutive meioses are one
+    // descent-graph word.  A lane takes one meiosis; a draw is consumed only
+    // below a homozygous parent, and a ballot prefix gives each draw its index.
+    {
+        int64_t cursor = base + P.K;
+        const int nb = 2 * P.Nnf;
+        for (int w = 0; w < P.W; ++w) {
+            const int b = 32 * w + lane;
+            int mi = 0, need = 0;
+            T p0 = T(1), p1 = T(1);
+            if (b < nb) {
+                const int i = P.F + (b >> 1), par = b & 1;
+                const int tr = assign[i];
+                const int ptr = assign[par == 0 ? P.mother[i] : P.father[i]];
+                const int allele = par == 0 ? ((tr == UU || tr == UA) ? 0 : 1) : ((tr == UU || tr == AU) ? 0 : 1);
+                if (ptr == UA || ptr == AU) {
+                    mi = allele == 0 ? (ptr == UA ? 0 : 1) : (ptr == UA ? 1 : 0);
+                } else {
+                    need = 1;
+                    if (hasL) {
+                        const int d = dgbit(colL, b);
+                        p0 = Ar::mul(p0, d == 0 ? an2 : th2);
+                        p1 = Ar::mul(p1, d == 1 ? an2 : th2);
+                    }
+                    if (hasR) {
+                        const int d = dgbit(colR, b);
+                        p0 = Ar::mul(p0, d == 0 ? an : th);
+                        p1 = Ar::mul(p1, d == 1 ? an : th);
+                    }
+                }
+            }
+            const unsigned nmask = __ballot_sync(FULLMASK, need);
+            if (need) {
+                const double r = draws.get(cr, chain, unit, cursor + __popc(nmask & ((1u << lane) - 1u)));
+                mi = (r < (double)Ar::div(p0, Ar::add(p0, p1))) ? 0 : 1;
+            }
+            cursor += __popc(nmask);
+            const unsigned word = __ballot_sync(FULLMASK, mi != 0);
+            if (lane == 0) colC[w] = word;   // bits past 2 Nnf stay zero
+        }
+        __syncwarp();
+        return (int)(cursor - base);
+    }
+}
+
+// One warp per (chain, locus) task; the listed loci must be pairwise
+// non-adjacent so each task owns its descent-graph column.
 template <typename T>
 __global__ void __launch_bounds__(128) lsampler_kernel(ProblemDev P, uint32_t* dg, int first, int nchain,
                                                        const int32_t* loci, int nloci, Draws draws,
                                                        const uint8_t* sel, int want, int* status) {
-    using Ar = Ls<T>;
-    constexpr bool kRescale = sizeof(T) == 4;   // FP32: each rfunction scaled to a maximum of about 1
     extern __shared__ __align__(16) unsigned char smem[];
     const int wpb = blockDim.x >> 5, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    unsigned char* base = smem + (size_t)warp * ls_warp_bytes<T>(P);
-    T* A = (T*)base;
-    T* dist = A + P.arena;
-    int8_t* assign = (int8_t*)(dist + 16 * P.max_child);
+    unsigned char* wsmem = smem + (size_t)warp * ls_warp_bytes<T>(P);
     const int64_t ntask = (int64_t)nchain * nloci;
     for (int64_t t = (int64_t)blockIdx.x * wpb + warp; t < ntask; t += (int64_t)gridDim.x * wpb) {
         const int cr = (int)(t / nloci);
         if (sel && sel[cr] != want) continue;
-        const int chain = first + cr;
         const int l = loci[t % nloci];
-        uint32_t* colC = dg + ((size_t)chain * P.M + l) * P.W;
-        const uint32_t* colL = l > 0 ? colC - P.W : nullptr;
-        const uint32_t* colR = l < P.M - 1 ? colC + P.W : nullptr;
-        T th = T(1), an = T(1), th2 = T(1), an2 = T(1);
-        if constexpr (sizeof(T) == 4) {
-            const float* tf = P.c_theta_f + (size_t)chain * (P.M - 1);
-            if (l > 0) { th2 = tf[l - 1]; an2 = 1.f - th2; }
-            if (l < P.M - 1) { th = tf[l]; an = 1.f - th; }
-        } else {
-            const double* td = P.c_theta + (size_t)chain * (P.M - 1);
-            if (l > 0) { th2 = td[l - 1]; an2 = DSUB(1.0, td[l - 1]); }
-            if (l < P.M - 1) { th = td[l]; an = DSUB(1.0, td[l]); }
+        ls_locus<T>(P, dg, cr, first + cr, l, l > 0, l < P.M - 1, draws, l, 0, wsmem, lane, status, nullptr);
+    }
+}
+
+// Sequential imputation (LocusSampler::start_from, locus_sampler2.cc:214-241),
+// one warp per chain: the start locus with neither neighbour, then leftwards
+// with the right neighbour only, then rightwards with the left neighbour only;
+// draws are consumed in one sequence (unit `unit`), the weight is the sum of
+// log(root) over the steps (-DBL_MAX when a locus has likelihood 0).
+template <typename T>
+__global__ void __launch_bounds__(128) si_kernel(ProblemDev P, uint32_t* dg, int first, int nchain,
+                                                 const int32_t* starts, Draws draws, int64_t unit, double* weights,
+                                                 int* status) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int wpb = blockDim.x >> 5, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    unsigned char* wsmem = smem + (size_t)warp * ls_warp_bytes<T>(P);
+    for (int cr = blockIdx.x * wpb + warp; cr < nchain; cr += gridDim.x * wpb) {
+        const int chain = first + cr, M = P.M, start = starts[cr];
+        int64_t base = 0;
+        double w = 0.0;
+        bool ok = true;
+        for (int v = 0; v < M && ok; ++v) {
+            const int l = v == 0 ? start : (v <= start ? start - v : v);
+            const bool hasL = v > start && l > 0;
+            const bool hasR = v > 0 && v <= start && l < M - 1;
+            double lr = 0.0;
+            const int used = ls_locus<T>(P, dg, cr, chain, l, hasL, hasR, draws, unit, base, wsmem, lane, status, &lr);
+            if (used < 0) {
+                ok = false;
+                break;
+            }
+            base += used;
+            w += __shfl_sync(FULLMASK, lr, 0);
         }
-        const uint8_t* gcol = P.geno + (size_t)l * P.N;
-        const T* pri;
-        if constexpr (sizeof(T) == 4) pri = (const T*)(P.prior_f + (size_t)l * 16);
-        else pri = (const T*)(P.prior + (size_t)l * 16);
-        // forward peel over the valid cells of every rfunction
-        for (int k = 0; k < P.K; ++k) {
-            const OpDev op = P.ops[k];
-            ls_dists<T>(P, op, colL, colR, l, th, an, th2, an2, dist, lane);
-            __syncwarp();
-            const int ncell = 1 << (2 * op.c);
-            const int32_t* cut = P.opdata + op.cut_at;
-            const T* trait = pri + 4 * (gcol[op.peel] & 3);
-            T* out = A + op.mat_off;
-            T mx = T(0);
-            for (int cell = lane; cell < ncell; cell += 32) {
-                T total = T(0);
-                if (ls_valid(cut, op.c, gcol, cell)) {
-                    for (int v = 0; v < 4; ++v) {
-                        const T tv = trait[v];
-                        if (tv == T(0)) continue;
-                        total = Ar::add(total, ls_term<T>(P, op, A, dist, cell, v, tv));
-                    }
-                }
-                out[cell] = total;
-                mx = total > mx ? total : mx;
-            }
-            if (kRescale) {
-                // the sampling draws from ratios within one rfunction, so a
-                // power-of-two factor per rfunction changes no decision
-                for (int dd = 16; dd >= 1; dd >>= 1) {
-                    const T o = __shfl_xor_sync(FULLMASK, mx, dd);
-                    mx = o > mx ? o : mx;
-                }
-                if (mx > T(0)) {
-                    const float f = scalbnf(1.0f, -ilogbf((float)mx));
-                    for (int cell = lane; cell < ncell; cell += 32) out[cell] = (T)((float)out[cell] * f);
-                }
-            }
-            __syncwarp();
-        }
-        const T root = A[P.ops[P.K - 1].mat_off];
-        if (root == T(0)) {
-            if (lane == 0) set_status(status, ST_ZERO_LIK);
-            __syncwarp();
-            continue;
-        }
-        for (int i = lane; i < P.N; i += 32) assign[i] = -1;
-        __syncwarp();
-        // backward sampling of ordered genotypes (SamplerRfunction::sample)
-        for (int k = P.K - 1; k >= 0; --k) {
-            const OpDev op = P.ops[k];
-            ls_dists<T>(P, op, colL, colR, l, th, an, th2, an2, dist, lane);
-            __syncwarp();
-            const int32_t* cut = P.opdata + op.cut_at;
-            const T* trait = pri + 4 * (gcol[op.peel] & 3);
-            int cellidx = 0;
-            bool known = true;
-            for (int q = 0; q < op.c; ++q) {
-                const int a = assign[cut[q]];
-                known &= a >= 0;
-                cellidx |= (a & 3) << (2 * q);
-            }
-            T pv = T(0);
-            if (lane < 4 && known) {
-                const T tv = trait[lane];
-                if (tv != T(0) && ls_valid(cut, op.c, gcol, cellidx)) pv = ls_term<T>(P, op, A, dist, cellidx, lane, tv);
-            }
-            const T p0 = __shfl_sync(FULLMASK, pv, 0), p1 = __shfl_sync(FULLMASK, pv, 1);
-            const T p2 = __shfl_sync(FULLMASK, pv, 2), p3 = __shfl_sync(FULLMASK, pv, 3);
-            if (lane == 0) {
-                if (!known) set_status(status, ST_ILLEGAL_DG);
-                T pd[4] = {p0, p1, p2, p3};
-                const T tot = Ar::add(Ar::add(Ar::add(p0, p1), p2), p3);
-                if (tot != T(0))
-                    for (int v = 0; v < 4; ++v) pd[v] = Ar::div(pd[v], tot);
-                const double r = draws.get(cr, chain, l, P.K - 1 - k);
-                T acc = T(0);
-                int lastv = 0, pick = -1;
-                for (int v = 0; v < 4; ++v) {
-                    acc = Ar::add(acc, pd[v]);
-                    if (r < (double)acc) { pick = v; break; }
-                    if (pd[v] != T(0)) lastv = v;
-                }
-                assign[op.peel] = (int8_t)(pick >= 0 ? pick : lastv);
-            }
-            __syncwarp();
-        }
-        // meiosis indicators (locus_sampler2.cc:32-125) in person order, maternal
-        // first: bit b = 2 (person - F) + parent, so 32 consecutive meioses are one
-        // descent-graph word.  A lane takes one meiosis; a draw is consumed only
-        // below a homozygous parent, and a ballot prefix gives each draw its index.
-        {
-            int64_t cursor = P.K;
-            const int nb = 2 * P.Nnf;
-            for (int w = 0; w < P.W; ++w) {
-                const int b = 32 * w + lane;
-                int mi = 0, need = 0;
-                T p0 = T(1), p1 = T(1);
-                if (b < nb) {
-                    const int i = P.F + (b >> 1), par = b & 1;
-                    const int tr = assign[i];
-                    const int ptr = assign[par == 0 ? P.mother[i] : P.father[i]];
-                    const int allele = par == 0 ? ((tr == UU || tr == UA) ? 0 : 1) : ((tr == UU || tr == AU) ? 0 : 1);
-                    if (ptr == UA || ptr == AU) {
-                        mi = allele == 0 ? (ptr == UA ? 0 : 1) : (ptr == UA ? 1 : 0);
-                    } else {
-                        need = 1;
-                        if (l != 0) {
-                            const int d = dgbit(colL, b);
-                            p0 = Ar::mul(p0, d == 0 ? an2 : th2);
-                            p1 = Ar::mul(p1, d == 1 ? an2 : th2);
-                        }
-                        if (l != P.M - 1) {
-                            const int d = dgbit(colR, b);
-                            p0 = Ar::mul(p0, d == 0 ? an : th);
-                            p1 = Ar::mul(p1, d == 1 ? an : th);
-                        }
-                    }
-                }
-                const unsigned nmask = __ballot_sync(FULLMASK, need);
-                if (need) {
-                    const double r = draws.get(cr, chain, l, cursor + __popc(nmask & ((1u << lane) - 1u)));
-                    mi = (r < (double)Ar::div(p0, Ar::add(p0, p1))) ? 0 : 1;
-                }
-                cursor += __popc(nmask);
-                const unsigned word = __ballot_sync(FULLMASK, mi != 0);
-                if (lane == 0) colC[w] = word;   // bits past 2 Nnf stay zero
-            }
-        }
+        if (lane == 0) weights[cr] = ok ? w : -DBL_MAX;
         __syncwarp();
     }
 }
@@ -2177,6 +2229,51 @@ cudaError_t launch_lsampler(const ProblemDev& P, uint32_t* dg, int first, int nc
     else
         lsampler_kernel<double><<<(int)grid, wpb * 32, smem, s>>>(P, dg, first, nchain, loci, nloci, d, sel, want,
                                                                   status);
+    return cudaGetLastError();
+}
+
+// Keep each chain's better imputation: copy the pass's graph and weight where
+// it beats the best so far (SequentialImputation::run, sequential_imputation.cc:
+// 14-43: `tmp_prob > best_prob`, starting from LOG_ZERO).
+__global__ void si_select_kernel(const uint32_t* scratch, uint32_t* dg, int first, int nchain, size_t words,
+                                 const double* w, double* best) {
+    for (int cr = blockIdx.x; cr < nchain; cr += gridDim.x) {
+        const bool take = w[cr] > best[cr];
+        __syncthreads();
+        if (!take) continue;
+        for (size_t i = threadIdx.x; i < words; i += blockDim.x)
+            dg[(size_t)(first + cr) * words + i] = scratch[(size_t)cr * words + i];
+        __syncthreads();
+        if (threadIdx.x == 0) best[cr] = w[cr];
+    }
+}
+
+cudaError_t launch_si(const ProblemDev& P, uint32_t* dg, int first, int nchain, const int32_t* starts,
+                      const double* u, int64_t ucs, uint64_t seed, uint64_t pass, double* weights, int* status,
+                      cudaStream_t s, int wpb) {
+    const size_t smem = wpb * lsampler_smem_per_warp(P);
+    static size_t configured[2] = {0, 0};
+    const int f = P.ls_fast ? 1 : 0;
+    if (smem > configured[f]) {
+        cudaError_t e = f ? cudaFuncSetAttribute(si_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 (int)smem)
+                          : cudaFuncSetAttribute(si_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 (int)smem);
+        if (e != cudaSuccess) return e;
+        configured[f] = smem;
+    }
+    Draws d{u, ucs, 0, seed, pass, 5, nullptr};
+    const int grid = (nchain + wpb - 1) / wpb;
+    if (f)
+        si_kernel<float><<<grid, wpb * 32, smem, s>>>(P, dg, first, nchain, starts, d, 0, weights, status);
+    else
+        si_kernel<double><<<grid, wpb * 32, smem, s>>>(P, dg, first, nchain, starts, d, 0, weights, status);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_si_select(const uint32_t* scratch, uint32_t* dg, int first, int nchain, size_t words,
+                             const double* w, double* best, cudaStream_t s) {
+    si_select_kernel<<<nchain < 1024 ? nchain : 1024, 256, 0, s>>>(scratch, dg, first, nchain, words, w, best);
     return cudaGetLastError();
 }
 
