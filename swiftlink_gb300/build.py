@@ -8,6 +8,8 @@ LOD kernels when a context is created):
   csrc/sl_host.cc     (g++ against the CUDA runtime headers)
   csrc/sl_jit.cc      (g++, NVRTC source generator and loader)
   csrc/sl_peel.cc     (g++, peel-sequence generator)
+and the program swiftlink_gb300/_build/swift_gb300 (csrc/sl_cli.cc, the
+LINKAGE-file front end) linked against the library.
 """
 from __future__ import annotations
 
@@ -21,6 +23,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libswiftlink_gb300.so")
+CLI = os.path.join(OUT, "swift_gb300")
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 
 
@@ -61,6 +64,8 @@ def build(verbose: bool = False, force: bool = False) -> str:
     jc_o = os.path.join(OUT, "sl_jit.o")
     pc = os.path.join(CSRC, "sl_peel.cc")
     pc_o = os.path.join(OUT, "sl_peel.o")
+    cli = os.path.join(CSRC, "sl_cli.cc")
+    cli_o = os.path.join(OUT, "sl_cli.o")
     cu_o = os.path.join(OUT, "sl_kernels.o")
     cu2_o = os.path.join(OUT, "sl_noalloc.o")
     cc_o = os.path.join(OUT, "sl_host.o")
@@ -69,7 +74,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
         if force or _stale(obj, [src] + hdrs):
             jobs.append([nvcc, GENCODE, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                          "-Xptxas", "-v", "-c", src, "-o", obj])
-    for src, obj in ((cc, cc_o), (jc, jc_o), (pc, pc_o)):
+    for src, obj in ((cc, cc_o), (jc, jc_o), (pc, pc_o), (cli, cli_o)):
         if force or _stale(obj, [src] + hdrs):
             # no contraction of a * b + c into FMA: host FP64 (priors, tempered maps,
             # likelihood sums) must round as the reference's x86-64 build does, on aarch64 too
@@ -84,6 +89,10 @@ def build(verbose: bool = False, force: bool = False) -> str:
         lib64 = os.path.join(cuda, "lib64")
         logs.append(_run([nvcc, GENCODE, "-shared", "-cudart", "static", "-o", LIB, cu_o, cu2_o, cc_o, jc_o, pc_o,
                           "-L" + lib64, "-lnvrtc", "-Xlinker", "-rpath=" + lib64]))
+    if force or _stale(CLI, [cli_o, LIB]):
+        lib64 = os.path.join(cuda, "lib64")
+        logs.append(_run(["g++", "-o", CLI, cli_o, "-L" + OUT, "-lswiftlink_gb300",
+                          "-Wl,-rpath,$ORIGIN", "-Wl,-rpath-link," + lib64]))
     if verbose:
         for l in logs:
             sys.stdout.write(l)
