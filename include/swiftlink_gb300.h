@@ -217,7 +217,8 @@ typedef struct sl_run_options {
     double lsampler_prob;
     uint64_t seed;
     int32_t exchange_period;    /* MC3: iterations between exchanges of adjacent chains' graphs, 0 = none
-                                   (Mc3::run, mc3.cc:83-162) */
+                                   (Mc3::run, mc3.cc:83-162); an exchange follows every iteration count
+                                   that is a multiple of it, so split runs exchange as one run does */
 } sl_run_options;
 
 /* MC3 temperatures, one per chain in exchange order (chain 0 the coldest; the

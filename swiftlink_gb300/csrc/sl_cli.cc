@@ -17,6 +17,7 @@
 
 #include <algorithm>
 #include <cerrno>
+#include <cfloat>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -35,8 +36,10 @@ namespace {
 struct Options {
     std::string ped, map, dat, out = "swiftlink.out", trace_prefix = "trace", seeds, dump;
     int iterations = 50000, burnin = 50000, si = 1000, period = 10, lods = 5, runs = 1;
+    int chains = 1, exchange = 10;   // MC3 (defaults.h:9, 12)
     double lprob = 0.5;
-    bool trace = false, affected_only = false, verbose = false, exact = false;
+    std::vector<double> temps;
+    bool trace = false, affected_only = false, verbose = false, exact = false, mc3 = false;
 };
 
 std::vector<std::string> tokens(const std::string& line) {
@@ -245,6 +248,26 @@ bool parse_dat(const std::string& path, Model& m, bool& sexlinked) {
     return true;
 }
 
+// log_sum (logarithms.cc:14-25), LOG_ZERO = -DBL_MAX
+double log_sum(double a, double b) {
+    if (a == -DBL_MAX) return b;
+    if (b == -DBL_MAX) return a;
+    return std::log(std::exp(b - a) + 1) + a;
+}
+
+bool csv_doubles(const char* s, std::vector<double>& v) {
+    std::stringstream ss(s);
+    std::string w;
+    v.clear();
+    while (std::getline(ss, w, ',')) {
+        char* end;
+        const double x = strtod(w.c_str(), &end);
+        if (w.empty() || *end != '\0' || !(x >= 0.0 && x <= 1.0)) return false;
+        v.push_back(x);
+    }
+    return !v.empty();
+}
+
 double haldane(double m) { return 0.5 * (1.0 - std::exp(-2.0 * m)); }
 double inverse_haldane(double r) { return -0.5 * std::log(1 - (2 * r)); }
 
@@ -402,6 +425,10 @@ void usage(const char* prog) {
             "  -q NUM    --peelseqiter=NUM         (accepted; the peel sequence search is the library's)\n"
             "  -r FILE   --randomseeds=FILE        (the first integer seeds the device streams)\n"
             "  -a        --affectedonly, -v --verbose, -h --help\n"
+            "  -M        --mcmcmc                  (MC3: -z tempered chains per run, exchanges every -y iterations)\n"
+            "  -z NUM    --chains=NUM              (default = 1)\n"
+            "  -y NUM    --exchangeperiod=NUM      (default = 10)\n"
+            "  -t LIST   --temperatures=LIST       (comma separated, the first 1.0; default 1 / (1 + 0.001 2^i))\n"
             "  -E        --exact                   (FP64 samplers and LOD, the reference's arithmetic)\n"
             "  -D FILE   --dumpproblem=FILE        (write the problem tables of every family and stop)\n",
             prog);
@@ -433,9 +460,13 @@ int main(int argc, char** argv) {
         {"sexlinked", no_argument, 0, 'X'},       {"elod", no_argument, 0, 'e'},
         {"verbose", no_argument, 0, 'v'},         {"help", no_argument, 0, 'h'},
         {"exact", no_argument, 0, 'E'},           {"dumpproblem", required_argument, 0, 'D'},
+        {"mcmcmc", no_argument, 0, 'M'},          {"chains", required_argument, 0, 'z'},
+        {"exchangeperiod", required_argument, 0, 'y'}, {"temperatures", required_argument, 0, 't'},
+        {"frequency", required_argument, 0, 'f'}, {"penetrance", required_argument, 0, 'k'},
+        {"replicates", required_argument, 0, 'u'}, {"separation", required_argument, 0, 'w'},
         {0, 0, 0, 0}};
     int ch, ignored;
-    while ((ch = getopt_long(argc, argv, "p:m:d:o:i:b:s:x:l:n:R:TP:c:gq:r:aXevhED:", longopts, nullptr)) != -1) {
+    while ((ch = getopt_long(argc, argv, "p:m:d:o:i:b:s:x:l:n:R:TP:c:gq:r:aXevhED:Mz:y:t:f:k:u:w:", longopts, nullptr)) != -1) {
         switch (ch) {
             case 'p': o.ped = optarg; break;
             case 'm': o.map = optarg; break;
@@ -459,12 +490,28 @@ int main(int argc, char** argv) {
             case 'v': o.verbose = true; break;
             case 'E': o.exact = true; break;
             case 'D': o.dump = optarg; break;
+            case 'M': o.mc3 = true; break;
+            case 'z': if (!to_int(optarg, o.chains) || o.chains < 1) { fprintf(stderr, "option '-z' requires an int > 0\n"); return 1; } break;
+            case 'y': if (!to_int(optarg, o.exchange) || o.exchange < 1) { fprintf(stderr, "option '-y' requires an int > 0\n"); return 1; } break;
+            case 't':
+                if (!csv_doubles(optarg, o.temps)) {
+                    fprintf(stderr, "temperatures must be comma delimited floats from 0.0 - 1.0 inclusive, e.g.: 1.0,0.9,0.8,0.7\n");
+                    return 1;
+                }
+                break;
+            case 'f': case 'k': case 'u': case 'w':
+                fprintf(stderr, "error: ELOD is not part of this program\n");
+                return 1;
             case 'h': usage(argv[0]); return 0;
             default: usage(argv[0]); return 1;
         }
     }
     if (o.ped.empty() || o.map.empty() || o.dat.empty()) {
         usage(argv[0]);
+        return 1;
+    }
+    if (o.mc3 && !o.temps.empty() && ((int)o.temps.size() != o.chains || o.temps[0] != 1.0)) {
+        fprintf(stderr, "error: -t needs one temperature per chain (-z), the first 1.0\n");
         return 1;
     }
     if (o.iterations < 1 || o.burnin < 0 || o.period < 1 || o.lods < 1 || o.runs < 1 || o.si < 0 ||
@@ -513,9 +560,22 @@ int main(int argc, char** argv) {
     for (size_t f = 0; f < fams.size(); ++f)
         if (!build_family(fams[f], model, map, o.affected_only, probs[f])) return 1;
     if (!o.dump.empty()) return dump_problems(o.dump, fams, probs, map, model, theta, partial) ? 0 : 1;
+    // Contexts: without MC3 one per family holding its -R runs as chains; with MC3
+    // one per (family, run) holding the -z tempered chains, chain 0 at t = 1.
+    struct Unit {
+        size_t fam;
+        int run;
+        sl_ctx* ctx;
+    };
+    std::vector<Unit> units;
     std::vector<sl_ctx*> ctxs;
+    const int per_ctx = o.mc3 ? o.chains : o.runs;
+    std::vector<double> temps(per_ctx, 1.0);
+    if (o.mc3)
+        for (int i = 0; i < o.chains; ++i)   // Mc3::_init (mc3.cc:30-44)
+            temps[i] = !o.temps.empty() ? o.temps[i] : (i == 0 ? 1.0 : 1.0 / (1.0 + (0.001 * std::pow(2.0, i))));
     int rc = 0;
-    for (size_t f = 0; f < fams.size(); ++f) {
+    for (size_t f = 0; f < fams.size() && !rc; ++f) {
         Problem& p = probs[f];
         sl_problem_desc d{};
         d.n_members = p.N;
@@ -541,26 +601,36 @@ int main(int argc, char** argv) {
         d.children_off = p.ch_off.data();
         d.children = p.ch.data();
         sl_options so{};
-        so.n_chains = o.runs;
+        so.n_chains = per_ctx;
         so.lod_precision = o.exact ? SL_LOD_FP64 : SL_LOD_FP32_RESCALED;
         so.sampler_precision = o.exact ? SL_SAMPLER_EXACT : SL_SAMPLER_FAST;
         so.lod_flags = SL_LOD_ZERO_OK;
-        sl_ctx* ctx = nullptr;
-        if (sl_create(&d, &so, &ctx) != SL_OK) {
-            fprintf(stderr, "error: pedigree '%s': %s\n", fams[f].id.c_str(), sl_last_error(nullptr));
-            rc = 1;
-            break;
+        for (int r = 0; r < (o.mc3 ? o.runs : 1) && !rc; ++r) {
+            sl_ctx* ctx = nullptr;
+            if (sl_create(&d, &so, &ctx) != SL_OK) {
+                fprintf(stderr, "error: pedigree '%s': %s\n", fams[f].id.c_str(), sl_last_error(nullptr));
+                rc = 1;
+                break;
+            }
+            const uint64_t si_seed = seed + ctxs.size();
+            ctxs.push_back(ctx);
+            units.push_back({f, r, ctx});
+            if (o.mc3 && sl_set_temperatures(ctx, temps.data()) != SL_OK) {
+                fprintf(stderr, "error: pedigree '%s': %s\n", fams[f].id.c_str(), sl_last_error(ctx));
+                rc = 1;
+                break;
+            }
+            // sequential imputation (LinkageProgram::run_pedigree): every chain starts from its best pass
+            std::vector<double> best(per_ctx);
+            if (sl_sequential_imputation_run(ctx, std::max(1, o.si), si_seed, best.data()) != SL_OK) {
+                fprintf(stderr, "error: pedigree '%s': %s\n", fams[f].id.c_str(), sl_last_error(ctx));
+                rc = 1;
+                break;
+            }
+            if (r == 0)
+                fprintf(stderr, "pedigree %s: %d members, starting likelihood (log10) = %.3f\n", fams[f].id.c_str(),
+                        p.N, best[0] / std::log(10.0));
         }
-        ctxs.push_back(ctx);
-        // sequential imputation (LinkageProgram::run_pedigree): every run's chain starts from its best pass
-        std::vector<double> best(o.runs);
-        if (sl_sequential_imputation_run(ctx, std::max(1, o.si), seed + f, best.data()) != SL_OK) {
-            fprintf(stderr, "error: pedigree '%s': %s\n", fams[f].id.c_str(), sl_last_error(ctx));
-            rc = 1;
-            break;
-        }
-        fprintf(stderr, "pedigree %s: %d members, starting likelihood (log10) = %.3f\n", fams[f].id.c_str(), p.N,
-                best[0] / std::log(10.0));
     }
     // the MCMC of every pedigree in one batch (with -T: one scoring period at a time, tracing in between)
     if (!rc) {
@@ -569,14 +639,28 @@ int main(int argc, char** argv) {
             fprintf(stderr, "error: %s\n", sl_last_error(nullptr));
             rc = 1;
         } else {
-            std::vector<FILE*> traces;
+            // trace targets: run r of family f is chain r of the family's context, or chain 0 (t = 1)
+            // of its own context under MC3
+            struct Trace {
+                sl_ctx* ctx;
+                int chain;
+                FILE* fh;
+            };
+            std::vector<Trace> traces;
             if (o.trace)
-                for (size_t f = 0; f < fams.size(); ++f)
-                    for (int r = 0; r < o.runs; ++r) {
-                        const std::string fn = o.trace_prefix + ".ped" + fams[f].id + ".run" + std::to_string(r);
+                for (const Unit& u : units)
+                    for (int r = 0; r < (o.mc3 ? 1 : o.runs); ++r) {
+                        const int run = o.mc3 ? u.run : r;
+                        const std::string fn = o.trace_prefix + ".ped" + fams[u.fam].id + ".run" + std::to_string(run);
                         FILE* fh = fopen(fn.c_str(), "w");
-                        if (fh) fprintf(fh, "iteration likelihood\n");
-                        traces.push_back(fh);
+                        if (!fh) {
+                            fprintf(stderr, "error: could not open trace file '%s'\n", fn.c_str());
+                            rc = 1;
+                            break;
+                        }
+                        fprintf(fh, "iteration likelihood\n");
+                        fprintf(stderr, "opened trace file (%s)\n", fn.c_str());
+                        traces.push_back({u.ctx, o.mc3 ? 0 : r, fh});
                     }
             const int total = o.burnin + o.iterations;
             for (int it = 0, it1; it < total && !rc; it = it1) {
@@ -595,6 +679,7 @@ int main(int argc, char** argv) {
                 ro.first_iteration = it;
                 ro.lsampler_prob = o.lprob;
                 ro.seed = seed;
+                ro.exchange_period = o.mc3 && o.chains > 1 ? o.exchange : 0;
                 if (it1 <= o.burnin) {
                     ro.iterations = 0;
                     ro.burnin = it1;
@@ -606,28 +691,48 @@ int main(int argc, char** argv) {
                 }
                 const int last = it1 - 1;
                 if (o.trace && last >= o.burnin && last % o.period == 0)
-                    for (size_t f = 0; f < ctxs.size(); ++f)
-                        for (int r = 0; r < o.runs; ++r) {
-                            double ll = 0.0;
-                            if (sl_chain_loglik(ctxs[f], r, r, &ll) == SL_OK && traces[f * o.runs + r])
-                                fprintf(traces[f * o.runs + r], "%d\t%f\n", last + 1, ll);
+                    for (const Trace& t : traces) {
+                        double ll = 0.0;
+                        if (sl_chain_loglik(t.ctx, t.chain, t.chain, &ll) != SL_OK) {
+                            fprintf(stderr, "error: %s\n", sl_last_error(t.ctx));
+                            rc = 1;
+                            break;
                         }
+                        fprintf(t.fh, "%d\t%f\n", last + 1, ll);
+                    }
             }
-            for (FILE* fh : traces)
-                if (fh) fclose(fh);
+            for (const Trace& t : traces) fclose(t.fh);
+            if (o.mc3 && o.verbose && !rc)
+                for (const Unit& u : units) {
+                    std::vector<int64_t> acc(std::max(1, o.chains - 1)), prop(acc.size());
+                    if (o.chains > 1 && sl_mc3_stats(u.ctx, acc.data(), prop.data()) == SL_OK)
+                        for (int c = 0; c + 1 < o.chains; ++c)
+                            fprintf(stderr, "pedigree %s run %d: exchanges %d <-> %d: %lld of %lld accepted\n",
+                                    fams[u.fam].id.c_str(), u.run, c, c + 1, (long long)acc[c], (long long)prop[c]);
+                }
             sl_batch_destroy(b);
         }
     }
-    // LOD table (LinkageWriter::write): per family (raw - log count - P(T)) / log(10), summed
-    std::vector<std::vector<double>> lod(ctxs.size(), std::vector<double>((size_t)(M - 1) * n));
-    for (size_t f = 0; f < ctxs.size() && !rc; ++f) {
-        std::vector<double> raw((size_t)(M - 1) * n);
-        uint64_t count = 0;
+    // LOD table (LinkageWriter::write): per family (raw - log count - P(T)) / log(10), summed; a family's
+    // runs in separate contexts are merged first (LODscores::merge_results, lod_score.h:98-105)
+    std::vector<std::vector<double>> lod(fams.size(), std::vector<double>((size_t)(M - 1) * n));
+    for (size_t f = 0; f < fams.size() && !rc; ++f) {
+        std::vector<double> raw, r1((size_t)(M - 1) * n);
+        uint64_t count = 0, c1 = 0;
         double tp = 0.0;
-        if (sl_lod_results(ctxs[f], raw.data(), &count, &tp) != SL_OK) {
-            fprintf(stderr, "error: pedigree '%s': %s\n", fams[f].id.c_str(), sl_last_error(ctxs[f]));
-            rc = 1;
-            break;
+        for (const Unit& u : units) {
+            if (u.fam != f) continue;
+            if (sl_lod_results(u.ctx, r1.data(), &c1, &tp) != SL_OK) {
+                fprintf(stderr, "error: pedigree '%s': %s\n", fams[f].id.c_str(), sl_last_error(u.ctx));
+                rc = 1;
+                break;
+            }
+            if (raw.empty()) {
+                raw = r1;
+            } else {
+                for (size_t k = 0; k < raw.size(); ++k) raw[k] = log_sum(raw[k], r1[k]);
+            }
+            count += c1;
         }
         for (size_t k = 0; k < raw.size(); ++k)
             lod[f][k] = (raw[k] - std::log((double)count) - tp) / std::log(10.0);

@@ -138,6 +138,7 @@ struct sl_ctx {
     uint64_t* d_keys = nullptr;       // [C][2] each chain's Philox seed and iteration
     double* d_acc_c = nullptr;        // [C][npos] each chain's LOD log-sums of the run
     uint8_t* d_init_c = nullptr;      // [C][npos]
+    bool chain_tables_pending = false; // chain tables hold scores not yet merged into d_acc
     // trait-peel adjoint (present when the problem carries the disease model)
     bool has_adjoint = false;
     AdjDev adj{};
@@ -1474,7 +1475,7 @@ int sl_msampler_sweep(sl_ctx* ctx, int32_t first, int32_t n_chains, const int32_
     if ((rc = stage_draws(ctx, u, (size_t)n_chains * ucs))) return rc;
     CK(cudaMemcpyAsync(ctx->d_mlist, meioses, sizeof(int32_t) * n_meioses, cudaMemcpyHostToDevice, ctx->stream));
     { Prof pf_(ctx, SL_KERNEL_MSAMPLER);
-      ctx->launches += 2 * n_meioses;
+      ctx->launches += 2 * (int64_t)n_meioses - 1;   // a pair of kernels per meiosis, one counted by Prof
       CK(launch_msampler(P, ctx->d_dg, first, n_chains, ctx->d_mlist, 0, n_meioses, ctx->d_u, ucs, 0, 0, nullptr, 0,
                        ctx->d_raw, ctx->d_raw32, ctx->d_fb, ctx->d_badc, ctx->d_maps, ctx->d_status, ctx->ms_threads,
                        ctx->sampler_precision == SL_SAMPLER_EXACT, ctx->stream));
@@ -1525,9 +1526,23 @@ static int autotune_lod(sl_ctx* ctx, const uint32_t* graphs, int G) {
     return SL_OK;
 }
 
+// Merge the chains' run tables into the context's table, chain by chain in
+// chain order (LODscores::merge_results, lod_score.h:98-105), before the table
+// is read or scored into.
+static int flush_chain_tables(sl_ctx* ctx) {
+    if (!ctx->chain_tables_pending) return SL_OK;
+    const int64_t npos = (int64_t)(ctx->P.M - 1) * ctx->P.n_lod;
+    CK(cudaSetDevice(ctx->device));
+    { Prof pf_(ctx, SL_KERNEL_LOD_MERGE);
+    CK(launch_chain_merge(ctx->d_acc_c, ctx->d_init_c, ctx->n_chains, npos, ctx->d_acc, ctx->d_init, ctx->stream)); }
+    ctx->chain_tables_pending = false;
+    return SL_OK;
+}
+
 static int score_device_graphs(sl_ctx* ctx, const uint32_t* graphs, int G) {
     const ProblemDev& P = ctx->P;
     const int64_t npos = (int64_t)(P.M - 1) * P.n_lod;
+    if (int rc = flush_chain_tables(ctx)) return rc;
     for (int g0 = 0; g0 < G; g0 += ctx->vals_graphs) {
         const int g = std::min(ctx->vals_graphs, G - g0);
         const uint32_t* gr = graphs + (size_t)g0 * P.M * P.W;
@@ -1582,7 +1597,9 @@ int sl_lod_score_graphs(sl_ctx* ctx, int32_t n_graphs, const int32_t* dgs) {
 
 int sl_lod_results(sl_ctx* ctx, double* raw, uint64_t* count, double* trait_prob) {
     if (!ctx) return fail(ctx, SL_EINVAL, "null context");
-    int rc = sl_synchronize(ctx);
+    int rc = flush_chain_tables(ctx);
+    if (rc) return rc;
+    rc = sl_synchronize(ctx);
     if (rc) return rc;
     const int64_t npos = (int64_t)(ctx->P.M - 1) * ctx->P.n_lod;
     if (raw) CK(cudaMemcpy(raw, ctx->d_acc, sizeof(double) * npos, cudaMemcpyDeviceToHost));
@@ -1597,6 +1614,8 @@ int sl_lod_reset(sl_ctx* ctx) {
     CK(cudaSetDevice(ctx->device));
     CK(cudaMemsetAsync(ctx->d_acc, 0, sizeof(double) * npos, ctx->stream));
     CK(cudaMemsetAsync(ctx->d_init, 0, npos, ctx->stream));
+    if (ctx->d_init_c) CK(cudaMemsetAsync(ctx->d_init_c, 0, (size_t)ctx->n_chains * npos, ctx->stream));
+    ctx->chain_tables_pending = false;
     ctx->lod_count = 0;
     return sl_synchronize(ctx);
 }
@@ -2055,9 +2074,10 @@ static cudaError_t capture_run_nodes(sl_ctx* ctx, cudaStream_t s, cudaStream_t s
         whiles.push_back(wn);
         if ((e = capture_chain_body(ctx, c, p.conditional.phGraph_out[0], hw, s1, s2)) != cudaSuccess) return e;
     }
-    e = cudaStreamUpdateCaptureDependencies(s, whiles.data(), nullptr, whiles.size(), cudaStreamSetCaptureDependencies);
-    if (e != cudaSuccess) return e;
-    return launch_chain_merge(ctx->d_acc_c, ctx->d_init_c, C, npos, ctx->d_acc, ctx->d_init, s);
+    // the chains' tables stay apart across launches (merged when results are read), so a
+    // run split over several calls accumulates every chain's scores as one call does
+    return cudaStreamUpdateCaptureDependencies(s, whiles.data(), nullptr, whiles.size(),
+                                               cudaStreamSetCaptureDependencies);
 }
 
 static int build_run_graph(sl_ctx* ctx) {
@@ -2108,7 +2128,6 @@ static int loglik_pairs(sl_ctx* ctx, const int* g, const int* t, int npair, doub
     for (int k = 0; k < npair; ++k) { g4[k] = g[k]; t4[k] = t[k]; }
     { Prof pf_(ctx, SL_KERNEL_OTHER);
     CK(launch_loglik_parts(P, ctx->d_dg, g4, t4, npair, ctx->d_llfag, ctx->d_llrec, ctx->stream)); }
-    ctx->launches += 1;
     std::vector<double> fag((size_t)npair * M), rec((size_t)npair * (M - 1));
     CK(cudaMemcpyAsync(fag.data(), ctx->d_llfag, sizeof(double) * fag.size(), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaMemcpyAsync(rec.data(), ctx->d_llrec, sizeof(double) * rec.size(), cudaMemcpyDeviceToHost, ctx->stream));
@@ -2224,10 +2243,13 @@ static int build_ms_graph(sl_ctx* ctx) {
 static void account_span(sl_ctx* ctx, const sl_run_options* o, int first, int end) {
     const int C = ctx->n_chains, nm = (int)ctx->meioses.size();
     const int cold = scored_chains(ctx);
-    int64_t kernels = 2;   // init, merge
+    int64_t kernels = 1;   // init
     for (int it = first; it < end; ++it) {
         const bool score = it >= o->burnin && it % o->scoring_period == 0;
-        if (score) ctx->lod_count += (uint64_t)cold;
+        if (score) {
+            ctx->lod_count += (uint64_t)cold;
+            ctx->chain_tables_pending = true;
+        }
         for (int c = 0; c < C; ++c) {
             const uint64_t hi = ((uint64_t)c << 40) ^ ((uint64_t)it << 4) ^ 7u;
             const bool is_l = host_philox_u01(o->seed, hi, 0) < o->lsampler_prob;
@@ -2299,12 +2321,16 @@ int sl_run(sl_ctx* ctx, const sl_run_options* o) {
     if (o->first_iteration >= total) return SL_OK;
     if (o->exchange_period == 0 || C < 2) return run_span(ctx, o, o->first_iteration, total);
     // MC3: spurts of exchange_period iterations, each followed by an exchange
-    // (Mc3::run, mc3.cc:117-158; iterations are numbered consecutively)
-    for (int it0 = o->first_iteration; it0 < total; it0 += o->exchange_period) {
-        const int it1 = std::min(total, it0 + o->exchange_period);
+    // (Mc3::run, mc3.cc:117-158; iterations are numbered consecutively).  Spurts
+    // end at multiples of exchange_period counted from iteration 0, so a run
+    // resumed at any first_iteration exchanges where an unbroken run does.
+    const int P = o->exchange_period;
+    for (int it0 = o->first_iteration; it0 < total;) {
+        const int it1 = std::min(total, (it0 / P + 1) * P);
         int rc = run_span(ctx, o, it0, it1);
         if (rc) return rc;
-        if (it1 - it0 == o->exchange_period && (rc = mc3_exchange(ctx, o->seed, it1))) return rc;
+        if (it1 % P == 0 && (rc = mc3_exchange(ctx, o->seed, it1))) return rc;
+        it0 = it1;
     }
     return SL_OK;
 }
@@ -2411,9 +2437,10 @@ int sl_batch_run(sl_batch* b, const sl_run_options* o) {
         if (rc) return rc;
     }
     const int total = o->burnin + o->iterations;
-    const int period = o->exchange_period > 0 ? o->exchange_period : std::max(1, total - o->first_iteration);
-    for (int it0 = o->first_iteration; it0 < total; it0 += period) {
-        const int it1 = std::min(total, it0 + period);
+    const int P = o->exchange_period;
+    for (int it0 = o->first_iteration, it1; it0 < total; it0 = it1) {
+        // spurts end at multiples of the exchange period counted from iteration 0 (as in sl_run)
+        it1 = P > 0 ? std::min(total, (it0 / P + 1) * P) : total;
         for (size_t j = 0; j < b->ctxs.size(); ++j) {
             sl_ctx* c = b->ctxs[j];
             const RunParams rp{it0, it1, o->burnin, o->scoring_period, o->lsampler_prob, o->seed};
@@ -2429,7 +2456,7 @@ int sl_batch_run(sl_batch* b, const sl_run_options* o) {
                 return fail(c, SL_ECUDA, "ordering the context after the batch");
             account_span(c, o, it0, it1);
         }
-        if (o->exchange_period > 0 && it1 - it0 == o->exchange_period)
+        if (P > 0 && it1 % P == 0)
             for (sl_ctx* c : b->ctxs)
                 if (c->n_chains > 1) {
                     int rc = mc3_exchange(c, o->seed, it1);

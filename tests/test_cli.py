@@ -7,8 +7,10 @@ files: member order, parents, genotypes, disease probabilities, theta,
 partial theta, MAFs, positions), families of one pedigree file kept apart,
 and the input errors it reports.  GPU: the LOD table it writes against the
 library driven through the Python API with the same problem, seeds and run
-options; the CODA trace lines (MarkovChain::run, markov_chain.cc:357-370);
-a traced run's table is the untraced run's table.
+options, with and without MC3 (one context of tempered chains per run, the
+runs' tables merged as LODscores::merge_results does); the CODA trace lines
+(MarkovChain::run, markov_chain.cc:357-370); a traced run's table is the
+untraced run's table, also when MC3 exchanges fall inside traced spans.
 """
 import os
 import subprocess
@@ -210,10 +212,13 @@ def test_lod_table_matches_the_library(tmp_path, exact):
 
 
 @pytest.mark.gpu
-def test_trace_lines_and_the_table_do_not_depend_on_tracing(tmp_path):
+@pytest.mark.parametrize("mc3", [False, True])
+def test_trace_lines_and_the_table_do_not_depend_on_tracing(tmp_path, mc3):
     ped, mapf, dat = synth.workload_files(1, str(tmp_path))
     seedf = _write(tmp_path / "seeds", "5\n")
     common = ["-p", ped, "-m", mapf, "-d", dat, "-R", 2, "-s", 10, "-i", 45, "-b", 20, "-x", 10, "-r", seedf, "-E"]
+    if mc3:   # exchanges every 7 iterations: not aligned with the traced spans
+        common += ["-M", "-z", 3, "-y", 7]
     run_cli(*common, "-o", tmp_path / "plain.out")
     run_cli(*common, "-o", tmp_path / "traced.out", "-T", "-P", tmp_path / "tr")
     assert (tmp_path / "plain.out").read_text() == (tmp_path / "traced.out").read_text()
@@ -225,3 +230,48 @@ def test_trace_lines_and_the_table_do_not_depend_on_tracing(tmp_path):
         assert its == [21, 31, 41, 51, 61]
         ll = np.array([float(x.split("\t")[1]) for x in lines[1:]])
         assert np.all(np.isfinite(ll)) and np.all(ll < 0)
+
+
+def log_sum(a, b):
+    """log_sum (logarithms.cc:14-25) elementwise, LOG_ZERO = -DBL_MAX."""
+    lz = -np.finfo(np.float64).max
+    return np.where(a == lz, b, np.where(b == lz, a, np.log(np.exp(b - a) + 1) + a))
+
+
+@pytest.mark.gpu
+def test_mc3_runs_match_the_library(tmp_path):
+    ped, mapf, dat = synth.workload_files(1, str(tmp_path))
+    (d,) = dump(tmp_path, ped, mapf, dat)
+    seed, R, Z, Y = 31, 2, 3, 5
+    seedf = _write(tmp_path / "seeds", f"{seed}\n")
+    out = tmp_path / "mc3.out"
+    run_cli("-p", ped, "-m", mapf, "-d", dat, "-o", out, "-R", R, "-s", 10, "-i", 200, "-b", 50, "-x", 10,
+            "-r", seedf, "-E", "-M", "-z", Z, "-y", Y, "-v")
+    t = cli.read_lod_table(str(out))
+    temps = [1.0] + [1.0 / (1.0 + 0.001 * 2.0 ** i) for i in range(1, Z)]
+    ot, op, cut, prev, ch = api.peel_sequence(d["mother"].astype(np.int32), d["father"].astype(np.int32))
+    arrays = dict(N=d["N"], F=d["F"], M=d["M"], n_lod=5, mother=d["mother"].astype(np.int32),
+                  father=d["father"].astype(np.int32), sex=d["sex"].astype(np.int32),
+                  typed=d["typed"].astype(np.uint8), genotypes=d["genotypes"].astype(np.uint8),
+                  disease_prob=d["disease_prob"], theta=d["theta"], partial=d["partial"], minor=d["minor"],
+                  op_type=ot, op_peel=op, op_cutset=cut, op_prev=prev, op_children=ch)
+    ctxs = []
+    for r in range(R):
+        c = api.Context(api.Problem.from_arrays(arrays, with_legal=False), n_chains=Z,
+                        lod_precision=api.SL_LOD_FP64, sampler_precision=api.SL_SAMPLER_EXACT,
+                        lod_flags=api.SL_LOD_ZERO_OK)
+        c.set_temperatures(temps)
+        c.sequential_imputation_run(10, seed + r)
+        ctxs.append(c)
+    b = api.Batch(ctxs)
+    b.run(iterations=200, burnin=50, period=10, lprob=0.5, seed=seed, exchange_period=Y)
+    res = [c.lod_results() for c in ctxs]
+    stats = [c.mc3_stats() for c in ctxs]
+    b.close()
+    for c in ctxs:
+        c.close()
+    raw = log_sum(res[0][0], res[1][0])
+    lod = api.lod_table(raw, res[0][1] + res[1][1], res[0][2])
+    check_table(t, [d], [lod], 2e-6)
+    # one exchange proposed per full spurt of Y iterations in each run
+    assert all(int(p.sum()) == 250 // Y for _, p in stats)

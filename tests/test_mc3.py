@@ -170,3 +170,34 @@ def test_temperatures_are_validated():
             ctx.set_temperatures([1.0, 0.0])
         with pytest.raises(api.SwiftLinkError):
             ctx.set_temperatures([1.0, 1.5])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("batched", [False, True])
+def test_split_run_exchanges_as_one_run(batched):
+    """Exchanges follow multiples of the exchange period counted from iteration
+    0, so a run resumed at any first_iteration is the unbroken run."""
+    g = load_golden("cfg1")
+    C, seed, iters, burnin, period, exchange = len(TEMPS), 91, 20, 4, 2, 3
+    outs = []
+    for splits in ([], [5, 11, 12]):
+        with api.Context(api.Problem.from_arrays(g), n_chains=C) as ctx:
+            ctx.set_temperatures(TEMPS)
+            ctx.set_graphs(np.stack([g["dg0"]] * C))
+            runner = api.Batch([ctx]) if batched else ctx
+            total = iters + burnin
+            bounds = [0] + splits + [total]
+            for a, b in zip(bounds[:-1], bounds[1:]):
+                runner.run(iterations=b - burnin if b > burnin else 0, burnin=burnin if b > burnin else b,
+                           period=period, lprob=0.5, seed=seed, first_iteration=a, exchange_period=exchange)
+            ctx.synchronize()
+            outs.append((ctx.get_graphs(), ctx.lod_results(), ctx.mc3_stats()))
+            if batched:
+                runner.close()
+    (g0, l0, s0), (g1, l1, s1) = outs
+    assert np.array_equal(g0, g1)
+    np.testing.assert_array_equal(l0[0], l1[0])
+    assert l0[1] == l1[1] and l0[2] == l1[2]
+    np.testing.assert_array_equal(s0[0], s1[0])
+    np.testing.assert_array_equal(s0[1], s1[1])
+    assert s0[1].sum() == total // exchange
