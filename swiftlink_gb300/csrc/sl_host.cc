@@ -33,7 +33,7 @@ cudaError_t launch_msampler(const ProblemDev& P, uint32_t* dg, int first, int nc
                             int64_t mstride, int nm, const double* u, int64_t ucs, uint64_t seed, uint64_t iter,
                             const uint8_t* sel, int want, double* raw64, float* raw32, void* fb, uint8_t* badc,
                             uint8_t* maps, int* status, int fag_threads, int exact, cudaStream_t s,
-                            const uint64_t* key = nullptr);
+                            const uint64_t* key = nullptr, double* ubuf = nullptr);
 cudaError_t launch_set_key(uint64_t* key, uint64_t seed, uint64_t iter, cudaStream_t s);
 cudaError_t launch_si(const ProblemDev& P, uint32_t* dg, int first, int nchain, const int32_t* starts,
                       const double* u, int64_t ucs, uint64_t seed, uint64_t pass, double* weights, int* status,
@@ -120,6 +120,7 @@ struct sl_ctx {
     double* d_fb = nullptr;
     uint8_t* d_badc = nullptr;
     uint8_t* d_maps = nullptr;       // [C][M] backward decision maps of the fast filter
+    double* d_mu = nullptr;          // [C][M] the fast M-step's draws by index
     int* d_status = nullptr;
     uint8_t* d_sel = nullptr;
     uint32_t* h_stage = nullptr;     // pinned staging for packed descent graphs
@@ -174,6 +175,10 @@ cudaEvent_t take_event(sl_ctx* c) {
     return e;
 }
 // Bracket one launch with events when profiling is on.
+// Kernels one M-sweep of nm meioses launches for a chain: a reset, then per
+// meiosis a likelihood and a filter kernel.
+static int64_t msweep_kernels(const sl_ctx*, int nm) { return 1 + 2 * (int64_t)nm; }
+
 struct Prof {
     sl_ctx* c;
     int kernel;
@@ -1198,6 +1203,7 @@ int sl_create(const sl_problem_desc* d, const sl_options* opt, sl_ctx** out) {
     if ((rc = dev_alloc(ctx, &ctx->d_raw32, (size_t)C * 2 * M))) return bail(rc);
     if ((rc = dev_alloc(ctx, &ctx->d_badc, C))) return bail(rc);
     if ((rc = dev_alloc(ctx, &ctx->d_maps, (size_t)C * M))) return bail(rc);
+    if ((rc = dev_alloc(ctx, &ctx->d_mu, (size_t)C * M))) return bail(rc);
     CK(cudaMemset(ctx->d_badc, 0, C));
     if ((rc = dev_alloc(ctx, &ctx->d_status, 1))) return bail(rc);
     if ((rc = dev_alloc(ctx, &ctx->d_sel, C))) return bail(rc);
@@ -1475,10 +1481,10 @@ int sl_msampler_sweep(sl_ctx* ctx, int32_t first, int32_t n_chains, const int32_
     if ((rc = stage_draws(ctx, u, (size_t)n_chains * ucs))) return rc;
     CK(cudaMemcpyAsync(ctx->d_mlist, meioses, sizeof(int32_t) * n_meioses, cudaMemcpyHostToDevice, ctx->stream));
     { Prof pf_(ctx, SL_KERNEL_MSAMPLER);
-      ctx->launches += 2 * (int64_t)n_meioses - 1;   // a pair of kernels per meiosis, one counted by Prof
+      ctx->launches += msweep_kernels(ctx, n_meioses) - 1;   // one counted by Prof
       CK(launch_msampler(P, ctx->d_dg, first, n_chains, ctx->d_mlist, 0, n_meioses, ctx->d_u, ucs, 0, 0, nullptr, 0,
                        ctx->d_raw, ctx->d_raw32, ctx->d_fb, ctx->d_badc, ctx->d_maps, ctx->d_status, ctx->ms_threads,
-                       ctx->sampler_precision == SL_SAMPLER_EXACT, ctx->stream));
+                       ctx->sampler_precision == SL_SAMPLER_EXACT, ctx->stream, nullptr, ctx->d_mu));
     }
     return sl_synchronize(ctx);
 }
@@ -1966,7 +1972,7 @@ static cudaError_t capture_chain_body(sl_ctx* ctx, int c, cudaGraph_t body, cuda
     void* fb = exact ? (void*)((double*)ctx->d_fb + (size_t)c * 2 * M) : (void*)((float*)ctx->d_fb + (size_t)c * 2 * M);
     e = launch_msampler(P, ctx->d_dg, c, 1, ctx->d_morder + (size_t)c * nm, nm, nm, nullptr, 0, 0, 0, nullptr, 0, raw,
                         ctx->d_raw32 + (size_t)c * 2 * M, fb, ctx->d_badc + c, ctx->d_maps + (size_t)c * M,
-                        ctx->d_status, ctx->ms_threads, exact ? 1 : 0, s2, key);
+                        ctx->d_status, ctx->ms_threads, exact ? 1 : 0, s2, key, ctx->d_mu + (size_t)c * M);
     e2 = cudaStreamEndCapture(s2, &sw[1]);
     if (e != cudaSuccess || (e = e2) != cudaSuccess) return e;
     // scoring of chain c into its own table
@@ -2012,7 +2018,7 @@ static int prepare_run_graph(sl_ctx* ctx) {
     CK(cudaMemsetAsync(ctx->d_sel, 0, (size_t)C, ctx->stream));
     CK(launch_msampler(P, ctx->d_dg, 0, C, ctx->d_morder, nm, 0, nullptr, 0, 0, 0, ctx->d_sel, 2, ctx->d_raw,
                        ctx->d_raw32, ctx->d_fb, ctx->d_badc, ctx->d_maps, ctx->d_status, ctx->ms_threads, exact ? 1 : 0,
-                       ctx->stream, ctx->d_keys));
+                       ctx->stream, ctx->d_keys, ctx->d_mu));
     CK(launch_lsampler(P, ctx->d_dg, 0, C, ctx->d_even, (int)ctx->even.size(), nullptr, 0, 0, 0, 0, ctx->d_sel, 2,
                        ctx->d_status, ctx->stream, ctx->ls_grid, ctx->ls_wpb, ctx->d_keys));
     // the scoring kernel is fixed in the graph: time the candidates now if needed
@@ -2197,7 +2203,7 @@ static int build_ms_graph(sl_ctx* ctx) {
     CK(launch_set_key(ctx->d_key, 0, 0, ctx->stream));
     CK(launch_msampler(P, ctx->d_dg, 0, C, ctx->d_morder, nm, 0, nullptr, 0, 0, 0, ctx->d_sel, 2, ctx->d_raw,
                        ctx->d_raw32, ctx->d_fb, ctx->d_badc, ctx->d_maps, ctx->d_status, ctx->ms_threads, exact ? 1 : 0,
-                       ctx->stream, ctx->d_key));
+                       ctx->stream, ctx->d_key, ctx->d_mu));
     CK(cudaStreamSynchronize(ctx->stream));
     while ((int)ctx->cap_streams.size() < C + 1) {
         cudaStream_t st;
@@ -2219,7 +2225,7 @@ static int build_ms_graph(sl_ctx* ctx) {
         err = launch_msampler(P, ctx->d_dg, c, 1, ctx->d_morder + (size_t)c * nm, nm, nm, nullptr, 0, 0, 0,
                               ctx->d_sel + c, 0, raw, ctx->d_raw32 + (size_t)c * 2 * M, fb, ctx->d_badc + c,
                               ctx->d_maps + (size_t)c * M, ctx->d_status, ctx->ms_threads, exact ? 1 : 0, sc,
-                              ctx->d_key);
+                              ctx->d_key, ctx->d_mu + (size_t)c * M);
         if (err != cudaSuccess) break;
         err = cudaEventRecord(ctx->cap_events[c], sc);
         if (err != cudaSuccess) break;
@@ -2234,7 +2240,7 @@ static int build_ms_graph(sl_ctx* ctx) {
         ctx->ms_graph = nullptr;
         return fail(ctx, SL_ECUDA, "capturing the M-sweep graph: %s", cudaGetErrorString(err));
     }
-    ctx->ms_graph_kernels = (int64_t)C * (2 * nm + 1);
+    ctx->ms_graph_kernels = (int64_t)C * msweep_kernels(ctx, nm);
     return SL_OK;
 }
 
@@ -2253,7 +2259,7 @@ static void account_span(sl_ctx* ctx, const sl_run_options* o, int first, int en
         for (int c = 0; c < C; ++c) {
             const uint64_t hi = ((uint64_t)c << 40) ^ ((uint64_t)it << 4) ^ 7u;
             const bool is_l = host_philox_u01(o->seed, hi, 0) < o->lsampler_prob;
-            kernels += 2 + (is_l ? 2 : 2 * (int64_t)nm + 1) + (score && ctx->temps[c] == 1.0 ? 2 : 0);
+            kernels += 2 + (is_l ? 2 : msweep_kernels(ctx, nm)) + (score && ctx->temps[c] == 1.0 ? 2 : 0);
         }
     }
     ctx->launches += kernels;

@@ -937,69 +937,104 @@ __global__ void __launch_bounds__(128) fag_kernel(ProblemDev P, uint32_t* dg, in
 // ---------------------------------------------------------------------------
 constexpr int kFagWarpsPerBlock = 8;
 
-__host__ __device__ inline size_t fagw_tables(int N) { return ((size_t)N * 7 + 15) & ~(size_t)15; }
+__host__ __device__ inline size_t fagw_tables(int N) {
+    return (((size_t)N * 7 + 15) & ~(size_t)15) + (((size_t)4 * (N + 1) + 15) & ~(size_t)15);
+}
 __host__ __device__ inline size_t fagw_warp_bytes(int N, int F) {
     return (((size_t)4 * N + 15) & ~(size_t)15) + (size_t)2 * F * 12 + (size_t)4 * N;
 }
 size_t fagw_block_bytes(int N, int F) { return fagw_tables(N) + kFagWarpsPerBlock * fagw_warp_bytes(N, F); }
 
-__global__ void __launch_bounds__(kFagWarpsPerBlock * 32) fag_warp_kernel(ProblemDev P, uint32_t* dg, int first,
-                                                                         int nchain, const int32_t* order,
-                                                                         int64_t ostride, int step, const uint8_t* sel,
-                                                                         int want, float* rawbuf, float* raw32,
-                                                                         uint8_t* badc, int* status) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    const int N = P.N, F = P.F, nfa = 2 * F, M = P.M;
-    int16_t* s_lvl = (int16_t*)smem;
-    int16_t* s_mo = s_lvl + N;
-    int16_t* s_fa = s_mo + N;
-    uint8_t* s_typed = (uint8_t*)(s_fa + N);
+// The tables every warp of a block shares, loaded into the block's shared memory.
+struct FagwTables {
+    int16_t* lvl;
+    int16_t* mo;
+    int16_t* fa;
+    uint8_t* typed;
+    int32_t* lvl_off;   // [n_lvl + 1]
+};
+
+__device__ FagwTables fagw_load_tables(const ProblemDev& P, unsigned char* smem) {
+    const int N = P.N;
+    FagwTables t;
+    t.lvl = (int16_t*)smem;
+    t.mo = t.lvl + N;
+    t.fa = t.mo + N;
+    t.typed = (uint8_t*)(t.fa + N);
+    t.lvl_off = (int32_t*)(smem + (((size_t)N * 7 + 15) & ~(size_t)15));
     for (int i = threadIdx.x; i < N; i += blockDim.x) {
-        s_lvl[i] = P.lvl_order[i];
-        s_mo[i] = P.mother[i];
-        s_fa[i] = P.father[i];
-        s_typed[i] = P.typed[i];
+        t.lvl[i] = P.lvl_order[i];
+        t.mo[i] = P.mother[i];
+        t.fa[i] = P.father[i];
+        t.typed[i] = P.typed[i];
     }
-    __syncthreads();
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, wpb = blockDim.x >> 5;
-    unsigned char* wbase = smem + fagw_tables(N) + (size_t)warp * fagw_warp_bytes(N, F);
+    for (int i = threadIdx.x; i <= P.n_lvl; i += blockDim.x) t.lvl_off[i] = P.lvl_off[i];
+    return t;
+}
+
+// One (chain, locus) task by one warp: step < 0 stores the likelihood of the
+// column at meiosis order[0]; step >= 0 the likelihoods at both values of
+// meiosis order[step] (the kept one from the previous step).
+__device__ __forceinline__ void fagw_task(const ProblemDev& P, const FagwTables& tab, unsigned char* wbase, const uint32_t* dg,
+                          int chain, int cr, int l, const int32_t* ord, int step, float* rawbuf, float* raw32,
+                          uint8_t* badc, int* status) {
+    const int N = P.N, F = P.F, nfa = 2 * F, M = P.M;
+    const int lane = threadIdx.x & 31;
+    const int16_t* s_lvl = tab.lvl;
+    const int16_t* s_mo = tab.mo;
+    const int16_t* s_fa = tab.fa;
     uint16_t* e = (uint16_t*)wbase;                                   // [2N] founder allele of each allele
     volatile int* Lb = (volatile int*)(wbase + (((size_t)4 * N + 15) & ~(size_t)15));   // [2F] 2 * label + parity
     int* fl = (int*)(Lb + nfa);                                       // [2F] bit0 used, bit1 fixed A, bit2 fixed B
     int* cnt = fl + nfa;                                              // [2F] per component: counts, forbidden colourings
     uint32_t* hed = (uint32_t*)(cnt + nfa);                           // [N] heterozygote edges, u | v << 16
-    const int64_t ntask = (int64_t)nchain * M;
-    for (int64_t t = (int64_t)blockIdx.x * wpb + warp; t < ntask; t += (int64_t)gridDim.x * wpb) {
-        const int cr = (int)(t / M);
-        const int l = (int)(t % M);
-        if (sel && sel[cr] != want) continue;
-        const int chain = first + cr;
+    const int32_t* s_off = tab.lvl_off;
+    {
         const uint32_t* col = dg + ((size_t)chain * M + l) * P.W;
-        const int32_t* ord = order + cr * ostride;
         float* raw = rawbuf + (size_t)cr * 2 * M;
         const uint8_t* gcol = P.geno + (size_t)l * N;
+        // the task's global reads issued together: the column's words (lane w
+        // holds word w, read by shuffles), the genotype codes of this lane's
+        // members (16 x 2 bits; untyped members read as 0), the minor-allele
+        // frequency
+        const bool wreg = P.W <= 32;
+        const uint32_t cw = wreg && lane < P.W ? col[lane] : 0u;
+        uint32_t gpack = 0u;
+#pragma unroll
+        for (int k = 0; k < 16; ++k)
+            if (k * 32 + lane < N) gpack |= (uint32_t)(gcol[k * 32 + lane] & 3) << (2 * k);
+        const double minor_d = P.c_minor[(size_t)chain * M + l];
+        auto cbit = [&](int b) -> int {
+            const uint32_t w = wreg ? __shfl_sync(FULLMASK, cw, b >> 5) : col[b >> 5];
+            return (int)((w >> (b & 31)) & 1u);
+        };
         int flip = -1, tb = 0;
         float keep = 0.f;
         if (step >= 0) {
             const int m = ord[step];
             const int last = ord[step > 0 ? step - 1 : 0];
-            tb = dgbit(col, m);
-            keep = raw[2 * l + dgbit(col, last)];
+            tb = cbit(m);
+            keep = raw[2 * l + cbit(last)];
             flip = m;
         }
         // 1. founder alleles, one generation level at a time
-        for (int q = lane; q < P.lvl_off[1]; q += 32) {
+        for (int q = lane; q < s_off[1]; q += 32) {
             const int pid = s_lvl[q];
             e[2 * pid] = (uint16_t)(2 * pid);
             e[2 * pid + 1] = (uint16_t)(2 * pid + 1);
         }
         __syncwarp();
         for (int k = 1; k < P.n_lvl; ++k) {
-            for (int q = P.lvl_off[k] + lane; q < P.lvl_off[k + 1]; q += 32) {
-                const int pid = s_lvl[q];
+            // every lane takes part in the shuffles, members or not
+            for (int q0 = s_off[k]; q0 < s_off[k + 1]; q0 += 32) {
+                const int q = q0 + lane;
+                const bool act = q < s_off[k + 1];
+                const int pid = act ? s_lvl[q] : F;
                 const int b = 2 * (pid - F);
-                const int vm = dgbit(col, b) ^ (flip == b);
-                const int vp = dgbit(col, b + 1) ^ (flip == b + 1);
+                const uint32_t w = wreg ? __shfl_sync(FULLMASK, cw, b >> 5) : col[b >> 5];
+                if (!act) continue;
+                const int vm = (int)((w >> (b & 31)) & 1u) ^ (flip == b);
+                const int vp = (int)((w >> ((b + 1) & 31)) & 1u) ^ (flip == b + 1);
                 e[2 * pid] = e[2 * s_mo[pid] + vm];
                 e[2 * pid + 1] = e[2 * s_fa[pid] + vp];
             }
@@ -1013,13 +1048,15 @@ __global__ void __launch_bounds__(kFagWarpsPerBlock * 32) fag_warp_kernel(Proble
         __syncwarp();
         // heterozygote edges are also listed, compacted, for the labelling rounds
         int bad = 0, nhet = 0;
-        for (int base = 0; base < N; base += 32) {
+        for (int base = 0, k = 0; base < N; base += 32, ++k) {
             const int i = base + lane;
             int g = G_UNTYPED, u = 0, v = 0;
-            if (i < N && s_typed[i]) {
-                g = gcol[i] & 3;
-                u = e[2 * i];
-                v = e[2 * i + 1];
+            if (i < N) {
+                g = k < 16 ? (int)((gpack >> (2 * k)) & 3u) : (gcol[i] & 3);
+                if (g != G_UNTYPED) {
+                    u = e[2 * i];
+                    v = e[2 * i + 1];
+                }
             }
             const bool het = g == G_HETERO;
             const unsigned hm = __ballot_sync(FULLMASK, het);
@@ -1095,7 +1132,6 @@ __global__ void __launch_bounds__(kFagWarpsPerBlock * 32) fag_warp_kernel(Proble
                 if (forbid) atomicOr(&cnt[r], forbid);
             }
             __syncwarp();
-            const double minor_d = P.c_minor[(size_t)chain * M + l];
             const float lmaj = log2f((float)(1.0 - minor_d)), lmin = log2f((float)minor_d);
             float sum = 0.f;
             int zero = 0;
@@ -1304,24 +1340,16 @@ __device__ __forceinline__ void mat_mul_left(float& p00, float& p01, float& p10,
 //             parallel; each locus's choice given the locus above is a 2-bit
 //             map, and a suffix composition of the chunks' maps gives each
 //             chunk the state entering it from above.
-__global__ void __launch_bounds__(1024) ffbs_scan_kernel(ProblemDev P, uint32_t* dg, int first, int nchain,
-                                                         const int32_t* order, int64_t ostride, int step,
-                                                         Draws draws, const uint8_t* sel, int want,
-                                                         const uint8_t* badc, const float* raw32, float* fbbuf,
-                                                         uint8_t* mapbuf, int staged) {
-    extern __shared__ __align__(16) unsigned char fsm[];
-    const int cr = blockIdx.x;
-    if (cr >= nchain) return;
-    if (sel && sel[cr] != want) return;
-    if (badc[cr]) return;
+// The body for chain `chain` (relative index cr), meiosis m, run by a whole
+// block.  upre (may be null) holds the step's draws by index, precomputed;
+// with cg, the pairs and draws written by other blocks of the same launch are
+// read past L1.
+__device__ __forceinline__ void ffbs_scan_chain(const ProblemDev& P, uint32_t* dg, int chain, int cr, int m, int step,
+                                const Draws& draws, const double* upre, const float* r, float* fb, uint8_t* maps,
+                                int staged, bool cg, unsigned char* fsm) {
     const int T = blockDim.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = T >> 5;
-    const int chain = first + cr;
-    const int m = order[cr * ostride + step];
     const int M = P.M;
     uint32_t* G = dg + (size_t)chain * M * P.W;
-    const float* r = raw32 + (size_t)cr * 2 * M;
-    float* fb = fbbuf + (size_t)cr * 2 * M;
-    uint8_t* maps = mapbuf + (size_t)cr * M;
     float* th = nullptr;        // theta as floats, [M]
     uint32_t* words = nullptr;  // the meiosis's descent-graph word at each locus, [M]
     ScanScratch sc;
@@ -1338,7 +1366,7 @@ __global__ void __launch_bounds__(1024) ffbs_scan_kernel(ProblemDev P, uint32_t*
         words = (uint32_t*)(th + M);
         uint8_t* smaps = (uint8_t*)(words + M);
         for (int i = tid; i < M; i += T) words[i] = G[(size_t)i * P.W + (m >> 5)];
-        for (int i = tid; i < 2 * M; i += T) sr[i] = r[i];
+        for (int i = tid; i < 2 * M; i += T) sr[i] = cg ? __ldcg(r + i) : r[i];
         for (int i = tid; i < M; i += T) th[i] = i > 0 ? P.c_theta_f[(size_t)chain * (M - 1) + i - 1] : 0.f;
         r = sr;
         fb = sfb;
@@ -1346,12 +1374,14 @@ __global__ void __launch_bounds__(1024) ffbs_scan_kernel(ProblemDev P, uint32_t*
     }
     __syncthreads();
     auto tof = [&](int i) { return th ? th[i] : (i > 0 ? P.c_theta_f[(size_t)chain * (M - 1) + i - 1] : 0.f); };
+    const bool rcg = cg && !staged;   // the pairs still in global memory, written by other blocks
+    auto rq = [&](int i) { return rcg ? __ldcg(r + i) : r[i]; };
     const int L = (M + T - 1) / T;
     const int s0 = min(M, tid * L), s1 = min(M, s0 + L);
     // chunk product P = A_{s1-1} ... A_{s0} (A_0 = diag(r_0)); an empty chunk is the identity
     float p00 = 1.f, p01 = 0.f, p10 = 0.f, p11 = 1.f;
     for (int i = s0; i < s1; ++i) {
-        const float q0 = r[2 * i], q1 = r[2 * i + 1];
+        const float q0 = rq(2 * i), q1 = rq(2 * i + 1);
         const float t = tof(i), a = 1.f - t;
         const float n00 = q0 * (a * p00 + t * p10), n01 = q0 * (a * p01 + t * p11);
         const float n10 = q1 * (t * p00 + a * p10), n11 = q1 * (t * p01 + a * p11);
@@ -1402,7 +1432,7 @@ __global__ void __launch_bounds__(1024) ffbs_scan_kernel(ProblemDev P, uint32_t*
     }
     int cnt = 0;
     for (int i = s0; i < s1; ++i) {
-        const float q0 = r[2 * i], q1 = r[2 * i + 1];
+        const float q0 = rq(2 * i), q1 = rq(2 * i + 1);
         const float t = tof(i), a = 1.f - t;
         float f0 = q0 * (a * v0 + t * v1), f1 = q1 * (t * v0 + a * v1);
         const float tot = f0 + f1;
@@ -1440,7 +1470,10 @@ __global__ void __launch_bounds__(1024) ffbs_scan_kernel(ProblemDev P, uint32_t*
         else {
             if (ub == 4) {
 #pragma unroll
-                for (int q = 0; q < 4; ++q) ubuf[q] = idx + q < M ? draws.get(cr, chain, step, idx + q) : 0.0;
+                for (int q = 0; q < 4; ++q)
+                    ubuf[q] = idx + q >= M ? 0.0
+                              : upre ? (cg ? __ldcg(upre + idx + q) : upre[idx + q])
+                                     : draws.get(cr, chain, step, idx + q);
                 ub = 0;
             }
             const double u = ubuf[ub++];
@@ -1492,6 +1525,51 @@ __global__ void __launch_bounds__(1024) ffbs_scan_kernel(ProblemDev P, uint32_t*
         const int cur = (int)((w >> (m & 31)) & 1u);
         if (sv != cur) *wp = w ^ (1u << (m & 31));
     }
+}
+
+__global__ void __launch_bounds__(1024, 1) ffbs_scan_kernel(ProblemDev P, uint32_t* dg, int first, int nchain,
+                                                         const int32_t* order, int64_t ostride, int step,
+                                                         Draws draws, const uint8_t* sel, int want,
+                                                         const uint8_t* badc, const float* raw32, float* fbbuf,
+                                                         uint8_t* mapbuf, int staged, const double* ubuf) {
+    extern __shared__ __align__(16) unsigned char fsm[];
+    const int cr = blockIdx.x;
+    if (cr >= nchain) return;
+    if (sel && sel[cr] != want) return;
+    if (badc[cr]) return;
+    const int M = P.M;
+    ffbs_scan_chain(P, dg, first + cr, cr, order[cr * ostride + step], step, draws,
+                    ubuf ? ubuf + (size_t)cr * M : nullptr,
+                    raw32 + (size_t)cr * 2 * M, fbbuf + (size_t)cr * 2 * M, mapbuf + (size_t)cr * M, staged, false,
+                    fsm);
+}
+
+// ---------------------------------------------------------------------------
+// Fast M-sampler likelihoods of one meiosis step: grid (blocks per chain,
+// chains), one warp per locus (fagw_task).  With ubuf, the first 32-locus
+// slice of warps also draws the step's uniforms by index, one per lane, so
+// ffbs_scan_kernel only reads them.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kFagWarpsPerBlock * 32) fag_warp_kernel(ProblemDev P, uint32_t* dg, int first,
+                                                                         const int32_t* order, int64_t ostride,
+                                                                         int step, Draws draws, const uint8_t* sel,
+                                                                         int want, float* rawbuf, float* raw32,
+                                                                         uint8_t* badc, int* status, double* ubuf) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int cr = blockIdx.y;
+    if (sel && sel[cr] != want) return;
+    const int M = P.M;
+    const FagwTables tab = fagw_load_tables(P, smem);
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int chain = first + cr;
+    const int32_t* ord = order + cr * ostride;
+    const int gw = blockIdx.x * kFagWarpsPerBlock + warp;
+    if (ubuf && step >= 0 && gw * 32 + lane < M)
+        ubuf[(size_t)cr * M + gw * 32 + lane] = draws.get(cr, chain, step, gw * 32 + lane);
+    if (gw < M)
+        fagw_task(P, tab, smem + fagw_tables(P.N) + (size_t)warp * fagw_warp_bytes(P.N, P.F), dg, chain, cr, gw, ord,
+                  step, rawbuf, raw32, badc, status);
 }
 
 // Threads per chain of ffbs_scan_kernel: runs of about 4 loci.
@@ -2282,8 +2360,11 @@ static cudaError_t launch_msampler_t(const ProblemDev& P, uint32_t* dg, int firs
                                      int64_t mstride, int nm, const double* u, int64_t ucs, uint64_t seed,
                                      uint64_t iter, const uint8_t* sel, int want, typename PP::T* raw, float* raw32,
                                      void* fb, uint8_t* badc, uint8_t* maps, int* status, int fag_threads, int exact,
-                                     cudaStream_t s, const uint64_t* key) {
+                                     cudaStream_t s, const uint64_t* key, double* ubuf) {
     const int fast = exact ? 0 : 1;
+    Draws d{u, ucs, P.M, seed, iter, 2, key};
+    cudaError_t e0 = cudaMemsetAsync(badc, 0, (size_t)nchain, s);
+    if (e0 != cudaSuccess) return e0;
     const size_t smem = fag_block_bytes(P.N, P.F, fag_threads, fast);
     static size_t configured = 0;
     if (smem > configured) {
@@ -2291,7 +2372,6 @@ static cudaError_t launch_msampler_t(const ProblemDev& P, uint32_t* dg, int firs
         if (e != cudaSuccess) return e;
         configured = smem;
     }
-    Draws d{u, ucs, P.M, seed, iter, 2, key};
     const int scan_threads = ffbs_scan_threads(P.M);
     size_t scan_smem = ffbs_scan_smem(P.M);
     int staged = 1;
@@ -2300,18 +2380,16 @@ static cudaError_t launch_msampler_t(const ProblemDev& P, uint32_t* dg, int firs
         staged = 0;
     }
     static size_t scan_configured = 0;
-    if (scan_smem > scan_configured) {
+    if (!exact && scan_smem > scan_configured) {
         cudaError_t e = cudaFuncSetAttribute(ffbs_scan_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)scan_smem);
         if (e != cudaSuccess) return e;
         scan_configured = scan_smem;
     }
-    cudaError_t e0 = cudaMemsetAsync(badc, 0, (size_t)nchain, s);
-    if (e0 != cudaSuccess) return e0;
     const int64_t ntask = (int64_t)nchain * P.M;
     const int grid = (int)((ntask + fag_threads - 1) / fag_threads);
-    // fast mode: one warp per (chain, locus)
+    // fast mode: one warp per (chain, locus), else the thread-per-locus kernel
+    // in log2 (component counts are 13-bit fields)
     const size_t wsm = fagw_block_bytes(P.N, P.F);
-    // else the thread-per-locus kernel in log2 (component counts are 13-bit fields)
     const bool warp_like = !exact && wsm <= 200 * 1024 && 2 * P.F < 8192;
     static size_t wconfigured = 0;
     if (warp_like && wsm > wconfigured) {
@@ -2319,24 +2397,23 @@ static cudaError_t launch_msampler_t(const ProblemDev& P, uint32_t* dg, int firs
         if (e != cudaSuccess) return e;
         wconfigured = wsm;
     }
-    const int wgrid = (int)((ntask + kFagWarpsPerBlock - 1) / kFagWarpsPerBlock);
-    auto like = [&](int j) {
+    const dim3 wgrid((unsigned)((P.M + kFagWarpsPerBlock - 1) / kFagWarpsPerBlock), (unsigned)nchain);
+    double* upre = warp_like ? ubuf : nullptr;
+    for (int j = -1; j < nm; ++j) {
         if (!warp_like)
             fag_kernel<IX, PP><<<grid, fag_threads, smem, s>>>(P, dg, first, nchain, meioses, mstride, j, sel, want,
                                                                raw, exact ? nullptr : raw32, badc, status, fast);
         else
-            fag_warp_kernel<<<wgrid, kFagWarpsPerBlock * 32, wsm, s>>>(P, dg, first, nchain, meioses, mstride, j, sel,
-                                                                       want, (float*)raw, raw32, badc, status);
-    };
-    like(-1);
-    for (int j = 0; j < nm; ++j) {
-        like(j);
+            fag_warp_kernel<<<wgrid, kFagWarpsPerBlock * 32, wsm, s>>>(P, dg, first, meioses, mstride, j, d, sel,
+                                                                       want, (float*)raw, raw32, badc, status, upre);
+        if (j < 0) continue;
         if (exact)
             ffbs_kernel<double><<<nchain, 32, 0, s>>>(P, dg, first, nchain, meioses, mstride, j, d, sel, want, badc,
                                                       (const double*)raw, nullptr, (double*)fb);
         else
             ffbs_scan_kernel<<<nchain, scan_threads, scan_smem, s>>>(P, dg, first, nchain, meioses, mstride, j, d, sel,
-                                                                     want, badc, raw32, (float*)fb, maps, staged);
+                                                                     want, badc, raw32, (float*)fb, maps, staged,
+                                                                     upre);
     }
     return cudaGetLastError();
 }
@@ -2350,25 +2427,25 @@ cudaError_t launch_msampler(const ProblemDev& P, uint32_t* dg, int first, int nc
                             int64_t mstride, int nm, const double* u, int64_t ucs, uint64_t seed, uint64_t iter,
                             const uint8_t* sel, int want, double* raw64, float* raw32, void* fb, uint8_t* badc,
                             uint8_t* maps, int* status, int fag_threads, int exact, cudaStream_t s,
-                            const uint64_t* key) {
+                            const uint64_t* key, double* ubuf) {
     // the fast mode keeps log2 likelihoods as floats in the first half of the raw buffer
     float* rawl = (float*)raw64;
     if (2 * P.F <= 255) {
         if (exact)
             return launch_msampler_t<uint8_t, ProbExact>(P, dg, first, nchain, meioses, mstride, nm, u, ucs, seed,
                                                          iter, sel, want, raw64, raw32, fb, badc, maps, status,
-                                                         fag_threads, exact, s, key);
+                                                         fag_threads, exact, s, key, ubuf);
         return launch_msampler_t<uint8_t, ProbLog2>(P, dg, first, nchain, meioses, mstride, nm, u, ucs, seed, iter,
                                                     sel, want, rawl, raw32, fb, badc, maps, status, fag_threads,
-                                                    exact, s, key);
+                                                    exact, s, key, ubuf);
     }
     if (exact)
         return launch_msampler_t<uint16_t, ProbExact>(P, dg, first, nchain, meioses, mstride, nm, u, ucs, seed, iter,
                                                       sel, want, raw64, raw32, fb, badc, maps, status, fag_threads,
-                                                      exact, s, key);
+                                                      exact, s, key, ubuf);
     return launch_msampler_t<uint16_t, ProbLog2>(P, dg, first, nchain, meioses, mstride, nm, u, ucs, seed, iter, sel,
                                                  want, rawl, raw32, fb, badc, maps, status, fag_threads, exact, s,
-                                                 key);
+                                                 key, ubuf);
 }
 
 size_t fag_smem(int N, int F, int threads, int fast) { return fag_block_bytes(N, F, threads, fast); }
