@@ -945,6 +945,22 @@ __host__ __device__ inline size_t fagw_warp_bytes(int N, int F) {
 }
 size_t fagw_block_bytes(int N, int F) { return fagw_tables(N) + kFagWarpsPerBlock * fagw_warp_bytes(N, F); }
 
+// Root of founder allele x in a forest of 2 * parent + parity entries, and
+// x's parity to it.  Parents have smaller indices than their children, so the
+// walk ends within x steps.
+__device__ __forceinline__ int pf_find(volatile int* L, int x, int& parity) {
+    int p = 0, y = x;
+    for (int it = 0; it < 8192; ++it) {
+        const int v = L[y];
+        const int up = v >> 1;
+        if (up == y) break;
+        p ^= v & 1;
+        y = up;
+    }
+    parity = p;
+    return y;
+}
+
 // The tables every warp of a block shares, loaded into the block's shared memory.
 struct FagwTables {
     int16_t* lvl;
@@ -1074,41 +1090,44 @@ __device__ __forceinline__ void fagw_task(const ProblemDev& P, const FagwTables&
         }
         bad = __any_sync(FULLMASK, bad);
         __syncwarp();
-        // 3. components of the heterozygote edges with parities
+        // 3. components of the heterozygote edges with parities: a lock-free
+        // union-find forest in Lb (2 * parent + parity to the parent), each
+        // lane joining its edges by hooking the larger root under the smaller
+        // with a compare-and-swap (so a root is its component's smallest
+        // allele); an edge whose ends already share a root must have ends of
+        // opposite parity.  A failed hook means another lane's hook succeeded,
+        // so a lane retries fewer than 2F times.  Then every allele points at
+        // its root.
         if (!bad && nhet > 0) {
-            // labels only decrease and a path of k edges settles within k rounds:
-            // 2F + 2 rounds always suffice (the bound only guards the loop)
-            for (int round = 0;; ++round) {
-                if (round > nfa + 2) {
-                    bad = 1;
-                    if (lane == 0) set_status(status, ST_ILLEGAL_DG);
-                    break;
-                }
-                int ch = 0;
-                for (int q = lane; q < nhet; q += 32) {
-                    const uint32_t h = hed[q];
-                    const int u = (int)(h & 0xffffu), v = (int)(h >> 16);
-                    const int a = Lb[u], b = Lb[v];
-                    if ((a ^ 1) < b) { atomicMin((int*)&Lb[v], a ^ 1); ch = 1; }
-                    if ((b ^ 1) < a) { atomicMin((int*)&Lb[u], b ^ 1); ch = 1; }
-                }
-                __syncwarp();
-                for (int x = lane; x < nfa; x += 32) {
-                    const int a = Lb[x], r = a >> 1;
-                    if (r != x) {
-                        const int b = Lb[r];
-                        const int nv = (b & ~1) | ((a ^ b) & 1);
-                        if (nv < a) { atomicMin((int*)&Lb[x], nv); ch = 1; }
-                    }
-                }
-                __syncwarp();
-                if (!__any_sync(FULLMASK, ch)) break;
-            }
             for (int q = lane; q < nhet; q += 32) {
                 const uint32_t h = hed[q];
-                if ((Lb[h & 0xffffu] ^ Lb[h >> 16]) != 1) bad = 1;   // same label, parities must differ
+                const int u = (int)(h & 0xffffu), v = (int)(h >> 16);
+                for (int tries = 0;; ++tries) {
+                    if (tries > nfa) {
+                        bad = 1;
+                        set_status(status, ST_ILLEGAL_DG);
+                        break;
+                    }
+                    int pu, pv;
+                    const int ru = pf_find(Lb, u, pu), rv = pf_find(Lb, v, pv);
+                    if (ru == rv) {
+                        if ((pu ^ pv) != 1) bad = 1;   // an odd cycle of heterozygote edges
+                        break;
+                    }
+                    const int lo = min(ru, rv), hi = max(ru, rv);
+                    if (atomicCAS((int*)&Lb[hi], hi << 1, (lo << 1) | (pu ^ pv ^ 1)) == (hi << 1)) break;
+                }
             }
             bad = __any_sync(FULLMASK, bad);
+            __syncwarp();
+            if (!bad) {
+                for (int x = lane; x < nfa; x += 32) {
+                    int p;
+                    const int r = pf_find(Lb, x, p);
+                    Lb[x] = (r << 1) | p;
+                }
+                __syncwarp();
+            }
         }
         // 4. sum over each component's colourings, log2: every member allele
         // contributes log2 of the major or the minor frequency, so a component
