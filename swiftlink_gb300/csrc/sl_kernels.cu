@@ -191,9 +191,16 @@ __device__ T ls_term(const ProblemDev& P, const OpDev& op, const T* Am, const T*
     return tmp;
 }
 
+// A warp's shared bytes: the rfunctions [arena], the children's transmission
+// distributions [16 per child], the sampled states [N], the peel's draws [K]
+// (doubles, 16-byte aligned); a multiple of 16 so every warp's base is aligned.
+template <typename T>
+__host__ __device__ __forceinline__ size_t ls_draws_at(const ProblemDev& P) {
+    return ((size_t)P.arena * sizeof(T) + (size_t)P.max_child * 16 * sizeof(T) + (size_t)P.N + 15) & ~(size_t)15;
+}
 template <typename T>
 __host__ __device__ __forceinline__ size_t ls_warp_bytes(const ProblemDev& P) {
-    return (size_t)P.arena * sizeof(T) + (size_t)P.max_child * 16 * sizeof(T) + (((size_t)P.N + 15) & ~(size_t)15);
+    return (ls_draws_at<T>(P) + 8 * (size_t)P.K + 15) & ~(size_t)15;
 }
 
 // One warp per (chain, locus) task; the listed loci must be pairwise
@@ -213,6 +220,7 @@ __device__ int ls_locus(const ProblemDev& P, uint32_t* dg, int cr, int chain, in
     T* A = (T*)wsmem;
     T* dist = A + P.arena;
     int8_t* assign = (int8_t*)(dist + 16 * P.max_child);
+    double* sdraw = (double*)(wsmem + ls_draws_at<T>(P));
     uint32_t* colC = dg + ((size_t)chain * P.M + l) * P.W;
     const uint32_t* colL = hasL ? colC - P.W : nullptr;
     const uint32_t* colR = hasR ? colC + P.W : nullptr;
@@ -241,17 +249,23 @@ __device__ int ls_locus(const ProblemDev& P, uint32_t* dg, int cr, int chain, in
         const T* trait = pri + 4 * (gcol[op.peel] & 3);
         T* out = A + op.mat_off;
         T mx = T(0);
-        for (int cell = lane; cell < ncell; cell += 32) {
-            T total = T(0);
-            if (ls_valid(cut, op.c, gcol, cell)) {
-                for (int v = 0; v < 4; ++v) {
-                    const T tv = trait[v];
-                    if (tv == T(0)) continue;
-                    total = Ar::add(total, ls_term<T>(P, op, A, dist, cell, v, tv));
-                }
+        // one (cell, state) term per lane, four lanes per cell; the cell's
+        // total adds its terms in state order from zero, as the reference's
+        // loop does (a skipped term is an exact zero)
+        const int nitem = 4 * ncell, grp = lane & ~3, v = lane & 3;
+        const T tv = trait[v];
+        for (int it0 = 0; it0 < nitem; it0 += 32) {
+            const int cell = (it0 + lane) >> 2;
+            T term = T(0);
+            if (it0 + lane < nitem && tv != T(0) && ls_valid(cut, op.c, gcol, cell))
+                term = ls_term<T>(P, op, A, dist, cell, v, tv);
+            const T t0 = __shfl_sync(FULLMASK, term, grp), t1 = __shfl_sync(FULLMASK, term, grp + 1);
+            const T t2 = __shfl_sync(FULLMASK, term, grp + 2), t3 = __shfl_sync(FULLMASK, term, grp + 3);
+            if (v == 0 && it0 + lane < nitem) {
+                const T total = Ar::add(Ar::add(Ar::add(Ar::add(T(0), t0), t1), t2), t3);
+                out[cell] = total;
+                mx = total > mx ? total : mx;
             }
-            out[cell] = total;
-            mx = total > mx ? total : mx;
         }
         if (kRescale) {
             // the sampling draws from ratios within one rfunction, so a
@@ -275,6 +289,8 @@ __device__ int ls_locus(const ProblemDev& P, uint32_t* dg, int cr, int chain, in
     }
     if (lane == 0 && logroot) *logroot = log((double)root) + (double)scale * 0.69314718055994530942;
     for (int i = lane; i < P.N; i += 32) assign[i] = -1;
+    // the backward pass's draws, one per operation, generated together
+    for (int j = lane; j < P.K; j += 32) sdraw[j] = draws.get(cr, chain, unit, base + j);
     __syncwarp();
     // backward sampling of ordered genotypes (SamplerRfunction::sample)
     for (int k = P.K - 1; k >= 0; --k) {
@@ -303,7 +319,7 @@ __device__ int ls_locus(const ProblemDev& P, uint32_t* dg, int cr, int chain, in
             const T tot = Ar::add(Ar::add(Ar::add(p0, p1), p2), p3);
             if (tot != T(0))
                 for (int v = 0; v < 4; ++v) pd[v] = Ar::div(pd[v], tot);
-            const double r = draws.get(cr, chain, unit, base + P.K - 1 - k);
+            const double r = sdraw[P.K - 1 - k];
             T acc = T(0);
             int lastv = 0, pick = -1;
             for (int v = 0; v < 4; ++v) {
