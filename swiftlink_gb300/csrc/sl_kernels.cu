@@ -954,7 +954,7 @@ __global__ void __launch_bounds__(128) fag_kernel(ProblemDev P, uint32_t* dg, in
 constexpr int kFagWarpsPerBlock = 8;
 
 __host__ __device__ inline size_t fagw_tables(int N) {
-    return (((size_t)N * 7 + 15) & ~(size_t)15) + (((size_t)4 * (N + 1) + 15) & ~(size_t)15);
+    return (((size_t)N * 8 + 15) & ~(size_t)15) + (((size_t)4 * (N + 1) + 15) & ~(size_t)15);
 }
 __host__ __device__ inline size_t fagw_warp_bytes(int N, int F) {
     return (((size_t)4 * N + 15) & ~(size_t)15) + (size_t)2 * F * 12 + (size_t)4 * N;
@@ -963,15 +963,27 @@ size_t fagw_block_bytes(int N, int F) { return fagw_tables(N) + kFagWarpsPerBloc
 
 // Root of founder allele x in a forest of 2 * parent + parity entries, and
 // x's parity to it.  Parents have smaller indices than their children, so the
-// walk ends within x steps.
+// walk ends within x steps.  On the way every other entry is pointed at its
+// grandparent with the composed parity (path halving): only entries that are
+// not roots are rewritten, always to an ancestor, so the forest stays valid
+// whatever other lanes do meanwhile.
 __device__ __forceinline__ int pf_find(volatile int* L, int x, int& parity) {
     int p = 0, y = x;
     for (int it = 0; it < 8192; ++it) {
         const int v = L[y];
         const int up = v >> 1;
         if (up == y) break;
-        p ^= v & 1;
-        y = up;
+        const int w = L[up];
+        const int gp = w >> 1;
+        if (gp == up) {   // up is the root
+            p ^= v & 1;
+            y = up;
+            break;
+        }
+        const int pg = (v ^ w) & 1;   // parity of y to its grandparent
+        L[y] = (gp << 1) | pg;
+        p ^= pg;
+        y = gp;
     }
     parity = p;
     return y;
@@ -979,26 +991,19 @@ __device__ __forceinline__ int pf_find(volatile int* L, int x, int& parity) {
 
 // The tables every warp of a block shares, loaded into the block's shared memory.
 struct FagwTables {
-    int16_t* lvl;
-    int16_t* mo;
-    int16_t* fa;
-    uint8_t* typed;
+    uint2* lvl;         // [N] members by generation level: x = member, y = 2 mother | 2 father << 16
     int32_t* lvl_off;   // [n_lvl + 1]
 };
 
 __device__ FagwTables fagw_load_tables(const ProblemDev& P, unsigned char* smem) {
     const int N = P.N;
     FagwTables t;
-    t.lvl = (int16_t*)smem;
-    t.mo = t.lvl + N;
-    t.fa = t.mo + N;
-    t.typed = (uint8_t*)(t.fa + N);
-    t.lvl_off = (int32_t*)(smem + (((size_t)N * 7 + 15) & ~(size_t)15));
-    for (int i = threadIdx.x; i < N; i += blockDim.x) {
-        t.lvl[i] = P.lvl_order[i];
-        t.mo[i] = P.mother[i];
-        t.fa[i] = P.father[i];
-        t.typed[i] = P.typed[i];
+    t.lvl = (uint2*)smem;
+    t.lvl_off = (int32_t*)(smem + (((size_t)N * 8 + 15) & ~(size_t)15));
+    for (int q = threadIdx.x; q < N; q += blockDim.x) {
+        const int pid = P.lvl_order[q];
+        const int mo = P.mother[pid], fa = P.father[pid];
+        t.lvl[q] = make_uint2((unsigned)pid, mo < 0 ? 0u : (unsigned)(2 * mo) | ((unsigned)(2 * fa) << 16));
     }
     for (int i = threadIdx.x; i <= P.n_lvl; i += blockDim.x) t.lvl_off[i] = P.lvl_off[i];
     return t;
@@ -1012,9 +1017,7 @@ __device__ __forceinline__ void fagw_task(const ProblemDev& P, const FagwTables&
                           uint8_t* badc, int* status) {
     const int N = P.N, F = P.F, nfa = 2 * F, M = P.M;
     const int lane = threadIdx.x & 31;
-    const int16_t* s_lvl = tab.lvl;
-    const int16_t* s_mo = tab.mo;
-    const int16_t* s_fa = tab.fa;
+    const uint2* s_lvl = tab.lvl;
     uint16_t* e = (uint16_t*)wbase;                                   // [2N] founder allele of each allele
     volatile int* Lb = (volatile int*)(wbase + (((size_t)4 * N + 15) & ~(size_t)15));   // [2F] 2 * label + parity
     int* fl = (int*)(Lb + nfa);                                       // [2F] bit0 used, bit1 fixed A, bit2 fixed B
@@ -1033,8 +1036,10 @@ __device__ __forceinline__ void fagw_task(const ProblemDev& P, const FagwTables&
         const uint32_t cw = wreg && lane < P.W ? col[lane] : 0u;
         uint32_t gpack = 0u;
 #pragma unroll
-        for (int k = 0; k < 16; ++k)
+        for (int k = 0; k < 16; ++k) {
+            if (k * 32 >= N) break;
             if (k * 32 + lane < N) gpack |= (uint32_t)(gcol[k * 32 + lane] & 3) << (2 * k);
+        }
         const double minor_d = P.c_minor[(size_t)chain * M + l];
         auto cbit = [&](int b) -> int {
             const uint32_t w = wreg ? __shfl_sync(FULLMASK, cw, b >> 5) : col[b >> 5];
@@ -1051,7 +1056,7 @@ __device__ __forceinline__ void fagw_task(const ProblemDev& P, const FagwTables&
         }
         // 1. founder alleles, one generation level at a time
         for (int q = lane; q < s_off[1]; q += 32) {
-            const int pid = s_lvl[q];
+            const int pid = (int)s_lvl[q].x;
             e[2 * pid] = (uint16_t)(2 * pid);
             e[2 * pid + 1] = (uint16_t)(2 * pid + 1);
         }
@@ -1061,14 +1066,15 @@ __device__ __forceinline__ void fagw_task(const ProblemDev& P, const FagwTables&
             for (int q0 = s_off[k]; q0 < s_off[k + 1]; q0 += 32) {
                 const int q = q0 + lane;
                 const bool act = q < s_off[k + 1];
-                const int pid = act ? s_lvl[q] : F;
+                const uint2 ent = act ? s_lvl[q] : make_uint2((unsigned)F, 0u);
+                const int pid = (int)ent.x;
                 const int b = 2 * (pid - F);
                 const uint32_t w = wreg ? __shfl_sync(FULLMASK, cw, b >> 5) : col[b >> 5];
                 if (!act) continue;
                 const int vm = (int)((w >> (b & 31)) & 1u) ^ (flip == b);
                 const int vp = (int)((w >> ((b + 1) & 31)) & 1u) ^ (flip == b + 1);
-                e[2 * pid] = e[2 * s_mo[pid] + vm];
-                e[2 * pid + 1] = e[2 * s_fa[pid] + vp];
+                e[2 * pid] = e[(ent.y & 0xffffu) + vm];
+                e[2 * pid + 1] = e[(ent.y >> 16) + vp];
             }
             __syncwarp();
         }
