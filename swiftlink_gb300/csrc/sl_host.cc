@@ -33,7 +33,7 @@ cudaError_t launch_msampler(const ProblemDev& P, uint32_t* dg, int first, int nc
                             int64_t mstride, int nm, const double* u, int64_t ucs, uint64_t seed, uint64_t iter,
                             const uint8_t* sel, int want, double* raw64, float* raw32, void* fb, uint8_t* badc,
                             uint8_t* maps, int* status, int fag_threads, int exact, cudaStream_t s,
-                            const uint64_t* key = nullptr, double* ubuf = nullptr);
+                            const uint64_t* key = nullptr, double* ubuf = nullptr, int pairs = 0);
 cudaError_t launch_set_key(uint64_t* key, uint64_t seed, uint64_t iter, cudaStream_t s);
 cudaError_t launch_si(const ProblemDev& P, uint32_t* dg, int first, int nchain, const int32_t* starts,
                       const double* u, int64_t ucs, uint64_t seed, uint64_t pass, double* weights, int* status,
@@ -178,6 +178,11 @@ cudaEvent_t take_event(sl_ctx* c) {
 // Kernels one M-sweep of nm meioses launches for a chain: a reset, then per
 // meiosis a likelihood and a filter kernel.
 static int64_t msweep_kernels(const sl_ctx*, int nm) { return 1 + 2 * (int64_t)nm; }
+
+// The fast M-step's likelihood kernel puts two loci in a warp (fewer
+// instructions per locus, a longer launch) when the context holds enough
+// chains for the GPU to be throughput-bound.
+static int msampler_pairs(const sl_ctx* ctx) { return ctx->n_chains >= 8 ? 1 : 0; }
 
 struct Prof {
     sl_ctx* c;
@@ -1484,7 +1489,7 @@ int sl_msampler_sweep(sl_ctx* ctx, int32_t first, int32_t n_chains, const int32_
       ctx->launches += msweep_kernels(ctx, n_meioses) - 1;   // one counted by Prof
       CK(launch_msampler(P, ctx->d_dg, first, n_chains, ctx->d_mlist, 0, n_meioses, ctx->d_u, ucs, 0, 0, nullptr, 0,
                        ctx->d_raw, ctx->d_raw32, ctx->d_fb, ctx->d_badc, ctx->d_maps, ctx->d_status, ctx->ms_threads,
-                       ctx->sampler_precision == SL_SAMPLER_EXACT, ctx->stream, nullptr, ctx->d_mu));
+                       ctx->sampler_precision == SL_SAMPLER_EXACT, ctx->stream, nullptr, ctx->d_mu, msampler_pairs(ctx)));
     }
     return sl_synchronize(ctx);
 }
@@ -1972,7 +1977,7 @@ static cudaError_t capture_chain_body(sl_ctx* ctx, int c, cudaGraph_t body, cuda
     void* fb = exact ? (void*)((double*)ctx->d_fb + (size_t)c * 2 * M) : (void*)((float*)ctx->d_fb + (size_t)c * 2 * M);
     e = launch_msampler(P, ctx->d_dg, c, 1, ctx->d_morder + (size_t)c * nm, nm, nm, nullptr, 0, 0, 0, nullptr, 0, raw,
                         ctx->d_raw32 + (size_t)c * 2 * M, fb, ctx->d_badc + c, ctx->d_maps + (size_t)c * M,
-                        ctx->d_status, ctx->ms_threads, exact ? 1 : 0, s2, key, ctx->d_mu + (size_t)c * M);
+                        ctx->d_status, ctx->ms_threads, exact ? 1 : 0, s2, key, ctx->d_mu + (size_t)c * M, msampler_pairs(ctx));
     e2 = cudaStreamEndCapture(s2, &sw[1]);
     if (e != cudaSuccess || (e = e2) != cudaSuccess) return e;
     // scoring of chain c into its own table
@@ -1996,8 +2001,7 @@ static cudaError_t capture_chain_body(sl_ctx* ctx, int c, cudaGraph_t body, cuda
     return cudaStreamEndCapture(s1, &body);
 }
 
-// The run graph: init -> one WHILE node per chain (in parallel) -> merge of
-// the chains' LOD tables into the context's.
+// The run graph: init -> one WHILE node per chain (in parallel).
 // Everything the run graph needs that cannot happen inside a capture:
 // buffers, the kernels' shared-memory limits (set by direct launches that do
 // nothing), the timed choice of the scoring kernel, capture streams.
@@ -2018,7 +2022,7 @@ static int prepare_run_graph(sl_ctx* ctx) {
     CK(cudaMemsetAsync(ctx->d_sel, 0, (size_t)C, ctx->stream));
     CK(launch_msampler(P, ctx->d_dg, 0, C, ctx->d_morder, nm, 0, nullptr, 0, 0, 0, ctx->d_sel, 2, ctx->d_raw,
                        ctx->d_raw32, ctx->d_fb, ctx->d_badc, ctx->d_maps, ctx->d_status, ctx->ms_threads, exact ? 1 : 0,
-                       ctx->stream, ctx->d_keys, ctx->d_mu));
+                       ctx->stream, ctx->d_keys, ctx->d_mu, msampler_pairs(ctx)));
     CK(launch_lsampler(P, ctx->d_dg, 0, C, ctx->d_even, (int)ctx->even.size(), nullptr, 0, 0, 0, 0, ctx->d_sel, 2,
                        ctx->d_status, ctx->stream, ctx->ls_grid, ctx->ls_wpb, ctx->d_keys));
     // the scoring kernel is fixed in the graph: time the candidates now if needed
@@ -2053,11 +2057,11 @@ static int prepare_run_graph(sl_ctx* ctx) {
 }
 
 // Capture one context's run nodes at the current point of stream s (which
-// is capturing): init -> one WHILE node per chain (in parallel) -> merge of the
-// chains' LOD tables into the context's.  s1 and s2 capture the bodies.
+// is capturing): init -> one WHILE node per chain (in parallel).  The chains'
+// LOD tables are merged into the context's when read (flush_chain_tables).
+// s1 and s2 capture the bodies.
 static cudaError_t capture_run_nodes(sl_ctx* ctx, cudaStream_t s, cudaStream_t s1, cudaStream_t s2) {
     const int C = ctx->n_chains;
-    const int64_t npos = (int64_t)(ctx->P.M - 1) * ctx->P.n_lod;
     cudaError_t e = launch_run_init(ctx->d_run, ctx->d_chain_it, C, s);
     if (e != cudaSuccess) return e;
     cudaStreamCaptureStatus st;
@@ -2203,7 +2207,7 @@ static int build_ms_graph(sl_ctx* ctx) {
     CK(launch_set_key(ctx->d_key, 0, 0, ctx->stream));
     CK(launch_msampler(P, ctx->d_dg, 0, C, ctx->d_morder, nm, 0, nullptr, 0, 0, 0, ctx->d_sel, 2, ctx->d_raw,
                        ctx->d_raw32, ctx->d_fb, ctx->d_badc, ctx->d_maps, ctx->d_status, ctx->ms_threads, exact ? 1 : 0,
-                       ctx->stream, ctx->d_key, ctx->d_mu));
+                       ctx->stream, ctx->d_key, ctx->d_mu, msampler_pairs(ctx)));
     CK(cudaStreamSynchronize(ctx->stream));
     while ((int)ctx->cap_streams.size() < C + 1) {
         cudaStream_t st;
@@ -2225,7 +2229,7 @@ static int build_ms_graph(sl_ctx* ctx) {
         err = launch_msampler(P, ctx->d_dg, c, 1, ctx->d_morder + (size_t)c * nm, nm, nm, nullptr, 0, 0, 0,
                               ctx->d_sel + c, 0, raw, ctx->d_raw32 + (size_t)c * 2 * M, fb, ctx->d_badc + c,
                               ctx->d_maps + (size_t)c * M, ctx->d_status, ctx->ms_threads, exact ? 1 : 0, sc,
-                              ctx->d_key, ctx->d_mu + (size_t)c * M);
+                              ctx->d_key, ctx->d_mu + (size_t)c * M, msampler_pairs(ctx));
         if (err != cudaSuccess) break;
         err = cudaEventRecord(ctx->cap_events[c], sc);
         if (err != cudaSuccess) break;
