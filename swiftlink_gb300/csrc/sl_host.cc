@@ -25,6 +25,7 @@
 namespace sl {
 // kernels (sl_kernels.cu)
 size_t lsampler_smem_per_warp(const ProblemDev& P);
+size_t lsampler_smem_shared(const ProblemDev& P);
 cudaError_t launch_lsampler(const ProblemDev& P, uint32_t* dg, int first, int nchain, const int32_t* loci,
                             int nloci, const double* u, int64_t ucs, int64_t uls, uint64_t seed, uint64_t iter,
                             const uint8_t* sel, int want, int* status, cudaStream_t s, int grid_cap, int wpb,
@@ -1161,21 +1162,22 @@ int sl_create(const sl_problem_desc* d, const sl_options* opt, sl_ctx** out) {
     if ((rc = upload(ctx, (uint8_t**)&P.dmask, dmask.data(), N))) return bail(rc);
     if ((rc = upload(ctx, (OpDev**)&P.ops, ops.data(), K))) return bail(rc);
     if ((rc = upload(ctx, (int32_t**)&P.opdata, od.data(), od.size()))) return bail(rc);
+    P.opdata_n = (int32_t)od.size();
     if ((rc = upload(ctx, (int16_t**)&P.fag_order, order.data(), N))) return bail(rc);
     if ((rc = upload(ctx, (int16_t**)&P.lvl_order, lvl_order.data(), N))) return bail(rc);
     if ((rc = upload(ctx, (int32_t**)&P.lvl_off, lvl_off.data(), lvl_off.size()))) return bail(rc);
     P.n_lvl = (int32_t)lvl_off.size() - 1;
 
     // ---- launch shapes from the shared-memory footprint of one task
-    const size_t lsw = lsampler_smem_per_warp(P);
+    const size_t lsw = lsampler_smem_per_warp(P), lst = lsampler_smem_shared(P);
     const size_t lodw = (size_t)arena * (ctx->lod_precision == SL_LOD_FP32_RESCALED ? 4 : 8);
-    if (lsw > kSmemBudget || lodw > kSmemBudget)
+    if (lst + lsw > kSmemBudget || lodw > kSmemBudget)
         return bail(fail(nullptr, SL_EINVAL, "peel sequence needs %zu bytes per task, above the shared-memory budget",
                          std::max(lsw, lodw)));
-    ctx->ls_wpb = (int)std::max<size_t>(1, std::min<size_t>(4, kSmemBudget / lsw));
+    ctx->ls_wpb = (int)std::max<size_t>(1, std::min<size_t>(4, (kSmemBudget - lst) / lsw));
     ctx->lod_wpb = (int)std::max<size_t>(1, std::min<size_t>(4, kSmemBudget / lodw));
     const size_t per_sm = prop.sharedMemPerMultiprocessor;
-    const int ls_blocks = std::max(1, (int)std::min<size_t>(16, per_sm / (ctx->ls_wpb * lsw + 1024)));
+    const int ls_blocks = std::max(1, (int)std::min<size_t>(16, per_sm / (lst + ctx->ls_wpb * lsw + 1024)));
     const int lod_blocks = std::max(1, (int)std::min<size_t>(16, per_sm / (ctx->lod_wpb * lodw + 1024)));
     ctx->ls_grid = ctx->sms * ls_blocks;
     ctx->lod_grid = ctx->sms * lod_blocks;

@@ -43,6 +43,7 @@ struct ProblemDev {
     const uint8_t* dmask;                // [N] bit v set when dprob[v] != 0
     const OpDev* ops;                    // [K]
     const int32_t* opdata;
+    int32_t opdata_n;                    // words of opdata
     const int16_t* fag_order;            // [N] parents before children, founders first
     const int16_t* lvl_order;            // [N] persons by generation level (founders = level 0)
     const int32_t* lvl_off;              // [n_lvl + 1] start of each level in lvl_order

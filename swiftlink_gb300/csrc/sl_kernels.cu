@@ -142,11 +142,12 @@ __device__ void ls_dist_one(const ProblemDev& P, int person, const uint32_t* col
 }
 
 template <typename T>
-__device__ __forceinline__ void ls_dists(const ProblemDev& P, const OpDev& op, const uint32_t* colL,
-                                         const uint32_t* colR, int l, T th, T an, T th2, T an2, T* dist, int lane) {
+__device__ __forceinline__ void ls_dists(const ProblemDev& P, const OpDev& op, const int32_t* opd,
+                                         const uint32_t* colL, const uint32_t* colR, int l, T th, T an, T th2, T an2,
+                                         T* dist, int lane) {
     const int nch = op.type == CHILD ? 1 : (op.type == PARENT ? op.n_child : 0);
     if (lane < nch) {
-        const int person = op.type == CHILD ? op.peel : P.opdata[op.child_at + 4 * lane];
+        const int person = op.type == CHILD ? op.peel : opd[op.child_at + 4 * lane];
         ls_dist_one<T>(P, person, colL, colR, l, th, an, th2, an2, dist + 16 * lane);
     }
 }
@@ -160,7 +161,7 @@ __device__ __forceinline__ bool ls_valid(const int32_t* cut, int c, const uint8_
 // One presum entry (cell, peel state v) in the reference's product order
 // (sampler_rfunction.cc:190-287, rfunction.cc:116-142).
 template <typename T>
-__device__ T ls_term(const ProblemDev& P, const OpDev& op, const T* Am, const T* dist, int cell, int v, T tv) {
+__device__ T ls_term(const OpDev& op, const int32_t* opd, const T* Am, const T* dist, int cell, int v, T tv) {
     using A = Ls<T>;
     const int ext = cell | (v << (2 * op.c));
     T tmp = tv;
@@ -169,7 +170,7 @@ __device__ T ls_term(const ProblemDev& P, const OpDev& op, const T* Am, const T*
         const T tr = A::mul(dist[mt * 2 + mat_allele(v)], dist[8 + pt * 2 + pat_allele(v)]);
         tmp = A::mul(tmp, tr);
     }
-    const int32_t* pd = P.opdata + op.prev_at;
+    const int32_t* pd = opd + op.prev_at;
     for (int j = 0; j < op.n_prev; ++j) {
         const int moff = pd[0], pc = pd[1];
         int idx = 0;
@@ -179,7 +180,7 @@ __device__ T ls_term(const ProblemDev& P, const OpDev& op, const T* Am, const T*
     }
     if (op.type == PARENT) {
         T cp = T(1);
-        const int32_t* cd = P.opdata + op.child_at;
+        const int32_t* cd = opd + op.child_at;
         for (int c = 0; c < op.n_child; ++c, cd += 4) {
             const int kt = digit(ext, cd[1]), other = digit(ext, cd[2]);
             const int mt = cd[3] ? v : other, pt = cd[3] ? other : v;
@@ -193,14 +194,47 @@ __device__ T ls_term(const ProblemDev& P, const OpDev& op, const T* Am, const T*
 
 // A warp's shared bytes: the rfunctions [arena], the children's transmission
 // distributions [16 per child], the sampled states [N], the peel's draws [K]
-// (doubles, 16-byte aligned); a multiple of 16 so every warp's base is aligned.
+// (doubles), the locus's genotype codes and masks [N], its neighbours'
+// descent-graph words [2 W] and its prior row [16]; each part 16-byte aligned,
+// so every warp's base is aligned.
+__host__ __device__ __forceinline__ size_t al16(size_t x) { return (x + 15) & ~(size_t)15; }
 template <typename T>
 __host__ __device__ __forceinline__ size_t ls_draws_at(const ProblemDev& P) {
-    return ((size_t)P.arena * sizeof(T) + (size_t)P.max_child * 16 * sizeof(T) + (size_t)P.N + 15) & ~(size_t)15;
+    return al16((size_t)P.arena * sizeof(T) + (size_t)P.max_child * 16 * sizeof(T) + (size_t)P.N);
+}
+template <typename T>
+__host__ __device__ __forceinline__ size_t ls_gcol_at(const ProblemDev& P) {
+    return al16(ls_draws_at<T>(P) + 8 * (size_t)P.K);
+}
+template <typename T>
+__host__ __device__ __forceinline__ size_t ls_cols_at(const ProblemDev& P) {
+    return al16(ls_gcol_at<T>(P) + (size_t)P.N);
+}
+template <typename T>
+__host__ __device__ __forceinline__ size_t ls_pri_at(const ProblemDev& P) {
+    return al16(ls_cols_at<T>(P) + 8 * (size_t)P.W);
 }
 template <typename T>
 __host__ __device__ __forceinline__ size_t ls_warp_bytes(const ProblemDev& P) {
-    return (ls_draws_at<T>(P) + 8 * (size_t)P.K + 15) & ~(size_t)15;
+    return al16(ls_pri_at<T>(P) + 16 * sizeof(T));
+}
+
+// Block-shared copies of the peel's operations and their lists: every lane
+// reads them at every operation, and L1 holds little beside the arenas.
+__host__ __device__ __forceinline__ size_t ls_tables_bytes(const ProblemDev& P) {
+    return al16((size_t)P.K * sizeof(OpDev)) + al16((size_t)P.opdata_n * 4);
+}
+
+__device__ __forceinline__ void ls_stage_tables(const ProblemDev& P, unsigned char* smem, const OpDev*& ops,
+                                                const int32_t*& opd) {
+    int32_t* so = (int32_t*)smem;
+    int32_t* sd = (int32_t*)(smem + al16((size_t)P.K * sizeof(OpDev)));
+    const int32_t* src = (const int32_t*)P.ops;
+    const int nw = P.K * (int)(sizeof(OpDev) / 4);
+    for (int i = threadIdx.x; i < nw; i += blockDim.x) so[i] = src[i];
+    for (int i = threadIdx.x; i < P.opdata_n; i += blockDim.x) sd[i] = P.opdata[i];
+    ops = (const OpDev*)so;
+    opd = sd;
 }
 
 // One warp per (chain, locus) task; the listed loci must be pairwise
@@ -212,9 +246,9 @@ __host__ __device__ __forceinline__ size_t ls_warp_bytes(const ProblemDev& P) {
 // of the unit's stream.  Returns the number of draws used, or -1 when the
 // locus has likelihood 0; *logroot (lane 0) receives log of the peel's result.
 template <typename T>
-__device__ int ls_locus(const ProblemDev& P, uint32_t* dg, int cr, int chain, int l, bool hasL, bool hasR,
-                        const Draws& draws, int64_t unit, int64_t base, unsigned char* wsmem, int lane, int* status,
-                        double* logroot) {
+__device__ int ls_locus(const ProblemDev& P, const OpDev* ops, const int32_t* opd, uint32_t* dg, int cr, int chain,
+                        int l, bool hasL, bool hasR, const Draws& draws, int64_t unit, int64_t base,
+                        unsigned char* wsmem, int lane, int* status, double* logroot) {
     using Ar = Ls<T>;
     constexpr bool kRescale = sizeof(T) == 4;   // FP32: each rfunction scaled to a maximum of about 1
     T* A = (T*)wsmem;
@@ -222,8 +256,26 @@ __device__ int ls_locus(const ProblemDev& P, uint32_t* dg, int cr, int chain, in
     int8_t* assign = (int8_t*)(dist + 16 * P.max_child);
     double* sdraw = (double*)(wsmem + ls_draws_at<T>(P));
     uint32_t* colC = dg + ((size_t)chain * P.M + l) * P.W;
-    const uint32_t* colL = hasL ? colC - P.W : nullptr;
-    const uint32_t* colR = hasR ? colC + P.W : nullptr;
+    // the locus's inputs copied to the warp's shared memory first
+    uint8_t* sg = (uint8_t*)(wsmem + ls_gcol_at<T>(P));
+    uint32_t* sL = (uint32_t*)(wsmem + ls_cols_at<T>(P));
+    uint32_t* sR = sL + P.W;
+    T* spri = (T*)(wsmem + ls_pri_at<T>(P));
+    {
+        const uint8_t* gsrc = P.geno + (size_t)l * P.N;
+        for (int i = lane; i < P.N; i += 32) sg[i] = gsrc[i];
+        for (int w = lane; w < P.W; w += 32) {
+            if (hasL) sL[w] = colC[w - P.W];
+            if (hasR) sR[w] = colC[w + P.W];
+        }
+        if (lane < 16) {
+            if constexpr (sizeof(T) == 4) spri[lane] = (T)P.prior_f[(size_t)l * 16 + lane];
+            else spri[lane] = (T)P.prior[(size_t)l * 16 + lane];
+        }
+        __syncwarp();
+    }
+    const uint32_t* colL = hasL ? sL : nullptr;
+    const uint32_t* colR = hasR ? sR : nullptr;
     T th = T(1), an = T(1), th2 = T(1), an2 = T(1);
     if constexpr (sizeof(T) == 4) {
         const float* tf = P.c_theta_f + (size_t)chain * (P.M - 1);
@@ -234,18 +286,16 @@ __device__ int ls_locus(const ProblemDev& P, uint32_t* dg, int cr, int chain, in
         if (hasL) { th2 = td[l - 1]; an2 = DSUB(1.0, td[l - 1]); }
         if (hasR) { th = td[l]; an = DSUB(1.0, td[l]); }
     }
-    const uint8_t* gcol = P.geno + (size_t)l * P.N;
-    const T* pri;
-    if constexpr (sizeof(T) == 4) pri = (const T*)(P.prior_f + (size_t)l * 16);
-    else pri = (const T*)(P.prior + (size_t)l * 16);
+    const uint8_t* gcol = sg;
+    const T* pri = spri;
     int scale = 0;
     // forward peel over the valid cells of every rfunction
     for (int k = 0; k < P.K; ++k) {
-        const OpDev op = P.ops[k];
-        ls_dists<T>(P, op, colL, colR, l, th, an, th2, an2, dist, lane);
+        const OpDev op = ops[k];
+        ls_dists<T>(P, op, opd, colL, colR, l, th, an, th2, an2, dist, lane);
         __syncwarp();
         const int ncell = 1 << (2 * op.c);
-        const int32_t* cut = P.opdata + op.cut_at;
+        const int32_t* cut = opd + op.cut_at;
         const T* trait = pri + 4 * (gcol[op.peel] & 3);
         T* out = A + op.mat_off;
         T mx = T(0);
@@ -258,7 +308,7 @@ __device__ int ls_locus(const ProblemDev& P, uint32_t* dg, int cr, int chain, in
             const int cell = (it0 + lane) >> 2;
             T term = T(0);
             if (it0 + lane < nitem && tv != T(0) && ls_valid(cut, op.c, gcol, cell))
-                term = ls_term<T>(P, op, A, dist, cell, v, tv);
+                term = ls_term<T>(op, opd, A, dist, cell, v, tv);
             const T t0 = __shfl_sync(FULLMASK, term, grp), t1 = __shfl_sync(FULLMASK, term, grp + 1);
             const T t2 = __shfl_sync(FULLMASK, term, grp + 2), t3 = __shfl_sync(FULLMASK, term, grp + 3);
             if (v == 0 && it0 + lane < nitem) {
@@ -281,7 +331,7 @@ __device__ int ls_locus(const ProblemDev& P, uint32_t* dg, int cr, int chain, in
         }
         __syncwarp();
     }
-    const T root = A[P.ops[P.K - 1].mat_off];
+    const T root = A[ops[P.K - 1].mat_off];
     if (root == T(0)) {
         if (lane == 0) set_status(status, ST_ZERO_LIK);
         __syncwarp();
@@ -294,10 +344,10 @@ __device__ int ls_locus(const ProblemDev& P, uint32_t* dg, int cr, int chain, in
     __syncwarp();
     // backward sampling of ordered genotypes (SamplerRfunction::sample)
     for (int k = P.K - 1; k >= 0; --k) {
-        const OpDev op = P.ops[k];
-        ls_dists<T>(P, op, colL, colR, l, th, an, th2, an2, dist, lane);
+        const OpDev op = ops[k];
+        ls_dists<T>(P, op, opd, colL, colR, l, th, an, th2, an2, dist, lane);
         __syncwarp();
-        const int32_t* cut = P.opdata + op.cut_at;
+        const int32_t* cut = opd + op.cut_at;
         const T* trait = pri + 4 * (gcol[op.peel] & 3);
         int cellidx = 0;
         bool known = true;
@@ -309,7 +359,7 @@ __device__ int ls_locus(const ProblemDev& P, uint32_t* dg, int cr, int chain, in
         T pv = T(0);
         if (lane < 4 && known) {
             const T tv = trait[lane];
-            if (tv != T(0) && ls_valid(cut, op.c, gcol, cellidx)) pv = ls_term<T>(P, op, A, dist, cellidx, lane, tv);
+            if (tv != T(0) && ls_valid(cut, op.c, gcol, cellidx)) pv = ls_term<T>(op, opd, A, dist, cellidx, lane, tv);
         }
         const T p0 = __shfl_sync(FULLMASK, pv, 0), p1 = __shfl_sync(FULLMASK, pv, 1);
         const T p2 = __shfl_sync(FULLMASK, pv, 2), p3 = __shfl_sync(FULLMASK, pv, 3);
@@ -385,13 +435,18 @@ __global__ void __launch_bounds__(128) lsampler_kernel(ProblemDev P, uint32_t* d
                                                        const uint8_t* sel, int want, int* status) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int wpb = blockDim.x >> 5, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    unsigned char* wsmem = smem + (size_t)warp * ls_warp_bytes<T>(P);
+    const OpDev* ops;
+    const int32_t* opd;
+    ls_stage_tables(P, smem, ops, opd);
+    __syncthreads();
+    unsigned char* wsmem = smem + ls_tables_bytes(P) + (size_t)warp * ls_warp_bytes<T>(P);
     const int64_t ntask = (int64_t)nchain * nloci;
     for (int64_t t = (int64_t)blockIdx.x * wpb + warp; t < ntask; t += (int64_t)gridDim.x * wpb) {
         const int cr = (int)(t / nloci);
         if (sel && sel[cr] != want) continue;
         const int l = loci[t % nloci];
-        ls_locus<T>(P, dg, cr, first + cr, l, l > 0, l < P.M - 1, draws, l, 0, wsmem, lane, status, nullptr);
+        ls_locus<T>(P, ops, opd, dg, cr, first + cr, l, l > 0, l < P.M - 1, draws, l, 0, wsmem, lane, status,
+                    nullptr);
     }
 }
 
@@ -406,7 +461,11 @@ __global__ void __launch_bounds__(128) si_kernel(ProblemDev P, uint32_t* dg, int
                                                  int* status) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int wpb = blockDim.x >> 5, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    unsigned char* wsmem = smem + (size_t)warp * ls_warp_bytes<T>(P);
+    const OpDev* ops;
+    const int32_t* opd;
+    ls_stage_tables(P, smem, ops, opd);
+    __syncthreads();
+    unsigned char* wsmem = smem + ls_tables_bytes(P) + (size_t)warp * ls_warp_bytes<T>(P);
     for (int cr = blockIdx.x * wpb + warp; cr < nchain; cr += gridDim.x * wpb) {
         const int chain = first + cr, M = P.M, start = starts[cr];
         int64_t base = 0;
@@ -417,7 +476,8 @@ __global__ void __launch_bounds__(128) si_kernel(ProblemDev P, uint32_t* dg, int
             const bool hasL = v > start && l > 0;
             const bool hasR = v > 0 && v <= start && l < M - 1;
             double lr = 0.0;
-            const int used = ls_locus<T>(P, dg, cr, chain, l, hasL, hasR, draws, unit, base, wsmem, lane, status, &lr);
+            const int used = ls_locus<T>(P, ops, opd, dg, cr, chain, l, hasL, hasR, draws, unit, base, wsmem, lane,
+                                         status, &lr);
             if (used < 0) {
                 ok = false;
                 break;
@@ -2350,12 +2410,14 @@ size_t lsampler_smem_per_warp(const ProblemDev& P) {
     return P.ls_fast ? ls_warp_bytes<float>(P) : ls_warp_bytes<double>(P);
 }
 
+size_t lsampler_smem_shared(const ProblemDev& P) { return ls_tables_bytes(P); }
+
 
 cudaError_t launch_lsampler(const ProblemDev& P, uint32_t* dg, int first, int nchain, const int32_t* loci, int nloci,
                             const double* u, int64_t ucs, int64_t uls, uint64_t seed, uint64_t iter,
                             const uint8_t* sel, int want, int* status, cudaStream_t s, int grid_cap, int wpb,
                             const uint64_t* key) {
-    const size_t smem = wpb * lsampler_smem_per_warp(P);
+    const size_t smem = ls_tables_bytes(P) + wpb * lsampler_smem_per_warp(P);
     static size_t configured[2] = {0, 0};
     const int f = P.ls_fast ? 1 : 0;
     if (smem > configured[f]) {
@@ -2399,7 +2461,7 @@ __global__ void si_select_kernel(const uint32_t* scratch, uint32_t* dg, int firs
 cudaError_t launch_si(const ProblemDev& P, uint32_t* dg, int first, int nchain, const int32_t* starts,
                       const double* u, int64_t ucs, uint64_t seed, uint64_t pass, double* weights, int* status,
                       cudaStream_t s, int wpb) {
-    const size_t smem = wpb * lsampler_smem_per_warp(P);
+    const size_t smem = ls_tables_bytes(P) + wpb * lsampler_smem_per_warp(P);
     static size_t configured[2] = {0, 0};
     const int f = P.ls_fast ? 1 : 0;
     if (smem > configured[f]) {
