@@ -106,7 +106,17 @@ typedef struct sl_options {
     int32_t sampler_precision;  /* SL_SAMPLER_EXACT or SL_SAMPLER_FAST */
     int32_t lod_kernel;         /* SL_LOD_KERNEL_*: the batched scorer's kernel (0 = timed choice) */
     int32_t lod_flags;          /* SL_LOD_ZERO_OK or 0 */
+    int32_t ls_kernel;          /* SL_LS_KERNEL_*: the FP32 L-sampler's kernel */
 } sl_options;
+
+/* Kernels of the FP32 L-sampler (SL_SAMPLER_FAST).  GENERIC interprets the
+ * peel operations.  SPECIALISED compiles, at sl_create, a kernel with the
+ * pedigree's operations written in as constants (NVRTC for sm_103a: seconds to
+ * tens of seconds for a 100-member pedigree; sl_create fails if it does not
+ * build); it performs the same rounded operations in the same order, so both
+ * draw bit-identical graphs, and it pays off on long runs. */
+#define SL_LS_KERNEL_GENERIC 0
+#define SL_LS_KERNEL_SPECIALISED 1
 
 /* A LOD position whose trait likelihood is 0 (an affected and an unaffected
  * member IBD 2 under a fully penetrant model, for instance) stops the
@@ -340,6 +350,10 @@ int sl_problem_trait_backward_eval(const sl_problem_desc* problem, const int32_t
  * scoring has timed the candidates) and the milliseconds spent compiling the
  * specialised forms at sl_create. */
 int sl_lod_kernel_info(sl_ctx* ctx, int32_t* kernel, double* compile_ms);
+
+/* The L-sampler kernel in use (SL_LS_KERNEL_GENERIC or SL_LS_KERNEL_SPECIALISED)
+ * and the milliseconds spent compiling the specialised form at sl_create. */
+int sl_ls_kernel_info(sl_ctx* ctx, int32_t* kernel, double* compile_ms);
 
 /*
  * A peel sequence for a pedigree (members founders first, mother/father -1 for

@@ -21,6 +21,7 @@ SL_LOD_FP64, SL_LOD_FP32_RESCALED, SL_LOD_FP64_RESCALED = 0, 1, 2
 SL_SAMPLER_EXACT, SL_SAMPLER_FAST = 0, 1
 SL_LOD_KERNEL_AUTO, SL_LOD_KERNEL_INTERP, SL_LOD_KERNEL_JIT_REG, SL_LOD_KERNEL_JIT_SMEM = 0, 1, 2, 3
 SL_LOD_ZERO_OK = 1
+SL_LS_KERNEL_GENERIC, SL_LS_KERNEL_SPECIALISED = 0, 1
 
 EXPORTED = [
     "sl_create", "sl_destroy", "sl_last_error", "sl_set_descent_graphs", "sl_get_descent_graphs",
@@ -29,7 +30,7 @@ EXPORTED = [
     "sl_lod_reset", "sl_run", "sl_synchronize", "sl_device_status", "sl_launch_count",
     "sl_version", "sl_get_stream", "sl_profile", "sl_profile_read", "sl_problem_legal_masks",
     "sl_problem_trait_priors", "sl_problem_trait_prob", "sl_trait_backward",
-    "sl_problem_trait_backward_eval", "sl_lod_kernel_info", "sl_set_temperatures", "sl_mc3_stats",
+    "sl_problem_trait_backward_eval", "sl_lod_kernel_info", "sl_ls_kernel_info", "sl_set_temperatures", "sl_mc3_stats",
     "sl_chain_loglik", "sl_peel_sequence", "sl_batch_create", "sl_batch_run", "sl_batch_destroy",
     "sl_sequential_imputation", "sl_sequential_imputation_run",
 ]
@@ -60,7 +61,7 @@ class ProblemDesc(ctypes.Structure):
 class Options(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int32), ("n_chains", ctypes.c_int32),
                 ("lod_precision", ctypes.c_int32), ("sampler_precision", ctypes.c_int32),
-                ("lod_kernel", ctypes.c_int32), ("lod_flags", ctypes.c_int32)]
+                ("lod_kernel", ctypes.c_int32), ("lod_flags", ctypes.c_int32), ("ls_kernel", ctypes.c_int32)]
 
 
 class RunOptions(ctypes.Structure):
@@ -206,10 +207,10 @@ class Context:
 
     def __init__(self, problem: Problem, n_chains: int = 1, lod_precision: int = SL_LOD_FP64,
                  device: int = 0, sampler_precision: int = SL_SAMPLER_EXACT, lod_kernel: int = SL_LOD_KERNEL_AUTO,
-                 lod_flags: int = 0):
+                 lod_flags: int = 0, ls_kernel: int = SL_LS_KERNEL_GENERIC):
         self.problem = problem
         self._desc = problem.desc()
-        opt = Options(device, n_chains, lod_precision, sampler_precision, lod_kernel, lod_flags)
+        opt = Options(device, n_chains, lod_precision, sampler_precision, lod_kernel, lod_flags, ls_kernel)
         h = _vp()
         rc = lib().sl_create(ctypes.byref(self._desc), ctypes.byref(opt), ctypes.byref(h))
         if rc != SL_OK:
@@ -304,6 +305,13 @@ class Context:
 
     def lod_reset(self):
         self._check(lib().sl_lod_reset(self.h))
+
+    def ls_kernel_info(self):
+        """(SL_LS_KERNEL_GENERIC or SL_LS_KERNEL_SPECIALISED in use, milliseconds spent compiling it)."""
+        k = ctypes.c_int32()
+        ms = ctypes.c_double()
+        self._check(lib().sl_ls_kernel_info(self.h, ctypes.byref(k), ctypes.byref(ms)))
+        return k.value, ms.value
 
     def lod_kernel_info(self):
         """(SL_LOD_KERNEL_* in use, milliseconds spent compiling specialised forms)."""

@@ -1,6 +1,6 @@
 """Build the in-tree CUDA library swiftlink_gb300/_build/libswiftlink_gb300.so.
 
-Five translation units compiled in parallel for sm_103a only, then linked
+Six translation units compiled in parallel for sm_103a only, then linked
 with the static CUDA runtime and NVRTC (which compiles the problem-specialised
 LOD kernels when a context is created):
   csrc/sl_kernels.cu  (nvcc, -gencode arch=compute_103a,code=sm_103a)
@@ -8,6 +8,9 @@ LOD kernels when a context is created):
   csrc/sl_host.cc     (g++ against the CUDA runtime headers)
   csrc/sl_jit.cc      (g++, NVRTC source generator and loader)
   csrc/sl_peel.cc     (g++, peel-sequence generator)
+  csrc/sl_lsjit.cc    (g++, the L-sampler specialised per pedigree, NVRTC;
+                       it embeds csrc/sl_philox.cuh, the Philox shared with
+                       sl_kernels.cu, as a string generated into _build)
 and the program swiftlink_gb300/_build/swift_gb300 (csrc/sl_cli.cc, the
 LINKAGE-file front end) linked against the library.
 """
@@ -55,8 +58,16 @@ def build(verbose: bool = False, force: bool = False) -> str:
     cuda = _cuda_home()
     nvcc = os.path.join(cuda, "bin", "nvcc")
     os.makedirs(OUT, exist_ok=True)
-    hdrs = [os.path.join(CSRC, "sl_internal.h"), os.path.join(CSRC, "sl_jit.h"),
-            os.path.join(os.path.dirname(HERE), "include", "swiftlink_gb300.h")]
+    philox = os.path.join(CSRC, "sl_philox.cuh")
+    hdrs = [os.path.join(CSRC, "sl_internal.h"), os.path.join(CSRC, "sl_jit.h"), os.path.join(CSRC, "sl_lsjit.h"),
+            philox, os.path.join(os.path.dirname(HERE), "include", "swiftlink_gb300.h")]
+    # the Philox source as a C++ string literal, for the run-time compiled kernels
+    inc = os.path.join(OUT, "sl_philox_src.inc")
+    if force or _stale(inc, [philox]):
+        with open(philox) as f:
+            text = f.read()
+        with open(inc, "w") as f:
+            f.write('R"SLPHILOX(' + text + ')SLPHILOX"\n')
     cu = os.path.join(CSRC, "sl_kernels.cu")
     cu2 = os.path.join(CSRC, "sl_noalloc.cu")
     cc = os.path.join(CSRC, "sl_host.cc")
@@ -64,6 +75,8 @@ def build(verbose: bool = False, force: bool = False) -> str:
     jc_o = os.path.join(OUT, "sl_jit.o")
     pc = os.path.join(CSRC, "sl_peel.cc")
     pc_o = os.path.join(OUT, "sl_peel.o")
+    lj = os.path.join(CSRC, "sl_lsjit.cc")
+    lj_o = os.path.join(OUT, "sl_lsjit.o")
     cli = os.path.join(CSRC, "sl_cli.cc")
     cli_o = os.path.join(OUT, "sl_cli.o")
     cu_o = os.path.join(OUT, "sl_kernels.o")
@@ -74,20 +87,20 @@ def build(verbose: bool = False, force: bool = False) -> str:
         if force or _stale(obj, [src] + hdrs):
             jobs.append([nvcc, GENCODE, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                          "-Xptxas", "-v", "-c", src, "-o", obj])
-    for src, obj in ((cc, cc_o), (jc, jc_o), (pc, pc_o), (cli, cli_o)):
-        if force or _stale(obj, [src] + hdrs):
+    for src, obj in ((cc, cc_o), (jc, jc_o), (pc, pc_o), (cli, cli_o), (lj, lj_o)):
+        if force or _stale(obj, [src] + hdrs + ([inc] if src == lj else [])):
             # no contraction of a * b + c into FMA: host FP64 (priors, tempered maps,
             # likelihood sums) must round as the reference's x86-64 build does, on aarch64 too
             jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-Wall", "-ffp-contract=off",
-                         "-I" + os.path.join(cuda, "include"),
+                         "-I" + os.path.join(cuda, "include"), "-I" + OUT,
                          "-c", src, "-o", obj])
     logs = []
     if jobs:
         with cf.ThreadPoolExecutor(len(jobs)) as ex:
             logs = list(ex.map(_run, jobs))
-    if force or jobs or _stale(LIB, [cu_o, cu2_o, cc_o, jc_o, pc_o]):
+    if force or jobs or _stale(LIB, [cu_o, cu2_o, cc_o, jc_o, pc_o, lj_o]):
         lib64 = os.path.join(cuda, "lib64")
-        logs.append(_run([nvcc, GENCODE, "-shared", "-cudart", "static", "-o", LIB, cu_o, cu2_o, cc_o, jc_o, pc_o,
+        logs.append(_run([nvcc, GENCODE, "-shared", "-cudart", "static", "-o", LIB, cu_o, cu2_o, cc_o, jc_o, pc_o, lj_o,
                           "-L" + lib64, "-lnvrtc", "-Xlinker", "-rpath=" + lib64]))
     if force or _stale(CLI, [cli_o, LIB]):
         lib64 = os.path.join(cuda, "lib64")

@@ -21,6 +21,7 @@
 #include "../../include/swiftlink_gb300.h"
 #include "sl_internal.h"
 #include "sl_jit.h"
+#include "sl_lsjit.h"
 
 namespace sl {
 // kernels (sl_kernels.cu)
@@ -151,6 +152,8 @@ struct sl_ctx {
     int64_t adj_chunk = 0;
     // batched LOD kernel: the interpreter, or a problem-specialised form
     int lod_kernel_req = SL_LOD_KERNEL_AUTO;
+    JitLs jit_ls;                     // the FP32 L-sampler specialised to the pedigree (kern null: generic)
+    double jit_ls_ms = 0.0;
     int lod_kernel_sel = SL_LOD_KERNEL_INTERP;   // AUTO while the first scoring has not timed them
     JitLod jit_reg, jit_smem;
     double jit_ms = 0.0;
@@ -184,6 +187,19 @@ static int64_t msweep_kernels(const sl_ctx*, int nm) { return 1 + 2 * (int64_t)n
 // instructions per locus, a longer launch) when the context holds enough
 // chains for the GPU to be throughput-bound.
 static int msampler_pairs(const sl_ctx* ctx) { return ctx->n_chains >= 8 ? 1 : 0; }
+
+// An L-sampler launch: the kernel specialised to the pedigree when it was
+// built, else the generic one.
+static cudaError_t ls_launch(sl_ctx* ctx, int first, int nchain, const int32_t* loci, int nloci, const double* u,
+                             int64_t ucs, int64_t uls, uint64_t seed, uint64_t iter, const uint8_t* sel, int want,
+                             cudaStream_t s, const uint64_t* key = nullptr) {
+    const ProblemDev& P = ctx->P;
+    if (ctx->jit_ls.kern)
+        return jit_ls_launch(ctx->jit_ls, ctx->d_dg, first, nchain, loci, nloci, u, ucs, uls, seed, iter, key, sel,
+                             want, ctx->d_status, P.geno, P.prior_f, P.c_theta_f, ctx->sms, s);
+    return launch_lsampler(P, ctx->d_dg, first, nchain, loci, nloci, u, ucs, uls, seed, iter, sel, want, ctx->d_status,
+                           s, ctx->ls_grid, ctx->ls_wpb, key);
+}
 
 struct Prof {
     sl_ctx* c;
@@ -996,6 +1012,7 @@ void sl_destroy(sl_ctx* ctx) {
     if (ctx->lstream) cudaStreamDestroy(ctx->lstream);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     jit_lod_release(&ctx->jit_reg);
+    jit_ls_release(&ctx->jit_ls);
     jit_lod_release(&ctx->jit_smem);
     if (ctx->ms_graph) cudaGraphExecDestroy(ctx->ms_graph);
     if (ctx->run_graph) cudaGraphExecDestroy(ctx->run_graph);
@@ -1276,6 +1293,19 @@ int sl_create(const sl_problem_desc* d, const sl_options* opt, sl_ctx** out) {
         else if (req == SL_LOD_KERNEL_AUTO) ctx->lod_kernel_sel = SL_LOD_KERNEL_AUTO;
         else ctx->lod_kernel_sel = req;
     }
+    {   // the FP32 L-sampler specialised to the pedigree, on request
+        const int req = opt->ls_kernel;
+        if (req != SL_LS_KERNEL_GENERIC && req != SL_LS_KERNEL_SPECIALISED)
+            return bail(fail(nullptr, SL_EINVAL, "unknown ls_kernel %d", req));
+        if (P.ls_fast && req == SL_LS_KERNEL_SPECIALISED) {
+            const JitLsIn in{ops.data(), od.data(), K, N, F, M, P.W, N - F, arena, max_child, d->mother, d->father};
+            const auto t0 = std::chrono::steady_clock::now();
+            std::string log;
+            if (jit_ls_compile(in, ctx->ls_wpb, &ctx->jit_ls, &log))
+                return bail(fail(nullptr, SL_EINVAL, "specialised L-sampler failed: %.300s", log.c_str()));
+            ctx->jit_ls_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        }
+    }
     if (d->affection) {
         LodProgram full;
         compile_lod_program(d, ops, od, full, true);
@@ -1440,8 +1470,8 @@ int sl_lsampler_loci(sl_ctx* ctx, int32_t first, int32_t n_chains, const int32_t
     if ((rc = stage_draws(ctx, u, (size_t)n_chains * ucs))) return rc;
     CK(cudaMemcpyAsync(ctx->d_loci, loci, sizeof(int32_t) * n_loci, cudaMemcpyHostToDevice, ctx->stream));
     { Prof pf_(ctx, SL_KERNEL_LSAMPLER);
-      CK(launch_lsampler(P, ctx->d_dg, first, n_chains, ctx->d_loci, n_loci, ctx->d_u, ucs, uls, 0, 0, nullptr, 0,
-                       ctx->d_status, ctx->stream, ctx->ls_grid, ctx->ls_wpb));
+      CK(ls_launch(ctx, first, n_chains, ctx->d_loci, n_loci, ctx->d_u, ucs, uls, 0, 0, nullptr, 0,
+                       ctx->stream));
     }
     return sl_synchronize(ctx);
 }
@@ -1456,12 +1486,12 @@ int sl_lsampler_sweep(sl_ctx* ctx, int32_t first, int32_t n_chains, const double
     CK(cudaSetDevice(ctx->device));
     if ((rc = stage_draws(ctx, u, (size_t)n_chains * ucs))) return rc;
     { Prof pf_(ctx, SL_KERNEL_LSAMPLER);
-      CK(launch_lsampler(P, ctx->d_dg, first, n_chains, ctx->d_even, (int)ctx->even.size(), ctx->d_u, ucs, uls, 0, 0,
-                       nullptr, 0, ctx->d_status, ctx->stream, ctx->ls_grid, ctx->ls_wpb));
+      CK(ls_launch(ctx, first, n_chains, ctx->d_even, (int)ctx->even.size(), ctx->d_u, ucs, uls, 0, 0,
+                       nullptr, 0, ctx->stream));
     }
     { Prof pf_(ctx, SL_KERNEL_LSAMPLER);
-      CK(launch_lsampler(P, ctx->d_dg, first, n_chains, ctx->d_odd, (int)ctx->odd.size(), ctx->d_u, ucs, uls, 0, 0,
-                       nullptr, 0, ctx->d_status, ctx->stream, ctx->ls_grid, ctx->ls_wpb));
+      CK(ls_launch(ctx, first, n_chains, ctx->d_odd, (int)ctx->odd.size(), ctx->d_u, ucs, uls, 0, 0,
+                       nullptr, 0, ctx->stream));
     }
     return sl_synchronize(ctx);
 }
@@ -1826,6 +1856,13 @@ int sl_set_temperatures(sl_ctx* ctx, const double* temps) {
     return upload_chain_maps(ctx);
 }
 
+int sl_ls_kernel_info(sl_ctx* ctx, int32_t* kernel, double* compile_ms) {
+    if (!ctx) return fail(ctx, SL_EINVAL, "null context");
+    if (kernel) *kernel = ctx->jit_ls.kern ? SL_LS_KERNEL_SPECIALISED : SL_LS_KERNEL_GENERIC;
+    if (compile_ms) *compile_ms = ctx->jit_ls_ms;
+    return SL_OK;
+}
+
 int sl_lod_kernel_info(sl_ctx* ctx, int32_t* kernel, double* compile_ms) {
     if (!ctx) return fail(ctx, SL_EINVAL, "null context");
     if (kernel) *kernel = ctx->lod_precision == SL_LOD_FP32_RESCALED ? ctx->lod_kernel_sel : SL_LOD_KERNEL_INTERP;
@@ -1966,11 +2003,11 @@ static cudaError_t capture_chain_body(sl_ctx* ctx, int c, cudaGraph_t body, cuda
     if ((e = capture_conditional(s1, hsw, cudaGraphCondTypeSwitch, 2, sw)) != cudaSuccess) return e;
     // L-sweep of chain c
     if ((e = cudaStreamBeginCaptureToGraph(s2, sw[0], nullptr, nullptr, 0, mode)) != cudaSuccess) return e;
-    e = launch_lsampler(P, ctx->d_dg, c, 1, ctx->d_even, (int)ctx->even.size(), nullptr, 0, 0, 0, 0, nullptr, 1,
-                        ctx->d_status, s2, ctx->ls_grid, ctx->ls_wpb, key);
+    e = ls_launch(ctx, c, 1, ctx->d_even, (int)ctx->even.size(), nullptr, 0, 0, 0, 0, nullptr, 1,
+                        s2, key);
     if (e == cudaSuccess)
-        e = launch_lsampler(P, ctx->d_dg, c, 1, ctx->d_odd, (int)ctx->odd.size(), nullptr, 0, 0, 0, 0, nullptr, 1,
-                            ctx->d_status, s2, ctx->ls_grid, ctx->ls_wpb, key);
+        e = ls_launch(ctx, c, 1, ctx->d_odd, (int)ctx->odd.size(), nullptr, 0, 0, 0, 0, nullptr, 1,
+                            s2, key);
     cudaError_t e2 = cudaStreamEndCapture(s2, &sw[0]);
     if (e != cudaSuccess || (e = e2) != cudaSuccess) return e;
     // M-sweep of chain c
@@ -2025,8 +2062,8 @@ static int prepare_run_graph(sl_ctx* ctx) {
     CK(launch_msampler(P, ctx->d_dg, 0, C, ctx->d_morder, nm, 0, nullptr, 0, 0, 0, ctx->d_sel, 2, ctx->d_raw,
                        ctx->d_raw32, ctx->d_fb, ctx->d_badc, ctx->d_maps, ctx->d_status, ctx->ms_threads, exact ? 1 : 0,
                        ctx->stream, ctx->d_keys, ctx->d_mu, msampler_pairs(ctx)));
-    CK(launch_lsampler(P, ctx->d_dg, 0, C, ctx->d_even, (int)ctx->even.size(), nullptr, 0, 0, 0, 0, ctx->d_sel, 2,
-                       ctx->d_status, ctx->stream, ctx->ls_grid, ctx->ls_wpb, ctx->d_keys));
+    CK(ls_launch(ctx, 0, C, ctx->d_even, (int)ctx->even.size(), nullptr, 0, 0, 0, 0, ctx->d_sel, 2,
+                       ctx->stream, ctx->d_keys));
     // the scoring kernel is fixed in the graph: time the candidates now if needed
     if (ctx->lod_precision == SL_LOD_FP32_RESCALED && ctx->lod_kernel_sel == SL_LOD_KERNEL_AUTO) {
         int st = 0;
@@ -2303,11 +2340,11 @@ static int run_span(sl_ctx* ctx, const sl_run_options* o, int first, int end) {
         CK(cudaEventRecord(ctx->ev_fork, ctx->stream));
         CK(cudaStreamWaitEvent(ctx->lstream, ctx->ev_fork, 0));
         { Prof pf_(ctx, SL_KERNEL_LSAMPLER, ctx->lstream);
-            CK(launch_lsampler(P, ctx->d_dg, 0, C, ctx->d_even, (int)ctx->even.size(), nullptr, 0, 0, o->seed, iter,
-                               ctx->d_sel, 1, ctx->d_status, ctx->lstream, ctx->ls_grid, ctx->ls_wpb)); }
+            CK(ls_launch(ctx, 0, C, ctx->d_even, (int)ctx->even.size(), nullptr, 0, 0, o->seed, iter,
+                               ctx->d_sel, 1, ctx->lstream)); }
         { Prof pf_(ctx, SL_KERNEL_LSAMPLER, ctx->lstream);
-            CK(launch_lsampler(P, ctx->d_dg, 0, C, ctx->d_odd, (int)ctx->odd.size(), nullptr, 0, 0, o->seed, iter,
-                               ctx->d_sel, 1, ctx->d_status, ctx->lstream, ctx->ls_grid, ctx->ls_wpb)); }
+            CK(ls_launch(ctx, 0, C, ctx->d_odd, (int)ctx->odd.size(), nullptr, 0, 0, o->seed, iter,
+                               ctx->d_sel, 1, ctx->lstream)); }
         { Prof pf_(ctx, SL_KERNEL_MSAMPLER);
             CK(launch_set_key(ctx->d_key, o->seed, iter, ctx->stream));
             CK(cudaGraphLaunch(ctx->ms_graph, ctx->stream));

@@ -185,9 +185,12 @@ std::string jit_source(const JitProgramIn& in, int threads, bool shared) {
     return s;
 }
 
-int compile_one(const std::string& src, const char* name, JitLod* out, std::string* log) {
+}  // namespace
+
+int jit_compile_kernel(const std::string& src, const char* file, const char* kernel, void** lib_out, void** kern_out,
+                       std::string* log) {
     nvrtcProgram prog;
-    if (nvrtcCreateProgram(&prog, src.c_str(), name, 0, nullptr, nullptr) != NVRTC_SUCCESS) {
+    if (nvrtcCreateProgram(&prog, src.c_str(), file, 0, nullptr, nullptr) != NVRTC_SUCCESS) {
         *log = "nvrtcCreateProgram failed";
         return -1;
     }
@@ -217,18 +220,16 @@ int compile_one(const std::string& src, const char* name, JitLod* out, std::stri
         return -1;
     }
     cudaKernel_t k = nullptr;
-    e = cudaLibraryGetKernel(&k, lib, "sl_lod_jit");
+    e = cudaLibraryGetKernel(&k, lib, kernel);
     if (e != cudaSuccess) {
         cudaLibraryUnload(lib);
         *log = std::string("cudaLibraryGetKernel: ") + cudaGetErrorString(e);
         return -1;
     }
-    out->lib = lib;
-    out->kern = (void*)k;
+    *lib_out = lib;
+    *kern_out = (void*)k;
     return 0;
 }
-
-}  // namespace
 
 std::string jit_lod_source(const JitProgramIn& in, int threads, bool shared) {
     return jit_source(in, threads, shared);
@@ -238,7 +239,9 @@ int jit_lod_compile(const JitProgramIn& in, int threads, bool shared, JitLod* ou
     *out = JitLod{};
     const auto t0 = std::chrono::steady_clock::now();
     const std::string src = jit_source(in, threads, shared);
-    if (compile_one(src, shared ? "sl_lod_jit_smem.cu" : "sl_lod_jit_reg.cu", out, log)) return -1;
+    if (jit_compile_kernel(src, shared ? "sl_lod_jit_smem.cu" : "sl_lod_jit_reg.cu", "sl_lod_jit", &out->lib,
+                           &out->kern, log))
+        return -1;
     out->threads = threads;
     out->shared = shared;
     out->smem = shared ? (size_t)threads * in.slots * sizeof(float) : 0;

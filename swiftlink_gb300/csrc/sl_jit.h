@@ -31,6 +31,11 @@ struct JitLod {
     double compile_ms = 0.0;
 };
 
+// NVRTC-compile `src` for sm_103a and load `kernel` from it (a cudaLibrary_t
+// and a cudaKernel_t); 0 on success, else -1 with the reason in *log.
+int jit_compile_kernel(const std::string& src, const char* file, const char* kernel, void** lib, void** kern,
+                       std::string* log);
+
 std::string jit_lod_source(const JitProgramIn& in, int threads, bool shared);
 int jit_lod_compile(const JitProgramIn& in, int threads, bool shared, JitLod* out, std::string* log);
 void jit_lod_release(JitLod* j);

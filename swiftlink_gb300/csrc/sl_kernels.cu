@@ -20,6 +20,7 @@
 #include <stdint.h>
 
 #include "sl_internal.h"
+#include "sl_philox.cuh"
 
 namespace sl {
 
@@ -37,28 +38,8 @@ __device__ __forceinline__ void set_status(int* st, int code) { atomicCAS(st, 0,
 __device__ __forceinline__ int mat_allele(int s) { return (s == AA || s == AU) ? 1 : 0; }
 __device__ __forceinline__ int pat_allele(int s) { return (s == AA || s == UA) ? 1 : 0; }
 
-// ---------------------------------------------------------------------------
-// Philox4x32-10 (Salmon et al., SC'11): counter-based uniform in [0, 1).
-// ---------------------------------------------------------------------------
 __device__ __forceinline__ double philox_u01(uint64_t key, uint64_t c_hi, uint64_t c_lo) {
-    uint32_t c0 = (uint32_t)c_lo, c1 = (uint32_t)(c_lo >> 32);
-    uint32_t c2 = (uint32_t)c_hi, c3 = (uint32_t)(c_hi >> 32);
-    uint32_t k0 = (uint32_t)key, k1 = (uint32_t)(key >> 32);
-#pragma unroll
-    for (int r = 0; r < 10; ++r) {
-        uint32_t hi0 = __umulhi(0xD2511F53u, c0), lo0 = 0xD2511F53u * c0;
-        uint32_t hi1 = __umulhi(0xCD9E8D57u, c2), lo1 = 0xCD9E8D57u * c2;
-        uint32_t n0 = hi1 ^ c1 ^ k0;
-        uint32_t n2 = hi0 ^ c3 ^ k1;
-        c1 = lo1;
-        c3 = lo0;
-        c0 = n0;
-        c2 = n2;
-        k0 += 0x9E3779B9u;
-        k1 += 0xBB67AE85u;
-    }
-    uint64_t hi = c0 >> 5, lo = c1 >> 6;
-    return (double)(hi * 67108864ull + lo) * (1.0 / 9007199254740992.0);
+    return sl_philox_u01(key, c_hi, c_lo);
 }
 
 // Where uniform draws come from: a caller-supplied array (bit-exact replay of
@@ -97,11 +78,11 @@ struct Ls<double> {
     static __device__ __forceinline__ double div(double a, double b) { return DDIV(a, b); }
 };
 template <>
-struct Ls<float> {
-    static __device__ __forceinline__ float mul(float a, float b) { return a * b; }
-    static __device__ __forceinline__ float add(float a, float b) { return a + b; }
-    static __device__ __forceinline__ float sub(float a, float b) { return a - b; }
-    static __device__ __forceinline__ float div(float a, float b) { return a / b; }
+struct Ls<float> {   // rounded operations, never contracted: the kernel specialised at run time matches them
+    static __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
+    static __device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
+    static __device__ __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
+    static __device__ __forceinline__ float div(float a, float b) { return __fdiv_rn(a, b); }
 };
 
 // ---------------------------------------------------------------------------
@@ -325,7 +306,11 @@ __device__ int ls_locus(const ProblemDev& P, const OpDev* ops, const int32_t* op
                 mx = o > mx ? o : mx;
             }
             if (mx > T(0)) {
-                const float f = scalbnf(1.0f, -ilogbf((float)mx));
+                // every rfunction enters the root exactly once, so the root's
+                // logarithm is the scaled root's plus the removed exponents
+                const int ex = ilogbf((float)mx);
+                scale += ex;
+                const float f = scalbnf(1.0f, -ex);
                 for (int cell = lane; cell < ncell; cell += 32) out[cell] = (T)((float)out[cell] * f);
             }
         }

@@ -400,3 +400,28 @@ def test_fp64_rescaled_lod_equals_plain(name):
         raw, cnt, tp = ctx.lod_results()
     want = api.lod_table(g["lod_raw"], g["lod_count"], g["lod_trait_prob"])
     assert np.abs(api.lod_table(raw, cnt, tp) - want).max() <= FP64_LOD_TOL
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["loop", "east", "cfg1"])
+def test_specialised_lsampler_is_bit_identical(name):
+    """The L-sampler compiled for the pedigree (operations as constants) and
+    the generic one perform the same rounded FP32 operations in the same
+    order: on the same graphs and draws, explicit or from the Philox stream,
+    they leave bit-identical graphs."""
+    g = load_golden(name)
+    C = 3
+    u = np.random.default_rng(23).random((C, g["M"], g["K"] + 2 * g["N"]))
+    out = {}
+    for lk in (api.SL_LS_KERNEL_GENERIC, api.SL_LS_KERNEL_SPECIALISED):
+        with api.Context(api.Problem.from_arrays(g), n_chains=C, sampler_precision=api.SL_SAMPLER_FAST,
+                         ls_kernel=lk) as ctx:
+            assert ctx.ls_kernel_info()[0] == lk
+            ctx.set_graphs(np.stack([g["dg0"]] * C))
+            ctx.lsampler_sweep(u, 0, C)
+            swept = ctx.get_graphs()
+            ctx.run(iterations=12, burnin=0, period=4, lprob=1.0, seed=9)
+            out[lk] = (swept, ctx.get_graphs())
+    a, b = out[api.SL_LS_KERNEL_GENERIC], out[api.SL_LS_KERNEL_SPECIALISED]
+    assert np.array_equal(a[0], b[0])
+    assert np.array_equal(a[1], b[1])

@@ -5,8 +5,10 @@ start locus with neither neighbour, then the loci to its left with only the
 right neighbour, then those to its right with only the left neighbour, each a
 full L-sampler step; the weight is the sum of the log peel results.  The
 oracle's pass equals the reference's own (same start, same draws) bit for bit;
-the device pass (exact mode) equals the oracle's; the Philox-driven best-of-n
-run leaves every chain with a legal graph.
+the device pass (exact mode) equals the oracle's; in the FP32 mode (every
+rfunction rescaled by a power of two) the weights keep the removed exponents,
+so they match the oracle's to FP32 accuracy; the Philox-driven best-of-n run
+leaves every chain with a legal graph.
 """
 import numpy as np
 import pytest
@@ -53,6 +55,35 @@ def test_device_pass_equals_oracle(name):
         dg, _, want_w = P.si(np.zeros((g["M"], g["N"], 2), np.int32), int(starts[c]), u[c])
         assert np.array_equal(out[c], dg), c
         assert abs(w[c] - want_w) <= 1e-12 * abs(want_w)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["east", "cfg1"])
+def test_fast_pass_weights_match_oracle(name):
+    """The FP32 pass's weights against the FP64 pass's on the same start
+    loci and draws: equal to FP32 accuracy where both drew the same graph, of
+    the same magnitude where a near-tie drew differently.  Rescaled
+    rfunctions would leave the FP32 weights short by every removed exponent
+    (tens of natural-log units per locus)."""
+    g = load_golden(name)
+    C = 3
+    rng = np.random.default_rng(8)
+    starts = np.array([0, g["M"] // 2, g["M"] - 1], np.int32)
+    L = g["M"] * (g["K"] + 2 * g["N"])
+    u = rng.random((C, L))
+    out = {}
+    for prec in (api.SL_SAMPLER_EXACT, api.SL_SAMPLER_FAST):
+        with api.Context(api.Problem.from_arrays(g), n_chains=C, sampler_precision=prec) as ctx:
+            ctx.set_graphs(np.zeros((C, g["M"], g["N"], 2), np.int32))
+            w = ctx.sequential_imputation(starts, u)
+            out[prec] = (w, ctx.get_graphs())
+    we, ge = out[api.SL_SAMPLER_EXACT]
+    wf, gf = out[api.SL_SAMPLER_FAST]
+    for c in range(C):
+        if np.array_equal(ge[c], gf[c]):   # same graph: same weight up to FP32 rounding
+            assert abs(wf[c] - we[c]) <= 1e-4 * abs(we[c]) + 1e-3, (c, wf[c], we[c])
+        else:                              # a near-tie drew differently: same order of magnitude
+            assert abs(wf[c] - we[c]) <= 0.05 * abs(we[c]), (c, wf[c], we[c])
 
 
 @pytest.mark.gpu
