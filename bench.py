@@ -39,6 +39,7 @@ METRIC = "descent-graph steps/s + LOD positions/s, batched vs plain GB300, |ΔLO
 UNIT = "steps/s"
 CHAINS = 10
 PERIOD = 100
+STEP_ITERS = PERIOD   # MCMC iterations per timed step: one scoring period
 LPROB = 0.5
 SEED = 20261205
 WORKLOAD = "cfg2"
@@ -48,7 +49,7 @@ L2_FLUSH_BYTES = 256 << 20  # larger than the 129 MB L2
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--skip-uneven", action="store_true", help="leave out the uneven multi-pedigree batch")
     ap.add_argument("--skip-large", action="store_true", help="leave out the 400-member, 10,000-SNP workload")
@@ -70,6 +71,8 @@ def config(world):
             "members": 120, "markers": 2000, "chains_per_gpu": CHAINS, "scoring_period": PERIOD,
             "lod_positions_per_graph": 9995, "lsampler_prob": LPROB,
             "parallelism": f"replicas x{world}",
+            "step": "one scoring period: 100 MCMC iterations of every chain and one LOD scoring of every "
+                    "chain's graph, one run-graph launch; value = chain-iterations/s",
             "l2": "flushed (256 MB write) before every timed step",
             "zero_likelihood_positions": "counted as zero terms of the log-sum (SL_LOD_ZERO_OK); the "
                                          "reference exits at the first one (peeler.cc:89-92)"}
@@ -279,12 +282,16 @@ def run_ours(args):
     seed = SEED + 7919 * rank
 
     # ---------------- batched form: all chains per launch, FP32-rescaled LOD
+    # the L-sampler compiled for this pedigree (bit-identical to the generic kernel)
     ctx = api.Context(prob, n_chains=C, lod_precision=api.SL_LOD_FP32_RESCALED, device=local,
-                      sampler_precision=api.SL_SAMPLER_FAST, lod_flags=api.SL_LOD_ZERO_OK)
+                      sampler_precision=api.SL_SAMPLER_FAST, lod_flags=api.SL_LOD_ZERO_OK,
+                      ls_kernel=api.SL_LS_KERNEL_SPECIALISED)
+    ls_sel, ls_ms = ctx.ls_kernel_info()
     ctx.set_graphs(np.stack([d["dg0"]] * C))
     stream = torch.cuda.ExternalStream(ctx.stream_handle())
     W, K = args.warmup, args.steps
-    ctx.run(iterations=W, burnin=0, period=PERIOD, lprob=LPROB, seed=seed)
+    P_ = STEP_ITERS
+    ctx.run(iterations=W * P_, burnin=0, period=PERIOD, lprob=LPROB, seed=seed)
     ctx.synchronize()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
     clocks = Clocks(local)
@@ -292,12 +299,15 @@ def run_ours(args):
     barrier()
     torch.cuda.synchronize()
     clocks.start()
-    # each step is one launch of the run graph: one MCMC iteration of every chain
+    # each step is one launch of the run graph: one scoring period, 100 MCMC
+    # iterations of every chain (each chain running its own iterations) and the
+    # scoring of every chain's graph at the period's first iteration
     for i in range(K):
         with torch.cuda.stream(stream):
             flush.fill_(i & 0xff)
             ev[i][0].record(stream)
-        ctx.run(iterations=W + i + 1, burnin=0, period=PERIOD, lprob=LPROB, seed=seed, first_iteration=W + i)
+        ctx.run(iterations=(W + i + 1) * P_, burnin=0, period=PERIOD, lprob=LPROB, seed=seed,
+                first_iteration=(W + i) * P_)
         with torch.cuda.stream(stream):
             ev[i][1].record(stream)
     ctx.synchronize()
@@ -307,14 +317,30 @@ def run_ours(args):
     gpu_launches = ctx.launches - launches0
     step_ms = [a.elapsed_time(b) for a, b in ev]
     t_s = allmax(sum(step_ms) / 1e3)
-    value = K * C * world / t_s
+    value = K * P_ * C * world / t_s
+
+    # the same chains with one launch per MCMC iteration (every chain waits for
+    # the slowest one at every iteration), for comparison
+    Ki = min(K, 50)
+    evi = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(Ki)]
+    it0 = (W + K) * P_
+    for i in range(Ki):
+        with torch.cuda.stream(stream):
+            flush.fill_(i & 0xff)
+            evi[i][0].record(stream)
+        ctx.run(iterations=it0 + i + 1, burnin=0, period=PERIOD, lprob=LPROB, seed=seed, first_iteration=it0 + i)
+        with torch.cuda.stream(stream):
+            evi[i][1].record(stream)
+    ctx.synchronize()
+    per_iter = {"value": Ki * C * world / allmax(sum(a.elapsed_time(b) for a, b in evi) / 1e3), "unit": UNIT,
+                "note": "one run-graph launch (and L2 flush) per MCMC iteration: every chain waits for the "
+                        "slowest at every iteration"}
 
     # algorithmic bytes of the timed run-graph launches: every chain-step moves
     # step_bytes, every scored graph position_bytes per position
-    n_l = [sum(philox.chooses_l(seed, c, W + i, LPROB) for c in range(C)) for i in range(K)]
     sb = step_bytes(N, F, M)
-    scorings = sum(1 for i in range(K) if (W + i) % PERIOD == 0)
-    alg_total = K * C * sb + scorings * C * npos * position_bytes(N, F, n)
+    scorings = K * P_ // PERIOD
+    alg_total = K * P_ * C * sb + scorings * C * npos * position_bytes(N, F, n)
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
         os.path.join(ROOT, "MEASURED_PEAKS.json")) else {"hbm_gbs": 6800.0}
     peak = float(peaks.get("hbm_gbs", 6800.0))
@@ -328,11 +354,12 @@ def run_ours(args):
     lod_kernel_names = {api.SL_LOD_KERNEL_INTERP: "lod_prog_kernel", api.SL_LOD_KERNEL_JIT_REG: "sl_lod_jit (registers)",
                         api.SL_LOD_KERNEL_JIT_SMEM: "sl_lod_jit (shared memory)"}
     sel, jit_ms = ctx.lod_kernel_info()
-    names = {0: "lsampler_kernel<float>", 1: "fag_warp_kernel+ffbs_scan_kernel", 2: lod_kernel_names.get(sel, "lod_kernel"),
+    ls_name = "sl_ls_jit (specialised)" if ls_sel == api.SL_LS_KERNEL_SPECIALISED else "lsampler_kernel<float>"
+    names = {0: ls_name, 1: "fag_warp_kernel+ffbs_scan_kernel", 2: lod_kernel_names.get(sel, "lod_kernel"),
              3: "lod_merge_kernel", 4: "choose/shuffle"}
     Kp = min(K, 10)
     ctx.profile(True)
-    ctx.run(iterations=W + K + Kp, burnin=0, period=PERIOD, lprob=LPROB, seed=seed, first_iteration=W + K)
+    ctx.run(iterations=it0 + Ki + Kp, burnin=0, period=PERIOD, lprob=LPROB, seed=seed, first_iteration=it0 + Ki)
     ctx.synchronize()
     kern = {k: ctx.profile_read(k) for k in range(5)}
     ctx.profile(False)
@@ -398,24 +425,27 @@ def run_ours(args):
 
     # ---------------- end to end through the public API with host buffers
     ectx = api.Context(prob, n_chains=C, lod_precision=api.SL_LOD_FP32_RESCALED, device=local,
-                       sampler_precision=api.SL_SAMPLER_FAST, lod_flags=api.SL_LOD_ZERO_OK)
+                       sampler_precision=api.SL_SAMPLER_FAST, lod_flags=api.SL_LOD_ZERO_OK,
+                       ls_kernel=api.SL_LS_KERNEL_SPECIALISED)
     host_graphs = np.ascontiguousarray(np.stack([d["dg0"]] * C))
     ectx.set_graphs(host_graphs)
-    ectx.run(iterations=W, burnin=0, period=PERIOD, lprob=LPROB, seed=seed)
+    ectx.run(iterations=W * P_, burnin=0, period=PERIOD, lprob=LPROB, seed=seed)
     ectx.synchronize()
     host_graphs = ectx.get_graphs()
-    Ke = min(K, 50)
+    Ke = min(K, 20)
     barrier()
     t0 = time.perf_counter()
     for i in range(Ke):
         ectx.set_graphs(host_graphs)                                   # H2D: the step's state
-        ectx.run(iterations=W + i + 1, burnin=0, period=PERIOD, lprob=LPROB, seed=seed, first_iteration=W + i)
+        ectx.run(iterations=(W + i + 1) * P_, burnin=0, period=PERIOD, lprob=LPROB, seed=seed,
+                 first_iteration=(W + i) * P_)
         host_graphs = ectx.get_graphs()                                # D2H: the step's result
     e2e_t = allmax(time.perf_counter() - t0)
     words = M * ((2 * (N - F) + 31) // 32)
-    e2e = {"value": Ke * C * world / e2e_t, "unit": UNIT, "h2d_bytes_per_step": 4 * words * C,
+    e2e = {"value": Ke * P_ * C * world / e2e_t, "unit": UNIT, "h2d_bytes_per_step": 4 * words * C,
            "d2h_bytes_per_step": 4 * words * C,
-           "path": "sl_set_descent_graphs (pinned, packed) + sl_run(1 iteration) + sl_get_descent_graphs per step"}
+           "path": "sl_set_descent_graphs (pinned, packed) + sl_run(one scoring period, 100 iterations) + "
+                   "sl_get_descent_graphs per step"}
 
     if rank == 0:
         out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
@@ -428,6 +458,9 @@ def run_ours(args):
                "lod_kernel": {"selected": lod_kernel_names.get(lsel, str(lsel)),
                               "specialised_compile_ms": round(ljit_ms, 1),
                               "selection": "timed at the first scoring (SL_LOD_KERNEL_AUTO)"},
+               "ls_kernel": {"selected": ls_name, "specialised_compile_ms": round(ls_ms, 1),
+                             "selection": "SL_LS_KERNEL_SPECIALISED (NVRTC at context creation, outside the timed "
+                                          "region; draws bit-identical graphs to the generic kernel)"},
                "plain": {"steps_per_s": plain_steps_s * world, "lod_positions_per_s": plain_lod_pos_s * world,
                          "form": "one chain per launch, exact FP64 samplers, FP64 LOD peel"},
                "batched_vs_plain": {"steps": value / (plain_steps_s * world),
@@ -436,6 +469,7 @@ def run_ours(args):
                "adjoint": adj,
                "uneven_batch": uneven,
                "large_scale": large,
+               "per_iteration_launches": per_iter,
                "gpu_launches": int(gpu_launches), "roofline": roofline, "clocks": clk, "e2e": e2e}
         if world == 1:
             out["cpu_baseline"] = cpu_baseline_sample()

@@ -605,6 +605,8 @@ int main(int argc, char** argv) {
         so.lod_precision = o.exact ? SL_LOD_FP64 : SL_LOD_FP32_RESCALED;
         so.sampler_precision = o.exact ? SL_SAMPLER_EXACT : SL_SAMPLER_FAST;
         so.lod_flags = SL_LOD_ZERO_OK;
+        // long runs amortise compiling the L-sampler for the pedigree (same draws, same graphs)
+        so.ls_kernel = !o.exact && o.burnin + o.iterations >= 10000 ? SL_LS_KERNEL_SPECIALISED : SL_LS_KERNEL_GENERIC;
         for (int r = 0; r < (o.mc3 ? o.runs : 1) && !rc; ++r) {
             sl_ctx* ctx = nullptr;
             if (sl_create(&d, &so, &ctx) != SL_OK) {

@@ -1180,6 +1180,9 @@ int sl_create(const sl_problem_desc* d, const sl_options* opt, sl_ctx** out) {
     if ((rc = upload(ctx, (OpDev**)&P.ops, ops.data(), K))) return bail(rc);
     if ((rc = upload(ctx, (int32_t**)&P.opdata, od.data(), od.size()))) return bail(rc);
     P.opdata_n = (int32_t)od.size();
+    // small operation tables are copied to every L-sampler block; large ones
+    // (hundreds of members) would take residency from the arenas
+    P.ls_stage_ops = K * sizeof(OpDev) + od.size() * 4 <= 16 * 1024 ? 1 : 0;
     if ((rc = upload(ctx, (int16_t**)&P.fag_order, order.data(), N))) return bail(rc);
     if ((rc = upload(ctx, (int16_t**)&P.lvl_order, lvl_order.data(), N))) return bail(rc);
     if ((rc = upload(ctx, (int32_t**)&P.lvl_off, lvl_off.data(), lvl_off.size()))) return bail(rc);

@@ -44,6 +44,7 @@ struct ProblemDev {
     const OpDev* ops;                    // [K]
     const int32_t* opdata;
     int32_t opdata_n;                    // words of opdata
+    int32_t ls_stage_ops;                // the L-sampler copies ops and opdata to each block's shared memory
     const int16_t* fag_order;            // [N] parents before children, founders first
     const int16_t* lvl_order;            // [N] persons by generation level (founders = level 0)
     const int32_t* lvl_off;              // [n_lvl + 1] start of each level in lvl_order

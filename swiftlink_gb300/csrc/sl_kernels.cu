@@ -203,11 +203,16 @@ __host__ __device__ __forceinline__ size_t ls_warp_bytes(const ProblemDev& P) {
 // Block-shared copies of the peel's operations and their lists: every lane
 // reads them at every operation, and L1 holds little beside the arenas.
 __host__ __device__ __forceinline__ size_t ls_tables_bytes(const ProblemDev& P) {
-    return al16((size_t)P.K * sizeof(OpDev)) + al16((size_t)P.opdata_n * 4);
+    return P.ls_stage_ops ? al16((size_t)P.K * sizeof(OpDev)) + al16((size_t)P.opdata_n * 4) : 0;
 }
 
 __device__ __forceinline__ void ls_stage_tables(const ProblemDev& P, unsigned char* smem, const OpDev*& ops,
                                                 const int32_t*& opd) {
+    if (!P.ls_stage_ops) {   // tables too large to share a block's shared memory with the arenas
+        ops = P.ops;
+        opd = P.opdata;
+        return;
+    }
     int32_t* so = (int32_t*)smem;
     int32_t* sd = (int32_t*)(smem + al16((size_t)P.K * sizeof(OpDev)));
     const int32_t* src = (const int32_t*)P.ops;
