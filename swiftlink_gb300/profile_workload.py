@@ -1,14 +1,15 @@
 """A short, fixed workload for ncu captures of the library's kernels.
 
     python -m swiftlink_gb300.profile_workload [--iterations 2] [--chains 10]
-        [--lprob 0.5] [--adjoint 0] [--graph] [--lod-kernel K]
+        [--lprob 0.5] [--adjoint 0] [--graph] [--lod-kernel K] [--ls-specialised]
 
 On the 120-member, 2000-SNP pedigree it runs `iterations` device-driven MCMC
 iterations of `chains` chains in the fast sampler mode, kernels launched one
 by one with per-class event marks (with --graph: as one launch of the run
 graph, no marks), then one batched FP32 LOD scoring of every chain (the first
 scoring also times the LOD kernel candidates unless --lod-kernel forces one of
-SL_LOD_KERNEL_*), and, with --adjoint G, the
+SL_LOD_KERNEL_*; --ls-specialised runs the L-sampler compiled for the
+pedigree), and, with --adjoint G, the
 trait-peel adjoint of G graphs under the dominant model (0.01, 0.8, 0.9),
 q = 1e-3.  It prints the per-kernel-class event times of the sampling part.
 """
@@ -31,13 +32,15 @@ def main(argv=None):
     ap.add_argument("--seed", type=int, default=5)
     ap.add_argument("--graph", action="store_true")
     ap.add_argument("--lod-kernel", type=int, default=api.SL_LOD_KERNEL_AUTO)
+    ap.add_argument("--ls-specialised", action="store_true")
     a = ap.parse_args(argv)
     d = load_problem("cfg2")
     C = a.chains
     prob = api.Problem.from_arrays(d, with_legal=False)
     with api.Context(prob, n_chains=C, lod_precision=api.SL_LOD_FP32_RESCALED,
                      sampler_precision=api.SL_SAMPLER_FAST, lod_flags=api.SL_LOD_ZERO_OK,
-                     lod_kernel=a.lod_kernel) as ctx:
+                     lod_kernel=a.lod_kernel,
+                     ls_kernel=api.SL_LS_KERNEL_SPECIALISED if a.ls_specialised else api.SL_LS_KERNEL_GENERIC) as ctx:
         ctx.set_graphs(np.stack([d["dg0"]] * C))
         ctx.profile(not a.graph)
         ctx.run(iterations=a.iterations, burnin=0, period=1 << 30, lprob=a.lprob, seed=a.seed)
