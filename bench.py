@@ -347,7 +347,12 @@ def run_ours(args):
     per_launch = alg_total / K
     avg_s = sum(step_ms) / 1e3 / K
     achieved = per_launch / avg_s / 1e9
-    run_graph_name = "run graph (one MCMC iteration of every chain)"
+    run_graph_name = "run graph (one scoring period: 100 MCMC iterations of every chain)"
+    # DRAM bytes per launch: the captured 2-iteration graph launch (per iteration in
+    # profiles/traffic.md) times the iterations of one launch, an upper estimate (a
+    # longer launch keeps more of its state in L2 between iterations)
+    t_iter = traffic_from_profiles("run graph (one MCMC iteration of every chain)")
+    traffic = t_iter * P_ if t_iter is not None else None
 
     # kernel shares from a separate profiled pass: the same iterations with
     # per-kernel-class events (the host-driven path, kernels launched one by one)
@@ -365,7 +370,8 @@ def run_ours(args):
     ctx.profile(False)
     tot = max(1e-9, sum(x[0] for x in kern.values()))
     roofline = {"bound": "hbm", "kernel": run_graph_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": traffic_from_profiles(run_graph_name),
+                "frac": achieved / peak, "traffic": traffic,
+                "traffic_source": "profiles/traffic.md: ncu DRAM bytes of the run graph per iteration x 100",
                 "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if "when" in peaks else "fallback",
                 "algorithmic_bytes_per_launch": per_launch, "avg_launch_ms": 1e3 * avg_s,
                 "note": "latency-bound integer and FP32 work on small rfunctions: the HBM fraction is small by "

@@ -39,7 +39,7 @@ struct Options {
     int chains = 1, exchange = 10;   // MC3 (defaults.h:9, 12)
     double lprob = 0.5;
     std::vector<double> temps;
-    bool trace = false, affected_only = false, verbose = false, exact = false, mc3 = false;
+    bool trace = false, affected_only = false, verbose = false, exact = false, mc3 = false, generic_ls = false;
 };
 
 std::vector<std::string> tokens(const std::string& line) {
@@ -430,6 +430,7 @@ void usage(const char* prog) {
             "  -y NUM    --exchangeperiod=NUM      (default = 10)\n"
             "  -t LIST   --temperatures=LIST       (comma separated, the first 1.0; default 1 / (1 + 0.001 2^i))\n"
             "  -E        --exact                   (FP64 samplers and LOD, the reference's arithmetic)\n"
+            "  -G        --genericls               (no L-sampler compiled for the pedigree on long runs)\n"
             "  -D FILE   --dumpproblem=FILE        (write the problem tables of every family and stop)\n",
             prog);
 }
@@ -460,13 +461,14 @@ int main(int argc, char** argv) {
         {"sexlinked", no_argument, 0, 'X'},       {"elod", no_argument, 0, 'e'},
         {"verbose", no_argument, 0, 'v'},         {"help", no_argument, 0, 'h'},
         {"exact", no_argument, 0, 'E'},           {"dumpproblem", required_argument, 0, 'D'},
+        {"genericls", no_argument, 0, 'G'},
         {"mcmcmc", no_argument, 0, 'M'},          {"chains", required_argument, 0, 'z'},
         {"exchangeperiod", required_argument, 0, 'y'}, {"temperatures", required_argument, 0, 't'},
         {"frequency", required_argument, 0, 'f'}, {"penetrance", required_argument, 0, 'k'},
         {"replicates", required_argument, 0, 'u'}, {"separation", required_argument, 0, 'w'},
         {0, 0, 0, 0}};
     int ch, ignored;
-    while ((ch = getopt_long(argc, argv, "p:m:d:o:i:b:s:x:l:n:R:TP:c:gq:r:aXevhED:Mz:y:t:f:k:u:w:", longopts, nullptr)) != -1) {
+    while ((ch = getopt_long(argc, argv, "p:m:d:o:i:b:s:x:l:n:R:TP:c:gq:r:aXevhED:Mz:y:t:f:k:u:w:G", longopts, nullptr)) != -1) {
         switch (ch) {
             case 'p': o.ped = optarg; break;
             case 'm': o.map = optarg; break;
@@ -491,6 +493,7 @@ int main(int argc, char** argv) {
             case 'E': o.exact = true; break;
             case 'D': o.dump = optarg; break;
             case 'M': o.mc3 = true; break;
+            case 'G': o.generic_ls = true; break;
             case 'z': if (!to_int(optarg, o.chains) || o.chains < 1) { fprintf(stderr, "option '-z' requires an int > 0\n"); return 1; } break;
             case 'y': if (!to_int(optarg, o.exchange) || o.exchange < 1) { fprintf(stderr, "option '-y' requires an int > 0\n"); return 1; } break;
             case 't':
@@ -606,7 +609,8 @@ int main(int argc, char** argv) {
         so.sampler_precision = o.exact ? SL_SAMPLER_EXACT : SL_SAMPLER_FAST;
         so.lod_flags = SL_LOD_ZERO_OK;
         // long runs amortise compiling the L-sampler for the pedigree (same draws, same graphs)
-        so.ls_kernel = !o.exact && o.burnin + o.iterations >= 10000 ? SL_LS_KERNEL_SPECIALISED : SL_LS_KERNEL_GENERIC;
+        so.ls_kernel = !o.exact && !o.generic_ls && o.burnin + o.iterations >= 10000 ? SL_LS_KERNEL_SPECIALISED
+                                                                                     : SL_LS_KERNEL_GENERIC;
         for (int r = 0; r < (o.mc3 ? o.runs : 1) && !rc; ++r) {
             sl_ctx* ctx = nullptr;
             if (sl_create(&d, &so, &ctx) != SL_OK) {
