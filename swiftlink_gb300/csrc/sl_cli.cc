@@ -613,7 +613,16 @@ int main(int argc, char** argv) {
                                                                                      : SL_LS_KERNEL_GENERIC;
         for (int r = 0; r < (o.mc3 ? o.runs : 1) && !rc; ++r) {
             sl_ctx* ctx = nullptr;
-            if (sl_create(&d, &so, &ctx) != SL_OK) {
+            // a fixed scoring kernel keeps the table a function of the seed: the specialised
+            // kernel with values in registers, else the slot-program interpreter (the timed
+            // choice of SL_LOD_KERNEL_AUTO can differ from run to run in the last FP32 bits)
+            if (!o.exact) so.lod_kernel = SL_LOD_KERNEL_JIT_REG;
+            if (sl_create(&d, &so, &ctx) != SL_OK && !o.exact) {
+                so.lod_kernel = SL_LOD_KERNEL_INTERP;
+                ctx = nullptr;
+                if (sl_create(&d, &so, &ctx) != SL_OK) ctx = nullptr;
+            }
+            if (!ctx) {
                 fprintf(stderr, "error: pedigree '%s': %s\n", fams[f].id.c_str(), sl_last_error(nullptr));
                 rc = 1;
                 break;
