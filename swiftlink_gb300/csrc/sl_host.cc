@@ -39,9 +39,9 @@ cudaError_t launch_msampler(const ProblemDev& P, uint32_t* dg, int first, int nc
 cudaError_t launch_set_key(uint64_t* key, uint64_t seed, uint64_t iter, cudaStream_t s);
 cudaError_t launch_si(const ProblemDev& P, uint32_t* dg, int first, int nchain, const int32_t* starts,
                       const double* u, int64_t ucs, uint64_t seed, uint64_t pass, double* weights, int* status,
-                      cudaStream_t s, int wpb);
+                      cudaStream_t s, int wpb, int npass, int64_t pass_stride, int grid_cap);
 cudaError_t launch_si_select(const uint32_t* scratch, uint32_t* dg, int first, int nchain, size_t words,
-                             const double* w, double* best, cudaStream_t s);
+                             const double* w, double* best, int npass, cudaStream_t s);
 cudaError_t launch_run_init(const RunParams* rp, int64_t* it, int C, cudaStream_t s);
 cudaError_t launch_chain_iter(const RunParams* rp, const int64_t* it, int c, uint64_t* key, const int32_t* base,
                               int nm, int32_t* order, const double* temp, cudaGraphConditionalHandle hsw,
@@ -2551,7 +2551,7 @@ int sl_sequential_imputation(sl_ctx* ctx, int32_t first, int32_t n_chains, const
     CK(cudaMemcpyAsync(d_starts, start_loci, sizeof(int32_t) * n_chains, cudaMemcpyHostToDevice, ctx->stream));
     { Prof pf_(ctx, SL_KERNEL_LSAMPLER);
     CK(launch_si(ctx->P, ctx->d_dg, first, n_chains, d_starts, ctx->d_u, chain_stride, 0, 0, d_w, ctx->d_status,
-                 ctx->stream, ctx->ls_wpb)); }
+                 ctx->stream, ctx->ls_wpb, 1, 0, ctx->ls_grid)); }
     CK(cudaMemcpyAsync(weights, d_w, sizeof(double) * n_chains, cudaMemcpyDeviceToHost, ctx->stream));
     rc = sl_synchronize(ctx);
     for (void* p : {(void*)d_starts, (void*)d_w}) {
@@ -2567,32 +2567,39 @@ int sl_sequential_imputation_run(sl_ctx* ctx, int32_t iterations, uint64_t seed,
     const ProblemDev& P = ctx->P;
     const int C = ctx->n_chains, M = P.M;
     const size_t words = (size_t)M * P.W;
+    // passes are independent (SequentialImputation::parallel_run, sequential_imputation.cc:
+    // 47-114): a batch of them runs at once, one warp per (pass, chain), its graphs in
+    // scratch; the batch is bounded by a 256 MB scratch budget
+    const int batch = (int)std::max<size_t>(1, std::min<size_t>((size_t)iterations,
+                                                                 (256u << 20) / (sizeof(uint32_t) * words * C)));
     uint32_t* scratch = nullptr;
     int32_t* d_starts = nullptr;
     double *d_w = nullptr, *d_best = nullptr;
     int rc;
-    if ((rc = dev_alloc(ctx, &scratch, words * C))) return rc;
-    if ((rc = dev_alloc(ctx, &d_starts, (size_t)C))) return rc;
-    if ((rc = dev_alloc(ctx, &d_w, (size_t)C))) return rc;
+    if ((rc = dev_alloc(ctx, &scratch, words * C * batch))) return rc;
+    if ((rc = dev_alloc(ctx, &d_starts, (size_t)C * batch))) return rc;
+    if ((rc = dev_alloc(ctx, &d_w, (size_t)C * batch))) return rc;
     if ((rc = dev_alloc(ctx, &d_best, (size_t)C))) return rc;
     std::vector<double> lowest(C, -DBL_MAX);
     CK(cudaMemcpyAsync(d_best, lowest.data(), sizeof(double) * C, cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaMemsetAsync(scratch, 0, sizeof(uint32_t) * words * C, ctx->stream));
-    std::vector<int32_t> starts(C);
-    for (int pass = 0; pass < iterations; ++pass) {
-        // the start locus (get_random_locus) from its own Philox stage
-        for (int c = 0; c < C; ++c) {
-            const uint64_t hi = ((uint64_t)c << 40) ^ ((uint64_t)pass << 4) ^ 6u;
-            starts[c] = std::min(M - 1, (int)(host_philox_u01(seed, hi, 0) * M));
-        }
-        CK(cudaMemcpyAsync(d_starts, starts.data(), sizeof(int32_t) * C, cudaMemcpyHostToDevice, ctx->stream));
-        CK(cudaStreamSynchronize(ctx->stream));   // the host vector is reused next pass
-        // the pass writes chain c's graph into scratch slot c (first = 0 on the scratch array)
+    CK(cudaMemsetAsync(scratch, 0, sizeof(uint32_t) * words * C * batch, ctx->stream));
+    std::vector<int32_t> starts((size_t)C * batch);
+    for (int p0 = 0; p0 < iterations; p0 += batch) {
+        const int np = std::min(batch, iterations - p0);
+        // each pass's start locus (get_random_locus) from its own Philox stage
+        for (int q = 0; q < np; ++q)
+            for (int c = 0; c < C; ++c) {
+                const uint64_t hi = ((uint64_t)c << 40) ^ ((uint64_t)(p0 + q) << 4) ^ 6u;
+                starts[(size_t)q * C + c] = std::min(M - 1, (int)(host_philox_u01(seed, hi, 0) * M));
+            }
+        CK(cudaMemcpyAsync(d_starts, starts.data(), sizeof(int32_t) * C * np, cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));   // the host vector is reused next batch
+        // pass q of chain c writes graph slot q * C + c of scratch
         { Prof pf_(ctx, SL_KERNEL_LSAMPLER);
-        CK(launch_si(P, scratch, 0, C, d_starts, nullptr, 0, seed, (uint64_t)pass, d_w, ctx->d_status, ctx->stream,
-                     ctx->ls_wpb)); }
+        CK(launch_si(P, scratch, 0, C, d_starts, nullptr, 0, seed, (uint64_t)p0, d_w, ctx->d_status, ctx->stream,
+                     ctx->ls_wpb, np, (int64_t)(words * C), ctx->ls_grid)); }
         { Prof pf_(ctx, SL_KERNEL_OTHER);
-        CK(launch_si_select(scratch, ctx->d_dg, 0, C, words, d_w, d_best, ctx->stream)); }
+        CK(launch_si_select(scratch, ctx->d_dg, 0, C, words, d_w, d_best, np, ctx->stream)); }
     }
     if (best_weights)
         CK(cudaMemcpyAsync(best_weights, d_best, sizeof(double) * C, cudaMemcpyDeviceToHost, ctx->stream));

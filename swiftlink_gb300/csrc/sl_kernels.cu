@@ -445,10 +445,14 @@ __global__ void __launch_bounds__(128) lsampler_kernel(ProblemDev P, uint32_t* d
 // with the right neighbour only, then rightwards with the left neighbour only;
 // draws are consumed in one sequence (unit `unit`), the weight is the sum of
 // log(root) over the steps (-DBL_MAX when a locus has likelihood 0).
+// npass independent passes of every chain run as separate warps: pass q of
+// chain cr writes the graph set at dg + q * pass_stride, draws from the
+// Philox stream of pass draws.iter + q, starts at starts[q * nchain + cr] and
+// leaves its weight at weights[q * nchain + cr].
 template <typename T>
 __global__ void __launch_bounds__(128) si_kernel(ProblemDev P, uint32_t* dg, int first, int nchain,
                                                  const int32_t* starts, Draws draws, int64_t unit, double* weights,
-                                                 int* status) {
+                                                 int* status, int npass, int64_t pass_stride) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int wpb = blockDim.x >> 5, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const OpDev* ops;
@@ -456,8 +460,12 @@ __global__ void __launch_bounds__(128) si_kernel(ProblemDev P, uint32_t* dg, int
     ls_stage_tables(P, smem, ops, opd);
     __syncthreads();
     unsigned char* wsmem = smem + ls_tables_bytes(P) + (size_t)warp * ls_warp_bytes<T>(P);
-    for (int cr = blockIdx.x * wpb + warp; cr < nchain; cr += gridDim.x * wpb) {
-        const int chain = first + cr, M = P.M, start = starts[cr];
+    for (int t = blockIdx.x * wpb + warp; t < nchain * npass; t += gridDim.x * wpb) {
+        const int cr = t % nchain, q = t / nchain;
+        const int chain = first + cr, M = P.M, start = starts[t];
+        uint32_t* dgq = dg + (size_t)q * pass_stride;
+        Draws dq = draws;
+        dq.iter = draws.iter + (uint64_t)q;
         int64_t base = 0;
         double w = 0.0;
         bool ok = true;
@@ -466,7 +474,7 @@ __global__ void __launch_bounds__(128) si_kernel(ProblemDev P, uint32_t* dg, int
             const bool hasL = v > start && l > 0;
             const bool hasR = v > 0 && v <= start && l < M - 1;
             double lr = 0.0;
-            const int used = ls_locus<T>(P, ops, opd, dg, cr, chain, l, hasL, hasR, draws, unit, base, wsmem, lane,
+            const int used = ls_locus<T>(P, ops, opd, dgq, cr, chain, l, hasL, hasR, dq, unit, base, wsmem, lane,
                                          status, &lr);
             if (used < 0) {
                 ok = false;
@@ -475,7 +483,7 @@ __global__ void __launch_bounds__(128) si_kernel(ProblemDev P, uint32_t* dg, int
             base += used;
             w += __shfl_sync(FULLMASK, lr, 0);
         }
-        if (lane == 0) weights[cr] = ok ? w : -DBL_MAX;
+        if (lane == 0) weights[t] = ok ? w : -DBL_MAX;
         __syncwarp();
     }
 }
@@ -2432,25 +2440,32 @@ cudaError_t launch_lsampler(const ProblemDev& P, uint32_t* dg, int first, int nc
     return cudaGetLastError();
 }
 
-// Keep each chain's better imputation: copy the pass's graph and weight where
-// it beats the best so far (SequentialImputation::run, sequential_imputation.cc:
-// 14-43: `tmp_prob > best_prob`, starting from LOG_ZERO).
+// Keep each chain's best imputation: over the batch's passes in pass order,
+// the first whose weight beats the best so far (SequentialImputation::run,
+// sequential_imputation.cc:14-43: `tmp_prob > best_prob`, starting from
+// LOG_ZERO); its graph is copied in.  One block per chain.
 __global__ void si_select_kernel(const uint32_t* scratch, uint32_t* dg, int first, int nchain, size_t words,
-                                 const double* w, double* best) {
+                                 const double* w, double* best, int npass) {
     for (int cr = blockIdx.x; cr < nchain; cr += gridDim.x) {
-        const bool take = w[cr] > best[cr];
+        double bw = best[cr];
+        int bq = -1;
+        for (int q = 0; q < npass; ++q)
+            if (w[(size_t)q * nchain + cr] > bw) {
+                bw = w[(size_t)q * nchain + cr];
+                bq = q;
+            }
         __syncthreads();
-        if (!take) continue;
-        for (size_t i = threadIdx.x; i < words; i += blockDim.x)
-            dg[(size_t)(first + cr) * words + i] = scratch[(size_t)cr * words + i];
+        if (bq < 0) continue;
+        const uint32_t* src = scratch + ((size_t)bq * nchain + cr) * words;
+        for (size_t i = threadIdx.x; i < words; i += blockDim.x) dg[(size_t)(first + cr) * words + i] = src[i];
         __syncthreads();
-        if (threadIdx.x == 0) best[cr] = w[cr];
+        if (threadIdx.x == 0) best[cr] = bw;
     }
 }
 
 cudaError_t launch_si(const ProblemDev& P, uint32_t* dg, int first, int nchain, const int32_t* starts,
                       const double* u, int64_t ucs, uint64_t seed, uint64_t pass, double* weights, int* status,
-                      cudaStream_t s, int wpb) {
+                      cudaStream_t s, int wpb, int npass, int64_t pass_stride, int grid_cap) {
     const size_t smem = ls_tables_bytes(P) + wpb * lsampler_smem_per_warp(P);
     static size_t configured[2] = {0, 0};
     const int f = P.ls_fast ? 1 : 0;
@@ -2463,17 +2478,20 @@ cudaError_t launch_si(const ProblemDev& P, uint32_t* dg, int first, int nchain, 
         configured[f] = smem;
     }
     Draws d{u, ucs, 0, seed, pass, 5, nullptr};
-    const int grid = (nchain + wpb - 1) / wpb;
+    int grid = (nchain * npass + wpb - 1) / wpb;
+    if (grid > grid_cap) grid = grid_cap;
     if (f)
-        si_kernel<float><<<grid, wpb * 32, smem, s>>>(P, dg, first, nchain, starts, d, 0, weights, status);
+        si_kernel<float><<<grid, wpb * 32, smem, s>>>(P, dg, first, nchain, starts, d, 0, weights, status, npass,
+                                                      pass_stride);
     else
-        si_kernel<double><<<grid, wpb * 32, smem, s>>>(P, dg, first, nchain, starts, d, 0, weights, status);
+        si_kernel<double><<<grid, wpb * 32, smem, s>>>(P, dg, first, nchain, starts, d, 0, weights, status, npass,
+                                                       pass_stride);
     return cudaGetLastError();
 }
 
 cudaError_t launch_si_select(const uint32_t* scratch, uint32_t* dg, int first, int nchain, size_t words,
-                             const double* w, double* best, cudaStream_t s) {
-    si_select_kernel<<<nchain < 1024 ? nchain : 1024, 256, 0, s>>>(scratch, dg, first, nchain, words, w, best);
+                             const double* w, double* best, int npass, cudaStream_t s) {
+    si_select_kernel<<<nchain < 1024 ? nchain : 1024, 256, 0, s>>>(scratch, dg, first, nchain, words, w, best, npass);
     return cudaGetLastError();
 }
 

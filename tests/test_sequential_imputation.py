@@ -100,3 +100,36 @@ def test_best_of_n_imputation_gives_legal_graphs(fast):
         ll = P.loglik(out[c])
         assert ll > -1e300
         assert np.isfinite(best[c])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["east", "cfg1"])
+def test_batched_best_of_n_equals_pass_by_pass(name):
+    """sl_sequential_imputation_run runs its passes as one batch of
+    independent warps; replaying each pass alone (sl_sequential_imputation
+    with the same start loci and the same Philox draws) and keeping the first
+    strictly better weight gives the same graphs and weights."""
+    from swiftlink_gb300 import philox as ph
+    g = load_golden(name)
+    C, n, seed = 3, 6, 4242
+    M = g["M"]
+    L = M * (g["K"] + 2 * g["N"])
+    with api.Context(api.Problem.from_arrays(g), n_chains=C) as ctx:
+        best = ctx.sequential_imputation_run(iterations=n, seed=seed)
+        batched = ctx.get_graphs()
+    want_w = np.full(C, -np.finfo(np.float64).max)
+    want_g = [None] * C
+    with api.Context(api.Problem.from_arrays(g), n_chains=C) as ctx:
+        for p in range(n):
+            starts = np.array([min(M - 1, int(ph.uniform(seed, ph.stage_hi(c, p, 6), 0) * M)) for c in range(C)],
+                              np.int32)
+            u = np.stack([ph.uniform(seed, ph.stage_hi(c, p, 5), np.arange(L, dtype=np.uint64)) for c in range(C)])
+            ctx.set_graphs(np.zeros((C, M, g["N"], 2), np.int32))
+            w = ctx.sequential_imputation(starts, u)
+            out = ctx.get_graphs()
+            for c in range(C):
+                if w[c] > want_w[c]:
+                    want_w[c], want_g[c] = w[c], out[c].copy()
+    np.testing.assert_array_equal(best, want_w)
+    for c in range(C):
+        assert np.array_equal(batched[c], want_g[c]), c
