@@ -609,8 +609,10 @@ int main(int argc, char** argv) {
         so.sampler_precision = o.exact ? SL_SAMPLER_EXACT : SL_SAMPLER_FAST;
         so.lod_flags = SL_LOD_ZERO_OK;
         // long runs amortise compiling the L-sampler for the pedigree (same draws, same graphs)
-        so.ls_kernel = !o.exact && !o.generic_ls && o.burnin + o.iterations >= 10000 ? SL_LS_KERNEL_SPECIALISED
-                                                                                     : SL_LS_KERNEL_GENERIC;
+        // (up to 500 members: the generated source grows with the peel, and so does its compile time)
+        so.ls_kernel = !o.exact && !o.generic_ls && o.burnin + o.iterations >= 10000 && p.N <= 500
+                           ? SL_LS_KERNEL_SPECIALISED
+                           : SL_LS_KERNEL_GENERIC;
         for (int r = 0; r < (o.mc3 ? o.runs : 1) && !rc; ++r) {
             sl_ctx* ctx = nullptr;
             // a fixed scoring kernel keeps the table a function of the seed: the specialised
