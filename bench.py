@@ -500,7 +500,8 @@ def large_scale(device, C=32, K=4):
     d = pedigree.problem_from_workload(synth.make_workload(5))
     prob = api.Problem.from_arrays(d, with_legal=False)
     ctx = api.Context(prob, n_chains=C, device=device, lod_precision=api.SL_LOD_FP32_RESCALED,
-                      sampler_precision=api.SL_SAMPLER_FAST, lod_flags=api.SL_LOD_ZERO_OK)
+                      sampler_precision=api.SL_SAMPLER_FAST, lod_flags=api.SL_LOD_ZERO_OK,
+                      ls_kernel=api.SL_LS_KERNEL_SPECIALISED)
     ctx.set_graphs(np.stack([d["dg0"]] * C))
     ctx.run(iterations=2, burnin=0, period=1, lprob=LPROB, seed=SEED)
     ctx.synchronize()

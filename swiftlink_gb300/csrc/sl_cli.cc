@@ -609,8 +609,8 @@ int main(int argc, char** argv) {
         so.sampler_precision = o.exact ? SL_SAMPLER_EXACT : SL_SAMPLER_FAST;
         so.lod_flags = SL_LOD_ZERO_OK;
         // long runs amortise compiling the L-sampler for the pedigree (same draws, same graphs)
-        // (up to 500 members: the generated source grows with the peel, and so does its compile time)
-        so.ls_kernel = !o.exact && !o.generic_ls && o.burnin + o.iterations >= 10000 && p.N <= 500
+        // (up to 2000 members: the generated source grows with the peel's shapes, and so does its compile time)
+        so.ls_kernel = !o.exact && !o.generic_ls && o.burnin + o.iterations >= 10000 && p.N <= 2000
                            ? SL_LS_KERNEL_SPECIALISED
                            : SL_LS_KERNEL_GENERIC;
         for (int r = 0; r < (o.mc3 ? o.runs : 1) && !rc; ++r) {

@@ -77,35 +77,124 @@ std::string dig(const char* var, int pos) {
     return b;
 }
 
+// Operations of the same shape (type, cutset size, the positions the terms
+// read, the children's structure) share one generated function; what differs
+// between them (the peel node, the cutset members, the rfunction offsets, the
+// children's meiosis bits) is passed in.  Fewer, reused functions compile
+// faster and keep the instruction footprint small.
+struct Shape {
+    std::string key;
+    int type, c, mpos, fpos, n_prev, n_child;
+    std::vector<std::vector<int>> prev_pos;   // per previous rfunction: its keys' positions
+    std::vector<int> cpos, opos, pim;         // per child: its position, the other parent's, peel is mother
+};
+
+Shape shape_of(const JitLsIn& in, const OpDev& op) {
+    Shape sh;
+    sh.type = op.type;
+    sh.c = op.c;
+    sh.mpos = op.type == CHILD ? op.mpos : -1;
+    sh.fpos = op.type == CHILD ? op.fpos : -1;
+    sh.n_prev = op.n_prev;
+    sh.n_child = op.type == PARENT ? op.n_child : 0;
+    std::string k = std::to_string(sh.type) + "|" + std::to_string(sh.c) + "|" + std::to_string(sh.mpos) + "," +
+                    std::to_string(sh.fpos) + "|";
+    const int32_t* pd = in.opdata + op.prev_at;
+    for (int j = 0; j < op.n_prev; ++j) {
+        const int pc = pd[1];
+        std::vector<int> pos(pd + 2, pd + 2 + pc);
+        k += "p";
+        for (int x : pos) k += std::to_string(x) + ".";
+        sh.prev_pos.push_back(pos);
+        pd += 2 + pc;
+    }
+    k += "|";
+    const int32_t* cd = in.opdata + op.child_at;
+    for (int c = 0; c < sh.n_child; ++c, cd += 4) {
+        sh.cpos.push_back(cd[1]);
+        sh.opos.push_back(cd[2]);
+        sh.pim.push_back(cd[3]);
+        k += "c" + std::to_string(cd[1]) + "." + std::to_string(cd[2]) + "." + std::to_string(cd[3]);
+    }
+    sh.key = k;
+    return sh;
+}
+
+// the operation's run-time values, in the order of the shape functions' trailing parameters
+std::string call_args(const JitLsIn& in, const OpDev& op) {
+    std::string a = std::to_string(op.peel) + ", " + std::to_string(op.mat_off);
+    const int32_t* cut = in.opdata + op.cut_at;
+    for (int q = 0; q < op.c; ++q) a += ", " + std::to_string(cut[q]);
+    const int32_t* pd = in.opdata + op.prev_at;
+    for (int j = 0; j < op.n_prev; ++j) {
+        a += ", " + std::to_string(pd[0]);
+        pd += 2 + pd[1];
+    }
+    if (op.type == CHILD) a += ", " + std::to_string(2 * (op.peel - in.F));
+    if (op.type == PARENT) {
+        const int32_t* cd = in.opdata + op.child_at;
+        for (int c = 0; c < op.n_child; ++c) a += ", " + std::to_string(2 * (cd[4 * c] - in.F));
+    }
+    return a;
+}
+
+// the same values as constants, for a function made for one operation
+std::string const_prologue(const JitLsIn& in, const OpDev& op, const Shape& sh) {
+    std::string names = "pe, mat";
+    for (int q = 0; q < sh.c; ++q) names += ", cu" + std::to_string(q);
+    for (int j = 0; j < sh.n_prev; ++j) names += ", mo" + std::to_string(j);
+    if (sh.type == CHILD) names += ", cb0";
+    for (int c = 0; c < sh.n_child; ++c) names += ", cb" + std::to_string(c);
+    // pair the names with the call arguments
+    std::string vals = call_args(in, op), out = "  const int ";
+    size_t a = 0, b = 0;
+    bool first = true;
+    while (a < names.size()) {
+        size_t na = names.find(", ", a), nb = vals.find(", ", b);
+        const std::string n = names.substr(a, na == std::string::npos ? std::string::npos : na - a);
+        const std::string v = vals.substr(b, nb == std::string::npos ? std::string::npos : nb - b);
+        out += (first ? "" : ", ") + n + " = " + v;
+        first = false;
+        if (na == std::string::npos) break;
+        a = na + 2;
+        b = nb + 2;
+    }
+    return out + ";\n";
+}
+
+std::string params(const Shape& sh) {
+    std::string p = "int pe, int mat";
+    for (int q = 0; q < sh.c; ++q) p += ", int cu" + std::to_string(q);
+    for (int j = 0; j < sh.n_prev; ++j) p += ", int mo" + std::to_string(j);
+    if (sh.type == CHILD) p += ", int cb0";
+    for (int c = 0; c < sh.n_child; ++c) p += ", int cb" + std::to_string(c);
+    return p;
+}
+
 // The product of one (cell, state) presum entry: tv times the child's
 // transmission, the previous rfunctions in order, the children's
 // transmissions (ls_term in sl_kernels.cu).
-void emit_term(std::string& s, const JitLsIn& in, const OpDev& op, const char* ind) {
-    const int32_t* od = in.opdata;
+void emit_term(std::string& s, const Shape& sh, const char* ind) {
     emitf(s, "%sfloat tmp = tv;\n", ind);
-    if (op.type == CHILD)
+    if (sh.type == CHILD)
         emitf(s, "%stmp = __fmul_rn(tmp, __fmul_rn(dist[%s * 2 + matA(v)], dist[8 + %s * 2 + patA(v)]));\n", ind,
-              dig("ext", op.mpos).c_str(), dig("ext", op.fpos).c_str());
-    const int32_t* pd = od + op.prev_at;
-    for (int j = 0; j < op.n_prev; ++j) {
-        const int moff = pd[0], pc = pd[1];
+              dig("ext", sh.mpos).c_str(), dig("ext", sh.fpos).c_str());
+    for (int j = 0; j < sh.n_prev; ++j) {
         std::string idx;
-        for (int q = 0; q < pc; ++q) {
+        for (size_t q = 0; q < sh.prev_pos[j].size(); ++q) {
             if (q) idx += " | ";
             char b[96];
-            snprintf(b, sizeof b, "(%s << %d)", dig("ext", pd[2 + q]).c_str(), 2 * q);
+            snprintf(b, sizeof b, "(%s << %d)", dig("ext", sh.prev_pos[j][q]).c_str(), 2 * (int)q);
             idx += b;
         }
         if (idx.empty()) idx = "0";
-        emitf(s, "%stmp = __fmul_rn(tmp, A[%d + (%s)]);\n", ind, moff, idx.c_str());
-        pd += 2 + pc;
+        emitf(s, "%stmp = __fmul_rn(tmp, A[mo%d + (%s)]);\n", ind, j, idx.c_str());
     }
-    if (op.type == PARENT) {
+    if (sh.type == PARENT) {
         emitf(s, "%s{\n%s  float cp = 1.0f;\n", ind, ind);
-        const int32_t* cd = od + op.child_at;
-        for (int c = 0; c < op.n_child; ++c, cd += 4) {
-            const std::string kt = dig("ext", cd[1]), ot = dig("ext", cd[2]);
-            const std::string mt = cd[3] ? "v" : ot, pt = cd[3] ? ot : "v";
+        for (int c = 0; c < sh.n_child; ++c) {
+            const std::string kt = dig("ext", sh.cpos[c]), ot = dig("ext", sh.opos[c]);
+            const std::string mt = sh.pim[c] ? "v" : ot, pt = sh.pim[c] ? ot : "v";
             emitf(s, "%s  { const int kt = %s; cp = __fmul_rn(cp, __fmul_rn(dist[%d + (%s) * 2 + matA(kt)], dist[%d + (%s) * 2 + patA(kt)])); }\n",
                   ind, kt.c_str(), 16 * c, mt.c_str(), 16 * c + 8, pt.c_str());
         }
@@ -114,9 +203,9 @@ void emit_term(std::string& s, const JitLsIn& in, const OpDev& op, const char* i
 }
 
 // the validity of a cutset index under the members' genotype-elimination masks
-std::string valid_expr(const JitLsIn& in, const OpDev& op, const char* var) {
+std::string valid_expr(const Shape& sh, const char* var) {
     std::string e;
-    for (int q = 0; q < op.c; ++q) {
+    for (int q = 0; q < sh.c; ++q) {
         char b[96];
         snprintf(b, sizeof b, "%s((g%d >> ((%s >> %d) & 3)) & 1)", q ? " && " : "", q, var, 2 * q);
         e += b;
@@ -124,86 +213,83 @@ std::string valid_expr(const JitLsIn& in, const OpDev& op, const char* var) {
     return e.empty() ? std::string("true") : e;
 }
 
-void emit_dists(std::string& s, const JitLsIn& in, const OpDev& op) {
-    const int F = in.F;
-    if (op.type == CHILD) {
-        emitf(s, "      if (lane == 0) dist_one(%d, cL, cR, th, an, th2, an2, dist);\n", 2 * (op.peel - F));
-    } else if (op.type == PARENT && op.n_child > 0) {
-        const int32_t* cd = in.opdata + op.child_at;
-        s += "      if (lane < " + std::to_string(op.n_child) + ") {\n        int b = 0;\n";
-        for (int c = 0; c < op.n_child; ++c)
-            emitf(s, "        if (lane == %d) b = %d;\n", c, 2 * (cd[4 * c] - F));
+void emit_dists(std::string& s, const Shape& sh) {
+    if (sh.type == CHILD) {
+        s += "      if (lane == 0) dist_one(cb0, cL, cR, th, an, th2, an2, dist);\n";
+    } else if (sh.n_child > 0) {
+        s += "      if (lane < " + std::to_string(sh.n_child) + ") {\n        int b = 0;\n";
+        for (int c = 0; c < sh.n_child; ++c) emitf(s, "        if (lane == %d) b = cb%d;\n", c, c);
         s += "        dist_one(b, cL, cR, th, an, th2, an2, dist + 16 * lane);\n      }\n";
     }
     s += "      __syncwarp();\n";
 }
 
-void emit_cut_masks(std::string& s, const JitLsIn& in, const OpDev& op) {
-    const int32_t* cut = in.opdata + op.cut_at;
-    for (int q = 0; q < op.c; ++q) emitf(s, "      const int g%d = sg[%d] >> 4;\n", q, cut[q]);
+void emit_cut_masks(std::string& s, const Shape& sh) {
+    for (int q = 0; q < sh.c; ++q) emitf(s, "      const int g%d = sg[cu%d] >> 4;\n", q, q);
 }
 
-void emit_forward(std::string& s, const JitLsIn& in, int k) {
-    const OpDev& op = in.ops[k];
-    const int ncell = 1 << (2 * op.c), nitem = 4 * ncell;
+// consts: empty for a function shared by a shape (values as parameters), else
+// the one operation's values as constants
+void emit_forward(std::string& s, const Shape& sh, int id, const std::string& consts) {
+    const int ncell = 1 << (2 * sh.c), nitem = 4 * ncell;
     emitf(s,
-          "// operation %d: type %d, peel %d, cutset %d\n"
+          "// forward %d: %s\n"
           "__device__ __noinline__ void fwd%d(float* __restrict__ A, float* __restrict__ dist,\n"
           "    const unsigned char* __restrict__ sg, const float* __restrict__ spri, const u32* cL, const u32* cR,\n"
-          "    float th, float an, float th2, float an2, int lane) {\n"
+          "    float th, float an, float th2, float an2, int lane%s%s) {\n%s"
           "  const int v = lane & 3, grp = lane & ~3;\n  {\n",
-          k, op.type, op.peel, op.c, k);
-    emit_dists(s, in, op);
-    emitf(s, "      const float tv = spri[4 * (sg[%d] & 3) + v];\n", op.peel);
-    emit_cut_masks(s, in, op);
+          id, sh.key.c_str(), id, consts.empty() ? ", " : "", consts.empty() ? params(sh).c_str() : "",
+          consts.c_str());
+    emit_dists(s, sh);
+    s += "      const float tv = spri[4 * (sg[pe] & 3) + v];\n";
+    emit_cut_masks(s, sh);
     s += "      float mx = 0.0f;\n";
     emitf(s, "      for (int it0 = 0; it0 < %d; it0 += 32) {\n", nitem);
     s += "        const int cell = (it0 + lane) >> 2;\n        float term = 0.0f;\n";
-    emitf(s, "        if (it0 + lane < %d && tv != 0.0f && %s) {\n", nitem, valid_expr(in, op, "cell").c_str());
-    emitf(s, "          const int ext = cell | (v << %d);\n", 2 * op.c);
-    emit_term(s, in, op, "          ");
+    emitf(s, "        if (it0 + lane < %d && tv != 0.0f && %s) {\n", nitem, valid_expr(sh, "cell").c_str());
+    emitf(s, "          const int ext = cell | (v << %d);\n", 2 * sh.c);
+    emit_term(s, sh, "          ");
     s += "          term = tmp;\n        }\n";
     s += "        const float t0 = __shfl_sync(FULL, term, grp), t1 = __shfl_sync(FULL, term, grp + 1);\n"
          "        const float t2 = __shfl_sync(FULL, term, grp + 2), t3 = __shfl_sync(FULL, term, grp + 3);\n";
     emitf(s,
           "        if (v == 0 && it0 + lane < %d) {\n"
           "          const float total = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(0.0f, t0), t1), t2), t3);\n"
-          "          A[%d + cell] = total;\n"
+          "          A[mat + cell] = total;\n"
           "          mx = total > mx ? total : mx;\n"
           "        }\n      }\n",
-          nitem, op.mat_off);
+          nitem);
     emitf(s,
           "      for (int dd = 16; dd >= 1; dd >>= 1) { const float o = __shfl_xor_sync(FULL, mx, dd); mx = o > mx ? o : mx; }\n"
           "      if (mx > 0.0f) {\n"
           "        const float f = scalbnf(1.0f, -ilogbf(mx));\n"
-          "        for (int cell = lane; cell < %d; cell += 32) A[%d + cell] = A[%d + cell] * f;\n"
+          "        for (int cell = lane; cell < %d; cell += 32) A[mat + cell] = A[mat + cell] * f;\n"
           "      }\n"
           "      __syncwarp();\n  }\n}\n",
-          ncell, op.mat_off, op.mat_off);
+          ncell);
 }
 
-void emit_backward(std::string& s, const JitLsIn& in, int k) {
-    const OpDev& op = in.ops[k];
-    const int32_t* cut = in.opdata + op.cut_at;
+void emit_backward(std::string& s, const Shape& sh, int id, const std::string& consts, int di) {
     emitf(s,
-          "// sample operation %d\n"
+          "// backward %d: %s\n"
           "__device__ __noinline__ void bwd%d(const float* __restrict__ A, float* __restrict__ dist,\n"
           "    const unsigned char* __restrict__ sg, const float* __restrict__ spri, const u32* cL, const u32* cR,\n"
           "    float th, float an, float th2, float an2, int lane, signed char* assign, const double* sdraw,\n"
-          "    int* status) {\n"
+          "    int* status%s%s) {\n%s"
           "  const int v = lane & 3;\n  {\n",
-          k, k);
-    emit_dists(s, in, op);
-    emit_cut_masks(s, in, op);
+          id, sh.key.c_str(), id, consts.empty() ? ", int di, " : "", consts.empty() ? params(sh).c_str() : "",
+          consts.empty() ? "" : (consts + "  const int di = " + std::to_string(di) + ";\n  (void)mat;\n").c_str());
+    emit_dists(s, sh);
+    emit_cut_masks(s, sh);
     s += "      int cellidx = 0;\n      bool known = true;\n";
-    for (int q = 0; q < op.c; ++q)
-        emitf(s, "      { const int a = assign[%d]; known = known && a >= 0; cellidx |= (a & 3) << %d; }\n", cut[q],
+    for (int q = 0; q < sh.c; ++q)
+        emitf(s, "      { const int a = assign[cu%d]; known = known && a >= 0; cellidx |= (a & 3) << %d; }\n", q,
               2 * q);
     s += "      float pv = 0.0f;\n";
-    emitf(s, "      if (lane < 4 && known) {\n        const float tv = spri[4 * (sg[%d] & 3) + lane];\n", op.peel);
-    emitf(s, "        if (tv != 0.0f && %s) {\n", valid_expr(in, op, "cellidx").c_str());
-    emitf(s, "          const int ext = cellidx | (v << %d);\n", 2 * op.c);
-    emit_term(s, in, op, "          ");
+    s += "      if (lane < 4 && known) {\n        const float tv = spri[4 * (sg[pe] & 3) + lane];\n";
+    emitf(s, "        if (tv != 0.0f && %s) {\n", valid_expr(sh, "cellidx").c_str());
+    emitf(s, "          const int ext = cellidx | (v << %d);\n", 2 * sh.c);
+    emit_term(s, sh, "          ");
     s += "          pv = tmp;\n        }\n      }\n";
     emitf(s,
           "      const float p0 = __shfl_sync(FULL, pv, 0), p1 = __shfl_sync(FULL, pv, 1);\n"
@@ -214,7 +300,7 @@ void emit_backward(std::string& s, const JitLsIn& in, int k) {
           "        const float tot = __fadd_rn(__fadd_rn(__fadd_rn(p0, p1), p2), p3);\n"
           "        if (tot != 0.0f)\n"
           "          for (int q = 0; q < 4; ++q) pd[q] = __fdiv_rn(pd[q], tot);\n"
-          "        const double r = sdraw[%d];\n"
+          "        const double r = sdraw[di];\n"
           "        float acc = 0.0f;\n"
           "        int lastv = 0, pick = -1;\n"
           "        for (int q = 0; q < 4; ++q) {\n"
@@ -222,10 +308,10 @@ void emit_backward(std::string& s, const JitLsIn& in, int k) {
           "          if (r < (double)acc) { pick = q; break; }\n"
           "          if (pd[q] != 0.0f) lastv = q;\n"
           "        }\n"
-          "        assign[%d] = (signed char)(pick >= 0 ? pick : lastv);\n"
+          "        assign[pe] = (signed char)(pick >= 0 ? pick : lastv);\n"
           "      }\n"
           "      __syncwarp();\n  }\n}\n",
-          (int)ST_ILLEGAL_DG, in.K - 1 - k, op.peel);
+          (int)ST_ILLEGAL_DG);
 }
 
 std::string source(const JitLsIn& in, int wpb) {
@@ -269,10 +355,35 @@ std::string source(const JitLsIn& in, int wpb) {
     }
     if (nb == 0) s += "0";
     s += "};\n";
-    // one function per operation and pass: small functions keep NVRTC's
-    // optimiser (superlinear in a function's size) fast
-    for (int k = 0; k < in.K; ++k) emit_forward(s, in, k);
-    for (int k = in.K - 1; k >= 0; --k) emit_backward(s, in, k);
+    // small functions keep NVRTC's optimiser (superlinear in a function's
+    // size) fast: up to 150 operations, one per operation and pass with the
+    // operation's values as constants (the fastest code); above, one per
+    // operation shape and pass, the values passed in (a few dozen functions:
+    // seconds to compile, a smaller instruction footprint, somewhat more
+    // address arithmetic)
+    const bool per_op = in.K <= 150;
+    std::vector<int> shape_id(in.K);
+    std::vector<std::string> keys;
+    for (int k = 0; k < in.K; ++k) {
+        const Shape sh = shape_of(in, in.ops[k]);
+        if (per_op) {
+            const std::string cp = const_prologue(in, in.ops[k], sh);
+            emit_forward(s, sh, k, cp);
+            emit_backward(s, sh, k, cp, in.K - 1 - k);
+            shape_id[k] = k;
+            continue;
+        }
+        int id = -1;
+        for (size_t i = 0; i < keys.size(); ++i)
+            if (keys[i] == sh.key) id = (int)i;
+        if (id < 0) {
+            id = (int)keys.size();
+            keys.push_back(sh.key);
+            emit_forward(s, sh, id, "");
+            emit_backward(s, sh, id, "", 0);
+        }
+        shape_id[k] = id;
+    }
     emitf(s,
           "extern \"C\" __global__ void __launch_bounds__(WPB * 32) sl_ls_jit(u32* dg, int first, int nchain,\n"
           "    const int* loci, int nloci, const double* u, long long ucs, long long uls, u64 seed, u64 iter,\n"
@@ -313,7 +424,9 @@ std::string source(const JitLsIn& in, int wpb) {
           "      if (hasL) { th2 = tf[l - 1]; an2 = 1.0f - th2; }\n"
           "      if (hasR) { th = tf[l]; an = 1.0f - th; } }\n",
           in.N, in.N, in.W, in.W, in.W, in.M - 1);
-    for (int k = 0; k < in.K; ++k) emitf(s, "    fwd%d(A, dist, sg, spri, cL, cR, th, an, th2, an2, lane);\n", k);
+    for (int k = 0; k < in.K; ++k)
+        emitf(s, "    fwd%d(A, dist, sg, spri, cL, cR, th, an, th2, an2, lane%s%s);\n", shape_id[k],
+              per_op ? "" : ", ", per_op ? "" : call_args(in, in.ops[k]).c_str());
     emitf(s,
           "    if (A[%d] == 0.0f) {\n"
           "      if (lane == 0) atomicCAS(status, 0, %d);\n"
@@ -328,8 +441,13 @@ std::string source(const JitLsIn& in, int wpb) {
           "    }\n"
           "    __syncwarp();\n",
           in.ops[in.K - 1].mat_off, (int)ST_ZERO_LIK, in.N, in.K);
-    for (int k = in.K - 1; k >= 0; --k)
-        emitf(s, "    bwd%d(A, dist, sg, spri, cL, cR, th, an, th2, an2, lane, assign, sdraw, status);\n", k);
+    for (int k = in.K - 1; k >= 0; --k) {
+        if (per_op)
+            emitf(s, "    bwd%d(A, dist, sg, spri, cL, cR, th, an, th2, an2, lane, assign, sdraw, status);\n", k);
+        else
+            emitf(s, "    bwd%d(A, dist, sg, spri, cL, cR, th, an, th2, an2, lane, assign, sdraw, status, %d, %s);\n",
+                  shape_id[k], in.K - 1 - k, call_args(in, in.ops[k]).c_str());
+    }
     // meiosis indicators (locus_sampler2.cc:32-125)
     emitf(s,
           "    {\n"
