@@ -120,54 +120,53 @@ Shape shape_of(const JitLsIn& in, const OpDev& op) {
     return sh;
 }
 
-// the operation's run-time values, in the order of the shape functions' trailing parameters
-std::string call_args(const JitLsIn& in, const OpDev& op) {
-    std::string a = std::to_string(op.peel) + ", " + std::to_string(op.mat_off);
+// An operation's values that a shape function takes as parameters: the peel
+// node, its rfunction's offset, the cutset members, the previous rfunctions'
+// offsets, the children's (or the peeled child's) first meiosis bits.
+std::vector<std::string> value_names(const Shape& sh) {
+    std::vector<std::string> n = {"pe", "mat"};
+    for (int q = 0; q < sh.c; ++q) n.push_back("cu" + std::to_string(q));
+    for (int j = 0; j < sh.n_prev; ++j) n.push_back("mo" + std::to_string(j));
+    if (sh.type == CHILD) n.push_back("cb0");
+    for (int c = 0; c < sh.n_child; ++c) n.push_back("cb" + std::to_string(c));
+    return n;
+}
+
+std::vector<int> op_values(const JitLsIn& in, const OpDev& op) {
+    std::vector<int> v = {op.peel, op.mat_off};
     const int32_t* cut = in.opdata + op.cut_at;
-    for (int q = 0; q < op.c; ++q) a += ", " + std::to_string(cut[q]);
+    for (int q = 0; q < op.c; ++q) v.push_back(cut[q]);
     const int32_t* pd = in.opdata + op.prev_at;
     for (int j = 0; j < op.n_prev; ++j) {
-        a += ", " + std::to_string(pd[0]);
+        v.push_back(pd[0]);
         pd += 2 + pd[1];
     }
-    if (op.type == CHILD) a += ", " + std::to_string(2 * (op.peel - in.F));
+    if (op.type == CHILD) v.push_back(2 * (op.peel - in.F));
     if (op.type == PARENT) {
         const int32_t* cd = in.opdata + op.child_at;
-        for (int c = 0; c < op.n_child; ++c) a += ", " + std::to_string(2 * (cd[4 * c] - in.F));
+        for (int c = 0; c < op.n_child; ++c) v.push_back(2 * (cd[4 * c] - in.F));
     }
+    return v;
+}
+
+std::string call_args(const JitLsIn& in, const OpDev& op) {
+    std::string a;
+    for (int x : op_values(in, op)) a += (a.empty() ? "" : ", ") + std::to_string(x);
     return a;
 }
 
 // the same values as constants, for a function made for one operation
 std::string const_prologue(const JitLsIn& in, const OpDev& op, const Shape& sh) {
-    std::string names = "pe, mat";
-    for (int q = 0; q < sh.c; ++q) names += ", cu" + std::to_string(q);
-    for (int j = 0; j < sh.n_prev; ++j) names += ", mo" + std::to_string(j);
-    if (sh.type == CHILD) names += ", cb0";
-    for (int c = 0; c < sh.n_child; ++c) names += ", cb" + std::to_string(c);
-    // pair the names with the call arguments
-    std::string vals = call_args(in, op), out = "  const int ";
-    size_t a = 0, b = 0;
-    bool first = true;
-    while (a < names.size()) {
-        size_t na = names.find(", ", a), nb = vals.find(", ", b);
-        const std::string n = names.substr(a, na == std::string::npos ? std::string::npos : na - a);
-        const std::string v = vals.substr(b, nb == std::string::npos ? std::string::npos : nb - b);
-        out += (first ? "" : ", ") + n + " = " + v;
-        first = false;
-        if (na == std::string::npos) break;
-        a = na + 2;
-        b = nb + 2;
-    }
+    const std::vector<std::string> n = value_names(sh);
+    const std::vector<int> v = op_values(in, op);
+    std::string out = "  const int ";
+    for (size_t i = 0; i < n.size(); ++i) out += (i ? ", " : "") + n[i] + " = " + std::to_string(v[i]);
     return out + ";\n";
 }
 
 std::string params(const Shape& sh) {
-    std::string p = "int pe, int mat";
-    for (int q = 0; q < sh.c; ++q) p += ", int cu" + std::to_string(q);
-    for (int j = 0; j < sh.n_prev; ++j) p += ", int mo" + std::to_string(j);
-    if (sh.type == CHILD) p += ", int cb0";
-    for (int c = 0; c < sh.n_child; ++c) p += ", int cb" + std::to_string(c);
+    std::string p;
+    for (const std::string& x : value_names(sh)) p += (p.empty() ? "int " : ", int ") + x;
     return p;
 }
 
