@@ -425,3 +425,25 @@ def test_specialised_lsampler_is_bit_identical(name):
     a, b = out[api.SL_LS_KERNEL_GENERIC], out[api.SL_LS_KERNEL_SPECIALISED]
     assert np.array_equal(a[0], b[0])
     assert np.array_equal(a[1], b[1])
+
+
+@pytest.mark.gpu
+def test_specialised_lsampler_shared_shapes_is_bit_identical():
+    """Above 150 operations the compiled L-sampler shares one function among
+    operations of the same shape and passes their values in; it too leaves the
+    generic kernel's graphs bit for bit (a 170-member synthetic pedigree)."""
+    from swiftlink_gb300 import pedigree, synth
+    spec = synth.WorkloadSpec(n_members=170, generations=5, loops=3, affected=20, markers=60, spacing_cm=0.5,
+                              maf=(0.05, 0.5), missing_all=0.05)
+    d = pedigree.problem_from_workload(synth.make_workload(3, seed=77, spec=spec))
+    assert d["K"] > 150
+    C = 4
+    out = {}
+    for lk in (api.SL_LS_KERNEL_GENERIC, api.SL_LS_KERNEL_SPECIALISED):
+        with api.Context(api.Problem.from_arrays(d, with_legal=False), n_chains=C,
+                         sampler_precision=api.SL_SAMPLER_FAST, ls_kernel=lk) as ctx:
+            assert ctx.ls_kernel_info()[0] == lk
+            ctx.set_graphs(np.stack([d["dg0"]] * C))
+            ctx.run(iterations=8, burnin=0, period=4, lprob=1.0, seed=5)
+            out[lk] = ctx.get_graphs()
+    assert np.array_equal(out[api.SL_LS_KERNEL_GENERIC], out[api.SL_LS_KERNEL_SPECIALISED])
