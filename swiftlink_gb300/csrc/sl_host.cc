@@ -1154,6 +1154,29 @@ int sl_create(const sl_problem_desc* d, const sl_options* opt, sl_ctx** out) {
     if ((rc = upload(ctx, (int16_t**)&P.mother, mo.data(), N))) return bail(rc);
     if ((rc = upload(ctx, (int16_t**)&P.father, fa.data(), N))) return bail(rc);
     if ((rc = upload(ctx, (uint8_t**)&P.geno, geno.data(), geno.size()))) return bail(rc);
+    {   // each locus's typed members for the founder-allele graphs, heterozygotes first
+        if (N > 16383) return bail(fail(nullptr, SL_EINVAL, "more than 16383 members"));
+        std::vector<int32_t> off(M + 1, 0);
+        std::vector<uint16_t> ent, nhet(M);
+        ent.reserve((size_t)M * N);
+        for (int l = 0; l < M; ++l) {
+            off[l] = (int32_t)ent.size();
+            int nh = 0;
+            for (int pass = 0; pass < 2; ++pass)
+                for (int i = 0; i < N; ++i) {
+                    const int g = geno[(size_t)l * N + i] & 3;
+                    if (g == G_UNTYPED || (g == G_HETERO) != (pass == 0)) continue;
+                    ent.push_back((uint16_t)(i << 2 | g));
+                    nh += pass == 0;
+                }
+            nhet[l] = (uint16_t)nh;
+        }
+        off[M] = (int32_t)ent.size();
+        if (ent.empty()) ent.push_back(0);
+        if ((rc = upload(ctx, (int32_t**)&P.typ_off, off.data(), off.size()))) return bail(rc);
+        if ((rc = upload(ctx, (uint16_t**)&P.typ_ent, ent.data(), ent.size()))) return bail(rc);
+        if ((rc = upload(ctx, (uint16_t**)&P.typ_nhet, nhet.data(), nhet.size()))) return bail(rc);
+    }
     if ((rc = upload(ctx, (uint8_t**)&P.typed, typed.data(), N))) return bail(rc);
     if ((rc = upload(ctx, (double**)&P.prior, ctx->prior_table.data(), ctx->prior_table.size()))) return bail(rc);
     if ((rc = upload(ctx, (double**)&P.theta, d->theta, M - 1))) return bail(rc);

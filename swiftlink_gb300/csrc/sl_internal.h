@@ -34,6 +34,9 @@ struct ProblemDev {
     const int16_t* mother;               // [N], -1 for founders
     const int16_t* father;
     const uint8_t* geno;                 // [M][N]: bits 0-1 genotype code, bits 4-7 legal mask
+    const int32_t* typ_off;              // [M+1] each locus's typed members in typ_ent
+    const uint16_t* typ_ent;             // member << 2 | genotype code, heterozygotes first, members in order
+    const uint16_t* typ_nhet;            // [M] heterozygotes per locus
     const uint8_t* typed;                // [N]
     const double* prior;                 // [M][4 genotype codes][4 states]
     const double* theta;                 // [M-1]

@@ -1107,24 +1107,19 @@ __device__ __forceinline__ void fagw_task(const ProblemDev& P, const FagwTables&
     volatile int* Lb = (volatile int*)(wbase + (((size_t)4 * N + 15) & ~(size_t)15));   // [2F] 2 * parent + parity
     int* fl = (int*)(Lb + nfa);                                       // [2F] bit0 used, bit1 fixed A, bit2 fixed B
     int* cnt = fl + nfa;                                              // [2F] per component: counts, forbidden colourings
-    uint32_t* hed = (uint32_t*)(cnt + nfa);                           // [N] heterozygote edges, u | v << 16
+    uint16_t* typ = (uint16_t*)(cnt + nfa);                           // [N] the locus's typed members
     const int lc = valid ? l : 0;
     const uint32_t* col = dg + ((size_t)chain * M + lc) * P.W;
     float* raw = rawbuf + (size_t)cr * 2 * M;
-    const uint8_t* gcol = P.geno + (size_t)lc * N;
     // the task's global reads issued together: the column's words (lane w of
-    // the group holds word w, read by shuffles), the genotype codes of this
-    // lane's members (16 x 2 bits; untyped members read as 0), the minor-allele
-    // frequency
+    // the group holds word w, read by shuffles), the locus's typed members
+    // (member << 2 | genotype code, heterozygotes first: fixed by the
+    // genotypes, listed once at context creation), the minor-allele frequency
     const bool wreg = P.W <= G;
     const uint32_t cw = wreg && gl < P.W ? col[gl] : 0u;
-    uint32_t gpack = 0u;
-#pragma unroll
-    for (int k = 0; k < 16; ++k) {
-        if (k * G >= N) break;
-        if (k * G + gl < N) gpack |= (uint32_t)(gcol[k * G + gl] & 3) << (2 * k);
-    }
+    const int t0 = P.typ_off[lc], ntyp = P.typ_off[lc + 1] - t0, nhet = P.typ_nhet[lc];
     const double minor_d = P.c_minor[(size_t)chain * M + lc];
+    for (int x = gl; x < ntyp; x += G) typ[x] = P.typ_ent[t0 + x];
     auto cbit = [&](int b) -> int {
         const uint32_t w = wreg ? grp.shfl(cw, b >> 5) : col[b >> 5];
         return (int)((w >> (b & 31)) & 1u);
@@ -1168,31 +1163,20 @@ __device__ __forceinline__ void fagw_task(const ProblemDev& P, const FagwTables&
         fl[x] = 0;
     }
     __syncwarp();
-    // heterozygote edges are also listed, compacted, for the union phase
-    int bad = 0, nhet = 0;
-    for (int base = 0, k = 0; base < N; base += G, ++k) {
-        const int i = base + gl;
-        int g = G_UNTYPED, u = 0, v = 0;
-        if (i < N) {
-            g = k < 16 ? (int)((gpack >> (2 * k)) & 3u) : (gcol[i] & 3);
-            if (g != G_UNTYPED) {
-                u = e[2 * i];
-                v = e[2 * i + 1];
-            }
-        }
-        const bool het = g == G_HETERO;
-        const unsigned hm = grp.ballot(het);
-        if (het) {
+    // the typed members mark their founder alleles (no warp primitive inside:
+    // the groups' loci have lists of their own lengths)
+    int bad = 0;
+    for (int x = gl; x < ntyp; x += G) {
+        const int ent = typ[x], i = ent >> 2, g = ent & 3;
+        const int u = e[2 * i], v = e[2 * i + 1];
+        int bits = 1;
+        if (g == G_HETERO) {
             if (u == v) bad = 1;
-            atomicOr(&fl[u], 1);
-            atomicOr(&fl[v], 1);
-            hed[nhet + __popc(hm & ((1u << gl) - 1u))] = (uint32_t)u | ((uint32_t)v << 16);
-        } else if (g != G_UNTYPED) {
-            const int bits = 1 | (g == G_HOMOZ_A ? 2 : 4);
-            atomicOr(&fl[u], bits);
-            atomicOr(&fl[v], bits);
+        } else {
+            bits |= g == G_HOMOZ_A ? 2 : 4;
         }
-        nhet += __popc(hm);
+        atomicOr(&fl[u], bits);
+        atomicOr(&fl[v], bits);
     }
     bad = grp.any(bad);
     __syncwarp();
@@ -1206,8 +1190,8 @@ __device__ __forceinline__ void fagw_task(const ProblemDev& P, const FagwTables&
     const bool unite = !bad && nhet > 0;
     if (unite) {
         for (int q = gl; q < nhet; q += G) {
-            const uint32_t h = hed[q];
-            const int u = (int)(h & 0xffffu), v = (int)(h >> 16);
+            const int i = typ[q] >> 2;   // the heterozygotes lead the list
+            const int u = e[2 * i], v = e[2 * i + 1];
             for (int tries = 0;; ++tries) {
                 if (tries > nfa) {
                     bad = 1;
