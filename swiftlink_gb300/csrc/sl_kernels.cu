@@ -1161,6 +1161,7 @@ __device__ __forceinline__ void fagw_task(const ProblemDev& P, const FagwTables&
     for (int x = gl; x < nfa; x += G) {
         Lb[x] = x << 1;
         fl[x] = 0;
+        cnt[x] = 0;
     }
     __syncwarp();
     // the typed members mark their founder alleles (no warp primitive inside:
@@ -1186,7 +1187,7 @@ __device__ __forceinline__ void fagw_task(const ProblemDev& P, const FagwTables&
     // compare-and-swap (so a root is its component's smallest allele); an edge
     // whose ends already share a root must have ends of opposite parity.  A
     // failed hook means another lane's hook succeeded, so a lane retries fewer
-    // than 2F times.  Then every allele points at its root.
+    // than 2F times.
     const bool unite = !bad && nhet > 0;
     if (unite) {
         for (int q = gl; q < nhet; q += G) {
@@ -1211,26 +1212,17 @@ __device__ __forceinline__ void fagw_task(const ProblemDev& P, const FagwTables&
     }
     bad = grp.any(bad);
     __syncwarp();
-    if (unite && !bad)
-        for (int x = gl; x < nfa; x += G) {
-            int p;
-            const int r = pf_find(Lb, x, p);
-            Lb[x] = (r << 1) | p;
-        }
-    __syncwarp();
     // 4. sum over each component's colourings, log2: every member allele
     // contributes log2 of the major or the minor frequency, so a component
     // needs only its member count, how many members have even parity and
     // which colourings its fixed members forbid (integer shared-memory
     // atomics, the same result in any order)
     if (!bad)
-        for (int x = gl; x < nfa; x += G) cnt[x] = 0;
-    __syncwarp();
-    if (!bad)
         for (int x = gl; x < nfa; x += G) {
             const int f = fl[x];
             if (!(f & 1)) continue;
-            const int lx = Lb[x], r = lx >> 1, p = lx & 1;
+            int p = 0;
+            const int r = unite ? pf_find(Lb, x, p) : x;   // the forest is final: the unions are done
             // bit 16 + n: member count; bits 0-15: even-parity members; bits 29/30: colouring 0/1 forbidden
             const int add = (1 << 16) + (p ? 0 : 1);
             int forbid = 0;
