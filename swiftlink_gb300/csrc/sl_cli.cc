@@ -620,7 +620,11 @@ int main(int argc, char** argv) {
             // choice of SL_LOD_KERNEL_AUTO can differ from run to run in the last FP32 bits)
             if (!o.exact) so.lod_kernel = SL_LOD_KERNEL_JIT_REG;
             if (sl_create(&d, &so, &ctx) != SL_OK && !o.exact) {
+                // a kernel compiled at run time did not build: the generic kernels
+                fprintf(stderr, "note: pedigree '%s': %s; using the generic kernels\n", fams[f].id.c_str(),
+                        sl_last_error(nullptr));
                 so.lod_kernel = SL_LOD_KERNEL_INTERP;
+                so.ls_kernel = SL_LS_KERNEL_GENERIC;
                 ctx = nullptr;
                 if (sl_create(&d, &so, &ctx) != SL_OK) ctx = nullptr;
             }
