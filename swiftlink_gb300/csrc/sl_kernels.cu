@@ -19,10 +19,33 @@
 #include <float.h>
 #include <stdint.h>
 
+#include <map>
+#include <mutex>
+#include <utility>
+
 #include "sl_internal.h"
 #include "sl_philox.cuh"
 
 namespace sl {
+
+// Raises a kernel's dynamic shared-memory limit on the current device when a
+// launch needs more than it was given so far.  The attribute is per device
+// and contexts on several devices or threads may launch the same kernel, so
+// the record is keyed by (kernel, device) and taken under a lock.
+static cudaError_t ensure_smem(const void* func, size_t bytes) {
+    if (bytes <= 48 * 1024) return cudaSuccess;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    static std::mutex mu;
+    static std::map<std::pair<const void*, int>, size_t> given;
+    std::lock_guard<std::mutex> lock(mu);
+    size_t& have = given[std::make_pair(func, dev)];
+    if (bytes <= have) return cudaSuccess;
+    e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess) have = bytes;
+    return e;
+}
 
 #define DMUL __dmul_rn
 #define DADD __dadd_rn
@@ -2246,15 +2269,11 @@ cudaError_t launch_loglik_parts(const ProblemDev& P, const uint32_t* dg, const i
                                 double* fag_out, double* rec_out, cudaStream_t s) {
     const int S = 64;
     const size_t smem = fag_block_bytes(P.N, P.F, S, 0);
-    static size_t configured[2] = {0, 0};
     const int wide = 2 * P.F > 255 ? 1 : 0;
-    if (smem > configured[wide]) {
-        cudaError_t e = wide ? cudaFuncSetAttribute(loglik_fag_kernel<uint16_t>,
-                                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
-                             : cudaFuncSetAttribute(loglik_fag_kernel<uint8_t>,
-                                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    {
+        cudaError_t e = ensure_smem(wide ? (const void*)loglik_fag_kernel<uint16_t> : (const void*)loglik_fag_kernel<uint8_t>,
+                                    smem);
         if (e != cudaSuccess) return e;
-        configured[wide] = smem;
     }
     const int4 g4 = make_int4(gch[0], gch[1], gch[2], gch[3]), t4 = make_int4(tch[0], tch[1], tch[2], tch[3]);
     const int64_t nf = (int64_t)npair * P.M;
@@ -2392,22 +2411,16 @@ cudaError_t launch_lsampler(const ProblemDev& P, uint32_t* dg, int first, int nc
                             const uint8_t* sel, int want, int* status, cudaStream_t s, int grid_cap, int wpb,
                             const uint64_t* key) {
     const size_t smem = ls_tables_bytes(P) + wpb * lsampler_smem_per_warp(P);
-    static size_t configured[2] = {0, 0};
-    const int f = P.ls_fast ? 1 : 0;
-    if (smem > configured[f]) {
-        cudaError_t e = f ? cudaFuncSetAttribute(lsampler_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                 (int)smem)
-                          : cudaFuncSetAttribute(lsampler_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                 (int)smem);
+    {
+        cudaError_t e = ensure_smem(P.ls_fast ? (const void*)lsampler_kernel<float> : (const void*)lsampler_kernel<double>, smem);
         if (e != cudaSuccess) return e;
-        configured[f] = smem;
     }
     Draws d{u, ucs, uls, seed, iter, 1, key};
     const int64_t ntask = (int64_t)nchain * nloci;
     int64_t grid = (ntask + wpb - 1) / wpb;
     if (grid > grid_cap) grid = grid_cap;
     if (grid < 1) grid = 1;
-    if (f)
+    if (P.ls_fast)
         lsampler_kernel<float><<<(int)grid, wpb * 32, smem, s>>>(P, dg, first, nchain, loci, nloci, d, sel, want,
                                                                  status);
     else
@@ -2443,20 +2456,14 @@ cudaError_t launch_si(const ProblemDev& P, uint32_t* dg, int first, int nchain, 
                       const double* u, int64_t ucs, uint64_t seed, uint64_t pass, double* weights, int* status,
                       cudaStream_t s, int wpb, int npass, int64_t pass_stride, int grid_cap) {
     const size_t smem = ls_tables_bytes(P) + wpb * lsampler_smem_per_warp(P);
-    static size_t configured[2] = {0, 0};
-    const int f = P.ls_fast ? 1 : 0;
-    if (smem > configured[f]) {
-        cudaError_t e = f ? cudaFuncSetAttribute(si_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                 (int)smem)
-                          : cudaFuncSetAttribute(si_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                 (int)smem);
+    {
+        cudaError_t e = ensure_smem(P.ls_fast ? (const void*)si_kernel<float> : (const void*)si_kernel<double>, smem);
         if (e != cudaSuccess) return e;
-        configured[f] = smem;
     }
     Draws d{u, ucs, 0, seed, pass, 5, nullptr};
     int grid = (nchain * npass + wpb - 1) / wpb;
     if (grid > grid_cap) grid = grid_cap;
-    if (f)
+    if (P.ls_fast)
         si_kernel<float><<<grid, wpb * 32, smem, s>>>(P, dg, first, nchain, starts, d, 0, weights, status, npass,
                                                       pass_stride);
     else
@@ -2482,11 +2489,9 @@ static cudaError_t launch_msampler_t(const ProblemDev& P, uint32_t* dg, int firs
     cudaError_t e0 = cudaMemsetAsync(badc, 0, (size_t)nchain, s);
     if (e0 != cudaSuccess) return e0;
     const size_t smem = fag_block_bytes(P.N, P.F, fag_threads, fast);
-    static size_t configured = 0;
-    if (smem > configured) {
-        cudaError_t e = cudaFuncSetAttribute(fag_kernel<IX, PP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    {
+        cudaError_t e = ensure_smem((const void*)fag_kernel<IX, PP>, smem);
         if (e != cudaSuccess) return e;
-        configured = smem;
     }
     const int scan_threads = ffbs_scan_threads(P.M);
     size_t scan_smem = ffbs_scan_smem(P.M);
@@ -2495,11 +2500,9 @@ static cudaError_t launch_msampler_t(const ProblemDev& P, uint32_t* dg, int firs
         scan_smem = ffbs_scan_scratch(scan_threads);
         staged = 0;
     }
-    static size_t scan_configured = 0;
-    if (!exact && scan_smem > scan_configured) {
-        cudaError_t e = cudaFuncSetAttribute(ffbs_scan_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)scan_smem);
+    if (!exact) {
+        cudaError_t e = ensure_smem((const void*)ffbs_scan_kernel, scan_smem);
         if (e != cudaSuccess) return e;
-        scan_configured = scan_smem;
     }
     const int64_t ntask = (int64_t)nchain * P.M;
     const int grid = (int)((ntask + fag_threads - 1) / fag_threads);
@@ -2511,12 +2514,9 @@ static cudaError_t launch_msampler_t(const ProblemDev& P, uint32_t* dg, int firs
     const int G = pairs && P.W <= 16 ? 16 : 32;
     const size_t wsm = fagw_block_bytes(P.N, P.F, G);
     const bool warp_like = !exact && wsm <= 200 * 1024 && 2 * P.F < 8192;
-    static size_t wconfigured[2] = {0, 0};
-    if (warp_like && wsm > wconfigured[G == 16]) {
-        cudaError_t e = cudaFuncSetAttribute(G == 16 ? fag_warp_kernel<16> : fag_warp_kernel<32>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wsm);
+    if (warp_like) {
+        cudaError_t e = ensure_smem(G == 16 ? (const void*)fag_warp_kernel<16> : (const void*)fag_warp_kernel<32>, wsm);
         if (e != cudaSuccess) return e;
-        wconfigured[G == 16] = wsm;
     }
     const int lpb = kFagWarpsPerBlock * (32 / G);   // loci per block
     const dim3 wgrid((unsigned)((P.M + lpb - 1) / lpb), (unsigned)nchain);
@@ -2585,41 +2585,33 @@ cudaError_t launch_lod(const ProblemDev& P, int precision, const uint32_t* graph
     if (grid < 1) grid = 1;
     if (precision == 0) {
         const size_t smem = (size_t)wpb * P.arena * sizeof(double);
-        static size_t configured = 0;
-        if (smem > configured) {
-            cudaError_t e = cudaFuncSetAttribute(lod_kernel<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        {
+            cudaError_t e = ensure_smem((const void*)lod_kernel<double, false>, smem);
             if (e != cudaSuccess) return e;
-            configured = smem;
         }
         lod_kernel<double, false><<<(int)grid, wpb * 32, smem, s>>>(P, graphs, graph_words, G, vals, status);
     } else if (precision == 2) {   // FP64 with per-rfunction power-of-two rescaling
         const size_t smem = (size_t)wpb * P.arena * sizeof(double);
-        static size_t configured = 0;
-        if (smem > configured) {
-            cudaError_t e = cudaFuncSetAttribute(lod_kernel<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        {
+            cudaError_t e = ensure_smem((const void*)lod_kernel<double, true>, smem);
             if (e != cudaSuccess) return e;
-            configured = smem;
         }
         lod_kernel<double, true><<<(int)grid, wpb * 32, smem, s>>>(P, graphs, graph_words, G, vals, status);
     } else if (P.prog) {
         const int S = P.prog_threads;
         const size_t smem = (size_t)S * P.prog_slots * sizeof(float);
-        static size_t configured_prog = 0;
-        if (smem > configured_prog) {
-            cudaError_t e = cudaFuncSetAttribute(lod_prog_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        {
+            cudaError_t e = ensure_smem((const void*)lod_prog_kernel, smem);
             if (e != cudaSuccess) return e;
-            configured_prog = smem;
         }
         int64_t pgrid = (ntask + S - 1) / S;
         if (pgrid > grid_cap * 4) pgrid = grid_cap * 4;
         lod_prog_kernel<<<(int)pgrid, S, smem, s>>>(P, graphs, graph_words, G, vals, status);
     } else {
         const size_t smem = (size_t)wpb * P.arena * sizeof(float);
-        static size_t configured = 0;
-        if (smem > configured) {
-            cudaError_t e = cudaFuncSetAttribute(lod_kernel<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        {
+            cudaError_t e = ensure_smem((const void*)lod_kernel<float, true>, smem);
             if (e != cudaSuccess) return e;
-            configured = smem;
         }
         lod_kernel<float, true><<<(int)grid, wpb * 32, smem, s>>>(P, graphs, graph_words, G, vals, status);
     }
