@@ -114,9 +114,17 @@ typedef struct sl_options {
  * pedigree's operations written in as constants (NVRTC for sm_103a: seconds to
  * tens of seconds for a 100-member pedigree; sl_create fails if it does not
  * build); it performs the same rounded operations in the same order, so both
- * draw bit-identical graphs, and it pays off on long runs. */
+ * draw bit-identical graphs, and it pays off on long runs.  BACKGROUND starts
+ * the same compile on a host thread at sl_create and runs the generic kernel
+ * until the compile ends; the context then switches to the specialised kernel
+ * at its next sl_run, sl_batch_run or L-sampler call (runs are issued in short
+ * spans meanwhile, so a long run switches while it runs), or keeps the generic
+ * kernel if the compile failed.  The graphs are the same either way.
+ * sl_destroy waits for a compile still running.  Identical sources compile
+ * once per process (a cache of recent kernels shared by all contexts). */
 #define SL_LS_KERNEL_GENERIC 0
 #define SL_LS_KERNEL_SPECIALISED 1
+#define SL_LS_KERNEL_BACKGROUND 2
 
 /* A LOD position whose trait likelihood is 0 (an affected and an unaffected
  * member IBD 2 under a fully penetrant model, for instance) stops the
@@ -352,7 +360,10 @@ int sl_problem_trait_backward_eval(const sl_problem_desc* problem, const int32_t
 int sl_lod_kernel_info(sl_ctx* ctx, int32_t* kernel, double* compile_ms);
 
 /* The L-sampler kernel in use (SL_LS_KERNEL_GENERIC or SL_LS_KERNEL_SPECIALISED)
- * and the milliseconds spent compiling the specialised form at sl_create. */
+ * and the milliseconds the specialised form took to compile (0 if none was
+ * asked for; -1 while a background compile is still running; a background
+ * compile that failed leaves GENERIC with its time, and its reason in
+ * sl_last_error).  A background compile that has ended is taken up here. */
 int sl_ls_kernel_info(sl_ctx* ctx, int32_t* kernel, double* compile_ms);
 
 /*

@@ -21,7 +21,7 @@ SL_LOD_FP64, SL_LOD_FP32_RESCALED, SL_LOD_FP64_RESCALED = 0, 1, 2
 SL_SAMPLER_EXACT, SL_SAMPLER_FAST = 0, 1
 SL_LOD_KERNEL_AUTO, SL_LOD_KERNEL_INTERP, SL_LOD_KERNEL_JIT_REG, SL_LOD_KERNEL_JIT_SMEM = 0, 1, 2, 3
 SL_LOD_ZERO_OK = 1
-SL_LS_KERNEL_GENERIC, SL_LS_KERNEL_SPECIALISED = 0, 1
+SL_LS_KERNEL_GENERIC, SL_LS_KERNEL_SPECIALISED, SL_LS_KERNEL_BACKGROUND = 0, 1, 2
 
 EXPORTED = [
     "sl_create", "sl_destroy", "sl_last_error", "sl_set_descent_graphs", "sl_get_descent_graphs",
@@ -307,7 +307,8 @@ class Context:
         self._check(lib().sl_lod_reset(self.h))
 
     def ls_kernel_info(self):
-        """(SL_LS_KERNEL_GENERIC or SL_LS_KERNEL_SPECIALISED in use, milliseconds spent compiling it)."""
+        """(SL_LS_KERNEL_GENERIC or SL_LS_KERNEL_SPECIALISED in use, milliseconds spent compiling it;
+        -1 while a background compile runs)."""
         k = ctypes.c_int32()
         ms = ctypes.c_double()
         self._check(lib().sl_ls_kernel_info(self.h, ctypes.byref(k), ctypes.byref(ms)))

@@ -608,10 +608,12 @@ int main(int argc, char** argv) {
         so.lod_precision = o.exact ? SL_LOD_FP64 : SL_LOD_FP32_RESCALED;
         so.sampler_precision = o.exact ? SL_SAMPLER_EXACT : SL_SAMPLER_FAST;
         so.lod_flags = SL_LOD_ZERO_OK;
-        // long runs amortise compiling the L-sampler for the pedigree (same draws, same graphs)
-        // (up to 2000 members: the generated source grows with the peel's shapes, and so does its compile time)
+        // long runs amortise compiling the L-sampler for the pedigree (same draws, same graphs); it
+        // compiles on a host thread while the run starts on the generic kernel, and pedigrees compile
+        // side by side (up to 2000 members: the generated source grows with the peel's shapes, and so
+        // does its compile time)
         so.ls_kernel = !o.exact && !o.generic_ls && o.burnin + o.iterations >= 10000 && p.N <= 2000
-                           ? SL_LS_KERNEL_SPECIALISED
+                           ? SL_LS_KERNEL_BACKGROUND
                            : SL_LS_KERNEL_GENERIC;
         for (int r = 0; r < (o.mc3 ? o.runs : 1) && !rc; ++r) {
             sl_ctx* ctx = nullptr;
@@ -723,6 +725,16 @@ int main(int argc, char** argv) {
                     }
             }
             for (const Trace& t : traces) fclose(t.fh);
+            for (const Unit& u : units) {
+                int32_t k = 0;
+                double ms = 0.0;
+                if (sl_ls_kernel_info(u.ctx, &k, &ms) != SL_OK) continue;
+                if (k == SL_LS_KERNEL_GENERIC && ms > 0.0)   // a compile that ended without a kernel
+                    fprintf(stderr, "note: pedigree '%s': %s\n", fams[u.fam].id.c_str(), sl_last_error(u.ctx));
+                else if (o.verbose && k == SL_LS_KERNEL_SPECIALISED)
+                    fprintf(stderr, "pedigree %s run %d: L-sampler compiled for the pedigree in %.1f s\n",
+                            fams[u.fam].id.c_str(), u.run, ms / 1000.0);
+            }
             if (o.mc3 && o.verbose && !rc)
                 for (const Unit& u : units) {
                     std::vector<int64_t> acc(std::max(1, o.chains - 1)), prop(acc.size());

@@ -6,11 +6,13 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <memory>
 #include <string>
 #include <cfloat>
 #include <chrono>
@@ -154,6 +156,14 @@ struct sl_ctx {
     int lod_kernel_req = SL_LOD_KERNEL_AUTO;
     JitLs jit_ls;                     // the FP32 L-sampler specialised to the pedigree (kern null: generic)
     double jit_ls_ms = 0.0;
+    // SL_LS_KERNEL_BACKGROUND: the compile runs on ls_thread; the context takes it up (ls_adopt) at its
+    // next run or L-sampler call after ls_pending turns 2
+    std::thread ls_thread;
+    std::atomic<int> ls_pending{0};             // 0 none, 1 compiling, 2 ended and not yet taken up
+    std::shared_ptr<const JitBinary> ls_bin;    // written by ls_thread before ls_pending = 2
+    double ls_thread_ms = 0.0;                  // likewise
+    size_t ls_warp_bytes = 0;
+    int ls_epoch = 0;                           // kernel switches (graphs captured before are redone)
     int lod_kernel_sel = SL_LOD_KERNEL_INTERP;   // AUTO while the first scoring has not timed them
     JitLod jit_reg, jit_smem;
     double jit_ms = 0.0;
@@ -200,6 +210,42 @@ static cudaError_t ls_launch(sl_ctx* ctx, int first, int nchain, const int32_t* 
     return launch_lsampler(P, ctx->d_dg, first, nchain, loci, nloci, u, ucs, uls, seed, iter, sel, want, ctx->d_status,
                            s, ctx->ls_grid, ctx->ls_wpb, key);
 }
+
+// Takes up a background compile of the specialised L-sampler that has ended:
+// loads it into the context's device and drops the run graph captured with the
+// generic kernel.  A compile or load that failed leaves the generic kernel and
+// its reason in the context's last error.
+static void ls_adopt(sl_ctx* ctx) {
+    if (ctx->ls_pending.load(std::memory_order_acquire) != 2) return;
+    ctx->ls_thread.join();
+    ctx->ls_pending.store(0, std::memory_order_relaxed);
+    ctx->jit_ls_ms = ctx->ls_thread_ms;
+    int cur = 0;
+    cudaGetDevice(&cur);
+    cudaSetDevice(ctx->device);
+    std::string log;
+    JitLs j;
+    if (jit_ls_load(*ctx->ls_bin, ctx->ls_wpb, ctx->ls_warp_bytes, &j, &log)) {
+        ctx->err = "specialised L-sampler failed (the generic kernel runs): " + log.substr(0, 300);
+    } else {
+        ctx->jit_ls = j;
+        ctx->jit_ls.compile_ms = ctx->ls_thread_ms;
+        if (ctx->run_graph) {
+            cudaStreamSynchronize(ctx->stream);   // no launch of it in flight
+            cudaGraphExecDestroy(ctx->run_graph);
+            ctx->run_graph = nullptr;
+        }
+        ++ctx->ls_epoch;
+    }
+    ctx->ls_bin.reset();
+    cudaSetDevice(cur);
+}
+
+static bool ls_compiling(const sl_ctx* ctx) { return ctx->ls_pending.load(std::memory_order_acquire) != 0; }
+
+// While a background compile runs, runs go in spans of this many iterations,
+// each waited for, so the context can switch kernels between two of them.
+constexpr int kPacedSpan = 10;
 
 struct Prof {
     sl_ctx* c;
@@ -998,6 +1044,7 @@ static int upload_chain_maps(sl_ctx* ctx) {
 
 void sl_destroy(sl_ctx* ctx) {
     if (!ctx) return;
+    if (ctx->ls_thread.joinable()) ctx->ls_thread.join();
     int cur = 0;
     cudaGetDevice(&cur);
     cudaSetDevice(ctx->device);
@@ -1319,10 +1366,17 @@ int sl_create(const sl_problem_desc* d, const sl_options* opt, sl_ctx** out) {
         else if (req == SL_LOD_KERNEL_AUTO) ctx->lod_kernel_sel = SL_LOD_KERNEL_AUTO;
         else ctx->lod_kernel_sel = req;
     }
+    std::string ls_src;
     {   // the FP32 L-sampler specialised to the pedigree, on request
         const int req = opt->ls_kernel;
-        if (req != SL_LS_KERNEL_GENERIC && req != SL_LS_KERNEL_SPECIALISED)
+        if (req != SL_LS_KERNEL_GENERIC && req != SL_LS_KERNEL_SPECIALISED && req != SL_LS_KERNEL_BACKGROUND)
             return bail(fail(nullptr, SL_EINVAL, "unknown ls_kernel %d", req));
+        if (P.ls_fast && req == SL_LS_KERNEL_BACKGROUND) {
+            // the source now (host tables in hand), the compile on a thread started once creation has succeeded
+            const JitLsIn in{ops.data(), od.data(), K, N, F, M, P.W, N - F, arena, max_child, d->mother, d->father};
+            ls_src = jit_ls_source(in, ctx->ls_wpb);
+            ctx->ls_warp_bytes = jit_ls_warp_bytes(in);
+        }
         if (P.ls_fast && req == SL_LS_KERNEL_SPECIALISED) {
             const JitLsIn in{ops.data(), od.data(), K, N, F, M, P.W, N - F, arena, max_child, d->mother, d->father};
             const auto t0 = std::chrono::steady_clock::now();
@@ -1351,6 +1405,16 @@ int sl_create(const sl_problem_desc* d, const sl_options* opt, sl_ctx** out) {
         D.slots = full.slots;
         D.nscale = full.nscale;
         ctx->has_adjoint = true;
+    }
+    if (!ls_src.empty()) {
+        ctx->ls_pending.store(1, std::memory_order_relaxed);
+        ctx->ls_thread = std::thread([ctx, src = std::move(ls_src)] {
+            const auto t0 = std::chrono::steady_clock::now();
+            std::shared_ptr<const JitBinary> bin = jit_binary(src, "sl_ls_jit.cu");
+            ctx->ls_thread_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+            ctx->ls_bin = std::move(bin);
+            ctx->ls_pending.store(2, std::memory_order_release);
+        });
     }
     *out = ctx;
     return SL_OK;
@@ -1493,6 +1557,7 @@ int sl_lsampler_loci(sl_ctx* ctx, int32_t first, int32_t n_chains, const int32_t
     if (uls < P.K + 2 * P.N || ucs < (int64_t)P.M * uls)
         return fail(ctx, SL_EINVAL, "draw strides too small (need locus stride >= K + 2N)");
     CK(cudaSetDevice(ctx->device));
+    ls_adopt(ctx);
     if ((rc = stage_draws(ctx, u, (size_t)n_chains * ucs))) return rc;
     CK(cudaMemcpyAsync(ctx->d_loci, loci, sizeof(int32_t) * n_loci, cudaMemcpyHostToDevice, ctx->stream));
     { Prof pf_(ctx, SL_KERNEL_LSAMPLER);
@@ -1510,6 +1575,7 @@ int sl_lsampler_sweep(sl_ctx* ctx, int32_t first, int32_t n_chains, const double
     if (uls < P.K + 2 * P.N || ucs < (int64_t)P.M * uls)
         return fail(ctx, SL_EINVAL, "draw strides too small (need locus stride >= K + 2N)");
     CK(cudaSetDevice(ctx->device));
+    ls_adopt(ctx);
     if ((rc = stage_draws(ctx, u, (size_t)n_chains * ucs))) return rc;
     { Prof pf_(ctx, SL_KERNEL_LSAMPLER);
       CK(ls_launch(ctx, first, n_chains, ctx->d_even, (int)ctx->even.size(), ctx->d_u, ucs, uls, 0, 0,
@@ -1884,8 +1950,9 @@ int sl_set_temperatures(sl_ctx* ctx, const double* temps) {
 
 int sl_ls_kernel_info(sl_ctx* ctx, int32_t* kernel, double* compile_ms) {
     if (!ctx) return fail(ctx, SL_EINVAL, "null context");
+    ls_adopt(ctx);
     if (kernel) *kernel = ctx->jit_ls.kern ? SL_LS_KERNEL_SPECIALISED : SL_LS_KERNEL_GENERIC;
-    if (compile_ms) *compile_ms = ctx->jit_ls_ms;
+    if (compile_ms) *compile_ms = ls_compiling(ctx) ? -1.0 : ctx->jit_ls_ms;
     return SL_OK;
 }
 
@@ -2080,8 +2147,12 @@ static int prepare_run_graph(sl_ctx* ctx) {
     if (!ctx->d_chain_it && (rc = dev_alloc(ctx, &ctx->d_chain_it, C))) return rc;
     if (!ctx->d_keys && (rc = dev_alloc(ctx, &ctx->d_keys, 2 * (size_t)C))) return rc;
     if (!ctx->d_acc_c && (rc = dev_alloc(ctx, &ctx->d_acc_c, (size_t)C * npos))) return rc;
-    if (!ctx->d_init_c && (rc = dev_alloc(ctx, &ctx->d_init_c, (size_t)C * npos))) return rc;
-    CK(cudaMemsetAsync(ctx->d_init_c, 0, (size_t)C * npos, ctx->stream));
+    if (!ctx->d_init_c) {
+        // the chains' tables start empty; a graph captured again later (a kernel switch)
+        // keeps the scores they hold
+        if ((rc = dev_alloc(ctx, &ctx->d_init_c, (size_t)C * npos))) return rc;
+        CK(cudaMemsetAsync(ctx->d_init_c, 0, (size_t)C * npos, ctx->stream));
+    }
     CK(cudaMemsetAsync(ctx->d_keys, 0, sizeof(uint64_t) * 2 * C, ctx->stream));
     // every chain's selector 0 and want = 2: these launches do nothing
     CK(cudaMemsetAsync(ctx->d_sel, 0, (size_t)C, ctx->stream));
@@ -2394,17 +2465,27 @@ int sl_run(sl_ctx* ctx, const sl_run_options* o) {
     const int C = ctx->n_chains;
     const int total = o->burnin + o->iterations;
     if (o->first_iteration >= total) return SL_OK;
-    if (o->exchange_period == 0 || C < 2) return run_span(ctx, o, o->first_iteration, total);
+    ls_adopt(ctx);
+    const bool mc3 = o->exchange_period > 0 && C >= 2;
+    if (!mc3 && !ls_compiling(ctx)) return run_span(ctx, o, o->first_iteration, total);
     // MC3: spurts of exchange_period iterations, each followed by an exchange
     // (Mc3::run, mc3.cc:117-158; iterations are numbered consecutively).  Spurts
     // end at multiples of exchange_period counted from iteration 0, so a run
     // resumed at any first_iteration exchanges where an unbroken run does.
+    // While the specialised L-sampler compiles, spans are short and waited for;
+    // a run split anywhere gives the same graphs and scores.
     const int P = o->exchange_period;
     for (int it0 = o->first_iteration; it0 < total;) {
-        const int it1 = std::min(total, (it0 / P + 1) * P);
+        int it1 = mc3 ? std::min(total, (it0 / P + 1) * P) : total;
+        const bool paced = ls_compiling(ctx);
+        if (paced) it1 = std::min(it1, it0 + kPacedSpan);
         int rc = run_span(ctx, o, it0, it1);
         if (rc) return rc;
-        if (it1 % P == 0 && (rc = mc3_exchange(ctx, o->seed, it1))) return rc;
+        if (paced) {
+            CK(cudaStreamSynchronize(ctx->stream));
+            ls_adopt(ctx);
+        }
+        if (mc3 && it1 % P == 0 && (rc = mc3_exchange(ctx, o->seed, it1))) return rc;
         it0 = it1;
     }
     return SL_OK;
@@ -2423,6 +2504,7 @@ struct sl_batch {
     std::vector<cudaEvent_t> evs;
     cudaEvent_t ev_root = nullptr, ev_done = nullptr;
     cudaGraphExec_t graph = nullptr;
+    std::vector<int> ls_epochs;   // each context's L-sampler kernel switches when the graph was captured
 };
 
 void sl_batch_destroy(sl_batch* b) {
@@ -2472,9 +2554,11 @@ int sl_batch_create(sl_ctx* const* ctxs, int32_t n, sl_batch** out) {
 }
 
 static int build_batch_graph(sl_batch* b) {
+    b->ls_epochs.clear();
     for (sl_ctx* c : b->ctxs) {
         int rc = prepare_run_graph(c);
         if (rc) return rc;
+        b->ls_epochs.push_back(c->ls_epoch);
     }
     cudaGraph_t top = nullptr;
     if (cudaGraphCreate(&top, 0) != cudaSuccess) return fail(nullptr, SL_ECUDA, "creating the batch graph");
@@ -2507,15 +2591,32 @@ int sl_batch_run(sl_batch* b, const sl_run_options* o) {
     if (cudaSetDevice(b->device) != cudaSuccess) return fail(nullptr, SL_ECUDA, "cudaSetDevice");
     for (sl_ctx* c : b->ctxs)
         if (c->profiling) return fail(c, SL_EINVAL, "a batch runs without per-kernel profiling");
-    if (!b->graph) {
-        int rc = build_batch_graph(b);
-        if (rc) return rc;
-    }
     const int total = o->burnin + o->iterations;
     const int P = o->exchange_period;
     for (int it0 = o->first_iteration, it1; it0 < total; it0 = it1) {
-        // spurts end at multiples of the exchange period counted from iteration 0 (as in sl_run)
+        // a context whose specialised L-sampler has compiled switches to it: the graph is captured again
+        bool paced = false;
+        for (sl_ctx* c : b->ctxs) {
+            ls_adopt(c);
+            paced = paced || ls_compiling(c);
+        }
+        if (b->graph)
+            for (size_t j = 0; j < b->ctxs.size(); ++j)
+                if (b->ls_epochs[j] != b->ctxs[j]->ls_epoch) {
+                    if (cudaStreamSynchronize(b->stream) != cudaSuccess)   // no launch of it in flight
+                        return fail(nullptr, SL_ECUDA, "waiting for the batch graph");
+                    cudaGraphExecDestroy(b->graph);
+                    b->graph = nullptr;
+                    break;
+                }
+        if (!b->graph) {
+            int rc = build_batch_graph(b);
+            if (rc) return rc;
+        }
+        // spurts end at multiples of the exchange period counted from iteration 0 (as in sl_run);
+        // while a compile runs, spans are short and waited for
         it1 = P > 0 ? std::min(total, (it0 / P + 1) * P) : total;
+        if (paced) it1 = std::min(it1, it0 + kPacedSpan);
         for (size_t j = 0; j < b->ctxs.size(); ++j) {
             sl_ctx* c = b->ctxs[j];
             const RunParams rp{it0, it1, o->burnin, o->scoring_period, o->lsampler_prob, o->seed};
@@ -2531,6 +2632,8 @@ int sl_batch_run(sl_batch* b, const sl_run_options* o) {
                 return fail(c, SL_ECUDA, "ordering the context after the batch");
             account_span(c, o, it0, it1);
         }
+        if (paced && cudaEventSynchronize(b->ev_done) != cudaSuccess)
+            return fail(nullptr, SL_ECUDA, "waiting for a batch span");
         if (P > 0 && it1 % P == 0)
             for (sl_ctx* c : b->ctxs)
                 if (c->n_chains > 1) {

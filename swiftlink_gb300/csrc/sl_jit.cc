@@ -19,12 +19,18 @@
 #include <cuda_runtime.h>
 #include <nvrtc.h>
 
+#include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <condition_variable>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <list>
+#include <memory>
+#include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "sl_internal.h"
@@ -187,8 +193,10 @@ std::string jit_source(const JitProgramIn& in, int threads, bool shared) {
 
 }  // namespace
 
-int jit_compile_kernel(const std::string& src, const char* file, const char* kernel, void** lib_out, void** kern_out,
-                       std::string* log) {
+namespace {
+
+// NVRTC for sm_103a: source to cubin, no CUDA context needed.
+int nvrtc_cubin(const std::string& src, const char* file, std::vector<char>* cubin, std::string* log) {
     nvrtcProgram prog;
     if (nvrtcCreateProgram(&prog, src.c_str(), file, 0, nullptr, nullptr) != NVRTC_SUCCESS) {
         *log = "nvrtcCreateProgram failed";
@@ -210,9 +218,96 @@ int jit_compile_kernel(const std::string& src, const char* file, const char* ker
     }
     size_t n = 0;
     nvrtcGetCUBINSize(prog, &n);
-    std::vector<char> cubin(n);
-    nvrtcGetCUBIN(prog, cubin.data());
+    cubin->resize(n);
+    nvrtcGetCUBIN(prog, cubin->data());
     nvrtcDestroyProgram(&prog);
+    return 0;
+}
+
+// Compiles running at once: each takes a core and up to a few hundred MB,
+// and a program may ask for one per pedigree.
+class CompileSlots {
+  public:
+    CompileSlots() {
+        const unsigned hw = std::thread::hardware_concurrency();
+        free_ = hw >= 4 ? (int)std::min(8u, hw / 2) : 2;
+    }
+    void take() {
+        std::unique_lock<std::mutex> lk(mu_);
+        cv_.wait(lk, [&] { return free_ > 0; });
+        --free_;
+    }
+    void give() {
+        { std::lock_guard<std::mutex> lk(mu_); ++free_; }
+        cv_.notify_one();
+    }
+
+  private:
+    std::mutex mu_;
+    std::condition_variable cv_;
+    int free_;
+};
+
+struct BinaryCache {
+    std::mutex mu;
+    std::condition_variable cv;
+    std::list<std::shared_ptr<JitBinary>> lru;   // most recent first
+    CompileSlots slots;
+};
+
+BinaryCache& binary_cache() {
+    static BinaryCache* c = new BinaryCache();   // never destroyed: background compiles may outlive main
+    return *c;
+}
+
+constexpr size_t kCachedBinaries = 32;
+
+}  // namespace
+
+std::shared_ptr<const JitBinary> jit_binary(const std::string& src, const char* file) {
+    BinaryCache& c = binary_cache();
+    std::shared_ptr<JitBinary> job;
+    {
+        std::unique_lock<std::mutex> lk(c.mu);
+        for (auto it = c.lru.begin(); it != c.lru.end(); ++it)
+            if ((*it)->source == src) {
+                job = *it;
+                c.lru.splice(c.lru.begin(), c.lru, it);
+                break;
+            }
+        if (!job) {
+            job = std::make_shared<JitBinary>();
+            job->source = src;
+            c.lru.push_front(job);
+            while (c.lru.size() > kCachedBinaries) c.lru.pop_back();
+        } else {
+            // another caller compiles this source: wait for its result
+            c.cv.wait(lk, [&] { return job->done; });
+            return job;
+        }
+    }
+    const auto t0 = std::chrono::steady_clock::now();
+    c.slots.take();
+    std::vector<char> cubin;
+    std::string log;
+    const int rc = nvrtc_cubin(src, file, &cubin, &log);
+    c.slots.give();
+    const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    {
+        std::lock_guard<std::mutex> lk(c.mu);
+        job->cubin.swap(cubin);
+        job->log = log;
+        job->rc = rc;
+        job->compile_ms = ms;
+        job->done = true;
+        if (rc) c.lru.remove(job);   // a failure is reported once, not cached
+    }
+    c.cv.notify_all();
+    return job;
+}
+
+int jit_load_kernel(const std::vector<char>& cubin, const char* kernel, void** lib_out, void** kern_out,
+                    std::string* log) {
     cudaLibrary_t lib = nullptr;
     cudaError_t e = cudaLibraryLoadData(&lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
     if (e != cudaSuccess) {
@@ -229,6 +324,16 @@ int jit_compile_kernel(const std::string& src, const char* file, const char* ker
     *lib_out = lib;
     *kern_out = (void*)k;
     return 0;
+}
+
+int jit_compile_kernel(const std::string& src, const char* file, const char* kernel, void** lib_out, void** kern_out,
+                       std::string* log) {
+    const std::shared_ptr<const JitBinary> bin = jit_binary(src, file);
+    if (bin->rc) {
+        *log = bin->log;
+        return -1;
+    }
+    return jit_load_kernel(bin->cubin, kernel, lib_out, kern_out, log);
 }
 
 std::string jit_lod_source(const JitProgramIn& in, int threads, bool shared) {

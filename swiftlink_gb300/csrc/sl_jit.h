@@ -5,7 +5,9 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <memory>
 #include <string>
+#include <vector>
 
 namespace sl {
 
@@ -31,8 +33,27 @@ struct JitLod {
     double compile_ms = 0.0;
 };
 
-// NVRTC-compile `src` for sm_103a and load `kernel` from it (a cudaLibrary_t
-// and a cudaKernel_t); 0 on success, else -1 with the reason in *log.
+// One NVRTC compile of a source for sm_103a.
+struct JitBinary {
+    std::string source;
+    std::vector<char> cubin;
+    std::string log;
+    int rc = -1;             // 0: cubin holds the binary
+    double compile_ms = 0.0;
+    bool done = false;
+};
+
+// The cubin of `src`, compiled on the calling thread (no CUDA context is
+// needed) or taken from a process-wide cache of recent sources; a caller
+// asking for a source another thread is compiling waits for that compile.
+// At most a few compiles run at once.  Thread-safe.
+std::shared_ptr<const JitBinary> jit_binary(const std::string& src, const char* file);
+
+// Load `kernel` from a cubin into the current device's context (a
+// cudaLibrary_t and a cudaKernel_t); 0 on success, else -1 with the reason.
+int jit_load_kernel(const std::vector<char>& cubin, const char* kernel, void** lib, void** kern, std::string* log);
+
+// jit_binary, then jit_load_kernel.
 int jit_compile_kernel(const std::string& src, const char* file, const char* kernel, void** lib, void** kern,
                        std::string* log);
 

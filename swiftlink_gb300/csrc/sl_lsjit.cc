@@ -17,6 +17,7 @@
 
 #include <cstdarg>
 #include <chrono>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -497,13 +498,15 @@ size_t jit_ls_warp_bytes(const JitLsIn& in) { return layout(in).total; }
 
 std::string jit_ls_source(const JitLsIn& in, int wpb) { return source(in, wpb); }
 
-int jit_ls_compile(const JitLsIn& in, int wpb, JitLs* out, std::string* log) {
+int jit_ls_load(const JitBinary& bin, int wpb, size_t warp_bytes, JitLs* out, std::string* log) {
     *out = JitLs{};
-    const auto t0 = std::chrono::steady_clock::now();
-    const std::string src = source(in, wpb);
-    if (jit_compile_kernel(src, "sl_ls_jit.cu", "sl_ls_jit", &out->lib, &out->kern, log)) return -1;
+    if (bin.rc) {
+        *log = bin.log;
+        return -1;
+    }
+    if (jit_load_kernel(bin.cubin, "sl_ls_jit", &out->lib, &out->kern, log)) return -1;
     out->wpb = wpb;
-    out->smem = (size_t)wpb * layout(in).total;
+    out->smem = (size_t)wpb * warp_bytes;
     if (cudaFuncSetAttribute((const void*)out->kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)out->smem) !=
         cudaSuccess) {
         jit_ls_release(out);
@@ -524,6 +527,13 @@ int jit_ls_compile(const JitLsIn& in, int wpb, JitLs* out, std::string* log) {
         return -1;
     }
     out->blocks_per_sm = blocks;
+    return 0;
+}
+
+int jit_ls_compile(const JitLsIn& in, int wpb, JitLs* out, std::string* log) {
+    const auto t0 = std::chrono::steady_clock::now();
+    const std::shared_ptr<const JitBinary> bin = jit_binary(source(in, wpb), "sl_ls_jit.cu");
+    if (jit_ls_load(*bin, wpb, layout(in).total, out, log)) return -1;
     out->compile_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     return 0;
 }

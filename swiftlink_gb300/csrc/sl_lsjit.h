@@ -8,6 +8,7 @@
 #include <string>
 
 #include "sl_internal.h"
+#include "sl_jit.h"
 
 namespace sl {
 
@@ -32,7 +33,11 @@ struct JitLs {
 
 size_t jit_ls_warp_bytes(const JitLsIn& in);
 std::string jit_ls_source(const JitLsIn& in, int wpb);
+// Source, compile (through the process-wide cache) and load.
 int jit_ls_compile(const JitLsIn& in, int wpb, JitLs* out, std::string* log);
+// Load a compiled source (jit_binary of jit_ls_source) into the current
+// device's context; warp_bytes = jit_ls_warp_bytes of the same input.
+int jit_ls_load(const JitBinary& bin, int wpb, size_t warp_bytes, JitLs* out, std::string* log);
 void jit_ls_release(JitLs* j);
 cudaError_t jit_ls_launch(const JitLs& j, uint32_t* dg, int first, int nchain, const int32_t* loci, int nloci,
                           const double* u, int64_t ucs, int64_t uls, uint64_t seed, uint64_t iter, const uint64_t* key,
