@@ -1010,27 +1010,28 @@ __global__ void __launch_bounds__(128) fag_kernel(ProblemDev P, uint32_t* dg, in
 }
 
 // ---------------------------------------------------------------------------
-// Fast-mode founder-allele-graph likelihood, one warp per (chain, locus).
-// The likelihood of the genotypes given the column's founder-allele graph
-// (FounderAlleleGraph4::likelihood, founder_allele_graph4.cc:34-442) is the
-// product over the connected components of the heterozygote edges of the sum,
-// over the component's two colourings (allele A = major, B = minor) that
-// satisfy every homozygote's fixed alleles, of the product of the founder
-// alleles' frequencies.  Here:
+// Fast-mode founder-allele-graph likelihood, one group of G lanes (a warp, or
+// half a warp) per (chain, locus).  The likelihood of the genotypes given the
+// column's founder-allele graph (FounderAlleleGraph4::likelihood,
+// founder_allele_graph4.cc:34-442) is the product over the connected
+// components of the heterozygote edges of the sum, over the component's two
+// colourings (allele A = major, B = minor) that satisfy every homozygote's
+// fixed alleles, of the product of the founder alleles' frequencies.  Here:
 //   1. the founder allele of every person's two alleles is propagated one
 //      generation level at a time, the lanes splitting a level's persons;
-//   2. typed persons mark their founder alleles used / fixed A / fixed B
-//      (shared-memory atomicOr) and a heterozygote on one founder allele is a
-//      zero likelihood;
-//   3. components with the parity of each allele to the component's smallest
-//      allele come from min-label propagation over the heterozygote edges plus
-//      pointer jumping (labels packed as 2 * label + parity, only ever
-//      lowered, so the result is the same whatever the interleaving); an edge
-//      whose endpoints end with equal parity closes an odd cycle: zero;
+//   2. the locus's typed persons (a list built at context creation,
+//      heterozygotes first) mark their founder alleles used / fixed A /
+//      fixed B (shared-memory atomicOr); a heterozygote on one founder allele
+//      is a zero likelihood;
+//   3. the heterozygote edges join components in a lock-free union-find with
+//      parities (pf_find; a compare-and-swap hooks the larger root under the
+//      smaller, so every root is its component's smallest allele whatever the
+//      interleaving); an edge whose ends already share a root with equal
+//      parity closes an odd cycle: zero;
 //   4. a component's two colourings weigh (even members) x log2 f(A) + (odd
 //      members) x log2 f(B) and the reverse, so each component needs only
-//      integer counts; a butterfly sum over the warp gives log2 of the
-//      likelihood.
+//      integer counts, taken at its root; a butterfly sum over the group
+//      gives log2 of the likelihood.
 // ---------------------------------------------------------------------------
 constexpr int kFagWarpsPerBlock = 8;
 
