@@ -39,6 +39,7 @@ cudaError_t launch_msampler(const ProblemDev& P, uint32_t* dg, int first, int nc
                             uint8_t* maps, int* status, int fag_threads, int exact, cudaStream_t s,
                             const uint64_t* key = nullptr, double* ubuf = nullptr, int pairs = 0);
 cudaError_t launch_set_key(uint64_t* key, uint64_t seed, uint64_t iter, cudaStream_t s);
+cudaError_t launch_lfreq(const double* minor, float2* out, int64_t n, cudaStream_t s);
 cudaError_t launch_si(const ProblemDev& P, uint32_t* dg, int first, int nchain, const int32_t* starts,
                       const double* u, int64_t ucs, uint64_t seed, uint64_t pass, double* weights, int* status,
                       cudaStream_t s, int wpb, int npass, int64_t pass_stride, int grid_cap);
@@ -1036,6 +1037,13 @@ static int upload_chain_maps(sl_ctx* ctx) {
     if ((rc = put((double**)&P.c_theta, th.data(), th.size()))) return rc;
     if ((rc = put((float**)&P.c_theta_f, thf.data(), thf.size()))) return rc;
     if ((rc = put((double**)&P.c_minor, mi.data(), mi.size()))) return rc;
+    if (!P.c_lfreq) {
+        float2* p = nullptr;
+        if ((rc = dev_alloc(ctx, &p, (size_t)C * M))) return rc;
+        P.c_lfreq = p;
+    }
+    CK(launch_lfreq(P.c_minor, const_cast<float2*>(P.c_lfreq), (int64_t)C * M, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
     if ((rc = put((double**)&P.c_log_theta, lt.data(), lt.size()))) return rc;
     if ((rc = put((double**)&P.c_log_itheta, la.data(), la.size()))) return rc;
     if ((rc = put((double**)&P.temp, ctx->temps.data(), ctx->temps.size()))) return rc;
@@ -1203,25 +1211,31 @@ int sl_create(const sl_problem_desc* d, const sl_options* opt, sl_ctx** out) {
     if ((rc = upload(ctx, (uint8_t**)&P.geno, geno.data(), geno.size()))) return bail(rc);
     {   // each locus's typed members for the founder-allele graphs, heterozygotes first
         if (N > 16383) return bail(fail(nullptr, SL_EINVAL, "more than 16383 members"));
-        std::vector<int32_t> off(M + 1, 0);
-        std::vector<uint16_t> ent, nhet(M);
-        ent.reserve((size_t)M * N);
+        // (every list starts on a 16-byte boundary and is padded to whole 16-byte chunks: the kernel
+        // copies it to shared memory with 16-byte asynchronous copies)
+        std::vector<int32_t> off(M, 0);
+        std::vector<uint16_t> ent, cnt(M), nhet(M);
+        ent.reserve((size_t)M * (N + 8));
         for (int l = 0; l < M; ++l) {
             off[l] = (int32_t)ent.size();
-            int nh = 0;
+            int nh = 0, nt = 0;
             for (int pass = 0; pass < 2; ++pass)
                 for (int i = 0; i < N; ++i) {
                     const int g = geno[(size_t)l * N + i] & 3;
                     if (g == G_UNTYPED || (g == G_HETERO) != (pass == 0)) continue;
                     ent.push_back((uint16_t)(i << 2 | g));
                     nh += pass == 0;
+                    ++nt;
                 }
+            while (ent.size() % 8) ent.push_back(0);
+            cnt[l] = (uint16_t)nt;
             nhet[l] = (uint16_t)nh;
         }
-        off[M] = (int32_t)ent.size();
-        if (ent.empty()) ent.push_back(0);
+        if (ent.empty()) ent.assign(8, 0);
+        if (ent.size() > (size_t)INT32_MAX) return bail(fail(nullptr, SL_EINVAL, "typed-member lists too long"));
         if ((rc = upload(ctx, (int32_t**)&P.typ_off, off.data(), off.size()))) return bail(rc);
         if ((rc = upload(ctx, (uint16_t**)&P.typ_ent, ent.data(), ent.size()))) return bail(rc);
+        if ((rc = upload(ctx, (uint16_t**)&P.typ_cnt, cnt.data(), cnt.size()))) return bail(rc);
         if ((rc = upload(ctx, (uint16_t**)&P.typ_nhet, nhet.data(), nhet.size()))) return bail(rc);
     }
     if ((rc = upload(ctx, (uint8_t**)&P.typed, typed.data(), N))) return bail(rc);

@@ -34,8 +34,10 @@ struct ProblemDev {
     const int16_t* mother;               // [N], -1 for founders
     const int16_t* father;
     const uint8_t* geno;                 // [M][N]: bits 0-1 genotype code, bits 4-7 legal mask
-    const int32_t* typ_off;              // [M+1] each locus's typed members in typ_ent
-    const uint16_t* typ_ent;             // member << 2 | genotype code, heterozygotes first, members in order
+    const int32_t* typ_off;              // [M] where each locus's typed members start in typ_ent (multiples of 8)
+    const uint16_t* typ_ent;             // member << 2 | genotype code, heterozygotes first, members in order;
+                                         // each list padded to a multiple of 8 entries (16-byte copies)
+    const uint16_t* typ_cnt;             // [M] typed members per locus
     const uint16_t* typ_nhet;            // [M] heterozygotes per locus
     const uint8_t* typed;                // [N]
     const double* prior;                 // [M][4 genotype codes][4 states]
@@ -69,6 +71,7 @@ struct ProblemDev {
     const double* c_theta;               // [C][M-1]
     const float* c_theta_f;              // [C][M-1]
     const double* c_minor;               // [C][M]
+    const float2* c_lfreq;               // [C][M] log2 of the major and the minor allele frequency, as floats
     const double* c_log_theta;           // [C][M-1] log(theta_t)
     const double* c_log_itheta;          // [C][M-1] log(1 - theta_t)
     const double* temp;                  // [C] temperatures

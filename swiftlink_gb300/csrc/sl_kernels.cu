@@ -1038,13 +1038,27 @@ constexpr int kFagWarpsPerBlock = 8;
 __host__ __device__ inline size_t fagw_tables(int N) {
     return (((size_t)N * 8 + 15) & ~(size_t)15) + (((size_t)4 * (N + 1) + 15) & ~(size_t)15);
 }
+// per lane group: e [2N] u16, then Lb / fl / cnt [2F] int each, then the
+// typed-member list [N] u16 on a 16-byte boundary in whole 16-byte chunks
+__host__ __device__ inline size_t fagw_typ_offset(int N, int F) {
+    return (((((size_t)4 * N + 15) & ~(size_t)15) + (size_t)2 * F * 12) + 15) & ~(size_t)15;
+}
 __host__ __device__ inline size_t fagw_warp_bytes(int N, int F) {
-    return (((size_t)4 * N + 15) & ~(size_t)15) + (size_t)2 * F * 12 + (size_t)4 * N;
+    return fagw_typ_offset(N, F) + (size_t)16 * ((N + 7) / 8);
 }
 // per block: the shared tables and one locus's arrays per lane group (G lanes)
 size_t fagw_block_bytes(int N, int F, int G) {
     return fagw_tables(N) + (size_t)kFagWarpsPerBlock * (32 / G) * fagw_warp_bytes(N, F);
 }
+
+// 16-byte global -> shared copies that complete asynchronously (cp.async,
+// sm_80 and later): both addresses 16-byte aligned.
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
 // Root of founder allele x in a forest of 2 * parent + parity entries, and
 // x's parity to it.  Parents have smaller indices than their children, so the
@@ -1131,19 +1145,22 @@ __device__ __forceinline__ void fagw_task(const ProblemDev& P, const FagwTables&
     volatile int* Lb = (volatile int*)(wbase + (((size_t)4 * N + 15) & ~(size_t)15));   // [2F] 2 * parent + parity
     int* fl = (int*)(Lb + nfa);                                       // [2F] bit0 used, bit1 fixed A, bit2 fixed B
     int* cnt = fl + nfa;                                              // [2F] per component: counts, forbidden colourings
-    uint16_t* typ = (uint16_t*)(cnt + nfa);                           // [N] the locus's typed members
+    uint16_t* typ = (uint16_t*)(wbase + fagw_typ_offset(N, F));       // [N] the locus's typed members
     const int lc = valid ? l : 0;
     const uint32_t* col = dg + ((size_t)chain * M + lc) * P.W;
     float* raw = rawbuf + (size_t)cr * 2 * M;
     // the task's global reads issued together: the column's words (lane w of
-    // the group holds word w, read by shuffles), the locus's typed members
-    // (member << 2 | genotype code, heterozygotes first: fixed by the
-    // genotypes, listed once at context creation), the minor-allele frequency
+    // the group holds word w, read by shuffles), the allele frequencies'
+    // log2, and the locus's typed members (member << 2 | genotype code,
+    // heterozygotes first: fixed by the genotypes, listed once at context
+    // creation), copied to shared memory in 16-byte asynchronous copies that
+    // complete while the founder alleles are propagated
     const bool wreg = P.W <= G;
     const uint32_t cw = wreg && gl < P.W ? col[gl] : 0u;
-    const int t0 = P.typ_off[lc], ntyp = P.typ_off[lc + 1] - t0, nhet = P.typ_nhet[lc];
-    const double minor_d = P.c_minor[(size_t)chain * M + lc];
-    for (int x = gl; x < ntyp; x += G) typ[x] = P.typ_ent[t0 + x];
+    const int t0 = P.typ_off[lc], ntyp = P.typ_cnt[lc], nhet = P.typ_nhet[lc];
+    const float2 lfreq = P.c_lfreq[(size_t)chain * M + lc];
+    for (int q = gl; q < (ntyp + 7) >> 3; q += G) cp_async16(typ + 8 * q, P.typ_ent + t0 + 8 * q);
+    cp_async_commit();
     auto cbit = [&](int b) -> int {
         const uint32_t w = wreg ? grp.shfl(cw, b >> 5) : col[b >> 5];
         return (int)((w >> (b & 31)) & 1u);
@@ -1187,6 +1204,7 @@ __device__ __forceinline__ void fagw_task(const ProblemDev& P, const FagwTables&
         fl[x] = 0;
         cnt[x] = 0;
     }
+    cp_async_wait_all();   // this lane's copies of the list; the barrier makes the group's visible
     __syncwarp();
     // the typed members mark their founder alleles (no warp primitive inside:
     // the groups' loci have lists of their own lengths)
@@ -1259,7 +1277,7 @@ __device__ __forceinline__ void fagw_task(const ProblemDev& P, const FagwTables&
     float sum = 0.f;
     int zero = 0;
     if (!bad) {
-        const float lmaj = log2f((float)(1.0 - minor_d)), lmin = log2f((float)minor_d);
+        const float lmaj = lfreq.x, lmin = lfreq.y;
         for (int x = gl; x < nfa; x += G) {
             const int c = cnt[x];
             const int n = (c >> 16) & 0x1fff, even = c & 0xffff;
@@ -2543,6 +2561,23 @@ static cudaError_t launch_msampler_t(const ProblemDev& P, uint32_t* dg, int firs
                                                                      want, badc, raw32, (float*)fb, maps, staged,
                                                                      upre);
     }
+    return cudaGetLastError();
+}
+
+// log2 of each chain's major and minor allele frequency at each locus, in
+// the founder-allele kernel's arithmetic (FP32 logs of the rounded frequencies)
+__global__ void lfreq_kernel(const double* minor, float2* out, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double m = minor[i];
+        out[i] = make_float2(log2f((float)(1.0 - m)), log2f((float)m));
+    }
+}
+
+cudaError_t launch_lfreq(const double* minor, float2* out, int64_t n, cudaStream_t s) {
+    int64_t grid = (n + 255) / 256;
+    if (grid > 4096) grid = 4096;
+    if (grid < 1) grid = 1;
+    lfreq_kernel<<<(int)grid, 256, 0, s>>>(minor, out, n);
     return cudaGetLastError();
 }
 
