@@ -33,6 +33,17 @@ def test_exports_every_declared_symbol():
     assert set(api.EXPORTED) <= set(syms)
 
 
+def test_python_constants_match_the_header():
+    """Every SL_* integer constant the Python mirror defines has the header's value."""
+    src = open(os.path.join(ROOT, "include", "swiftlink_gb300.h")).read()
+    defs = {k: int(v) for k, v in re.findall(r"#define\s+(SL_[A-Z0-9_]+)\s+(-?\d+)\b", src)}
+    mirrored = {k: getattr(api, k) for k in dir(api) if k.startswith("SL_") and isinstance(getattr(api, k), int)}
+    assert len(mirrored) >= 15
+    for k, v in mirrored.items():
+        assert k in defs, k
+        assert defs[k] == v, (k, defs[k], v)
+
+
 def test_version_and_null_handling():
     L = api.lib()
     assert b"sm_103a" in L.sl_version()
