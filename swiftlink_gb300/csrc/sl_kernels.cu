@@ -1718,9 +1718,10 @@ __global__ void __launch_bounds__(kFagWarpsPerBlock * 32) fag_warp_kernel(Proble
                      cr, l, l < M, ord, step, rawbuf, raw32, badc, status);
 }
 
-// Threads per chain of ffbs_scan_kernel: runs of about 4 loci.
+// Threads per chain of ffbs_scan_kernel: runs of about 2 loci (the scan is
+// on every meiosis step's critical path; shorter runs shorten its serial parts).
 int ffbs_scan_threads(int M) {
-    int t = ((M + 3) / 4 + 31) / 32 * 32;
+    int t = ((M + 1) / 2 + 31) / 32 * 32;
     return t < 32 ? 32 : (t > 1024 ? 1024 : t);
 }
 
