@@ -377,6 +377,13 @@ def run_ours(args):
                 "note": "latency-bound integer and FP32 work on small rfunctions: the HBM fraction is small by "
                         "construction; SM issue utilisation per kernel is in profiles/",
                 "kernel_share_profiled_pass": {names[k]: round(v[0] / tot, 4) for k, v in kern.items()}}
+    if WORKLOAD == "cfg2" and C == 10 and ls_sel == api.SL_LS_KERNEL_SPECIALISED:
+        try:
+            roofline["issue"] = issue_estimate(C, W * P_, (W + K) * P_, seed, LPROB, len(d["meioses"]),
+                                               (clk or {}).get("sm_mhz"), torch.cuda.get_device_properties(dev).multi_processor_count,
+                                               sum(step_ms) / 1e3)
+        except Exception as exc:   # an estimate only: never lose the bench line over it
+            roofline["issue"] = {"error": str(exc)[:200]}
 
     # ---------------- LOD positions/s, batched (many graphs per launch, FP32) vs plain (FP64, one graph)
     graphs = ctx.get_graphs()
@@ -622,6 +629,49 @@ def timed_lod(ctx, stream, flush, G, npos, reps):
     ctx.synchronize()
     t = sum(a.elapsed_time(b) for a, b in evs) / 1e3
     return reps * G * npos / t
+
+
+def inst_from_profiles(name):
+    """Warp instructions per launch (smsp__inst_executed.sum) from a committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", name)
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.startswith("| smsp__inst_executed.sum |"):
+            try:
+                return float(line.split("|")[2].split()[0].replace(",", ""))
+            except (ValueError, IndexError):
+                return None
+    return None
+
+
+def issue_estimate(C, it0, it1, seed, lprob, n_meioses, sm_mhz, sms, seconds):
+    """SM issue utilisation of timed run-graph launches on the 120-member,
+    2,000-SNP workload: the warp instructions of the L- and M-sweeps they ran
+    (each chain's L/M choice replayed with the same Philox draws; instructions
+    per sweep from the committed ncu summaries of this workload's kernels) over
+    the SMs' issue rate (4 schedulers per SM, one warp instruction per cycle
+    each, at the SM clock sampled during the launches)."""
+    from swiftlink_gb300 import philox
+    ls = inst_from_profiles("sl_ls_jit_cfg2.md")           # one half-sweep (1,000 loci) of 10 chains
+    fag = inst_from_profiles("fag_warp_kernel_cfg2.md")    # one meiosis step of one chain
+    scan = inst_from_profiles("ffbs_scan_kernel_cfg2.md")  # one meiosis step of one chain
+    if None in (ls, fag, scan) or not sm_mhz or not sms or seconds <= 0:
+        return None
+    c = np.arange(C, dtype=np.uint64)[:, None]
+    it = np.arange(it0, it1, dtype=np.uint64)[None, :]
+    hi = (c << np.uint64(40)) ^ (it << np.uint64(4)) ^ np.uint64(7)
+    n_l = int((philox.uniform(seed, hi, 0) < lprob).sum())
+    n_m = C * (it1 - it0) - n_l
+    per_l = 2 * ls / 10                                  # both halves, one chain
+    per_m = (n_meioses + 1) * fag + n_meioses * scan     # a reset launch, then a likelihood and a scan per meiosis
+    inst = n_l * per_l + n_m * per_m
+    peak = sms * 4 * sm_mhz * 1e6
+    return {"bound": "issue", "achieved": inst / seconds / 1e9, "peak": peak / 1e9, "unit": "G warp-inst/s",
+            "frac": inst / seconds / peak, "l_sweeps": n_l, "m_sweeps": n_m,
+            "warp_inst_per_l_sweep": per_l, "warp_inst_per_m_sweep": per_m,
+            "source": "instructions per launch: smsp__inst_executed.sum in profiles/sl_ls_jit_cfg2.md, "
+                      "fag_warp_kernel_cfg2.md, ffbs_scan_kernel_cfg2.md; the scoring launches are left out"}
 
 
 def traffic_from_profiles(kernel):
