@@ -1,16 +1,33 @@
 // sm_103a kernels for the SwiftLink MCMC hot path.
 //
-//  * lsampler_kernel   -- L-sampler, one warp per (chain, locus), FP64 with the
-//                         reference's operation order (bit-exact decisions).
-//  * fag_kernel        -- M-sampler likelihoods: founder-allele graph of every
-//                         (chain, locus) column with one meiosis toggled.
-//  * ffbs_kernel<T>    -- M-sampler forward filter / backward sample, one warp
-//                         per chain (T=double exact, T=float fast).
-//  * lod_kernel<T,R>   -- trait peel at every (graph, interval, position), one
-//                         warp per task; T=double is the plain FP64 form,
-//                         T=float with R=true rescales every rfunction by a
-//                         power of two and carries the exponent.
-//  * lod_merge_kernel  -- FP64 log-sum accumulation into the LOD table.
+// Samplers (one chain's descent graph per chain, bit-packed [chain][M][W]):
+//  * lsampler_kernel<T>   -- L-sampler, one warp per (chain, locus): T=double
+//                            with the reference's operation order (bit-exact
+//                            decisions), T=float the batched form.  The form
+//                            compiled per pedigree lives in sl_lsjit.cc.
+//  * si_kernel<T>, si_select_kernel -- sequential imputation passes (one-sided
+//                            L-steps from a start locus) and the best pass.
+//  * fag_kernel           -- M-sampler likelihoods, thread per (chain, locus):
+//                            founder-allele graph with one meiosis toggled
+//                            (exact mode, and fast mode past the warp form's
+//                            shared-memory limit).
+//  * fag_warp_kernel<G>   -- the same in lane groups of G (fast mode).
+//  * ffbs_kernel<T>       -- forward filter / backward sample of one meiosis,
+//                            one warp per chain, in the reference's order.
+//  * ffbs_scan_kernel     -- the same as block-wide scans (fast mode).
+//  * loglik_*_kernel      -- log P(G, graph) of (graph, map) chain pairs (MC3).
+// Scorer:
+//  * lod_kernel<T,R>      -- trait peel at every (graph, interval, position), one
+//                            warp per task; T=double is the plain FP64 form,
+//                            R=true rescales every rfunction by a power of two
+//                            and carries the exponent.
+//  * lod_prog_kernel      -- the FP32 rescaled peel as a slot-program
+//                            interpreter (specialised forms: sl_jit.cc).
+//  * trait_adjoint_kernel -- the hand-written adjoint of the rescaled peel.
+//  * lod_merge_kernel, chain_merge_kernel -- FP64 log-sum accumulation.
+// Run graph: run_init / chain_iter / chain_advance kernels drive each chain's
+// WHILE and SWITCH nodes; choose / shuffle / set_key draw the iteration's
+// choices; lfreq_kernel precomputes the allele frequencies' log2 per chain map.
 //
 // FP64 arithmetic on decision paths uses __dmul_rn/__dadd_rn/__ddiv_rn so no
 // multiply-add is contracted and the doubles match the reference's.
