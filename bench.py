@@ -64,6 +64,17 @@ def dist_env():
     return rank, world, local
 
 
+def rank_max(x, dist=None, device="cpu"):
+    """The maximum of x over the ranks of the process group (x itself without
+    one): the timed region's length is the slowest rank's."""
+    if not dist:
+        return x
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def config(world):
     return {"workload": "120-member 6-generation pedigree, 3 loops, 35 affected, 2000 SNPs at 0.2 cM, "
                         "recessive (0,0,1) q=1e-4, 10 replicate chains per GPU, scoring every 100th graph, "
@@ -267,11 +278,7 @@ def run_ours(args):
             dist.barrier()
 
     def allmax(x):
-        if not dist:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        return rank_max(x, dist, dev)
 
     d = load_problem(WORKLOAD)
     prob = api.Problem.from_arrays(d, with_legal=False)
