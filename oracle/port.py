@@ -32,6 +32,7 @@ def lib():
         _lib = ctypes.CDLL(LIB_PATH)
         _lib.slo_fag_likelihood.restype = ctypes.c_double
         _lib.slo_loglik.restype = ctypes.c_double
+        _lib.slo_margin.restype = ctypes.c_double
         _lib.slo_philox_uniform.restype = ctypes.c_double
         _lib.slo_philox_uniform.argtypes = [ctypes.c_uint64] * 3
     return _lib
@@ -101,6 +102,28 @@ class Port:
             raise RuntimeError(f"slo_lstep failed ({rc})")
         return dg, used.value
 
+    def lsweep(self, dg, u):
+        """slo_lsweep: even loci, then odd loci, in one call; u[l] holds locus
+        l's draws.  The graph is updated in place (no per-locus copies)."""
+        assert dg.dtype == np.int32 and dg.flags.c_contiguous
+        u = np.ascontiguousarray(u, np.float64)
+        rc = lib().slo_lsweep(ctypes.byref(self.s), _p(dg), _p(u), int(u.shape[1]))
+        if rc != 0:
+            raise RuntimeError(f"slo_lsweep failed ({rc})")
+        return dg
+
+    def lsteps(self, dg, loci, u):
+        """slo_lsteps: L-steps at the listed loci in order, in place; u[i] holds
+        the i-th listed locus's draws."""
+        assert dg.dtype == np.int32 and dg.flags.c_contiguous
+        loci = np.ascontiguousarray(loci, np.int32)
+        u = np.ascontiguousarray(u, np.float64)
+        assert u.shape[0] == loci.size
+        rc = lib().slo_lsteps(ctypes.byref(self.s), _p(dg), _p(loci), loci.size, _p(u), int(u.shape[1]))
+        if rc != 0:
+            raise RuntimeError(f"slo_lsteps failed ({rc})")
+        return dg
+
     def si(self, dg, start, u):
         """One sequential-imputation pass from locus `start`, draws consumed in
         order: (graph, draws used, weight)."""
@@ -135,6 +158,19 @@ class Port:
             raise RuntimeError("slo_lod failed")
         return raw, cnt.value, tp.value
 
+    def lod_range(self, dgs, l0, l1, rescale=True, zero_ok=False):
+        """slo_lod_range: the scores of intervals [l0, l1) only, plain or
+        with per-rfunction power-of-two rescaling."""
+        dgs = np.ascontiguousarray(dgs, np.int32)
+        raw = np.zeros(max(1, (l1 - l0) * self.n_lod))
+        cnt = ctypes.c_uint32()
+        tp = ctypes.c_double()
+        rc = lib().slo_lod_range(ctypes.byref(self.s), _p(dgs), dgs.shape[0], int(l0), int(l1), int(rescale),
+                                 _p(raw), ctypes.byref(cnt), ctypes.byref(tp), int(zero_ok))
+        if rc != 0:
+            raise RuntimeError(f"slo_lod_range failed ({rc})")
+        return raw[:(l1 - l0) * self.n_lod], cnt.value, tp.value
+
     def fag(self, dg, locus):
         dg = np.ascontiguousarray(dg, np.int32)
         return lib().slo_fag_likelihood(ctypes.byref(self.s), _p(dg), int(locus))
@@ -142,6 +178,27 @@ class Port:
     def loglik(self, dg):
         dg = np.ascontiguousarray(dg, np.int32)
         return lib().slo_loglik(ctypes.byref(self.s), _p(dg))
+
+
+def margin_reset():
+    lib().slo_margin_reset()
+
+
+def margin() -> float:
+    """Smallest |draw - decision boundary| since margin_reset()."""
+    return lib().slo_margin()
+
+
+def msweep_margins(P: "Port", dg, meiosis: int, u):
+    """One M-step (reset and step at `meiosis`) on the restatement, returning
+    (graph, per-locus margin of the backward draws: 1 where none was taken)."""
+    buf = np.ones(P.M)
+    lib().slo_margin_log(_p(buf))
+    try:
+        out, _ = P.msweep(dg, np.array([meiosis], np.int32), np.asarray(u, np.float64).reshape(1, -1))
+    finally:
+        lib().slo_margin_log(None)
+    return out, buf
 
 
 def derive_priors(genotypes, typed, minor):

@@ -194,6 +194,15 @@ class Ref:
             raise RuntimeError("uniform buffer overrun in msweep")
         return dg, used
 
+    def write_table(self, raw: np.ndarray, count: int, trait_prob: float, path: str):
+        """The reference's LinkageWriter::write on the given log-sums."""
+        raw = np.ascontiguousarray(raw, np.float64)
+        assert raw.size == (self.M - 1) * self.n_lod
+        rc = lib().ref_write_table(_p(self.h), _ptr(raw), ctypes.c_uint(count), ctypes.c_double(trait_prob),
+                                   path.encode())
+        if rc != 0:
+            raise RuntimeError("LinkageWriter::write failed")
+
     def lod(self, dgs: np.ndarray):
         dgs = np.ascontiguousarray(dgs, np.int32)
         n = dgs.shape[0]

@@ -20,6 +20,7 @@
 #include "linkage_parser.h"
 #include "locus_sampler2.h"
 #include "lod_score.h"
+#include "linkage_writer.h"
 #include "map_parser.h"
 #include "meiosis_sampler.h"
 #include "pedigree.h"
@@ -292,6 +293,19 @@ extern "C" int ref_lod(void* h, const int* dgs, int n_dgs, double* raw, unsigned
     *count = lod.get_count();
     *trait_prob = tp;
     return 0;
+}
+
+// The reference's LOD table writer (LinkageWriter::write, linkage_writer.cc:
+// 14-89) on given log-sums, count and log P(T) of the loaded family.
+extern "C" int ref_write_table(void* h, const double* raw, unsigned count, double trait_prob, const char* path) {
+    RefState* s = (RefState*)h;
+    LODscores lod(&s->map);
+    for (unsigned i = 0; i < lod.num_lodscores(); ++i) lod.set(i, raw[i]);
+    lod.set_count(count);
+    lod.set_trait_prob(trait_prob);
+    vector<LODscores*> all(1, &lod);
+    LinkageWriter w(&s->map, path, false);
+    return w.write(all) ? 0 : -1;
 }
 
 extern "C" int ref_meiosis_order(void* h, int* out, int* n_out) {

@@ -103,19 +103,88 @@ static inline int prev_index(const slo_problem* p, int j, const int* assign) {
 
 static double g_last_root = 0.0;
 
-int slo_lstep(const slo_problem* p, int32_t* dg, int locus, const double* u, int n_u, int* n_used) {
+/* Decision margins: the smallest |draw - boundary| of the sampling decisions
+ * since slo_margin_reset (the cumulative sums a draw is compared with in
+ * SamplerRfunction::sample, the homozygous-parent indicator threshold, the
+ * M-sampler's backward threshold).  A draw this close to a boundary can go
+ * either way under another rounding; the fast (FP32) samplers are checked
+ * against it.  Test instrumentation only: it changes no decision. */
+static double g_margin = 1.0;
+static inline void note_margin(double r, double b) {
+    double m = fabs(r - b);
+    if (m < g_margin) g_margin = m;
+}
+void slo_margin_reset(void) { g_margin = 1.0; }
+double slo_margin(void) { return g_margin; }
+/* per-locus margins of the M-step's backward draws (1 where no draw was taken) */
+static double* g_mlog = NULL;
+void slo_margin_log(double* per_locus) { g_mlog = per_locus; }
+
+static void lws_alloc(const slo_problem* p, lws* w) {
     int N = p->N, K = p->K;
-    lws w;
-    w.mat = (double**)calloc(K, sizeof(double*));
-    w.pre = (double**)calloc(K, sizeof(double*));
-    w.T = (double*)calloc((size_t)N * 64, sizeof(double));
-    w.assign = (int*)malloc(sizeof(int) * N);
-    int used = 0, rc = 0;
+    w->mat = (double**)calloc(K, sizeof(double*));
+    w->pre = (double**)calloc(K, sizeof(double*));
+    w->T = (double*)calloc((size_t)N * 64, sizeof(double));
+    w->assign = (int*)malloc(sizeof(int) * N);
     for (int k = 0; k < K; ++k) {
         int c = cut_len(p, k);
-        w.mat[k] = (double*)calloc(ipow4(c), sizeof(double));
-        w.pre[k] = (double*)calloc(ipow4(c + 1), sizeof(double));
+        w->mat[k] = (double*)calloc(ipow4(c), sizeof(double));
+        w->pre[k] = (double*)calloc(ipow4(c + 1), sizeof(double));
     }
+}
+
+static void lws_free(const slo_problem* p, lws* w) {
+    for (int k = 0; k < p->K; ++k) { free(w->mat[k]); free(w->pre[k]); }
+    free(w->mat); free(w->pre); free(w->T); free(w->assign);
+}
+
+/* one L-step on a workspace whose matrices are zero (cells the step does not
+   write -- invalid cells, zero-prior states -- read as 0, as in a fresh
+   PeelMatrix); the step leaves them zero again for the next call */
+static int lstep_ws(const slo_problem* p, lws* wp, int32_t* dg, int locus, const double* u, int n_u, int* n_used);
+
+int slo_lstep(const slo_problem* p, int32_t* dg, int locus, const double* u, int n_u, int* n_used) {
+    lws w;
+    lws_alloc(p, &w);
+    int rc = lstep_ws(p, &w, dg, locus, u, n_u, n_used);
+    lws_free(p, &w);
+    return rc;
+}
+
+/* L-steps at the listed loci, in list order, in place, with one workspace;
+ * loci[i]'s draws start at u[i * u_stride]. */
+int slo_lsteps(const slo_problem* p, int32_t* dg, const int32_t* loci, int n, const double* u, int u_stride) {
+    lws w;
+    lws_alloc(p, &w);
+    int rc = 0;
+    for (int i = 0; i < n && !rc; ++i) {
+        int used = 0;
+        rc = lstep_ws(p, &w, dg, loci[i], u + (size_t)i * u_stride, u_stride, &used);
+    }
+    lws_free(p, &w);
+    return rc;
+}
+
+/* A full L-sweep (the device's schedule: every even locus, then every odd
+ * locus, each set non-interfering, markov_chain.cc:406-416) in one call with
+ * one workspace; locus l's draws start at u[l * u_stride]. */
+int slo_lsweep(const slo_problem* p, int32_t* dg, const double* u, int u_stride) {
+    lws w;
+    lws_alloc(p, &w);
+    int rc = 0;
+    for (int par = 0; par < 2 && !rc; ++par)
+        for (int l = par; l < p->M && !rc; l += 2) {
+            int n = 0;
+            rc = lstep_ws(p, &w, dg, l, u + (size_t)l * u_stride, u_stride, &n);
+        }
+    lws_free(p, &w);
+    return rc;
+}
+
+static int lstep_ws(const slo_problem* p, lws* wp, int32_t* dg, int locus, const double* u, int n_u, int* n_used) {
+    int N = p->N, K = p->K;
+    lws w = *wp;
+    int used = 0, rc = 0;
     /* forward peel (rfunction.cc:172-198 with offset 0) */
     for (int k = 0; k < K; ++k) {
         int c = cut_len(p, k);
@@ -209,6 +278,10 @@ int slo_lstep(const slo_problem* p, int32_t* dg, int locus, const double* u, int
         double r = u[used++];
         double acc = 0.0;
         int last = 0, pick = -1;
+        {
+            double a2 = 0.0;   /* every boundary the draw could fall on */
+            for (int v = 0; v < 3; ++v) { a2 += pd[v]; if (pd[v] != 0.0) note_margin(r, a2); }
+        }
         for (int v = 0; v < 4; ++v) {
             acc += pd[v];
             if (r < acc) { pick = v; break; }
@@ -243,6 +316,7 @@ int slo_lstep(const slo_problem* p, int32_t* dg, int locus, const double* u, int
                     p1 *= (d == 1) ? an : th;
                 }
                 if (used >= n_u) { rc = -2; goto done; }
+                note_margin(u[used], p0 / (p0 + p1));
                 mi = (u[used++] < (p0 / (p0 + p1))) ? 0 : 1;
             }
             dgset(p, dg, i, locus, par, mi);
@@ -250,8 +324,11 @@ int slo_lstep(const slo_problem* p, int32_t* dg, int locus, const double* u, int
     }
 done:
     *n_used = used;
-    for (int k = 0; k < K; ++k) { free(w.mat[k]); free(w.pre[k]); }
-    free(w.mat); free(w.pre); free(w.T); free(w.assign);
+    for (int k = 0; k < K; ++k) {
+        int c = cut_len(p, k);
+        memset(w.mat[k], 0, sizeof(double) * ipow4(c));
+        memset(w.pre[k], 0, sizeof(double) * ipow4(c + 1));
+    }
     return rc;
 }
 
@@ -610,9 +687,14 @@ int slo_msweep(const slo_problem* p, int32_t* dg, const int32_t* meioses, int n,
                 for (int j = 0; j < 2; ++j) fb[2 * i + j] *= (nxt != j) ? th : an;
             }
             int samp;
+            if (g_mlog) g_mlog[i] = 1.0;
             if (fb[2 * i] == 0.0) samp = 1;
             else if (fb[2 * i + 1] == 0.0) samp = 0;
-            else samp = (us[used++] < (fb[2 * i] / (fb[2 * i] + fb[2 * i + 1]))) ? 0 : 1;
+            else {
+                note_margin(us[used], fb[2 * i] / (fb[2 * i] + fb[2 * i + 1]));
+                if (g_mlog) g_mlog[i] = fabs(us[used] - fb[2 * i] / (fb[2 * i] + fb[2 * i + 1]));
+                samp = (us[used++] < (fb[2 * i] / (fb[2 * i] + fb[2 * i + 1]))) ? 0 : 1;
+            }
             if (samp != dgget(p, dg, person, i, par)) dgset(p, dg, person, i, par, samp);
         }
         n_used[s] = used;
@@ -661,10 +743,19 @@ static inline double trait_rec(const slo_problem* p, const tctx* t, int person, 
     return tmp;
 }
 
-/* one full trait peel; returns the final rfunction value (peeler.cc:79-91) */
-static double trait_peel(const slo_problem* p, const tctx* t, double** mat, int* assign) {
+/* one full trait peel; returns the final rfunction value (peeler.cc:79-91).
+ * esum NULL: the reference's plain FP64 peel.  esum non-NULL: after each
+ * rfunction is complete, its cells are divided by 2^e, e the binary exponent
+ * of its largest valid cell (frexp), and e is added to *esum; the peel's value
+ * is then the returned value times 2^(*esum).  Dividing by a power of two is
+ * exact, so away from underflow the two forms agree to the last rounding of
+ * the logarithm, and the rescaled form does not underflow where the plain one
+ * does (hundreds of members). */
+static double trait_peel(const slo_problem* p, const tctx* t, double** mat, int* assign, long* esum) {
     int N = p->N;
+    if (esum) *esum = 0;
     for (int k = 0; k < p->K; ++k) {
+        double vmax = 0.0;
         int c = cut_len(p, k);
         const int* cs = p->cut + p->cut_off[k];
         int peel = p->op_peel[k], type = p->op_type[k];
@@ -735,6 +826,13 @@ static double trait_peel(const slo_problem* p, const tctx* t, double** mat, int*
                 }
             }
             mat[k][cell] = total;
+            if (total > vmax) vmax = total;
+        }
+        if (esum && vmax > 0.0) {
+            int e;
+            frexp(vmax, &e);
+            for (int cell = 0; cell < ipow4(c); ++cell) mat[k][cell] = ldexp(mat[k][cell], -e);
+            *esum += e;
         }
     }
     (void)N;
@@ -759,16 +857,30 @@ int slo_lod(const slo_problem* p, const int32_t* dgs, int n_dgs, double* raw, ui
  * (the value -DBL_MAX, which log_sum skips). */
 int slo_lod_ex(const slo_problem* p, const int32_t* dgs, int n_dgs, double* raw, uint32_t* count,
                double* trait_prob, int zero_ok) {
+    return slo_lod_range(p, dgs, n_dgs, 0, p->M - 1, 0, raw, count, trait_prob, zero_ok);
+}
+
+/* log of a peel's value: plain, or rescaled (log of the scaled value plus
+   esum ln 2) */
+static double peel_log(double r, const long* esum) {
+    return esum ? log(r) + (double)*esum * 0.69314718055994530942 : log(r);
+}
+
+int slo_lod_range(const slo_problem* p, const int32_t* dgs, int n_dgs, int l0, int l1, int rescale, double* raw,
+                  uint32_t* count, double* trait_prob, int zero_ok) {
     int K = p->K, M = p->M, n = p->n_lod, N = p->N;
+    if (l0 < 0 || l1 > M - 1 || l0 > l1) return -2;
     double** mat = (double**)calloc(K, sizeof(double*));
     for (int k = 0; k < K; ++k) mat[k] = (double*)calloc(ipow4(cut_len(p, k)), sizeof(double));
     int* assign = (int*)malloc(sizeof(int) * N);
+    long es = 0;
+    long* esum = rescale ? &es : NULL;
     tctx t;
     memset(&t, 0, sizeof(t));
     t.dg = NULL;
-    double tp = log(trait_peel(p, &t, mat, assign));  /* peeler.cc:65-73 */
-    int nscores = (M - 1) * n;
-    unsigned char* init = (unsigned char*)calloc(nscores, 1);
+    double tp = peel_log(trait_peel(p, &t, mat, assign, esum), esum);  /* peeler.cc:65-73 */
+    int nscores = (l1 - l0) * n;
+    unsigned char* init = (unsigned char*)calloc(nscores > 0 ? nscores : 1, 1);
     int nnf = N - p->F;
     double marker_trans = log(0.5) * (2 * nnf);  /* descent_graph.cc:22 */
     uint32_t cnt = 0;
@@ -776,7 +888,8 @@ int slo_lod_ex(const slo_problem* p, const int32_t* dgs, int n_dgs, double* raw,
     size_t stride = (size_t)2 * N * M;
     for (int d = 0; d < n_dgs; ++d) {
         const int32_t* dg = dgs + d * stride;
-        for (int l = 0; l < M - 1; ++l) {
+        ++cnt;
+        for (int l = l0; l < l1; ++l) {
             /* DescentGraph::get_recombination_prob (descent_graph.cc:212-242) */
             double lt = log(p->theta[l]), la = log(1.0 - p->theta[l]);
             double rec = 0.0;
@@ -791,13 +904,12 @@ int slo_lod_ex(const slo_problem* p, const int32_t* dgs, int n_dgs, double* raw,
                 t.an = 1.0 - t.th;
                 t.th2 = p->partial[l] * (n + 1 - (o + 1));
                 t.an2 = 1.0 - t.th2;
-                double r = trait_peel(p, &t, mat, assign);
+                double r = trait_peel(p, &t, mat, assign, esum);
                 if (r <= 0.0 && !zero_ok) { rc = -1; goto out; }
-                double prob = r > 0.0 ? log(r) - rec - marker_trans : -DBL_MAX;
-                int idx = l * n + o;
+                double prob = r > 0.0 ? peel_log(r, esum) - rec - marker_trans : -DBL_MAX;
+                int idx = (l - l0) * n + o;
                 raw[idx] = init[idx] ? log_sum(prob, raw[idx]) : prob;
                 init[idx] = 1;
-                if (l == 0 && o == 0) ++cnt;
             }
         }
     }

@@ -49,6 +49,13 @@ typedef struct {
  * the first, then one per homozygous-parent meiosis in person order, maternal
  * before paternal.  Returns 0, or -1 on zero likelihood, -2 on draw overrun. */
 int slo_lstep(const slo_problem* p, int32_t* dg, int locus, const double* u, int n_u, int* n_used);
+/* A full L-sweep: every even locus, then every odd locus; locus l's draws
+ * start at u[l * u_stride] (u_stride >= K + 2N).  Returns 0 or the first
+ * failing step's code. */
+int slo_lsweep(const slo_problem* p, int32_t* dg, const double* u, int u_stride);
+/* L-steps at the listed loci in list order (in place, one workspace); the
+ * i-th listed locus reads its draws from u[i * u_stride]. */
+int slo_lsteps(const slo_problem* p, int32_t* dg, const int32_t* loci, int n, const double* u, int u_stride);
 int slo_si(const slo_problem* p, int32_t* dg, int start, const double* u, int n_u, int* n_used, double* weight);
 
 /* One M-sweep: reset at meioses[0] then one step per listed meiosis
@@ -65,12 +72,31 @@ int slo_lod(const slo_problem* p, const int32_t* dgs, int n_dgs, double* raw, ui
 int slo_lod_ex(const slo_problem* p, const int32_t* dgs, int n_dgs, double* raw, uint32_t* count,
                double* trait_prob, int zero_ok);
 
+/* The same scoring restricted to intervals [l0, l1): raw holds (l1-l0)*n_lod
+ * accumulators, interval l0 first.  rescale = 1 divides every rfunction by
+ * a power of two after it is complete and carries the exponents (an FP64 peel
+ * that does not underflow on pedigrees of hundreds of members, where the
+ * reference's plain peel does and Peeler::process exits, peeler.cc:89-92);
+ * rescale = 0 is the plain peel.  Returns 0, -1 on a zero likelihood (unless
+ * zero_ok), -2 on a bad range. */
+int slo_lod_range(const slo_problem* p, const int32_t* dgs, int n_dgs, int l0, int l1, int rescale, double* raw,
+                  uint32_t* count, double* trait_prob, int zero_ok);
+
 /* Founder-allele-graph likelihood of one descent-graph column
  * (founder_allele_graph4.cc:34-442); 0.0 when the column is illegal. */
 double slo_fag_likelihood(const slo_problem* p, const int32_t* dg, int locus);
 
 /* log-likelihood of a whole descent graph (descent_graph.cc:184-267) */
 double slo_loglik(const slo_problem* p, const int32_t* dg);
+
+/* The smallest |draw - decision boundary| met by the sampler calls since the
+ * last reset (L-step genotype and indicator draws, M-step backward draws):
+ * test instrumentation for checking samplers that round differently. */
+void slo_margin_reset(void);
+double slo_margin(void);
+/* per_locus (M doubles, or NULL to stop): each M-step's backward pass writes
+ * the margin of its draw at every locus (1 where it takes none) */
+void slo_margin_log(double* per_locus);
 
 /* Philox4x32-10 uniform in [0,1) for (key, counter) (Salmon et al., SC'11) */
 double slo_philox_uniform(uint64_t key, uint64_t c_hi, uint64_t c_lo);

@@ -1,32 +1,46 @@
 """A short, fixed workload for ncu captures of the library's kernels.
 
-    python -m swiftlink_gb300.profile_workload [--iterations 2] [--chains 10]
+    python profile_workload.py [--workload cfg2|cfg5] [--iterations 2] [--chains C]
         [--lprob 0.5] [--adjoint 0] [--graph] [--lod-kernel K] [--ls-specialised]
 
-On the 120-member, 2000-SNP pedigree it runs `iterations` device-driven MCMC
-iterations of `chains` chains in the fast sampler mode, kernels launched one
-by one with per-class event marks (with --graph: as one launch of the run
-graph, no marks), then one batched FP32 LOD scoring of every chain (the first
-scoring also times the LOD kernel candidates unless --lod-kernel forces one of
-SL_LOD_KERNEL_*; --ls-specialised runs the L-sampler compiled for the
-pedigree), and, with --adjoint G, the
-trait-peel adjoint of G graphs under the dominant model (0.01, 0.8, 0.9),
-q = 1e-3.  It prints the per-kernel-class event times of the sampling part.
+cfg2 is the 120-member, 2000-SNP pedigree (10 chains by default); cfg5 the
+400-member, 10,000-SNP pedigree (32 chains by default).  It runs `iterations`
+device-driven MCMC iterations of `chains` chains in the fast sampler mode,
+kernels launched one by one with per-class event marks (with --graph: as one
+launch of the run graph, no marks), then one batched FP32 LOD scoring of every
+chain (the first scoring also times the LOD kernel candidates unless
+--lod-kernel forces one of SL_LOD_KERNEL_*; --ls-specialised runs the
+L-sampler compiled for the pedigree), and, with --adjoint G, the trait-peel
+adjoint of G graphs under the dominant model (0.01, 0.8, 0.9), q = 1e-3.  It
+prints the per-kernel-class event times of the sampling part.
 """
 from __future__ import annotations
 
 import argparse
+import os
+import sys
+import time
 
 import numpy as np
 
-from swiftlink_gb300 import api
-from swiftlink_gb300.workloads import disease_probs, load_problem
+sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+
+from swiftlink_gb300 import api  # noqa: E402
+from swiftlink_gb300.workloads import disease_probs, load_problem  # noqa: E402
+
+
+def problem(name):
+    if name == "cfg2":
+        return load_problem("cfg2")
+    from swiftlink_gb300 import pedigree, synth
+    return pedigree.problem_from_workload(synth.make_workload(int(name[3:])))
 
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
+    ap.add_argument("--workload", default="cfg2", choices=["cfg2", "cfg5"])
     ap.add_argument("--iterations", type=int, default=2)
-    ap.add_argument("--chains", type=int, default=10)
+    ap.add_argument("--chains", type=int, default=0)
     ap.add_argument("--lprob", type=float, default=0.5)
     ap.add_argument("--adjoint", type=int, default=0)
     ap.add_argument("--seed", type=int, default=5)
@@ -34,8 +48,8 @@ def main(argv=None):
     ap.add_argument("--lod-kernel", type=int, default=api.SL_LOD_KERNEL_AUTO)
     ap.add_argument("--ls-specialised", action="store_true")
     a = ap.parse_args(argv)
-    d = load_problem("cfg2")
-    C = a.chains
+    d = problem(a.workload)
+    C = a.chains or (10 if a.workload == "cfg2" else 32)
     prob = api.Problem.from_arrays(d, with_legal=False)
     with api.Context(prob, n_chains=C, lod_precision=api.SL_LOD_FP32_RESCALED,
                      sampler_precision=api.SL_SAMPLER_FAST, lod_flags=api.SL_LOD_ZERO_OK,
@@ -43,8 +57,10 @@ def main(argv=None):
                      ls_kernel=api.SL_LS_KERNEL_SPECIALISED if a.ls_specialised else api.SL_LS_KERNEL_GENERIC) as ctx:
         ctx.set_graphs(np.stack([d["dg0"]] * C))
         ctx.profile(not a.graph)
+        t = time.perf_counter()
         ctx.run(iterations=a.iterations, burnin=0, period=1 << 30, lprob=a.lprob, seed=a.seed)
         ctx.synchronize()
+        print(f"{a.iterations} iterations of {C} chains: {time.perf_counter() - t:.3f} s wall")
         if not a.graph:
             names = ["L-sampler", "M-sampler", "LOD", "LOD merge", "other"]
             for k in range(5):

@@ -34,7 +34,7 @@
 namespace {
 
 struct Options {
-    std::string ped, map, dat, out = "swiftlink.out", trace_prefix = "trace", seeds, dump;
+    std::string ped, map, dat, out = "swiftlink.out", trace_prefix = "trace", seeds, dump, write_from;
     int iterations = 50000, burnin = 50000, si = 1000, period = 10, lods = 5, runs = 1;
     int chains = 1, exchange = 10;   // MC3 (defaults.h:9, 12)
     double lprob = 0.5;
@@ -408,6 +408,65 @@ bool dump_problems(const std::string& path, const std::vector<Family>& fams, con
     return true;
 }
 
+// The LOD table in LinkageWriter::write's format (linkage_writer.cc:14-89):
+// a header, then per marker interval the marker's name and position (cM) and
+// one line per LOD position with its position, the LOD summed over families
+// and, with more than one family, each family's LOD; the last marker closes.
+// lod[f][(M-1) n] are the families' LODs, (raw - log count - P(T)) / log 10.
+bool write_table(const Options& o, const std::vector<Marker>& map, const std::vector<double>& partial,
+                 const std::vector<std::vector<double>>& lod) {
+    const int M = (int)map.size(), n = o.lods;
+    std::ofstream out(o.out, std::ios::out | std::ios::trunc);
+    if (!out) {
+        fprintf(stderr, "error: could not open linkage output file \"%s\"\n", o.out.c_str());
+        return false;
+    }
+    auto gpos = [&](int i, int off) { return map[i].g + (off ? inverse_haldane(partial[i] * off) : 0.0); };
+    out << "marker\tposition\tlod\n";
+    for (int i = 0; i + 1 < M; ++i) {
+        out << map[i].name << "\t" << 100.0 * gpos(i, 0) << "\n";
+        for (int j = 0; j < n; ++j) {
+            double t = lod[0][(size_t)i * n + j];
+            for (size_t k = 1; k < lod.size(); ++k) t += lod[k][(size_t)i * n + j];
+            std::stringstream ss;
+            ss << "-\t" << 100 * gpos(i, j + 1) << "\t" << t;
+            if (lod.size() > 1)
+                for (size_t k = 0; k < lod.size(); ++k) ss << "\t" << lod[k][(size_t)i * n + j];
+            ss << "\n";
+            out << ss.str();
+            if (o.verbose) fprintf(stderr, "%s", ss.str().c_str());
+        }
+    }
+    out << map[M - 1].name << "\t" << 100.0 * gpos(M - 1, 0) << "\n";
+    return true;
+}
+
+// -W: the families' log-sums, counts and log P(T) from a file, as LODs.
+bool read_logsums(const std::string& path, size_t nfam, size_t npos, std::vector<std::vector<double>>& lod) {
+    std::ifstream f(path);
+    if (!f) {
+        fprintf(stderr, "error: could not open '%s'\n", path.c_str());
+        return false;
+    }
+    lod.assign(nfam, std::vector<double>(npos));
+    for (size_t k = 0; k < nfam; ++k) {
+        double count = 0, tp = 0;
+        if (!(f >> count >> tp) || count < 1) {
+            fprintf(stderr, "error: '%s': family %zu: bad count or P(T)\n", path.c_str(), k + 1);
+            return false;
+        }
+        for (size_t i = 0; i < npos; ++i) {
+            double raw;
+            if (!(f >> raw)) {
+                fprintf(stderr, "error: '%s': family %zu: %zu of %zu log-sums\n", path.c_str(), k + 1, i, npos);
+                return false;
+            }
+            lod[k][i] = (raw - std::log(count) - tp) / std::log(10.0);
+        }
+    }
+    return true;
+}
+
 void usage(const char* prog) {
     fprintf(stderr,
             "Usage: %s -p pedfile -m mapfile -d datfile [options]\n"
@@ -431,7 +490,9 @@ void usage(const char* prog) {
             "  -t LIST   --temperatures=LIST       (comma separated, the first 1.0; default 1 / (1 + 0.001 2^i))\n"
             "  -E        --exact                   (FP64 samplers and LOD, the reference's arithmetic)\n"
             "  -G        --genericls               (no L-sampler compiled for the pedigree on long runs)\n"
-            "  -D FILE   --dumpproblem=FILE        (write the problem tables of every family and stop)\n",
+            "  -D FILE   --dumpproblem=FILE        (write the problem tables of every family and stop)\n"
+            "  -W FILE   --writetable=FILE         (write the LOD table from FILE's per-family log-sums and stop:\n"
+            "                                       per family a line \"count log_P(T)\", then (M-1)*n raw values)\n",
             prog);
 }
 
@@ -461,14 +522,14 @@ int main(int argc, char** argv) {
         {"sexlinked", no_argument, 0, 'X'},       {"elod", no_argument, 0, 'e'},
         {"verbose", no_argument, 0, 'v'},         {"help", no_argument, 0, 'h'},
         {"exact", no_argument, 0, 'E'},           {"dumpproblem", required_argument, 0, 'D'},
-        {"genericls", no_argument, 0, 'G'},
+        {"genericls", no_argument, 0, 'G'},     {"writetable", required_argument, 0, 'W'},
         {"mcmcmc", no_argument, 0, 'M'},          {"chains", required_argument, 0, 'z'},
         {"exchangeperiod", required_argument, 0, 'y'}, {"temperatures", required_argument, 0, 't'},
         {"frequency", required_argument, 0, 'f'}, {"penetrance", required_argument, 0, 'k'},
         {"replicates", required_argument, 0, 'u'}, {"separation", required_argument, 0, 'w'},
         {0, 0, 0, 0}};
     int ch, ignored;
-    while ((ch = getopt_long(argc, argv, "p:m:d:o:i:b:s:x:l:n:R:TP:c:gq:r:aXevhED:Mz:y:t:f:k:u:w:G", longopts, nullptr)) != -1) {
+    while ((ch = getopt_long(argc, argv, "p:m:d:o:i:b:s:x:l:n:R:TP:c:gq:r:aXevhED:Mz:y:t:f:k:u:w:GW:", longopts, nullptr)) != -1) {
         switch (ch) {
             case 'p': o.ped = optarg; break;
             case 'm': o.map = optarg; break;
@@ -494,6 +555,7 @@ int main(int argc, char** argv) {
             case 'D': o.dump = optarg; break;
             case 'M': o.mc3 = true; break;
             case 'G': o.generic_ls = true; break;
+            case 'W': o.write_from = optarg; break;
             case 'z': if (!to_int(optarg, o.chains) || o.chains < 1) { fprintf(stderr, "option '-z' requires an int > 0\n"); return 1; } break;
             case 'y': if (!to_int(optarg, o.exchange) || o.exchange < 1) { fprintf(stderr, "option '-y' requires an int > 0\n"); return 1; } break;
             case 't':
@@ -563,6 +625,11 @@ int main(int argc, char** argv) {
     for (size_t f = 0; f < fams.size(); ++f)
         if (!build_family(fams[f], model, map, o.affected_only, probs[f])) return 1;
     if (!o.dump.empty()) return dump_problems(o.dump, fams, probs, map, model, theta, partial) ? 0 : 1;
+    if (!o.write_from.empty()) {
+        std::vector<std::vector<double>> lod;
+        return read_logsums(o.write_from, fams.size(), (size_t)(M - 1) * n, lod) && write_table(o, map, partial, lod)
+                   ? 0 : 1;
+    }
     // Contexts: without MC3 one per family holding its -R runs as chains; with MC3
     // one per (family, run) holding the -z tempered chains, chain 0 at t = 1.
     struct Unit {
@@ -770,31 +837,7 @@ int main(int argc, char** argv) {
         for (size_t k = 0; k < raw.size(); ++k)
             lod[f][k] = (raw[k] - std::log((double)count) - tp) / std::log(10.0);
     }
-    if (!rc) {
-        std::ofstream out(o.out, std::ios::out | std::ios::trunc);
-        if (!out) {
-            fprintf(stderr, "error: could not open linkage output file \"%s\"\n", o.out.c_str());
-            rc = 1;
-        } else {
-            auto gpos = [&](int i, int off) { return map[i].g + (off ? inverse_haldane(partial[i] * off) : 0.0); };
-            out << "marker\tposition\tlod\n";
-            for (int i = 0; i + 1 < M; ++i) {
-                out << map[i].name << "\t" << 100.0 * gpos(i, 0) << "\n";
-                for (int j = 0; j < n; ++j) {
-                    double t = lod[0][(size_t)i * n + j];
-                    for (size_t k = 1; k < lod.size(); ++k) t += lod[k][(size_t)i * n + j];
-                    std::stringstream ss;
-                    ss << "-\t" << 100 * gpos(i, j + 1) << "\t" << t;
-                    if (lod.size() > 1)
-                        for (size_t k = 0; k < lod.size(); ++k) ss << "\t" << lod[k][(size_t)i * n + j];
-                    ss << "\n";
-                    out << ss.str();
-                    if (o.verbose) fprintf(stderr, "%s", ss.str().c_str());
-                }
-            }
-            out << map[M - 1].name << "\t" << 100.0 * gpos(M - 1, 0) << "\n";
-        }
-    }
+    if (!rc && !write_table(o, map, partial, lod)) rc = 1;
     for (sl_ctx* c : ctxs) sl_destroy(c);
     return rc;
 }

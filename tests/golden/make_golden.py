@@ -17,7 +17,9 @@ from __future__ import annotations
 
 import dataclasses
 import os
+import subprocess
 import sys
+import tempfile
 
 import numpy as np
 
@@ -28,7 +30,17 @@ from oracle import ref  # noqa: E402
 from swiftlink_gb300 import synth  # noqa: E402
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_EXAMPLES = "/root/reference/examples"
+
+
+def reference_root():
+    """The reference's root directory, as oracle/Makefile's REF names it."""
+    out = subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "print-ref"], check=True,
+                         capture_output=True, text=True).stdout.strip()
+    return out
+
+
+REF_EXAMPLES = os.path.join(reference_root(), "examples")
+INPUTS = tempfile.mkdtemp(prefix="swiftlink_golden_")
 
 
 def csr(lists):
@@ -43,8 +55,7 @@ def case_paths(name):
     if name in ("east", "loop"):
         return tuple(os.path.join(REF_EXAMPLES, f"{name}.{ext}") for ext in ("ped", "map", "dat"))
     cfg = int(name[3:])
-    out = os.path.join(ROOT, "_work", "golden_inputs")
-    return synth.workload_files(cfg, out)
+    return synth.workload_files(cfg, INPUTS)
 
 
 def make(name, seed):

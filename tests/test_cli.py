@@ -46,6 +46,28 @@ def golden_problem(name):
     return {k: z[k] for k in z.files}
 
 
+def test_table_writer_matches_the_reference_writer(tmp_path):
+    """The LOD table file for given log-sums, count and log P(T) (the
+    program's -W mode) is byte-identical to the reference's
+    LinkageWriter::write (linkage_writer.cc:14-89) on the same values and the
+    same LINKAGE files (positions from the map, names, number formatting)."""
+    from oracle import ref
+    if not ref.available():
+        pytest.skip("the reference build exists only where the reference sources are")
+    ped, mapf, dat = synth.workload_files(1, str(tmp_path))
+    r = ref.Ref(ped, mapf, dat, n_lod=5, peel_iters=100, seed=3)
+    npos = (r.M - 1) * r.n_lod
+    rng = np.random.default_rng(5)
+    raw = -800.0 + 30.0 * rng.standard_normal(npos)
+    count, tp = 123, -411.25
+    r.write_table(raw, count, tp, str(tmp_path / "ref.lod"))
+    r.close()
+    src = tmp_path / "logsums.txt"
+    src.write_text(f"{count} {tp!r}\n" + "\n".join(repr(float(x)) for x in raw) + "\n")
+    run_cli("-p", ped, "-m", mapf, "-d", dat, "-W", src, "-o", tmp_path / "ours.lod")
+    assert (tmp_path / "ours.lod").read_bytes() == (tmp_path / "ref.lod").read_bytes()
+
+
 @pytest.mark.parametrize("cfg", [1, 2])
 def test_tables_match_the_reference_parse(tmp_path, cfg):
     files = synth.workload_files(cfg, str(tmp_path))

@@ -43,6 +43,67 @@ def test_port_lsweep_matches_golden(name):
 
 
 @pytest.mark.parametrize("name", CASES)
+def test_port_one_call_lsweep_matches_golden(name):
+    """slo_lsweep (the whole even-then-odd sweep in one call, one workspace
+    reused by every locus, the timed CPU arm's L-sweep) equals the reference's
+    locus-by-locus sweep."""
+    g = load_golden(name)
+    P = port.Port(g)
+    dg = np.ascontiguousarray(g["dg0"].copy())
+    P.lsweep(dg, g["lsweep_u"])
+    assert np.array_equal(dg, g["lsweep_after"])
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_port_rescaled_lod_matches_golden(name):
+    """The FP64 peel with per-rfunction power-of-two rescaling (the checker for
+    pedigrees whose plain peel underflows) gives the reference's log-sums and
+    log P(T) where the plain peel does not underflow: equal to 1e-12 in LOD
+    units (log-sums / ln 10)."""
+    g = load_golden(name)
+    P = port.Port(g)
+    M, n = g["M"], g["n_lod"]
+    raw, cnt, tp = P.lod_range(g["lod_graphs"], 0, M - 1, rescale=True)
+    assert cnt == g["lod_count"]
+    assert abs(tp - g["lod_trait_prob"]) / np.log(10) <= 1e-12
+    assert np.abs(raw - g["lod_raw"]).max() / np.log(10) <= 1e-12
+    # a sub-range scores the same positions as the whole map
+    lo = M // 3
+    hi = min(M - 1, lo + 7)
+    sub, _, _ = P.lod_range(g["lod_graphs"], lo, hi, rescale=True)
+    np.testing.assert_array_equal(sub, raw[lo * n:hi * n])
+    plain, _, _ = P.lod_range(g["lod_graphs"], 0, M - 1, rescale=False)
+    np.testing.assert_array_equal(plain, g["lod_raw"])
+
+
+def test_rescaled_lod_where_the_plain_peel_underflows():
+    """On the 400-member pedigree the plain FP64 peel underflows (the reference
+    stops there, peeler.cc:89-92) while the rescaled peel gives finite scores;
+    the two agree on log P(T), which does not underflow."""
+    from swiftlink_gb300 import pedigree, synth
+    d = pedigree.problem_from_workload(synth.make_workload(5))
+    d["legal"] = host_legal(d)
+    d["trait_prior"] = port.derive_priors(d["genotypes"], d["typed"], d["minor"])
+    P = port.Port(d)
+    raw, cnt, tp = P.lod_range(d["dg0"][None], 100, 104, rescale=True)
+    assert np.isfinite(raw).all() and (raw > -1e300).all()
+    plain, _, tp0 = P.lod_range(d["dg0"][None], 100, 104, rescale=False, zero_ok=True)
+    assert (plain <= -1e300).all()
+    assert abs(tp - tp0) <= 1e-12 * abs(tp0)
+
+
+def host_legal(d):
+    """Genotype-elimination masks from the library's host code (no device)."""
+    import ctypes
+    from swiftlink_gb300 import api
+    desc = api.Problem.from_arrays(d, with_legal=False).desc()
+    out = np.zeros((d["M"], d["N"]), np.uint8)
+    rc = api.lib().sl_problem_legal_masks(ctypes.byref(desc), out.ctypes.data_as(ctypes.c_void_p))
+    assert rc == 0
+    return out
+
+
+@pytest.mark.parametrize("name", CASES)
 def test_port_msweep_matches_golden(name):
     g = load_golden(name)
     P = port.Port(g)
