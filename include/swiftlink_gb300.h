@@ -125,6 +125,19 @@ typedef struct sl_options {
 #define SL_LS_KERNEL_GENERIC 0
 #define SL_LS_KERNEL_SPECIALISED 1
 #define SL_LS_KERNEL_BACKGROUND 2
+/* AUTO compiles the specialised kernel at sl_create (falling back to the
+ * generic one if it does not build) and, before the first L-sampler work,
+ * times one half-sweep of every chain with each kernel on a copy of the
+ * chains' graphs and keeps the faster: the generic kernel stores only the
+ * rfunction cells allowed by genotype elimination and wins on pedigrees with
+ * large cutsets (hundreds of members), the specialised one on smaller ones. */
+#define SL_LS_KERNEL_AUTO 3
+/* GENERIC times 32 against 16 lanes per (chain, locus) task (two tasks per
+ * warp) before the first L-sampler work and keeps the faster, sharing the
+ * choice between contexts of one pedigree size class; these two force one
+ * (all forms draw the same graphs). */
+#define SL_LS_KERNEL_GENERIC32 4
+#define SL_LS_KERNEL_GENERIC16 5
 
 /* A LOD position whose trait likelihood is 0 (an affected and an unaffected
  * member IBD 2 under a fully penetrant model, for instance) stops the
@@ -309,7 +322,10 @@ int sl_problem_lod_program_eval(const sl_problem_desc* problem, const int32_t* d
  * point where they score: hosts whose own allocator reserves the device's
  * memory up front and forbids further driver allocations, and latency-bound
  * loops where a cudaMalloc/cudaFree, which can synchronise the whole device,
- * would stall other streams.  It does what sl_lod_score_graphs does, but the
+ * would stall other streams.  It scores as sl_lod_score_graphs does, with the
+ * kernel the context scores with (in the FP32-rescaled form, before the first
+ * sl_lod_score_* call has timed the candidates, the specialised kernel with
+ * values in registers if it was built, else the interpreter), but the
  * per-graph, per-position values live in a file-scope device array of
  * SL_NOALLOC_SCRATCH_BYTES (8 MiB) that every GPU loading the library holds
  * until exit, and the caller passes device buffers:
@@ -322,7 +338,8 @@ int sl_problem_lod_program_eval(const sl_problem_desc* problem, const int32_t* d
  * n_graphs * (M-1) * n must not exceed SL_NOALLOC_SCRATCH_BYTES / 8; larger
  * requests return SL_EINVAL.  The work is queued on the context's stream;
  * sl_synchronize reports device errors.  The first call on a device looks up
- * the array's device address (cudaGetSymbolAddress) once for that device.
+ * the array's device address (cudaGetSymbolAddress) once for that device; the
+ * calling thread's current device is the same after the call as before it.
  * All calls share the one array: calls that overlap on the GPU (several
  * contexts or streams at once) race on it.  The context's own accumulators
  * and count are not touched.

@@ -21,7 +21,8 @@ SL_LOD_FP64, SL_LOD_FP32_RESCALED, SL_LOD_FP64_RESCALED = 0, 1, 2
 SL_SAMPLER_EXACT, SL_SAMPLER_FAST = 0, 1
 SL_LOD_KERNEL_AUTO, SL_LOD_KERNEL_INTERP, SL_LOD_KERNEL_JIT_REG, SL_LOD_KERNEL_JIT_SMEM = 0, 1, 2, 3
 SL_LOD_ZERO_OK = 1
-SL_LS_KERNEL_GENERIC, SL_LS_KERNEL_SPECIALISED, SL_LS_KERNEL_BACKGROUND = 0, 1, 2
+SL_LS_KERNEL_GENERIC, SL_LS_KERNEL_SPECIALISED, SL_LS_KERNEL_BACKGROUND, SL_LS_KERNEL_AUTO = 0, 1, 2, 3
+SL_LS_KERNEL_GENERIC32, SL_LS_KERNEL_GENERIC16 = 4, 5
 
 EXPORTED = [
     "sl_create", "sl_destroy", "sl_last_error", "sl_set_descent_graphs", "sl_get_descent_graphs",

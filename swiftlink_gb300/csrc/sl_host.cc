@@ -18,6 +18,8 @@
 #include <chrono>
 #include <thread>
 #include <type_traits>
+#include <tuple>
+#include <mutex>
 #include <vector>
 
 #include "../../include/swiftlink_gb300.h"
@@ -32,7 +34,7 @@ size_t lsampler_smem_shared(const ProblemDev& P);
 cudaError_t launch_lsampler(const ProblemDev& P, uint32_t* dg, int first, int nchain, const int32_t* loci,
                             int nloci, const double* u, int64_t ucs, int64_t uls, uint64_t seed, uint64_t iter,
                             const uint8_t* sel, int want, int* status, cudaStream_t s, int grid_cap, int wpb,
-                            const uint64_t* key = nullptr);
+                            const uint64_t* key = nullptr, int lanes = 32);
 cudaError_t launch_msampler(const ProblemDev& P, uint32_t* dg, int first, int nchain, const int32_t* meioses,
                             int64_t mstride, int nm, const double* u, int64_t ucs, uint64_t seed, uint64_t iter,
                             const uint8_t* sel, int want, double* raw64, float* raw32, void* fb, uint8_t* badc,
@@ -75,6 +77,8 @@ namespace {
 thread_local std::string g_err;
 const size_t kSmemBudget = 200 * 1024;  // dynamic shared memory a block may use
 }  // namespace
+
+enum { LS_GEN32 = 0, LS_GEN16 = 1, LS_JIT = 2 };
 
 struct sl_ctx {
     int device = 0;
@@ -164,7 +168,13 @@ struct sl_ctx {
     std::shared_ptr<const JitBinary> ls_bin;    // written by ls_thread before ls_pending = 2
     double ls_thread_ms = 0.0;                  // likewise
     size_t ls_warp_bytes = 0;
+    int jit_ls_wpb = 1;                  // warps per block of the specialised L-sampler (its own arena layout)
     int ls_epoch = 0;                           // kernel switches (graphs captured before are redone)
+    // the L-sampler's kernel and lanes per task: the generic kernel with 32 or
+    // 16 lanes, or the specialised one; chosen by timing (ls_tune) unless forced
+    bool ls_tune_pending = false;
+    int ls_choice = 0;                          // LS_GEN32, LS_GEN16, LS_JIT
+    double ls_tune_ms[3] = {0.0, 0.0, 0.0};     // one timed half-sweep with each (0: not timed)
     int lod_kernel_sel = SL_LOD_KERNEL_INTERP;   // AUTO while the first scoring has not timed them
     JitLod jit_reg, jit_smem;
     double jit_ms = 0.0;
@@ -205,11 +215,11 @@ static cudaError_t ls_launch(sl_ctx* ctx, int first, int nchain, const int32_t* 
                              int64_t ucs, int64_t uls, uint64_t seed, uint64_t iter, const uint8_t* sel, int want,
                              cudaStream_t s, const uint64_t* key = nullptr) {
     const ProblemDev& P = ctx->P;
-    if (ctx->jit_ls.kern)
+    if (ctx->jit_ls.kern && ctx->ls_choice == LS_JIT)
         return jit_ls_launch(ctx->jit_ls, ctx->d_dg, first, nchain, loci, nloci, u, ucs, uls, seed, iter, key, sel,
                              want, ctx->d_status, P.geno, P.prior_f, P.c_theta_f, ctx->sms, s);
     return launch_lsampler(P, ctx->d_dg, first, nchain, loci, nloci, u, ucs, uls, seed, iter, sel, want, ctx->d_status,
-                           s, ctx->ls_grid, ctx->ls_wpb, key);
+                           s, ctx->ls_grid, ctx->ls_wpb, key, ctx->ls_choice == LS_GEN16 ? 16 : 32);
 }
 
 // Takes up a background compile of the specialised L-sampler that has ended:
@@ -226,10 +236,11 @@ static void ls_adopt(sl_ctx* ctx) {
     cudaSetDevice(ctx->device);
     std::string log;
     JitLs j;
-    if (jit_ls_load(*ctx->ls_bin, ctx->ls_wpb, ctx->ls_warp_bytes, &j, &log)) {
+    if (jit_ls_load(*ctx->ls_bin, ctx->jit_ls_wpb, ctx->ls_warp_bytes, &j, &log)) {
         ctx->err = "specialised L-sampler failed (the generic kernel runs): " + log.substr(0, 300);
     } else {
         ctx->jit_ls = j;
+        ctx->ls_choice = LS_JIT;
         ctx->jit_ls.compile_ms = ctx->ls_thread_ms;
         if (ctx->run_graph) {
             cudaStreamSynchronize(ctx->stream);   // no launch of it in flight
@@ -301,6 +312,91 @@ static int fail(sl_ctx* c, int code, const char* fmt, ...) {
             return fail(ctx, e_ == cudaErrorMemoryAllocation ? SL_ENOMEM : SL_ECUDA, "%s: %s", \
                         #call, cudaGetErrorString(e_));                                       \
     } while (0)
+
+// The L-sampler autotuner: times one even-locus half-sweep of every chain
+// with each candidate -- the generic kernel with 32 lanes per (chain, locus)
+// task and with 16 (two tasks per warp), and the specialised kernel when it
+// was built for SL_LS_KERNEL_AUTO -- on a copy of the chains' graphs (the
+// chains are not touched), and keeps the fastest, as the reference times its
+// launch shapes and locus groupings (gpu_lodscores.cc:541-596,
+// markov_chain.cc:269-311).  Every candidate draws the same graphs, so the
+// choice changes speed only.  Pedigrees of one size class (operations and
+// allowed rfunction cells, in steps of 25 and 128) share the timing: the
+// first context of a class on a device times, later ones (the members of an
+// uneven batch) reuse its choice.  Runs once per context, outside any
+// capture, before its first L-sampler work.
+static std::mutex g_ls_class_mu;
+static std::map<std::tuple<int, int, int, int, int, bool>, int> g_ls_class;
+
+static int ls_tune(sl_ctx* ctx) {
+    if (!ctx->ls_tune_pending) return SL_OK;
+    ctx->ls_tune_pending = false;
+    const ProblemDev& P = ctx->P;
+    const bool jit = ctx->jit_ls.kern != nullptr;
+    const auto key = std::make_tuple(ctx->device, P.ls_fast, P.K / 25, P.ls_arena / 128, std::min(ctx->n_chains, 64),
+                                     jit);
+    if (!jit) {
+        std::lock_guard<std::mutex> g(g_ls_class_mu);
+        auto it = g_ls_class.find(key);
+        if (it != g_ls_class.end()) {
+            if (it->second != ctx->ls_choice) ++ctx->ls_epoch;
+            ctx->ls_choice = it->second;
+            return SL_OK;
+        }
+    }
+    const int C = ctx->n_chains;
+    const size_t words = (size_t)C * P.M * P.W;
+    uint32_t* scratch = nullptr;
+    if (cudaMalloc(&scratch, sizeof(uint32_t) * words) != cudaSuccess) {
+        cudaGetLastError();
+        return SL_OK;   // untimed: the first candidate stays
+    }
+    int st = 0;
+    CK(cudaStreamSynchronize(ctx->stream));
+    CK(cudaMemcpy(&st, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpyAsync(scratch, ctx->d_dg, sizeof(uint32_t) * words, cudaMemcpyDeviceToDevice, ctx->stream));
+    cudaEvent_t a = take_event(ctx), b = take_event(ctx);
+    std::vector<int> cand = {LS_GEN32, LS_GEN16};
+    if (jit) cand.push_back(LS_JIT);
+    int best = ctx->ls_choice;
+    float best_ms = 0.f;
+    for (int k : cand) {
+        float ms = 0.f;
+        for (int rep = 0; rep < 2; ++rep) {
+            if (rep == 1) CK(cudaEventRecord(a, ctx->stream));
+            if (k == LS_JIT)
+                CK(jit_ls_launch(ctx->jit_ls, scratch, 0, C, ctx->d_even, (int)ctx->even.size(), nullptr, 0, 0, 1, 0,
+                                 nullptr, nullptr, 0, ctx->d_status, P.geno, P.prior_f, P.c_theta_f, ctx->sms,
+                                 ctx->stream));
+            else
+                CK(launch_lsampler(P, scratch, 0, C, ctx->d_even, (int)ctx->even.size(), nullptr, 0, 0, 1, 0,
+                                   nullptr, 0, ctx->d_status, ctx->stream, ctx->ls_grid, ctx->ls_wpb, nullptr,
+                                   k == LS_GEN16 ? 16 : 32));
+            if (rep == 1) {
+                CK(cudaEventRecord(b, ctx->stream));
+                CK(cudaEventSynchronize(b));
+                CK(cudaEventElapsedTime(&ms, a, b));
+            }
+        }
+        ctx->ls_tune_ms[k] = ms;
+        if (k == cand[0] || ms < best_ms) {
+            best = k;
+            best_ms = ms;
+        }
+    }
+    ctx->event_pool.push_back(a);
+    ctx->event_pool.push_back(b);
+    CK(cudaStreamSynchronize(ctx->stream));
+    cudaFree(scratch);
+    CK(cudaMemcpy(ctx->d_status, &st, sizeof(int), cudaMemcpyHostToDevice));   // the timing runs report nothing
+    if (best != ctx->ls_choice) ++ctx->ls_epoch;
+    ctx->ls_choice = best;
+    if (!jit) {
+        std::lock_guard<std::mutex> g(g_ls_class_mu);
+        g_ls_class[key] = best;
+    }
+    return SL_OK;
+}
 
 template <typename T>
 static int dev_alloc(sl_ctx* ctx, T** p, size_t n) {
@@ -603,12 +699,16 @@ static int build_ops(const sl_problem_desc* d, std::vector<OpDev>& ops, std::vec
         }
         o.mat_off = arena;
         arena += 1 << (2 * o.c);
+        o.prev_ops_at = (int)od.size();
+        for (int q = d->prev_off[k]; q < d->prev_off[k + 1]; ++q) od.push_back(d->prev[q]);
     }
-    if (ops[K - 1].c != 0) return (fail(nullptr, SL_EINVAL, "last op must have an empty cutset"));
-    if (max_child > 31) return (fail(nullptr, SL_EINVAL, "parent peel with %d children", max_child));
-
     if (ops[K - 1].c != 0) return fail(nullptr, SL_EINVAL, "last op must have an empty cutset");
     if (max_child > 31) return fail(nullptr, SL_EINVAL, "parent peel with %d children", max_child);
+    // the FP32 trait peel's scaling targets (LI_SCALE, sl_internal.h): each
+    // rfunction by the number of rfunctions its consumer multiplies
+    for (int k = 0; k < K; ++k)
+        for (int q = d->prev_off[k]; q < d->prev_off[k + 1]; ++q)
+            ops[d->prev[q]].scale_to = std::max(0, 120 / std::max(1, ops[k].n_prev) - 4);
     return SL_OK;
 }
 
@@ -826,6 +926,7 @@ static void compile_lod_program(const sl_problem_desc* d, const std::vector<OpDe
             W.push_back(LI_SCALE);
             W.push_back(first[k]);
             W.push_back(count[k]);
+            W.push_back(full ? 0 : op.scale_to);
         }
         // temporaries and consumed matrices are dead now
         for (size_t c = 0; c < kids.size(); ++c) sa.release(rec_slot[c], 4);
@@ -922,7 +1023,7 @@ static int host_backward(const sl_problem_desc* d, const LodProgram& prog, const
             for (int q = 0; q < pc[2]; ++q) mx = std::max(mx, A[pc[1] + q]);
             int e = 0;
             if (mx > 0.0) {
-                e = std::ilogb(mx);
+                e = std::ilogb(mx) - pc[3];
                 const double f = std::ldexp(1.0, -e);
                 for (int q = 0; q < pc[2]; ++q) A[pc[1] + q] *= f;
             }
@@ -1201,6 +1302,27 @@ int sl_create(const sl_problem_desc* d, const sl_options* opt, sl_ctx** out) {
     P.N = N; P.F = F; P.M = M; P.K = K; P.n_lod = n; P.Nnf = N - F;
     P.W = (2 * (N - F) + 31) / 32;
     P.arena = arena;
+    // the L-sampler's compact rfunctions (ls_locus, sl_kernels.cu): at a
+    // locus, op k's cells number 2^(the sum of its members' rank bits); the
+    // warp's arena holds the most any locus needs
+    {
+        auto rank_bits = [](int mask) {
+            const int s = __builtin_popcount(mask);
+            return s <= 1 ? 0 : (s == 2 ? 1 : 2);
+        };
+        int most = 1;
+        for (int l = 0; l < M; ++l) {
+            const uint8_t* lg = ctx->legal.data() + (size_t)l * N;
+            int tot = 0;
+            for (int k = 0; k < K; ++k) {
+                int b = 0;
+                for (int q = 0; q < ops[k].c; ++q) b += rank_bits(lg[od[ops[k].cut_at + q]] & 15);
+                tot += 1 << b;
+            }
+            most = std::max(most, tot);
+        }
+        P.ls_arena = most;
+    }
     P.max_child = max_child;
     P.fag_bytes = 0;
     P.marker_trans = std::log(0.5) * (2 * (N - F));
@@ -1383,21 +1505,31 @@ int sl_create(const sl_problem_desc* d, const sl_options* opt, sl_ctx** out) {
     std::string ls_src;
     {   // the FP32 L-sampler specialised to the pedigree, on request
         const int req = opt->ls_kernel;
-        if (req != SL_LS_KERNEL_GENERIC && req != SL_LS_KERNEL_SPECIALISED && req != SL_LS_KERNEL_BACKGROUND)
+        if (req != SL_LS_KERNEL_GENERIC && req != SL_LS_KERNEL_SPECIALISED && req != SL_LS_KERNEL_BACKGROUND &&
+            req != SL_LS_KERNEL_AUTO && req != SL_LS_KERNEL_GENERIC32 && req != SL_LS_KERNEL_GENERIC16)
             return bail(fail(nullptr, SL_EINVAL, "unknown ls_kernel %d", req));
+        if (req == SL_LS_KERNEL_GENERIC) ctx->ls_tune_pending = true;   // 32 or 16 lanes per task, by timing
+        if (req == SL_LS_KERNEL_GENERIC16) ctx->ls_choice = LS_GEN16;
         if (P.ls_fast && req == SL_LS_KERNEL_BACKGROUND) {
             // the source now (host tables in hand), the compile on a thread started once creation has succeeded
             const JitLsIn in{ops.data(), od.data(), K, N, F, M, P.W, N - F, arena, max_child, d->mother, d->father};
-            ls_src = jit_ls_source(in, ctx->ls_wpb);
             ctx->ls_warp_bytes = jit_ls_warp_bytes(in);
+            ctx->jit_ls_wpb = (int)std::max<size_t>(1, std::min<size_t>(4, kSmemBudget / ctx->ls_warp_bytes));
+            ls_src = jit_ls_source(in, ctx->jit_ls_wpb);
         }
-        if (P.ls_fast && req == SL_LS_KERNEL_SPECIALISED) {
+        if (P.ls_fast && (req == SL_LS_KERNEL_SPECIALISED || req == SL_LS_KERNEL_AUTO)) {
             const JitLsIn in{ops.data(), od.data(), K, N, F, M, P.W, N - F, arena, max_child, d->mother, d->father};
+            ctx->jit_ls_wpb = (int)std::max<size_t>(1, std::min<size_t>(4, kSmemBudget / jit_ls_warp_bytes(in)));
             const auto t0 = std::chrono::steady_clock::now();
             std::string log;
-            if (jit_ls_compile(in, ctx->ls_wpb, &ctx->jit_ls, &log))
-                return bail(fail(nullptr, SL_EINVAL, "specialised L-sampler failed: %.300s", log.c_str()));
+            if (jit_ls_compile(in, ctx->jit_ls_wpb, &ctx->jit_ls, &log)) {
+                if (req == SL_LS_KERNEL_SPECIALISED)
+                    return bail(fail(nullptr, SL_EINVAL, "specialised L-sampler failed: %.300s", log.c_str()));
+                ctx->jit_ls = JitLs{};   // AUTO: the generic kernels, timed
+            }
             ctx->jit_ls_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+            ctx->ls_choice = ctx->jit_ls.kern ? LS_JIT : LS_GEN32;
+            ctx->ls_tune_pending = req == SL_LS_KERNEL_AUTO;
         }
     }
     if (d->affection) {
@@ -1572,6 +1704,7 @@ int sl_lsampler_loci(sl_ctx* ctx, int32_t first, int32_t n_chains, const int32_t
         return fail(ctx, SL_EINVAL, "draw strides too small (need locus stride >= K + 2N)");
     CK(cudaSetDevice(ctx->device));
     ls_adopt(ctx);
+    if ((rc = ls_tune(ctx))) return rc;
     if ((rc = stage_draws(ctx, u, (size_t)n_chains * ucs))) return rc;
     CK(cudaMemcpyAsync(ctx->d_loci, loci, sizeof(int32_t) * n_loci, cudaMemcpyHostToDevice, ctx->stream));
     { Prof pf_(ctx, SL_KERNEL_LSAMPLER);
@@ -1590,6 +1723,7 @@ int sl_lsampler_sweep(sl_ctx* ctx, int32_t first, int32_t n_chains, const double
         return fail(ctx, SL_EINVAL, "draw strides too small (need locus stride >= K + 2N)");
     CK(cudaSetDevice(ctx->device));
     ls_adopt(ctx);
+    if ((rc = ls_tune(ctx))) return rc;
     if ((rc = stage_draws(ctx, u, (size_t)n_chains * ucs))) return rc;
     { Prof pf_(ctx, SL_KERNEL_LSAMPLER);
       CK(ls_launch(ctx, first, n_chains, ctx->d_even, (int)ctx->even.size(), ctx->d_u, ucs, uls, 0, 0,
@@ -1632,16 +1766,19 @@ int sl_msampler_sweep(sl_ctx* ctx, int32_t first, int32_t n_chains, const int32_
     return sl_synchronize(ctx);
 }
 
-// One launch of the batched scorer's kernel `which` over G graphs.
-static cudaError_t launch_lod_kernel(sl_ctx* ctx, int which, const uint32_t* graphs, int G) {
+// One launch of the batched scorer's kernel `which` over G graphs, the
+// per-position values into vals (the context's buffer unless given).
+static cudaError_t launch_lod_kernel(sl_ctx* ctx, int which, const uint32_t* graphs, int G,
+                                     double* vals = nullptr) {
     const ProblemDev& P = ctx->P;
     const int64_t npos = (int64_t)(P.M - 1) * P.n_lod;
+    if (!vals) vals = ctx->d_vals;
     if (which == SL_LOD_KERNEL_JIT_REG || which == SL_LOD_KERNEL_JIT_SMEM) {
         const JitLod& j = which == SL_LOD_KERNEL_JIT_REG ? ctx->jit_reg : ctx->jit_smem;
-        return jit_lod_launch(j, graphs, (int64_t)P.M * P.W, G, ctx->d_vals, ctx->d_status, P.partial_f, P.log_theta, P.log_itheta,
-                              npos * G, ctx->sms, ctx->stream);
+        return jit_lod_launch(j, graphs, (int64_t)P.M * P.W, G, vals, ctx->d_status, P.partial_f, P.log_theta,
+                              P.log_itheta, npos * G, ctx->sms, ctx->stream);
     }
-    return launch_lod(P, ctx->lod_precision, graphs, (int64_t)P.M * P.W, G, ctx->d_vals, ctx->d_status, ctx->stream,
+    return launch_lod(P, ctx->lod_precision, graphs, (int64_t)P.M * P.W, G, vals, ctx->d_status, ctx->stream,
                       ctx->lod_grid, ctx->lod_wpb);
 }
 
@@ -1829,6 +1966,21 @@ int ctx_view(sl_ctx* ctx, CtxView* v) {
     return SL_OK;
 }
 void ctx_fail(sl_ctx* ctx, int code, const char* msg) { fail(ctx, code, "%s", msg); }
+
+// The scorer the context scores with (sl_lod_score_graphs), G graphs' values
+// into vals, launched on the context's stream without synchronising: the
+// FP64 forms' kernel, or the FP32 form's selected kernel -- where the first
+// scoring has not yet timed the candidates, the specialised form with values
+// in registers if it was built, else the interpreter (no timing here, so the
+// call stays asynchronous).
+cudaError_t ctx_launch_lod(sl_ctx* ctx, const uint32_t* graphs, int G, double* vals) {
+    int which = SL_LOD_KERNEL_INTERP;
+    if (ctx->lod_precision == SL_LOD_FP32_RESCALED) {
+        which = ctx->lod_kernel_sel;
+        if (which == SL_LOD_KERNEL_AUTO) which = ctx->jit_reg.kern ? SL_LOD_KERNEL_JIT_REG : SL_LOD_KERNEL_INTERP;
+    }
+    return launch_lod_kernel(ctx, which, graphs, G, vals);
+}
 }  // namespace sl
 
 extern "C" {
@@ -1908,7 +2060,7 @@ int sl_problem_lod_program_eval(const sl_problem_desc* d, const int32_t* dg, int
             A[dst] = v;
             pc += 3 + ns;
         } else if (op == LI_SCALE) {
-            pc += 3;
+            pc += 4;
         } else {
             result = pc[1] >= 0 ? A[pc[1]] : 0.0;
             break;
@@ -1965,7 +2117,7 @@ int sl_set_temperatures(sl_ctx* ctx, const double* temps) {
 int sl_ls_kernel_info(sl_ctx* ctx, int32_t* kernel, double* compile_ms) {
     if (!ctx) return fail(ctx, SL_EINVAL, "null context");
     ls_adopt(ctx);
-    if (kernel) *kernel = ctx->jit_ls.kern ? SL_LS_KERNEL_SPECIALISED : SL_LS_KERNEL_GENERIC;
+    if (kernel) *kernel = ctx->jit_ls.kern && ctx->ls_choice == LS_JIT ? SL_LS_KERNEL_SPECIALISED : SL_LS_KERNEL_GENERIC;
     if (compile_ms) *compile_ms = ls_compiling(ctx) ? -1.0 : ctx->jit_ls_ms;
     return SL_OK;
 }
@@ -2157,6 +2309,7 @@ static int prepare_run_graph(sl_ctx* ctx) {
     const int64_t npos = (int64_t)(M - 1) * P.n_lod;
     const bool exact = ctx->sampler_precision == SL_SAMPLER_EXACT;
     int rc;
+    if ((rc = ls_tune(ctx))) return rc;
     if (!ctx->d_run && (rc = dev_alloc(ctx, (uint8_t**)&ctx->d_run, sizeof(RunParams)))) return rc;
     if (!ctx->d_chain_it && (rc = dev_alloc(ctx, &ctx->d_chain_it, C))) return rc;
     if (!ctx->d_keys && (rc = dev_alloc(ctx, &ctx->d_keys, 2 * (size_t)C))) return rc;

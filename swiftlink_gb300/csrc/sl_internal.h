@@ -21,13 +21,16 @@ struct OpDev {
     int32_t child_at;  // opdata offset: per child [child id, child pos, other-parent pos, peel is mother]
     int32_t mpos, fpos;  // child peel: cutset positions of the mother and the father
     int32_t mat_off;     // offset of this op's dense 4^c matrix in a task's arena
-    int32_t pad;
+    int32_t scale_to;    // FP32 trait peel: binary exponent this op's largest cell is scaled to (see LI_SCALE)
+    int32_t prev_ops_at; // opdata offset: the op index of each previous rfunction, in prev_at's order
 };
 
 // Everything a kernel needs about one problem; passed by value.
 struct ProblemDev {
     int32_t N, F, M, K, n_lod, Nnf, W;   // W = 32-bit words per descent-graph column
     int32_t arena;                       // sum over ops of 4^c
+    int32_t ls_arena;                    // the L-sampler's compact rfunctions: the largest, over loci, sum over
+                                         // ops of their cells in legal states (sl_kernels.cu, ls_locus)
     int32_t max_child;                   // max children of an op (>= 1)
     int32_t fag_bytes;                   // shared bytes one FAG evaluation needs
     double marker_trans;                 // log(0.5) * 2 * Nnf (descent_graph.cc:22)
@@ -82,7 +85,13 @@ struct ProblemDev {
 //   LI_SUM  dst n src...         A[dst] = sum of A[src]
 //   LI_CELL dst nterm, then per term: nf const_index slot x nf
 //                                A[dst] = sum over terms of const * product of A[slot]
-//   LI_SCALE first count         divide A[first .. first+count) by 2^e, e from their max
+//   LI_SCALE first count target  multiply A[first .. first+count) by 2^-e, e = ilogb(their max) - target:
+//                                the largest value becomes 2^target.  A consumer multiplying n_prev
+//                                rfunctions gets each scaled to 2^(120/n_prev - 4), so the product of
+//                                its inputs' largest cells stays below 2^120 while the cells its terms
+//                                actually read, often far below their rfunction's maximum, keep clear of
+//                                FP32 underflow (scaling every maximum to 1 underflowed on a 400-member
+//                                pedigree); the last rfunction's target is 0
 //   LI_END  slot                 the likelihood
 enum { LI_REC = 1, LI_SUM = 2, LI_CELL = 3, LI_SCALE = 4, LI_END = 5 };
 

@@ -159,17 +159,17 @@ std::string jit_source(const JitProgramIn& in, int threads, bool shared) {
             s += def(dst) + e + ";\n";
             pc += 3 + ns;
         } else if (op == LI_SCALE) {
-            const int first = pc[1], cnt = pc[2];
-            pc += 3;
+            const int first = pc[1], cnt = pc[2], target = pc[3];
+            pc += 4;
             const int k = sc++;
             std::string mx = "0.0f";
             for (int q = 0; q < cnt; ++q) mx = "fmaxf(" + mx + ", " + ref(first + q) + ")";
             emitf(s, "    const float mx%d = %s;\n", k, mx.c_str());
-            emitf(s, "    const int e%d = mx%d > 0.0f ? ilogbf(mx%d) : 0;\n", k, k, k);
-            emitf(s, "    const float f%d = scalbnf(1.0f, -e%d);\n    scale += e%d;\n", k, k, k);
+            emitf(s, "    const int e%d = mx%d > 0.0f ? ilogbf(mx%d) - %d : 0;\n    scale += e%d;\n", k, k, k,
+                  target, k);
             for (int q = 0; q < cnt; ++q) {
                 const std::string old = ref(first + q);
-                s += def(first + q) + old + " * f" + std::to_string(k) + ";\n";
+                s += def(first + q) + "ldexpf(" + old + ", -e" + std::to_string(k) + ");\n";
             }
         } else {   // LI_END
             const int rs = pc[1];

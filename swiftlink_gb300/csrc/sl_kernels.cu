@@ -125,6 +125,27 @@ struct Ls<float> {   // rounded operations, never contracted: the kernel special
     static __device__ __forceinline__ float div(float a, float b) { return __fdiv_rn(a, b); }
 };
 
+// The lanes working on one L-sampler task: a whole warp (G = 32) or half of
+// one (G = 16; two tasks per warp, for pedigrees whose rfunctions have few
+// allowed cells).  Shuffles and ballots stay within the group; lane numbers
+// are the group's own.
+template <int G>
+struct Lanes {
+    unsigned mask;
+    __device__ __forceinline__ Lanes() : mask(G == 32 ? FULLMASK : (0xffffu << (threadIdx.x & 16))) {}
+    template <typename V>
+    __device__ __forceinline__ V shfl(V v, int src) const { return __shfl_sync(mask, v, src, G); }
+    template <typename V>
+    __device__ __forceinline__ V shfl_xor(V v, int d) const { return __shfl_xor_sync(mask, v, d, G); }
+    template <typename V>
+    __device__ __forceinline__ V shfl_up(V v, int d) const { return __shfl_up_sync(mask, v, d, G); }
+    __device__ __forceinline__ unsigned ballot(bool p) const {
+        const unsigned b = __ballot_sync(mask, p);
+        return G == 32 ? b : (b >> (threadIdx.x & 16)) & 0xffffu;
+    }
+    __device__ __forceinline__ void sync() const { __syncwarp(mask); }
+};
+
 // ---------------------------------------------------------------------------
 // L-sampler
 // ---------------------------------------------------------------------------
@@ -162,29 +183,34 @@ __device__ void ls_dist_one(const ProblemDev& P, int person, const uint32_t* col
     }
 }
 
-template <typename T>
+template <typename T, int G>
 __device__ __forceinline__ void ls_dists(const ProblemDev& P, const OpDev& op, const int32_t* opd,
                                          const uint32_t* colL, const uint32_t* colR, int l, T th, T an, T th2, T an2,
                                          T* dist, int lane) {
     const int nch = op.type == CHILD ? 1 : (op.type == PARENT ? op.n_child : 0);
-    if (lane < nch) {
-        const int person = op.type == CHILD ? op.peel : opd[op.child_at + 4 * lane];
-        ls_dist_one<T>(P, person, colL, colR, l, th, an, th2, an2, dist + 16 * lane);
+    for (int c = lane; c < nch; c += G) {
+        const int person = op.type == CHILD ? op.peel : opd[op.child_at + 4 * c];
+        ls_dist_one<T>(P, person, colL, colR, l, th, an, th2, an2, dist + 16 * c);
     }
 }
 
-__device__ __forceinline__ bool ls_valid(const int32_t* cut, int c, const uint8_t* gcol, int cell) {
-    bool ok = true;
-    for (int q = 0; q < c; ++q) ok &= ((gcol[cut[q]] >> (4 + digit(cell, q))) & 1) != 0;
-    return ok;
-}
+// A cell of op k in the compact layout, with the peel node's state v: ext
+// holds the dense digits of (cutset states, v) as in peel_matrix.h:37-45, rk
+// the states' ranks and bits each position's rank bits (2 bits per position,
+// the peel node at position c), bad the positions whose state is not allowed
+// (only the peel node's can be, the cell itself being valid).
+struct LsCell {
+    int ext, rk, bits, bad;
+};
 
 // One presum entry (cell, peel state v) in the reference's product order
-// (sampler_rfunction.cc:190-287, rfunction.cc:116-142).
+// (sampler_rfunction.cc:190-287, rfunction.cc:116-142); a previous rfunction
+// is read at its compact index, or as zero where the dense matrix held zero.
 template <typename T>
-__device__ T ls_term(const OpDev& op, const int32_t* opd, const T* Am, const T* dist, int cell, int v, T tv) {
+__device__ T ls_term(const OpDev& op, const int32_t* opd, const T* Am, const int32_t* off, const T* dist,
+                     const LsCell& x, int v, T tv) {
     using A = Ls<T>;
-    const int ext = cell | (v << (2 * op.c));
+    const int ext = x.ext;
     T tmp = tv;
     if (op.type == CHILD) {
         const int mt = digit(ext, op.mpos), pt = digit(ext, op.fpos);
@@ -192,11 +218,17 @@ __device__ T ls_term(const OpDev& op, const int32_t* opd, const T* Am, const T* 
         tmp = A::mul(tmp, tr);
     }
     const int32_t* pd = opd + op.prev_at;
+    const int32_t* po = opd + op.prev_ops_at;
     for (int j = 0; j < op.n_prev; ++j) {
-        const int moff = pd[0], pc = pd[1];
-        int idx = 0;
-        for (int q = 0; q < pc; ++q) idx |= digit(ext, pd[2 + q]) << (2 * q);
-        tmp = A::mul(tmp, Am[moff + idx]);
+        const int pc = pd[1];
+        int idx = 0, sh = 0, bad = 0;
+        for (int q = 0; q < pc; ++q) {
+            const int pos = pd[2 + q];
+            idx |= ((x.rk >> (2 * pos)) & 3) << sh;
+            sh += (x.bits >> (2 * pos)) & 3;
+            bad |= (x.bad >> pos) & 1;
+        }
+        tmp = A::mul(tmp, bad ? T(0) : Am[off[po[j]] + idx]);
         pd += 2 + pc;
     }
     if (op.type == PARENT) {
@@ -213,15 +245,37 @@ __device__ T ls_term(const OpDev& op, const int32_t* opd, const T* Am, const T* 
     return tmp;
 }
 
-// A warp's shared bytes: the rfunctions [arena], the children's transmission
-// distributions [16 per child], the sampled states [N], the peel's draws [K]
-// (doubles), the locus's genotype codes and masks [N], its neighbours'
-// descent-graph words [2 W] and its prior row [16]; each part 16-byte aligned,
-// so every warp's base is aligned.
+// The L-sampler's compact rfunctions.  At locus l a member whose genotype-
+// elimination mask allows s states takes b = 0, 1 or 2 bits (s = 1, 2, 3-4)
+// of a cell's index, holding the rank of its state among the allowed ones, in
+// cutset order; op k's cells are the 2^B_k indices (B_k the sum of its
+// members' bits) at offset off[k] of the task's arena, a prefix sum over the
+// ops worked out at the start of each task.  Only cells whose members are all
+// in allowed states are stored -- on the 400-member pedigree at most 1,350
+// values against 11,485 for dense 4^c matrices -- and exactly those are the
+// cells the dense layout could hold non-zero: a gather that would reach a
+// dense cell with a disallowed state reads zero instead, and a rank past the
+// allowed count (s = 3) marks an invalid cell.
+__device__ __forceinline__ int rank_bits(int mask) {
+    const int s = __popc(mask);
+    return s <= 1 ? 0 : (s == 2 ? 1 : 2);
+}
+__device__ __forceinline__ int state_rank(int mask, int v) { return __popc(mask & ((1 << v) - 1)); }
+__device__ __forceinline__ int state_of_rank(int mask, int r) {   // the r-th allowed state (r < popc(mask))
+    for (int i = 0; i < r; ++i) mask &= mask - 1;
+    return __ffs(mask) - 1;
+}
+
+// A task's shared bytes: the rfunctions [ls_arena, compact], the children's
+// transmission distributions [16 per child], the sampled states [N], the
+// peel's draws [K] (doubles), the locus's genotype codes and masks [N], its
+// neighbours' descent-graph words [2 W], its prior row [16] and the ops'
+// compact offsets [K + 1]; each part 16-byte aligned, so every task's base
+// is aligned.
 __host__ __device__ __forceinline__ size_t al16(size_t x) { return (x + 15) & ~(size_t)15; }
 template <typename T>
 __host__ __device__ __forceinline__ size_t ls_draws_at(const ProblemDev& P) {
-    return al16((size_t)P.arena * sizeof(T) + (size_t)P.max_child * 16 * sizeof(T) + (size_t)P.N);
+    return al16((size_t)P.ls_arena * sizeof(T) + (size_t)P.max_child * 16 * sizeof(T) + (size_t)P.N);
 }
 template <typename T>
 __host__ __device__ __forceinline__ size_t ls_gcol_at(const ProblemDev& P) {
@@ -236,8 +290,12 @@ __host__ __device__ __forceinline__ size_t ls_pri_at(const ProblemDev& P) {
     return al16(ls_cols_at<T>(P) + 8 * (size_t)P.W);
 }
 template <typename T>
-__host__ __device__ __forceinline__ size_t ls_warp_bytes(const ProblemDev& P) {
+__host__ __device__ __forceinline__ size_t ls_off_at(const ProblemDev& P) {
     return al16(ls_pri_at<T>(P) + 16 * sizeof(T));
+}
+template <typename T>
+__host__ __device__ __forceinline__ size_t ls_warp_bytes(const ProblemDev& P) {
+    return al16(ls_off_at<T>(P) + 4 * ((size_t)P.K + 1));
 }
 
 // Block-shared copies of the peel's operations and their lists: every lane
@@ -271,26 +329,28 @@ __device__ __forceinline__ void ls_stage_tables(const ProblemDev& P, unsigned ch
 // sampler_rfunction.h:84-101).  Draws are taken at indices base, base + 1, ...
 // of the unit's stream.  Returns the number of draws used, or -1 when the
 // locus has likelihood 0; *logroot (lane 0) receives log of the peel's result.
-template <typename T>
+template <typename T, int G>
 __device__ int ls_locus(const ProblemDev& P, const OpDev* ops, const int32_t* opd, uint32_t* dg, int cr, int chain,
                         int l, bool hasL, bool hasR, const Draws& draws, int64_t unit, int64_t base,
                         unsigned char* wsmem, int lane, int* status, double* logroot) {
     using Ar = Ls<T>;
+    const Lanes<G> L;
     constexpr bool kRescale = sizeof(T) == 4;   // FP32: each rfunction scaled to a maximum of about 1
     T* A = (T*)wsmem;
-    T* dist = A + P.arena;
+    T* dist = A + P.ls_arena;
     int8_t* assign = (int8_t*)(dist + 16 * P.max_child);
+    int32_t* off = (int32_t*)(wsmem + ls_off_at<T>(P));
     double* sdraw = (double*)(wsmem + ls_draws_at<T>(P));
     uint32_t* colC = dg + ((size_t)chain * P.M + l) * P.W;
-    // the locus's inputs copied to the warp's shared memory first
+    // the locus's inputs copied to the task's shared memory first
     uint8_t* sg = (uint8_t*)(wsmem + ls_gcol_at<T>(P));
     uint32_t* sL = (uint32_t*)(wsmem + ls_cols_at<T>(P));
     uint32_t* sR = sL + P.W;
     T* spri = (T*)(wsmem + ls_pri_at<T>(P));
     {
         const uint8_t* gsrc = P.geno + (size_t)l * P.N;
-        for (int i = lane; i < P.N; i += 32) sg[i] = gsrc[i];
-        for (int w = lane; w < P.W; w += 32) {
+        for (int i = lane; i < P.N; i += G) sg[i] = gsrc[i];
+        for (int w = lane; w < P.W; w += G) {
             if (hasL) sL[w] = colC[w - P.W];
             if (hasR) sR[w] = colC[w + P.W];
         }
@@ -298,7 +358,7 @@ __device__ int ls_locus(const ProblemDev& P, const OpDev* ops, const int32_t* op
             if constexpr (sizeof(T) == 4) spri[lane] = (T)P.prior_f[(size_t)l * 16 + lane];
             else spri[lane] = (T)P.prior[(size_t)l * 16 + lane];
         }
-        __syncwarp();
+        L.sync();
     }
     const uint32_t* colL = hasL ? sL : nullptr;
     const uint32_t* colR = hasR ? sR : nullptr;
@@ -315,28 +375,90 @@ __device__ int ls_locus(const ProblemDev& P, const OpDev* ops, const int32_t* op
     const uint8_t* gcol = sg;
     const T* pri = spri;
     int scale = 0;
+    // the ops' compact offsets at this locus: each lane sums the cells of a
+    // run of ops, a scan over the group turns the sums into offsets
+    {
+        const int per = (P.K + G - 1) / G, k0 = min(P.K, lane * per), k1 = min(P.K, k0 + per);
+        int sum = 0;
+        for (int k = k0; k < k1; ++k) {
+            const OpDev& op = ops[k];
+            int b = 0;
+            for (int q = 0; q < op.c; ++q) b += rank_bits((gcol[opd[op.cut_at + q]] >> 4) & 15);
+            sum += 1 << b;
+        }
+        int incl = sum;
+        for (int dd = 1; dd < G; dd <<= 1) {
+            const int o = L.shfl_up(incl, dd);
+            if (lane >= dd) incl += o;
+        }
+        int run = incl - sum;
+        for (int k = k0; k < k1; ++k) {
+            const OpDev& op = ops[k];
+            int b = 0;
+            for (int q = 0; q < op.c; ++q) b += rank_bits((gcol[opd[op.cut_at + q]] >> 4) & 15);
+            off[k] = run;
+            run += 1 << b;
+        }
+        if (lane == G - 1) off[P.K] = incl;
+        L.sync();
+        if (off[P.K] > P.ls_arena) {   // cannot happen: the arena holds the most any locus needs
+            if (lane == 0) set_status(status, ST_ILLEGAL_DG);
+            return -1;
+        }
+    }
     // forward peel over the valid cells of every rfunction
     for (int k = 0; k < P.K; ++k) {
         const OpDev op = ops[k];
-        ls_dists<T>(P, op, opd, colL, colR, l, th, an, th2, an2, dist, lane);
-        __syncwarp();
-        const int ncell = 1 << (2 * op.c);
+        ls_dists<T, G>(P, op, opd, colL, colR, l, th, an, th2, an2, dist, lane);
+        L.sync();
         const int32_t* cut = opd + op.cut_at;
+        // the op's members: allowed states (4 bits each) and rank bits, the peel node last
+        unsigned long long mk = 0;
+        int bits = 0, B = 0;
+        for (int q = 0; q < op.c; ++q) {
+            const int m = (gcol[cut[q]] >> 4) & 15, b = rank_bits(m);
+            mk |= (unsigned long long)m << (4 * q);
+            bits |= b << (2 * q);
+            B += b;
+        }
+        const int mp = (gcol[op.peel] >> 4) & 15;
+        bits |= rank_bits(mp) << (2 * op.c);
+        const int ncell = 1 << B;
         const T* trait = pri + 4 * (gcol[op.peel] & 3);
-        T* out = A + op.mat_off;
+        T* out = A + off[k];
         T mx = T(0);
         // one (cell, state) term per lane, four lanes per cell; the cell's
         // total adds its terms in state order from zero, as the reference's
         // loop does (a skipped term is an exact zero)
         const int nitem = 4 * ncell, grp = lane & ~3, v = lane & 3;
         const T tv = trait[v];
-        for (int it0 = 0; it0 < nitem; it0 += 32) {
+        LsCell x;
+        x.bits = bits;
+        x.bad = ((mp >> v) & 1) ? 0 : 1 << op.c;
+        const int vrank = state_rank(mp, v);
+        for (int it0 = 0; it0 < nitem; it0 += G) {
             const int cell = (it0 + lane) >> 2;
             T term = T(0);
-            if (it0 + lane < nitem && tv != T(0) && ls_valid(cut, op.c, gcol, cell))
-                term = ls_term<T>(op, opd, A, dist, cell, v, tv);
-            const T t0 = __shfl_sync(FULLMASK, term, grp), t1 = __shfl_sync(FULLMASK, term, grp + 1);
-            const T t2 = __shfl_sync(FULLMASK, term, grp + 2), t3 = __shfl_sync(FULLMASK, term, grp + 3);
+            if (it0 + lane < nitem && tv != T(0)) {
+                // decode the compact index into states and ranks
+                int rem = cell, ext = 0, rk = 0;
+                bool ok = true;
+                for (int q = 0; q < op.c; ++q) {
+                    const int m = (int)(mk >> (4 * q)) & 15, b = (bits >> (2 * q)) & 3;
+                    const int r = rem & ((1 << b) - 1);
+                    rem >>= b;
+                    ok &= r < __popc(m);
+                    ext |= state_of_rank(m, r & 3) << (2 * q);
+                    rk |= r << (2 * q);
+                }
+                if (ok) {
+                    x.ext = ext | (v << (2 * op.c));
+                    x.rk = rk | (vrank << (2 * op.c));
+                    term = ls_term<T>(op, opd, A, off, dist, x, v, tv);
+                }
+            }
+            const T t0 = L.shfl(term, grp), t1 = L.shfl(term, grp + 1);
+            const T t2 = L.shfl(term, grp + 2), t3 = L.shfl(term, grp + 3);
             if (v == 0 && it0 + lane < nitem) {
                 const T total = Ar::add(Ar::add(Ar::add(Ar::add(T(0), t0), t1), t2), t3);
                 out[cell] = total;
@@ -346,8 +468,8 @@ __device__ int ls_locus(const ProblemDev& P, const OpDev* ops, const int32_t* op
         if (kRescale) {
             // the sampling draws from ratios within one rfunction, so a
             // power-of-two factor per rfunction changes no decision
-            for (int dd = 16; dd >= 1; dd >>= 1) {
-                const T o = __shfl_xor_sync(FULLMASK, mx, dd);
+            for (int dd = G / 2; dd >= 1; dd >>= 1) {
+                const T o = L.shfl_xor(mx, dd);
                 mx = o > mx ? o : mx;
             }
             if (mx > T(0)) {
@@ -356,43 +478,57 @@ __device__ int ls_locus(const ProblemDev& P, const OpDev* ops, const int32_t* op
                 const int ex = ilogbf((float)mx);
                 scale += ex;
                 const float f = scalbnf(1.0f, -ex);
-                for (int cell = lane; cell < ncell; cell += 32) out[cell] = (T)((float)out[cell] * f);
+                for (int cell = lane; cell < ncell; cell += G) out[cell] = (T)((float)out[cell] * f);
             }
         }
-        __syncwarp();
+        L.sync();
     }
-    const T root = A[ops[P.K - 1].mat_off];
+    const T root = A[off[P.K - 1]];
     if (root == T(0)) {
         if (lane == 0) set_status(status, ST_ZERO_LIK);
-        __syncwarp();
+        L.sync();
         return -1;
     }
     if (lane == 0 && logroot) *logroot = log((double)root) + (double)scale * 0.69314718055994530942;
-    for (int i = lane; i < P.N; i += 32) assign[i] = -1;
+    for (int i = lane; i < P.N; i += G) assign[i] = -1;
     // the backward pass's draws, one per operation, generated together
-    for (int j = lane; j < P.K; j += 32) sdraw[j] = draws.get(cr, chain, unit, base + j);
-    __syncwarp();
+    for (int j = lane; j < P.K; j += G) sdraw[j] = draws.get(cr, chain, unit, base + j);
+    L.sync();
     // backward sampling of ordered genotypes (SamplerRfunction::sample)
     for (int k = P.K - 1; k >= 0; --k) {
         const OpDev op = ops[k];
-        ls_dists<T>(P, op, opd, colL, colR, l, th, an, th2, an2, dist, lane);
-        __syncwarp();
+        ls_dists<T, G>(P, op, opd, colL, colR, l, th, an, th2, an2, dist, lane);
+        L.sync();
         const int32_t* cut = opd + op.cut_at;
         const T* trait = pri + 4 * (gcol[op.peel] & 3);
-        int cellidx = 0;
-        bool known = true;
+        // the sampled cutset states as a compact cell (invalid where a state
+        // is not allowed: the dense matrix held zero there)
+        int ext = 0, rk = 0, bits = 0;
+        bool known = true, ok = true;
         for (int q = 0; q < op.c; ++q) {
             const int a = assign[cut[q]];
+            const int m = (gcol[cut[q]] >> 4) & 15;
             known &= a >= 0;
-            cellidx |= (a & 3) << (2 * q);
+            ok &= ((m >> (a & 3)) & 1) != 0;
+            ext |= (a & 3) << (2 * q);
+            rk |= state_rank(m, a & 3) << (2 * q);
+            bits |= rank_bits(m) << (2 * q);
         }
+        const int mp = (gcol[op.peel] >> 4) & 15;
         T pv = T(0);
-        if (lane < 4 && known) {
+        if (lane < 4 && known && ok) {
             const T tv = trait[lane];
-            if (tv != T(0) && ls_valid(cut, op.c, gcol, cellidx)) pv = ls_term<T>(op, opd, A, dist, cellidx, lane, tv);
+            if (tv != T(0)) {
+                LsCell x;
+                x.ext = ext | (lane << (2 * op.c));
+                x.rk = rk | (state_rank(mp, lane) << (2 * op.c));
+                x.bits = bits | (rank_bits(mp) << (2 * op.c));
+                x.bad = ((mp >> lane) & 1) ? 0 : 1 << op.c;
+                pv = ls_term<T>(op, opd, A, off, dist, x, lane, tv);
+            }
         }
-        const T p0 = __shfl_sync(FULLMASK, pv, 0), p1 = __shfl_sync(FULLMASK, pv, 1);
-        const T p2 = __shfl_sync(FULLMASK, pv, 2), p3 = __shfl_sync(FULLMASK, pv, 3);
+        const T p0 = L.shfl(pv, 0), p1 = L.shfl(pv, 1);
+        const T p2 = L.shfl(pv, 2), p3 = L.shfl(pv, 3);
         if (lane == 0) {
             if (!known) set_status(status, ST_ILLEGAL_DG);
             T pd[4] = {p0, p1, p2, p3};
@@ -409,7 +545,7 @@ __device__ int ls_locus(const ProblemDev& P, const OpDev* ops, const int32_t* op
             }
             assign[op.peel] = (int8_t)(pick >= 0 ? pick : lastv);
         }
-        __syncwarp();
+        L.sync();
     }
     // meiosis indicators (locus_sampler2.cc:32-125) in person order, maternal
     // first: bit b = 2 (person - F) + parent, so 32 consecutive meioses are one
@@ -419,64 +555,70 @@ __device__ int ls_locus(const ProblemDev& P, const OpDev* ops, const int32_t* op
         int64_t cursor = base + P.K;
         const int nb = 2 * P.Nnf;
         for (int w = 0; w < P.W; ++w) {
-            const int b = 32 * w + lane;
-            int mi = 0, need = 0;
-            T p0 = T(1), p1 = T(1);
-            if (b < nb) {
-                const int i = P.F + (b >> 1), par = b & 1;
-                const int tr = assign[i];
-                const int ptr = assign[par == 0 ? P.mother[i] : P.father[i]];
-                const int allele = par == 0 ? ((tr == UU || tr == UA) ? 0 : 1) : ((tr == UU || tr == AU) ? 0 : 1);
-                if (ptr == UA || ptr == AU) {
-                    mi = allele == 0 ? (ptr == UA ? 0 : 1) : (ptr == UA ? 1 : 0);
-                } else {
-                    need = 1;
-                    if (hasL) {
-                        const int d = dgbit(colL, b);
-                        p0 = Ar::mul(p0, d == 0 ? an2 : th2);
-                        p1 = Ar::mul(p1, d == 1 ? an2 : th2);
-                    }
-                    if (hasR) {
-                        const int d = dgbit(colR, b);
-                        p0 = Ar::mul(p0, d == 0 ? an : th);
-                        p1 = Ar::mul(p1, d == 1 ? an : th);
+            uint32_t word = 0;
+            for (int h = 0; h < 32; h += G) {
+                const int b = 32 * w + h + lane;
+                int mi = 0, need = 0;
+                T p0 = T(1), p1 = T(1);
+                if (b < nb) {
+                    const int i = P.F + (b >> 1), par = b & 1;
+                    const int tr = assign[i];
+                    const int ptr = assign[par == 0 ? P.mother[i] : P.father[i]];
+                    const int allele = par == 0 ? ((tr == UU || tr == UA) ? 0 : 1) : ((tr == UU || tr == AU) ? 0 : 1);
+                    if (ptr == UA || ptr == AU) {
+                        mi = allele == 0 ? (ptr == UA ? 0 : 1) : (ptr == UA ? 1 : 0);
+                    } else {
+                        need = 1;
+                        if (hasL) {
+                            const int d = dgbit(colL, b);
+                            p0 = Ar::mul(p0, d == 0 ? an2 : th2);
+                            p1 = Ar::mul(p1, d == 1 ? an2 : th2);
+                        }
+                        if (hasR) {
+                            const int d = dgbit(colR, b);
+                            p0 = Ar::mul(p0, d == 0 ? an : th);
+                            p1 = Ar::mul(p1, d == 1 ? an : th);
+                        }
                     }
                 }
+                const unsigned nmask = L.ballot(need);
+                if (need) {
+                    const double r = draws.get(cr, chain, unit, cursor + __popc(nmask & ((1u << lane) - 1u)));
+                    mi = (r < (double)Ar::div(p0, Ar::add(p0, p1))) ? 0 : 1;
+                }
+                cursor += __popc(nmask);
+                word |= L.ballot(mi != 0) << h;
             }
-            const unsigned nmask = __ballot_sync(FULLMASK, need);
-            if (need) {
-                const double r = draws.get(cr, chain, unit, cursor + __popc(nmask & ((1u << lane) - 1u)));
-                mi = (r < (double)Ar::div(p0, Ar::add(p0, p1))) ? 0 : 1;
-            }
-            cursor += __popc(nmask);
-            const unsigned word = __ballot_sync(FULLMASK, mi != 0);
             if (lane == 0) colC[w] = word;   // bits past 2 Nnf stay zero
         }
-        __syncwarp();
+        L.sync();
         return (int)(cursor - base);
     }
 }
 
-// One warp per (chain, locus) task; the listed loci must be pairwise
-// non-adjacent so each task owns its descent-graph column.
-template <typename T>
+// One task per (chain, locus), G lanes each (a warp, or half of one); the
+// listed loci must be pairwise non-adjacent so each task owns its
+// descent-graph column.
+template <typename T, int G>
 __global__ void __launch_bounds__(128) lsampler_kernel(ProblemDev P, uint32_t* dg, int first, int nchain,
                                                        const int32_t* loci, int nloci, Draws draws,
                                                        const uint8_t* sel, int want, int* status) {
     extern __shared__ __align__(16) unsigned char smem[];
-    const int wpb = blockDim.x >> 5, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    constexpr int kPer = 32 / G;   // tasks per warp
+    const int tpb = (blockDim.x >> 5) * kPer, slot = (threadIdx.x >> 5) * kPer + ((threadIdx.x & 31) / G);
+    const int lane = threadIdx.x & (G - 1);
     const OpDev* ops;
     const int32_t* opd;
     ls_stage_tables(P, smem, ops, opd);
     __syncthreads();
-    unsigned char* wsmem = smem + ls_tables_bytes(P) + (size_t)warp * ls_warp_bytes<T>(P);
+    unsigned char* wsmem = smem + ls_tables_bytes(P) + (size_t)slot * ls_warp_bytes<T>(P);
     const int64_t ntask = (int64_t)nchain * nloci;
-    for (int64_t t = (int64_t)blockIdx.x * wpb + warp; t < ntask; t += (int64_t)gridDim.x * wpb) {
+    for (int64_t t = (int64_t)blockIdx.x * tpb + slot; t < ntask; t += (int64_t)gridDim.x * tpb) {
         const int cr = (int)(t / nloci);
         if (sel && sel[cr] != want) continue;
         const int l = loci[t % nloci];
-        ls_locus<T>(P, ops, opd, dg, cr, first + cr, l, l > 0, l < P.M - 1, draws, l, 0, wsmem, lane, status,
-                    nullptr);
+        ls_locus<T, G>(P, ops, opd, dg, cr, first + cr, l, l > 0, l < P.M - 1, draws, l, 0, wsmem, lane, status,
+                       nullptr);
     }
 }
 
@@ -514,7 +656,7 @@ __global__ void __launch_bounds__(128) si_kernel(ProblemDev P, uint32_t* dg, int
             const bool hasL = v > start && l > 0;
             const bool hasR = v > 0 && v <= start && l < M - 1;
             double lr = 0.0;
-            const int used = ls_locus<T>(P, ops, opd, dgq, cr, chain, l, hasL, hasR, dq, unit, base, wsmem, lane,
+            const int used = ls_locus<T, 32>(P, ops, opd, dgq, cr, chain, l, hasL, hasR, dq, unit, base, wsmem, lane,
                                          status, &lr);
             if (used < 0) {
                 ok = false;
@@ -1899,17 +2041,17 @@ __global__ void __launch_bounds__(128) lod_kernel(ProblemDev P, const uint32_t* 
                     mx = o2 > mx ? o2 : mx;
                 }
                 if (mx > (T)0) {
-                    int e;
-                    T f;
                     if constexpr (sizeof(T) == 8) {
-                        e = ilogb(mx);
-                        f = scalbn(1.0, -e);
+                        const int e = ilogb(mx);
+                        const T f = scalbn(1.0, -e);
+                        for (int cell = lane; cell < ncell; cell += 32) out[cell] *= f;
+                        scale += e;
                     } else {
-                        e = ilogbf(mx);
-                        f = scalbnf(1.0f, -e);
+                        // FP32: the largest cell to 2^scale_to (LI_SCALE, sl_internal.h)
+                        const int e = ilogbf(mx) - op.scale_to;
+                        for (int cell = lane; cell < ncell; cell += 32) out[cell] = ldexpf(out[cell], -e);
+                        scale += e;
                     }
-                    for (int cell = lane; cell < ncell; cell += 32) out[cell] *= f;
-                    scale += e;
                 }
                 __syncwarp();
             }
@@ -1988,14 +2130,14 @@ __global__ void __launch_bounds__(128) lod_prog_kernel(ProblemDev P, const uint3
                 A[dst * S] = v;
                 pc += 3 + ns;
             } else if (op == LI_SCALE) {
-                const int first = __ldg(pc + 1), cnt = __ldg(pc + 2);
-                pc += 3;
+                const int first = __ldg(pc + 1), cnt = __ldg(pc + 2), target = __ldg(pc + 3);
+                pc += 4;
                 float mx = 0.f;
                 for (int q = 0; q < cnt; ++q) mx = fmaxf(mx, A[(first + q) * S]);
                 if (mx > 0.f) {
-                    const int e = ilogbf(mx);
-                    const float f = scalbnf(1.0f, -e);
-                    for (int q = 0; q < cnt; ++q) A[(first + q) * S] *= f;
+                    // ldexpf: exact for any exponent, a subnormal maximum included
+                    const int e = ilogbf(mx) - target;
+                    for (int q = 0; q < cnt; ++q) A[(first + q) * S] = ldexpf(A[(first + q) * S], -e);
                     scale += e;
                 }
             } else {
@@ -2443,27 +2585,40 @@ size_t lsampler_smem_per_warp(const ProblemDev& P) {
 size_t lsampler_smem_shared(const ProblemDev& P) { return ls_tables_bytes(P); }
 
 
+template <typename T, int G>
+static cudaError_t launch_lsampler_g(const ProblemDev& P, uint32_t* dg, int first, int nchain, const int32_t* loci,
+                                     int nloci, const Draws& d, const uint8_t* sel, int want, int* status,
+                                     cudaStream_t s, int grid_cap, int wpb) {
+    const int tpb = wpb * (32 / G);
+    const size_t smem = ls_tables_bytes(P) + (size_t)tpb * ls_warp_bytes<T>(P);
+    {
+        cudaError_t e = ensure_smem((const void*)lsampler_kernel<T, G>, smem);
+        if (e != cudaSuccess) return e;
+    }
+    const int64_t ntask = (int64_t)nchain * nloci;
+    int64_t grid = (ntask + tpb - 1) / tpb;
+    if (grid > grid_cap) grid = grid_cap;
+    if (grid < 1) grid = 1;
+    lsampler_kernel<T, G><<<(int)grid, wpb * 32, smem, s>>>(P, dg, first, nchain, loci, nloci, d, sel, want, status);
+    return cudaGetLastError();
+}
+
+// lanes = 32 or 16 lanes per (chain, locus) task; both draw the same graphs.
 cudaError_t launch_lsampler(const ProblemDev& P, uint32_t* dg, int first, int nchain, const int32_t* loci, int nloci,
                             const double* u, int64_t ucs, int64_t uls, uint64_t seed, uint64_t iter,
                             const uint8_t* sel, int want, int* status, cudaStream_t s, int grid_cap, int wpb,
-                            const uint64_t* key) {
-    const size_t smem = ls_tables_bytes(P) + wpb * lsampler_smem_per_warp(P);
-    {
-        cudaError_t e = ensure_smem(P.ls_fast ? (const void*)lsampler_kernel<float> : (const void*)lsampler_kernel<double>, smem);
-        if (e != cudaSuccess) return e;
-    }
+                            const uint64_t* key, int lanes) {
     Draws d{u, ucs, uls, seed, iter, 1, key};
-    const int64_t ntask = (int64_t)nchain * nloci;
-    int64_t grid = (ntask + wpb - 1) / wpb;
-    if (grid > grid_cap) grid = grid_cap;
-    if (grid < 1) grid = 1;
+    if (lanes == 16) {
+        // two tasks per warp: half as many warps per block keeps the block's shared memory
+        const int w16 = wpb > 1 ? wpb / 2 : 1;
+        if (P.ls_fast) return launch_lsampler_g<float, 16>(P, dg, first, nchain, loci, nloci, d, sel, want, status, s,
+                                                           grid_cap, w16);
+        return launch_lsampler_g<double, 16>(P, dg, first, nchain, loci, nloci, d, sel, want, status, s, grid_cap, w16);
+    }
     if (P.ls_fast)
-        lsampler_kernel<float><<<(int)grid, wpb * 32, smem, s>>>(P, dg, first, nchain, loci, nloci, d, sel, want,
-                                                                 status);
-    else
-        lsampler_kernel<double><<<(int)grid, wpb * 32, smem, s>>>(P, dg, first, nchain, loci, nloci, d, sel, want,
-                                                                  status);
-    return cudaGetLastError();
+        return launch_lsampler_g<float, 32>(P, dg, first, nchain, loci, nloci, d, sel, want, status, s, grid_cap, wpb);
+    return launch_lsampler_g<double, 32>(P, dg, first, nchain, loci, nloci, d, sel, want, status, s, grid_cap, wpb);
 }
 
 // Keep each chain's best imputation: over the batch's passes in pass order,

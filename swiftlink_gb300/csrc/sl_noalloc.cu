@@ -10,9 +10,11 @@
 // library until the process exits.  Host code must not hand the array's name
 // to a kernel (on the host it is only a stand-in for the device symbol): the
 // device address is looked up with cudaGetSymbolAddress once per device, on
-// the first call made with that device current.  Every call overwrites the
-// whole region it uses before reading it, so nothing needs clearing; calls
-// that overlap on the GPU share the array and race.
+// the first call made with that device current; the caller's current device
+// is restored before the call returns.  Every call overwrites the whole
+// region it uses before reading it, so nothing needs clearing; calls that
+// overlap on the GPU share the array and race.  The scores come from the
+// kernel the context scores with (sl_lod_score_graphs).
 
 #include <cuda_runtime.h>
 #include <float.h>
@@ -24,8 +26,7 @@
 namespace sl {
 int ctx_view(sl_ctx* ctx, CtxView* v);
 void ctx_fail(sl_ctx* ctx, int code, const char* msg);
-cudaError_t launch_lod(const ProblemDev& P, int precision, const uint32_t* graphs, int64_t graph_words, int G,
-                       double* vals, int* status, cudaStream_t s, int grid_cap, int wpb);
+cudaError_t ctx_launch_lod(sl_ctx* ctx, const uint32_t* graphs, int G, double* vals);
 cudaError_t launch_lod_merge(const double* vals, int G, int64_t npos, double* acc, uint8_t* init, cudaStream_t s);
 }  // namespace sl
 
@@ -37,12 +38,12 @@ const int kMaxDevices = 64;
 std::mutex g_lock;
 double* g_scratch_addr[kMaxDevices] = {nullptr};
 
-// Device address of the scratch array on `device`, looked up once per device.
+// Device address of the scratch array on `device`, looked up once per device
+// (the caller has made `device` current).
 int scratch_for(int device, double** out) {
     if (device < 0 || device >= kMaxDevices) return SL_EINVAL;
     std::lock_guard<std::mutex> guard(g_lock);
     if (!g_scratch_addr[device]) {
-        if (cudaSetDevice(device) != cudaSuccess) return SL_ECUDA;
         void* ptr = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&ptr, g_lod_scratch);
         if (e != cudaSuccess || !ptr) return SL_ECUDA;
@@ -51,6 +52,20 @@ int scratch_for(int device, double** out) {
     *out = g_scratch_addr[device];
     return SL_OK;
 }
+
+// Makes the context's device current for the call and gives the caller's
+// thread its own current device back on return.
+struct DeviceGuard {
+    int prev = -1;
+    bool ok = false;
+    explicit DeviceGuard(int device) {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        ok = cudaSetDevice(device) == cudaSuccess;
+    }
+    ~DeviceGuard() {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+};
 }  // namespace
 
 extern "C" int sl_lod_score_device_graphs_noalloc(sl_ctx* ctx, int32_t n_graphs, const uint32_t* d_graphs,
@@ -69,7 +84,8 @@ extern "C" int sl_lod_score_device_graphs_noalloc(sl_ctx* ctx, int32_t n_graphs,
                  "(1048576 values); score fewer graphs per call");
         return SL_EINVAL;
     }
-    if (cudaSetDevice(v.device) != cudaSuccess) {
+    DeviceGuard dev(v.device);
+    if (!dev.ok) {
         ctx_fail(ctx, SL_ECUDA, "noalloc LOD scoring: cudaSetDevice failed");
         return SL_ECUDA;
     }
@@ -80,8 +96,7 @@ extern "C" int sl_lod_score_device_graphs_noalloc(sl_ctx* ctx, int32_t n_graphs,
         return rc;
     }
     cudaStream_t s = (cudaStream_t)v.stream;
-    cudaError_t e = launch_lod(v.P, v.lod_precision, d_graphs, (int64_t)v.P.M * v.P.W, n_graphs, scratch,
-                               v.d_status, s, v.lod_grid, v.lod_wpb);
+    cudaError_t e = ctx_launch_lod(ctx, d_graphs, n_graphs, scratch);
     if (e == cudaSuccess) e = launch_lod_merge(scratch, n_graphs, npos, d_logsum, nullptr, s);
     if (e != cudaSuccess) {
         ctx_fail(ctx, SL_ECUDA, cudaGetErrorString(e));

@@ -242,49 +242,138 @@ def test_rejects_interfering_loci():
         assert e.value.code == api.SL_EINVAL
 
 
-def test_fast_msampler_agrees_with_exact():
-    """The FP32 filter draws the same meiosis indicators as the exact FP64
-    filter except at near-ties; over a full cfg1 sweep the graphs agree in
-    at least 99.9% of bits (usually all)."""
-    g = load_golden("cfg1")
-    order = g["msweep_order"]
-    out = {}
-    for prec in (api.SL_SAMPLER_EXACT, api.SL_SAMPLER_FAST):
-        with api.Context(api.Problem.from_arrays(g), n_chains=1, sampler_precision=prec) as ctx:
-            ctx.set_graphs(g["lsweep_after"])
-            ctx.msampler_sweep(order, g["msweep_u"][None])
-            out[prec] = ctx.get_graphs()[0]
-    assert np.array_equal(out[api.SL_SAMPLER_EXACT], g["msweep_after"])
-    agree = float((out[api.SL_SAMPLER_FAST] == out[api.SL_SAMPLER_EXACT]).mean())
-    print(f"fast/exact M-sweep bit agreement {agree:.6f}")
-    assert agree >= 0.999
+# The fast (FP32) samplers round differently from the reference's FP64
+# arithmetic, so a draw that falls within rounding distance of a decision
+# boundary may go the other way.  The stated bound: a fast decision may differ
+# from the exact one only where the exact draw lies within DECISION_MARGIN of
+# its boundary (the FP32 sampling probabilities are within about 1e-6 of the
+# FP64 ones; the M-sampler's scan compounds that along the map).
+DECISION_MARGIN = 1e-4
+
+
+def _seeded(name):
+    if name == "cfg1":
+        g = load_golden("cfg1")
+        return g, g["lsweep_after"]
+    from swiftlink_gb300.workloads import load_problem
+    g = load_problem("cfg2")
+    return g, g["dg0"]
 
 
 @pytest.mark.parametrize("name", ["cfg1", "cfg2"])
-def test_fast_lsampler_agrees_with_exact(name):
-    """The FP32 L-sampler (every rfunction rescaled by a power of two) samples
-    the same ordered genotypes and meiosis indicators as the exact FP64 one
-    except at near-ties: one even-then-odd sweep with the same uniforms
-    leaves at least 99.9% of the indicator bits equal."""
-    if name == "cfg1":
-        g = load_golden("cfg1")
-        start, u = g["lsweep_after"], g["lsweep_u"]
-    else:
-        from swiftlink_gb300.workloads import load_problem
-        g = load_problem("cfg2")
-        start = g["dg0"]
-        u = np.random.default_rng(17).random((g["M"], g["K"] + 2 * g["N"]))
-    out = {}
-    for prec in (api.SL_SAMPLER_EXACT, api.SL_SAMPLER_FAST):
-        with api.Context(api.Problem.from_arrays(g), n_chains=1, sampler_precision=prec) as ctx:
-            ctx.set_graphs(start)
-            ctx.lsampler_sweep(u[None])
-            out[prec] = ctx.get_graphs()[0]
-    F = g["F"]
-    a, b = out[api.SL_SAMPLER_FAST][:, F:], out[api.SL_SAMPLER_EXACT][:, F:]
-    agree = float((a == b).mean())
-    print(f"fast/exact L-sweep bit agreement on {name}: {agree:.6f}")
-    assert agree >= 0.999
+def test_fast_lsampler_decisions_match_exact(name):
+    """Decision level, L-sampler (sampler_rfunction.cc:159-188,
+    locus_sampler2.cc:44-65): over 10 sweeps, every half-sweep is run from the
+    same graph in both modes with the same uniforms; each locus's new column
+    (its meiosis indicators) must be equal in the two modes, or the exact
+    step must have met a draw within DECISION_MARGIN of a cumulative boundary
+    (the smallest such distance of the step, from the C restatement)."""
+    g, state = _seeded(name)
+    M, st = g["M"], stride_of(g)
+    rng = np.random.default_rng(71)
+    steps = differ = 0
+    prob = api.Problem.from_arrays(g, with_legal=False)
+    with api.Context(prob, n_chains=1) as ex, \
+            api.Context(prob, n_chains=1, sampler_precision=api.SL_SAMPLER_FAST) as fa:
+        g = dict(g, legal=ex.legal_masks(), trait_prior=ex.trait_priors())
+        P = port.Port(g)
+        state = np.ascontiguousarray(state, np.int32)
+        for sweep in range(10):
+            for parity in (0, 1):
+                loci = np.arange(parity, M, 2, dtype=np.int32)
+                u = rng.random((1, M, st))
+                out = {}
+                for mode, ctx in (("exact", ex), ("fast", fa)):
+                    ctx.set_graphs(state[None])
+                    ctx.lsampler_loci(loci, u)
+                    out[mode] = ctx.get_graphs()[0]
+                bad = [int(l) for l in loci if not np.array_equal(out["exact"][l], out["fast"][l])]
+                for l in bad:
+                    port.margin_reset()
+                    P.lstep(state, l, u[0, l])
+                    m = port.margin()
+                    assert m < DECISION_MARGIN, f"sweep {sweep} locus {l}: columns differ, smallest margin {m:.3g}"
+                steps += loci.size
+                differ += len(bad)
+                state = out["exact"]
+    print(f"{name}: {differ} of {steps} fast L-steps differ from exact, each at a near-tie")
+    assert differ <= steps // 100
+
+
+@pytest.mark.parametrize("name", ["cfg1", "cfg2"])
+def test_fast_msampler_decisions_match_exact(name):
+    """Decision level, M-sampler (meiosis_sampler.cc:157-203): 40 meiosis
+    steps (reset and step at one meiosis, the FP64 filter against the FP32
+    founder-allele likelihoods and scan), each from the same graph with the
+    same uniforms in both modes.  Backward sampling runs from the last locus
+    down, so the first locus (from the top) where the two rows differ is
+    where the decisions parted: the exact draw there must lie within
+    DECISION_MARGIN of its threshold."""
+    g, state = _seeded(name)
+    M, F = g["M"], g["F"]
+    rng = np.random.default_rng(72)
+    prob = api.Problem.from_arrays(g, with_legal=False)
+    differ = 0
+    with api.Context(prob, n_chains=1) as ex, \
+            api.Context(prob, n_chains=1, sampler_precision=api.SL_SAMPLER_FAST) as fa:
+        g = dict(g, legal=ex.legal_masks(), trait_prior=ex.trait_priors())
+        P = port.Port(g)
+        state = np.ascontiguousarray(state, np.int32)
+        meioses = rng.permutation(g["meioses"])[:40]
+        for m in meioses:
+            u = rng.random((1, 1, M))
+            out = {}
+            for mode, ctx in (("exact", ex), ("fast", fa)):
+                ctx.set_graphs(state[None])
+                ctx.msampler_sweep([int(m)], u)
+                out[mode] = ctx.get_graphs()[0]
+            want, margins = port.msweep_margins(P, state, int(m), u[0, 0])
+            assert np.array_equal(out["exact"], want)
+            person, par = F + int(m) // 2, int(m) % 2
+            rows = out["exact"][:, person, par], out["fast"][:, person, par]
+            diff = np.nonzero(rows[0] != rows[1])[0]
+            assert np.array_equal(np.delete(out["exact"], person, axis=1), np.delete(out["fast"], person, axis=1))
+            if diff.size:
+                top = int(diff.max())
+                assert margins[top] < DECISION_MARGIN, f"meiosis {m}: rows part at locus {top}, margin {margins[top]:.3g}"
+                differ += 1
+            state = out["exact"]
+    print(f"{name}: {differ} of {meioses.size} fast M-steps differ from exact, each from a near-tie")
+    assert differ <= meioses.size // 4
+
+
+def test_fast_and_exact_long_runs_agree_within_monte_carlo_error():
+    """Long runs on the 30-member pedigree: 8 chains x 10 segments of 1,000
+    iterations, scoring every 10th graph, in the exact mode (FP64 samplers and
+    LOD) and in the fast mode (FP32 samplers, FP32-rescaled LOD), from the same
+    seeds.  Each segment's LOD table is an estimate; the two modes' mean tables
+    must agree within 5 combined standard errors at every position (the
+    segments' spread gives the errors)."""
+    g = load_golden("cfg1")
+    C, segs, seg_it = 8, 10, 1000
+    tables = {}
+    for mode, kw in (("exact", {}), ("fast", dict(sampler_precision=api.SL_SAMPLER_FAST,
+                                                  lod_precision=api.SL_LOD_FP32_RESCALED))):
+        est = []
+        with api.Context(api.Problem.from_arrays(g), n_chains=C, **kw) as ctx:
+            ctx.set_graphs(np.stack([g["lsweep_after"]] * C))
+            ctx.run(iterations=seg_it, burnin=0, period=10, lprob=0.5, seed=99)   # burn-in
+            ctx.lod_reset()
+            for s in range(segs):
+                ctx.run(iterations=(s + 2) * seg_it, burnin=0, period=10, lprob=0.5, seed=99,
+                        first_iteration=(s + 1) * seg_it)
+                raw, cnt, tp = ctx.lod_results()
+                assert cnt == C * seg_it // 10
+                est.append(api.lod_table(raw, cnt, tp))
+                ctx.lod_reset()
+        tables[mode] = np.array(est)
+    mean = {k: v.mean(0) for k, v in tables.items()}
+    se = {k: v.std(0, ddof=1) / np.sqrt(segs) for k, v in tables.items()}
+    comb = np.sqrt(se["exact"] ** 2 + se["fast"] ** 2)
+    z = np.abs(mean["exact"] - mean["fast"]) / np.maximum(comb, 1e-6)
+    print(f"max |mean dLOD| {np.abs(mean['exact'] - mean['fast']).max():.4f}, max z {z.max():.2f}, "
+          f"median SE {np.median(comb):.4f}")
+    assert z.max() <= 5.0
 
 
 LOD_KERNELS = [api.SL_LOD_KERNEL_INTERP, api.SL_LOD_KERNEL_JIT_REG, api.SL_LOD_KERNEL_JIT_SMEM,
@@ -413,18 +502,41 @@ def test_specialised_lsampler_is_bit_identical(name):
     C = 3
     u = np.random.default_rng(23).random((C, g["M"], g["K"] + 2 * g["N"]))
     out = {}
-    for lk in (api.SL_LS_KERNEL_GENERIC, api.SL_LS_KERNEL_SPECIALISED):
+    for lk in LS_FORMS:
         with api.Context(api.Problem.from_arrays(g), n_chains=C, sampler_precision=api.SL_SAMPLER_FAST,
                          ls_kernel=lk) as ctx:
-            assert ctx.ls_kernel_info()[0] == lk
+            assert ctx.ls_kernel_info()[0] == (lk if lk == api.SL_LS_KERNEL_SPECIALISED else api.SL_LS_KERNEL_GENERIC)
             ctx.set_graphs(np.stack([g["dg0"]] * C))
             ctx.lsampler_sweep(u, 0, C)
             swept = ctx.get_graphs()
             ctx.run(iterations=12, burnin=0, period=4, lprob=1.0, seed=9)
             out[lk] = (swept, ctx.get_graphs())
-    a, b = out[api.SL_LS_KERNEL_GENERIC], out[api.SL_LS_KERNEL_SPECIALISED]
-    assert np.array_equal(a[0], b[0])
-    assert np.array_equal(a[1], b[1])
+    b = out[api.SL_LS_KERNEL_SPECIALISED]
+    for lk in LS_FORMS:
+        assert np.array_equal(out[lk][0], b[0]), lk
+        assert np.array_equal(out[lk][1], b[1]), lk
+
+
+# the L-sampler's forms: generic with lanes per task by timing, forced to 32
+# or 16 lanes (two tasks per warp), and the kernel specialised to the pedigree
+LS_FORMS = (api.SL_LS_KERNEL_GENERIC, api.SL_LS_KERNEL_GENERIC32, api.SL_LS_KERNEL_GENERIC16,
+            api.SL_LS_KERNEL_SPECIALISED)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("lanes", [api.SL_LS_KERNEL_GENERIC32, api.SL_LS_KERNEL_GENERIC16])
+@pytest.mark.parametrize("name", CASES)
+def test_lsweep_bit_exact_both_lane_groups(name, lanes):
+    """Exact mode with 32 and with 16 lanes per (chain, locus) task: the
+    reference's L-sweep bit for bit (two chains, so a warp holds both tasks
+    of the 16-lane form)."""
+    g = load_golden(name)
+    with api.Context(api.Problem.from_arrays(g), n_chains=2, ls_kernel=lanes) as ctx:
+        ctx.set_graphs(np.stack([g["dg0"]] * 2))
+        ctx.lsampler_sweep(np.stack([g["lsweep_u"]] * 2), 0, 2)
+        out = ctx.get_graphs()
+    assert np.array_equal(out[0], g["lsweep_after"])
+    assert np.array_equal(out[1], g["lsweep_after"])
 
 
 @pytest.mark.gpu
@@ -439,11 +551,11 @@ def test_specialised_lsampler_shared_shapes_is_bit_identical():
     assert d["K"] > 150
     C = 4
     out = {}
-    for lk in (api.SL_LS_KERNEL_GENERIC, api.SL_LS_KERNEL_SPECIALISED):
+    for lk in LS_FORMS:
         with api.Context(api.Problem.from_arrays(d, with_legal=False), n_chains=C,
                          sampler_precision=api.SL_SAMPLER_FAST, ls_kernel=lk) as ctx:
-            assert ctx.ls_kernel_info()[0] == lk
             ctx.set_graphs(np.stack([d["dg0"]] * C))
             ctx.run(iterations=8, burnin=0, period=4, lprob=1.0, seed=5)
             out[lk] = ctx.get_graphs()
-    assert np.array_equal(out[api.SL_LS_KERNEL_GENERIC], out[api.SL_LS_KERNEL_SPECIALISED])
+    for lk in LS_FORMS:
+        assert np.array_equal(out[lk], out[api.SL_LS_KERNEL_SPECIALISED]), lk

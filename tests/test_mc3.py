@@ -136,10 +136,17 @@ def replay_mc3(g, temps, dg0, seed, iters, lprob, period, burnin, exchange):
     return dgs, scored, swaps
 
 
+# near-equal temperatures: the exchange ratio is close to 0, so most
+# proposed exchanges must be accepted (and are checked one by one)
+CLOSE_TEMPS = [1.0, 0.9995, 0.999]
+
+
 @pytest.mark.gpu
+@pytest.mark.parametrize("temps", [TEMPS, CLOSE_TEMPS], ids=["spread", "close"])
 @pytest.mark.parametrize("name", ["loop", "cfg1"])
-def test_mc3_run_matches_host_replay(name):
+def test_mc3_run_matches_host_replay(name, temps):
     g = load_golden(name)
+    TEMPS = temps
     C, seed, iters, burnin, period, exchange = len(TEMPS), 77, 8, 2, 2, 2
     with api.Context(api.Problem.from_arrays(g), n_chains=C) as ctx:
         ctx.set_temperatures(TEMPS)
@@ -156,6 +163,8 @@ def test_mc3_run_matches_host_replay(name):
     want_acc = np.bincount([r for r, a in swaps if a], minlength=C - 1)
     np.testing.assert_array_equal(prop, want_prop)
     np.testing.assert_array_equal(acc, want_acc)
+    if temps is CLOSE_TEMPS:
+        assert acc.sum() >= prop.sum() // 2 and acc.sum() > 0, (acc, prop)
     P = port.Port(g)
     ref_raw, ref_cnt, ref_tp = P.lod(np.stack(scored))
     assert cnt == ref_cnt

@@ -6,8 +6,8 @@ loop where an allocation's device-wide synchronisation would stall other
 streams); its scratch is a fixed device array inside the library.  This test
 scores two batches in a row through it, from device buffers the test itself
 allocates, and checks the accumulated LOD table after each call against
-sl_lod_score_graphs on the same graphs, within the FP64 LOD tolerance used by
-the other parity tests.  It lives in its own file, collected last.
+sl_lod_score_graphs on the same graphs, in each LOD form, within the LOD
+tolerances used by the other parity tests.  It lives in its own file, collected last.
 """
 import ctypes
 import sys
@@ -21,6 +21,7 @@ from swiftlink_gb300 import api
 pytestmark = pytest.mark.gpu
 
 FP64_LOD_TOL = 1e-10
+FP32_LOD_TOL = 1e-3
 LOG_ZERO = -sys.float_info.max
 
 
@@ -41,7 +42,14 @@ def pack(graphs, N, F, M):
     return out.astype(np.uint32)
 
 
-def test_noalloc_lod_matches_regular_entry_point_on_two_calls():
+@pytest.mark.parametrize("precision,tol", [(api.SL_LOD_FP64, FP64_LOD_TOL),
+                                           (api.SL_LOD_FP64_RESCALED, FP64_LOD_TOL),
+                                           (api.SL_LOD_FP32_RESCALED, FP32_LOD_TOL)])
+def test_noalloc_lod_matches_regular_entry_point_on_two_calls(precision, tol):
+    """In each LOD form -- the plain FP64 peel, the FP64 peel with rescaling,
+    and the batched FP32-rescaled peel (within the FP32 tolerance: the two
+    contexts may score with different FP32 kernels) -- and on two calls in a
+    row, so the second call starts from the first one's leftover scratch."""
     torch = pytest.importorskip("torch")
     g = load_golden("cfg1")
     N, F, M, n = g["N"], g["F"], g["M"], g["n_lod"]
@@ -49,8 +57,8 @@ def test_noalloc_lod_matches_regular_entry_point_on_two_calls():
     batches = [graphs[:2], graphs[2:]]
     fn = api.lib().sl_lod_score_device_graphs_noalloc
     fn.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p]
-    with api.Context(api.Problem.from_arrays(g), n_chains=1) as ref_ctx, \
-            api.Context(api.Problem.from_arrays(g), n_chains=1) as ctx:
+    with api.Context(api.Problem.from_arrays(g), n_chains=1, lod_precision=precision) as ref_ctx, \
+            api.Context(api.Problem.from_arrays(g), n_chains=1, lod_precision=precision) as ctx:
         acc = torch.full(((M - 1) * n,), LOG_ZERO, dtype=torch.float64, device="cuda")
         count = 0
         for batch in batches:
@@ -65,7 +73,8 @@ def test_noalloc_lod_matches_regular_entry_point_on_two_calls():
             got_raw = acc.cpu().numpy()
             assert count == want_count
             err = np.abs(api.lod_table(got_raw, count, tp) - api.lod_table(want_raw, want_count, tp)).max()
-            assert err <= FP64_LOD_TOL, err
+            assert err <= tol, err
+            assert torch.cuda.current_device() == 0
 
 
 def test_noalloc_rejects_batches_beyond_the_scratch_array():
