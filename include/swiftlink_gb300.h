@@ -361,9 +361,25 @@ int sl_lod_score_device_graphs_noalloc(sl_ctx* ctx, int32_t n_graphs, const uint
  * ptrait_grad[4] (may be NULL) receives d log P(T) / d (penetrances, frequency)
  * (Peeler::calc_trait_prob, peeler.cc:65-73).  Needs the disease-model fields
  * of the problem.  The peel is recomputed on the device in FP32 with
- * power-of-two rescaling; every forward value is kept for the reverse pass.
+ * power-of-two rescaling, one warp per (graph, interval, position) with the
+ * rfunctions in shared memory (sl_adjoint_memory: kept, or recomputed when
+ * they do not fit).
  */
 int sl_trait_backward(sl_ctx* ctx, int32_t n_graphs, const int32_t* dgs, double* grad, double* ptrait_grad);
+
+/*
+ * The adjoint's working memory.  Each task (graph, interval, position) keeps
+ * the peel's rfunctions and their adjoints in its warp's shared memory.  When
+ * every rfunction and its adjoint fit bytes_per_task (0: 32 KB), all are kept
+ * from the forward pass (one segment); otherwise the peel operations are
+ * split into segments, only rfunctions that a later segment reads are kept,
+ * and each earlier segment's other rfunctions are recomputed from those
+ * before its reverse pass -- forward cutsets recomputed instead of stored,
+ * at the cost of one more forward pass.  The plan used: *segments (1 =
+ * everything stored) and *used_bytes per task (either may be NULL).  Results
+ * agree between plans within FP32 rounding.
+ */
+int sl_adjoint_memory(sl_ctx* ctx, int64_t bytes_per_task, int32_t* segments, int64_t* used_bytes);
 
 /* The same adjoint for one graph and position evaluated on the host in FP64
  * (the reference gradient the device result is checked against); dg NULL

@@ -33,7 +33,7 @@ EXPORTED = [
     "sl_problem_trait_priors", "sl_problem_trait_prob", "sl_trait_backward",
     "sl_problem_trait_backward_eval", "sl_lod_kernel_info", "sl_ls_kernel_info", "sl_set_temperatures", "sl_mc3_stats",
     "sl_chain_loglik", "sl_peel_sequence", "sl_batch_create", "sl_batch_run", "sl_batch_destroy",
-    "sl_sequential_imputation", "sl_sequential_imputation_run",
+    "sl_sequential_imputation", "sl_sequential_imputation_run", "sl_adjoint_memory",
 ]
 
 
@@ -249,9 +249,15 @@ class Context:
         dgs = np.ascontiguousarray(dgs, np.int32).reshape(-1, self.M, self.N, 2)
         self._check(lib().sl_set_descent_graphs(self.h, first, dgs.shape[0], _p(dgs)))
 
-    def get_graphs(self, first: int = 0, n: Optional[int] = None) -> np.ndarray:
+    def get_graphs(self, first: int = 0, n: Optional[int] = None, out: Optional[np.ndarray] = None) -> np.ndarray:
+        """Graphs of chains [first, first + n) in the reference's int32 layout,
+        into `out` when given (C-contiguous int32 [n][M][N][2])."""
+        if out is not None:
+            assert out.dtype == np.int32 and out.flags.c_contiguous
+            n = out.size // (self.M * self.N * 2)
         n = self.n_chains - first if n is None else n
-        out = np.zeros((n, self.M, self.N, 2), np.int32)
+        if out is None:
+            out = np.empty((n, self.M, self.N, 2), np.int32)
         self._check(lib().sl_get_descent_graphs(self.h, first, n, _p(out)))
         return out
 
@@ -321,6 +327,16 @@ class Context:
         ms = ctypes.c_double()
         self._check(lib().sl_lod_kernel_info(self.h, ctypes.byref(k), ctypes.byref(ms)))
         return k.value, ms.value
+
+    def adjoint_memory(self, bytes_per_task: int = 0):
+        """Plan the trait-peel adjoint within bytes_per_task of shared memory
+        per task (0: the default); returns (segments, bytes used per task):
+        one segment keeps every rfunction, more recompute them."""
+        seg = ctypes.c_int32()
+        used = ctypes.c_int64()
+        self._check(lib().sl_adjoint_memory(self.h, ctypes.c_int64(bytes_per_task), ctypes.byref(seg),
+                                            ctypes.byref(used)))
+        return seg.value, used.value
 
     def trait_backward(self, dgs: Optional[np.ndarray] = None):
         """d log L / d (theta_L, theta_R, pen x3, frequency) at every LOD

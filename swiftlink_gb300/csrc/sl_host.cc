@@ -63,8 +63,7 @@ cudaError_t launch_lod(const ProblemDev& P, int precision, const uint32_t* graph
                        double* vals, int* status, cudaStream_t s, int grid_cap, int wpb);
 cudaError_t launch_lod_merge(const double* vals, int G, int64_t npos, double* acc, uint8_t* init, cudaStream_t s);
 cudaError_t launch_trait_adjoint(const ProblemDev& P, const AdjDev& D, const uint32_t* graphs, int64_t graph_words,
-                                 int64_t task0, int64_t ntask, int64_t stride, float* A, float* B, int* E,
-                                 double* grad, int* status, cudaStream_t s);
+                                 int64_t task0, int64_t ntask, double* grad, int* status, cudaStream_t s, int sms);
 cudaError_t launch_shuffle(const int32_t* base, int nm, int32_t* out, int first, int nchain, uint64_t seed,
                            uint64_t iter, cudaStream_t s);
 cudaError_t launch_choose(int first, int nchain, uint64_t seed, uint64_t iter, double lprob, uint8_t* is_l,
@@ -152,9 +151,10 @@ struct sl_ctx {
     // trait-peel adjoint (present when the problem carries the disease model)
     bool has_adjoint = false;
     AdjDev adj{};
-    float* d_adjA = nullptr;         // [slots][chunk] forward values
-    float* d_adjB = nullptr;         // [slots][chunk] adjoints
-    int* d_adjE = nullptr;           // [nscale][chunk] rescaling exponents
+    std::vector<OpDev> adj_ops;       // host copies the plan is built from
+    std::vector<int32_t> adj_prev;    // [K+1] CSR offsets and the previous ops, for the plan's consumers
+    std::vector<int32_t> adj_prevs;
+    size_t adj_budget = 0;            // shared bytes per warp the plan must fit (0: the default)
     double* d_adjG = nullptr;        // [chunk][6] gradients
     int64_t adj_chunk = 0;
     // batched LOD kernel: the interpreter, or a problem-specialised form
@@ -601,30 +601,61 @@ static double host_trait_prob(const sl_problem_desc* d, const std::vector<OpDev>
     return std::log(A[ops.back().mat_off]);
 }
 
-static void pack_graph(const int32_t* src, int N, int F, int M, int W, uint32_t* dst) {
-    std::memset(dst, 0, sizeof(uint32_t) * (size_t)M * W);
-    for (int l = 0; l < M; ++l) {
-        const int32_t* col = src + (size_t)2 * N * l;
-        uint32_t* out = dst + (size_t)l * W;
-        for (int i = F; i < N; ++i)
-            for (int par = 0; par < 2; ++par) {
-                const int b = 2 * (i - F) + par;
-                if (col[2 * i + par] & 1) out[b >> 5] |= 1u << (b & 31);
-            }
+// The reference's int32 [locus][person][2] graphs <-> the device's packed
+// columns: a column's non-founder indicators are the 2 Nnf consecutive int32
+// values from offset 2F, so each 32-bit word packs 32 of them in order.
+static void pack_columns(const int32_t* src, int N, int F, int W, uint32_t* dst, size_t c0, size_t c1) {
+    const int nb = 2 * (N - F);
+    for (size_t c = c0; c < c1; ++c) {
+        const int32_t* bits = src + (size_t)2 * N * c + 2 * F;
+        uint32_t* out = dst + c * W;
+        for (int w = 0; w < W; ++w) {
+            const int b0 = 32 * w, nbit = std::min(32, nb - b0);
+            uint32_t x = 0;
+            for (int k = 0; k < nbit; ++k) x |= (uint32_t)(bits[b0 + k] & 1) << k;
+            out[w] = x;
+        }
     }
 }
 
-static void unpack_graph(const uint32_t* src, int N, int F, int M, int W, int32_t* dst) {
-    std::memset(dst, 0, sizeof(int32_t) * (size_t)2 * N * M);
-    for (int l = 0; l < M; ++l) {
-        const uint32_t* col = src + (size_t)l * W;
-        int32_t* out = dst + (size_t)2 * N * l;
-        for (int i = F; i < N; ++i)
-            for (int par = 0; par < 2; ++par) {
-                const int b = 2 * (i - F) + par;
-                out[2 * i + par] = (col[b >> 5] >> (b & 31)) & 1;
-            }
+static void unpack_columns(const uint32_t* src, int N, int F, int W, int32_t* dst, size_t c0, size_t c1) {
+    const int nb = 2 * (N - F);
+    for (size_t c = c0; c < c1; ++c) {
+        int32_t* col = dst + (size_t)2 * N * c;
+        std::memset(col, 0, sizeof(int32_t) * 2 * F);
+        const uint32_t* in = src + c * W;
+        for (int b = 0; b < nb; ++b) col[2 * F + b] = (in[b >> 5] >> (b & 31)) & 1;
     }
+}
+
+// Runs f(c0, c1) over [0, n) columns, split across host threads when the
+// graphs are large (hundreds of megabytes for 32 chains of a 400-member,
+// 10,000-marker pedigree in the reference's layout).
+template <typename Fn>
+static void for_columns(size_t n, size_t bytes, Fn f) {
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const unsigned nt = bytes < (size_t(8) << 20) ? 1u : std::min<unsigned>(hw, 32u);
+    if (nt == 1) {
+        f((size_t)0, n);
+        return;
+    }
+    std::vector<std::thread> th;
+    const size_t per = (n + nt - 1) / nt;
+    for (unsigned t = 0; t < nt; ++t) {
+        const size_t a = t * per, b = std::min(n, a + per);
+        if (a < b) th.emplace_back([=] { f(a, b); });
+    }
+    for (auto& x : th) x.join();
+}
+
+static void pack_graphs(const int32_t* src, int n, int N, int F, int M, int W, uint32_t* dst) {
+    for_columns((size_t)n * M, (size_t)n * M * N * 8,
+                [&](size_t a, size_t b) { pack_columns(src, N, F, W, dst, a, b); });
+}
+
+static void unpack_graphs(const uint32_t* src, int n, int N, int F, int M, int W, int32_t* dst) {
+    for_columns((size_t)n * M, (size_t)n * M * N * 8,
+                [&](size_t a, size_t b) { unpack_columns(src, N, F, W, dst, a, b); });
 }
 
 // Peel-operation descriptors with gather maps: for every previous rfunction,
@@ -1178,6 +1209,8 @@ void sl_destroy(sl_ctx* ctx) {
     delete ctx;
 }
 
+static int plan_adjoint(sl_ctx* ctx);
+
 int sl_create(const sl_problem_desc* d, const sl_options* opt, sl_ctx** out) {
     sl_ctx* ctx = nullptr;
     if (!d || !opt || !out) return fail(ctx, SL_EINVAL, "null argument");
@@ -1533,24 +1566,26 @@ int sl_create(const sl_problem_desc* d, const sl_options* opt, sl_ctx** out) {
         }
     }
     if (d->affection) {
-        LodProgram full;
-        compile_lod_program(d, ops, od, full, true);
-        std::vector<float> dc(4 * std::max<size_t>(1, full.consts.size()), 0.f);
-        for (size_t i = 0; i < full.consts.size(); ++i) {
-            double g4[4];
-            disease_prob_grad(d, full.cperson[i], full.cstate[i], g4);
-            for (int k = 0; k < 4; ++k) dc[4 * i + k] = (float)g4[k];
+        bool ok = true;
+        for (int k = 0; k < K; ++k) ok &= ops[k].n_prev <= 8;
+        if (ok) {
+            std::vector<float> dpf(4 * (size_t)N), dgr(16 * (size_t)N);
+            for (int i = 0; i < N; ++i)
+                for (int v = 0; v < 4; ++v) {
+                    double g4[4];
+                    disease_prob_grad(d, i, v, g4);
+                    dpf[4 * i + v] = (float)d->disease_prob[4 * i + v];
+                    for (int q = 0; q < 4; ++q) dgr[16 * i + 4 * v + q] = (float)g4[q];
+                }
+            AdjDev& D = ctx->adj;
+            if ((rc = upload(ctx, (float**)&D.dprob, dpf.data(), dpf.size()))) return bail(rc);
+            if ((rc = upload(ctx, (float**)&D.dgrad, dgr.data(), dgr.size()))) return bail(rc);
+            ctx->adj_ops = ops;
+            ctx->adj_prev.assign(d->prev_off, d->prev_off + K + 1);
+            ctx->adj_prevs.assign(d->prev, d->prev + d->prev_off[K]);
+            if ((rc = plan_adjoint(ctx))) return bail(rc);
+            ctx->has_adjoint = true;
         }
-        AdjDev& D = ctx->adj;
-        if ((rc = upload(ctx, (int32_t**)&D.prog, full.words.data(), full.words.size()))) return bail(rc);
-        if ((rc = upload(ctx, (int32_t**)&D.starts, full.starts.data(), full.starts.size()))) return bail(rc);
-        if ((rc = upload(ctx, (float**)&D.pconst, full.consts.data(), std::max<size_t>(1, full.consts.size()))))
-            return bail(rc);
-        if ((rc = upload(ctx, (float**)&D.dconst, dc.data(), dc.size()))) return bail(rc);
-        D.n_instr = (int32_t)full.starts.size();
-        D.slots = full.slots;
-        D.nscale = full.nscale;
-        ctx->has_adjoint = true;
     }
     if (!ls_src.empty()) {
         ctx->ls_pending.store(1, std::memory_order_relaxed);
@@ -1626,8 +1661,7 @@ int sl_set_descent_graphs(sl_ctx* ctx, int32_t first, int32_t n, const int32_t* 
     CK(cudaSetDevice(ctx->device));
     CK(cudaStreamSynchronize(ctx->stream));
     if ((rc = stage_host(ctx, words * n))) return rc;
-    for (int i = 0; i < n; ++i)
-        pack_graph(dg + (size_t)i * 2 * P.N * P.M, P.N, P.F, P.M, P.W, ctx->h_stage + words * i);
+    pack_graphs(dg, n, P.N, P.F, P.M, P.W, ctx->h_stage);
     CK(cudaMemcpyAsync(ctx->d_dg + words * first, ctx->h_stage, sizeof(uint32_t) * words * n, cudaMemcpyHostToDevice,
                        ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
@@ -1646,8 +1680,7 @@ int sl_get_descent_graphs(sl_ctx* ctx, int32_t first, int32_t n, int32_t* dg) {
     CK(cudaMemcpyAsync(ctx->h_stage, ctx->d_dg + words * first, sizeof(uint32_t) * words * n, cudaMemcpyDeviceToHost,
                        ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
-    for (int i = 0; i < n; ++i)
-        unpack_graph(ctx->h_stage + words * i, P.N, P.F, P.M, P.W, dg + (size_t)i * 2 * P.N * P.M);
+    unpack_graphs(ctx->h_stage, n, P.N, P.F, P.M, P.W, dg);
     return SL_OK;
 }
 
@@ -1872,8 +1905,7 @@ int sl_lod_score_graphs(sl_ctx* ctx, int32_t n_graphs, const int32_t* dgs) {
         ctx->graphs_cap = n_graphs;
     }
     std::vector<uint32_t> buf(words * n_graphs);
-    for (int i = 0; i < n_graphs; ++i)
-        pack_graph(dgs + (size_t)i * 2 * P.N * P.M, P.N, P.F, P.M, P.W, buf.data() + words * i);
+    pack_graphs(dgs, n_graphs, P.N, P.F, P.M, P.W, buf.data());
     CK(cudaMemcpyAsync(ctx->d_graphs, buf.data(), sizeof(uint32_t) * words * n_graphs, cudaMemcpyHostToDevice,
                        ctx->stream));
     int rc = score_device_graphs(ctx, ctx->d_graphs, n_graphs);
@@ -2075,32 +2107,112 @@ int sl_problem_lod_program_eval(const sl_problem_desc* d, const int32_t* dg, int
     return SL_OK;
 }
 
-// Scratch of the adjoint: per task 2 x slots floats and nscale exponents,
-// processed in chunks of at most kAdjScratchBytes.
-static constexpr size_t kAdjScratchBytes = size_t(4) << 30;
+// The adjoint's gradients come back in chunks of at most kAdjChunkTasks
+// tasks (48 bytes each); its working values live in shared memory.
+static constexpr int64_t kAdjChunkTasks = int64_t(1) << 22;
 
 static int adjoint_chunk(sl_ctx* ctx, int64_t ntask) {
-    const AdjDev& D = ctx->adj;
-    const size_t per = (size_t)(2 * D.slots + D.nscale) * 4 + 6 * sizeof(double);
-    int64_t want = (int64_t)std::min<size_t>((size_t)ntask, kAdjScratchBytes / per);
-    want = std::max<int64_t>(1, want);
+    const int64_t want = std::max<int64_t>(1, std::min<int64_t>(ntask, kAdjChunkTasks));
     if (want <= ctx->adj_chunk) return SL_OK;
     cudaStreamSynchronize(ctx->stream);
-    for (void* p : {(void*)ctx->d_adjA, (void*)ctx->d_adjB, (void*)ctx->d_adjE, (void*)ctx->d_adjG}) {
+    if (ctx->d_adjG) {
+        cudaFree(ctx->d_adjG);
+        ctx->owned.erase(std::find(ctx->owned.begin(), ctx->owned.end(), (void*)ctx->d_adjG));
+        ctx->d_adjG = nullptr;
+    }
+    ctx->adj_chunk = 0;
+    int rc;
+    if ((rc = dev_alloc(ctx, &ctx->d_adjG, (size_t)6 * want))) return rc;
+    ctx->adj_chunk = want;
+    return SL_OK;
+}
+
+// Shared bytes per warp the adjoint aims at when it chooses between keeping
+// every matrix and recomputing: at most 32 KB keeps seven or more warps on an
+// SM; a plan that keeps everything within it is taken as is.
+static constexpr size_t kAdjDefaultBudget = 32 * 1024;
+
+// The adjoint's memory plan (AdjDev): store when every matrix and its
+// adjoint fit the budget, else the split into contiguous segments of about
+// equal cells that needs the least shared memory (matrices read across a
+// segment boundary kept, the rest recomputed).
+static int plan_adjoint(sl_ctx* ctx) {
+    const std::vector<OpDev>& ops = ctx->adj_ops;
+    const int K = (int)ops.size();
+    std::vector<int> consumer(K, -1);
+    for (int k = 0; k < K; ++k)
+        for (int q = ctx->adj_prev[k]; q < ctx->adj_prev[k + 1]; ++q) consumer[ctx->adj_prevs[q]] = k;
+    std::vector<int64_t> cells(K);
+    int64_t total = 0;
+    for (int k = 0; k < K; ++k) total += cells[k] = int64_t(1) << (2 * ops[k].c);
+    struct Plan {
+        std::vector<int32_t> aoff, seg;
+        std::vector<uint8_t> keep;
+        int64_t half = 0;
+        size_t bytes = 0;
+    };
+    auto make = [&](int nseg) {
+        Plan p;
+        p.seg.push_back(0);
+        int64_t run = 0;
+        for (int k = 0; k < K; ++k) {
+            run += cells[k];
+            if ((int)p.seg.size() < nseg && run * nseg >= total * (int64_t)p.seg.size() && k + 1 < K)
+                p.seg.push_back(k + 1);
+        }
+        p.seg.push_back(K);
+        const int ns = (int)p.seg.size() - 1;
+        std::vector<int> seg_of(K);
+        for (int g = 0; g < ns; ++g)
+            for (int k = p.seg[g]; k < p.seg[g + 1]; ++k) seg_of[k] = g;
+        p.keep.assign(K, 0);
+        int64_t perm = 0;
+        p.aoff.assign(K, 0);
+        for (int k = 0; k < K; ++k)
+            if (ns == 1 || (consumer[k] >= 0 && seg_of[consumer[k]] != seg_of[k])) {
+                p.keep[k] = 1;
+                p.aoff[k] = (int32_t)perm;
+                perm += cells[k];
+            }
+        int64_t segn = 0;
+        for (int g = 0; g < ns; ++g) {
+            int64_t o = 0;
+            for (int k = p.seg[g]; k < p.seg[g + 1]; ++k)
+                if (!p.keep[k]) {
+                    p.aoff[k] = (int32_t)(perm + o);
+                    o += cells[k];
+                }
+            segn = std::max(segn, o);
+        }
+        p.half = perm + segn;
+        p.bytes = (size_t)(8 * p.half + 4 * (K + ctx->P.max_child) + 15) & ~(size_t)15;
+        return p;
+    };
+    const size_t budget = ctx->adj_budget ? ctx->adj_budget : kAdjDefaultBudget;
+    Plan best = make(1);
+    if (best.bytes > budget)
+        for (int ns = 2; ns <= std::min(K, 64); ++ns) {
+            Plan p = make(ns);
+            if (best.seg.size() == 2 || p.bytes < best.bytes) best = std::move(p);   // the first split, then smaller
+            if (best.bytes <= budget) break;
+        }
+    if (best.bytes > kSmemBudget)
+        return fail(nullptr, SL_EINVAL, "the trait-peel adjoint needs %zu shared bytes per task", best.bytes);
+    AdjDev& D = ctx->adj;
+    int rc;
+    for (void* p : {(void*)D.aoff, (void*)D.seg, (void*)D.keep}) {
         if (!p) continue;
         cudaFree(p);
         ctx->owned.erase(std::find(ctx->owned.begin(), ctx->owned.end(), p));
     }
-    ctx->d_adjA = ctx->d_adjB = nullptr;
-    ctx->d_adjE = nullptr;
-    ctx->d_adjG = nullptr;
-    ctx->adj_chunk = 0;
-    int rc;
-    if ((rc = dev_alloc(ctx, &ctx->d_adjA, (size_t)D.slots * want))) return rc;
-    if ((rc = dev_alloc(ctx, &ctx->d_adjB, (size_t)D.slots * want))) return rc;
-    if ((rc = dev_alloc(ctx, &ctx->d_adjE, (size_t)std::max(1, D.nscale) * want))) return rc;
-    if ((rc = dev_alloc(ctx, &ctx->d_adjG, (size_t)6 * want))) return rc;
-    ctx->adj_chunk = want;
+    D.aoff = D.seg = nullptr;
+    D.keep = nullptr;
+    if ((rc = upload(ctx, (int32_t**)&D.aoff, best.aoff.data(), best.aoff.size()))) return rc;
+    if ((rc = upload(ctx, (int32_t**)&D.seg, best.seg.data(), best.seg.size()))) return rc;
+    if ((rc = upload(ctx, (uint8_t**)&D.keep, best.keep.data(), best.keep.size()))) return rc;
+    D.nseg = (int32_t)best.seg.size() - 1;
+    D.half = (int32_t)best.half;
+    D.warp_bytes = (int32_t)best.bytes;
     return SL_OK;
 }
 
@@ -2131,7 +2243,9 @@ int sl_lod_kernel_info(sl_ctx* ctx, int32_t* kernel, double* compile_ms) {
 
 int sl_trait_backward(sl_ctx* ctx, int32_t n_graphs, const int32_t* dgs, double* grad, double* ptrait_grad) {
     if (!ctx) return fail(ctx, SL_EINVAL, "null context");
-    if (!ctx->has_adjoint) return fail(ctx, SL_EINVAL, "the problem carries no disease model (affection is NULL)");
+    if (!ctx->has_adjoint)
+        return fail(ctx, SL_EINVAL, "no trait-peel adjoint: the problem carries no disease model (affection is NULL) "
+                                    "or an op multiplies more than 8 rfunctions");
     if (n_graphs < 0 || (n_graphs > 0 && (!dgs || !grad))) return fail(ctx, SL_EINVAL, "bad graph set");
     const ProblemDev& P = ctx->P;
     const size_t words = (size_t)P.M * P.W;
@@ -2141,8 +2255,7 @@ int sl_trait_backward(sl_ctx* ctx, int32_t n_graphs, const int32_t* dgs, double*
     if (ptrait_grad) {
         if ((rc = adjoint_chunk(ctx, 1))) return rc;
         Prof pr(ctx, SL_KERNEL_LOD);
-        CK(launch_trait_adjoint(P, ctx->adj, nullptr, 0, 0, 1, ctx->adj_chunk, ctx->d_adjA, ctx->d_adjB, ctx->d_adjE,
-                                ctx->d_adjG, ctx->d_status, ctx->stream));
+        CK(launch_trait_adjoint(P, ctx->adj, nullptr, 0, 0, 1, ctx->d_adjG, ctx->d_status, ctx->stream, ctx->sms));
         double g6[6];
         CK(cudaMemcpyAsync(g6, ctx->d_adjG, sizeof(g6), cudaMemcpyDeviceToHost, ctx->stream));
         if ((rc = sl_synchronize(ctx))) return rc;
@@ -2160,8 +2273,7 @@ int sl_trait_backward(sl_ctx* ctx, int32_t n_graphs, const int32_t* dgs, double*
         ctx->graphs_cap = n_graphs;
     }
     std::vector<uint32_t> buf(words * n_graphs);
-    for (int i = 0; i < n_graphs; ++i)
-        pack_graph(dgs + (size_t)i * 2 * P.N * P.M, P.N, P.F, P.M, P.W, buf.data() + words * i);
+    pack_graphs(dgs, n_graphs, P.N, P.F, P.M, P.W, buf.data());
     CK(cudaMemcpyAsync(ctx->d_graphs, buf.data(), sizeof(uint32_t) * words * n_graphs, cudaMemcpyHostToDevice,
                        ctx->stream));
     const int64_t ntask = npos * n_graphs;
@@ -2170,13 +2282,28 @@ int sl_trait_backward(sl_ctx* ctx, int32_t n_graphs, const int32_t* dgs, double*
         const int64_t nt = std::min(ctx->adj_chunk, ntask - t0);
         {
             Prof pr(ctx, SL_KERNEL_LOD);
-            CK(launch_trait_adjoint(P, ctx->adj, ctx->d_graphs, (int64_t)words, t0, nt, ctx->adj_chunk, ctx->d_adjA,
-                                    ctx->d_adjB, ctx->d_adjE, ctx->d_adjG, ctx->d_status, ctx->stream));
+            CK(launch_trait_adjoint(P, ctx->adj, ctx->d_graphs, (int64_t)words, t0, nt, ctx->d_adjG, ctx->d_status,
+                                    ctx->stream, ctx->sms));
         }
         CK(cudaMemcpyAsync(grad + t0 * 6, ctx->d_adjG, sizeof(double) * 6 * nt, cudaMemcpyDeviceToHost,
                            ctx->stream));
     }
     return sl_synchronize(ctx);
+}
+
+int sl_adjoint_memory(sl_ctx* ctx, int64_t bytes_per_task, int32_t* segments, int64_t* used_bytes) {
+    if (!ctx) return fail(ctx, SL_EINVAL, "null context");
+    if (!ctx->has_adjoint)
+        return fail(ctx, SL_EINVAL, "no trait-peel adjoint: the problem carries no disease model (affection is NULL) "
+                                    "or an op multiplies more than 8 rfunctions");
+    if (bytes_per_task < 0) return fail(ctx, SL_EINVAL, "negative memory budget");
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaStreamSynchronize(ctx->stream));
+    ctx->adj_budget = (size_t)bytes_per_task;
+    if (int rc = plan_adjoint(ctx)) return fail(ctx, rc, "%s", sl_last_error(nullptr));
+    if (segments) *segments = ctx->adj.nseg;
+    if (used_bytes) *used_bytes = ctx->adj.warp_bytes;
+    return SL_OK;
 }
 
 int sl_problem_trait_backward_eval(const sl_problem_desc* d, const int32_t* dg, int32_t locus, int32_t offset,

@@ -95,17 +95,22 @@ struct ProblemDev {
 //   LI_END  slot                 the likelihood
 enum { LI_REC = 1, LI_SUM = 2, LI_CELL = 3, LI_SCALE = 4, LI_END = 5 };
 
-// The trait peel compiled for the adjoint: every cell and term kept (a zero
-// disease probability still has a derivative), no slot reused (the reverse
-// pass reads every forward value).
+// The trait-peel adjoint's plan (trait_adjoint_kernel, one warp per task,
+// dense rfunctions in the warp's shared memory): where each op's matrix lives
+// and which matrices the first forward pass keeps.  With one segment every
+// matrix has its own place (store).  With several, an op's matrix is kept
+// (its own place in the first part of the arena) only when a later segment
+// reads it; the others share the second part, segment after segment, and are
+// recomputed before their segment's reverse pass (recompute).
 struct AdjDev {
-    const int32_t* prog;     // LI_* words
-    const int32_t* starts;   // word offset of every instruction, in order
-    const float* pconst;     // constants (disease probabilities)
-    const float4* dconst;    // d constant / d (pen HOMO_U, pen HETERO, pen HOMO_A, frequency)
-    int32_t n_instr;
-    int32_t slots;
-    int32_t nscale;          // LI_SCALE instructions
+    const int32_t* aoff;     // [K] float offset of op k's matrix; its adjoint is at aoff + half
+    const int32_t* seg;      // [nseg + 1] first op of each segment, then K
+    const uint8_t* keep;     // [K] 1 when the first forward pass's matrix stays in place
+    const float* dprob;      // [N][4] disease probabilities (person.cc:85-119), FP32
+    const float4* dgrad;     // [N][4] their derivatives by (pen HOMO_U, pen HETERO, pen HOMO_A, frequency)
+    int32_t nseg;
+    int32_t half;            // floats of the matrices (the adjoints take as many)
+    int32_t warp_bytes;      // shared bytes of one warp: matrices, adjoints, exponents [K], child bits
 };
 
 // Options of a device-driven run, read by the run graph's kernels.

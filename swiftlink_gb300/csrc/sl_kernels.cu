@@ -36,6 +36,7 @@
 #include <float.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <map>
 #include <mutex>
 #include <utility>
@@ -2162,176 +2163,322 @@ __global__ void __launch_bounds__(128) lod_prog_kernel(ProblemDev P, const uint3
     }
 }
 
-// Adjoint of the trait peel, one thread per (graph, interval, position) task:
-// the program of AdjDev run forward in FP32 with per-rfunction power-of-two
-// rescaling, every value kept in A[slot][task] (global scratch, coalesced
-// across the warp), then run backward over the same instructions.  The
-// rescaling factors are constants of the forward pass, so the reverse pass on
-// scaled values gives d log L exactly as on unscaled ones: B[root] = 1/A[root],
-// and a LI_SCALE that multiplied its values by f multiplies their adjoints by f.
-// graphs == nullptr peels without a graph (every recombination term 1/4,
-// Peeler::calc_trait_prob): one task, no theta derivatives.
-// grad[task - task0][6] = d log L / d (theta_L, theta_R, pen x3, frequency), FP64.
-constexpr int kAdjMaxFactors = 32;
+// Adjoint of the trait peel (the reverse sum-product of TraitRfunction's
+// peel, trait_rfunction.cc:28-137), one warp per (graph, interval, position)
+// task with the rfunctions in the warp's shared memory, dense [4^c] per op
+// (every cell and term kept: a zero disease probability still has a
+// derivative with respect to the model).
+//
+// Forward: as the FP32 scorer, one (cell, term) item per lane -- a child
+// peel's terms are its four transmissions (i, j), the others' the peel node's
+// four states -- each rfunction scaled so its largest cell is 2^scale_to, the
+// exponent kept.  Reverse: B[root] = 1 / root; op k's cell adjoint times
+// 2^-e_k (its scaling) is spread over the item's factors: to each previous
+// rfunction's cell (shared-memory atomics: cells of op k that differ only in
+// members outside that cutset meet there), to the peel node's disease
+// probability (its derivatives by the three penetrances and the frequency)
+// and, through the children's recombination terms, to theta_L and theta_R.
+// The exponents are constants of the pass, so working on scaled values gives
+// d log L exactly.
+//
+// Memory (AdjDev): with one segment every matrix is kept from the forward
+// pass (store).  When that does not fit the per-warp budget the ops are split
+// into segments: the first forward pass keeps only matrices a later segment
+// reads, and before each earlier segment's reverse pass its other matrices
+// are recomputed from the kept ones (recompute instead of store; one extra
+// forward pass).  graphs == nullptr peels without a graph (every
+// recombination term 1/4, Peeler::calc_trait_prob): one task, no theta
+// derivatives.  grad[task - task0][6] = d log L / d (theta_L, theta_R,
+// pen x3, frequency), FP64.
+constexpr int kAdjMaxPrev = 8;
+
+struct AdjTask {
+    const uint32_t* colL;
+    const uint32_t* colR;
+    float th, an, th2, an2;
+    bool graph;
+};
+
+// 0.25 x the recombination term of (i, j) and its derivatives by theta_L and
+// theta_R (TraitRfunction::get_recombination_probability, trait_rfunction.cc:9-24)
+__device__ __forceinline__ void adj_rec(const AdjTask& T, int bits, int i, int j, float& r, float& dl, float& dr) {
+    if (!T.graph) {
+        r = 0.25f;
+        dl = dr = 0.f;
+        return;
+    }
+    const bool ml = (bits & 1) == i, mr = ((bits >> 2) & 1) == i;
+    const bool pl = ((bits >> 1) & 1) == j, pr = ((bits >> 3) & 1) == j;
+    const float x0 = ml ? T.an : T.th, x1 = mr ? T.an2 : T.th2, x2 = pl ? T.an : T.th, x3 = pr ? T.an2 : T.th2;
+    const float s0 = ml ? -1.f : 1.f, s1 = mr ? -1.f : 1.f, s2 = pl ? -1.f : 1.f, s3 = pr ? -1.f : 1.f;
+    r = 0.25f * (x0 * x1 * x2 * x3);
+    dl = 0.25f * (s0 * x1 * x2 * x3 + x0 * x1 * s2 * x3);
+    dr = 0.25f * (x0 * s1 * x2 * x3 + x0 * x1 * x2 * s3);
+}
+
+// Op k's constants, worked out once per op by every lane: each previous
+// rfunction's arena offset, key count and key positions (4 bits each), and
+// the graph bits of a child peel's child.
+struct AdjOp {
+    OpDev op;
+    int n;
+    int base[kAdjMaxPrev], nk[kAdjMaxPrev], keys[kAdjMaxPrev];
+    int cbits;
+};
+
+__device__ __forceinline__ void adj_op(const ProblemDev& P, const AdjDev& D, const AdjTask& T, int k, AdjOp& o) {
+    o.op = P.ops[k];
+    const int32_t* pd = P.opdata + o.op.prev_at;
+    const int32_t* po = P.opdata + o.op.prev_ops_at;
+    o.n = o.op.n_prev;
+#pragma unroll
+    for (int j = 0; j < kAdjMaxPrev; ++j) {
+        o.base[j] = o.nk[j] = o.keys[j] = 0;
+        if (j < o.n) {
+            o.base[j] = D.aoff[po[j]];
+            o.nk[j] = pd[1];
+            int kk = 0;
+            for (int q = 0; q < pd[1]; ++q) kk |= pd[2 + q] << (4 * q);
+            o.keys[j] = kk;
+            pd += 2 + pd[1];
+        }
+    }
+    o.cbits = (o.op.type == CHILD && T.graph) ? person_bits(P, T.colL, T.colR, o.op.peel) : 0;
+}
+
+// One item of op k: the peel node's state s, the product R of the
+// recombination factors with its derivatives, and the previous rfunctions'
+// cells (arena offsets).
+struct AdjItem {
+    int s;
+    float R, dRl, dRr;
+    int idx[kAdjMaxPrev];
+};
+
+__device__ __forceinline__ void adj_item(const ProblemDev& P, const AdjTask& T, const AdjOp& o, const int* chbits,
+                                         int cell, int t, AdjItem& it) {
+    const OpDev& op = o.op;
+    int ext;
+    it.R = 1.f;
+    it.dRl = it.dRr = 0.f;
+    if (op.type == CHILD) {
+        const int i = t >> 1, j = t & 1;
+        it.s = phased_trait(digit(cell, op.mpos), digit(cell, op.fpos), i, j);
+        adj_rec(T, o.cbits, i, j, it.R, it.dRl, it.dRr);
+        ext = cell | (it.s << (2 * op.c));
+    } else {
+        it.s = t;
+        ext = cell | (t << (2 * op.c));
+        if (op.type == PARENT) {
+            // the product over children of the summed matching transmissions,
+            // its derivatives by the product rule as it is built
+            int mt = t, pt = t;
+            const int32_t* cd = P.opdata + op.child_at;
+            for (int c = 0; c < op.n_child; ++c, cd += 4) {
+                const int kt = digit(ext, cd[1]), other = digit(ext, cd[2]);
+                if (cd[3]) pt = other; else mt = other;
+                const int bits = chbits[c];
+                float sc = 0.f, sl = 0.f, sr = 0.f;
+                for (int i = 0; i < 2; ++i)
+                    for (int j = 0; j < 2; ++j) {
+                        if (phased_trait(mt, pt, i, j) != kt) continue;
+                        float r, dl, dr;
+                        adj_rec(T, bits, i, j, r, dl, dr);
+                        sc += r;
+                        sl += dl;
+                        sr += dr;
+                    }
+                it.dRl = it.dRl * sc + it.R * sl;
+                it.dRr = it.dRr * sc + it.R * sr;
+                it.R *= sc;
+            }
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < kAdjMaxPrev; ++j) {
+        int idx = 0;
+        if (j < o.n)
+            for (int q = 0; q < o.nk[j]; ++q) idx |= digit(ext, (o.keys[j] >> (4 * q)) & 15) << (2 * q);
+        it.idx[j] = o.base[j] + idx;
+    }
+}
+
+// The graph bits of a parent peel's children, into the warp's scratch.
+__device__ __forceinline__ void adj_child_bits(const ProblemDev& P, const AdjTask& T, const AdjOp& o, int* chbits,
+                                               int lane) {
+    if (o.op.type != PARENT) return;
+    for (int c = lane; c < o.op.n_child; c += 32)
+        chbits[c] = T.graph ? person_bits(P, T.colL, T.colR, P.opdata[o.op.child_at + 4 * c]) : 0;
+    __syncwarp();
+}
+
+// Forward of op k: its scaled matrix in A, its exponent in E[k].
+__device__ void adj_forward(const ProblemDev& P, const AdjDev& D, const AdjTask& T, int k, float* A, int* E,
+                            int* chbits, int lane) {
+    AdjOp o;
+    adj_op(P, D, T, k, o);
+    adj_child_bits(P, T, o, chbits, lane);
+    const int ncell = 1 << (2 * o.op.c), nitem = 4 * ncell;
+    float* out = A + D.aoff[k];
+    const float* dp = D.dprob + 4 * o.op.peel;
+    float mx = 0.f;
+    for (int it0 = 0; it0 < nitem; it0 += 32) {
+        const int item = it0 + lane, cell = item >> 2, t = item & 3;
+        float term = 0.f;
+        if (item < nitem) {
+            AdjItem it;
+            adj_item(P, T, o, chbits, cell, t, it);
+            term = dp[it.s];
+#pragma unroll
+            for (int j = 0; j < kAdjMaxPrev; ++j)
+                if (j < o.n) term *= A[it.idx[j]];
+            term *= it.R;
+        }
+        const int grp = lane & ~3;
+        const float t0 = __shfl_sync(FULLMASK, term, grp), t1 = __shfl_sync(FULLMASK, term, grp + 1);
+        const float t2 = __shfl_sync(FULLMASK, term, grp + 2), t3 = __shfl_sync(FULLMASK, term, grp + 3);
+        if (t == 0 && item < nitem) {
+            const float total = ((t0 + t1) + t2) + t3;
+            out[cell] = total;
+            mx = fmaxf(mx, total);
+        }
+    }
+    for (int dd = 16; dd >= 1; dd >>= 1) mx = fmaxf(mx, __shfl_xor_sync(FULLMASK, mx, dd));
+    const int e = mx > 0.f ? ilogbf(mx) - o.op.scale_to : 0;
+    __syncwarp();
+    for (int cell = lane; cell < ncell; cell += 32) out[cell] = ldexpf(out[cell], -e);
+    if (lane == 0) E[k] = e;
+    __syncwarp();
+}
+
+// Reverse of op k: adjoints into the previous rfunctions' cells (B), the
+// model derivatives into g.
+__device__ void adj_reverse(const ProblemDev& P, const AdjDev& D, const AdjTask& T, int k, const float* A, float* B,
+                            const int* E, int* chbits, int lane, double* g) {
+    AdjOp o;
+    adj_op(P, D, T, k, o);
+    adj_child_bits(P, T, o, chbits, lane);
+    const int ncell = 1 << (2 * o.op.c), nitem = 4 * ncell;
+    const float* bk = B + D.aoff[k];
+    const float* dp = D.dprob + 4 * o.op.peel;
+    const float4* dg = D.dgrad + 4 * o.op.peel;
+    const int e = E[k];
+    float gl = 0.f, gr = 0.f, g0 = 0.f, g1 = 0.f, g2 = 0.f, g3 = 0.f;
+    for (int it0 = 0; it0 < nitem; it0 += 32) {
+        const int item = it0 + lane, cell = item >> 2, t = item & 3;
+        if (item >= nitem) break;
+        const float gd = ldexpf(bk[cell], -e);   // the adjoint of the cell before its scaling
+        if (gd == 0.f) continue;
+        AdjItem it;
+        adj_item(P, T, o, chbits, cell, t, it);
+        float a[kAdjMaxPrev];
+        float pp = 1.f;
+#pragma unroll
+        for (int j = 0; j < kAdjMaxPrev; ++j) {
+            a[j] = j < o.n ? A[it.idx[j]] : 1.f;
+            pp *= a[j];
+        }
+        const float c = dp[it.s];
+        const float w = gd * pp;
+        const float4 dc = dg[it.s];
+        g0 += w * it.R * dc.x;
+        g1 += w * it.R * dc.y;
+        g2 += w * it.R * dc.z;
+        g3 += w * it.R * dc.w;
+        gl += w * c * it.dRl;
+        gr += w * c * it.dRr;
+        // each factor's adjoint: the product of the others, by prefix and suffix products
+        float pre[kAdjMaxPrev];
+        float run = gd * c * it.R;
+#pragma unroll
+        for (int j = 0; j < kAdjMaxPrev; ++j) {
+            pre[j] = run;
+            run *= a[j];
+        }
+        float suf = 1.f;
+#pragma unroll
+        for (int j = kAdjMaxPrev - 1; j >= 0; --j) {
+            if (j < o.n) {
+                const float v = pre[j] * suf;
+                if (v != 0.f) atomicAdd(B + it.idx[j], v);
+            }
+            suf *= a[j];
+        }
+    }
+    g[0] += (double)gl;
+    g[1] += (double)gr;
+    g[2] += (double)g0;
+    g[3] += (double)g1;
+    g[4] += (double)g2;
+    g[5] += (double)g3;
+    __syncwarp();
+}
 
 __global__ void __launch_bounds__(128) trait_adjoint_kernel(ProblemDev P, AdjDev D, const uint32_t* graphs,
                                                             int64_t graph_words, int64_t task0, int64_t ntask,
-                                                            int64_t stride, float* A, float* B, int* E,
                                                             double* grad, int* status) {
-    const int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (u >= ntask) return;
-    const int64_t t = task0 + u;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int wpb = blockDim.x >> 5, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float* A = (float*)(smem + (size_t)warp * D.warp_bytes);
+    float* B = A + D.half;
+    int* E = (int*)(B + D.half);
+    int* chbits = E + P.K;   // [max_child] a parent peel's children's graph bits
     const int n = P.n_lod;
     const int64_t npos = (int64_t)(P.M - 1) * n;
-    const uint32_t* colL = nullptr;
-    const uint32_t* colR = nullptr;
-    float th = 0.f, an = 0.f, th2 = 0.f, an2 = 0.f;
-    if (graphs) {
-        const int b = (int)(t / npos);
-        const int64_t pidx = t % npos;
-        const int l = (int)(pidx / n), o = (int)(pidx % n);
-        colL = graphs + (size_t)b * graph_words + (size_t)l * P.W;
-        colR = colL + P.W;
-        th = P.partial_f[l] * (float)(o + 1);
-        an = 1.f - th;
-        th2 = P.partial_f[l] * (float)(n - o);
-        an2 = 1.f - th2;
-    }
-    float* a = A + u;
-    float* g = B + u;
-    int* e = E + u;
-    // forward
-    int si = 0, res = -1;
-    for (int ii = 0; ii < D.n_instr; ++ii) {
-        const int32_t* pc = D.prog + __ldg(D.starts + ii);
-        const int op = __ldg(pc);
-        if (op == LI_CELL) {
-            const int dst = __ldg(pc + 1), nt = __ldg(pc + 2);
-            pc += 3;
-            float total = 0.f;
-            for (int q = 0; q < nt; ++q) {
-                const int nf = __ldg(pc);
-                float v = __ldg(D.pconst + __ldg(pc + 1));
-                pc += 2;
-                for (int f = 0; f < nf; ++f) v *= a[__ldg(pc + f) * stride];
-                pc += nf;
-                total += v;
-            }
-            a[dst * stride] = total;
-            g[dst * stride] = 0.f;
-        } else if (op == LI_REC) {
-            const int child = __ldg(pc + 1), dst = __ldg(pc + 2);
-            const int bits = graphs ? person_bits(P, colL, colR, child) : 0;
-            for (int k = 0; k < 4; ++k) {
-                a[(dst + k) * stride] = graphs ? 0.25f * trait_rec<float>(bits, k >> 1, k & 1, th, an, th2, an2) : 0.25f;
-                g[(dst + k) * stride] = 0.f;
-            }
-        } else if (op == LI_SUM) {
-            const int dst = __ldg(pc + 1), ns = __ldg(pc + 2);
-            float v = 0.f;
-            for (int q = 0; q < ns; ++q) v += a[__ldg(pc + 3 + q) * stride];
-            a[dst * stride] = v;
-            g[dst * stride] = 0.f;
-        } else if (op == LI_SCALE) {
-            const int first = __ldg(pc + 1), cnt = __ldg(pc + 2);
-            float mx = 0.f;
-            for (int q = 0; q < cnt; ++q) mx = fmaxf(mx, a[(first + q) * stride]);
-            int ex = 0;
-            if (mx > 0.f) {
-                ex = ilogbf(mx);
-                const float f = scalbnf(1.0f, -ex);
-                for (int q = 0; q < cnt; ++q) a[(first + q) * stride] *= f;
-            }
-            e[(si++) * stride] = ex;
-        } else {
-            res = __ldg(pc + 1);
+    for (int64_t u = (int64_t)blockIdx.x * wpb + warp; u < ntask; u += (int64_t)gridDim.x * wpb) {
+        const int64_t t = task0 + u;
+        AdjTask T;
+        T.graph = graphs != nullptr;
+        T.colL = T.colR = nullptr;
+        T.th = T.an = T.th2 = T.an2 = 0.f;
+        if (T.graph) {
+            const int b = (int)(t / npos);
+            const int64_t pidx = t % npos;
+            const int l = (int)(pidx / n), o = (int)(pidx % n);
+            T.colL = graphs + (size_t)b * graph_words + (size_t)l * P.W;
+            T.colR = T.colL + P.W;
+            T.th = P.partial_f[l] * (float)(o + 1);
+            T.an = 1.f - T.th;
+            T.th2 = P.partial_f[l] * (float)(n - o);
+            T.an2 = 1.f - T.th2;
         }
-    }
-    double acc[6] = {0, 0, 0, 0, 0, 0};
-    const float root = res >= 0 ? a[res * stride] : 0.f;
-    if (!(root > 0.f)) {
-        if (!P.lod_zero_ok) set_status(status, ST_LOD_NONPOS);
-        for (int k = 0; k < 6; ++k) grad[u * 6 + k] = __longlong_as_double(0x7ff8000000000000LL);   // NaN
-        return;
-    }
-    g[res * stride] = 1.0f / root;
-    // reverse
-    for (int ii = D.n_instr - 1; ii >= 0; --ii) {
-        const int32_t* pc = D.prog + __ldg(D.starts + ii);
-        const int op = __ldg(pc);
-        if (op == LI_SCALE) {
-            const int first = __ldg(pc + 1), cnt = __ldg(pc + 2);
-            const float f = scalbnf(1.0f, -e[(--si) * stride]);
-            for (int q = 0; q < cnt; ++q) g[(first + q) * stride] *= f;
-        } else if (op == LI_CELL) {
-            const int dst = __ldg(pc + 1), nt = __ldg(pc + 2);
-            const float gd = g[dst * stride];
-            pc += 3;
-            if (gd == 0.f) {
-                for (int q = 0; q < nt; ++q) pc += 2 + __ldg(pc);
-                continue;
+        // first forward pass: every op; matrices not kept are overwritten by later segments
+        for (int k = 0; k < P.K; ++k) adj_forward(P, D, T, k, A, E, chbits, lane);
+        const float root = A[D.aoff[P.K - 1]];
+        double g[6] = {0, 0, 0, 0, 0, 0};
+        if (!(root > 0.f)) {
+            if (lane == 0) {
+                if (!P.lod_zero_ok) set_status(status, ST_LOD_NONPOS);
+                for (int q = 0; q < 6; ++q) grad[u * 6 + q] = __longlong_as_double(0x7ff8000000000000LL);   // NaN
             }
-            float m0 = 0.f, m1 = 0.f, m2 = 0.f, m3 = 0.f;
-            for (int q = 0; q < nt; ++q) {
-                const int nf = __ldg(pc), ci = __ldg(pc + 1);
-                const int32_t* fs = pc + 2;
-                pc += 2 + nf;
-                const float c = __ldg(D.pconst + ci);
-                float prod = 1.f;
-                if (nf <= kAdjMaxFactors) {
-                    float pre[kAdjMaxFactors];
-                    for (int f = 0; f < nf; ++f) {
-                        pre[f] = prod;
-                        prod *= a[__ldg(fs + f) * stride];
-                    }
-                    float suf = gd * c;
-                    for (int f = nf - 1; f >= 0; --f) {
-                        const int sl = __ldg(fs + f);
-                        g[sl * stride] += suf * pre[f];
-                        suf *= a[sl * stride];
-                    }
-                } else {
-                    for (int f = 0; f < nf; ++f) prod *= a[__ldg(fs + f) * stride];
-                    for (int f = 0; f < nf; ++f) {
-                        float others = gd * c;
-                        for (int f2 = 0; f2 < nf; ++f2)
-                            if (f2 != f) others *= a[__ldg(fs + f2) * stride];
-                        g[__ldg(fs + f) * stride] += others;
-                    }
-                }
-                const float4 dc = __ldg(D.dconst + ci);
-                m0 += prod * dc.x;
-                m1 += prod * dc.y;
-                m2 += prod * dc.z;
-                m3 += prod * dc.w;
-            }
-            acc[2] += (double)(gd * m0);
-            acc[3] += (double)(gd * m1);
-            acc[4] += (double)(gd * m2);
-            acc[5] += (double)(gd * m3);
-        } else if (op == LI_SUM) {
-            const int dst = __ldg(pc + 1), ns = __ldg(pc + 2);
-            const float gd = g[dst * stride];
-            for (int q = 0; q < ns; ++q) g[__ldg(pc + 3 + q) * stride] += gd;
-        } else if (op == LI_REC && graphs) {
-            const int child = __ldg(pc + 1), dst = __ldg(pc + 2);
-            const int bits = person_bits(P, colL, colR, child);
-            float dl = 0.f, dr = 0.f;
-            for (int k = 0; k < 4; ++k) {
-                const int i = k >> 1, j = k & 1;
-                const float gb = 0.25f * g[(dst + k) * stride];
-                const bool ml = (bits & 1) == i, mr = ((bits >> 2) & 1) == i;
-                const bool pl = ((bits >> 1) & 1) == j, pr = ((bits >> 3) & 1) == j;
-                const float x0 = ml ? an : th, x1 = mr ? an2 : th2, x2 = pl ? an : th, x3 = pr ? an2 : th2;
-                const float s0 = ml ? -1.f : 1.f, s1 = mr ? -1.f : 1.f, s2 = pl ? -1.f : 1.f, s3 = pr ? -1.f : 1.f;
-                dl += gb * (s0 * x1 * x2 * x3 + x0 * x1 * s2 * x3);
-                dr += gb * (x0 * s1 * x2 * x3 + x0 * x1 * x2 * s3);
-            }
-            acc[0] += (double)dl;
-            acc[1] += (double)dr;
+            __syncwarp();
+            continue;
         }
+        for (int i = lane; i < D.half; i += 32) B[i] = 0.f;
+        __syncwarp();
+        for (int sg = D.nseg - 1; sg >= 0; --sg) {
+            const int k0 = D.seg[sg], k1 = D.seg[sg + 1];
+            if (sg < D.nseg - 1) {
+                // recompute the segment's matrices that were not kept, zero their adjoints
+                for (int k = k0; k < k1; ++k)
+                    if (!D.keep[k]) adj_forward(P, D, T, k, A, E, chbits, lane);
+                for (int k = k0; k < k1; ++k)
+                    if (!D.keep[k])
+                        for (int i = lane; i < (1 << (2 * P.ops[k].c)); i += 32) B[D.aoff[k] + i] = 0.f;
+                __syncwarp();
+            } else if (lane == 0) {
+                B[D.aoff[P.K - 1]] = 1.0f / root;
+            }
+            __syncwarp();
+            for (int k = k1 - 1; k >= k0; --k) adj_reverse(P, D, T, k, A, B, E, chbits, lane, g);
+        }
+        for (int q = 0; q < 6; ++q) {
+            double v = g[q];
+            for (int dd = 16; dd >= 1; dd >>= 1) v += __shfl_xor_sync(FULLMASK, v, dd);
+            if (lane == 0) grad[u * 6 + q] = v;
+        }
+        __syncwarp();
     }
-    for (int k = 0; k < 6; ++k) grad[u * 6 + k] = acc[k];
 }
 
 // log_sum (logarithms.cc:14-25)
@@ -2828,12 +2975,21 @@ cudaError_t launch_lod(const ProblemDev& P, int precision, const uint32_t* graph
 }
 
 cudaError_t launch_trait_adjoint(const ProblemDev& P, const AdjDev& D, const uint32_t* graphs, int64_t graph_words,
-                                 int64_t task0, int64_t ntask, int64_t stride, float* A, float* B, int* E,
-                                 double* grad, int* status, cudaStream_t s) {
-    const int threads = 128;
-    const int64_t grid = (ntask + threads - 1) / threads;
-    trait_adjoint_kernel<<<(int)grid, threads, 0, s>>>(P, D, graphs, graph_words, task0, ntask, stride, A, B, E,
-                                                       grad, status);
+                                 int64_t task0, int64_t ntask, double* grad, int* status, cudaStream_t s, int sms) {
+    const int wpb = (int)std::max<int64_t>(1, std::min<int64_t>(4, (200 * 1024) / std::max(1, D.warp_bytes)));
+    const size_t smem = (size_t)wpb * D.warp_bytes;
+    {
+        cudaError_t e = ensure_smem((const void*)trait_adjoint_kernel, smem);
+        if (e != cudaSuccess) return e;
+    }
+    int blocks = 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, (const void*)trait_adjoint_kernel, wpb * 32, smem) !=
+            cudaSuccess || blocks < 1)
+        blocks = 1;
+    int64_t grid = (ntask + wpb - 1) / wpb;
+    grid = std::min<int64_t>(grid, (int64_t)sms * blocks);
+    trait_adjoint_kernel<<<(int)std::max<int64_t>(1, grid), wpb * 32, smem, s>>>(P, D, graphs, graph_words, task0,
+                                                                                 ntask, grad, status);
     return cudaGetLastError();
 }
 

@@ -163,18 +163,28 @@ def rel_err(got, want):
     return np.linalg.norm(got - want) / max(np.linalg.norm(want), 1e-300)
 
 
+# shared bytes per task: 0 = the default plan (every rfunction kept on these
+# pedigrees), 256 = below any plan, so the smallest split into segments with
+# recomputation is taken
+BUDGETS = [0, 256]
+
+
 @pytest.mark.gpu
+@pytest.mark.parametrize("budget", BUDGETS)
 @pytest.mark.parametrize("model", ["recessive", "dominant"])
 @pytest.mark.parametrize("name", CASES)
-def test_device_adjoint_matches_host_fp64(name, model):
+def test_device_adjoint_matches_host_fp64(name, model, budget):
     """FP32 device adjoint with rescaling against the FP64 host adjoint, every
     position of every golden graph, each of the six components within 1e-4
-    of its norm; d log P(T) within 1e-4 relative."""
+    of its norm; d log P(T) within 1e-4 relative -- with every rfunction kept
+    and with the forward cutsets recomputed segment by segment."""
     g = load_golden(name)
     d = g if model == "recessive" else with_model(g, *DOMINANT)
     n = g["n_lod"]
     graphs = np.ascontiguousarray(g["lod_graphs"], np.int32)
     with api.Context(api.Problem.from_arrays(d), n_chains=1) as ctx:
+        seg, used = ctx.adjoint_memory(budget)
+        assert (seg == 1) == (budget == 0), (seg, used)
         grad, pt = ctx.trait_backward(graphs)
     positions = [(l, o) for l in range(g["M"] - 1) for o in range(n)]
     for b in range(graphs.shape[0]):
@@ -187,17 +197,47 @@ def test_device_adjoint_matches_host_fp64(name, model):
 
 
 @pytest.mark.gpu
-def test_device_adjoint_large_pedigree():
+@pytest.mark.parametrize("budget", BUDGETS)
+def test_device_adjoint_large_pedigree(budget):
     """The 120-member, 2000-SNP pedigree under the dominant model: the device
-    adjoint of its starting graph at sampled positions against the host."""
+    adjoint of its starting graph at sampled positions against the host, with
+    every rfunction kept (the default plan here) and recomputed."""
     from swiftlink_gb300.workloads import load_problem
     g = load_problem("cfg2")
     d = with_model(g, *DOMINANT)
     n = g["n_lod"]
     dg = np.ascontiguousarray(g["dg0"], np.int32)
     with api.Context(api.Problem.from_arrays(d), n_chains=1) as ctx:
+        seg, used = ctx.adjoint_memory(budget)
+        assert (seg == 1) == (budget == 0), (seg, used)
         grad, pt = ctx.trait_backward(dg[None])
     positions = [(l, o) for l in sample_loci(g["M"], 9) for o in range(n)]
+    want = host_all(d, dg, positions)
+    got = np.array([grad[0, l, o] for l, o in positions])
+    for k in range(6):
+        assert rel_err(got[:, k], want[:, k]) <= GRAD_RTOL, (k, rel_err(got[:, k], want[:, k]))
+    np.testing.assert_allclose(pt, host_grad(d, None, 0, 0)[2:], rtol=GRAD_RTOL)
+
+
+@pytest.mark.gpu
+def test_device_adjoint_400_member_pedigree_recomputes():
+    """The 400-member, 10,000-SNP pedigree under the dominant model: its
+    dense rfunctions and adjoints (about 92 KB per task) exceed the default
+    budget, so the default plan splits the peel into segments and
+    recomputes; the device adjoint of the starting graph at sampled positions
+    against the host FP64 adjoint (which rescales too: the plain peel
+    underflows here); the plan needs less than half the dense footprint."""
+    from swiftlink_gb300 import pedigree, synth
+    g = pedigree.problem_from_workload(synth.make_workload(5))
+    d = with_model(g, *DOMINANT)
+    n = g["n_lod"]
+    dg = np.ascontiguousarray(g["dg0"], np.int32)
+    with api.Context(api.Problem.from_arrays(d), n_chains=1) as ctx:
+        seg, used = ctx.adjoint_memory(0)
+        dense = 8 * sum(4 ** len(c) for c in g["op_cutset"])   # every matrix and its adjoint, FP32
+        assert seg > 1 and used < dense // 2, (seg, used, dense)
+        grad, pt = ctx.trait_backward(dg[None])
+    positions = [(l, o) for l in sample_loci(g["M"], 5) for o in range(n)]
     want = host_all(d, dg, positions)
     got = np.array([grad[0, l, o] for l, o in positions])
     for k in range(6):
