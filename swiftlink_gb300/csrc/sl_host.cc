@@ -52,7 +52,13 @@ cudaError_t launch_chain_iter(const RunParams* rp, const int64_t* it, int c, uin
                               int nm, int32_t* order, const double* temp, cudaGraphConditionalHandle hsw,
                               cudaGraphConditionalHandle hscore, cudaStream_t s);
 cudaError_t launch_loglik_parts(const ProblemDev& P, const uint32_t* dg, const int* gch, const int* tch, int npair,
-                                double* fag_out, double* rec_out, cudaStream_t s);
+                                double* fag_out, double* rec_out, cudaStream_t s, const Mc3Dev* m = nullptr);
+cudaError_t launch_mc3_exchange(const ProblemDev& P, Mc3Dev* m, const RunParams* rp, int64_t it_end, int C,
+                                uint32_t* dg, double* fag, double* rec, int64_t* accept, int64_t* propose,
+                                cudaStream_t s);
+cudaError_t launch_mc3_begin(Mc3Dev* m, RunParams* rp, cudaStream_t s);
+cudaError_t launch_mc3_end(Mc3Dev* m, const RunParams* rp, cudaGraphConditionalHandle h, int set, cudaStream_t s);
+cudaError_t launch_cond_set(const cudaGraphConditionalHandle* h, int n, unsigned v, cudaStream_t s);
 cudaError_t launch_swap_graphs(uint32_t* dg, size_t words, int a, int b, cudaStream_t s);
 cudaError_t launch_chain_advance(const RunParams* rp, int64_t* it, int c, cudaGraphConditionalHandle hwhile,
                                  cudaStream_t s);
@@ -93,10 +99,17 @@ struct sl_ctx {
     std::vector<double> prior_table;     // [M][4][4]
     std::vector<double> theta_h, minor_h;   // the map at temperature 1
     std::vector<double> temps;           // [C] MC3 temperatures
-    // MC3 exchange statistics per adjacent pair (mc3.cc:138-157)
-    std::vector<int64_t> swap_accept, swap_propose;
+    // MC3 exchange statistics per adjacent pair (mc3.cc:138-157), counted on the device
+    std::vector<int64_t> swap_accept, swap_propose;   // host copies read by sl_mc3_stats
+    int64_t* d_swap_acc = nullptr;    // [C-1]
+    int64_t* d_swap_prop = nullptr;   // [C-1]
+    Mc3Dev* d_mc3 = nullptr;          // the exchange's state: spurt bounds, proposal, pairs
     double* d_llfag = nullptr;        // [4][M] founder-allele-graph likelihoods of the exchange step
     double* d_llrec = nullptr;        // [4][M-1] recombination log-probabilities
+    // an MC3 run as one launch: an outer WHILE node over spurts, each the run
+    // nodes followed by the exchange
+    cudaGraphExec_t mc3_graph = nullptr;
+    int run_graph_epoch = 0, mc3_graph_epoch = 0;   // ls_epoch when each graph was captured
     std::vector<uint8_t> legal;          // [M][N]
     std::vector<int32_t> meioses;        // non-ignorable meioses (markov_chain.cc:70-80)
     std::vector<int32_t> even, odd;
@@ -242,12 +255,7 @@ static void ls_adopt(sl_ctx* ctx) {
         ctx->jit_ls = j;
         ctx->ls_choice = LS_JIT;
         ctx->jit_ls.compile_ms = ctx->ls_thread_ms;
-        if (ctx->run_graph) {
-            cudaStreamSynchronize(ctx->stream);   // no launch of it in flight
-            cudaGraphExecDestroy(ctx->run_graph);
-            ctx->run_graph = nullptr;
-        }
-        ++ctx->ls_epoch;
+        ++ctx->ls_epoch;   // the run graphs are captured again at their next launch
     }
     ctx->ls_bin.reset();
     cudaSetDevice(cur);
@@ -1203,6 +1211,7 @@ void sl_destroy(sl_ctx* ctx) {
     jit_lod_release(&ctx->jit_smem);
     if (ctx->ms_graph) cudaGraphExecDestroy(ctx->ms_graph);
     if (ctx->run_graph) cudaGraphExecDestroy(ctx->run_graph);
+    if (ctx->mc3_graph) cudaGraphExecDestroy(ctx->mc3_graph);
     for (auto st : ctx->cap_streams) cudaStreamDestroy(st);
     for (auto ev : ctx->cap_events) cudaEventDestroy(ev);
     cudaSetDevice(cur);
@@ -1486,6 +1495,14 @@ int sl_create(const sl_problem_desc* d, const sl_options* opt, sl_ctx** out) {
     ctx->temps.assign(C, 1.0);
     ctx->swap_accept.assign(std::max(1, C - 1), 0);
     ctx->swap_propose.assign(std::max(1, C - 1), 0);
+    if ((rc = dev_alloc(ctx, &ctx->d_swap_acc, ctx->swap_accept.size()))) return bail(rc);
+    if ((rc = dev_alloc(ctx, &ctx->d_swap_prop, ctx->swap_propose.size()))) return bail(rc);
+    CK(cudaMemset(ctx->d_swap_acc, 0, sizeof(int64_t) * ctx->swap_accept.size()));
+    CK(cudaMemset(ctx->d_swap_prop, 0, sizeof(int64_t) * ctx->swap_propose.size()));
+    if ((rc = dev_alloc(ctx, (uint8_t**)&ctx->d_mc3, sizeof(Mc3Dev)))) return bail(rc);
+    CK(cudaMemset(ctx->d_mc3, 0, sizeof(Mc3Dev)));
+    if ((rc = dev_alloc(ctx, &ctx->d_llfag, (size_t)4 * M))) return bail(rc);
+    if ((rc = dev_alloc(ctx, &ctx->d_llrec, (size_t)4 * (M - 1)))) return bail(rc);
     if ((rc = upload_chain_maps(ctx))) return bail(rc);
     ctx->trait_prob = host_trait_prob(d, ops, od, arena);
     // compiled trait peel for the batched LOD form
@@ -2475,7 +2492,7 @@ static int prepare_run_graph(sl_ctx* ctx) {
         CK(cudaMemcpy(ctx->d_status, &st, sizeof(int), cudaMemcpyHostToDevice));
     }
     CK(cudaStreamSynchronize(ctx->stream));
-    while ((int)ctx->cap_streams.size() < 3) {
+    while ((int)ctx->cap_streams.size() < 4) {
         cudaStream_t st;
         CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
         ctx->cap_streams.push_back(st);
@@ -2490,20 +2507,26 @@ static int prepare_run_graph(sl_ctx* ctx) {
 // is capturing): init -> one WHILE node per chain (in parallel).  The chains'
 // LOD tables are merged into the context's when read (flush_chain_tables).
 // s1 and s2 capture the bodies.
-static cudaError_t capture_run_nodes(sl_ctx* ctx, cudaStream_t s, cudaStream_t s1, cudaStream_t s2) {
+static cudaError_t capture_run_nodes(sl_ctx* ctx, cudaStream_t s, cudaStream_t s1, cudaStream_t s2,
+                                     bool nested = false) {
     const int C = ctx->n_chains;
-    cudaError_t e = launch_run_init(ctx->d_run, ctx->d_chain_it, C, s);
-    if (e != cudaSuccess) return e;
     cudaStreamCaptureStatus st;
     cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamGetCaptureInfo(s, &st, nullptr, &g, nullptr, nullptr, nullptr);
+    if (e != cudaSuccess) return e;
+    std::vector<cudaGraphConditionalHandle> hws(C);
+    for (int c = 0; c < C; ++c)
+        if ((e = cudaGraphConditionalHandleCreate(&hws[c], g, 1, cudaGraphCondAssignDefault)) != cudaSuccess) return e;
+    if ((e = launch_run_init(ctx->d_run, ctx->d_chain_it, C, s)) != cudaSuccess) return e;
+    // inside an outer loop's body the chains' loops are opened again at every pass
+    if (nested && (e = launch_cond_set(hws.data(), C, 1u, s)) != cudaSuccess) return e;
     const cudaGraphNode_t* deps = nullptr;
     size_t nd = 0;
     if ((e = cudaStreamGetCaptureInfo(s, &st, nullptr, &g, &deps, nullptr, &nd)) != cudaSuccess) return e;
     const std::vector<cudaGraphNode_t> init_deps(deps, deps + nd);
     std::vector<cudaGraphNode_t> whiles;
     for (int c = 0; c < C; ++c) {
-        cudaGraphConditionalHandle hw;
-        if ((e = cudaGraphConditionalHandleCreate(&hw, g, 1, cudaGraphCondAssignDefault)) != cudaSuccess) return e;
+        const cudaGraphConditionalHandle hw = hws[c];
         cudaGraphNodeParams p = {};
         p.type = cudaGraphNodeTypeConditional;
         p.conditional.handle = hw;
@@ -2523,6 +2546,7 @@ static cudaError_t capture_run_nodes(sl_ctx* ctx, cudaStream_t s, cudaStream_t s
 static int build_run_graph(sl_ctx* ctx) {
     int rc = prepare_run_graph(ctx);
     if (rc) return rc;
+    ctx->run_graph_epoch = ctx->ls_epoch;
     cudaStream_t s0 = ctx->cap_streams[0], s1 = ctx->cap_streams[1], s2 = ctx->cap_streams[2];
     cudaGraph_t top = nullptr;
     CK(cudaGraphCreate(&top, 0));
@@ -2538,6 +2562,87 @@ static int build_run_graph(sl_ctx* ctx) {
         return fail(ctx, SL_ECUDA, "capturing the run graph: %s", cudaGetErrorString(e));
     }
     return SL_OK;
+}
+
+// The body of an MC3 run's outer WHILE node, captured on stream s: the
+// spurt's bounds, the run nodes, the exchange (more than one chain) and the
+// step to the next spurt; `set` makes this context's step decide whether the
+// loop runs again.
+static cudaError_t capture_mc3_spurt(sl_ctx* ctx, cudaStream_t s, cudaGraphConditionalHandle h, int set) {
+    cudaError_t e = launch_mc3_begin(ctx->d_mc3, ctx->d_run, s);
+    if (e != cudaSuccess) return e;
+    if ((e = capture_run_nodes(ctx, s, ctx->cap_streams[1], ctx->cap_streams[2], true)) != cudaSuccess) return e;
+    if (ctx->n_chains > 1 &&
+        (e = launch_mc3_exchange(ctx->P, ctx->d_mc3, ctx->d_run, 0, ctx->n_chains, ctx->d_dg, ctx->d_llfag,
+                                 ctx->d_llrec, ctx->d_swap_acc, ctx->d_swap_prop, s)) != cudaSuccess)
+        return e;
+    return launch_mc3_end(ctx->d_mc3, ctx->d_run, h, set, s);
+}
+
+// Open an outer WHILE node (default 1) at the current point of stream s's
+// capture and begin capturing its body on stream sb.
+static cudaError_t begin_outer_while(cudaStream_t s, cudaStream_t sb, cudaGraphConditionalHandle* h) {
+    cudaStreamCaptureStatus st;
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamGetCaptureInfo(s, &st, nullptr, &g, nullptr, nullptr, nullptr);
+    if (e != cudaSuccess) return e;
+    if ((e = cudaGraphConditionalHandleCreate(h, g, 1, cudaGraphCondAssignDefault)) != cudaSuccess) return e;
+    cudaGraph_t body;
+    if ((e = capture_conditional(s, *h, cudaGraphCondTypeWhile, 1, &body)) != cudaSuccess) return e;
+    return cudaStreamBeginCaptureToGraph(sb, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+}
+
+// Instantiate the graph captured on stream s (the capture ends here in any case).
+static cudaError_t end_capture(cudaStream_t s, cudaGraph_t top, cudaError_t e, cudaGraphExec_t* out) {
+    cudaError_t e2 = cudaStreamEndCapture(s, &top);
+    if (e == cudaSuccess) e = e2;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(out, top, 0);
+    if (top) cudaGraphDestroy(top);
+    if (e != cudaSuccess) {
+        *out = nullptr;
+        cudaGetLastError();
+    }
+    return e;
+}
+
+// An MC3 run as one launch: WHILE (spurts left) { spurt bounds -> run nodes ->
+// exchange -> next spurt }.  Mc3::run's loop (mc3.cc:117-158) on the device.
+static int build_mc3_graph(sl_ctx* ctx) {
+    int rc = prepare_run_graph(ctx);
+    if (rc) return rc;
+    ctx->mc3_graph_epoch = ctx->ls_epoch;
+    cudaStream_t s0 = ctx->cap_streams[0], sb = ctx->cap_streams[3];
+    cudaGraph_t top = nullptr;
+    CK(cudaGraphCreate(&top, 0));
+    cudaGraphConditionalHandle h;
+    cudaError_t e = cudaStreamBeginCaptureToGraph(s0, top, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        e = begin_outer_while(s0, sb, &h);
+        if (e == cudaSuccess) {
+            e = capture_mc3_spurt(ctx, sb, h, 1);
+            cudaGraph_t body = nullptr;
+            cudaError_t e2 = cudaStreamEndCapture(sb, &body);
+            if (e == cudaSuccess) e = e2;
+        }
+    }
+    if ((e = end_capture(s0, top, e, &ctx->mc3_graph)) != cudaSuccess)
+        return fail(ctx, SL_ECUDA, "capturing the MC3 graph: %s", cudaGetErrorString(e));
+    return SL_OK;
+}
+
+// Drop a context's run graphs captured before its L-sampler kernel changed.
+static void drop_stale_graphs(sl_ctx* ctx) {
+    if ((ctx->run_graph && ctx->run_graph_epoch != ctx->ls_epoch) ||
+        (ctx->mc3_graph && ctx->mc3_graph_epoch != ctx->ls_epoch))
+        cudaStreamSynchronize(ctx->stream);   // no launch of them in flight
+    if (ctx->run_graph && ctx->run_graph_epoch != ctx->ls_epoch) {
+        cudaGraphExecDestroy(ctx->run_graph);
+        ctx->run_graph = nullptr;
+    }
+    if (ctx->mc3_graph && ctx->mc3_graph_epoch != ctx->ls_epoch) {
+        cudaGraphExecDestroy(ctx->mc3_graph);
+        ctx->mc3_graph = nullptr;
+    }
 }
 
 // log P(G, graph) from its parts in the reference's order: the interval sums
@@ -2561,9 +2666,6 @@ static double loglik_from_parts(const double* fag, const double* rec, int M, dou
 static int loglik_pairs(sl_ctx* ctx, const int* g, const int* t, int npair, double* out) {
     const ProblemDev& P = ctx->P;
     const int M = P.M;
-    int rc;
-    if (!ctx->d_llfag && (rc = dev_alloc(ctx, &ctx->d_llfag, (size_t)4 * M))) return rc;
-    if (!ctx->d_llrec && (rc = dev_alloc(ctx, &ctx->d_llrec, (size_t)4 * (M - 1)))) return rc;
     int g4[4] = {0, 0, 0, 0}, t4[4] = {0, 0, 0, 0};
     for (int k = 0; k < npair; ++k) { g4[k] = g[k]; t4[k] = t[k]; }
     { Prof pf_(ctx, SL_KERNEL_OTHER);
@@ -2577,27 +2679,22 @@ static int loglik_pairs(sl_ctx* ctx, const int* g, const int* t, int npair, doub
     return SL_OK;
 }
 
-// The MC3 exchange after a spurt ending at iteration `it_end` (mc3.cc:138-157):
-// a uniformly chosen adjacent pair (r, r+1) swaps graphs with probability
-// min(1, exp((xy + yx) - (xx + yy))).  Both uniforms come from the Philox
-// stream (stage 9, the spurt's end iteration, draws 0 and 1).
-static int mc3_exchange(sl_ctx* ctx, uint64_t seed, int it_end) {
-    const int C = ctx->n_chains;
-    const uint64_t hi = (0x3ffull << 40) ^ ((uint64_t)it_end << 4) ^ 9u;
-    int r = (int)((C - 1) * host_philox_u01(seed, hi, 0));
-    if (r > C - 2) r = C - 2;
-    const int g[4] = {r, r + 1, r + 1, r}, t[4] = {r, r + 1, r, r + 1};   // xx, yy, xy, yx
-    double ll[4];
-    int rc = loglik_pairs(ctx, g, t, 4, ll);
-    if (rc) return rc;
-    const double ratio = (ll[2] + ll[3]) - (ll[0] + ll[1]);
-    const double u = host_philox_u01(seed, hi, 1);
-    ctx->swap_propose[r] += 1;
-    if (u == 0.0 || std::log(u) < std::min(0.0, ratio)) {
-        { Prof pf_(ctx, SL_KERNEL_OTHER);
-        CK(launch_swap_graphs(ctx->d_dg, (size_t)ctx->P.M * ctx->P.W, r, r + 1, ctx->stream)); }
-        ctx->swap_accept[r] += 1;
-    }
+// The MC3 exchange after a spurt ending at iteration `it_end` (mc3.cc:138-157),
+// queued on the context's stream: a uniformly chosen adjacent pair (r, r+1)
+// swaps graphs with probability min(1, exp((xy + yx) - (xx + yy))).  Both
+// uniforms come from the Philox stream (stage 9, the spurt's end iteration,
+// draws 0 and 1).  The same kernels run inside the persistent MC3 graph.
+static int mc3_exchange(sl_ctx* ctx, const sl_run_options* o, int it_end) {
+    Mc3Dev m{};
+    m.next = it_end;
+    m.total = (int64_t)o->burnin + o->iterations;
+    m.period = o->exchange_period;
+    m.seed = o->seed;
+    CK(cudaMemcpyAsync(ctx->d_mc3, &m, sizeof(m), cudaMemcpyHostToDevice, ctx->stream));
+    { Prof pf_(ctx, SL_KERNEL_OTHER);
+    CK(launch_mc3_exchange(ctx->P, ctx->d_mc3, nullptr, it_end, ctx->n_chains, ctx->d_dg, ctx->d_llfag, ctx->d_llrec,
+                           ctx->d_swap_acc, ctx->d_swap_prop, ctx->stream)); }
+    ctx->launches += 4;
     return SL_OK;
 }
 
@@ -2706,6 +2803,7 @@ static int run_span(sl_ctx* ctx, const sl_run_options* o, int first, int end) {
     const int C = ctx->n_chains;
     const int nm = (int)ctx->meioses.size();
     if (!ctx->profiling) {
+        drop_stale_graphs(ctx);
         if (!ctx->run_graph) {
             int rc = build_run_graph(ctx);
             if (rc) return rc;
@@ -2750,6 +2848,28 @@ static int run_span(sl_ctx* ctx, const sl_run_options* o, int first, int end) {
     return SL_OK;
 }
 
+// Before a launch of an MC3 graph: the run's parameters and exchange state
+// on the context's stream, and the host's tally of the spurts it runs.
+static int launch_mc3_run(sl_ctx* ctx, const sl_run_options* o) {
+    const int64_t total = (int64_t)o->burnin + o->iterations;
+    const RunParams rp{o->first_iteration, o->first_iteration, o->burnin, o->scoring_period, o->lsampler_prob, o->seed};
+    Mc3Dev m{};
+    m.next = o->first_iteration;
+    m.total = total;
+    m.period = o->exchange_period;
+    m.seed = o->seed;
+    CK(cudaMemcpyAsync(ctx->d_run, &rp, sizeof(rp), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->d_mc3, &m, sizeof(m), cudaMemcpyHostToDevice, ctx->stream));
+    const int P = o->exchange_period;
+    for (int it0 = o->first_iteration; it0 < total;) {
+        const int it1 = (int)std::min<int64_t>(total, (it0 / P + 1) * (int64_t)P);
+        account_span(ctx, o, it0, it1);
+        ctx->launches += 2 + (ctx->n_chains + 63) / 64 + (ctx->n_chains > 1 ? 4 : 0);   // bounds, opens, exchange
+        it0 = it1;
+    }
+    return SL_OK;
+}
+
 int sl_run(sl_ctx* ctx, const sl_run_options* o) {
     if (!ctx || !o) return fail(ctx, SL_EINVAL, "null argument");
     if (o->iterations < 0 || o->burnin < 0 || o->scoring_period < 1 || o->first_iteration < 0 ||
@@ -2762,6 +2882,18 @@ int sl_run(sl_ctx* ctx, const sl_run_options* o) {
     ls_adopt(ctx);
     const bool mc3 = o->exchange_period > 0 && C >= 2;
     if (!mc3 && !ls_compiling(ctx)) return run_span(ctx, o, o->first_iteration, total);
+    if (mc3 && !ls_compiling(ctx) && !ctx->profiling) {
+        // every spurt and exchange in one launch
+        drop_stale_graphs(ctx);
+        if (!ctx->mc3_graph) {
+            int rc = build_mc3_graph(ctx);
+            if (rc) return rc;
+        }
+        int rc = launch_mc3_run(ctx, o);
+        if (rc) return rc;
+        CK(cudaGraphLaunch(ctx->mc3_graph, ctx->stream));
+        return SL_OK;
+    }
     // MC3: spurts of exchange_period iterations, each followed by an exchange
     // (Mc3::run, mc3.cc:117-158; iterations are numbered consecutively).  Spurts
     // end at multiples of exchange_period counted from iteration 0, so a run
@@ -2779,7 +2911,7 @@ int sl_run(sl_ctx* ctx, const sl_run_options* o) {
             CK(cudaStreamSynchronize(ctx->stream));
             ls_adopt(ctx);
         }
-        if (mc3 && it1 % P == 0 && (rc = mc3_exchange(ctx, o->seed, it1))) return rc;
+        if (mc3 && it1 % P == 0 && (rc = mc3_exchange(ctx, o, it1))) return rc;
         it0 = it1;
     }
     return SL_OK;
@@ -2799,6 +2931,10 @@ struct sl_batch {
     cudaEvent_t ev_root = nullptr, ev_done = nullptr;
     cudaGraphExec_t graph = nullptr;
     std::vector<int> ls_epochs;   // each context's L-sampler kernel switches when the graph was captured
+    // MC3 runs: every spurt and exchange of every context in one launch
+    cudaStream_t body = nullptr;  // captures the outer loop's body
+    cudaGraphExec_t mc3_graph = nullptr;
+    std::vector<int> mc3_epochs;
 };
 
 void sl_batch_destroy(sl_batch* b) {
@@ -2806,6 +2942,8 @@ void sl_batch_destroy(sl_batch* b) {
     cudaSetDevice(b->device);
     if (b->stream) cudaStreamSynchronize(b->stream);
     if (b->graph) cudaGraphExecDestroy(b->graph);
+    if (b->mc3_graph) cudaGraphExecDestroy(b->mc3_graph);
+    if (b->body) cudaStreamDestroy(b->body);
     for (auto st : b->fork) cudaStreamDestroy(st);
     for (auto ev : b->evs) cudaEventDestroy(ev);
     if (b->ev_root) cudaEventDestroy(b->ev_root);
@@ -2827,6 +2965,7 @@ int sl_batch_create(sl_ctx* const* ctxs, int32_t n, sl_batch** out) {
     b->ctxs.assign(ctxs, ctxs + n);
     b->device = ctxs[0]->device;
     if (cudaSetDevice(b->device) != cudaSuccess || cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) ||
+        cudaStreamCreateWithFlags(&b->body, cudaStreamNonBlocking) ||
         cudaEventCreateWithFlags(&b->ev_root, cudaEventDisableTiming) ||
         cudaEventCreateWithFlags(&b->ev_done, cudaEventDisableTiming)) {
         sl_batch_destroy(b);
@@ -2877,6 +3016,41 @@ static int build_batch_graph(sl_batch* b) {
     return SL_OK;
 }
 
+// A batch's MC3 run as one launch: WHILE (spurts left) { per context, in
+// parallel: spurt bounds -> run nodes -> exchange -> next spurt }.  All
+// contexts share the run's spurts; the first context's step decides whether
+// the loop runs again.
+static int build_batch_mc3_graph(sl_batch* b) {
+    b->mc3_epochs.clear();
+    for (sl_ctx* c : b->ctxs) {
+        int rc = prepare_run_graph(c);
+        if (rc) return rc;
+        b->mc3_epochs.push_back(c->ls_epoch);
+    }
+    cudaGraph_t top = nullptr;
+    if (cudaGraphCreate(&top, 0) != cudaSuccess) return fail(nullptr, SL_ECUDA, "creating the batch graph");
+    cudaGraphConditionalHandle h;
+    cudaError_t e = cudaStreamBeginCaptureToGraph(b->stream, top, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        e = begin_outer_while(b->stream, b->body, &h);
+        if (e == cudaSuccess) {
+            e = cudaEventRecord(b->ev_root, b->body);
+            for (size_t j = 0; j < b->ctxs.size() && e == cudaSuccess; ++j) {
+                if ((e = cudaStreamWaitEvent(b->fork[j], b->ev_root, 0)) != cudaSuccess) break;
+                if ((e = capture_mc3_spurt(b->ctxs[j], b->fork[j], h, j == 0)) != cudaSuccess) break;
+                if ((e = cudaEventRecord(b->evs[j], b->fork[j])) != cudaSuccess) break;
+                e = cudaStreamWaitEvent(b->body, b->evs[j], 0);
+            }
+            cudaGraph_t body = nullptr;
+            cudaError_t e2 = cudaStreamEndCapture(b->body, &body);
+            if (e == cudaSuccess) e = e2;
+        }
+    }
+    if ((e = end_capture(b->stream, top, e, &b->mc3_graph)) != cudaSuccess)
+        return fail(nullptr, SL_ECUDA, "capturing the batch's MC3 graph: %s", cudaGetErrorString(e));
+    return SL_OK;
+}
+
 int sl_batch_run(sl_batch* b, const sl_run_options* o) {
     if (!b || !o) return fail(nullptr, SL_EINVAL, "null argument");
     if (o->iterations < 0 || o->burnin < 0 || o->scoring_period < 1 || o->first_iteration < 0 ||
@@ -2887,6 +3061,42 @@ int sl_batch_run(sl_batch* b, const sl_run_options* o) {
         if (c->profiling) return fail(c, SL_EINVAL, "a batch runs without per-kernel profiling");
     const int total = o->burnin + o->iterations;
     const int P = o->exchange_period;
+    bool paced = false;
+    for (sl_ctx* c : b->ctxs) {
+        ls_adopt(c);
+        paced = paced || ls_compiling(c);
+    }
+    if (P > 0 && !paced && o->first_iteration < total) {
+        // every spurt and exchange of every context in one launch
+        if (b->mc3_graph)
+            for (size_t j = 0; j < b->ctxs.size(); ++j)
+                if (b->mc3_epochs[j] != b->ctxs[j]->ls_epoch) {
+                    if (cudaStreamSynchronize(b->stream) != cudaSuccess)
+                        return fail(nullptr, SL_ECUDA, "waiting for the batch graph");
+                    cudaGraphExecDestroy(b->mc3_graph);
+                    b->mc3_graph = nullptr;
+                    break;
+                }
+        if (!b->mc3_graph) {
+            int rc = build_batch_mc3_graph(b);
+            if (rc) return rc;
+        }
+        for (size_t j = 0; j < b->ctxs.size(); ++j) {
+            sl_ctx* c = b->ctxs[j];
+            int rc = launch_mc3_run(c, o);
+            if (rc) return rc;
+            if (cudaEventRecord(b->evs[j], c->stream) != cudaSuccess ||
+                cudaStreamWaitEvent(b->stream, b->evs[j], 0) != cudaSuccess)
+                return fail(c, SL_ECUDA, "ordering the batch after the context's work");
+        }
+        if (cudaGraphLaunch(b->mc3_graph, b->stream) != cudaSuccess ||
+            cudaEventRecord(b->ev_done, b->stream) != cudaSuccess)
+            return fail(nullptr, SL_ECUDA, "launching the batch's MC3 graph");
+        for (sl_ctx* c : b->ctxs)
+            if (cudaStreamWaitEvent(c->stream, b->ev_done, 0) != cudaSuccess)
+                return fail(c, SL_ECUDA, "ordering the context after the batch");
+        return SL_OK;
+    }
     for (int it0 = o->first_iteration, it1; it0 < total; it0 = it1) {
         // a context whose specialised L-sampler has compiled switches to it: the graph is captured again
         bool paced = false;
@@ -2931,7 +3141,7 @@ int sl_batch_run(sl_batch* b, const sl_run_options* o) {
         if (P > 0 && it1 % P == 0)
             for (sl_ctx* c : b->ctxs)
                 if (c->n_chains > 1) {
-                    int rc = mc3_exchange(c, o->seed, it1);
+                    int rc = mc3_exchange(c, o, it1);
                     if (rc) return rc;
                 }
     }
@@ -3037,6 +3247,14 @@ int sl_sequential_imputation_run(sl_ctx* ctx, int32_t iterations, uint64_t seed,
 
 int sl_mc3_stats(sl_ctx* ctx, int64_t* accepted, int64_t* proposed) {
     if (!ctx) return fail(ctx, SL_EINVAL, "null context");
+    CK(cudaSetDevice(ctx->device));
+    const size_t n = ctx->swap_accept.size();
+    CK(cudaMemcpyAsync(ctx->swap_accept.data(), ctx->d_swap_acc, sizeof(int64_t) * n, cudaMemcpyDeviceToHost,
+                       ctx->stream));
+    CK(cudaMemcpyAsync(ctx->swap_propose.data(), ctx->d_swap_prop, sizeof(int64_t) * n, cudaMemcpyDeviceToHost,
+                       ctx->stream));
+    int rc = sl_synchronize(ctx);
+    if (rc) return rc;
     for (int c = 0; c + 1 < ctx->n_chains; ++c) {
         if (accepted) accepted[c] = ctx->swap_accept[c];
         if (proposed) proposed[c] = ctx->swap_propose[c];

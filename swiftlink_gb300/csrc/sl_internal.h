@@ -120,6 +120,17 @@ struct RunParams {
     uint64_t seed;
 };
 
+// MC3 exchanges on the device (Mc3::run, mc3.cc:117-158): the spurts of a run
+// captured as one graph launch, and the exchange after each full spurt.
+struct Mc3Dev {
+    int64_t next, total, period;   // the next spurt's first iteration; the run's end; the exchange period
+    int64_t it_end;                // the end of the spurt the exchange follows
+    uint64_t seed;
+    int32_t active;                // the spurt just run ends on a multiple of the period: exchange
+    int32_t r;                     // the proposed pair (r, r + 1)
+    int32_t gch[4], tch[4];        // (graph chain, map chain): xx, yy, xy, yx
+};
+
 // What code outside sl_host.cc may read of a context.
 struct CtxView {
     ProblemDev P;

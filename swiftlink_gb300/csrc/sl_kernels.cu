@@ -2541,7 +2541,12 @@ __global__ void choose_kernel(int first, int nchain, uint64_t seed, uint64_t ite
 // ---------------------------------------------------------------------------
 template <typename IX>
 __global__ void __launch_bounds__(128) loglik_fag_kernel(ProblemDev P, const uint32_t* dg, int4 gch, int4 tch,
-                                                         int npair, double* out) {
+                                                         int npair, double* out, const Mc3Dev* m) {
+    if (m) {   // the pairs of the device-side exchange, if one is due
+        if (!m->active) return;
+        gch = make_int4(m->gch[0], m->gch[1], m->gch[2], m->gch[3]);
+        tch = make_int4(m->tch[0], m->tch[1], m->tch[2], m->tch[3]);
+    }
     extern __shared__ __align__(16) unsigned char smem[];
     const int S = blockDim.x;
     const size_t per = fag_block_bytes(P.N, P.F, S, 0) - (((size_t)P.N * 7 + 15) & ~(size_t)15);
@@ -2567,7 +2572,13 @@ __global__ void __launch_bounds__(128) loglik_fag_kernel(ProblemDev P, const uin
     out[t] = fag_like<ProbExact>(P.N, P.F, s_typed, P.geno + (size_t)l * P.N, P.c_minor[(size_t)tc * P.M + l], fs);
 }
 
-__global__ void loglik_rec_kernel(ProblemDev P, const uint32_t* dg, int4 gch, int4 tch, int npair, double* out) {
+__global__ void loglik_rec_kernel(ProblemDev P, const uint32_t* dg, int4 gch, int4 tch, int npair, double* out,
+                                  const Mc3Dev* m) {
+    if (m) {
+        if (!m->active) return;
+        gch = make_int4(m->gch[0], m->gch[1], m->gch[2], m->gch[3]);
+        tch = make_int4(m->tch[0], m->tch[1], m->tch[2], m->tch[3]);
+    }
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int I = P.M - 1;
     if (t >= (int64_t)npair * I) return;
@@ -2592,7 +2603,7 @@ __global__ void swap_graphs_kernel(uint32_t* dg, size_t words, int a, int b) {
 }
 
 cudaError_t launch_loglik_parts(const ProblemDev& P, const uint32_t* dg, const int* gch, const int* tch, int npair,
-                                double* fag_out, double* rec_out, cudaStream_t s) {
+                                double* fag_out, double* rec_out, cudaStream_t s, const Mc3Dev* m) {
     const int S = 64;
     const size_t smem = fag_block_bytes(P.N, P.F, S, 0);
     const int wide = 2 * P.F > 255 ? 1 : 0;
@@ -2601,14 +2612,162 @@ cudaError_t launch_loglik_parts(const ProblemDev& P, const uint32_t* dg, const i
                                     smem);
         if (e != cudaSuccess) return e;
     }
-    const int4 g4 = make_int4(gch[0], gch[1], gch[2], gch[3]), t4 = make_int4(tch[0], tch[1], tch[2], tch[3]);
+    const int4 g4 = gch ? make_int4(gch[0], gch[1], gch[2], gch[3]) : make_int4(0, 0, 0, 0);
+    const int4 t4 = tch ? make_int4(tch[0], tch[1], tch[2], tch[3]) : make_int4(0, 0, 0, 0);
     const int64_t nf = (int64_t)npair * P.M;
     if (wide)
-        loglik_fag_kernel<uint16_t><<<(int)((nf + S - 1) / S), S, smem, s>>>(P, dg, g4, t4, npair, fag_out);
+        loglik_fag_kernel<uint16_t><<<(int)((nf + S - 1) / S), S, smem, s>>>(P, dg, g4, t4, npair, fag_out, m);
     else
-        loglik_fag_kernel<uint8_t><<<(int)((nf + S - 1) / S), S, smem, s>>>(P, dg, g4, t4, npair, fag_out);
+        loglik_fag_kernel<uint8_t><<<(int)((nf + S - 1) / S), S, smem, s>>>(P, dg, g4, t4, npair, fag_out, m);
     const int64_t nr = (int64_t)npair * (P.M - 1);
-    loglik_rec_kernel<<<(int)((nr + 127) / 128), 128, 0, s>>>(P, dg, g4, t4, npair, rec_out);
+    loglik_rec_kernel<<<(int)((nr + 127) / 128), 128, 0, s>>>(P, dg, g4, t4, npair, rec_out, m);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// MC3 exchanges on the device (Mc3::run, mc3.cc:117-158).  After a spurt that
+// ends on a multiple of the exchange period, a uniformly chosen adjacent pair
+// (r, r + 1) swaps graphs with probability min(1, exp((xy + yx) - (xx + yy))),
+// the four log-likelihoods of DescentGraph::get_likelihood2 (descent_graph.cc:
+// 184-269).  Both uniforms come from the Philox stream: stage 9, counter high
+// word (0x3ff << 40) ^ (spurt end << 4), draws 0 and 1.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint64_t mc3_hi(int64_t it_end) {
+    return (0x3ffull << 40) ^ ((uint64_t)it_end << 4) ^ 9u;
+}
+
+// The proposal after the spurt ending at it_end (rp->end when rp is given;
+// one thread).
+__global__ void mc3_pick_kernel(Mc3Dev* m, const RunParams* rp, int64_t it_end, int C) {
+    if (rp) it_end = rp->end;
+    m->it_end = it_end;
+    m->active = (C >= 2 && m->period > 0 && it_end % m->period == 0) ? 1 : 0;
+    if (!m->active) return;
+    int r = (int)((C - 1) * philox_u01(m->seed, mc3_hi(it_end), 0));
+    if (r > C - 2) r = C - 2;
+    m->r = r;
+    const int g[4] = {r, r + 1, r + 1, r}, t[4] = {r, r + 1, r, r + 1};   // xx, yy, xy, yx
+    for (int k = 0; k < 4; ++k) {
+        m->gch[k] = g[k];
+        m->tch[k] = t[k];
+    }
+}
+
+// The decision (one block of 256): each pair's log-likelihood from its parts
+// in the reference's order -- the interval log-probabilities added from 0.0,
+// marker transmission first, then the log of every locus's founder-allele-graph
+// likelihood (LOG_ZERO = -DBL_MAX for an illegal graph), joined by log_product
+// (descent_graph.cc:184-269, logarithms.cc:27-29) -- the acceptance, the swap
+// and the counts.  The logs are taken in parallel (in place); one thread per
+// pair then sums in order.
+__global__ void __launch_bounds__(256) mc3_decide_kernel(Mc3Dev* m, int M, double marker_trans, double* fag,
+                                                         const double* rec, uint32_t* dg, size_t words,
+                                                         int64_t* accept, int64_t* propose) {
+    __shared__ int s_zero[4];
+    __shared__ double s_ll[4];
+    __shared__ int s_acc;
+    if (!m->active) return;
+    const int tid = threadIdx.x;
+    if (tid < 4) s_zero[tid] = 0;
+    __syncthreads();
+    for (int i = tid; i < 4 * M; i += 256) {
+        const double f = fag[i];
+        if (f == 0.0) atomicOr(&s_zero[i / M], 1);
+        else fag[i] = log(f);
+    }
+    __syncthreads();
+    if (tid < 4) {
+        const double LOG_ZERO = -DBL_MAX;
+        double r = 0.0;
+        const double* rk = rec + (size_t)tid * (M - 1);
+        for (int l = 0; l < M - 1; ++l) r += rk[l];
+        const double trans = marker_trans + r;
+        double prior = 0.0;
+        if (s_zero[tid]) {
+            prior = LOG_ZERO;
+        } else {
+            const double* fk = fag + (size_t)tid * M;
+            for (int l = 0; l < M; ++l) prior += fk[l];
+        }
+        s_ll[tid] = (trans == LOG_ZERO || prior == LOG_ZERO) ? LOG_ZERO : trans + prior;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        const double ratio = (s_ll[2] + s_ll[3]) - (s_ll[0] + s_ll[1]);
+        const double u = philox_u01(m->seed, mc3_hi(m->it_end), 1);
+        const int r = m->r;
+        propose[r] += 1;
+        s_acc = (u == 0.0 || log(u) < fmin(0.0, ratio)) ? 1 : 0;
+        if (s_acc) accept[r] += 1;
+    }
+    __syncthreads();
+    if (s_acc) {
+        uint32_t* a = dg + (size_t)m->r * words;
+        uint32_t* b = a + words;
+        for (size_t i = tid; i < words; i += 256) {
+            const uint32_t x = a[i];
+            a[i] = b[i];
+            b[i] = x;
+        }
+    }
+}
+
+// The persistent MC3 run's spurt bounds: the next spurt [next, end) into the
+// run parameters (one thread, first node of the outer loop's body).
+__global__ void mc3_begin_kernel(Mc3Dev* m, RunParams* rp) {
+    const int64_t it0 = m->next;
+    int64_t it1 = m->period > 0 ? (it0 / m->period + 1) * m->period : m->total;
+    if (it1 > m->total) it1 = m->total;
+    rp->first = it0;
+    rp->end = it1;
+}
+
+// After the spurt and its exchange: the next spurt, and (set) whether the
+// outer loop runs again.
+__global__ void mc3_end_kernel(Mc3Dev* m, const RunParams* rp, cudaGraphConditionalHandle h, int set) {
+    m->next = rp->end;
+    if (set) cudaGraphSetConditional(h, m->next < m->total ? 1u : 0u);
+}
+
+cudaError_t launch_mc3_exchange(const ProblemDev& P, Mc3Dev* m, const RunParams* rp, int64_t it_end, int C,
+                                uint32_t* dg, double* fag, double* rec, int64_t* accept, int64_t* propose,
+                                cudaStream_t s) {
+    mc3_pick_kernel<<<1, 1, 0, s>>>(m, rp, it_end, C);
+    cudaError_t e = launch_loglik_parts(P, dg, nullptr, nullptr, 4, fag, rec, s, m);
+    if (e != cudaSuccess) return e;
+    mc3_decide_kernel<<<1, 256, 0, s>>>(m, P.M, P.marker_trans, fag, rec, dg, (size_t)P.M * P.W, accept, propose);
+    return cudaGetLastError();
+}
+
+// Set conditional handles of the graph this kernel is a node of (up to 64 per launch).
+struct CondSet {
+    cudaGraphConditionalHandle h[64];
+    int n;
+    unsigned v;
+};
+
+__global__ void cond_set_kernel(CondSet cs) {
+    if ((int)threadIdx.x < cs.n) cudaGraphSetConditional(cs.h[threadIdx.x], cs.v);
+}
+
+cudaError_t launch_cond_set(const cudaGraphConditionalHandle* h, int n, unsigned v, cudaStream_t s) {
+    for (int i = 0; i < n; i += 64) {
+        CondSet cs;
+        cs.n = n - i < 64 ? n - i : 64;
+        cs.v = v;
+        for (int k = 0; k < cs.n; ++k) cs.h[k] = h[i + k];
+        cond_set_kernel<<<1, 64, 0, s>>>(cs);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mc3_begin(Mc3Dev* m, RunParams* rp, cudaStream_t s) {
+    mc3_begin_kernel<<<1, 1, 0, s>>>(m, rp);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mc3_end(Mc3Dev* m, const RunParams* rp, cudaGraphConditionalHandle h, int set, cudaStream_t s) {
+    mc3_end_kernel<<<1, 1, 0, s>>>(m, rp, h, set);
     return cudaGetLastError();
 }
 

@@ -210,3 +210,32 @@ def test_split_run_exchanges_as_one_run(batched):
     np.testing.assert_array_equal(s0[0], s1[0])
     np.testing.assert_array_equal(s0[1], s1[1])
     assert s0[1].sum() == total // exchange
+
+
+@pytest.mark.gpu
+def test_persistent_mc3_graph_equals_host_driven_spurts():
+    """An MC3 run is one launch of a graph whose outer loop runs every spurt and
+    its exchange on the device; with per-kernel profiling on, the same spurts
+    and exchanges are launched one by one from the host.  Both give the same
+    graphs, scores and exchange counts."""
+    g = load_golden("cfg1")
+    C, seed, iters, burnin, period, exchange = 4, 13, 30, 5, 5, 4
+    temps = [1.0, 0.999, 0.998, 0.997]
+    outs = []
+    for profiled in (False, True):
+        with api.Context(api.Problem.from_arrays(g), n_chains=C, sampler_precision=api.SL_SAMPLER_FAST,
+                         lod_precision=api.SL_LOD_FP32_RESCALED, lod_flags=api.SL_LOD_ZERO_OK) as ctx:
+            ctx.set_temperatures(temps)
+            ctx.set_graphs(np.stack([g["dg0"]] * C))
+            ctx.profile(profiled)
+            ctx.run(iterations=iters, burnin=burnin, period=period, lprob=0.5, seed=seed, exchange_period=exchange)
+            ctx.synchronize()
+            outs.append((ctx.get_graphs(), ctx.lod_results(), ctx.mc3_stats()))
+    (g0, l0, s0), (g1, l1, s1) = outs
+    assert np.array_equal(g0, g1)
+    np.testing.assert_array_equal(l0[0], l1[0])
+    assert l0[1] == l1[1]
+    np.testing.assert_array_equal(s0[0], s1[0])
+    np.testing.assert_array_equal(s0[1], s1[1])
+    assert s0[1].sum() == (iters + burnin) // exchange
+    assert s0[0].sum() > 0   # near-equal temperatures: exchanges are accepted
