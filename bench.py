@@ -1,29 +1,35 @@
 #!/usr/bin/env python
 """Benchmark of the SwiftLink MCMC hot path on GB300.
 
-Workload: the seeded synthetic 120-member, 6-generation pedigree with 3
-consanguinity loops and 35 affected, 2,000 SNPs at 0.2 cM, recessive model,
-10 replicate chains per GPU, scoring every 100th descent graph at 5 positions
-per marker interval (9,995 LOD positions per scored graph).
+Workload (headline): the seeded synthetic 400-member, 8-generation pedigree
+with 10 consanguinity loops and 60 affected, 10,000 SNPs at 0.1 cM, recessive
+model, 32 replicate chains per GPU, scoring every 100th descent graph at 5
+positions per marker interval (49,995 LOD positions per scored graph): the
+largest workload that fits one GPU.
 
-A step is one MCMC iteration (MarkovChain::run, markov_chain.cc:335-392) of
-every chain: an L-sweep over all 2,000 loci or an M-sweep over all 184
-non-ignorable meioses, chosen per chain with probability 0.5, plus LOD scoring
-on iterations that are multiples of 100.  `value` is descent-graph steps/s
-over all chains and GPUs (batched form: all chains in each launch, FP32
-rescaled LOD); LOD positions/s and the plain single-chain FP64 form are
-reported beside it.
+A step is 5 MCMC iterations (MarkovChain::run, markov_chain.cc:335-392) of
+every chain -- each an L-sweep over all 10,000 loci or an M-sweep over all
+non-ignorable meioses, chosen per chain with probability 0.5 -- plus LOD
+scoring on iterations that are multiples of 100; the timed window starts at
+iteration 100, so the 20 default steps score every chain once.  `value` is
+descent-graph steps/s (chain-iterations/s) over all chains and GPUs, batched
+form (all chains in one launch of the run graph, FP32 samplers, FP32-rescaled
+LOD peel with FP64 log-sums).  LOD positions/s, the plain single-chain form,
+the 120-member workload, the trait-peel adjoint on 1,000 graphs and the
+uneven 64-pedigree MC3 batch are reported beside it.
 
 Arms:
-  python bench.py [--gpus N --steps K --warmup W]           this implementation
-  python bench.py --impl reference ...                        the reference's CPU
-      path on the host cores (the C restatement in oracle/, one process per
-      core, the reference's own build being unavailable on this machine)
+  python bench.py [--gpus N --steps K --warmup W]   this implementation
+  python bench.py --impl reference ...               the reference's CPU path
+      on the host cores: the C restatement in oracle/ (the reference's own
+      program does not build on the Arm host), one process per core, each
+      timing bounded slices of the same workload's sweeps and scoring
 """
 from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import subprocess
 import sys
@@ -37,22 +43,27 @@ sys.path.insert(0, ROOT)
 
 METRIC = "descent-graph steps/s + LOD positions/s, batched vs plain GB300, |ΔLOD|≤1e-3"
 UNIT = "steps/s"
-CHAINS = 10
+CHAINS = 32
 PERIOD = 100
-STEP_ITERS = PERIOD   # MCMC iterations per timed step: one scoring period
+STEP_ITERS = 5        # MCMC iterations of every chain per timed step
 LPROB = 0.5
 SEED = 20261205
-WORKLOAD = "cfg2"
 L2_FLUSH_BYTES = 256 << 20  # larger than the 129 MB L2
+# bounded slices of the CPU arms
+SLICE_LOCI = 100
+SLICE_MEIOSES = 4
+SLICE_INTERVALS = 100
+REF_BUDGET_S = 150.0
+DLOD_INTERVALS = (4000, 4040)   # the oracle's check of the FP32 table: 200 positions
 
 
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
-    ap.add_argument("--skip-uneven", action="store_true", help="leave out the uneven multi-pedigree batch")
-    ap.add_argument("--skip-large", action="store_true", help="leave out the 400-member, 10,000-SNP workload")
+    ap.add_argument("--skip-extras", action="store_true",
+                    help="leave out the 120-member, adjoint and uneven-batch measurements")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     return ap.parse_args()
 
@@ -75,18 +86,30 @@ def rank_max(x, dist=None, device="cpu"):
     return float(t.item())
 
 
+def window(W, K):
+    """First iteration of the timed window (a multiple of the scoring period,
+    so the window scores every chain) and of the warm-up before it."""
+    it0 = PERIOD * max(1, math.ceil(W * STEP_ITERS / PERIOD))
+    return it0, it0 - W * STEP_ITERS
+
+
 def config(world):
-    return {"workload": "120-member 6-generation pedigree, 3 loops, 35 affected, 2000 SNPs at 0.2 cM, "
-                        "recessive (0,0,1) q=1e-4, 10 replicate chains per GPU, scoring every 100th graph, "
+    return {"workload": "400-member 8-generation pedigree, 10 loops, 60 affected, 10000 SNPs at 0.1 cM, "
+                        "recessive (0,0,1) q=1e-4, 32 replicate chains per GPU, scoring every 100th graph, "
                         "5 LOD positions per interval",
-            "members": 120, "markers": 2000, "chains_per_gpu": CHAINS, "scoring_period": PERIOD,
-            "lod_positions_per_graph": 9995, "lsampler_prob": LPROB,
+            "members": 400, "markers": 10000, "chains_per_gpu": CHAINS, "scoring_period": PERIOD,
+            "lod_positions_per_graph": 49995, "lsampler_prob": LPROB,
             "parallelism": f"replicas x{world}",
-            "step": "one scoring period: 100 MCMC iterations of every chain and one LOD scoring of every "
-                    "chain's graph, one run-graph launch; value = chain-iterations/s",
+            "step": f"{STEP_ITERS} MCMC iterations of every chain in one run-graph launch; the window starts at "
+                    f"iteration {PERIOD}, so it scores every chain's graph once; value = chain-iterations/s",
             "l2": "flushed (256 MB write) before every timed step",
-            "zero_likelihood_positions": "counted as zero terms of the log-sum (SL_LOD_ZERO_OK); the "
-                                         "reference exits at the first one (peeler.cc:89-92)"}
+            "zero_likelihood_positions": "counted as zero terms of the log-sum (SL_LOD_ZERO_OK); the FP32-"
+                                         "rescaled peel finds none on this pedigree"}
+
+
+def headline_problem():
+    from swiftlink_gb300 import pedigree, synth
+    return pedigree.problem_from_workload(synth.make_workload(5))
 
 
 # ---------------------------------------------------------------------------
@@ -98,19 +121,32 @@ class Clocks:
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self, device):
-        self.device = device
+        self.ids = [str(device)]
+        try:   # the GPU this process runs on, whatever CUDA_VISIBLE_DEVICES maps
+            import torch
+            u = str(torch.cuda.get_device_properties(device).uuid)
+            self.ids.insert(0, u if u.startswith("GPU-") else "GPU-" + u)
+        except Exception:
+            pass
         self.proc = None
         self.path = None
 
     def start(self):
-        try:
-            fd, self.path = tempfile.mkstemp(suffix=".csv")
-            os.close(fd)
-            self.f = open(self.path, "w")
-            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.QUERY}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
-                                         stdout=self.f, stderr=subprocess.DEVNULL)
-        except Exception:
+        for gid in self.ids:
+            try:
+                fd, self.path = tempfile.mkstemp(suffix=".csv")
+                os.close(fd)
+                self.f = open(self.path, "w")
+                self.proc = subprocess.Popen(["nvidia-smi", f"--id={gid}", f"--query-gpu={self.QUERY}",
+                                              "--format=csv,noheader,nounits", "-lms", "200"],
+                                             stdout=self.f, stderr=subprocess.DEVNULL)
+                time.sleep(0.3)
+                if self.proc.poll() is None:
+                    return
+                self.f.close()
+                os.unlink(self.path)
+            except Exception:
+                pass
             self.proc = None
 
     def stop(self):
@@ -144,84 +180,117 @@ class Clocks:
 
 
 # ---------------------------------------------------------------------------
-# CPU baseline: the C restatement of the reference (oracle/)
+# CPU arms: the C restatement of the reference (oracle/), bounded slices
 # ---------------------------------------------------------------------------
-def port_problem():
+def legal_masks(d):
+    """Genotype elimination's masks of the problem (the library's host-side
+    elimination, equal to the reference's GenotypeElimination): input tables
+    of the CPU port, computed before any timing."""
+    import ctypes
+    from swiftlink_gb300 import api
+    desc = api.Problem.from_arrays(d, with_legal=False).desc()
+    out = np.zeros((d["M"], d["N"]), np.uint8)
+    rc = api.lib().sl_problem_legal_masks(ctypes.byref(desc), out.ctypes.data_as(ctypes.c_void_p))
+    if rc != 0:
+        raise RuntimeError(f"sl_problem_legal_masks failed ({rc})")
+    return out
+
+
+def cpu_problem(d=None):
     from oracle import port
-    from swiftlink_gb300.workloads import load_problem
-    d = load_problem(WORKLOAD)
+    d = dict(headline_problem() if d is None else d)
+    d["legal"] = legal_masks(d)
     d["trait_prior"] = port.derive_priors(d["genotypes"], d["typed"], d["minor"])
     return d
 
 
-def port_iteration(P, d, dg, chain, it):
-    """One MarkovChain::run iteration of one chain on the CPU port with the
-    same Philox draw streams the device driver uses."""
+def slice_times(P, d, dg, chain, rounds, budget_s, seed=SEED):
+    """Time bounded slices of one chain's work on the CPU port, with the
+    device driver's Philox draws: L-steps at SLICE_LOCI consecutive even loci
+    (slo_lsteps, in place), an M-sweep over SLICE_MEIOSES meioses of the
+    shuffled order (slo_msweep), and the rescaled FP64 trait peel of
+    SLICE_INTERVALS intervals.  Returns seconds per full L-sweep, per full
+    M-sweep and per scoring of one graph, extrapolated by the slices' share."""
     from swiftlink_gb300 import philox
     M, K, N = d["M"], d["K"], d["N"]
-    if philox.chooses_l(SEED, chain, it, LPROB):
-        u = philox.lsweep_draws(SEED, chain, it, M, K + 2 * N)
-        for l in list(range(0, M, 2)) + list(range(1, M, 2)):
-            dg, _ = P.lstep(dg, l, u[l])
-    else:
-        order = philox.shuffled(SEED, chain, it, d["meioses"])
-        u = philox.msweep_draws(SEED, chain, it, order.size, M)
-        dg, _ = P.msweep(dg, order, u)
-    return dg
+    nm = len(d["meioses"])
+    tl = tm = ts = 0.0
+    nl = nmm = ns = 0
+    t_start = time.perf_counter()
+    for r in range(rounds):
+        it = PERIOD + r
+        lo = (2 * SLICE_LOCI * r) % (M - 2 * SLICE_LOCI)
+        loci = np.arange(lo, lo + 2 * SLICE_LOCI, 2, dtype=np.int32)
+        u = philox.uniform(seed, philox.stage_hi(chain, it, 1),
+                           (loci.astype(np.uint64)[:, None] << np.uint64(24))
+                           ^ np.arange(K + 2 * N, dtype=np.uint64)[None, :])
+        t = time.perf_counter()
+        P.lsteps(dg, loci, u)
+        tl += time.perf_counter() - t
+        nl += loci.size
+        order = philox.shuffled(seed, chain, it, d["meioses"])[:SLICE_MEIOSES]
+        um = philox.msweep_draws(seed, chain, it, order.size, M)
+        t = time.perf_counter()
+        dg2, _ = P.msweep(dg, order, um)
+        tm += time.perf_counter() - t
+        nmm += order.size
+        dg[...] = dg2
+        l0 = (SLICE_INTERVALS * r) % (M - 1 - SLICE_INTERVALS)
+        t = time.perf_counter()
+        P.lod_range(dg[None], l0, l0 + SLICE_INTERVALS, rescale=True, zero_ok=True)
+        ts += time.perf_counter() - t
+        ns += SLICE_INTERVALS
+        if time.perf_counter() - t_start > budget_s:
+            break
+    return {"lsweep_s": tl / nl * M, "msweep_s": tm / nmm * nm, "score_s": ts / ns * (M - 1),
+            "loci": nl, "meioses": nmm, "intervals": ns}
 
 
-def cpu_baseline_sample():
-    """~10-30 s of single-core CPU work: one L-sweep, one M-sweep and one LOD
-    scoring of one chain, from which steps/s and positions/s follow."""
+def per_iteration_s(t, lprob=LPROB):
+    """CPU seconds of one chain-iteration: an L- or M-sweep by the run's
+    choice probability, and the scoring of every PERIOD-th graph."""
+    return lprob * t["lsweep_s"] + (1 - lprob) * t["msweep_s"] + t["score_s"] / PERIOD
+
+
+def cpu_baseline_sample(d, graphs, table32):
+    """About 10-30 s of single-core CPU work on the same workload: slices of
+    L-steps, M-sweep steps and scoring timed on the port and extrapolated to
+    chain-iterations/s; plus the oracle's check of the device's FP32 LOD table
+    (one scoring of every chain's graph) on 200 positions."""
     from oracle import port
     port.build()
-    d = port_problem()
-    P = port.Port(d)
-    M, K, N = d["M"], d["K"], d["N"]
-    rng = np.random.default_rng(1)
-    dg = d["dg0"].copy()
-    t0 = time.perf_counter()
-    u = rng.random((M, K + 2 * N))
-    for l in list(range(0, M, 2)) + list(range(1, M, 2)):
-        dg, _ = P.lstep(dg, l, u[l])
-    tl = time.perf_counter() - t0
-    order = d["meioses"].copy()
-    rng.shuffle(order)
-    t0 = time.perf_counter()
-    dg, _ = P.msweep(dg, order, rng.random((order.size, M)))
-    tm = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    P.lod(dg[None], zero_ok=True)
-    tlod = time.perf_counter() - t0
-    steps_per_s = 2.0 / (tl + tm)
-    return {"value": steps_per_s, "unit": UNIT, "cores": 1, "kind": "port",
-            "lod_positions_per_s": (M - 1) * d["n_lod"] / tlod,
-            "sample": f"one chain: 1 L-sweep ({tl:.2f} s) + 1 M-sweep over {order.size} meioses ({tm:.2f} s) "
-                      f"+ 1 LOD scoring of 9995 positions ({tlod:.2f} s), single thread"}
+    dc = cpu_problem(d)
+    P = port.Port(dc)
+    dg = np.ascontiguousarray(graphs[0], np.int32).copy()
+    t = slice_times(P, dc, dg, 0, rounds=10, budget_s=20.0)
+    rate = 1.0 / per_iteration_s(t)
+    l0, l1 = DLOD_INTERVALS
+    raw, cnt, tp = P.lod_range(graphs, l0, l1, rescale=True)
+    from swiftlink_gb300 import api
+    want = api.lod_table(raw, cnt, tp)
+    n = d["n_lod"]
+    dlod = float(np.abs(table32[l0 * n:l1 * n] - want).max())
+    return {"value": rate, "unit": UNIT, "cores": 1, "kind": "port",
+            "lod_positions_per_s": 1.0 / (t["score_s"] / ((d["M"] - 1) * n)),
+            "sample": f"one chain, single thread: L-steps at {t['loci']} loci, M-sweep steps of {t['meioses']} "
+                      f"meioses over all loci, rescaled FP64 scoring of {t['intervals']} intervals; extrapolated "
+                      f"to {t['lsweep_s']:.1f} s per L-sweep, {t['msweep_s']:.1f} s per M-sweep, "
+                      f"{t['score_s']:.1f} s per scoring",
+            "max_abs_dlod_vs_oracle": dlod,
+            "dlod_check": f"device FP32-rescaled table of one scoring of all {graphs.shape[0]} chains' graphs "
+                          f"against the oracle's rescaled FP64 peel of the same graphs, intervals [{l0}, {l1})"}
 
 
 def _ref_worker(args):
-    chains, steps, warmup, budget_s = args
+    chain, rounds, budget_s = args
     from oracle import port
-    d = port_problem()
+    d = cpu_problem()
     P = port.Port(d)
-    dgs = {c: d["dg0"].copy() for c in chains}
-    for it in range(warmup):
-        for c in chains:
-            dgs[c] = port_iteration(P, d, dgs[c], c, it)
+    dg = np.ascontiguousarray(d["dg0"], np.int32).copy()
     t0 = time.perf_counter()
-    done = 0
-    scored = 0
-    for it in range(warmup, warmup + steps):
-        for c in chains:
-            dgs[c] = port_iteration(P, d, dgs[c], c, it)
-        if it % PERIOD == 0:
-            P.lod(np.stack([dgs[c] for c in chains]), zero_ok=True)
-            scored += len(chains)
-        done += 1
-        if time.perf_counter() - t0 > budget_s:
-            break
-    return done * len(chains), time.perf_counter() - t0, scored
+    t = slice_times(P, d, dg, chain, rounds, budget_s)
+    t["wall"] = time.perf_counter() - t0
+    return t
 
 
 def run_reference(args):
@@ -233,26 +302,31 @@ def run_reference(args):
     port.build()
     cores = os.cpu_count() or 1
     workers = max(1, min(cores, CHAINS * args.gpus))
-    total_chains = CHAINS * args.gpus
-    groups = [list(range(w, total_chains, workers)) for w in range(workers)]
-    budget = 60.0
+    rounds = max(1, args.steps + args.warmup)
     ctx = mp.get_context("spawn")
     t0 = time.perf_counter()
     with ctx.Pool(workers) as pool:
-        res = pool.map(_ref_worker, [(g, args.steps, args.warmup, budget) for g in groups])
+        res = pool.map(_ref_worker, [(w, rounds, REF_BUDGET_S) for w in range(workers)])
     wall = time.perf_counter() - t0
-    chain_steps = sum(r[0] for r in res)
-    tmax = max(r[1] for r in res)
-    value = chain_steps / tmax
-    min_steps = min(r[0] // max(1, len(g)) for r, g in zip(res, groups))
+    it_s = float(np.mean([per_iteration_s(t) for t in res]))   # CPU seconds per chain-iteration
+    value = workers / it_s
+    step_s = CHAINS * args.gpus * STEP_ITERS * it_s / workers
+    lsw = float(np.mean([t["lsweep_s"] for t in res]))
+    msw = float(np.mean([t["msweep_s"] for t in res]))
+    sc = float(np.mean([t["score_s"] for t in res]))
     out = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
-           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tmax / max(1, min_steps),
-           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * step_s,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f64 (samplers, peel and log-sums)",
            "data": "synthetic (seeded generator, swiftlink_gb300/synth.py)", "config": config(args.gpus),
+           "lod_positions_per_s": workers * 49995 / sc,
            "cpu_baseline": {"value": value, "unit": UNIT, "cores": workers, "kind": "port",
-                            "sample": f"C restatement of the reference, {workers} processes over "
-                                      f"{total_chains} chains, {min_steps} timed iterations per chain "
-                                      f"(capped at {budget:.0f} s), wall {wall:.1f} s"},
+                            "sample": f"C restatement of the reference, {workers} processes (one chain each), "
+                                      f"slices per process: L-steps at {res[0]['loci']} loci, M-sweep steps of "
+                                      f"{res[0]['meioses']} meioses over all 10000 loci, rescaled FP64 scoring of "
+                                      f"{res[0]['intervals']} intervals (capped at {REF_BUDGET_S:.0f} s); per chain "
+                                      f"{lsw:.2f} s per L-sweep, {msw:.2f} s per M-sweep, {sc:.2f} s per scoring; "
+                                      f"wall {wall:.1f} s"},
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
 
@@ -260,365 +334,47 @@ def run_reference(args):
 # ---------------------------------------------------------------------------
 # this implementation
 # ---------------------------------------------------------------------------
-def run_ours(args):
-    import torch
-    from swiftlink_gb300 import api, philox
-    from swiftlink_gb300.workloads import load_problem, step_bytes, position_bytes
-
-    rank, world, local = dist_env()
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
-    torch.cuda.set_device(local)
-    dev = torch.device("cuda", local)
-
-    def barrier():
-        if dist:
-            dist.barrier()
-
-    def allmax(x):
-        return rank_max(x, dist, dev)
-
-    d = load_problem(WORKLOAD)
-    prob = api.Problem.from_arrays(d, with_legal=False)
-    N, F, M, n = d["N"], d["F"], d["M"], d["n_lod"]
-    npos = (M - 1) * n
-    C = CHAINS
-    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
-    seed = SEED + 7919 * rank
-
-    # ---------------- batched form: all chains per launch, FP32-rescaled LOD
-    # the L-sampler compiled for this pedigree (bit-identical to the generic kernel)
-    ctx = api.Context(prob, n_chains=C, lod_precision=api.SL_LOD_FP32_RESCALED, device=local,
-                      sampler_precision=api.SL_SAMPLER_FAST, lod_flags=api.SL_LOD_ZERO_OK,
-                      ls_kernel=api.SL_LS_KERNEL_SPECIALISED)
-    ls_sel, ls_ms = ctx.ls_kernel_info()
-    ctx.set_graphs(np.stack([d["dg0"]] * C))
-    stream = torch.cuda.ExternalStream(ctx.stream_handle())
-    W, K = args.warmup, args.steps
-    P_ = STEP_ITERS
-    ctx.run(iterations=W * P_, burnin=0, period=PERIOD, lprob=LPROB, seed=seed)
-    ctx.synchronize()
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
-    clocks = Clocks(local)
-    launches0 = ctx.launches
-    barrier()
-    torch.cuda.synchronize()
-    clocks.start()
-    # each step is one launch of the run graph: one scoring period, 100 MCMC
-    # iterations of every chain (each chain running its own iterations) and the
-    # scoring of every chain's graph at the period's first iteration
-    for i in range(K):
-        with torch.cuda.stream(stream):
-            flush.fill_(i & 0xff)
-            ev[i][0].record(stream)
-        ctx.run(iterations=(W + i + 1) * P_, burnin=0, period=PERIOD, lprob=LPROB, seed=seed,
-                first_iteration=(W + i) * P_)
-        with torch.cuda.stream(stream):
-            ev[i][1].record(stream)
-    ctx.synchronize()
-    torch.cuda.synchronize()
-    barrier()
-    clk = clocks.stop()
-    gpu_launches = ctx.launches - launches0
-    step_ms = [a.elapsed_time(b) for a, b in ev]
-    t_s = allmax(sum(step_ms) / 1e3)
-    value = K * P_ * C * world / t_s
-
-    # the same chains with one launch per MCMC iteration (every chain waits for
-    # the slowest one at every iteration), for comparison
-    Ki = min(K, 50)
-    evi = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(Ki)]
-    it0 = (W + K) * P_
-    for i in range(Ki):
-        with torch.cuda.stream(stream):
-            flush.fill_(i & 0xff)
-            evi[i][0].record(stream)
-        ctx.run(iterations=it0 + i + 1, burnin=0, period=PERIOD, lprob=LPROB, seed=seed, first_iteration=it0 + i)
-        with torch.cuda.stream(stream):
-            evi[i][1].record(stream)
-    ctx.synchronize()
-    per_iter = {"value": Ki * C * world / allmax(sum(a.elapsed_time(b) for a, b in evi) / 1e3), "unit": UNIT,
-                "note": "one run-graph launch (and L2 flush) per MCMC iteration: every chain waits for the "
-                        "slowest at every iteration"}
-
-    # algorithmic bytes of the timed run-graph launches: every chain-step moves
-    # step_bytes, every scored graph position_bytes per position
-    sb = step_bytes(N, F, M)
-    scorings = K * P_ // PERIOD
-    alg_total = K * P_ * C * sb + scorings * C * npos * position_bytes(N, F, n)
-    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
-        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {"hbm_gbs": 6800.0}
-    peak = float(peaks.get("hbm_gbs", 6800.0))
-    per_launch = alg_total / K
-    avg_s = sum(step_ms) / 1e3 / K
-    achieved = per_launch / avg_s / 1e9
-    run_graph_name = "run graph (one scoring period: 100 MCMC iterations of every chain)"
-    # DRAM bytes per launch: the captured 2-iteration graph launch (per iteration in
-    # profiles/traffic.md) times the iterations of one launch, an upper estimate (a
-    # longer launch keeps more of its state in L2 between iterations)
-    t_iter = traffic_from_profiles("run graph (one MCMC iteration of every chain)")
-    traffic = t_iter * P_ if t_iter is not None else None
-
-    # kernel shares from a separate profiled pass: the same iterations with
-    # per-kernel-class events (the host-driven path, kernels launched one by one)
-    lod_kernel_names = {api.SL_LOD_KERNEL_INTERP: "lod_prog_kernel", api.SL_LOD_KERNEL_JIT_REG: "sl_lod_jit (registers)",
-                        api.SL_LOD_KERNEL_JIT_SMEM: "sl_lod_jit (shared memory)"}
-    sel, jit_ms = ctx.lod_kernel_info()
-    ls_name = "sl_ls_jit (specialised)" if ls_sel == api.SL_LS_KERNEL_SPECIALISED else "lsampler_kernel<float>"
-    names = {0: ls_name, 1: "fag_warp_kernel+ffbs_scan_kernel", 2: lod_kernel_names.get(sel, "lod_kernel"),
-             3: "lod_merge_kernel", 4: "choose/shuffle"}
-    Kp = min(K, 10)
-    ctx.profile(True)
-    ctx.run(iterations=it0 + Ki + Kp, burnin=0, period=PERIOD, lprob=LPROB, seed=seed, first_iteration=it0 + Ki)
-    ctx.synchronize()
-    kern = {k: ctx.profile_read(k) for k in range(5)}
-    ctx.profile(False)
-    tot = max(1e-9, sum(x[0] for x in kern.values()))
-    roofline = {"bound": "hbm", "kernel": run_graph_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": traffic,
-                "traffic_source": "profiles/traffic.md: ncu DRAM bytes of the run graph per iteration x 100",
-                "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if "when" in peaks else "fallback",
-                "algorithmic_bytes_per_launch": per_launch, "avg_launch_ms": 1e3 * avg_s,
-                "note": "latency-bound integer and FP32 work on small rfunctions: the HBM fraction is small by "
-                        "construction; SM issue utilisation per kernel is in profiles/",
-                "kernel_share_profiled_pass": {names[k]: round(v[0] / tot, 4) for k, v in kern.items()}}
-    if WORKLOAD == "cfg2" and C == 10 and ls_sel == api.SL_LS_KERNEL_SPECIALISED:
-        try:
-            roofline["issue"] = issue_estimate(C, W * P_, (W + K) * P_, seed, LPROB, len(d["meioses"]),
-                                               (clk or {}).get("sm_mhz"), torch.cuda.get_device_properties(dev).multi_processor_count,
-                                               sum(step_ms) / 1e3)
-        except Exception as exc:   # an estimate only: never lose the bench line over it
-            roofline["issue"] = {"error": str(exc)[:200]}
-
-    # ---------------- LOD positions/s, batched (many graphs per launch, FP32) vs plain (FP64, one graph)
-    graphs = ctx.get_graphs()
-    G = 64
-    gset = np.stack([graphs[i % C] for i in range(G)])
-    lctx = api.Context(prob, n_chains=G, lod_precision=api.SL_LOD_FP32_RESCALED, device=local, lod_flags=api.SL_LOD_ZERO_OK)
-    lctx.set_graphs(gset)
-    lstream = torch.cuda.ExternalStream(lctx.stream_handle())
-    lod_pos_s = timed_lod(lctx, lstream, flush, G, npos, reps=5)
-    lsel, ljit_ms = lctx.lod_kernel_info()
-    pctx = api.Context(prob, n_chains=1, lod_precision=api.SL_LOD_FP64, device=local, lod_flags=api.SL_LOD_ZERO_OK)
-    pctx.set_graphs(gset[:1])
-    pstream = torch.cuda.ExternalStream(pctx.stream_handle())
-    plain_lod_pos_s = timed_lod(pctx, pstream, flush, 1, npos, reps=3)
-
-    # ---------------- the error of the batched form: one scoring of the 64-graph set in
-    # FP32 with rescaling against FP64, per-position |dLOD|
-    lctx.lod_reset()
-    lctx.lod_score_chains()
-    raw32, c32, tp32 = lctx.lod_results()
-    with api.Context(prob, n_chains=G, lod_precision=api.SL_LOD_FP64, device=local,
-                     lod_flags=api.SL_LOD_ZERO_OK) as p64:
-        p64.set_graphs(gset)
-        p64.lod_score_chains()
-        raw64, c64, tp64 = p64.lod_results()
-    fin = raw64 > -1e300
-    dlod = float(np.abs(api.lod_table(raw32, c32, tp32) - api.lod_table(raw64, c64, tp64))[fin].max())
-
-    # ---------------- adjoint of the trait peel (dominant model 0.01/0.8/0.9, q = 1e-3) over
-    # the 64 stored graphs, through sl_trait_backward with host graphs and gradients
-    adj = adjoint_rate(d, gset, local)
-
-    # ---------------- the uneven batch: 64 pedigrees of 20-150 members, 8 MC3 chains each
-    uneven = uneven_batch_rate(local) if not args.skip_uneven else None
-    # ---------------- large scale: 400 members, 10,000 SNPs, 32 chains
-    large = large_scale(local) if not args.skip_large else None
-
-    # ---------------- plain form: one chain, FP64 LOD
-    pctx.run(iterations=W, burnin=0, period=PERIOD, lprob=LPROB, seed=seed)
-    pctx.synchronize()
-    Kp = min(K, 40)
-    evp = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(Kp)]
-    for i in range(Kp):
-        with torch.cuda.stream(pstream):
-            flush.fill_(i & 0xff)
-            evp[i][0].record(pstream)
-        pctx.run(iterations=W + i + 1, burnin=0, period=PERIOD, lprob=LPROB, seed=seed, first_iteration=W + i)
-        with torch.cuda.stream(pstream):
-            evp[i][1].record(pstream)
-    pctx.synchronize()
-    plain_steps_s = Kp / (sum(a.elapsed_time(b) for a, b in evp) / 1e3)
-
-    # ---------------- end to end through the public API with host buffers
-    ectx = api.Context(prob, n_chains=C, lod_precision=api.SL_LOD_FP32_RESCALED, device=local,
-                       sampler_precision=api.SL_SAMPLER_FAST, lod_flags=api.SL_LOD_ZERO_OK,
-                       ls_kernel=api.SL_LS_KERNEL_SPECIALISED)
-    host_graphs = np.ascontiguousarray(np.stack([d["dg0"]] * C))
-    ectx.set_graphs(host_graphs)
-    ectx.run(iterations=W * P_, burnin=0, period=PERIOD, lprob=LPROB, seed=seed)
-    ectx.synchronize()
-    host_graphs = ectx.get_graphs()
-    Ke = min(K, 20)
-    barrier()
-    t0 = time.perf_counter()
-    for i in range(Ke):
-        ectx.set_graphs(host_graphs)                                   # H2D: the step's state
-        ectx.run(iterations=(W + i + 1) * P_, burnin=0, period=PERIOD, lprob=LPROB, seed=seed,
-                 first_iteration=(W + i) * P_)
-        host_graphs = ectx.get_graphs()                                # D2H: the step's result
-    e2e_t = allmax(time.perf_counter() - t0)
-    words = M * ((2 * (N - F) + 31) // 32)
-    e2e = {"value": Ke * P_ * C * world / e2e_t, "unit": UNIT, "h2d_bytes_per_step": 4 * words * C,
-           "d2h_bytes_per_step": 4 * words * C,
-           "path": "sl_set_descent_graphs (pinned, packed) + sl_run(one scoring period, 100 iterations) + "
-                   "sl_get_descent_graphs per step"}
-
-    if rank == 0:
-        out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
-               "ms_per_step": t_s * 1e3 / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-               "dtype": "f64 peel and founder-allele graphs, f32 M-sampler filter, f32-rescaled LOD peel with "
-                        "f64 accumulation (plain form: f64 throughout, bit-exact)",
-               "data": "synthetic (seeded generator, swiftlink_gb300/synth.py; no public dataset)",
-               "config": config(world), "impl": "ours",
-               "lod_positions_per_s": lod_pos_s * world,
-               "lod_kernel": {"selected": lod_kernel_names.get(lsel, str(lsel)),
-                              "specialised_compile_ms": round(ljit_ms, 1),
-                              "selection": "timed at the first scoring (SL_LOD_KERNEL_AUTO)"},
-               "ls_kernel": {"selected": ls_name, "specialised_compile_ms": round(ls_ms, 1),
-                             "selection": "SL_LS_KERNEL_SPECIALISED (NVRTC at context creation, outside the timed "
-                                          "region; draws bit-identical graphs to the generic kernel)"},
-               "plain": {"steps_per_s": plain_steps_s * world, "lod_positions_per_s": plain_lod_pos_s * world,
-                         "form": "one chain per launch, exact FP64 samplers, FP64 LOD peel"},
-               "batched_vs_plain": {"steps": value / (plain_steps_s * world),
-                                    "lod_positions": lod_pos_s / plain_lod_pos_s},
-               "max_abs_dlod_fp32_vs_fp64": dlod,
-               "adjoint": adj,
-               "uneven_batch": uneven,
-               "large_scale": large,
-               "per_iteration_launches": per_iter,
-               "gpu_launches": int(gpu_launches), "roofline": roofline, "clocks": clk, "e2e": e2e}
-        if world == 1:
-            out["cpu_baseline"] = cpu_baseline_sample()
-        print(json.dumps(out))
-    for c in (ctx, lctx, pctx, ectx):
-        c.close()
-    if dist:
-        dist.destroy_process_group()
+def counters():
+    """ncu figures of the kernels (DRAM bytes and warp instructions per
+    launch, with the workload each was captured on), if recorded."""
+    path = os.path.join(ROOT, "profiles", "counters.json")
+    if not os.path.exists(path):
+        return {}
+    with open(path) as f:
+        return json.load(f)
 
 
-def large_scale(device, C=32, K=4):
-    """The 400-member, 8-generation, 10-loop pedigree with 10,000 SNPs at 0.1 cM
-    (seeded, host-built peel sequence, the gene drop's graph as the start), 32
-    chains: steps/s of the batched form (wall clock around sl_run of K
-    iterations, one run-graph launch), LOD positions/s of the batched FP32 form
-    against the plain FP64 form on the chains' 32 graphs, and the FP32 form's
-    max |dLOD| against the FP64 peel with rescaling.  The plain FP64 peel (the
-    reference's arithmetic) underflows to 0 at every position of this
-    pedigree, so the rescaled FP64 peel is the accuracy yardstick."""
-    from swiftlink_gb300 import api, pedigree, synth
-    t0 = time.perf_counter()
-    d = pedigree.problem_from_workload(synth.make_workload(5))
-    prob = api.Problem.from_arrays(d, with_legal=False)
-    ctx = api.Context(prob, n_chains=C, device=device, lod_precision=api.SL_LOD_FP32_RESCALED,
-                      sampler_precision=api.SL_SAMPLER_FAST, lod_flags=api.SL_LOD_ZERO_OK,
-                      ls_kernel=api.SL_LS_KERNEL_SPECIALISED)
-    ctx.set_graphs(np.stack([d["dg0"]] * C))
-    ctx.run(iterations=2, burnin=0, period=1, lprob=LPROB, seed=SEED)
-    ctx.synchronize()
-    setup_s = time.perf_counter() - t0
-    t = time.perf_counter()
-    ctx.run(iterations=2 + K, burnin=0, period=1 << 30, lprob=LPROB, seed=SEED, first_iteration=2)
-    ctx.synchronize()
-    steps_s = K * C / (time.perf_counter() - t)
-    npos = (d["M"] - 1) * d["n_lod"]
-
-    def lod_rate(c, reps):
-        c.lod_score_chains()
-        c.synchronize()
-        c.lod_reset()
-        t = time.perf_counter()
-        for _ in range(reps):
-            c.lod_score_chains()
-        c.synchronize()
-        return reps * C * npos / (time.perf_counter() - t)
-
-    graphs = ctx.get_graphs()
-    fp32 = lod_rate(ctx, 3)
-    ctx.lod_reset()
-    ctx.lod_score_chains()
-    raw32, c32, tp32 = ctx.lod_results()
-    out = {"members": d["N"], "founders": d["F"], "markers": d["M"], "chains": C, "steps_per_s": steps_s,
-           "lod_positions_per_s": fp32, "setup_s": round(setup_s, 1),
-           "max_cutset": int(max(len(c) for c in d["op_cutset"]))}
-    for name, prec in (("plain_fp64", api.SL_LOD_FP64), ("fp64_rescaled", api.SL_LOD_FP64_RESCALED)):
-        with api.Context(prob, n_chains=C, device=device, lod_precision=prec, lod_flags=api.SL_LOD_ZERO_OK) as c64:
-            c64.set_graphs(graphs)
-            rate = lod_rate(c64, 1)
-            c64.lod_reset()
-            c64.lod_score_chains()
-            raw64, c_64, tp64 = c64.lod_results()
-        fin = raw64 > -1e300
-        out[name] = {"lod_positions_per_s": rate, "positions_underflowed": int((~fin).sum()),
-                     "max_abs_dlod_fp32": float(np.abs(api.lod_table(raw32, c32, tp32)
-                                                       - api.lod_table(raw64, c_64, tp64))[fin].max())
-                     if fin.any() else None}
-    out["batched_vs_plain_lod"] = fp32 / out["plain_fp64"]["lod_positions_per_s"]
-    ctx.close()
-    return out
+def lm_choices(C, it0, it1, seed, lprob):
+    """Per iteration of [it0, it1), how many chains chose the L-sampler
+    (the run's Philox choice replayed)."""
+    from swiftlink_gb300 import philox
+    c = np.arange(C, dtype=np.uint64)[:, None]
+    it = np.arange(it0, it1, dtype=np.uint64)[None, :]
+    hi = (c << np.uint64(40)) ^ (it << np.uint64(4)) ^ np.uint64(7)
+    return (philox.uniform(seed, hi, 0) < lprob).sum(axis=0)
 
 
-def uneven_batch_rate(device, n_ped=64, chains=8, K=20):
-    """Chain-steps/s of the uneven batch: 64 seeded pedigrees of 20-150
-    members (0-4 loops, 1,000 SNPs at 0.5 cM), 8 MC3 chains each at
-    temperatures 0.3^(j/7), fast samplers, FP32 LOD (the slot-program
-    interpreter: no per-pedigree compilation), exchange and scoring every 10
-    iterations, all pedigrees in one graph launch per spurt."""
-    from swiftlink_gb300 import api, pedigree, synth
-    t0 = time.perf_counter()
-    probs = [pedigree.problem_from_workload(w) for w in synth.uneven_batch(n_ped)]
-    temps = [0.3 ** (j / 7) for j in range(chains)]
-    ctxs = []
-    for pd in probs:
-        ctx = api.Context(api.Problem.from_arrays(pd, with_legal=False), n_chains=chains, device=device,
-                          lod_precision=api.SL_LOD_FP32_RESCALED, sampler_precision=api.SL_SAMPLER_FAST,
-                          lod_flags=api.SL_LOD_ZERO_OK, lod_kernel=api.SL_LOD_KERNEL_INTERP)
-        ctx.set_temperatures(temps)
-        ctx.set_graphs(np.stack([pd["dg0"]] * chains))
-        ctxs.append(ctx)
-    setup_s = time.perf_counter() - t0
-    opts = dict(burnin=0, period=10, lprob=LPROB, seed=SEED, exchange_period=10)
-    with api.Batch(ctxs) as b:
-        b.run(iterations=10, **opts)                      # builds the graph, warms up
-        for c in ctxs:
-            c.synchronize()
-        t = time.perf_counter()
-        b.run(iterations=10 + K, first_iteration=10, **opts)
-        for c in ctxs:
-            c.synchronize()
-        dt = time.perf_counter() - t
-    acc = sum(int(c.mc3_stats()[0].sum()) for c in ctxs)
-    prop = sum(int(c.mc3_stats()[1].sum()) for c in ctxs)
-    sizes = [pd["N"] for pd in probs]
-    for c in ctxs:
-        c.close()
-    return {"value": K * chains * n_ped / dt, "unit": "chain-steps/s", "pedigrees": n_ped, "chains_per_pedigree": chains,
-            "members": [min(sizes), max(sizes)], "markers": 1000, "iterations_timed": K,
-            "exchanges_accepted": acc, "exchanges_proposed": prop, "setup_s": round(setup_s, 1),
-            "timing": "wall clock around sl_batch_run + synchronize (host-side MC3 exchanges included)"}
-
-
-def adjoint_rate(d, graphs, device):
-    from swiftlink_gb300 import api
-    from swiftlink_gb300.workloads import disease_probs
-    pen, q = (0.01, 0.8, 0.9), 1e-3
-    dd = dict(d, penetrance=np.array(pen), freq=np.float64(q),
-              disease_prob=disease_probs(d["affection"], d["mother"] < 0, q, pen))
-    npos = (d["M"] - 1) * d["n_lod"]
-    with api.Context(api.Problem.from_arrays(dd, with_legal=False), n_chains=1, device=device,
-                     lod_precision=api.SL_LOD_FP32_RESCALED, lod_flags=api.SL_LOD_ZERO_OK) as ctx:
-        ctx.trait_backward(graphs[:1])
-        reps = 3
-        t = time.perf_counter()
-        for _ in range(reps):
-            grad, pt = ctx.trait_backward(graphs)
-        dt = (time.perf_counter() - t) / reps
-    return {"value": graphs.shape[0] * npos / dt, "unit": "positions/s", "graphs": int(graphs.shape[0]),
-            "model": "dominant (0.01, 0.8, 0.9), q = 1e-3",
-            "path": "sl_trait_backward: host graphs in, d log L / d (theta_L, theta_R, penetrances, q) out"}
+def issue_estimate(C, it0, it1, seed, lprob, n_meioses, sm_mhz, sms, seconds, counts):
+    """SM issue utilisation of timed run-graph launches: the warp instructions
+    of the L- and M-sweeps they ran (each chain's L/M choice replayed with the
+    same Philox draws; instructions per unit from ncu counts of the same
+    workload: one chain's L half-sweep, one chain's meiosis step in the
+    founder-allele-graph and filter kernels) over the SMs' issue rate (4
+    schedulers per SM, one warp instruction per cycle each, at the SM clock
+    sampled during the launches).  The scoring launches are left out."""
+    need = ("l_half_sweep_per_chain", "fag_per_meiosis_step", "scan_per_meiosis_step")
+    if not counts or any(counts.get(k) is None for k in need) or not sm_mhz or not sms or seconds <= 0:
+        return None
+    n_l = int(lm_choices(C, it0, it1, seed, lprob).sum())
+    n_m = C * (it1 - it0) - n_l
+    per_l = 2 * counts["l_half_sweep_per_chain"]
+    per_m = (n_meioses + 1) * counts["fag_per_meiosis_step"] + n_meioses * counts["scan_per_meiosis_step"]
+    inst = n_l * per_l + n_m * per_m
+    peak = sms * 4 * sm_mhz * 1e6
+    return {"bound": "issue", "achieved": inst / seconds / 1e9, "peak": peak / 1e9, "unit": "G warp-inst/s",
+            "frac": inst / seconds / peak, "l_sweeps": n_l, "m_sweeps": n_m,
+            "warp_inst_per_l_sweep": per_l, "warp_inst_per_m_sweep": per_m,
+            "source": counts.get("source", "ncu smsp__inst_executed.sum")}
 
 
 def timed_lod(ctx, stream, flush, G, npos, reps):
@@ -638,62 +394,357 @@ def timed_lod(ctx, stream, flush, G, npos, reps):
     return reps * G * npos / t
 
 
-def inst_from_profiles(name):
-    """Warp instructions per launch (smsp__inst_executed.sum) from a committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", name)
-    if not os.path.exists(path):
-        return None
-    for line in open(path):
-        if line.startswith("| smsp__inst_executed.sum |"):
-            try:
-                return float(line.split("|")[2].split()[0].replace(",", ""))
-            except (ValueError, IndexError):
-                return None
-    return None
+def run_ours(args):
+    import torch
+    from swiftlink_gb300 import api
+    from swiftlink_gb300.workloads import step_bytes, position_bytes
+
+    rank, world, local = dist_env()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    def barrier():
+        if dist:
+            dist.barrier()
+
+    def allmax(x):
+        return rank_max(x, dist, dev)
+
+    t_setup = time.perf_counter()
+    d = headline_problem()
+    setup_s = time.perf_counter() - t_setup
+    prob = api.Problem.from_arrays(d, with_legal=False)
+    N, F, M, n = d["N"], d["F"], d["M"], d["n_lod"]
+    nm = len(d["meioses"])
+    npos = (M - 1) * n
+    C = CHAINS
+    S = STEP_ITERS
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
+    seed = SEED + 7919 * rank
+    W, K = args.warmup, args.steps
+    it0, itw = window(W, K)
+    run = dict(burnin=0, period=PERIOD, lprob=LPROB, seed=seed)
+
+    # ---------------- batched form: all chains per launch, FP32 samplers, FP32-rescaled LOD
+    ctx = api.Context(prob, n_chains=C, lod_precision=api.SL_LOD_FP32_RESCALED, device=local,
+                      sampler_precision=api.SL_SAMPLER_FAST, lod_flags=api.SL_LOD_ZERO_OK,
+                      ls_kernel=api.SL_LS_KERNEL_GENERIC)
+    ctx.set_graphs(np.stack([d["dg0"]] * C))
+    stream = torch.cuda.ExternalStream(ctx.stream_handle())
+    ctx.run(iterations=it0, first_iteration=itw, **run)
+    ctx.synchronize()
+    ctx.lod_reset()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+    clocks = Clocks(local)
+    launches0 = ctx.launches
+    barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    for i in range(K):
+        with torch.cuda.stream(stream):
+            flush.fill_(i & 0xff)
+            ev[i][0].record(stream)
+        ctx.run(iterations=it0 + (i + 1) * S, first_iteration=it0 + i * S, **run)
+        with torch.cuda.stream(stream):
+            ev[i][1].record(stream)
+    ctx.synchronize()
+    torch.cuda.synchronize()
+    barrier()
+    clk = clocks.stop()
+    gpu_launches = ctx.launches - launches0
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    t_s = allmax(sum(step_ms) / 1e3)
+    value = K * S * C * world / t_s
+    raw_run, cnt_run, tp_run = ctx.lod_results()
+    graphs = ctx.get_graphs()
+
+    # ---------------- kernel shares and the dominant kernel's roofline, from a profiled
+    # pass: the same kind of iterations, kernels launched one by one with per-class events
+    itp = it0 + K * S
+    Kp = 2
+    ctx.profile(True)
+    ctx.run(iterations=itp + Kp, first_iteration=itp, **dict(run, period=1 << 30))
+    ctx.synchronize()
+    kern = {k: ctx.profile_read(k) for k in range(5)}
+    ctx.profile(False)
+    n_l = lm_choices(C, itp, itp + Kp, seed, LPROB)
+    per_locus = -(-N // 4) + 2 * (-(-(N - F) // 4)) + 8
+    sb = step_bytes(N, F, M)
+    classes = {
+        0: ("lsampler_kernel<float> (one half-sweep of the chains that chose L)",
+            float(n_l.sum()) * (M // 2) * per_locus / max(1, kern[0][1])),
+        1: ("M-sweep graph (fag_warp_kernel + ffbs_scan_kernel, every meiosis of the chains that chose M)",
+            float((C - n_l).sum()) * sb / max(1, kern[1][1])),
+    }
+    tot = max(1e-9, sum(x[0] for x in kern.values()))
+    names = {0: "lsampler_kernel", 1: "fag_warp_kernel+ffbs_scan_kernel", 2: "LOD scoring kernel",
+             3: "lod_merge_kernel", 4: "choose/shuffle"}
+    dom = 0 if kern[0][0] >= kern[1][0] else 1
+    dom_name, dom_bytes = classes[dom]
+    dom_s = kern[dom][0] / 1e3 / max(1, kern[dom][1])
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    peaks = json.load(open(peaks_path)) if os.path.exists(peaks_path) else {}
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    achieved = dom_bytes / dom_s / 1e9
+    cnt = counters()
+    ck = cnt.get("lsampler_kernel_cfg5" if dom == 0 else "msweep_cfg5", {})
+    traffic = None
+    if ck.get("dram_bytes_per_unit") is not None:
+        units = float(n_l.sum()) * (M // 2) / max(1, kern[0][1]) if dom == 0 else \
+            float((C - n_l).sum()) / max(1, kern[1][1])
+        traffic = ck["dram_bytes_per_unit"] * units
+    roofline = {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": traffic,
+                "peak_source": "of measured (MEASURED_PEAKS.json hbm_gbs)" if "hbm_gbs" in peaks
+                else "of fallback (6.8 TB/s)",
+                "algorithmic_bytes_per_launch": dom_bytes, "avg_launch_ms": 1e3 * dom_s,
+                "bytes_per_unit": per_locus if dom == 0 else sb,
+                "unit_of_work": "one (chain, locus) L-step: 2-bit genotypes of every member, the non-founder "
+                                "indicators read and written, 8 bytes of map" if dom == 0 else
+                                "one chain's M-sweep: every locus's genotypes, indicators read and written, map",
+                "traffic_source": ck.get("source"),
+                "note": "latency- and issue-bound integer and FP32 work on small rfunctions: the HBM fraction is "
+                        "small by construction; the issue estimate below is the binding bound",
+                "kernel_share_profiled_pass": {names[k]: round(v[0] / tot, 4) for k, v in kern.items()}}
+    try:
+        roofline["issue"] = issue_estimate(C, it0, it0 + K * S, seed, LPROB, nm, (clk or {}).get("sm_mhz"),
+                                           torch.cuda.get_device_properties(dev).multi_processor_count,
+                                           sum(step_ms) / 1e3, cnt.get("issue_cfg5"))
+    except Exception as exc:   # an estimate only: never lose the bench line over it
+        roofline["issue"] = {"error": str(exc)[:200]}
+
+    # ---------------- LOD positions/s: batched (all chains' graphs per launch, FP32-rescaled)
+    # against plain (one graph per launch, FP64 with rescaling: the plain FP64 peel
+    # underflows at every position of this pedigree, as the reference's does)
+    lod_pos_s = timed_lod(ctx, stream, flush, C, npos, reps=5)
+    lsel, ljit_ms = ctx.lod_kernel_info()
+    pctx = api.Context(prob, n_chains=1, lod_precision=api.SL_LOD_FP64_RESCALED, device=local,
+                       lod_flags=api.SL_LOD_ZERO_OK)
+    pctx.set_graphs(graphs[:1])
+    pstream = torch.cuda.ExternalStream(pctx.stream_handle())
+    plain_lod_pos_s = timed_lod(pctx, pstream, flush, 1, npos, reps=3)
+
+    # ---------------- FP32 error: one scoring of the chains' graphs in FP32 against FP64 with rescaling
+    ctx.lod_reset()
+    ctx.lod_score_graphs(graphs)
+    raw32, c32, tp32 = ctx.lod_results()
+    table32 = api.lod_table(raw32, c32, tp32)
+    with api.Context(prob, n_chains=C, lod_precision=api.SL_LOD_FP64_RESCALED, device=local,
+                     lod_flags=api.SL_LOD_ZERO_OK) as p64:
+        p64.set_graphs(graphs)
+        p64.lod_score_chains()
+        raw64, c64, tp64 = p64.lod_results()
+    fin = raw64 > -1e300
+    dlod = float(np.abs(table32 - api.lod_table(raw64, c64, tp64))[fin].max())
+    with api.Context(prob, n_chains=1, lod_precision=api.SL_LOD_FP64, device=local,
+                     lod_flags=api.SL_LOD_ZERO_OK) as plain64:
+        plain64.set_graphs(graphs[:1])
+        plain64.lod_score_chains()
+        rawp, _, _ = plain64.lod_results()
+    plain_underflow = int((rawp <= -1e300).sum())
+
+    # ---------------- plain form: one chain, exact FP64 samplers, FP64-rescaled LOD
+    xctx = api.Context(prob, n_chains=1, lod_precision=api.SL_LOD_FP64_RESCALED, device=local,
+                       lod_flags=api.SL_LOD_ZERO_OK)
+    xctx.set_graphs(graphs[:1])
+    xstream = torch.cuda.ExternalStream(xctx.stream_handle())
+    xctx.run(iterations=it0, first_iteration=it0 - 1, **run)
+    xctx.synchronize()
+    Kx = 3
+    evx = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(Kx)]
+    for i in range(Kx):
+        with torch.cuda.stream(xstream):
+            flush.fill_(i & 0xff)
+            evx[i][0].record(xstream)
+        xctx.run(iterations=it0 + i + 1, first_iteration=it0 + i, **run)
+        with torch.cuda.stream(xstream):
+            evx[i][1].record(xstream)
+    xctx.synchronize()
+    plain_steps_s = Kx / (sum(a.elapsed_time(b) for a, b in evx) / 1e3)
+    xctx.close()
+
+    # ---------------- end to end through the public API with host buffers: every step
+    # uploads the chains' graphs (H2D), runs the step's iterations and reads them back (D2H)
+    host_graphs = graphs.copy()
+    Ke = min(K, 6)
+    ite = it0 + K * S + Kp
+    barrier()
+    t0 = time.perf_counter()
+    for i in range(Ke):
+        ctx.set_graphs(host_graphs)
+        ctx.run(iterations=ite + (i + 1) * S, first_iteration=ite + i * S, **run)
+        ctx.get_graphs(out=host_graphs)
+    e2e_t = allmax(time.perf_counter() - t0)
+    words = M * ((2 * (N - F) + 31) // 32)
+    e2e = {"value": Ke * S * C * world / e2e_t, "unit": UNIT, "h2d_bytes_per_step": 4 * words * C,
+           "d2h_bytes_per_step": 4 * words * C,
+           "path": f"sl_set_descent_graphs (packed on the host, pinned copy) + sl_run ({S} iterations of "
+                   f"{C} chains) + sl_get_descent_graphs per step, wall clock"}
+
+    extras = {}
+    if not args.skip_extras:
+        extras["cfg2"] = cfg2_rate(local, dist, dev)
+        extras["adjoint_cfg4"] = adjoint_rate(local)
+        extras["uneven_batch_cfg3"] = uneven_batch_rate(local, dist, dev)
+
+    if rank == 0:
+        out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
+               "ms_per_step": t_s * 1e3 / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+               "dtype": "f32 samplers (L-sampler, founder-allele graphs, meiosis filter) and f32 trait peel "
+                        "with power-of-two rescaling; f64 LOD log-sums",
+               "data": "synthetic (seeded generator, swiftlink_gb300/synth.py; no public dataset)",
+               "config": config(world), "impl": "ours",
+               "setup_s": round(setup_s, 1),
+               "timed_window": {"iterations": [it0, it0 + K * S], "scored_graphs": int(cnt_run),
+                                "steps_ms": [round(x, 2) for x in step_ms]},
+               "lod_positions_per_s": lod_pos_s * world,
+               "lod_kernel": {"selected": int(lsel), "specialised_compile_ms": round(ljit_ms, 1),
+                              "selection": "timed at the first scoring (SL_LOD_KERNEL_AUTO)"},
+               "ls_kernel": {"selected": "lsampler_kernel<float> (compact rfunctions)",
+                             "selection": "SL_LS_KERNEL_GENERIC: 32 or 16 lanes per (chain, locus) task, "
+                                          "timed before the first sweep"},
+               "plain": {"steps_per_s": plain_steps_s * world, "lod_positions_per_s": plain_lod_pos_s * world,
+                         "form": "one chain per launch, exact FP64 samplers, FP64 LOD peel with rescaling",
+                         "plain_fp64_positions_underflowed": plain_underflow},
+               "batched_vs_plain": {"steps": value / (plain_steps_s * world),
+                                    "lod_positions": lod_pos_s / plain_lod_pos_s},
+               "max_abs_dlod_fp32_vs_fp64_rescaled": dlod,
+               "gpu_launches": int(gpu_launches), "roofline": roofline, "clocks": clk, "e2e": e2e}
+        out.update(extras)
+        if world == 1:
+            out["cpu_baseline"] = cpu_baseline_sample(d, graphs, table32)
+        print(json.dumps(out))
+    for c in (ctx, pctx):
+        c.close()
+    if dist:
+        dist.destroy_process_group()
 
 
-def issue_estimate(C, it0, it1, seed, lprob, n_meioses, sm_mhz, sms, seconds):
-    """SM issue utilisation of timed run-graph launches on the 120-member,
-    2,000-SNP workload: the warp instructions of the L- and M-sweeps they ran
-    (each chain's L/M choice replayed with the same Philox draws; instructions
-    per sweep from the committed ncu summaries of this workload's kernels) over
-    the SMs' issue rate (4 schedulers per SM, one warp instruction per cycle
-    each, at the SM clock sampled during the launches)."""
-    from swiftlink_gb300 import philox
-    ls = inst_from_profiles("sl_ls_jit_cfg2.md")           # one half-sweep (1,000 loci) of 10 chains
-    fag = inst_from_profiles("fag_warp_kernel_cfg2.md")    # one meiosis step of one chain
-    scan = inst_from_profiles("ffbs_scan_kernel_cfg2.md")  # one meiosis step of one chain
-    if None in (ls, fag, scan) or not sm_mhz or not sms or seconds <= 0:
-        return None
-    c = np.arange(C, dtype=np.uint64)[:, None]
-    it = np.arange(it0, it1, dtype=np.uint64)[None, :]
-    hi = (c << np.uint64(40)) ^ (it << np.uint64(4)) ^ np.uint64(7)
-    n_l = int((philox.uniform(seed, hi, 0) < lprob).sum())
-    n_m = C * (it1 - it0) - n_l
-    per_l = 2 * ls / 10                                  # both halves, one chain
-    per_m = (n_meioses + 1) * fag + n_meioses * scan     # a reset launch, then a likelihood and a scan per meiosis
-    inst = n_l * per_l + n_m * per_m
-    peak = sms * 4 * sm_mhz * 1e6
-    return {"bound": "issue", "achieved": inst / seconds / 1e9, "peak": peak / 1e9, "unit": "G warp-inst/s",
-            "frac": inst / seconds / peak, "l_sweeps": n_l, "m_sweeps": n_m,
-            "warp_inst_per_l_sweep": per_l, "warp_inst_per_m_sweep": per_m,
-            "source": "instructions per launch: smsp__inst_executed.sum in profiles/sl_ls_jit_cfg2.md, "
-                      "fag_warp_kernel_cfg2.md, ffbs_scan_kernel_cfg2.md; the scoring launches are left out"}
+def cfg2_rate(device, dist, dev, C=10, K=10, S=20):
+    """The 120-member, 6-generation, 3-loop pedigree with 2,000 SNPs at 0.2 cM,
+    10 chains: chain-iterations/s of K run-graph launches of S iterations each
+    (CUDA events, L2 flushed), the L-sampler chosen by SL_LS_KERNEL_AUTO."""
+    import torch
+    from swiftlink_gb300 import api
+    from swiftlink_gb300.workloads import load_problem
+    d = load_problem("cfg2")
+    t = time.perf_counter()
+    ctx = api.Context(api.Problem.from_arrays(d, with_legal=False), n_chains=C, device=device,
+                      lod_precision=api.SL_LOD_FP32_RESCALED, sampler_precision=api.SL_SAMPLER_FAST,
+                      lod_flags=api.SL_LOD_ZERO_OK, ls_kernel=api.SL_LS_KERNEL_AUTO)
+    create_s = time.perf_counter() - t
+    ctx.set_graphs(np.stack([d["dg0"]] * C))
+    stream = torch.cuda.ExternalStream(ctx.stream_handle())
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
+    run = dict(burnin=0, period=PERIOD, lprob=LPROB, seed=SEED)
+    ctx.run(iterations=PERIOD, first_iteration=PERIOD - 3 * S, **run)
+    ctx.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+    for i in range(K):
+        with torch.cuda.stream(stream):
+            flush.fill_(i & 0xff)
+            ev[i][0].record(stream)
+        ctx.run(iterations=PERIOD + (i + 1) * S, first_iteration=PERIOD + i * S, **run)
+        with torch.cuda.stream(stream):
+            ev[i][1].record(stream)
+    ctx.synchronize()
+    ts = rank_max(sum(a.elapsed_time(b) for a, b in ev) / 1e3, dist, dev)
+    sel, ms = ctx.ls_kernel_info()
+    ctx.close()
+    return {"value": K * S * C / ts, "unit": "chain-steps/s per GPU", "chains": C, "iterations_timed": K * S,
+            "ls_kernel": "specialised (sl_ls_jit)" if sel == api.SL_LS_KERNEL_SPECIALISED else "generic",
+            "ls_compile_ms": round(ms, 1), "context_create_s": round(create_s, 1)}
 
 
-def traffic_from_profiles(kernel):
-    """DRAM bytes per launch from the committed ncu summary, if one exists."""
-    path = os.path.join(ROOT, "profiles", "traffic.md")
-    if not os.path.exists(path):
-        return None
-    for line in open(path):
-        if line.startswith("|") and kernel in line:
-            cells = [c.strip() for c in line.strip().strip("|").split("|")]
-            try:
-                return float(cells[-1])
-            except ValueError:
-                return None
-    return None
+def adjoint_rate(device, G=1000, chunk=250):
+    """The trait-peel adjoint on the 120-member, 2,000-SNP pedigree under the
+    dominant model (0.01, 0.8, 0.9), q = 1e-3: 1,000 stored graphs (10 chains'
+    graphs after 5 MCMC iterations, repeated) x 9,995 positions through
+    sl_trait_backward with host graphs in and host gradients out, in chunks
+    of 250 graphs; wall clock."""
+    from swiftlink_gb300 import api
+    from swiftlink_gb300.workloads import disease_probs, load_problem
+    d = load_problem("cfg2")
+    pen, q = (0.01, 0.8, 0.9), 1e-3
+    dd = dict(d, penetrance=np.array(pen), freq=np.float64(q),
+              disease_prob=disease_probs(d["affection"], d["mother"] < 0, q, pen))
+    prob = api.Problem.from_arrays(dd, with_legal=False)
+    with api.Context(prob, n_chains=10, device=device, sampler_precision=api.SL_SAMPLER_FAST,
+                     lod_precision=api.SL_LOD_FP32_RESCALED, lod_flags=api.SL_LOD_ZERO_OK) as sctx:
+        sctx.set_graphs(np.stack([d["dg0"]] * 10))
+        sctx.run(iterations=5, burnin=0, period=1 << 30, lprob=LPROB, seed=SEED)
+        base = sctx.get_graphs()
+    gset = np.stack([base[i % 10] for i in range(chunk)])
+    npos = (d["M"] - 1) * d["n_lod"]
+    with api.Context(prob, n_chains=1, device=device, lod_precision=api.SL_LOD_FP32_RESCALED,
+                     lod_flags=api.SL_LOD_ZERO_OK) as ctx:
+        segs, used = ctx.adjoint_memory()
+        ctx.trait_backward(gset[:10])
+        t = time.perf_counter()
+        done = 0
+        while done < G:
+            grad, pt = ctx.trait_backward(gset[:min(chunk, G - done)])
+            done += min(chunk, G - done)
+        dt = time.perf_counter() - t
+        # the forward FP32 scorer on the same graphs, for the ratio
+        ctx.lod_score_graphs(gset)
+        ctx.synchronize()
+        t = time.perf_counter()
+        ctx.lod_score_graphs(gset)
+        ctx.synchronize()
+        fwd = chunk * npos / (time.perf_counter() - t)
+    return {"value": G * npos / dt, "unit": "positions/s", "graphs": G, "positions_per_graph": npos,
+            "forward_fp32_positions_per_s": fwd, "adjoint_segments": segs, "shared_bytes_per_warp": used,
+            "model": "dominant (0.01, 0.8, 0.9), q = 1e-3",
+            "path": "sl_trait_backward: host graphs in, d log L / d (theta_L, theta_R, penetrances, q) out"}
+
+
+def uneven_batch_rate(device, dist, dev, n_ped=64, chains=8, K=20):
+    """Chain-steps/s of the uneven batch: 64 seeded pedigrees of 20-150
+    members (0-4 loops, 1,000 SNPs at 0.5 cM), 8 MC3 chains each at
+    temperatures 0.3^(j/7), fast samplers, FP32 LOD (the slot-program
+    interpreter: no per-pedigree compilation), exchange and scoring every 10
+    iterations: all pedigrees, spurts and exchanges in one graph launch."""
+    import torch
+    from swiftlink_gb300 import api, pedigree, synth
+    t0 = time.perf_counter()
+    probs = [pedigree.problem_from_workload(w) for w in synth.uneven_batch(n_ped)]
+    temps = [0.3 ** (j / 7) for j in range(chains)]
+    ctxs = []
+    for pd in probs:
+        ctx = api.Context(api.Problem.from_arrays(pd, with_legal=False), n_chains=chains, device=device,
+                          lod_precision=api.SL_LOD_FP32_RESCALED, sampler_precision=api.SL_SAMPLER_FAST,
+                          lod_flags=api.SL_LOD_ZERO_OK, lod_kernel=api.SL_LOD_KERNEL_INTERP)
+        ctx.set_temperatures(temps)
+        ctx.set_graphs(np.stack([pd["dg0"]] * chains))
+        ctxs.append(ctx)
+    setup_s = time.perf_counter() - t0
+    opts = dict(burnin=0, period=10, lprob=LPROB, seed=SEED, exchange_period=10)
+    with api.Batch(ctxs) as b:
+        b.run(iterations=10, **opts)                      # builds the graph, warms up
+        for c in ctxs:
+            c.synchronize()
+        launches0 = sum(c.launches for c in ctxs)
+        t = time.perf_counter()
+        b.run(iterations=10 + K, first_iteration=10, **opts)
+        for c in ctxs:
+            c.synchronize()
+        dt = rank_max(time.perf_counter() - t, dist, dev)
+    acc = sum(int(c.mc3_stats()[0].sum()) for c in ctxs)
+    prop = sum(int(c.mc3_stats()[1].sum()) for c in ctxs)
+    sizes = [pd["N"] for pd in probs]
+    for c in ctxs:
+        c.close()
+    return {"value": K * chains * n_ped / dt, "unit": "chain-steps/s", "pedigrees": n_ped,
+            "chains_per_pedigree": chains, "members": [min(sizes), max(sizes)], "markers": 1000,
+            "iterations_timed": K, "exchanges_accepted": acc, "exchanges_proposed": prop,
+            "setup_s": round(setup_s, 1),
+            "timing": "wall clock around one sl_batch_run (one graph launch: every pedigree's spurts and MC3 "
+                      "exchanges on the device) + synchronize"}
 
 
 def main():
