@@ -165,6 +165,7 @@ struct sl_ctx {
     bool has_adjoint = false;
     AdjDev adj{};
     std::vector<OpDev> adj_ops;       // host copies the plan is built from
+    std::vector<int32_t> adj_od;      // their opdata
     std::vector<int32_t> adj_prev;    // [K+1] CSR offsets and the previous ops, for the plan's consumers
     std::vector<int32_t> adj_prevs;
     size_t adj_budget = 0;            // shared bytes per warp the plan must fit (0: the default)
@@ -1598,6 +1599,7 @@ int sl_create(const sl_problem_desc* d, const sl_options* opt, sl_ctx** out) {
             if ((rc = upload(ctx, (float**)&D.dprob, dpf.data(), dpf.size()))) return bail(rc);
             if ((rc = upload(ctx, (float**)&D.dgrad, dgr.data(), dgr.size()))) return bail(rc);
             ctx->adj_ops = ops;
+            ctx->adj_od = od;
             ctx->adj_prev.assign(d->prev_off, d->prev_off + K + 1);
             ctx->adj_prevs.assign(d->prev, d->prev + d->prev_off[K]);
             if ((rc = plan_adjoint(ctx))) return bail(rc);
@@ -2202,7 +2204,7 @@ static int plan_adjoint(sl_ctx* ctx) {
             segn = std::max(segn, o);
         }
         p.half = perm + segn;
-        p.bytes = (size_t)(8 * p.half + 4 * (K + ctx->P.max_child) + 15) & ~(size_t)15;
+        p.bytes = (size_t)(8 * p.half + 4 * (K + ctx->P.max_child) + 48 * ctx->P.max_child + 15) & ~(size_t)15;
         return p;
     };
     const size_t budget = ctx->adj_budget ? ctx->adj_budget : kAdjDefaultBudget;
@@ -2215,15 +2217,68 @@ static int plan_adjoint(sl_ctx* ctx) {
         }
     if (best.bytes > kSmemBudget)
         return fail(nullptr, SL_EINVAL, "the trait-peel adjoint needs %zu shared bytes per task", best.bytes);
+    // the items of every op under this plan's arena offsets (the gathers of
+    // TraitRfunction's peel, trait_rfunction.cc:28-137: the peel node's state,
+    // each child's matching transmissions, each previous rfunction's cell)
+    std::vector<uint32_t> items;
+    std::vector<int32_t> item_at(K);
+    {
+        const std::vector<int32_t>& od = ctx->adj_od;
+        auto dig = [](int ext, int pos) { return (ext >> (2 * pos)) & 3; };
+        for (int k = 0; k < K; ++k) {
+            const OpDev& op = ops[k];
+            item_at[k] = (int32_t)items.size();
+            const int nw = adj_item_words(op.n_prev, op.n_child);
+            const int ncell = 1 << (2 * op.c);
+            for (int cell = 0; cell < ncell; ++cell)
+                for (int t = 0; t < 4; ++t) {
+                    std::vector<uint32_t> w(nw, 0u);
+                    int s;
+                    if (op.type == CHILD) s = phased_trait_host(dig(cell, op.mpos), dig(cell, op.fpos), t >> 1, t & 1);
+                    else s = t;
+                    const int ext = cell | (s << (2 * op.c));
+                    w[0] = (uint32_t)s;
+                    if (op.type == PARENT) {
+                        int mt = t, pt = t;
+                        for (int c = 0; c < op.n_child; ++c) {
+                            const int32_t* cd = od.data() + op.child_at + 4 * c;
+                            const int kt = dig(ext, cd[1]), other = dig(ext, cd[2]);
+                            if (cd[3]) pt = other; else mt = other;
+                            uint32_t mask = 0;
+                            for (int i = 0; i < 2; ++i)
+                                for (int j = 0; j < 2; ++j)
+                                    if (phased_trait_host(mt, pt, i, j) == kt) mask |= 1u << (2 * i + j);
+                            if (c < 7) w[0] |= mask << (2 + 4 * c);
+                            else w[1 + (op.n_prev + 1) / 2 + (c - 7) / 8] |= mask << (4 * ((c - 7) % 8));
+                        }
+                    }
+                    const int32_t* pd = od.data() + op.prev_at;
+                    const int32_t* po = od.data() + op.prev_ops_at;
+                    for (int j = 0; j < op.n_prev; ++j) {
+                        int idx = 0;
+                        for (int q = 0; q < pd[1]; ++q) idx |= dig(ext, pd[2 + q]) << (2 * q);
+                        const uint32_t off = (uint32_t)(best.aoff[po[j]] + idx);
+                        w[1 + j / 2] |= off << (16 * (j & 1));
+                        pd += 2 + pd[1];
+                    }
+                    items.insert(items.end(), w.begin(), w.end());
+                }
+        }
+    }
+    if (best.half > 65535) return fail(nullptr, SL_EINVAL, "the trait-peel adjoint's arena exceeds 16-bit offsets");
     AdjDev& D = ctx->adj;
     int rc;
-    for (void* p : {(void*)D.aoff, (void*)D.seg, (void*)D.keep}) {
+    for (void* p : {(void*)D.aoff, (void*)D.seg, (void*)D.keep, (void*)D.items, (void*)D.item_at}) {
         if (!p) continue;
         cudaFree(p);
         ctx->owned.erase(std::find(ctx->owned.begin(), ctx->owned.end(), p));
     }
     D.aoff = D.seg = nullptr;
     D.keep = nullptr;
+    D.items = nullptr;
+    D.item_at = nullptr;
+    if ((rc = upload(ctx, (uint32_t**)&D.items, items.data(), items.size()))) return rc;
+    if ((rc = upload(ctx, (int32_t**)&D.item_at, item_at.data(), item_at.size()))) return rc;
     if ((rc = upload(ctx, (int32_t**)&D.aoff, best.aoff.data(), best.aoff.size()))) return rc;
     if ((rc = upload(ctx, (int32_t**)&D.seg, best.seg.data(), best.seg.size()))) return rc;
     if ((rc = upload(ctx, (uint8_t**)&D.keep, best.keep.data(), best.keep.size()))) return rc;

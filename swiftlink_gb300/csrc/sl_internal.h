@@ -108,10 +108,22 @@ struct AdjDev {
     const uint8_t* keep;     // [K] 1 when the first forward pass's matrix stays in place
     const float* dprob;      // [N][4] disease probabilities (person.cc:85-119), FP32
     const float4* dgrad;     // [N][4] their derivatives by (pen HOMO_U, pen HETERO, pen HOMO_A, frequency)
+    // every op's (cell, term) items, cell-major (item = 4 cell + term): word 0 the peel node's state
+    // (bits 0-1) and, for a parent peel, each child's transmission mask (4 bits per child from bit 2,
+    // children 7 on in the words after the offsets, 8 per word); then the arena offsets of the item's
+    // factors in the previous rfunctions, two 16-bit offsets per word.  The same for every task.
+    const uint32_t* items;
+    const int32_t* item_at;  // [K] first word of op k's items
     int32_t nseg;
     int32_t half;            // floats of the matrices (the adjoints take as many)
-    int32_t warp_bytes;      // shared bytes of one warp: matrices, adjoints, exponents [K], child bits
+    int32_t warp_bytes;      // shared bytes of one warp: matrices, adjoints, exponents [K], child bits,
+                             // recombination terms [12 max_child]
 };
+
+// Words per item of op k in AdjDev::items.
+__host__ __device__ inline int adj_item_words(int n_prev, int n_child) {
+    return 1 + (n_prev + 1) / 2 + (n_child > 7 ? (n_child - 7 + 7) / 8 : 0);
+}
 
 // Options of a device-driven run, read by the run graph's kernels.
 struct RunParams {

@@ -1358,7 +1358,10 @@ __device__ __forceinline__ void fagw_task(const ProblemDev& P, const FagwTables&
         }
         __syncwarp();
     }
-    // 2. used / fixed founder alleles
+    // 2. fixed founder alleles: the homozygous typed members (after the
+    // heterozygotes in the list) mark theirs with the colour their genotype
+    // forces (no warp primitive inside: the groups' loci have lists of their
+    // own lengths)
     for (int x = gl; x < nfa; x += G) {
         Lb[x] = x << 1;
         fl[x] = 0;
@@ -1366,22 +1369,12 @@ __device__ __forceinline__ void fagw_task(const ProblemDev& P, const FagwTables&
     }
     cp_async_wait_all();   // this lane's copies of the list; the barrier makes the group's visible
     __syncwarp();
-    // the typed members mark their founder alleles (no warp primitive inside:
-    // the groups' loci have lists of their own lengths)
-    int bad = 0;
-    for (int x = gl; x < ntyp; x += G) {
+    for (int x = nhet + gl; x < ntyp; x += G) {
         const int ent = typ[x], i = ent >> 2, g = ent & 3;
-        const int u = e[2 * i], v = e[2 * i + 1];
-        int bits = 1;
-        if (g == G_HETERO) {
-            if (u == v) bad = 1;
-        } else {
-            bits |= g == G_HOMOZ_A ? 2 : 4;
-        }
-        atomicOr(&fl[u], bits);
-        atomicOr(&fl[v], bits);
+        const int bits = g == G_HOMOZ_A ? 3 : 5;   // used, fixed A / fixed B
+        atomicOr(&fl[e[2 * i]], bits);
+        atomicOr(&fl[e[2 * i + 1]], bits);
     }
-    bad = grp.any(bad);
     __syncwarp();
     // 3. components of the heterozygote edges with parities: a lock-free
     // union-find forest in Lb (2 * parent + parity to the parent), each lane
@@ -1389,27 +1382,40 @@ __device__ __forceinline__ void fagw_task(const ProblemDev& P, const FagwTables&
     // compare-and-swap (so a root is its component's smallest allele); an edge
     // whose ends already share a root must have ends of opposite parity.  A
     // failed hook means another lane's hook succeeded, so a lane retries fewer
-    // than 2F times.
-    const bool unite = !bad && nhet > 0;
-    if (unite) {
-        for (int q = gl; q < nhet; q += G) {
-            const int i = typ[q] >> 2;   // the heterozygotes lead the list
-            const int u = e[2 * i], v = e[2 * i + 1];
-            for (int tries = 0;; ++tries) {
-                if (tries > nfa) {
-                    bad = 1;
-                    set_status(status, ST_ILLEGAL_DG);
-                    break;
-                }
-                int pu, pv;
-                const int ru = pf_find(Lb, u, pu), rv = pf_find(Lb, v, pv);
-                if (ru == rv) {
-                    if ((pu ^ pv) != 1) bad = 1;   // an odd cycle of heterozygote edges
-                    break;
-                }
-                const int lo = min(ru, rv), hi = max(ru, rv);
-                if (atomicCAS((int*)&Lb[hi], hi << 1, (lo << 1) | (pu ^ pv ^ 1)) == (hi << 1)) break;
+    // than 2F times.  An edge whose two ends are both fixed only needs their
+    // colours to differ: the two sides' colourings are then determined apart,
+    // and the likelihood is the product of the two sides' terms, so the edge
+    // joins nothing.  The ends of the other edges are marked used and joined
+    // (bit 3: in the forest).
+    int bad = 0;
+    for (int q = gl; q < nhet; q += G) {
+        const int i = typ[q] >> 2;   // the heterozygotes lead the list
+        const int u = e[2 * i], v = e[2 * i + 1];
+        if (u == v) {   // one founder allele cannot give both alleles of a heterozygote
+            bad = 1;
+            continue;
+        }
+        const int fu = fl[u], fv = fl[v];
+        if ((fu & 6) && (fv & 6)) {
+            if (fu & fv & 6) bad = 1;   // both ends forced to the same colour
+            continue;
+        }
+        atomicOr(&fl[u], 9);
+        atomicOr(&fl[v], 9);
+        for (int tries = 0;; ++tries) {
+            if (tries > nfa) {
+                bad = 1;
+                set_status(status, ST_ILLEGAL_DG);
+                break;
             }
+            int pu, pv;
+            const int ru = pf_find(Lb, u, pu), rv = pf_find(Lb, v, pv);
+            if (ru == rv) {
+                if ((pu ^ pv) != 1) bad = 1;   // an odd cycle of heterozygote edges
+                break;
+            }
+            const int lo = min(ru, rv), hi = max(ru, rv);
+            if (atomicCAS((int*)&Lb[hi], hi << 1, (lo << 1) | (pu ^ pv ^ 1)) == (hi << 1)) break;
         }
     }
     bad = grp.any(bad);
@@ -1418,13 +1424,22 @@ __device__ __forceinline__ void fagw_task(const ProblemDev& P, const FagwTables&
     // contributes log2 of the major or the minor frequency, so a component
     // needs only its member count, how many members have even parity and
     // which colourings its fixed members forbid (integer shared-memory
-    // atomics, the same result in any order)
+    // atomics, the same result in any order).  A fixed allele outside the
+    // forest is a component of its own: its term is added directly.
+    float sum = 0.f;
+    int zero = 0;
+    const float lmaj = lfreq.x, lmin = lfreq.y;
     if (!bad)
         for (int x = gl; x < nfa; x += G) {
             const int f = fl[x];
             if (!(f & 1)) continue;
+            if (!(f & 8)) {
+                if ((f & 6) == 6) zero = 1;
+                else sum += (f & 2) ? lmaj : lmin;
+                continue;
+            }
             int p = 0;
-            const int r = unite ? pf_find(Lb, x, p) : x;   // the forest is final: the unions are done
+            const int r = pf_find(Lb, x, p);   // the forest is final: the unions are done
             // bit 16 + n: member count; bits 0-15: even-parity members; bits 29/30: colouring 0/1 forbidden
             const int add = (1 << 16) + (p ? 0 : 1);
             int forbid = 0;
@@ -1434,10 +1449,7 @@ __device__ __forceinline__ void fagw_task(const ProblemDev& P, const FagwTables&
             if (forbid) atomicOr(&cnt[r], forbid);
         }
     __syncwarp();
-    float sum = 0.f;
-    int zero = 0;
     if (!bad) {
-        const float lmaj = lfreq.x, lmin = lfreq.y;
         for (int x = gl; x < nfa; x += G) {
             const int c = cnt[x];
             const int n = (c >> 16) & 0x1fff, even = c & 0xffff;
@@ -2216,123 +2228,91 @@ __device__ __forceinline__ void adj_rec(const AdjTask& T, int bits, int i, int j
     dr = 0.25f * (x0 * s1 * x2 * x3 + x0 * x1 * x2 * s3);
 }
 
-// Op k's constants, worked out once per op by every lane: each previous
-// rfunction's arena offset, key count and key positions (4 bits each), and
-// the graph bits of a child peel's child.
-struct AdjOp {
-    OpDev op;
-    int n;
-    int base[kAdjMaxPrev], nk[kAdjMaxPrev], keys[kAdjMaxPrev];
-    int cbits;
-};
-
-__device__ __forceinline__ void adj_op(const ProblemDev& P, const AdjDev& D, const AdjTask& T, int k, AdjOp& o) {
-    o.op = P.ops[k];
-    const int32_t* pd = P.opdata + o.op.prev_at;
-    const int32_t* po = P.opdata + o.op.prev_ops_at;
-    o.n = o.op.n_prev;
-#pragma unroll
-    for (int j = 0; j < kAdjMaxPrev; ++j) {
-        o.base[j] = o.nk[j] = o.keys[j] = 0;
-        if (j < o.n) {
-            o.base[j] = D.aoff[po[j]];
-            o.nk[j] = pd[1];
-            int kk = 0;
-            for (int q = 0; q < pd[1]; ++q) kk |= pd[2 + q] << (4 * q);
-            o.keys[j] = kk;
-            pd += 2 + pd[1];
-        }
+// Op k's recombination terms at this task, for a child peel its child's and
+// for a parent peel each child's: for (i, j) = 2i + j, 0.25 x the term and its
+// derivatives by theta_L and theta_R at rt[12 c + b], rt[12 c + 4 + b],
+// rt[12 c + 8 + b] (the warp's scratch; its items read them).
+__device__ __forceinline__ void adj_rtab(const ProblemDev& P, const AdjTask& T, const OpDev& op, float* rt, int lane) {
+    const int nch = op.type == CHILD ? 1 : (op.type == PARENT ? op.n_child : 0);
+    for (int q = lane; q < 4 * nch; q += 32) {
+        const int c = q >> 2, b = q & 3;
+        const int child = op.type == CHILD ? op.peel : P.opdata[op.child_at + 4 * c];
+        const int bits = T.graph ? person_bits(P, T.colL, T.colR, child) : 0;
+        float r, dl, dr;
+        adj_rec(T, bits, b >> 1, b & 1, r, dl, dr);
+        rt[12 * c + b] = r;
+        rt[12 * c + 4 + b] = dl;
+        rt[12 * c + 8 + b] = dr;
     }
-    o.cbits = (o.op.type == CHILD && T.graph) ? person_bits(P, T.colL, T.colR, o.op.peel) : 0;
-}
-
-// One item of op k: the peel node's state s, the product R of the
-// recombination factors with its derivatives, and the previous rfunctions'
-// cells (arena offsets).
-struct AdjItem {
-    int s;
-    float R, dRl, dRr;
-    int idx[kAdjMaxPrev];
-};
-
-__device__ __forceinline__ void adj_item(const ProblemDev& P, const AdjTask& T, const AdjOp& o, const int* chbits,
-                                         int cell, int t, AdjItem& it) {
-    const OpDev& op = o.op;
-    int ext;
-    it.R = 1.f;
-    it.dRl = it.dRr = 0.f;
-    if (op.type == CHILD) {
-        const int i = t >> 1, j = t & 1;
-        it.s = phased_trait(digit(cell, op.mpos), digit(cell, op.fpos), i, j);
-        adj_rec(T, o.cbits, i, j, it.R, it.dRl, it.dRr);
-        ext = cell | (it.s << (2 * op.c));
-    } else {
-        it.s = t;
-        ext = cell | (t << (2 * op.c));
-        if (op.type == PARENT) {
-            // the product over children of the summed matching transmissions,
-            // its derivatives by the product rule as it is built
-            int mt = t, pt = t;
-            const int32_t* cd = P.opdata + op.child_at;
-            for (int c = 0; c < op.n_child; ++c, cd += 4) {
-                const int kt = digit(ext, cd[1]), other = digit(ext, cd[2]);
-                if (cd[3]) pt = other; else mt = other;
-                const int bits = chbits[c];
-                float sc = 0.f, sl = 0.f, sr = 0.f;
-                for (int i = 0; i < 2; ++i)
-                    for (int j = 0; j < 2; ++j) {
-                        if (phased_trait(mt, pt, i, j) != kt) continue;
-                        float r, dl, dr;
-                        adj_rec(T, bits, i, j, r, dl, dr);
-                        sc += r;
-                        sl += dl;
-                        sr += dr;
-                    }
-                it.dRl = it.dRl * sc + it.R * sl;
-                it.dRr = it.dRr * sc + it.R * sr;
-                it.R *= sc;
-            }
-        }
-    }
-#pragma unroll
-    for (int j = 0; j < kAdjMaxPrev; ++j) {
-        int idx = 0;
-        if (j < o.n)
-            for (int q = 0; q < o.nk[j]; ++q) idx |= digit(ext, (o.keys[j] >> (4 * q)) & 15) << (2 * q);
-        it.idx[j] = o.base[j] + idx;
-    }
-}
-
-// The graph bits of a parent peel's children, into the warp's scratch.
-__device__ __forceinline__ void adj_child_bits(const ProblemDev& P, const AdjTask& T, const AdjOp& o, int* chbits,
-                                               int lane) {
-    if (o.op.type != PARENT) return;
-    for (int c = lane; c < o.op.n_child; c += 32)
-        chbits[c] = T.graph ? person_bits(P, T.colL, T.colR, P.opdata[o.op.child_at + 4 * c]) : 0;
     __syncwarp();
 }
 
-// Forward of op k: its scaled matrix in A, its exponent in E[k].
-__device__ void adj_forward(const ProblemDev& P, const AdjDev& D, const AdjTask& T, int k, float* A, int* E,
-                            int* chbits, int lane) {
-    AdjOp o;
-    adj_op(P, D, T, k, o);
-    adj_child_bits(P, T, o, chbits, lane);
-    const int ncell = 1 << (2 * o.op.c), nitem = 4 * ncell;
+// Child c's transmission mask of an item of a parent peel (AdjDev::items).
+__device__ __forceinline__ uint32_t adj_mask(const uint32_t* w, int pw, int c) {
+    return c < 7 ? (w[0] >> (2 + 4 * c)) & 15u : (w[1 + pw + (c - 7) / 8] >> (4 * ((c - 7) % 8))) & 15u;
+}
+
+// The item's product of recombination factors (and, with D, its derivatives
+// by theta_L and theta_R by the product rule as it is built): a child peel's
+// one term, a parent peel's per-child sums of the transmissions its mask
+// lets through, in transmission order.
+template <bool D>
+__device__ __forceinline__ void adj_R(const OpDev& op, const uint32_t* w, int pw, int t, const float* rt, float& R,
+                                      float& dRl, float& dRr) {
+    R = 1.f;
+    dRl = dRr = 0.f;
+    if (op.type == CHILD) {
+        R = rt[t];
+        if (D) {
+            dRl = rt[4 + t];
+            dRr = rt[8 + t];
+        }
+    } else if (op.type == PARENT) {
+        for (int c = 0; c < op.n_child; ++c) {
+            const uint32_t mask = adj_mask(w, pw, c);
+            float sc = 0.f, sl = 0.f, sr = 0.f;
+#pragma unroll
+            for (int b = 0; b < 4; ++b)
+                if (mask & (1u << b)) {
+                    sc += rt[12 * c + b];
+                    if (D) {
+                        sl += rt[12 * c + 4 + b];
+                        sr += rt[12 * c + 8 + b];
+                    }
+                }
+            if (D) {
+                dRl = dRl * sc + R * sl;
+                dRr = dRr * sc + R * sr;
+            }
+            R *= sc;
+        }
+    }
+}
+
+// Forward of op k: its scaled matrix in A, its exponent in E[k].  One item
+// per lane: the peel node's disease probability times the previous
+// rfunctions' cells times the recombination factors; the four items of a
+// cell added by shuffles.
+__device__ void adj_forward(const ProblemDev& P, const AdjDev& D, const AdjTask& T, int k, float* A, int* E, float* rt,
+                            int lane) {
+    const OpDev op = P.ops[k];
+    adj_rtab(P, T, op, rt, lane);
+    const int ncell = 1 << (2 * op.c), nitem = 4 * ncell;
+    const int nw = adj_item_words(op.n_prev, op.n_child), pw = (op.n_prev + 1) / 2;
+    const uint32_t* tab = D.items + D.item_at[k];
     float* out = A + D.aoff[k];
-    const float* dp = D.dprob + 4 * o.op.peel;
+    const float* dp = D.dprob + 4 * op.peel;
     float mx = 0.f;
     for (int it0 = 0; it0 < nitem; it0 += 32) {
         const int item = it0 + lane, cell = item >> 2, t = item & 3;
         float term = 0.f;
         if (item < nitem) {
-            AdjItem it;
-            adj_item(P, T, o, chbits, cell, t, it);
-            term = dp[it.s];
-#pragma unroll
-            for (int j = 0; j < kAdjMaxPrev; ++j)
-                if (j < o.n) term *= A[it.idx[j]];
-            term *= it.R;
+            const uint32_t* w = tab + (size_t)item * nw;
+            term = dp[w[0] & 3u];
+            for (int j = 0; j < op.n_prev; ++j) term *= A[(w[1 + (j >> 1)] >> (16 * (j & 1))) & 0xffffu];
+            float R, dl, dr;
+            adj_R<false>(op, w, pw, t, rt, R, dl, dr);
+            term *= R;
         }
         const int grp = lane & ~3;
         const float t0 = __shfl_sync(FULLMASK, term, grp), t1 = __shfl_sync(FULLMASK, term, grp + 1);
@@ -2344,7 +2324,7 @@ __device__ void adj_forward(const ProblemDev& P, const AdjDev& D, const AdjTask&
         }
     }
     for (int dd = 16; dd >= 1; dd >>= 1) mx = fmaxf(mx, __shfl_xor_sync(FULLMASK, mx, dd));
-    const int e = mx > 0.f ? ilogbf(mx) - o.op.scale_to : 0;
+    const int e = mx > 0.f ? ilogbf(mx) - op.scale_to : 0;
     __syncwarp();
     for (int cell = lane; cell < ncell; cell += 32) out[cell] = ldexpf(out[cell], -e);
     if (lane == 0) E[k] = e;
@@ -2354,14 +2334,15 @@ __device__ void adj_forward(const ProblemDev& P, const AdjDev& D, const AdjTask&
 // Reverse of op k: adjoints into the previous rfunctions' cells (B), the
 // model derivatives into g.
 __device__ void adj_reverse(const ProblemDev& P, const AdjDev& D, const AdjTask& T, int k, const float* A, float* B,
-                            const int* E, int* chbits, int lane, double* g) {
-    AdjOp o;
-    adj_op(P, D, T, k, o);
-    adj_child_bits(P, T, o, chbits, lane);
-    const int ncell = 1 << (2 * o.op.c), nitem = 4 * ncell;
+                            const int* E, float* rt, int lane, double* g) {
+    const OpDev op = P.ops[k];
+    adj_rtab(P, T, op, rt, lane);
+    const int ncell = 1 << (2 * op.c), nitem = 4 * ncell;
+    const int nw = adj_item_words(op.n_prev, op.n_child), pw = (op.n_prev + 1) / 2;
+    const uint32_t* tab = D.items + D.item_at[k];
     const float* bk = B + D.aoff[k];
-    const float* dp = D.dprob + 4 * o.op.peel;
-    const float4* dg = D.dgrad + 4 * o.op.peel;
+    const float* dp = D.dprob + 4 * op.peel;
+    const float4* dg = D.dgrad + 4 * op.peel;
     const int e = E[k];
     float gl = 0.f, gr = 0.f, g0 = 0.f, g1 = 0.f, g2 = 0.f, g3 = 0.f;
     for (int it0 = 0; it0 < nitem; it0 += 32) {
@@ -2369,27 +2350,31 @@ __device__ void adj_reverse(const ProblemDev& P, const AdjDev& D, const AdjTask&
         if (item >= nitem) break;
         const float gd = ldexpf(bk[cell], -e);   // the adjoint of the cell before its scaling
         if (gd == 0.f) continue;
-        AdjItem it;
-        adj_item(P, T, o, chbits, cell, t, it);
+        const uint32_t* w = tab + (size_t)item * nw;
+        const int s = (int)(w[0] & 3u);
         float a[kAdjMaxPrev];
+        int off[kAdjMaxPrev];
         float pp = 1.f;
 #pragma unroll
         for (int j = 0; j < kAdjMaxPrev; ++j) {
-            a[j] = j < o.n ? A[it.idx[j]] : 1.f;
+            off[j] = j < op.n_prev ? (int)((w[1 + (j >> 1)] >> (16 * (j & 1))) & 0xffffu) : 0;
+            a[j] = j < op.n_prev ? A[off[j]] : 1.f;
             pp *= a[j];
         }
-        const float c = dp[it.s];
-        const float w = gd * pp;
-        const float4 dc = dg[it.s];
-        g0 += w * it.R * dc.x;
-        g1 += w * it.R * dc.y;
-        g2 += w * it.R * dc.z;
-        g3 += w * it.R * dc.w;
-        gl += w * c * it.dRl;
-        gr += w * c * it.dRr;
+        float R, dRl, dRr;
+        adj_R<true>(op, w, pw, t, rt, R, dRl, dRr);
+        const float c = dp[s];
+        const float wgt = gd * pp;
+        const float4 dc = dg[s];
+        g0 += wgt * R * dc.x;
+        g1 += wgt * R * dc.y;
+        g2 += wgt * R * dc.z;
+        g3 += wgt * R * dc.w;
+        gl += wgt * c * dRl;
+        gr += wgt * c * dRr;
         // each factor's adjoint: the product of the others, by prefix and suffix products
         float pre[kAdjMaxPrev];
-        float run = gd * c * it.R;
+        float run = gd * c * R;
 #pragma unroll
         for (int j = 0; j < kAdjMaxPrev; ++j) {
             pre[j] = run;
@@ -2398,9 +2383,9 @@ __device__ void adj_reverse(const ProblemDev& P, const AdjDev& D, const AdjTask&
         float suf = 1.f;
 #pragma unroll
         for (int j = kAdjMaxPrev - 1; j >= 0; --j) {
-            if (j < o.n) {
+            if (j < op.n_prev) {
                 const float v = pre[j] * suf;
-                if (v != 0.f) atomicAdd(B + it.idx[j], v);
+                if (v != 0.f) atomicAdd(B + off[j], v);
             }
             suf *= a[j];
         }
@@ -2422,7 +2407,7 @@ __global__ void __launch_bounds__(128) trait_adjoint_kernel(ProblemDev P, AdjDev
     float* A = (float*)(smem + (size_t)warp * D.warp_bytes);
     float* B = A + D.half;
     int* E = (int*)(B + D.half);
-    int* chbits = E + P.K;   // [max_child] a parent peel's children's graph bits
+    float* rt = (float*)(E + P.K);   // [12 max_child] the op's recombination terms
     const int n = P.n_lod;
     const int64_t npos = (int64_t)(P.M - 1) * n;
     for (int64_t u = (int64_t)blockIdx.x * wpb + warp; u < ntask; u += (int64_t)gridDim.x * wpb) {
@@ -2443,7 +2428,7 @@ __global__ void __launch_bounds__(128) trait_adjoint_kernel(ProblemDev P, AdjDev
             T.an2 = 1.f - T.th2;
         }
         // first forward pass: every op; matrices not kept are overwritten by later segments
-        for (int k = 0; k < P.K; ++k) adj_forward(P, D, T, k, A, E, chbits, lane);
+        for (int k = 0; k < P.K; ++k) adj_forward(P, D, T, k, A, E, rt, lane);
         const float root = A[D.aoff[P.K - 1]];
         double g[6] = {0, 0, 0, 0, 0, 0};
         if (!(root > 0.f)) {
@@ -2461,7 +2446,7 @@ __global__ void __launch_bounds__(128) trait_adjoint_kernel(ProblemDev P, AdjDev
             if (sg < D.nseg - 1) {
                 // recompute the segment's matrices that were not kept, zero their adjoints
                 for (int k = k0; k < k1; ++k)
-                    if (!D.keep[k]) adj_forward(P, D, T, k, A, E, chbits, lane);
+                    if (!D.keep[k]) adj_forward(P, D, T, k, A, E, rt, lane);
                 for (int k = k0; k < k1; ++k)
                     if (!D.keep[k])
                         for (int i = lane; i < (1 << (2 * P.ops[k].c)); i += 32) B[D.aoff[k] + i] = 0.f;
@@ -2470,7 +2455,7 @@ __global__ void __launch_bounds__(128) trait_adjoint_kernel(ProblemDev P, AdjDev
                 B[D.aoff[P.K - 1]] = 1.0f / root;
             }
             __syncwarp();
-            for (int k = k1 - 1; k >= k0; --k) adj_reverse(P, D, T, k, A, B, E, chbits, lane, g);
+            for (int k = k1 - 1; k >= k0; --k) adj_reverse(P, D, T, k, A, B, E, rt, lane, g);
         }
         for (int q = 0; q < 6; ++q) {
             double v = g[q];
@@ -3008,7 +2993,9 @@ static cudaError_t launch_msampler_t(const ProblemDev& P, uint32_t* dg, int firs
     // in log2 (component counts are 13-bit fields)
     // two loci per warp (16 lanes each: 17% fewer instructions per locus, 30%
     // longer per launch) when the caller asks for throughput and a column
-    // fits in 16 words
+    // fits in 16 words (with longer columns read from global memory and the
+    // block's shared memory doubled, the 400-member pedigree's M-sweeps were
+    // 16% slower than with 32 lanes)
     const int G = pairs && P.W <= 16 ? 16 : 32;
     const size_t wsm = fagw_block_bytes(P.N, P.F, G);
     const bool warp_like = !exact && wsm <= 200 * 1024 && 2 * P.F < 8192;

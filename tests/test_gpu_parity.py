@@ -342,6 +342,38 @@ def test_fast_msampler_decisions_match_exact(name):
     assert differ <= meioses.size // 4
 
 
+@pytest.mark.parametrize("name", ["cfg1", "cfg2", "cfg5"])
+@pytest.mark.parametrize("nchain", [1, 8])
+def test_fast_msweep_equals_its_steps_one_by_one(name, nchain):
+    """A fast M-sweep reuses, at each step, the likelihoods of the current
+    column that the previous step computed (raw[l][current],
+    meiosis_sampler.cc:123-124); a sweep of one meiosis computes them afresh.
+    A sweep over 24 meioses must give the graph, bit for bit, that 24
+    one-meiosis sweeps with the same uniforms give (8 chains: the
+    founder-allele kernel's two-loci-per-warp form where a column fits)."""
+    if name == "cfg5":
+        from swiftlink_gb300 import pedigree, synth
+        g = pedigree.problem_from_workload(synth.make_workload(5))
+        state = g["dg0"]
+    else:
+        g, state = _seeded(name)
+    M = g["M"]
+    rng = np.random.default_rng(73)
+    order = rng.permutation(g["meioses"])[:24].astype(np.int32)
+    u = rng.random((nchain, order.size, M))
+    prob = api.Problem.from_arrays(g, with_legal=False)
+    with api.Context(prob, n_chains=nchain, sampler_precision=api.SL_SAMPLER_FAST) as fa:
+        fa.set_graphs(np.stack([state] * nchain))
+        fa.msampler_sweep(order, u, n_chains=nchain)
+        whole = fa.get_graphs()
+        fa.set_graphs(np.stack([state] * nchain))
+        for j, m in enumerate(order):
+            fa.msampler_sweep([int(m)], u[:, j:j + 1], n_chains=nchain)
+        steps = fa.get_graphs()
+    assert np.array_equal(whole, steps)
+    assert not np.array_equal(whole[0], state)
+
+
 def test_fast_and_exact_long_runs_agree_within_monte_carlo_error():
     """Long runs on the 30-member pedigree: 8 chains x 10 segments of 1,000
     iterations, scoring every 10th graph, in the exact mode (FP64 samplers and

@@ -233,7 +233,10 @@ def test_persistent_mc3_graph_equals_host_driven_spurts():
             outs.append((ctx.get_graphs(), ctx.lod_results(), ctx.mc3_stats()))
     (g0, l0, s0), (g1, l1, s1) = outs
     assert np.array_equal(g0, g1)
-    np.testing.assert_array_equal(l0[0], l1[0])
+    # the same graphs scored; the one-by-one path merges each scoring's graphs
+    # as it goes and may time the FP32 scorer's forms, so the log-sums agree to
+    # FP32 rounding rather than bit for bit
+    np.testing.assert_allclose(l0[0], l1[0], rtol=0, atol=1e-5)
     assert l0[1] == l1[1]
     np.testing.assert_array_equal(s0[0], s1[0])
     np.testing.assert_array_equal(s0[1], s1[1])
