@@ -684,12 +684,15 @@ def adjoint_rate(device, G=1000, chunk=250):
                      lod_flags=api.SL_LOD_ZERO_OK) as ctx:
         segs, used = ctx.adjoint_memory()
         ctx.trait_backward(gset[:10])
+        ctx.profile(True)   # event marks around the adjoint's launches: the device's share of the wall time
         t = time.perf_counter()
         done = 0
         while done < G:
             grad, pt = ctx.trait_backward(gset[:min(chunk, G - done)])
             done += min(chunk, G - done)
         dt = time.perf_counter() - t
+        kern_ms, kern_n = ctx.profile_read(api.SL_KERNEL_LOD)
+        ctx.profile(False)
         # the forward FP32 scorer on the same graphs, for the ratio
         ctx.lod_score_graphs(gset)
         ctx.synchronize()
@@ -698,6 +701,8 @@ def adjoint_rate(device, G=1000, chunk=250):
         ctx.synchronize()
         fwd = chunk * npos / (time.perf_counter() - t)
     return {"value": G * npos / dt, "unit": "positions/s", "graphs": G, "positions_per_graph": npos,
+            "kernel_positions_per_s": G * npos / (kern_ms / 1e3) if kern_ms > 0 else None,
+            "kernel_launches": int(kern_n),
             "forward_fp32_positions_per_s": fwd, "adjoint_segments": segs, "shared_bytes_per_warp": used,
             "model": "dominant (0.01, 0.8, 0.9), q = 1e-3",
             "path": "sl_trait_backward: host graphs in, d log L / d (theta_L, theta_R, penetrances, q) out"}

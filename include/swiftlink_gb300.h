@@ -361,9 +361,13 @@ int sl_lod_score_device_graphs_noalloc(sl_ctx* ctx, int32_t n_graphs, const uint
  * ptrait_grad[4] (may be NULL) receives d log P(T) / d (penetrances, frequency)
  * (Peeler::calc_trait_prob, peeler.cc:65-73).  Needs the disease-model fields
  * of the problem.  The peel is recomputed on the device in FP32 with
- * power-of-two rescaling, one warp per (graph, interval, position) with the
- * rfunctions in shared memory (sl_adjoint_memory: kept, or recomputed when
- * they do not fit).
+ * power-of-two rescaling, in one of two forms: one warp per (graph, interval,
+ * position) with the rfunctions in shared memory, or one thread per position
+ * with them in a global arena (up to 4 GiB, a column per thread).  The first
+ * call with graphs times both on its first tasks and keeps the faster
+ * (sl_adjoint_info); both follow the memory plan of sl_adjoint_memory (kept,
+ * or recomputed when they do not fit) and give the same values up to the
+ * order of FP32 additions into shared adjoints.
  */
 int sl_trait_backward(sl_ctx* ctx, int32_t n_graphs, const int32_t* dgs, double* grad, double* ptrait_grad);
 
@@ -380,6 +384,13 @@ int sl_trait_backward(sl_ctx* ctx, int32_t n_graphs, const int32_t* dgs, double*
  * agree between plans within FP32 rounding.
  */
 int sl_adjoint_memory(sl_ctx* ctx, int64_t bytes_per_task, int32_t* segments, int64_t* used_bytes);
+
+/* The adjoint's form (SL_ADJOINT_WARP or SL_ADJOINT_THREAD; 0 before the
+ * first call with graphs, and again after sl_adjoint_memory) and the times
+ * of the timed launch of each (milliseconds; either pointer may be NULL). */
+#define SL_ADJOINT_WARP 1
+#define SL_ADJOINT_THREAD 2
+int sl_adjoint_info(sl_ctx* ctx, int32_t* form, double* warp_ms, double* thread_ms);
 
 /* The same adjoint for one graph and position evaluated on the host in FP64
  * (the reference gradient the device result is checked against); dg NULL

@@ -23,6 +23,8 @@ SL_LOD_KERNEL_AUTO, SL_LOD_KERNEL_INTERP, SL_LOD_KERNEL_JIT_REG, SL_LOD_KERNEL_J
 SL_LOD_ZERO_OK = 1
 SL_LS_KERNEL_GENERIC, SL_LS_KERNEL_SPECIALISED, SL_LS_KERNEL_BACKGROUND, SL_LS_KERNEL_AUTO = 0, 1, 2, 3
 SL_LS_KERNEL_GENERIC32, SL_LS_KERNEL_GENERIC16 = 4, 5
+SL_KERNEL_LSAMPLER, SL_KERNEL_MSAMPLER, SL_KERNEL_LOD, SL_KERNEL_LOD_MERGE, SL_KERNEL_OTHER = 0, 1, 2, 3, 4
+SL_ADJOINT_WARP, SL_ADJOINT_THREAD = 1, 2
 
 EXPORTED = [
     "sl_create", "sl_destroy", "sl_last_error", "sl_set_descent_graphs", "sl_get_descent_graphs",
@@ -33,7 +35,7 @@ EXPORTED = [
     "sl_problem_trait_priors", "sl_problem_trait_prob", "sl_trait_backward",
     "sl_problem_trait_backward_eval", "sl_lod_kernel_info", "sl_ls_kernel_info", "sl_set_temperatures", "sl_mc3_stats",
     "sl_chain_loglik", "sl_peel_sequence", "sl_batch_create", "sl_batch_run", "sl_batch_destroy",
-    "sl_sequential_imputation", "sl_sequential_imputation_run", "sl_adjoint_memory",
+    "sl_sequential_imputation", "sl_sequential_imputation_run", "sl_adjoint_memory", "sl_adjoint_info",
 ]
 
 
@@ -337,6 +339,15 @@ class Context:
         self._check(lib().sl_adjoint_memory(self.h, ctypes.c_int64(bytes_per_task), ctypes.byref(seg),
                                             ctypes.byref(used)))
         return seg.value, used.value
+
+    def adjoint_info(self):
+        """(SL_ADJOINT_WARP / SL_ADJOINT_THREAD or 0 before the first timed call,
+        the timed launch of each form in ms)."""
+        f = ctypes.c_int32()
+        a = ctypes.c_double()
+        b = ctypes.c_double()
+        self._check(lib().sl_adjoint_info(self.h, ctypes.byref(f), ctypes.byref(a), ctypes.byref(b)))
+        return f.value, a.value, b.value
 
     def trait_backward(self, dgs: Optional[np.ndarray] = None):
         """d log L / d (theta_L, theta_R, pen x3, frequency) at every LOD

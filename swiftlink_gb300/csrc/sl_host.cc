@@ -70,6 +70,10 @@ cudaError_t launch_lod(const ProblemDev& P, int precision, const uint32_t* graph
 cudaError_t launch_lod_merge(const double* vals, int G, int64_t npos, double* acc, uint8_t* init, cudaStream_t s);
 cudaError_t launch_trait_adjoint(const ProblemDev& P, const AdjDev& D, const uint32_t* graphs, int64_t graph_words,
                                  int64_t task0, int64_t ntask, double* grad, int* status, cudaStream_t s, int sms);
+int trait_adjoint_thr_blocks();
+cudaError_t launch_trait_adjoint_thr(const ProblemDev& P, const AdjDev& D, const uint32_t* graphs, int64_t graph_words,
+                                     int64_t task0, int64_t ntask, double* grad, int* status, float* arena, int* expo,
+                                     int64_t arena_threads, cudaStream_t s);
 cudaError_t launch_shuffle(const int32_t* base, int nm, int32_t* out, int first, int nchain, uint64_t seed,
                            uint64_t iter, cudaStream_t s);
 cudaError_t launch_choose(int first, int nchain, uint64_t seed, uint64_t iter, double lprob, uint8_t* is_l,
@@ -171,6 +175,14 @@ struct sl_ctx {
     size_t adj_budget = 0;            // shared bytes per warp the plan must fit (0: the default)
     double* d_adjG = nullptr;        // [chunk][6] gradients
     int64_t adj_chunk = 0;
+    // the adjoint's two forms: one warp per task with its matrices in shared memory, or one thread
+    // per task with them in a global arena (a column per thread); chosen by timing the first call
+    int adj_form = 0;                 // 0 not yet timed, SL_ADJOINT_WARP, SL_ADJOINT_THREAD
+    double adj_form_ms[2] = {0.0, 0.0};
+    float* d_adjA = nullptr;          // [2 half][threads] matrices and adjoints of the thread form
+    int* d_adjE = nullptr;            // [K][threads] their exponents
+    int64_t adj_thr = 0;              // threads the arena holds
+    size_t adj_thr_bytes = 0;
     // batched LOD kernel: the interpreter, or a problem-specialised form
     int lod_kernel_req = SL_LOD_KERNEL_AUTO;
     JitLs jit_ls;                     // the FP32 L-sampler specialised to the pedigree (kern null: generic)
@@ -2313,6 +2325,74 @@ int sl_lod_kernel_info(sl_ctx* ctx, int32_t* kernel, double* compile_ms) {
     return SL_OK;
 }
 
+// The thread form's arena: a column of 2 half floats and K exponents per
+// thread, for the blocks of 128 threads that stay resident on every SM,
+// within 4 GiB.
+static int adjoint_arena(sl_ctx* ctx, int64_t ntask) {
+    const int64_t per = (int64_t)8 * ctx->adj.half + 4 * (int64_t)ctx->P.K;
+    int64_t thr = std::min<int64_t>((int64_t)ctx->sms * trait_adjoint_thr_blocks() * 128, (int64_t(4) << 30) / per);
+    thr = std::min<int64_t>(thr, (ntask + 127) / 128 * 128);
+    thr = thr / 128 * 128;
+    if (thr < 128) return fail(ctx, SL_ENOMEM, "the trait-peel adjoint's arena needs %lld bytes per thread", (long long)per);
+    const size_t bytes = (size_t)thr * per;
+    if (ctx->d_adjA && bytes <= ctx->adj_thr_bytes && (size_t)thr * 8 * ctx->adj.half <= ctx->adj_thr_bytes &&
+        thr == ctx->adj_thr)
+        return SL_OK;
+    cudaStreamSynchronize(ctx->stream);
+    for (void* p : {(void*)ctx->d_adjA, (void*)ctx->d_adjE}) {
+        if (!p) continue;
+        cudaFree(p);
+        ctx->owned.erase(std::find(ctx->owned.begin(), ctx->owned.end(), p));
+    }
+    ctx->d_adjA = nullptr;
+    ctx->d_adjE = nullptr;
+    ctx->adj_thr = 0;
+    ctx->adj_thr_bytes = 0;
+    int rc;
+    if ((rc = dev_alloc(ctx, &ctx->d_adjA, (size_t)thr * 2 * ctx->adj.half))) return rc;
+    if ((rc = dev_alloc(ctx, &ctx->d_adjE, (size_t)thr * ctx->P.K))) return rc;
+    ctx->adj_thr = thr;
+    ctx->adj_thr_bytes = bytes;
+    return SL_OK;
+}
+
+static cudaError_t adjoint_launch(sl_ctx* ctx, int form, const uint32_t* graphs, int64_t words, int64_t t0,
+                                  int64_t nt) {
+    const ProblemDev& P = ctx->P;
+    if (form == SL_ADJOINT_THREAD)
+        return launch_trait_adjoint_thr(P, ctx->adj, graphs, words, t0, nt, ctx->d_adjG, ctx->d_status, ctx->d_adjA,
+                                        ctx->d_adjE, ctx->adj_thr, ctx->stream);
+    return launch_trait_adjoint(P, ctx->adj, graphs, words, t0, nt, ctx->d_adjG, ctx->d_status, ctx->stream, ctx->sms);
+}
+
+// The first call with graphs times both forms on its first tasks (up to
+// 65,536) and keeps the faster for the context.
+static int adjoint_choose(sl_ctx* ctx, const uint32_t* graphs, int64_t words, int64_t ntask) {
+    if (ctx->adj_form) return SL_OK;
+    const int64_t nt = std::min<int64_t>(ntask, 65536);
+    int rc;
+    if ((rc = adjoint_arena(ctx, nt))) return rc;
+    int st = 0;
+    CK(cudaStreamSynchronize(ctx->stream));
+    CK(cudaMemcpy(&st, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost));
+    cudaEvent_t a = take_event(ctx), b = take_event(ctx);
+    for (int form : {SL_ADJOINT_WARP, SL_ADJOINT_THREAD}) {
+        CK(adjoint_launch(ctx, form, graphs, words, 0, std::min<int64_t>(nt, 1024)));   // warm-up
+        CK(cudaEventRecord(a, ctx->stream));
+        CK(adjoint_launch(ctx, form, graphs, words, 0, nt));
+        CK(cudaEventRecord(b, ctx->stream));
+        CK(cudaEventSynchronize(b));
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, a, b));
+        ctx->adj_form_ms[form - 1] = ms;
+    }
+    ctx->event_pool.push_back(a);
+    ctx->event_pool.push_back(b);
+    CK(cudaMemcpy(ctx->d_status, &st, sizeof(int), cudaMemcpyHostToDevice));   // the timing runs report nothing
+    ctx->adj_form = ctx->adj_form_ms[1] < ctx->adj_form_ms[0] ? SL_ADJOINT_THREAD : SL_ADJOINT_WARP;
+    return SL_OK;
+}
+
 int sl_trait_backward(sl_ctx* ctx, int32_t n_graphs, const int32_t* dgs, double* grad, double* ptrait_grad) {
     if (!ctx) return fail(ctx, SL_EINVAL, "null context");
     if (!ctx->has_adjoint)
@@ -2350,12 +2430,13 @@ int sl_trait_backward(sl_ctx* ctx, int32_t n_graphs, const int32_t* dgs, double*
                        ctx->stream));
     const int64_t ntask = npos * n_graphs;
     if ((rc = adjoint_chunk(ctx, ntask))) return rc;
+    if ((rc = adjoint_choose(ctx, ctx->d_graphs, (int64_t)words, ntask))) return rc;
+    if (ctx->adj_form == SL_ADJOINT_THREAD && (rc = adjoint_arena(ctx, std::min(ctx->adj_chunk, ntask)))) return rc;
     for (int64_t t0 = 0; t0 < ntask; t0 += ctx->adj_chunk) {
         const int64_t nt = std::min(ctx->adj_chunk, ntask - t0);
         {
             Prof pr(ctx, SL_KERNEL_LOD);
-            CK(launch_trait_adjoint(P, ctx->adj, ctx->d_graphs, (int64_t)words, t0, nt, ctx->d_adjG, ctx->d_status,
-                                    ctx->stream, ctx->sms));
+            CK(adjoint_launch(ctx, ctx->adj_form, ctx->d_graphs, (int64_t)words, t0, nt));
         }
         CK(cudaMemcpyAsync(grad + t0 * 6, ctx->d_adjG, sizeof(double) * 6 * nt, cudaMemcpyDeviceToHost,
                            ctx->stream));
@@ -2373,8 +2454,17 @@ int sl_adjoint_memory(sl_ctx* ctx, int64_t bytes_per_task, int32_t* segments, in
     CK(cudaStreamSynchronize(ctx->stream));
     ctx->adj_budget = (size_t)bytes_per_task;
     if (int rc = plan_adjoint(ctx)) return fail(ctx, rc, "%s", sl_last_error(nullptr));
+    ctx->adj_form = 0;   // timed again under the new plan
     if (segments) *segments = ctx->adj.nseg;
     if (used_bytes) *used_bytes = ctx->adj.warp_bytes;
+    return SL_OK;
+}
+
+int sl_adjoint_info(sl_ctx* ctx, int32_t* form, double* warp_ms, double* thread_ms) {
+    if (!ctx) return fail(ctx, SL_EINVAL, "null context");
+    if (form) *form = ctx->adj_form;
+    if (warp_ms) *warp_ms = ctx->adj_form_ms[0];
+    if (thread_ms) *thread_ms = ctx->adj_form_ms[1];
     return SL_OK;
 }
 
@@ -2854,7 +2944,6 @@ static void account_span(sl_ctx* ctx, const sl_run_options* o, int first, int en
 // Iterations [first, end) of a run: one launch of the run graph, or with
 // profiling on the same kernels launched one by one with per-class marks.
 static int run_span(sl_ctx* ctx, const sl_run_options* o, int first, int end) {
-    const ProblemDev& P = ctx->P;
     const int C = ctx->n_chains;
     const int nm = (int)ctx->meioses.size();
     if (!ctx->profiling) {

@@ -2289,6 +2289,12 @@ __device__ __forceinline__ void adj_R(const OpDev& op, const uint32_t* w, int pw
     }
 }
 
+// 2^-e as a float multiplier when it is a normal number (the op's scaling,
+// exact), else 0 (the caller then scales with ldexpf).
+__device__ __forceinline__ float adj_pow2(int e) {
+    return (e >= -127 && e <= 126) ? __int_as_float((127 - e) << 23) : 0.f;
+}
+
 // Forward of op k: its scaled matrix in A, its exponent in E[k].  One item
 // per lane: the peel node's disease probability times the previous
 // rfunctions' cells times the recombination factors; the four items of a
@@ -2325,10 +2331,69 @@ __device__ void adj_forward(const ProblemDev& P, const AdjDev& D, const AdjTask&
     }
     for (int dd = 16; dd >= 1; dd >>= 1) mx = fmaxf(mx, __shfl_xor_sync(FULLMASK, mx, dd));
     const int e = mx > 0.f ? ilogbf(mx) - op.scale_to : 0;
+    const float sc = adj_pow2(e);
     __syncwarp();
-    for (int cell = lane; cell < ncell; cell += 32) out[cell] = ldexpf(out[cell], -e);
+    for (int cell = lane; cell < ncell; cell += 32) out[cell] = sc != 0.f ? out[cell] * sc : ldexpf(out[cell], -e);
     if (lane == 0) E[k] = e;
     __syncwarp();
+}
+
+// The items of op k in the reverse pass, NP previous rfunctions (unrolled).
+template <int NP>
+__device__ __forceinline__ void adj_reverse_items(const OpDev& op, const uint32_t* tab, int nw, int pw, int nitem,
+                                                  const float* bk, int e, const float* A, float* B, const float* dp,
+                                                  const float4* dg, const float* rt, int lane, float* acc) {
+    const float sc = adj_pow2(e);
+    float gl = 0.f, gr = 0.f, g0 = 0.f, g1 = 0.f, g2 = 0.f, g3 = 0.f;
+    for (int it0 = 0; it0 < nitem; it0 += 32) {
+        const int item = it0 + lane, cell = item >> 2, t = item & 3;
+        if (item >= nitem) break;
+        const float gd = sc != 0.f ? bk[cell] * sc : ldexpf(bk[cell], -e);   // the cell's adjoint before its scaling
+        if (gd == 0.f) continue;
+        const uint32_t* w = tab + (size_t)item * nw;
+        const int s = (int)(w[0] & 3u);
+        float a[NP > 0 ? NP : 1];
+        int off[NP > 0 ? NP : 1];
+        float pp = 1.f;
+#pragma unroll
+        for (int j = 0; j < NP; ++j) {
+            off[j] = (int)((w[1 + (j >> 1)] >> (16 * (j & 1))) & 0xffffu);
+            a[j] = A[off[j]];
+            pp *= a[j];
+        }
+        float R, dRl, dRr;
+        adj_R<true>(op, w, pw, t, rt, R, dRl, dRr);
+        const float c = dp[s];
+        const float wgt = gd * pp;
+        const float4 dc = dg[s];
+        g0 += wgt * R * dc.x;
+        g1 += wgt * R * dc.y;
+        g2 += wgt * R * dc.z;
+        g3 += wgt * R * dc.w;
+        gl += wgt * c * dRl;
+        gr += wgt * c * dRr;
+        // each factor's adjoint: the product of the others, by prefix and suffix products
+        float pre[NP > 0 ? NP : 1];
+        float run = gd * c * R;
+#pragma unroll
+        for (int j = 0; j < NP; ++j) {
+            pre[j] = run;
+            run *= a[j];
+        }
+        float suf = 1.f;
+#pragma unroll
+        for (int j = NP - 1; j >= 0; --j) {
+            const float v = pre[j] * suf;
+            if (v != 0.f) atomicAdd(B + off[j], v);
+            suf *= a[j];
+        }
+    }
+    acc[0] += gl;
+    acc[1] += gr;
+    acc[2] += g0;
+    acc[3] += g1;
+    acc[4] += g2;
+    acc[5] += g3;
 }
 
 // Reverse of op k: adjoints into the previous rfunctions' cells (B), the
@@ -2344,58 +2409,16 @@ __device__ void adj_reverse(const ProblemDev& P, const AdjDev& D, const AdjTask&
     const float* dp = D.dprob + 4 * op.peel;
     const float4* dg = D.dgrad + 4 * op.peel;
     const int e = E[k];
-    float gl = 0.f, gr = 0.f, g0 = 0.f, g1 = 0.f, g2 = 0.f, g3 = 0.f;
-    for (int it0 = 0; it0 < nitem; it0 += 32) {
-        const int item = it0 + lane, cell = item >> 2, t = item & 3;
-        if (item >= nitem) break;
-        const float gd = ldexpf(bk[cell], -e);   // the adjoint of the cell before its scaling
-        if (gd == 0.f) continue;
-        const uint32_t* w = tab + (size_t)item * nw;
-        const int s = (int)(w[0] & 3u);
-        float a[kAdjMaxPrev];
-        int off[kAdjMaxPrev];
-        float pp = 1.f;
-#pragma unroll
-        for (int j = 0; j < kAdjMaxPrev; ++j) {
-            off[j] = j < op.n_prev ? (int)((w[1 + (j >> 1)] >> (16 * (j & 1))) & 0xffffu) : 0;
-            a[j] = j < op.n_prev ? A[off[j]] : 1.f;
-            pp *= a[j];
-        }
-        float R, dRl, dRr;
-        adj_R<true>(op, w, pw, t, rt, R, dRl, dRr);
-        const float c = dp[s];
-        const float wgt = gd * pp;
-        const float4 dc = dg[s];
-        g0 += wgt * R * dc.x;
-        g1 += wgt * R * dc.y;
-        g2 += wgt * R * dc.z;
-        g3 += wgt * R * dc.w;
-        gl += wgt * c * dRl;
-        gr += wgt * c * dRr;
-        // each factor's adjoint: the product of the others, by prefix and suffix products
-        float pre[kAdjMaxPrev];
-        float run = gd * c * R;
-#pragma unroll
-        for (int j = 0; j < kAdjMaxPrev; ++j) {
-            pre[j] = run;
-            run *= a[j];
-        }
-        float suf = 1.f;
-#pragma unroll
-        for (int j = kAdjMaxPrev - 1; j >= 0; --j) {
-            if (j < op.n_prev) {
-                const float v = pre[j] * suf;
-                if (v != 0.f) atomicAdd(B + off[j], v);
-            }
-            suf *= a[j];
-        }
+    float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    switch (op.n_prev) {
+#define SL_ADJ_NP(n) \
+        case n: adj_reverse_items<n>(op, tab, nw, pw, nitem, bk, e, A, B, dp, dg, rt, lane, acc); break;
+        SL_ADJ_NP(0) SL_ADJ_NP(1) SL_ADJ_NP(2) SL_ADJ_NP(3) SL_ADJ_NP(4)
+        SL_ADJ_NP(5) SL_ADJ_NP(6) SL_ADJ_NP(7) SL_ADJ_NP(8)
+#undef SL_ADJ_NP
+        default: break;
     }
-    g[0] += (double)gl;
-    g[1] += (double)gr;
-    g[2] += (double)g0;
-    g[3] += (double)g1;
-    g[4] += (double)g2;
-    g[5] += (double)g3;
+    for (int q = 0; q < 6; ++q) g[q] += (double)acc[q];
     __syncwarp();
 }
 
@@ -2463,6 +2486,228 @@ __global__ void __launch_bounds__(128) trait_adjoint_kernel(ProblemDev P, AdjDev
             if (lane == 0) grad[u * 6 + q] = v;
         }
         __syncwarp();
+    }
+}
+
+// The same adjoint with one thread per task: each thread's matrices and
+// adjoints live in global memory, a column of the arena per resident thread
+// (float offset o of thread r at o * nthr + r, so the threads of a warp, all
+// at the same item, touch one 128-byte line), and every item of an op is the
+// thread's own serial loop, so small rfunctions leave no lane idle and the
+// adjoints need no atomics.  Matrices are stored unscaled with their
+// exponents; a factor is scaled as it is read, which gives the scaled form's
+// values exactly.  Same plan (offsets, segments, kept matrices) and item
+// tables as the warp form.
+struct AdjThr {
+    float* A;       // arena base of this thread: A[o * nthr]
+    float* B;       // adjoints: B[o * nthr]
+    int* E;         // exponents: E[k * nthr]
+    int64_t nthr;
+};
+
+// The thread's recombination terms of op k, rt[12 c + b] as in adj_rtab.
+__device__ __forceinline__ void adj_rtab_thr(const ProblemDev& P, const AdjTask& T, const OpDev& op, float* rt) {
+    const int nch = op.type == CHILD ? 1 : (op.type == PARENT ? op.n_child : 0);
+    for (int c = 0; c < nch; ++c) {
+        const int child = op.type == CHILD ? op.peel : P.opdata[op.child_at + 4 * c];
+        const int bits = T.graph ? person_bits(P, T.colL, T.colR, child) : 0;
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+            float r, dl, dr;
+            adj_rec(T, bits, b >> 1, b & 1, r, dl, dr);
+            rt[12 * c + b] = r;
+            rt[12 * c + 4 + b] = dl;
+            rt[12 * c + 8 + b] = dr;
+        }
+    }
+}
+
+// Factor j's scale and exponent for op k's previous rfunctions.
+__device__ __forceinline__ void adj_prev_scales(const ProblemDev& P, const AdjThr& R, const OpDev& op, float* sj,
+                                                int* ej) {
+    const int32_t* po = P.opdata + op.prev_ops_at;
+    for (int j = 0; j < op.n_prev; ++j) {
+        ej[j] = R.E[(int64_t)po[j] * R.nthr];
+        sj[j] = adj_pow2(ej[j]);
+    }
+}
+
+__device__ __forceinline__ float adj_scaled(float v, float sc, int e) { return sc != 0.f ? v * sc : ldexpf(v, -e); }
+
+__device__ void adj_forward_thr(const ProblemDev& P, const AdjDev& D, const AdjTask& T, const AdjThr& R, int k,
+                                float* rt) {
+    const OpDev op = P.ops[k];
+    adj_rtab_thr(P, T, op, rt);
+    float sj[kAdjMaxPrev];
+    int ej[kAdjMaxPrev];
+    adj_prev_scales(P, R, op, sj, ej);
+    const int ncell = 1 << (2 * op.c);
+    const int nw = adj_item_words(op.n_prev, op.n_child), pw = (op.n_prev + 1) / 2;
+    const uint32_t* tab = D.items + D.item_at[k];
+    float* out = R.A + (int64_t)D.aoff[k] * R.nthr;
+    const float* dp = D.dprob + 4 * op.peel;
+    float mx = 0.f;
+    for (int cell = 0; cell < ncell; ++cell) {
+        float tv[4];
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+            const uint32_t* w = tab + (size_t)(4 * cell + t) * nw;
+            float term = dp[w[0] & 3u];
+            for (int j = 0; j < op.n_prev; ++j) {
+                const int off = (int)((w[1 + (j >> 1)] >> (16 * (j & 1))) & 0xffffu);
+                term *= adj_scaled(R.A[(int64_t)off * R.nthr], sj[j], ej[j]);
+            }
+            float Rr, dl, dr;
+            adj_R<false>(op, w, pw, t, rt, Rr, dl, dr);
+            tv[t] = term * Rr;
+        }
+        const float total = ((tv[0] + tv[1]) + tv[2]) + tv[3];
+        out[(int64_t)cell * R.nthr] = total;
+        mx = fmaxf(mx, total);
+    }
+    R.E[(int64_t)k * R.nthr] = mx > 0.f ? ilogbf(mx) - op.scale_to : 0;
+}
+
+template <int NP>
+__device__ __forceinline__ void adj_reverse_thr_items(const OpDev& op, const uint32_t* tab, int nw, int pw, int ncell,
+                                                      const AdjThr& R, const float* bk, float sk, int ek,
+                                                      const float* sj, const int* ej, const float* dp,
+                                                      const float4* dg, const float* rt, float* acc) {
+    float gl = 0.f, gr = 0.f, g0 = 0.f, g1 = 0.f, g2 = 0.f, g3 = 0.f;
+    for (int cell = 0; cell < ncell; ++cell) {
+        const float gd = adj_scaled(bk[(int64_t)cell * R.nthr], sk, ek);   // the cell's adjoint before its scaling
+        if (gd == 0.f) continue;
+#pragma unroll 1
+        for (int t = 0; t < 4; ++t) {
+            const uint32_t* w = tab + (size_t)(4 * cell + t) * nw;
+            const int s = (int)(w[0] & 3u);
+            float a[NP > 0 ? NP : 1];
+            int off[NP > 0 ? NP : 1];
+            float pp = 1.f;
+#pragma unroll
+            for (int j = 0; j < NP; ++j) {
+                off[j] = (int)((w[1 + (j >> 1)] >> (16 * (j & 1))) & 0xffffu);
+                a[j] = adj_scaled(R.A[(int64_t)off[j] * R.nthr], sj[j], ej[j]);
+                pp *= a[j];
+            }
+            float Rr, dRl, dRr;
+            adj_R<true>(op, w, pw, t, rt, Rr, dRl, dRr);
+            const float c = dp[s];
+            const float wgt = gd * pp;
+            const float4 dc = dg[s];
+            g0 += wgt * Rr * dc.x;
+            g1 += wgt * Rr * dc.y;
+            g2 += wgt * Rr * dc.z;
+            g3 += wgt * Rr * dc.w;
+            gl += wgt * c * dRl;
+            gr += wgt * c * dRr;
+            float pre[NP > 0 ? NP : 1];
+            float run = gd * c * Rr;
+#pragma unroll
+            for (int j = 0; j < NP; ++j) {
+                pre[j] = run;
+                run *= a[j];
+            }
+            float suf = 1.f;
+#pragma unroll
+            for (int j = NP - 1; j >= 0; --j) {
+                const float v = pre[j] * suf;
+                if (v != 0.f) R.B[(int64_t)off[j] * R.nthr] += v;
+                suf *= a[j];
+            }
+        }
+    }
+    acc[0] += gl;
+    acc[1] += gr;
+    acc[2] += g0;
+    acc[3] += g1;
+    acc[4] += g2;
+    acc[5] += g3;
+}
+
+__device__ void adj_reverse_thr(const ProblemDev& P, const AdjDev& D, const AdjTask& T, const AdjThr& R, int k,
+                                float* rt, double* g) {
+    const OpDev op = P.ops[k];
+    adj_rtab_thr(P, T, op, rt);
+    float sj[kAdjMaxPrev];
+    int ej[kAdjMaxPrev];
+    adj_prev_scales(P, R, op, sj, ej);
+    const int ncell = 1 << (2 * op.c);
+    const int nw = adj_item_words(op.n_prev, op.n_child), pw = (op.n_prev + 1) / 2;
+    const uint32_t* tab = D.items + D.item_at[k];
+    const float* bk = R.B + (int64_t)D.aoff[k] * R.nthr;
+    const int ek = R.E[(int64_t)k * R.nthr];
+    const float sk = adj_pow2(ek);
+    const float* dp = D.dprob + 4 * op.peel;
+    const float4* dg = D.dgrad + 4 * op.peel;
+    float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    switch (op.n_prev) {
+#define SL_ADJ_NP(n) \
+        case n: adj_reverse_thr_items<n>(op, tab, nw, pw, ncell, R, bk, sk, ek, sj, ej, dp, dg, rt, acc); break;
+        SL_ADJ_NP(0) SL_ADJ_NP(1) SL_ADJ_NP(2) SL_ADJ_NP(3) SL_ADJ_NP(4)
+        SL_ADJ_NP(5) SL_ADJ_NP(6) SL_ADJ_NP(7) SL_ADJ_NP(8)
+#undef SL_ADJ_NP
+        default: break;
+    }
+    for (int q = 0; q < 6; ++q) g[q] += (double)acc[q];
+}
+
+__global__ void __launch_bounds__(128) trait_adjoint_thr_kernel(ProblemDev P, AdjDev D, const uint32_t* graphs,
+                                                                int64_t graph_words, int64_t task0, int64_t ntask,
+                                                                double* grad, int* status, float* arena, int* expo) {
+    const int64_t nthr = (int64_t)gridDim.x * blockDim.x;
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    AdjThr R;
+    R.nthr = nthr;
+    R.A = arena + r;
+    R.B = arena + (int64_t)D.half * nthr + r;
+    R.E = expo + r;
+    float rt[12 * 32];   // the op's recombination terms (local memory)
+    const int n = P.n_lod;
+    const int64_t npos = (int64_t)(P.M - 1) * n;
+    for (int64_t u = r; u < ntask; u += nthr) {
+        const int64_t t = task0 + u;
+        AdjTask T;
+        T.graph = graphs != nullptr;
+        T.colL = T.colR = nullptr;
+        T.th = T.an = T.th2 = T.an2 = 0.f;
+        if (T.graph) {
+            const int b = (int)(t / npos);
+            const int64_t pidx = t % npos;
+            const int l = (int)(pidx / n), o = (int)(pidx % n);
+            T.colL = graphs + (size_t)b * graph_words + (size_t)l * P.W;
+            T.colR = T.colL + P.W;
+            T.th = P.partial_f[l] * (float)(o + 1);
+            T.an = 1.f - T.th;
+            T.th2 = P.partial_f[l] * (float)(n - o);
+            T.an2 = 1.f - T.th2;
+        }
+        for (int k = 0; k < P.K; ++k) adj_forward_thr(P, D, T, R, k, rt);
+        const int kr = P.K - 1;
+        const int er = R.E[(int64_t)kr * nthr];
+        const float root = adj_scaled(R.A[(int64_t)D.aoff[kr] * nthr], adj_pow2(er), er);
+        double g[6] = {0, 0, 0, 0, 0, 0};
+        if (!(root > 0.f)) {
+            if (!P.lod_zero_ok) set_status(status, ST_LOD_NONPOS);
+            for (int q = 0; q < 6; ++q) grad[u * 6 + q] = __longlong_as_double(0x7ff8000000000000LL);   // NaN
+            continue;
+        }
+        for (int i = 0; i < D.half; ++i) R.B[(int64_t)i * nthr] = 0.f;
+        for (int sg = D.nseg - 1; sg >= 0; --sg) {
+            const int k0 = D.seg[sg], k1 = D.seg[sg + 1];
+            if (sg < D.nseg - 1) {
+                // recompute the segment's matrices that were not kept, zero their adjoints
+                for (int k = k0; k < k1; ++k)
+                    if (!D.keep[k]) adj_forward_thr(P, D, T, R, k, rt);
+                for (int k = k0; k < k1; ++k)
+                    if (!D.keep[k])
+                        for (int i = 0; i < (1 << (2 * P.ops[k].c)); ++i) R.B[(int64_t)(D.aoff[k] + i) * nthr] = 0.f;
+            } else {
+                R.B[(int64_t)D.aoff[kr] * nthr] = 1.0f / root;
+            }
+            for (int k = k1 - 1; k >= k0; --k) adj_reverse_thr(P, D, T, R, k, rt, g);
+        }
+        for (int q = 0; q < 6; ++q) grad[u * 6 + q] = g[q];
     }
 }
 
@@ -3136,6 +3381,29 @@ cudaError_t launch_trait_adjoint(const ProblemDev& P, const AdjDev& D, const uin
     grid = std::min<int64_t>(grid, (int64_t)sms * blocks);
     trait_adjoint_kernel<<<(int)std::max<int64_t>(1, grid), wpb * 32, smem, s>>>(P, D, graphs, graph_words, task0,
                                                                                  ntask, grad, status);
+    return cudaGetLastError();
+}
+
+// Resident blocks of 128 threads per SM of the one-thread-per-task form.
+int trait_adjoint_thr_blocks() {
+    int blocks = 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, (const void*)trait_adjoint_thr_kernel, 128, 0) !=
+            cudaSuccess || blocks < 1) {
+        cudaGetLastError();
+        blocks = 1;
+    }
+    return blocks;
+}
+
+// One block of 128 threads per 128 threads of the arena (arena_threads, the
+// resident threads of every SM); the threads stride over the tasks.
+cudaError_t launch_trait_adjoint_thr(const ProblemDev& P, const AdjDev& D, const uint32_t* graphs, int64_t graph_words,
+                                     int64_t task0, int64_t ntask, double* grad, int* status, float* arena, int* expo,
+                                     int64_t arena_threads, cudaStream_t s) {
+    const int64_t blocks = arena_threads / 128;
+    if (blocks < 1) return cudaErrorInvalidValue;
+    trait_adjoint_thr_kernel<<<(int)blocks, 128, 0, s>>>(P, D, graphs, graph_words, task0, ntask, grad, status, arena,
+                                                         expo);
     return cudaGetLastError();
 }
 
