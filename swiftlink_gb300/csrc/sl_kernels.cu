@@ -2652,7 +2652,7 @@ __device__ void adj_reverse_thr(const ProblemDev& P, const AdjDev& D, const AdjT
     for (int q = 0; q < 6; ++q) g[q] += (double)acc[q];
 }
 
-__global__ void __launch_bounds__(128) trait_adjoint_thr_kernel(ProblemDev P, AdjDev D, const uint32_t* graphs,
+__global__ void __launch_bounds__(128, 6) trait_adjoint_thr_kernel(ProblemDev P, AdjDev D, const uint32_t* graphs,
                                                                 int64_t graph_words, int64_t task0, int64_t ntask,
                                                                 double* grad, int* status, float* arena, int* expo) {
     const int64_t nthr = (int64_t)gridDim.x * blockDim.x;
