@@ -132,12 +132,13 @@ typedef struct sl_options {
  * rfunction cells allowed by genotype elimination and wins on pedigrees with
  * large cutsets (hundreds of members), the specialised one on smaller ones. */
 #define SL_LS_KERNEL_AUTO 3
-/* GENERIC times 32 against 16 lanes per (chain, locus) task (two tasks per
- * warp) before the first L-sampler work and keeps the faster, sharing the
- * choice between contexts of one pedigree size class; these two force one
- * (all forms draw the same graphs). */
+/* GENERIC times 32, 16 and 8 lanes per (chain, locus) task (one, two or four
+ * tasks per warp) before the first L-sampler work and keeps the fastest,
+ * sharing the choice between contexts of one pedigree size class; these
+ * three force one (all forms draw the same graphs). */
 #define SL_LS_KERNEL_GENERIC32 4
 #define SL_LS_KERNEL_GENERIC16 5
+#define SL_LS_KERNEL_GENERIC8 6
 
 /* A LOD position whose trait likelihood is 0 (an affected and an unaffected
  * member IBD 2 under a fully penetrant model, for instance) stops the

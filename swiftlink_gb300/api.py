@@ -22,7 +22,7 @@ SL_SAMPLER_EXACT, SL_SAMPLER_FAST = 0, 1
 SL_LOD_KERNEL_AUTO, SL_LOD_KERNEL_INTERP, SL_LOD_KERNEL_JIT_REG, SL_LOD_KERNEL_JIT_SMEM = 0, 1, 2, 3
 SL_LOD_ZERO_OK = 1
 SL_LS_KERNEL_GENERIC, SL_LS_KERNEL_SPECIALISED, SL_LS_KERNEL_BACKGROUND, SL_LS_KERNEL_AUTO = 0, 1, 2, 3
-SL_LS_KERNEL_GENERIC32, SL_LS_KERNEL_GENERIC16 = 4, 5
+SL_LS_KERNEL_GENERIC32, SL_LS_KERNEL_GENERIC16, SL_LS_KERNEL_GENERIC8 = 4, 5, 6
 SL_KERNEL_LSAMPLER, SL_KERNEL_MSAMPLER, SL_KERNEL_LOD, SL_KERNEL_LOD_MERGE, SL_KERNEL_OTHER = 0, 1, 2, 3, 4
 SL_ADJOINT_WARP, SL_ADJOINT_THREAD = 1, 2
 

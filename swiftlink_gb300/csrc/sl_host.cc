@@ -87,7 +87,8 @@ thread_local std::string g_err;
 const size_t kSmemBudget = 200 * 1024;  // dynamic shared memory a block may use
 }  // namespace
 
-enum { LS_GEN32 = 0, LS_GEN16 = 1, LS_JIT = 2 };
+enum { LS_GEN32 = 0, LS_GEN16 = 1, LS_JIT = 2, LS_GEN8 = 3 };
+static int ls_lanes(int choice) { return choice == LS_GEN16 ? 16 : (choice == LS_GEN8 ? 8 : 32); }
 
 struct sl_ctx {
     int device = 0;
@@ -199,8 +200,8 @@ struct sl_ctx {
     // the L-sampler's kernel and lanes per task: the generic kernel with 32 or
     // 16 lanes, or the specialised one; chosen by timing (ls_tune) unless forced
     bool ls_tune_pending = false;
-    int ls_choice = 0;                          // LS_GEN32, LS_GEN16, LS_JIT
-    double ls_tune_ms[3] = {0.0, 0.0, 0.0};     // one timed half-sweep with each (0: not timed)
+    int ls_choice = 0;                          // LS_GEN32, LS_GEN16, LS_GEN8, LS_JIT
+    double ls_tune_ms[4] = {0.0, 0.0, 0.0, 0.0};   // one timed half-sweep with each (0: not timed)
     int lod_kernel_sel = SL_LOD_KERNEL_INTERP;   // AUTO while the first scoring has not timed them
     JitLod jit_reg, jit_smem;
     double jit_ms = 0.0;
@@ -245,7 +246,7 @@ static cudaError_t ls_launch(sl_ctx* ctx, int first, int nchain, const int32_t* 
         return jit_ls_launch(ctx->jit_ls, ctx->d_dg, first, nchain, loci, nloci, u, ucs, uls, seed, iter, key, sel,
                              want, ctx->d_status, P.geno, P.prior_f, P.c_theta_f, ctx->sms, s);
     return launch_lsampler(P, ctx->d_dg, first, nchain, loci, nloci, u, ucs, uls, seed, iter, sel, want, ctx->d_status,
-                           s, ctx->ls_grid, ctx->ls_wpb, key, ctx->ls_choice == LS_GEN16 ? 16 : 32);
+                           s, ctx->ls_grid, ctx->ls_wpb, key, ls_lanes(ctx->ls_choice));
 }
 
 // Takes up a background compile of the specialised L-sampler that has ended:
@@ -377,7 +378,7 @@ static int ls_tune(sl_ctx* ctx) {
     CK(cudaMemcpy(&st, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost));
     CK(cudaMemcpyAsync(scratch, ctx->d_dg, sizeof(uint32_t) * words, cudaMemcpyDeviceToDevice, ctx->stream));
     cudaEvent_t a = take_event(ctx), b = take_event(ctx);
-    std::vector<int> cand = {LS_GEN32, LS_GEN16};
+    std::vector<int> cand = {LS_GEN32, LS_GEN16, LS_GEN8};
     if (jit) cand.push_back(LS_JIT);
     int best = ctx->ls_choice;
     float best_ms = 0.f;
@@ -392,7 +393,7 @@ static int ls_tune(sl_ctx* ctx) {
             else
                 CK(launch_lsampler(P, scratch, 0, C, ctx->d_even, (int)ctx->even.size(), nullptr, 0, 0, 1, 0,
                                    nullptr, 0, ctx->d_status, ctx->stream, ctx->ls_grid, ctx->ls_wpb, nullptr,
-                                   k == LS_GEN16 ? 16 : 32));
+                                   ls_lanes(k)));
             if (rep == 1) {
                 CK(cudaEventRecord(b, ctx->stream));
                 CK(cudaEventSynchronize(b));
@@ -1569,10 +1570,12 @@ int sl_create(const sl_problem_desc* d, const sl_options* opt, sl_ctx** out) {
     {   // the FP32 L-sampler specialised to the pedigree, on request
         const int req = opt->ls_kernel;
         if (req != SL_LS_KERNEL_GENERIC && req != SL_LS_KERNEL_SPECIALISED && req != SL_LS_KERNEL_BACKGROUND &&
-            req != SL_LS_KERNEL_AUTO && req != SL_LS_KERNEL_GENERIC32 && req != SL_LS_KERNEL_GENERIC16)
+            req != SL_LS_KERNEL_AUTO && req != SL_LS_KERNEL_GENERIC32 && req != SL_LS_KERNEL_GENERIC16 &&
+            req != SL_LS_KERNEL_GENERIC8)
             return bail(fail(nullptr, SL_EINVAL, "unknown ls_kernel %d", req));
-        if (req == SL_LS_KERNEL_GENERIC) ctx->ls_tune_pending = true;   // 32 or 16 lanes per task, by timing
+        if (req == SL_LS_KERNEL_GENERIC) ctx->ls_tune_pending = true;   // 32, 16 or 8 lanes per task, by timing
         if (req == SL_LS_KERNEL_GENERIC16) ctx->ls_choice = LS_GEN16;
+        if (req == SL_LS_KERNEL_GENERIC8) ctx->ls_choice = LS_GEN8;
         if (P.ls_fast && req == SL_LS_KERNEL_BACKGROUND) {
             // the source now (host tables in hand), the compile on a thread started once creation has succeeded
             const JitLsIn in{ops.data(), od.data(), K, N, F, M, P.W, N - F, arena, max_child, d->mother, d->father};

@@ -126,14 +126,17 @@ struct Ls<float> {   // rounded operations, never contracted: the kernel special
     static __device__ __forceinline__ float div(float a, float b) { return __fdiv_rn(a, b); }
 };
 
-// The lanes working on one L-sampler task: a whole warp (G = 32) or half of
-// one (G = 16; two tasks per warp, for pedigrees whose rfunctions have few
-// allowed cells).  Shuffles and ballots stay within the group; lane numbers
+// The lanes working on one L-sampler task: a whole warp (G = 32), half of one
+// or a quarter (G = 16 or 8; two or four tasks per warp, for pedigrees whose
+// rfunctions have few allowed cells).  Shuffles and ballots stay within the
+// group, whose tasks may diverge from the warp's other groups; lane numbers
 // are the group's own.
 template <int G>
 struct Lanes {
+    static_assert(G == 32 || G == 16 || G == 8, "a lane group is 32, 16 or 8 lanes of one warp");
     unsigned mask;
-    __device__ __forceinline__ Lanes() : mask(G == 32 ? FULLMASK : (0xffffu << (threadIdx.x & 16))) {}
+    // the group's lanes: G consecutive lanes starting at a multiple of G
+    __device__ __forceinline__ Lanes() : mask(G == 32 ? FULLMASK : (((1u << G) - 1u) << (threadIdx.x & (32 - G)))) {}
     template <typename V>
     __device__ __forceinline__ V shfl(V v, int src) const { return __shfl_sync(mask, v, src, G); }
     template <typename V>
@@ -142,7 +145,7 @@ struct Lanes {
     __device__ __forceinline__ V shfl_up(V v, int d) const { return __shfl_up_sync(mask, v, d, G); }
     __device__ __forceinline__ unsigned ballot(bool p) const {
         const unsigned b = __ballot_sync(mask, p);
-        return G == 32 ? b : (b >> (threadIdx.x & 16)) & 0xffffu;
+        return G == 32 ? b : (b >> (threadIdx.x & (32 - G))) & ((1u << G) - 1u);
     }
     __device__ __forceinline__ void sync() const { __syncwarp(mask); }
 };
@@ -355,9 +358,9 @@ __device__ int ls_locus(const ProblemDev& P, const OpDev* ops, const int32_t* op
             if (hasL) sL[w] = colC[w - P.W];
             if (hasR) sR[w] = colC[w + P.W];
         }
-        if (lane < 16) {
-            if constexpr (sizeof(T) == 4) spri[lane] = (T)P.prior_f[(size_t)l * 16 + lane];
-            else spri[lane] = (T)P.prior[(size_t)l * 16 + lane];
+        for (int i = lane; i < 16; i += G) {
+            if constexpr (sizeof(T) == 4) spri[i] = (T)P.prior_f[(size_t)l * 16 + i];
+            else spri[i] = (T)P.prior[(size_t)l * 16 + i];
         }
         L.sync();
     }
@@ -1194,6 +1197,7 @@ __global__ void __launch_bounds__(128) fag_kernel(ProblemDev P, uint32_t* dg, in
 //      gives log2 of the likelihood.
 // ---------------------------------------------------------------------------
 constexpr int kFagWarpsPerBlock = 8;
+constexpr int kFagRounds = 4;   // rounds of colour propagation along heterozygote edges
 
 __host__ __device__ inline size_t fagw_tables(int N) {
     return (((size_t)N * 8 + 15) & ~(size_t)15) + (((size_t)4 * (N + 1) + 15) & ~(size_t)15);
@@ -1386,7 +1390,25 @@ __device__ __forceinline__ void fagw_task(const ProblemDev& P, const FagwTables&
     // colours to differ: the two sides' colourings are then determined apart,
     // and the likelihood is the product of the two sides' terms, so the edge
     // joins nothing.  The ends of the other edges are marked used and joined
-    // (bit 3: in the forest).
+    // (bit 3: in the forest).  First, a heterozygote with exactly one fixed
+    // end fixes the other to the opposite colour, in rounds until nothing
+    // changes (at most kFagRounds): most edges then have both ends fixed, and
+    // a fixed allele's colour is its component's, so its term is the same.
+    for (int round = 0; round < kFagRounds; ++round) {
+        int changed = 0;
+        for (int q = gl; q < nhet; q += G) {
+            const int i = typ[q] >> 2;
+            const int u = e[2 * i], v = e[2 * i + 1];
+            const int fu = fl[u] & 6, fv = fl[v] & 6;
+            if ((fu != 0) == (fv != 0)) continue;   // both ends fixed, or neither
+            const int cf = fu ? fu : fv;
+            const int opp = cf == 2 ? 4 : (cf == 4 ? 2 : 6);
+            atomicOr(&fl[fu ? v : u], opp | 1);
+            changed = 1;
+        }
+        __syncwarp();
+        if (!__any_sync(FULLMASK, changed)) break;   // the whole warp, as its groups share the loop
+    }
     int bad = 0;
     for (int q = gl; q < nhet; q += G) {
         const int i = typ[q] >> 2;   // the heterozygotes lead the list
@@ -3139,12 +3161,19 @@ static cudaError_t launch_lsampler_g(const ProblemDev& P, uint32_t* dg, int firs
     return cudaGetLastError();
 }
 
-// lanes = 32 or 16 lanes per (chain, locus) task; both draw the same graphs.
+// lanes = 32, 16 or 8 lanes per (chain, locus) task; all draw the same graphs.
 cudaError_t launch_lsampler(const ProblemDev& P, uint32_t* dg, int first, int nchain, const int32_t* loci, int nloci,
                             const double* u, int64_t ucs, int64_t uls, uint64_t seed, uint64_t iter,
                             const uint8_t* sel, int want, int* status, cudaStream_t s, int grid_cap, int wpb,
                             const uint64_t* key, int lanes) {
     Draws d{u, ucs, uls, seed, iter, 1, key};
+    if (lanes == 8) {
+        // four tasks per warp: a quarter of the warps per block keeps the block's shared memory
+        const int w8 = wpb > 3 ? wpb / 4 : 1;
+        if (P.ls_fast) return launch_lsampler_g<float, 8>(P, dg, first, nchain, loci, nloci, d, sel, want, status, s,
+                                                          grid_cap, w8);
+        return launch_lsampler_g<double, 8>(P, dg, first, nchain, loci, nloci, d, sel, want, status, s, grid_cap, w8);
+    }
     if (lanes == 16) {
         // two tasks per warp: half as many warps per block keeps the block's shared memory
         const int w16 = wpb > 1 ? wpb / 2 : 1;

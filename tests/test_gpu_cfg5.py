@@ -44,7 +44,8 @@ def cfg5():
     return d, port.Port(d)
 
 
-@pytest.mark.parametrize("lanes", [api.SL_LS_KERNEL_GENERIC32, api.SL_LS_KERNEL_GENERIC16])
+@pytest.mark.parametrize("lanes", [api.SL_LS_KERNEL_GENERIC32, api.SL_LS_KERNEL_GENERIC16,
+                                   api.SL_LS_KERNEL_GENERIC8])
 def test_cfg5_exact_lsteps_bit_exact(cfg5, lanes):
     d, P = cfg5
     M, K, N = d["M"], d["K"], d["N"]

@@ -548,16 +548,18 @@ def test_specialised_lsampler_is_bit_identical(name):
         assert np.array_equal(out[lk][1], b[1]), lk
 
 
-# the L-sampler's forms: generic with lanes per task by timing, forced to 32
-# or 16 lanes (two tasks per warp), and the kernel specialised to the pedigree
+# the L-sampler's forms: generic with lanes per task by timing, forced to 32,
+# 16 or 8 lanes (one, two or four tasks per warp), and the kernel specialised
+# to the pedigree
 LS_FORMS = (api.SL_LS_KERNEL_GENERIC, api.SL_LS_KERNEL_GENERIC32, api.SL_LS_KERNEL_GENERIC16,
-            api.SL_LS_KERNEL_SPECIALISED)
+            api.SL_LS_KERNEL_GENERIC8, api.SL_LS_KERNEL_SPECIALISED)
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("lanes", [api.SL_LS_KERNEL_GENERIC32, api.SL_LS_KERNEL_GENERIC16])
+@pytest.mark.parametrize("lanes", [api.SL_LS_KERNEL_GENERIC32, api.SL_LS_KERNEL_GENERIC16,
+                                   api.SL_LS_KERNEL_GENERIC8])
 @pytest.mark.parametrize("name", CASES)
-def test_lsweep_bit_exact_both_lane_groups(name, lanes):
+def test_lsweep_bit_exact_every_lane_group(name, lanes):
     """Exact mode with 32 and with 16 lanes per (chain, locus) task: the
     reference's L-sweep bit for bit (two chains, so a warp holds both tasks
     of the 16-lane form)."""
