@@ -272,10 +272,11 @@ __device__ __forceinline__ int state_of_rank(int mask, int r) {   // the r-th al
 
 // A task's shared bytes: the rfunctions [ls_arena, compact], the children's
 // transmission distributions [16 per child], the sampled states [N], the
-// peel's draws [K] (doubles), the locus's genotype codes and masks [N], its
-// neighbours' descent-graph words [2 W], its prior row [16] and the ops'
-// compact offsets [K + 1]; each part 16-byte aligned, so every task's base
-// is aligned.
+// locus's genotype codes and masks [N], its neighbours' descent-graph words
+// [2 W], its prior row [16] and the ops' compact offsets [K + 1]; each part
+// 16-byte aligned, so every task's base is aligned.  (The backward pass's
+// draws are made as it goes, one per operation: storing them took K doubles,
+// a third of a task on the 400-member pedigree.)
 __host__ __device__ __forceinline__ size_t al16(size_t x) { return (x + 15) & ~(size_t)15; }
 template <typename T>
 __host__ __device__ __forceinline__ size_t ls_draws_at(const ProblemDev& P) {
@@ -283,7 +284,7 @@ __host__ __device__ __forceinline__ size_t ls_draws_at(const ProblemDev& P) {
 }
 template <typename T>
 __host__ __device__ __forceinline__ size_t ls_gcol_at(const ProblemDev& P) {
-    return al16(ls_draws_at<T>(P) + 8 * (size_t)P.K);
+    return ls_draws_at<T>(P);
 }
 template <typename T>
 __host__ __device__ __forceinline__ size_t ls_cols_at(const ProblemDev& P) {
@@ -344,7 +345,6 @@ __device__ int ls_locus(const ProblemDev& P, const OpDev* ops, const int32_t* op
     T* dist = A + P.ls_arena;
     int8_t* assign = (int8_t*)(dist + 16 * P.max_child);
     int32_t* off = (int32_t*)(wsmem + ls_off_at<T>(P));
-    double* sdraw = (double*)(wsmem + ls_draws_at<T>(P));
     uint32_t* colC = dg + ((size_t)chain * P.M + l) * P.W;
     // the locus's inputs copied to the task's shared memory first
     uint8_t* sg = (uint8_t*)(wsmem + ls_gcol_at<T>(P));
@@ -495,12 +495,13 @@ __device__ int ls_locus(const ProblemDev& P, const OpDev* ops, const int32_t* op
     }
     if (lane == 0 && logroot) *logroot = log((double)root) + (double)scale * 0.69314718055994530942;
     for (int i = lane; i < P.N; i += G) assign[i] = -1;
-    // the backward pass's draws, one per operation, generated together
-    for (int j = lane; j < P.K; j += G) sdraw[j] = draws.get(cr, chain, unit, base + j);
     L.sync();
-    // backward sampling of ordered genotypes (SamplerRfunction::sample)
+    // backward sampling of ordered genotypes (SamplerRfunction::sample); the
+    // group's last lane draws the operation's uniform (one per operation, in
+    // the backward order) while the others work out its terms
     for (int k = P.K - 1; k >= 0; --k) {
         const OpDev op = ops[k];
+        const double rdraw = lane == G - 1 ? draws.get(cr, chain, unit, base + (P.K - 1 - k)) : 0.0;
         ls_dists<T, G>(P, op, opd, colL, colR, l, th, an, th2, an2, dist, lane);
         L.sync();
         const int32_t* cut = opd + op.cut_at;
@@ -531,6 +532,7 @@ __device__ int ls_locus(const ProblemDev& P, const OpDev* ops, const int32_t* op
                 pv = ls_term<T>(op, opd, A, off, dist, x, lane, tv);
             }
         }
+        const double rk_draw = L.shfl(rdraw, G - 1);
         const T p0 = L.shfl(pv, 0), p1 = L.shfl(pv, 1);
         const T p2 = L.shfl(pv, 2), p3 = L.shfl(pv, 3);
         if (lane == 0) {
@@ -539,7 +541,7 @@ __device__ int ls_locus(const ProblemDev& P, const OpDev* ops, const int32_t* op
             const T tot = Ar::add(Ar::add(Ar::add(p0, p1), p2), p3);
             if (tot != T(0))
                 for (int v = 0; v < 4; ++v) pd[v] = Ar::div(pd[v], tot);
-            const double r = sdraw[P.K - 1 - k];
+            const double r = rk_draw;
             T acc = T(0);
             int lastv = 0, pick = -1;
             for (int v = 0; v < 4; ++v) {
