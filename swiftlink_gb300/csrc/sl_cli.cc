@@ -39,7 +39,8 @@ struct Options {
     int chains = 1, exchange = 10;   // MC3 (defaults.h:9, 12)
     double lprob = 0.5;
     std::vector<double> temps;
-    bool trace = false, affected_only = false, verbose = false, exact = false, mc3 = false, generic_ls = false;
+    bool trace = false, affected_only = false, verbose = false, exact = false, mc3 = false, generic_ls = false,
+         compiled_ls = false;
 };
 
 std::vector<std::string> tokens(const std::string& line) {
@@ -489,7 +490,8 @@ void usage(const char* prog) {
             "  -y NUM    --exchangeperiod=NUM      (default = 10)\n"
             "  -t LIST   --temperatures=LIST       (comma separated, the first 1.0; default 1 / (1 + 0.001 2^i))\n"
             "  -E        --exact                   (FP64 samplers and LOD, the reference's arithmetic)\n"
-            "  -G        --genericls               (no L-sampler compiled for the pedigree on long runs)\n"
+            "  -G        --genericls               (the generic L-sampler, lanes per task by timing: the default)\n"
+            "  -J        --compiledls              (long runs: also compile the L-sampler for each pedigree)\n"
             "  -D FILE   --dumpproblem=FILE        (write the problem tables of every family and stop)\n"
             "  -W FILE   --writetable=FILE         (write the LOD table from FILE's per-family log-sums and stop:\n"
             "                                       per family a line \"count log_P(T)\", then (M-1)*n raw values)\n",
@@ -522,14 +524,14 @@ int main(int argc, char** argv) {
         {"sexlinked", no_argument, 0, 'X'},       {"elod", no_argument, 0, 'e'},
         {"verbose", no_argument, 0, 'v'},         {"help", no_argument, 0, 'h'},
         {"exact", no_argument, 0, 'E'},           {"dumpproblem", required_argument, 0, 'D'},
-        {"genericls", no_argument, 0, 'G'},     {"writetable", required_argument, 0, 'W'},
+        {"genericls", no_argument, 0, 'G'},     {"compiledls", no_argument, 0, 'J'},     {"writetable", required_argument, 0, 'W'},
         {"mcmcmc", no_argument, 0, 'M'},          {"chains", required_argument, 0, 'z'},
         {"exchangeperiod", required_argument, 0, 'y'}, {"temperatures", required_argument, 0, 't'},
         {"frequency", required_argument, 0, 'f'}, {"penetrance", required_argument, 0, 'k'},
         {"replicates", required_argument, 0, 'u'}, {"separation", required_argument, 0, 'w'},
         {0, 0, 0, 0}};
     int ch, ignored;
-    while ((ch = getopt_long(argc, argv, "p:m:d:o:i:b:s:x:l:n:R:TP:c:gq:r:aXevhED:Mz:y:t:f:k:u:w:GW:", longopts, nullptr)) != -1) {
+    while ((ch = getopt_long(argc, argv, "p:m:d:o:i:b:s:x:l:n:R:TP:c:gq:r:aXevhED:Mz:y:t:f:k:u:w:GJW:", longopts, nullptr)) != -1) {
         switch (ch) {
             case 'p': o.ped = optarg; break;
             case 'm': o.map = optarg; break;
@@ -555,6 +557,7 @@ int main(int argc, char** argv) {
             case 'D': o.dump = optarg; break;
             case 'M': o.mc3 = true; break;
             case 'G': o.generic_ls = true; break;
+            case 'J': o.compiled_ls = true; break;
             case 'W': o.write_from = optarg; break;
             case 'z': if (!to_int(optarg, o.chains) || o.chains < 1) { fprintf(stderr, "option '-z' requires an int > 0\n"); return 1; } break;
             case 'y': if (!to_int(optarg, o.exchange) || o.exchange < 1) { fprintf(stderr, "option '-y' requires an int > 0\n"); return 1; } break;
@@ -675,11 +678,12 @@ int main(int argc, char** argv) {
         so.lod_precision = o.exact ? SL_LOD_FP64 : SL_LOD_FP32_RESCALED;
         so.sampler_precision = o.exact ? SL_SAMPLER_EXACT : SL_SAMPLER_FAST;
         so.lod_flags = SL_LOD_ZERO_OK;
-        // long runs amortise compiling the L-sampler for the pedigree (same draws, same graphs); it
-        // compiles on a host thread while the run starts on the generic kernel, and pedigrees compile
-        // side by side (up to 2000 members: the generated source grows with the peel's shapes, and so
-        // does its compile time)
-        so.ls_kernel = !o.exact && !o.generic_ls && o.burnin + o.iterations >= 10000 && p.N <= 2000
+        // the generic L-sampler with its lanes per task chosen by timing (the compact rfunctions made
+        // it the faster kernel on the pedigrees measured); with -J, long runs also compile the
+        // L-sampler for the pedigree (same draws, same graphs) on a host thread while the run starts
+        // on the generic kernel, pedigrees side by side (up to 2000 members: the generated source
+        // grows with the peel's shapes, and so does its compile time)
+        so.ls_kernel = o.compiled_ls && !o.exact && !o.generic_ls && o.burnin + o.iterations >= 10000 && p.N <= 2000
                            ? SL_LS_KERNEL_BACKGROUND
                            : SL_LS_KERNEL_GENERIC;
         for (int r = 0; r < (o.mc3 ? o.runs : 1) && !rc; ++r) {

@@ -1377,6 +1377,8 @@ int sl_create(const sl_problem_desc* d, const sl_options* opt, sl_ctx** out) {
             }
             most = std::max(most, tot);
         }
+        if (most > 65535)   // the tasks' offsets are 16-bit (and such an arena would not fit shared memory)
+            return bail(fail(nullptr, SL_EINVAL, "L-sampler needs %d rfunction cells at one locus", most));
         P.ls_arena = most;
     }
     P.max_child = max_child;

@@ -211,7 +211,7 @@ struct LsCell {
 // (sampler_rfunction.cc:190-287, rfunction.cc:116-142); a previous rfunction
 // is read at its compact index, or as zero where the dense matrix held zero.
 template <typename T>
-__device__ T ls_term(const OpDev& op, const int32_t* opd, const T* Am, const int32_t* off, const T* dist,
+__device__ T ls_term(const OpDev& op, const int32_t* opd, const T* Am, const uint16_t* off, const T* dist,
                      const LsCell& x, int v, T tv) {
     using A = Ls<T>;
     const int ext = x.ext;
@@ -273,7 +273,7 @@ __device__ __forceinline__ int state_of_rank(int mask, int r) {   // the r-th al
 // A task's shared bytes: the rfunctions [ls_arena, compact], the children's
 // transmission distributions [16 per child], the sampled states [N], the
 // locus's genotype codes and masks [N], its neighbours' descent-graph words
-// [2 W], its prior row [16] and the ops' compact offsets [K + 1]; each part
+// [2 W], its prior row [16] and the ops' compact offsets [K + 1] (16-bit); each part
 // 16-byte aligned, so every task's base is aligned.  (The backward pass's
 // draws are made as it goes, one per operation: storing them took K doubles,
 // a third of a task on the 400-member pedigree.)
@@ -300,7 +300,7 @@ __host__ __device__ __forceinline__ size_t ls_off_at(const ProblemDev& P) {
 }
 template <typename T>
 __host__ __device__ __forceinline__ size_t ls_warp_bytes(const ProblemDev& P) {
-    return al16(ls_off_at<T>(P) + 4 * ((size_t)P.K + 1));
+    return al16(ls_off_at<T>(P) + 2 * ((size_t)P.K + 1));   // 16-bit offsets: the arena holds < 65,536 cells
 }
 
 // Block-shared copies of the peel's operations and their lists: every lane
@@ -344,7 +344,7 @@ __device__ int ls_locus(const ProblemDev& P, const OpDev* ops, const int32_t* op
     T* A = (T*)wsmem;
     T* dist = A + P.ls_arena;
     int8_t* assign = (int8_t*)(dist + 16 * P.max_child);
-    int32_t* off = (int32_t*)(wsmem + ls_off_at<T>(P));
+    uint16_t* off = (uint16_t*)(wsmem + ls_off_at<T>(P));
     uint32_t* colC = dg + ((size_t)chain * P.M + l) * P.W;
     // the locus's inputs copied to the task's shared memory first
     uint8_t* sg = (uint8_t*)(wsmem + ls_gcol_at<T>(P));
@@ -400,12 +400,12 @@ __device__ int ls_locus(const ProblemDev& P, const OpDev* ops, const int32_t* op
             const OpDev& op = ops[k];
             int b = 0;
             for (int q = 0; q < op.c; ++q) b += rank_bits((gcol[opd[op.cut_at + q]] >> 4) & 15);
-            off[k] = run;
+            off[k] = (uint16_t)run;
             run += 1 << b;
         }
-        if (lane == G - 1) off[P.K] = incl;
+        if (lane == G - 1) off[P.K] = (uint16_t)incl;
         L.sync();
-        if (off[P.K] > P.ls_arena) {   // cannot happen: the arena holds the most any locus needs
+        if (L.shfl(incl, G - 1) > P.ls_arena) {   // cannot happen: the arena holds the most any locus needs
             if (lane == 0) set_status(status, ST_ILLEGAL_DG);
             return -1;
         }
@@ -1451,7 +1451,7 @@ __device__ __forceinline__ void fagw_task(const ProblemDev& P, const FagwTables&
     // atomics, the same result in any order).  A fixed allele outside the
     // forest is a component of its own: its term is added directly.
     float sum = 0.f;
-    int zero = 0;
+    int zero = 0, forest = 0;
     const float lmaj = lfreq.x, lmin = lfreq.y;
     if (!bad)
         for (int x = gl; x < nfa; x += G) {
@@ -1462,6 +1462,7 @@ __device__ __forceinline__ void fagw_task(const ProblemDev& P, const FagwTables&
                 else sum += (f & 2) ? lmaj : lmin;
                 continue;
             }
+            forest = 1;
             int p = 0;
             const int r = pf_find(Lb, x, p);   // the forest is final: the unions are done
             // bit 16 + n: member count; bits 0-15: even-parity members; bits 29/30: colouring 0/1 forbidden
@@ -1472,8 +1473,9 @@ __device__ __forceinline__ void fagw_task(const ProblemDev& P, const FagwTables&
             atomicAdd(&cnt[r], add);
             if (forbid) atomicOr(&cnt[r], forbid);
         }
+    forest = grp.any(forest);   // no union: every term is in already
     __syncwarp();
-    if (!bad) {
+    if (!bad && forest) {
         for (int x = gl; x < nfa; x += G) {
             const int c = cnt[x];
             const int n = (c >> 16) & 0x1fff, even = c & 0xffff;

@@ -301,12 +301,12 @@ def test_mc3_runs_match_the_library(tmp_path):
 
 @pytest.mark.gpu
 def test_long_runs_compile_the_lsampler_with_the_same_table(tmp_path):
-    """Runs of 10,000 iterations or more use the L-sampler compiled for the
-    pedigree; it draws the generic kernel's graphs bit for bit, so the table
-    equals the one of the same run with -G (generic kernel)."""
+    """With -J, runs of 10,000 iterations or more use the L-sampler compiled
+    for the pedigree; it draws the generic kernel's graphs bit for bit, so the
+    table equals the one of the same run with -G (generic kernel)."""
     ped, mapf, dat = synth.workload_files(1, str(tmp_path))
     seedf = _write(tmp_path / "seeds", "3\n")
     common = ["-p", ped, "-m", mapf, "-d", dat, "-R", 2, "-s", 10, "-i", 6000, "-b", 4000, "-x", 50, "-r", seedf]
-    run_cli(*common, "-o", tmp_path / "spec.out")
+    run_cli(*common, "-o", tmp_path / "spec.out", "-J")
     run_cli(*common, "-o", tmp_path / "gen.out", "-G")
     assert (tmp_path / "spec.out").read_text() == (tmp_path / "gen.out").read_text()
