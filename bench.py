@@ -693,7 +693,8 @@ def adjoint_rate(device, G=1000, chunk=250):
         dt = time.perf_counter() - t
         kern_ms, kern_n = ctx.profile_read(api.SL_KERNEL_LOD)
         ctx.profile(False)
-        form, warp_ms, thread_ms = ctx.adjoint_info()
+        form, warp_ms, thread_ms, spec_ms = ctx.adjoint_info()
+        shapes, regs, compile_ms = ctx.adjoint_kernel_info()
         # the forward FP32 scorer on the same graphs, for the ratio
         ctx.lod_score_graphs(gset)
         ctx.synchronize()
@@ -706,9 +707,13 @@ def adjoint_rate(device, G=1000, chunk=250):
             "kernel_launches": int(kern_n),
             "forward_fp32_positions_per_s": fwd, "adjoint_segments": segs, "shared_bytes_per_warp": used,
             "form": {api.SL_ADJOINT_WARP: "one warp per position, shared memory",
-                     api.SL_ADJOINT_THREAD: "one thread per position, global arena"}.get(form, str(form)),
+                     api.SL_ADJOINT_THREAD: "one thread per position, global arena",
+                     api.SL_ADJOINT_SPECIALISED: "the peel's adjoint compiled for the pedigree, one thread per "
+                                                 "position, global arena"}.get(form, str(form)),
             "form_timing_ms": {"warp": round(warp_ms, 3), "thread": round(thread_ms, 3),
+                               "specialised": round(spec_ms, 3),
                                "tasks": 65536, "selection": "timed on the first call's first tasks"},
+            "specialised": {"shapes": shapes, "registers": regs, "compile_ms": round(compile_ms, 1)},
             "model": "dominant (0.01, 0.8, 0.9), q = 1e-3",
             "path": "sl_trait_backward: host graphs in, d log L / d (theta_L, theta_R, penetrances, q) out"}
 

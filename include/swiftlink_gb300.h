@@ -362,13 +362,17 @@ int sl_lod_score_device_graphs_noalloc(sl_ctx* ctx, int32_t n_graphs, const uint
  * ptrait_grad[4] (may be NULL) receives d log P(T) / d (penetrances, frequency)
  * (Peeler::calc_trait_prob, peeler.cc:65-73).  Needs the disease-model fields
  * of the problem.  The peel is recomputed on the device in FP32 with
- * power-of-two rescaling, in one of two forms: one warp per (graph, interval,
- * position) with the rfunctions in shared memory, or one thread per position
- * with them in a global arena (up to 4 GiB, a column per thread).  The first
- * call with graphs times both on its first tasks and keeps the faster
- * (sl_adjoint_info); both follow the memory plan of sl_adjoint_memory (kept,
- * or recomputed when they do not fit) and give the same values up to the
- * order of FP32 additions into shared adjoints.
+ * power-of-two rescaling, in one of three forms: one warp per (graph,
+ * interval, position) with the rfunctions in shared memory; one thread per
+ * position with them in a global arena (up to 4 GiB, a column per thread);
+ * or the peel and its reverse written out for this pedigree and compiled
+ * with NVRTC at the first call (one thread per position, every rfunction in a
+ * global arena of up to 4 GiB; only when the memory plan keeps every
+ * rfunction).  The first call with graphs times the forms on its first tasks
+ * and keeps the fastest (sl_adjoint_info), unless sl_adjoint_set_form fixed
+ * one; the first two follow the memory plan of sl_adjoint_memory (kept, or
+ * recomputed when they do not fit).  The forms give the same values up to the
+ * order of FP32 additions.
  */
 int sl_trait_backward(sl_ctx* ctx, int32_t n_graphs, const int32_t* dgs, double* grad, double* ptrait_grad);
 
@@ -386,12 +390,38 @@ int sl_trait_backward(sl_ctx* ctx, int32_t n_graphs, const int32_t* dgs, double*
  */
 int sl_adjoint_memory(sl_ctx* ctx, int64_t bytes_per_task, int32_t* segments, int64_t* used_bytes);
 
-/* The adjoint's form (SL_ADJOINT_WARP or SL_ADJOINT_THREAD; 0 before the
- * first call with graphs, and again after sl_adjoint_memory) and the times
- * of the timed launch of each (milliseconds; either pointer may be NULL). */
+/* The adjoint's form (SL_ADJOINT_WARP, SL_ADJOINT_THREAD or
+ * SL_ADJOINT_SPECIALISED; 0 before the first call with graphs, and again
+ * after sl_adjoint_memory or sl_adjoint_set_form) and the times of the timed
+ * launch of each (milliseconds, 0 for a form not timed; any pointer may be
+ * NULL). */
 #define SL_ADJOINT_WARP 1
 #define SL_ADJOINT_THREAD 2
-int sl_adjoint_info(sl_ctx* ctx, int32_t* form, double* warp_ms, double* thread_ms);
+#define SL_ADJOINT_SPECIALISED 3
+int sl_adjoint_info(sl_ctx* ctx, int32_t* form, double* warp_ms, double* thread_ms, double* specialised_ms);
+
+/* Fix the adjoint's form for the following calls (0: choose by timing, the
+ * default).  SL_ADJOINT_SPECIALISED needs a memory plan that keeps every
+ * rfunction (sl_adjoint_memory: one segment), else SL_EINVAL; a later plan
+ * that splits the peel returns the choice to timing.  If its NVRTC compile
+ * fails, the next sl_trait_backward returns SL_EINVAL with the compiler's
+ * log. */
+int sl_adjoint_set_form(sl_ctx* ctx, int32_t form);
+
+/* The specialised adjoint: the operation shapes it was generated with (one
+ * forward and one reverse function each), its registers per thread and its
+ * compile time in milliseconds (0 before it was needed, -1 if its compile
+ * failed); any pointer may be NULL. */
+int sl_adjoint_kernel_info(sl_ctx* ctx, int32_t* shapes, int32_t* regs, double* compile_ms);
+
+/* The specialised adjoint's CUDA C++ source for a problem (no device
+ * needed): up to cap - 1 bytes and a terminating zero into buf (buf may be
+ * NULL with cap 0), its length into *len and its operation shapes into
+ * *shapes; with compile != 0 it is also compiled with NVRTC for sm_103a
+ * (milliseconds into *compile_ms; SL_EINVAL with the compiler's log when it
+ * fails).  Any output pointer may be NULL. */
+int sl_problem_adjoint_source(const sl_problem_desc* problem, int32_t compile, char* buf, int64_t cap, int64_t* len,
+                              int32_t* shapes, double* compile_ms);
 
 /* The same adjoint for one graph and position evaluated on the host in FP64
  * (the reference gradient the device result is checked against); dg NULL

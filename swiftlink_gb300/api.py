@@ -24,7 +24,7 @@ SL_LOD_ZERO_OK = 1
 SL_LS_KERNEL_GENERIC, SL_LS_KERNEL_SPECIALISED, SL_LS_KERNEL_BACKGROUND, SL_LS_KERNEL_AUTO = 0, 1, 2, 3
 SL_LS_KERNEL_GENERIC32, SL_LS_KERNEL_GENERIC16, SL_LS_KERNEL_GENERIC8 = 4, 5, 6
 SL_KERNEL_LSAMPLER, SL_KERNEL_MSAMPLER, SL_KERNEL_LOD, SL_KERNEL_LOD_MERGE, SL_KERNEL_OTHER = 0, 1, 2, 3, 4
-SL_ADJOINT_WARP, SL_ADJOINT_THREAD = 1, 2
+SL_ADJOINT_WARP, SL_ADJOINT_THREAD, SL_ADJOINT_SPECIALISED = 1, 2, 3
 
 EXPORTED = [
     "sl_create", "sl_destroy", "sl_last_error", "sl_set_descent_graphs", "sl_get_descent_graphs",
@@ -36,6 +36,7 @@ EXPORTED = [
     "sl_problem_trait_backward_eval", "sl_lod_kernel_info", "sl_ls_kernel_info", "sl_set_temperatures", "sl_mc3_stats",
     "sl_chain_loglik", "sl_peel_sequence", "sl_batch_create", "sl_batch_run", "sl_batch_destroy",
     "sl_sequential_imputation", "sl_sequential_imputation_run", "sl_adjoint_memory", "sl_adjoint_info",
+    "sl_adjoint_set_form", "sl_adjoint_kernel_info", "sl_problem_adjoint_source",
 ]
 
 
@@ -341,13 +342,30 @@ class Context:
         return seg.value, used.value
 
     def adjoint_info(self):
-        """(SL_ADJOINT_WARP / SL_ADJOINT_THREAD or 0 before the first timed call,
-        the timed launch of each form in ms)."""
+        """(SL_ADJOINT_WARP / _THREAD / _SPECIALISED or 0 before the first
+        call, the timed launch of the warp, thread and specialised forms in ms,
+        0 for a form not timed)."""
         f = ctypes.c_int32()
         a = ctypes.c_double()
         b = ctypes.c_double()
-        self._check(lib().sl_adjoint_info(self.h, ctypes.byref(f), ctypes.byref(a), ctypes.byref(b)))
-        return f.value, a.value, b.value
+        c = ctypes.c_double()
+        self._check(lib().sl_adjoint_info(self.h, ctypes.byref(f), ctypes.byref(a), ctypes.byref(b),
+                                          ctypes.byref(c)))
+        return f.value, a.value, b.value, c.value
+
+    def adjoint_set_form(self, form: int = 0):
+        """Fix the adjoint's form (SL_ADJOINT_*), or 0 to choose by timing."""
+        self._check(lib().sl_adjoint_set_form(self.h, ctypes.c_int32(form)))
+
+    def adjoint_kernel_info(self):
+        """(operation shapes, registers per thread, compile ms) of the
+        specialised adjoint; compile ms 0 before it was needed, -1 if it did
+        not build."""
+        n = ctypes.c_int32()
+        r = ctypes.c_int32()
+        ms = ctypes.c_double()
+        self._check(lib().sl_adjoint_kernel_info(self.h, ctypes.byref(n), ctypes.byref(r), ctypes.byref(ms)))
+        return n.value, r.value, ms.value
 
     def trait_backward(self, dgs: Optional[np.ndarray] = None):
         """d log L / d (theta_L, theta_R, pen x3, frequency) at every LOD

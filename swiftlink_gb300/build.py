@@ -1,8 +1,8 @@
 """Build the in-tree CUDA library swiftlink_gb300/_build/libswiftlink_gb300.so.
 
-Six translation units compiled in parallel for sm_103a only, then linked
+Seven translation units compiled in parallel for sm_103a only, then linked
 with the static CUDA runtime and NVRTC (which compiles the problem-specialised
-LOD kernels when a context is created):
+kernels at run time):
   csrc/sl_kernels.cu  (nvcc, -gencode arch=compute_103a,code=sm_103a)
   csrc/sl_noalloc.cu  (nvcc, same flags)
   csrc/sl_host.cc     (g++ against the CUDA runtime headers)
@@ -11,6 +11,8 @@ LOD kernels when a context is created):
   csrc/sl_lsjit.cc    (g++, the L-sampler specialised per pedigree, NVRTC;
                        it embeds csrc/sl_philox.cuh, the Philox shared with
                        sl_kernels.cu, as a string generated into _build)
+  csrc/sl_adjjit.cc   (g++, the trait-peel adjoint specialised per pedigree,
+                       NVRTC)
 and the program swiftlink_gb300/_build/swift_gb300 (csrc/sl_cli.cc, the
 LINKAGE-file front end) linked against the library.
 """
@@ -60,7 +62,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
     os.makedirs(OUT, exist_ok=True)
     philox = os.path.join(CSRC, "sl_philox.cuh")
     hdrs = [os.path.join(CSRC, "sl_internal.h"), os.path.join(CSRC, "sl_jit.h"), os.path.join(CSRC, "sl_lsjit.h"),
-            philox, os.path.join(os.path.dirname(HERE), "include", "swiftlink_gb300.h")]
+            os.path.join(CSRC, "sl_adjjit.h"), philox, os.path.join(os.path.dirname(HERE), "include", "swiftlink_gb300.h")]
     # the Philox source as a C++ string literal, for the run-time compiled kernels
     inc = os.path.join(OUT, "sl_philox_src.inc")
     if force or _stale(inc, [philox]):
@@ -77,6 +79,8 @@ def build(verbose: bool = False, force: bool = False) -> str:
     pc_o = os.path.join(OUT, "sl_peel.o")
     lj = os.path.join(CSRC, "sl_lsjit.cc")
     lj_o = os.path.join(OUT, "sl_lsjit.o")
+    aj = os.path.join(CSRC, "sl_adjjit.cc")
+    aj_o = os.path.join(OUT, "sl_adjjit.o")
     cli = os.path.join(CSRC, "sl_cli.cc")
     cli_o = os.path.join(OUT, "sl_cli.o")
     cu_o = os.path.join(OUT, "sl_kernels.o")
@@ -87,7 +91,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
         if force or _stale(obj, [src] + hdrs):
             jobs.append([nvcc, GENCODE, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                          "-Xptxas", "-v", "-c", src, "-o", obj])
-    for src, obj in ((cc, cc_o), (jc, jc_o), (pc, pc_o), (cli, cli_o), (lj, lj_o)):
+    for src, obj in ((cc, cc_o), (jc, jc_o), (pc, pc_o), (cli, cli_o), (lj, lj_o), (aj, aj_o)):
         if force or _stale(obj, [src] + hdrs + ([inc] if src == lj else [])):
             # no contraction of a * b + c into FMA: host FP64 (priors, tempered maps,
             # likelihood sums) must round as the reference's x86-64 build does, on aarch64 too
@@ -98,9 +102,9 @@ def build(verbose: bool = False, force: bool = False) -> str:
     if jobs:
         with cf.ThreadPoolExecutor(len(jobs)) as ex:
             logs = list(ex.map(_run, jobs))
-    if force or jobs or _stale(LIB, [cu_o, cu2_o, cc_o, jc_o, pc_o, lj_o]):
+    if force or jobs or _stale(LIB, [cu_o, cu2_o, cc_o, jc_o, pc_o, lj_o, aj_o]):
         lib64 = os.path.join(cuda, "lib64")
-        logs.append(_run([nvcc, GENCODE, "-shared", "-cudart", "static", "-o", LIB, cu_o, cu2_o, cc_o, jc_o, pc_o, lj_o,
+        logs.append(_run([nvcc, GENCODE, "-shared", "-cudart", "static", "-o", LIB, cu_o, cu2_o, cc_o, jc_o, pc_o, lj_o, aj_o,
                           "-L" + lib64, "-lnvrtc", "-Xlinker", "-rpath=" + lib64]))
     if force or _stale(CLI, [cli_o, LIB]):
         lib64 = os.path.join(cuda, "lib64")

@@ -23,6 +23,7 @@
 #include <vector>
 
 #include "../../include/swiftlink_gb300.h"
+#include "sl_adjjit.h"
 #include "sl_internal.h"
 #include "sl_jit.h"
 #include "sl_lsjit.h"
@@ -176,14 +177,22 @@ struct sl_ctx {
     size_t adj_budget = 0;            // shared bytes per warp the plan must fit (0: the default)
     double* d_adjG = nullptr;        // [chunk][6] gradients
     int64_t adj_chunk = 0;
-    // the adjoint's two forms: one warp per task with its matrices in shared memory, or one thread
-    // per task with them in a global arena (a column per thread); chosen by timing the first call
-    int adj_form = 0;                 // 0 not yet timed, SL_ADJOINT_WARP, SL_ADJOINT_THREAD
-    double adj_form_ms[2] = {0.0, 0.0};
+    // the adjoint's forms: one warp per task with its matrices in shared memory, one thread per
+    // task with them in a global arena (a column per thread), or the peel's adjoint compiled for
+    // this pedigree (one thread per task, sl_adjjit.cc; only under a plan that keeps every
+    // matrix); chosen by timing the first call unless the caller fixed one (sl_adjoint_set_form)
+    int adj_form = 0;                 // 0 not yet timed, SL_ADJOINT_WARP, _THREAD, _SPECIALISED
+    int adj_form_req = 0;             // 0: by timing
+    double adj_form_ms[3] = {0.0, 0.0, 0.0};
     float* d_adjA = nullptr;          // [2 half][threads] matrices and adjoints of the thread form
     int* d_adjE = nullptr;            // [K][threads] their exponents
     int64_t adj_thr = 0;              // threads the arena holds
     size_t adj_thr_bytes = 0;
+    AdjJit adj_jit;                   // the specialised form (kern null: not built)
+    int adj_jit_state = 0;            // 0 not tried, 1 built, -1 its compile failed
+    std::string adj_jit_log;
+    float* d_adjJ = nullptr;          // its arena: blocks x adj_jit_block_floats
+    int64_t adj_jit_blocks = 0;
     // batched LOD kernel: the interpreter, or a problem-specialised form
     int lod_kernel_req = SL_LOD_KERNEL_AUTO;
     JitLs jit_ls;                     // the FP32 L-sampler specialised to the pedigree (kern null: generic)
@@ -1223,6 +1232,7 @@ void sl_destroy(sl_ctx* ctx) {
     jit_lod_release(&ctx->jit_reg);
     jit_ls_release(&ctx->jit_ls);
     jit_lod_release(&ctx->jit_smem);
+    adj_jit_release(&ctx->adj_jit);
     if (ctx->ms_graph) cudaGraphExecDestroy(ctx->ms_graph);
     if (ctx->run_graph) cudaGraphExecDestroy(ctx->run_graph);
     if (ctx->mc3_graph) cudaGraphExecDestroy(ctx->mc3_graph);
@@ -2361,27 +2371,96 @@ static int adjoint_arena(sl_ctx* ctx, int64_t ntask) {
     return SL_OK;
 }
 
+// The specialised form: compiled at its first use (NVRTC, sl_adjjit.cc), for
+// plans that keep every matrix.  Returns SL_OK with adj_jit_state 1 when it
+// can run.
+static int adjoint_jit_build(sl_ctx* ctx) {
+    if (ctx->adj_jit_state) return SL_OK;
+    AdjJitIn in;
+    in.ops = ctx->adj_ops.data();
+    in.K = (int)ctx->adj_ops.size();
+    in.od = ctx->adj_od.data();
+    in.F = ctx->P.F;
+    in.M = ctx->P.M;
+    in.n = ctx->P.n_lod;
+    in.W = ctx->P.W;
+    std::string log;
+    if (adj_jit_compile(in, &ctx->adj_jit, &log)) {
+        ctx->adj_jit_state = -1;
+        ctx->adj_jit_log = log;
+        return SL_OK;
+    }
+    ctx->adj_jit_state = 1;
+    return SL_OK;
+}
+
+static bool adjoint_jit_eligible(const sl_ctx* ctx) { return ctx->adj.nseg == 1; }
+
+// The specialised form's arena: the blocks that stay resident on every SM
+// (fewer for fewer tasks), each with its slice, within 4 GiB.
+static int adjoint_jit_arena(sl_ctx* ctx, int64_t ntask) {
+    const int64_t per = adj_jit_block_floats(ctx->adj_jit.half, ctx->P.K) * (int64_t)sizeof(float);
+    int64_t blocks = std::min<int64_t>((int64_t)ctx->sms * ctx->adj_jit.blocks_per_sm,
+                                       (ntask + kAdjJitThreads - 1) / kAdjJitThreads);
+    blocks = std::min<int64_t>(blocks, (int64_t(4) << 30) / per);
+    if (blocks < 1) return fail(ctx, SL_ENOMEM, "the specialised adjoint's arena needs %lld bytes per block", (long long)per);
+    if (ctx->d_adjJ && blocks <= ctx->adj_jit_blocks) return SL_OK;
+    cudaStreamSynchronize(ctx->stream);
+    if (ctx->d_adjJ) {
+        cudaFree(ctx->d_adjJ);
+        ctx->owned.erase(std::find(ctx->owned.begin(), ctx->owned.end(), (void*)ctx->d_adjJ));
+        ctx->d_adjJ = nullptr;
+        ctx->adj_jit_blocks = 0;
+    }
+    int rc;
+    if ((rc = dev_alloc(ctx, &ctx->d_adjJ, (size_t)(blocks * per / (int64_t)sizeof(float))))) return rc;
+    ctx->adj_jit_blocks = blocks;
+    return SL_OK;
+}
+
 static cudaError_t adjoint_launch(sl_ctx* ctx, int form, const uint32_t* graphs, int64_t words, int64_t t0,
                                   int64_t nt) {
     const ProblemDev& P = ctx->P;
+    if (form == SL_ADJOINT_SPECIALISED)
+        return adj_jit_launch(ctx->adj_jit, graphs, words, t0, nt, ctx->d_adjG, ctx->d_status, P.partial_f,
+                              ctx->d_adjJ, ctx->adj_jit_blocks, ctx->adj.dprob, ctx->adj.dgrad, P.lod_zero_ok,
+                              ctx->stream);
     if (form == SL_ADJOINT_THREAD)
         return launch_trait_adjoint_thr(P, ctx->adj, graphs, words, t0, nt, ctx->d_adjG, ctx->d_status, ctx->d_adjA,
                                         ctx->d_adjE, ctx->adj_thr, ctx->stream);
     return launch_trait_adjoint(P, ctx->adj, graphs, words, t0, nt, ctx->d_adjG, ctx->d_status, ctx->stream, ctx->sms);
 }
 
-// The first call with graphs times both forms on its first tasks (up to
-// 65,536) and keeps the faster for the context.
+// The first call with graphs times the forms on its first tasks (up to
+// 65,536) and keeps the fastest for the context; a form the caller fixed is
+// taken as is.
 static int adjoint_choose(sl_ctx* ctx, const uint32_t* graphs, int64_t words, int64_t ntask) {
     if (ctx->adj_form) return SL_OK;
-    const int64_t nt = std::min<int64_t>(ntask, 65536);
     int rc;
+    if (ctx->adj_form_req) {
+        if (ctx->adj_form_req == SL_ADJOINT_SPECIALISED) {
+            if ((rc = adjoint_jit_build(ctx))) return rc;
+            if (ctx->adj_jit_state != 1)
+                return fail(ctx, SL_EINVAL, "the specialised adjoint did not build: %s", ctx->adj_jit_log.c_str());
+        }
+        ctx->adj_form = ctx->adj_form_req;
+        return SL_OK;
+    }
+    const int64_t nt = std::min<int64_t>(ntask, 65536);
+    std::vector<int> forms = {SL_ADJOINT_WARP, SL_ADJOINT_THREAD};
+    if (adjoint_jit_eligible(ctx)) {
+        if ((rc = adjoint_jit_build(ctx))) return rc;
+        if (ctx->adj_jit_state == 1) forms.push_back(SL_ADJOINT_SPECIALISED);
+    }
     if ((rc = adjoint_arena(ctx, nt))) return rc;
+    if (ctx->adj_jit_state == 1 && adjoint_jit_eligible(ctx) && (rc = adjoint_jit_arena(ctx, nt))) return rc;
     int st = 0;
     CK(cudaStreamSynchronize(ctx->stream));
     CK(cudaMemcpy(&st, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost));
     cudaEvent_t a = take_event(ctx), b = take_event(ctx);
-    for (int form : {SL_ADJOINT_WARP, SL_ADJOINT_THREAD}) {
+    for (int i = 0; i < 3; ++i) ctx->adj_form_ms[i] = 0.0;
+    int best = 0;
+    for (int form : forms) {
         CK(adjoint_launch(ctx, form, graphs, words, 0, std::min<int64_t>(nt, 1024)));   // warm-up
         CK(cudaEventRecord(a, ctx->stream));
         CK(adjoint_launch(ctx, form, graphs, words, 0, nt));
@@ -2390,11 +2469,12 @@ static int adjoint_choose(sl_ctx* ctx, const uint32_t* graphs, int64_t words, in
         float ms = 0.f;
         CK(cudaEventElapsedTime(&ms, a, b));
         ctx->adj_form_ms[form - 1] = ms;
+        if (!best || ms < ctx->adj_form_ms[best - 1]) best = form;
     }
     ctx->event_pool.push_back(a);
     ctx->event_pool.push_back(b);
     CK(cudaMemcpy(ctx->d_status, &st, sizeof(int), cudaMemcpyHostToDevice));   // the timing runs report nothing
-    ctx->adj_form = ctx->adj_form_ms[1] < ctx->adj_form_ms[0] ? SL_ADJOINT_THREAD : SL_ADJOINT_WARP;
+    ctx->adj_form = best;
     return SL_OK;
 }
 
@@ -2437,6 +2517,8 @@ int sl_trait_backward(sl_ctx* ctx, int32_t n_graphs, const int32_t* dgs, double*
     if ((rc = adjoint_chunk(ctx, ntask))) return rc;
     if ((rc = adjoint_choose(ctx, ctx->d_graphs, (int64_t)words, ntask))) return rc;
     if (ctx->adj_form == SL_ADJOINT_THREAD && (rc = adjoint_arena(ctx, std::min(ctx->adj_chunk, ntask)))) return rc;
+    if (ctx->adj_form == SL_ADJOINT_SPECIALISED && (rc = adjoint_jit_arena(ctx, std::min(ctx->adj_chunk, ntask))))
+        return rc;
     for (int64_t t0 = 0; t0 < ntask; t0 += ctx->adj_chunk) {
         const int64_t nt = std::min(ctx->adj_chunk, ntask - t0);
         {
@@ -2460,16 +2542,41 @@ int sl_adjoint_memory(sl_ctx* ctx, int64_t bytes_per_task, int32_t* segments, in
     ctx->adj_budget = (size_t)bytes_per_task;
     if (int rc = plan_adjoint(ctx)) return fail(ctx, rc, "%s", sl_last_error(nullptr));
     ctx->adj_form = 0;   // timed again under the new plan
+    if (ctx->adj_form_req == SL_ADJOINT_SPECIALISED && !adjoint_jit_eligible(ctx))
+        ctx->adj_form_req = 0;   // the specialised form keeps every matrix: not under a split plan
     if (segments) *segments = ctx->adj.nseg;
     if (used_bytes) *used_bytes = ctx->adj.warp_bytes;
     return SL_OK;
 }
 
-int sl_adjoint_info(sl_ctx* ctx, int32_t* form, double* warp_ms, double* thread_ms) {
+int sl_adjoint_info(sl_ctx* ctx, int32_t* form, double* warp_ms, double* thread_ms, double* specialised_ms) {
     if (!ctx) return fail(ctx, SL_EINVAL, "null context");
     if (form) *form = ctx->adj_form;
     if (warp_ms) *warp_ms = ctx->adj_form_ms[0];
     if (thread_ms) *thread_ms = ctx->adj_form_ms[1];
+    if (specialised_ms) *specialised_ms = ctx->adj_form_ms[2];
+    return SL_OK;
+}
+
+int sl_adjoint_set_form(sl_ctx* ctx, int32_t form) {
+    if (!ctx) return fail(ctx, SL_EINVAL, "null context");
+    if (!ctx->has_adjoint)
+        return fail(ctx, SL_EINVAL, "no trait-peel adjoint: the problem carries no disease model (affection is NULL) "
+                                    "or an op multiplies more than 8 rfunctions");
+    if (form < 0 || form > SL_ADJOINT_SPECIALISED) return fail(ctx, SL_EINVAL, "unknown adjoint form %d", form);
+    if (form == SL_ADJOINT_SPECIALISED && !adjoint_jit_eligible(ctx))
+        return fail(ctx, SL_EINVAL, "the specialised adjoint keeps every matrix: the memory plan splits the peel "
+                                    "into %d segments", ctx->adj.nseg);
+    ctx->adj_form_req = form;
+    ctx->adj_form = 0;
+    return SL_OK;
+}
+
+int sl_adjoint_kernel_info(sl_ctx* ctx, int32_t* shapes, int32_t* regs, double* compile_ms) {
+    if (!ctx) return fail(ctx, SL_EINVAL, "null context");
+    if (shapes) *shapes = ctx->adj_jit_state == 1 ? ctx->adj_jit.shapes : 0;
+    if (regs) *regs = ctx->adj_jit_state == 1 ? ctx->adj_jit.regs : 0;
+    if (compile_ms) *compile_ms = ctx->adj_jit_state == 1 ? ctx->adj_jit.compile_ms : (ctx->adj_jit_state ? -1.0 : 0.0);
     return SL_OK;
 }
 
@@ -2486,6 +2593,42 @@ int sl_problem_trait_backward_eval(const sl_problem_desc* d, const int32_t* dg, 
     LodProgram prog;
     compile_lod_program(d, ops, od, prog, true);
     return host_backward(d, prog, dg, locus, offset, grad, nullptr);
+}
+
+int sl_problem_adjoint_source(const sl_problem_desc* d, int32_t compile, char* buf, int64_t cap, int64_t* len,
+                              int32_t* shapes, double* compile_ms) {
+    int rc = check_desc(d);
+    if (rc) return rc;
+    if (cap < 0 || (cap > 0 && !buf)) return fail(nullptr, SL_EINVAL, "bad buffer");
+    std::vector<OpDev> ops;
+    std::vector<int32_t> od;
+    int arena = 0, max_child = 1;
+    if ((rc = build_ops(d, ops, od, arena, max_child))) return rc;
+    AdjJitIn in;
+    in.ops = ops.data();
+    in.K = (int)ops.size();
+    in.od = od.data();
+    in.F = d->n_founders;
+    in.M = d->n_markers;
+    in.n = d->lod_per_interval;
+    in.W = (2 * (d->n_members - d->n_founders) + 31) / 32;
+    int ns = 0, half = 0;
+    const std::string src = adj_jit_source(in, &ns, &half);
+    if (len) *len = (int64_t)src.size();
+    if (shapes) *shapes = ns;
+    if (buf && cap > 0) {
+        const size_t n = std::min<size_t>(src.size(), (size_t)cap - 1);
+        std::memcpy(buf, src.data(), n);
+        buf[n] = 0;
+    }
+    if (compile) {
+        const auto t0 = std::chrono::steady_clock::now();
+        const std::shared_ptr<const JitBinary> bin = jit_binary(src, "sl_adj_jit.cu");
+        if (compile_ms)
+            *compile_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        if (bin->rc) return fail(nullptr, SL_EINVAL, "the specialised adjoint did not compile: %s", bin->log.c_str());
+    }
+    return SL_OK;
 }
 
 // Philox4x32-10 uniform, the device stream's host twin (the L/M choice of a

@@ -246,6 +246,67 @@ def test_device_adjoint_400_member_pedigree_recomputes():
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("form", [api.SL_ADJOINT_WARP, api.SL_ADJOINT_THREAD, api.SL_ADJOINT_SPECIALISED])
+@pytest.mark.parametrize("model", ["recessive", "dominant"])
+@pytest.mark.parametrize("name", CASES)
+def test_each_adjoint_form_matches_host_fp64(name, model, form):
+    """Each form fixed by sl_adjoint_set_form -- the warp form, the thread
+    form and the peel's adjoint compiled for the pedigree -- against the
+    FP64 host adjoint at every position of every golden graph."""
+    g = load_golden(name)
+    d = g if model == "recessive" else with_model(g, *DOMINANT)
+    n = g["n_lod"]
+    graphs = np.ascontiguousarray(g["lod_graphs"], np.int32)
+    with api.Context(api.Problem.from_arrays(d), n_chains=1) as ctx:
+        ctx.adjoint_set_form(form)
+        grad, _ = ctx.trait_backward(graphs)
+        assert ctx.adjoint_info()[0] == form
+        if form == api.SL_ADJOINT_SPECIALISED:
+            shapes, regs, ms = ctx.adjoint_kernel_info()
+            assert shapes >= 1 and regs > 0 and ms > 0
+    positions = [(l, o) for l in range(g["M"] - 1) for o in range(n)]
+    for b in range(graphs.shape[0]):
+        want = host_all(d, graphs[b], positions)
+        got = grad[b].reshape(-1, 6)
+        for k in range(6):
+            assert rel_err(got[:, k], want[:, k]) <= GRAD_RTOL, (b, k, rel_err(got[:, k], want[:, k]))
+
+
+@pytest.mark.gpu
+def test_specialised_adjoint_large_pedigree_and_timed_choice():
+    """The 120-member, 2000-SNP pedigree under the dominant model: the
+    compiled adjoint of its starting graph at sampled positions against the
+    host; the timed choice then covers all three forms.  Under a plan that
+    splits the peel the compiled form (which keeps every rfunction) is
+    refused and left out of the timing."""
+    from swiftlink_gb300.workloads import load_problem
+    g = load_problem("cfg2")
+    d = with_model(g, *DOMINANT)
+    n = g["n_lod"]
+    dg = np.ascontiguousarray(g["dg0"], np.int32)
+    positions = [(l, o) for l in sample_loci(g["M"], 11) for o in range(n)]
+    want = host_all(d, dg, positions)
+    with api.Context(api.Problem.from_arrays(d), n_chains=1) as ctx:
+        ctx.adjoint_set_form(api.SL_ADJOINT_SPECIALISED)
+        grad, _ = ctx.trait_backward(dg[None])
+        got = np.array([grad[0, l, o] for l, o in positions])
+        for k in range(6):
+            assert rel_err(got[:, k], want[:, k]) <= GRAD_RTOL, (k, rel_err(got[:, k], want[:, k]))
+        ctx.adjoint_set_form(0)
+        ctx.trait_backward(dg[None])
+        form, warp_ms, thread_ms, spec_ms = ctx.adjoint_info()
+        assert warp_ms > 0 and thread_ms > 0 and spec_ms > 0
+        assert form in (api.SL_ADJOINT_WARP, api.SL_ADJOINT_THREAD, api.SL_ADJOINT_SPECIALISED)
+        seg, _ = ctx.adjoint_memory(256)
+        assert seg > 1
+        with pytest.raises(api.SwiftLinkError):
+            ctx.adjoint_set_form(api.SL_ADJOINT_SPECIALISED)
+        ctx.trait_backward(dg[None])
+        form, warp_ms, thread_ms, spec_ms = ctx.adjoint_info()
+        assert spec_ms == 0 and form in (api.SL_ADJOINT_WARP, api.SL_ADJOINT_THREAD)
+
+
+@pytest.mark.gpu
 def test_autograd_function_wrapper_matches_finite_differences():
     """The C-ABI backward behind a torch.autograd.Function (test harness only):
     log L [G][M-1][n] as a function of partial theta [M-1], the penetrances
