@@ -366,9 +366,9 @@ int sl_lod_score_device_graphs_noalloc(sl_ctx* ctx, int32_t n_graphs, const uint
  * interval, position) with the rfunctions in shared memory; one thread per
  * position with them in a global arena (up to 4 GiB, a column per thread);
  * or the peel and its reverse written out for this pedigree and compiled
- * with NVRTC at the first call (one thread per position, every rfunction in a
- * global arena of up to 4 GiB; only when the memory plan keeps every
- * rfunction).  The first call with graphs times the forms on its first tasks
+ * with NVRTC at the first call, in SL_ADJOINT_VARIANTS variants (one thread per
+ * position, every rfunction in a global arena of up to 4 GiB; only when the
+ * memory plan keeps every rfunction).  The first call with graphs times the forms on its first tasks
  * and keeps the fastest (sl_adjoint_info), unless sl_adjoint_set_form fixed
  * one; the first two follow the memory plan of sl_adjoint_memory (kept, or
  * recomputed when they do not fit).  The forms give the same values up to the
@@ -409,19 +409,23 @@ int sl_adjoint_info(sl_ctx* ctx, int32_t* form, double* warp_ms, double* thread_
 int sl_adjoint_set_form(sl_ctx* ctx, int32_t form);
 
 /* The specialised adjoint: the operation shapes it was generated with (one
- * forward and one reverse function each), its registers per thread and its
- * compile time in milliseconds (0 before it was needed, -1 if its compile
- * failed); any pointer may be NULL. */
+ * forward and one reverse function each), the registers per thread of the
+ * variant in use (the fastest when timed; see sl_problem_adjoint_source) and
+ * the compile time of its variants in milliseconds (0 before it was needed,
+ * -1 if its compile failed); any pointer may be NULL. */
 int sl_adjoint_kernel_info(sl_ctx* ctx, int32_t* shapes, int32_t* regs, double* compile_ms);
 
 /* The specialised adjoint's CUDA C++ source for a problem (no device
- * needed): up to cap - 1 bytes and a terminating zero into buf (buf may be
- * NULL with cap 0), its length into *len and its operation shapes into
- * *shapes; with compile != 0 it is also compiled with NVRTC for sm_103a
- * (milliseconds into *compile_ms; SL_EINVAL with the compiler's log when it
- * fails).  Any output pointer may be NULL. */
-int sl_problem_adjoint_source(const sl_problem_desc* problem, int32_t compile, char* buf, int64_t cap, int64_t* len,
-                              int32_t* shapes, double* compile_ms);
+ * needed), one of its SL_ADJOINT_VARIANTS variants (0: 4 blocks per SM, 1: 8,
+ * 2 and 3 the same with L2 prefetches of each next operation's arena lines):
+ * up to cap - 1 bytes and a terminating zero into buf (buf may be NULL with
+ * cap 0), its length into *len and its operation shapes into *shapes; with
+ * compile != 0 it is also compiled with NVRTC for sm_103a (milliseconds into
+ * *compile_ms; SL_EINVAL with the compiler's log when it fails).  Any output
+ * pointer may be NULL. */
+#define SL_ADJOINT_VARIANTS 4
+int sl_problem_adjoint_source(const sl_problem_desc* problem, int32_t variant, int32_t compile, char* buf,
+                              int64_t cap, int64_t* len, int32_t* shapes, double* compile_ms);
 
 /* The same adjoint for one graph and position evaluated on the host in FP64
  * (the reference gradient the device result is checked against); dg NULL

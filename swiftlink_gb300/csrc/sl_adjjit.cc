@@ -511,6 +511,7 @@ std::string adj_jit_source(const AdjJitIn& in, int* shapes_out, int* half_out) {
     emitf(s, "#define HB %lld\n", (long long)half * kAdjJitThreads);
     s += "struct G6 { float l, r, p0, p1, p2, q; };\n";
     s += kPow2;
+    s += "__device__ __forceinline__ void pfl2(const float* p) { asm volatile(\"prefetch.global.L2 [%0];\" :: \"l\"(p)); }\n";
     for (size_t i = 0; i < uniq.size(); ++i) {
         emit_forward(s, uniq[i], (int)i);
         emit_reverse(s, uniq[i], (int)i);
@@ -526,7 +527,7 @@ std::string adj_jit_source(const AdjJitIn& in, int* shapes_out, int* half_out) {
           "    long long task0, long long ntask, double* __restrict__ grad, int* status,\n"
           "    const float* __restrict__ partial, float* __restrict__ arena, const float* __restrict__ dprob,\n"
           "    const float4* __restrict__ dgrad, int zero_ok) {\n",
-          kAdjJitThreads, kAdjJitMinBlocks);
+          kAdjJitThreads, in.min_blocks > 0 ? in.min_blocks : 1);
     emitf(s, "  float* Ab = arena + (long long)blockIdx.x * %lldLL + threadIdx.x;\n",
           (long long)adj_jit_block_floats(half, K));
     emitf(s, "  const long long npos = %lldLL;\n", (long long)npos);
@@ -556,7 +557,22 @@ std::string adj_jit_source(const AdjJitIn& in, int* shapes_out, int* half_out) {
         a += ", th, an, th2, an2";
         return a;
     };
-    for (int k = 0; k < K; ++k) emitf(s, "    F%d(%s);\n", sid[k], args(k, false).c_str());
+    // with prefetch: before each op, the lines the op after it reads are
+    // asked into L2 (its previous rfunctions' matrices; in the reverse, also
+    // its cells' adjoints), one 128-byte line per warp and arena slot
+    auto prefetch = [&](int k, bool reverse) {
+        if (!in.prefetch || k < 0 || k >= K) return;
+        if (reverse)
+            emitf(s, "    for (int q = 0; q < %d; ++q) pfl2(Ab + HB + %d + q * %d);\n", 1 << (2 * in.ops[k].c),
+                  aoff[k] * kAdjJitThreads, kAdjJitThreads);
+        for (const Prev& p : shapes[k].prev)
+            emitf(s, "    for (int q = 0; q < %d; ++q) pfl2(Ab + %d + q * %d);\n", 1 << (2 * p.c),
+                  aoff[p.op] * kAdjJitThreads, kAdjJitThreads);
+    };
+    for (int k = 0; k < K; ++k) {
+        prefetch(k + 1, false);
+        emitf(s, "    F%d(%s);\n", sid[k], args(k, false).c_str());
+    }
     emitf(s, "    const float root = Ab[%d];\n", aoff[K - 1] * kAdjJitThreads);
     emitf(s,
           "    if (!(root > 0.0f)) {\n"
@@ -566,11 +582,13 @@ std::string adj_jit_source(const AdjJitIn& in, int* shapes_out, int* half_out) {
           (int)ST_LOD_NONPOS);
     emitf(s, "    Ab[HB + %d] = 1.0f / root;\n", aoff[K - 1] * kAdjJitThreads);
     s += "    double g0 = 0.0, g1 = 0.0, g2 = 0.0, g3 = 0.0, g4 = 0.0, g5 = 0.0;\n";
-    for (int k = K - 1; k >= 0; --k)
+    for (int k = K - 1; k >= 0; --k) {
+        prefetch(k - 1, true);
         emitf(s,
               "    { const G6 r = R%d(%s); g0 += (double)r.l; g1 += (double)r.r; g2 += (double)r.p0; g3 += (double)r.p1; "
               "g4 += (double)r.p2; g5 += (double)r.q; }\n",
               sid[k], args(k, true).c_str());
+    }
     s += "    double* gp = grad + u * 6;\n";
     s += "    gp[0] = g0; gp[1] = g1; gp[2] = g2; gp[3] = g3; gp[4] = g4; gp[5] = g5;\n";
     s += "  }\n}\n";
@@ -587,6 +605,7 @@ int adj_jit_compile(const AdjJitIn& in, AdjJit* out, std::string* log) {
     if (jit_compile_kernel(src, "sl_adj_jit.cu", "sl_adj_jit", &out->lib, &out->kern, log)) return -1;
     out->half = half;
     out->shapes = shapes;
+    out->min_blocks = in.min_blocks;
     cudaFuncAttributes fa{};
     if (cudaFuncGetAttributes(&fa, (const void*)out->kern) == cudaSuccess) {
         out->regs = fa.numRegs;

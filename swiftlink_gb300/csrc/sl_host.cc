@@ -188,7 +188,8 @@ struct sl_ctx {
     int* d_adjE = nullptr;            // [K][threads] their exponents
     int64_t adj_thr = 0;              // threads the arena holds
     size_t adj_thr_bytes = 0;
-    AdjJit adj_jit;                   // the specialised form (kern null: not built)
+    AdjJit adj_jit_v[kAdjJitVariants];   // the specialised form at each register budget
+    int adj_jit_sel = 0;              // the variant in use (timed with the forms)
     int adj_jit_state = 0;            // 0 not tried, 1 built, -1 its compile failed
     std::string adj_jit_log;
     float* d_adjJ = nullptr;          // its arena: blocks x adj_jit_block_floats
@@ -1232,7 +1233,7 @@ void sl_destroy(sl_ctx* ctx) {
     jit_lod_release(&ctx->jit_reg);
     jit_ls_release(&ctx->jit_ls);
     jit_lod_release(&ctx->jit_smem);
-    adj_jit_release(&ctx->adj_jit);
+    for (AdjJit& j : ctx->adj_jit_v) adj_jit_release(&j);
     if (ctx->ms_graph) cudaGraphExecDestroy(ctx->ms_graph);
     if (ctx->run_graph) cudaGraphExecDestroy(ctx->run_graph);
     if (ctx->mc3_graph) cudaGraphExecDestroy(ctx->mc3_graph);
@@ -2384,12 +2385,18 @@ static int adjoint_jit_build(sl_ctx* ctx) {
     in.M = ctx->P.M;
     in.n = ctx->P.n_lod;
     in.W = ctx->P.W;
-    std::string log;
-    if (adj_jit_compile(in, &ctx->adj_jit, &log)) {
-        ctx->adj_jit_state = -1;
-        ctx->adj_jit_log = log;
-        return SL_OK;
+    for (int v = 0; v < kAdjJitVariants; ++v) {
+        in.min_blocks = kAdjJitMinBlocks[v];
+        in.prefetch = kAdjJitPrefetch[v];
+        std::string log;
+        if (adj_jit_compile(in, &ctx->adj_jit_v[v], &log)) {
+            for (AdjJit& j : ctx->adj_jit_v) adj_jit_release(&j);
+            ctx->adj_jit_state = -1;
+            ctx->adj_jit_log = log;
+            return SL_OK;
+        }
     }
+    ctx->adj_jit_sel = 0;
     ctx->adj_jit_state = 1;
     return SL_OK;
 }
@@ -2398,9 +2405,9 @@ static bool adjoint_jit_eligible(const sl_ctx* ctx) { return ctx->adj.nseg == 1;
 
 // The specialised form's arena: the blocks that stay resident on every SM
 // (fewer for fewer tasks), each with its slice, within 4 GiB.
-static int adjoint_jit_arena(sl_ctx* ctx, int64_t ntask) {
-    const int64_t per = adj_jit_block_floats(ctx->adj_jit.half, ctx->P.K) * (int64_t)sizeof(float);
-    int64_t blocks = std::min<int64_t>((int64_t)ctx->sms * ctx->adj_jit.blocks_per_sm,
+static int adjoint_jit_arena(sl_ctx* ctx, int64_t ntask, const AdjJit& j) {
+    const int64_t per = adj_jit_block_floats(j.half, ctx->P.K) * (int64_t)sizeof(float);
+    int64_t blocks = std::min<int64_t>((int64_t)ctx->sms * j.blocks_per_sm,
                                        (ntask + kAdjJitThreads - 1) / kAdjJitThreads);
     blocks = std::min<int64_t>(blocks, (int64_t(4) << 30) / per);
     if (blocks < 1) return fail(ctx, SL_ENOMEM, "the specialised adjoint's arena needs %lld bytes per block", (long long)per);
@@ -2422,7 +2429,7 @@ static cudaError_t adjoint_launch(sl_ctx* ctx, int form, const uint32_t* graphs,
                                   int64_t nt) {
     const ProblemDev& P = ctx->P;
     if (form == SL_ADJOINT_SPECIALISED)
-        return adj_jit_launch(ctx->adj_jit, graphs, words, t0, nt, ctx->d_adjG, ctx->d_status, P.partial_f,
+        return adj_jit_launch(ctx->adj_jit_v[ctx->adj_jit_sel], graphs, words, t0, nt, ctx->d_adjG, ctx->d_status, P.partial_f,
                               ctx->d_adjJ, ctx->adj_jit_blocks, ctx->adj.dprob, ctx->adj.dgrad, P.lod_zero_ok,
                               ctx->stream);
     if (form == SL_ADJOINT_THREAD)
@@ -2453,7 +2460,9 @@ static int adjoint_choose(sl_ctx* ctx, const uint32_t* graphs, int64_t words, in
         if (ctx->adj_jit_state == 1) forms.push_back(SL_ADJOINT_SPECIALISED);
     }
     if ((rc = adjoint_arena(ctx, nt))) return rc;
-    if (ctx->adj_jit_state == 1 && adjoint_jit_eligible(ctx) && (rc = adjoint_jit_arena(ctx, nt))) return rc;
+    if (ctx->adj_jit_state == 1 && adjoint_jit_eligible(ctx))
+        for (const AdjJit& j : ctx->adj_jit_v)
+            if ((rc = adjoint_jit_arena(ctx, nt, j))) return rc;
     int st = 0;
     CK(cudaStreamSynchronize(ctx->stream));
     CK(cudaMemcpy(&st, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost));
@@ -2461,15 +2470,25 @@ static int adjoint_choose(sl_ctx* ctx, const uint32_t* graphs, int64_t words, in
     for (int i = 0; i < 3; ++i) ctx->adj_form_ms[i] = 0.0;
     int best = 0;
     for (int form : forms) {
-        CK(adjoint_launch(ctx, form, graphs, words, 0, std::min<int64_t>(nt, 1024)));   // warm-up
-        CK(cudaEventRecord(a, ctx->stream));
-        CK(adjoint_launch(ctx, form, graphs, words, 0, nt));
-        CK(cudaEventRecord(b, ctx->stream));
-        CK(cudaEventSynchronize(b));
-        float ms = 0.f;
-        CK(cudaEventElapsedTime(&ms, a, b));
-        ctx->adj_form_ms[form - 1] = ms;
-        if (!best || ms < ctx->adj_form_ms[best - 1]) best = form;
+        // the compiled form: each register budget, the faster kept
+        const int nv = form == SL_ADJOINT_SPECIALISED ? kAdjJitVariants : 1;
+        int best_v = 0;
+        for (int v = 0; v < nv; ++v) {
+            if (form == SL_ADJOINT_SPECIALISED) ctx->adj_jit_sel = v;
+            CK(adjoint_launch(ctx, form, graphs, words, 0, std::min<int64_t>(nt, 1024)));   // warm-up
+            CK(cudaEventRecord(a, ctx->stream));
+            CK(adjoint_launch(ctx, form, graphs, words, 0, nt));
+            CK(cudaEventRecord(b, ctx->stream));
+            CK(cudaEventSynchronize(b));
+            float ms = 0.f;
+            CK(cudaEventElapsedTime(&ms, a, b));
+            if (v == 0 || ms < ctx->adj_form_ms[form - 1]) {
+                ctx->adj_form_ms[form - 1] = ms;
+                best_v = v;
+            }
+        }
+        if (form == SL_ADJOINT_SPECIALISED) ctx->adj_jit_sel = best_v;
+        if (!best || ctx->adj_form_ms[form - 1] < ctx->adj_form_ms[best - 1]) best = form;
     }
     ctx->event_pool.push_back(a);
     ctx->event_pool.push_back(b);
@@ -2517,7 +2536,8 @@ int sl_trait_backward(sl_ctx* ctx, int32_t n_graphs, const int32_t* dgs, double*
     if ((rc = adjoint_chunk(ctx, ntask))) return rc;
     if ((rc = adjoint_choose(ctx, ctx->d_graphs, (int64_t)words, ntask))) return rc;
     if (ctx->adj_form == SL_ADJOINT_THREAD && (rc = adjoint_arena(ctx, std::min(ctx->adj_chunk, ntask)))) return rc;
-    if (ctx->adj_form == SL_ADJOINT_SPECIALISED && (rc = adjoint_jit_arena(ctx, std::min(ctx->adj_chunk, ntask))))
+    if (ctx->adj_form == SL_ADJOINT_SPECIALISED &&
+        (rc = adjoint_jit_arena(ctx, std::min(ctx->adj_chunk, ntask), ctx->adj_jit_v[ctx->adj_jit_sel])))
         return rc;
     for (int64_t t0 = 0; t0 < ntask; t0 += ctx->adj_chunk) {
         const int64_t nt = std::min(ctx->adj_chunk, ntask - t0);
@@ -2574,9 +2594,12 @@ int sl_adjoint_set_form(sl_ctx* ctx, int32_t form) {
 
 int sl_adjoint_kernel_info(sl_ctx* ctx, int32_t* shapes, int32_t* regs, double* compile_ms) {
     if (!ctx) return fail(ctx, SL_EINVAL, "null context");
-    if (shapes) *shapes = ctx->adj_jit_state == 1 ? ctx->adj_jit.shapes : 0;
-    if (regs) *regs = ctx->adj_jit_state == 1 ? ctx->adj_jit.regs : 0;
-    if (compile_ms) *compile_ms = ctx->adj_jit_state == 1 ? ctx->adj_jit.compile_ms : (ctx->adj_jit_state ? -1.0 : 0.0);
+    const AdjJit& j = ctx->adj_jit_v[ctx->adj_jit_sel];
+    double ms = 0.0;
+    for (const AdjJit& v : ctx->adj_jit_v) ms += v.compile_ms;
+    if (shapes) *shapes = ctx->adj_jit_state == 1 ? j.shapes : 0;
+    if (regs) *regs = ctx->adj_jit_state == 1 ? j.regs : 0;
+    if (compile_ms) *compile_ms = ctx->adj_jit_state == 1 ? ms : (ctx->adj_jit_state ? -1.0 : 0.0);
     return SL_OK;
 }
 
@@ -2595,11 +2618,12 @@ int sl_problem_trait_backward_eval(const sl_problem_desc* d, const int32_t* dg, 
     return host_backward(d, prog, dg, locus, offset, grad, nullptr);
 }
 
-int sl_problem_adjoint_source(const sl_problem_desc* d, int32_t compile, char* buf, int64_t cap, int64_t* len,
-                              int32_t* shapes, double* compile_ms) {
+int sl_problem_adjoint_source(const sl_problem_desc* d, int32_t variant, int32_t compile, char* buf, int64_t cap,
+                              int64_t* len, int32_t* shapes, double* compile_ms) {
     int rc = check_desc(d);
     if (rc) return rc;
     if (cap < 0 || (cap > 0 && !buf)) return fail(nullptr, SL_EINVAL, "bad buffer");
+    if (variant < 0 || variant >= kAdjJitVariants) return fail(nullptr, SL_EINVAL, "no variant %d", variant);
     std::vector<OpDev> ops;
     std::vector<int32_t> od;
     int arena = 0, max_child = 1;
@@ -2612,6 +2636,8 @@ int sl_problem_adjoint_source(const sl_problem_desc* d, int32_t compile, char* b
     in.M = d->n_markers;
     in.n = d->lod_per_interval;
     in.W = (2 * (d->n_members - d->n_founders) + 31) / 32;
+    in.min_blocks = kAdjJitMinBlocks[variant];
+    in.prefetch = kAdjJitPrefetch[variant];
     int ns = 0, half = 0;
     const std::string src = adj_jit_source(in, &ns, &half);
     if (len) *len = (int64_t)src.size();

@@ -43,14 +43,14 @@ def with_model(g, pen, freq):
     return d
 
 
-def source(desc, compile_=False):
+def source(desc, compile_=False, variant=0):
     f = api.lib().sl_problem_adjoint_source
     n = ctypes.c_int64()
     shapes = ctypes.c_int32()
     ms = ctypes.c_double()
-    assert f(ctypes.byref(desc), 0, None, 0, ctypes.byref(n), ctypes.byref(shapes), None) == 0
+    assert f(ctypes.byref(desc), variant, 0, None, 0, ctypes.byref(n), ctypes.byref(shapes), None) == 0
     buf = ctypes.create_string_buffer(n.value + 1)
-    rc = f(ctypes.byref(desc), int(compile_), buf, n.value + 1, None, None, ctypes.byref(ms))
+    rc = f(ctypes.byref(desc), variant, int(compile_), buf, n.value + 1, None, None, ctypes.byref(ms))
     assert rc == 0, api.lib().sl_last_error(None)
     return buf.value.decode(), shapes.value, ms.value
 
@@ -157,8 +157,14 @@ def test_generated_adjoint_matches_host_fp64(name, model, tmp_path):
         assert err <= GRAD_RTOL, (k, err)
 
 
-def test_generated_adjoint_compiles_for_sm103a():
-    """The same source through NVRTC for sm_103a (no device needed)."""
+@pytest.mark.parametrize("variant", range(4))
+def test_generated_adjoint_compiles_for_sm103a(variant):
+    """The same source through NVRTC for sm_103a (no device needed), in each
+    variant the library compiles: two register budgets, without and with L2
+    prefetches (their arithmetic is the same source)."""
     g = load_golden("cfg1")
-    _, shapes, ms = source(api.Problem.from_arrays(with_model(g, *DOMINANT)).desc(), compile_=True)
+    src, shapes, ms = source(api.Problem.from_arrays(with_model(g, *DOMINANT)).desc(), compile_=True,
+                             variant=variant)
     assert shapes >= 1 and ms > 0
+    assert ("pfl2(Ab" in src) == (variant >= 2)
+    assert "__launch_bounds__(128, %d)" % (4 if variant % 2 == 0 else 8) in src

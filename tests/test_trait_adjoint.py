@@ -293,10 +293,13 @@ def test_specialised_adjoint_large_pedigree_and_timed_choice():
         for k in range(6):
             assert rel_err(got[:, k], want[:, k]) <= GRAD_RTOL, (k, rel_err(got[:, k], want[:, k]))
         ctx.adjoint_set_form(0)
-        ctx.trait_backward(dg[None])
+        grad, _ = ctx.trait_backward(dg[None])
         form, warp_ms, thread_ms, spec_ms = ctx.adjoint_info()
         assert warp_ms > 0 and thread_ms > 0 and spec_ms > 0
         assert form in (api.SL_ADJOINT_WARP, api.SL_ADJOINT_THREAD, api.SL_ADJOINT_SPECIALISED)
+        got = np.array([grad[0, l, o] for l, o in positions])   # the form (and register budget) timing kept
+        for k in range(6):
+            assert rel_err(got[:, k], want[:, k]) <= GRAD_RTOL, (k, rel_err(got[:, k], want[:, k]))
         seg, _ = ctx.adjoint_memory(256)
         assert seg > 1
         with pytest.raises(api.SwiftLinkError):
