@@ -1204,18 +1204,22 @@ constexpr int kFagRounds = 4;   // rounds of colour propagation along heterozygo
 __host__ __device__ inline size_t fagw_tables(int N) {
     return (((size_t)N * 8 + 15) & ~(size_t)15) + (((size_t)4 * (N + 1) + 15) & ~(size_t)15);
 }
-// per lane group: e [2N] u16, then Lb / fl / cnt [2F] int each, then the
-// typed-member list [N] u16 on a 16-byte boundary in whole 16-byte chunks
-__host__ __device__ inline size_t fagw_typ_offset(int N, int F) {
-    return (((((size_t)4 * N + 15) & ~(size_t)15) + (size_t)2 * F * 12) + 15) & ~(size_t)15;
+// per lane group: e [2N] founder-allele labels of eb bytes each (1 when the
+// 2F labels fit a byte: less shared memory per block, more blocks per SM),
+// then Lb / fl / cnt [2F] int each, then the typed-member list [N] u16 on a
+// 16-byte boundary in whole 16-byte chunks
+__host__ __device__ inline size_t fagw_typ_offset(int N, int F, int eb) {
+    return (((((size_t)2 * eb * N + 15) & ~(size_t)15) + (size_t)2 * F * 12) + 15) & ~(size_t)15;
 }
-__host__ __device__ inline size_t fagw_warp_bytes(int N, int F) {
-    return fagw_typ_offset(N, F) + (size_t)16 * ((N + 7) / 8);
+__host__ __device__ inline size_t fagw_warp_bytes(int N, int F, int eb) {
+    return fagw_typ_offset(N, F, eb) + (size_t)16 * ((N + 7) / 8);
 }
 // per block: the shared tables and one locus's arrays per lane group (G lanes)
-size_t fagw_block_bytes(int N, int F, int G) {
-    return fagw_tables(N) + (size_t)kFagWarpsPerBlock * (32 / G) * fagw_warp_bytes(N, F);
+size_t fagw_block_bytes(int N, int F, int G, int eb) {
+    return fagw_tables(N) + (size_t)kFagWarpsPerBlock * (32 / G) * fagw_warp_bytes(N, F, eb);
 }
+// bytes of a founder-allele label: one while the 2F labels fit
+__host__ __device__ inline int fagw_label_bytes(int F) { return 2 * F <= 256 ? 1 : 2; }
 
 // 16-byte global -> shared copies that complete asynchronously (cp.async,
 // sm_80 and later): both addresses 16-byte aligned.
@@ -1298,7 +1302,7 @@ struct LaneGroup {
 // of the column at meiosis order[0]; step >= 0 the likelihoods at both values
 // of meiosis order[step] (the kept one from the previous step).  A group past
 // the last locus (valid false) works on locus 0 and stores nothing.
-template <int G>
+template <int G, typename E>
 __device__ __forceinline__ void fagw_task(const ProblemDev& P, const FagwTables& tab, unsigned char* wbase,
                                           const uint32_t* dg, int chain, int cr, int l, bool valid,
                                           const int32_t* ord, int step, float* rawbuf, float* raw32, uint8_t* badc,
@@ -1307,11 +1311,11 @@ __device__ __forceinline__ void fagw_task(const ProblemDev& P, const FagwTables&
     const int N = P.N, F = P.F, nfa = 2 * F, M = P.M, gl = grp.gl;
     const uint2* s_lvl = tab.lvl;
     const int32_t* s_off = tab.lvl_off;
-    uint16_t* e = (uint16_t*)wbase;                                   // [2N] founder allele of each allele
-    volatile int* Lb = (volatile int*)(wbase + (((size_t)4 * N + 15) & ~(size_t)15));   // [2F] 2 * parent + parity
+    E* e = (E*)wbase;                                                 // [2N] founder allele of each allele
+    volatile int* Lb = (volatile int*)(wbase + (((size_t)2 * sizeof(E) * N + 15) & ~(size_t)15));   // [2F] 2 * parent + parity
     int* fl = (int*)(Lb + nfa);                                       // [2F] bit0 used, bit1 fixed A, bit2 fixed B
     int* cnt = fl + nfa;                                              // [2F] per component: counts, forbidden colourings
-    uint16_t* typ = (uint16_t*)(wbase + fagw_typ_offset(N, F));       // [N] the locus's typed members
+    uint16_t* typ = (uint16_t*)(wbase + fagw_typ_offset(N, F, (int)sizeof(E)));   // [N] the locus's typed members
     const int lc = valid ? l : 0;
     const uint32_t* col = dg + ((size_t)chain * M + lc) * P.W;
     float* raw = rawbuf + (size_t)cr * 2 * M;
@@ -1343,8 +1347,8 @@ __device__ __forceinline__ void fagw_task(const ProblemDev& P, const FagwTables&
     // 1. founder alleles, one generation level at a time
     for (int q = gl; q < s_off[1]; q += G) {
         const int pid = (int)s_lvl[q].x;
-        e[2 * pid] = (uint16_t)(2 * pid);
-        e[2 * pid + 1] = (uint16_t)(2 * pid + 1);
+        e[2 * pid] = (E)(2 * pid);
+        e[2 * pid + 1] = (E)(2 * pid + 1);
     }
     __syncwarp();
     for (int k = 1; k < P.n_lvl; ++k) {
@@ -1890,7 +1894,7 @@ __global__ void __launch_bounds__(1024, 1) ffbs_scan_kernel(ProblemDev P, uint32
 // slice of warps also draws the step's uniforms by index, one per lane, so
 // ffbs_scan_kernel only reads them.
 // ---------------------------------------------------------------------------
-template <int G>
+template <int G, typename E>
 __global__ void __launch_bounds__(kFagWarpsPerBlock * 32) fag_warp_kernel(ProblemDev P, uint32_t* dg, int first,
                                                                          const int32_t* order, int64_t ostride,
                                                                          int step, Draws draws, const uint8_t* sel,
@@ -1911,8 +1915,9 @@ __global__ void __launch_bounds__(kFagWarpsPerBlock * 32) fag_warp_kernel(Proble
         ubuf[(size_t)cr * M + gw * 32 + lane] = draws.get(cr, chain, step, gw * 32 + lane);
     const int gi = lane / G, l = gw * kLoci + gi;
     if (gw * kLoci < M)
-        fagw_task<G>(P, tab,
-                     smem + fagw_tables(P.N) + ((size_t)warp * kLoci + gi) * fagw_warp_bytes(P.N, P.F), dg, chain,
+        fagw_task<G, E>(P, tab,
+                        smem + fagw_tables(P.N) + ((size_t)warp * kLoci + gi) * fagw_warp_bytes(P.N, P.F, (int)sizeof(E)),
+                        dg, chain,
                      cr, l, l < M, ord, step, rawbuf, raw32, badc, status);
 }
 
@@ -3275,10 +3280,13 @@ static cudaError_t launch_msampler_t(const ProblemDev& P, uint32_t* dg, int firs
     // block's shared memory doubled, the 400-member pedigree's M-sweeps were
     // 16% slower than with 32 lanes)
     const int G = pairs && P.W <= 16 ? 16 : 32;
-    const size_t wsm = fagw_block_bytes(P.N, P.F, G);
+    const int eb = fagw_label_bytes(P.F);
+    const size_t wsm = fagw_block_bytes(P.N, P.F, G, eb);
     const bool warp_like = !exact && wsm <= 200 * 1024 && 2 * P.F < 8192;
+    const void* fk = G == 16 ? (eb == 1 ? (const void*)fag_warp_kernel<16, uint8_t> : (const void*)fag_warp_kernel<16, uint16_t>)
+                             : (eb == 1 ? (const void*)fag_warp_kernel<32, uint8_t> : (const void*)fag_warp_kernel<32, uint16_t>);
     if (warp_like) {
-        cudaError_t e = ensure_smem(G == 16 ? (const void*)fag_warp_kernel<16> : (const void*)fag_warp_kernel<32>, wsm);
+        cudaError_t e = ensure_smem(fk, wsm);
         if (e != cudaSuccess) return e;
     }
     const int lpb = kFagWarpsPerBlock * (32 / G);   // loci per block
@@ -3288,14 +3296,14 @@ static cudaError_t launch_msampler_t(const ProblemDev& P, uint32_t* dg, int firs
         if (!warp_like)
             fag_kernel<IX, PP><<<grid, fag_threads, smem, s>>>(P, dg, first, nchain, meioses, mstride, j, sel, want,
                                                                raw, exact ? nullptr : raw32, badc, status, fast);
-        else if (G == 16)
-            fag_warp_kernel<16><<<wgrid, kFagWarpsPerBlock * 32, wsm, s>>>(P, dg, first, meioses, mstride, j, d, sel,
-                                                                           want, (float*)raw, raw32, badc, status,
-                                                                           upre);
-        else
-            fag_warp_kernel<32><<<wgrid, kFagWarpsPerBlock * 32, wsm, s>>>(P, dg, first, meioses, mstride, j, d, sel,
-                                                                           want, (float*)raw, raw32, badc, status,
-                                                                           upre);
+        else {
+            float* rawf = (float*)raw;
+            void* args[] = {(void*)&P, (void*)&dg, (void*)&first, (void*)&meioses, (void*)&mstride, (void*)&j,
+                            (void*)&d, (void*)&sel, (void*)&want, (void*)&rawf, (void*)&raw32, (void*)&badc,
+                            (void*)&status, (void*)&upre};
+            cudaError_t e = cudaLaunchKernel(fk, wgrid, dim3(kFagWarpsPerBlock * 32), args, wsm, s);
+            if (e != cudaSuccess) return e;
+        }
         if (j < 0) continue;
         if (exact)
             ffbs_kernel<double><<<nchain, 32, 0, s>>>(P, dg, first, nchain, meioses, mstride, j, d, sel, want, badc,
