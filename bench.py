@@ -694,7 +694,7 @@ def adjoint_rate(device, G=1000, chunk=250):
         kern_ms, kern_n = ctx.profile_read(api.SL_KERNEL_LOD)
         ctx.profile(False)
         form, warp_ms, thread_ms, spec_ms = ctx.adjoint_info()
-        shapes, regs, compile_ms = ctx.adjoint_kernel_info()
+        shapes, variant, regs, compile_ms = ctx.adjoint_kernel_info()
         # the forward FP32 scorer on the same graphs, for the ratio
         ctx.lod_score_graphs(gset)
         ctx.synchronize()
@@ -713,7 +713,9 @@ def adjoint_rate(device, G=1000, chunk=250):
             "form_timing_ms": {"warp": round(warp_ms, 3), "thread": round(thread_ms, 3),
                                "specialised": round(spec_ms, 3),
                                "tasks": 65536, "selection": "timed on the first call's first tasks"},
-            "specialised": {"shapes": shapes, "registers": regs, "compile_ms": round(compile_ms, 1)},
+            "specialised": {"shapes": shapes, "registers": regs, "compile_ms": round(compile_ms, 1),
+                            "variant": {0: "4 blocks per SM", 1: "8 blocks per SM", 2: "4 blocks per SM, L2 prefetch",
+                                        3: "8 blocks per SM, L2 prefetch"}.get(variant, str(variant))},
             "model": "dominant (0.01, 0.8, 0.9), q = 1e-3",
             "path": "sl_trait_backward: host graphs in, d log L / d (theta_L, theta_R, penetrances, q) out"}
 

@@ -401,19 +401,22 @@ int sl_adjoint_memory(sl_ctx* ctx, int64_t bytes_per_task, int32_t* segments, in
 int sl_adjoint_info(sl_ctx* ctx, int32_t* form, double* warp_ms, double* thread_ms, double* specialised_ms);
 
 /* Fix the adjoint's form for the following calls (0: choose by timing, the
- * default).  SL_ADJOINT_SPECIALISED needs a memory plan that keeps every
+ * default), and for SL_ADJOINT_SPECIALISED its variant (0 to
+ * SL_ADJOINT_VARIANTS - 1, see sl_problem_adjoint_source; ignored by the
+ * other forms).  SL_ADJOINT_SPECIALISED needs a memory plan that keeps every
  * rfunction (sl_adjoint_memory: one segment), else SL_EINVAL; a later plan
  * that splits the peel returns the choice to timing.  If its NVRTC compile
  * fails, the next sl_trait_backward returns SL_EINVAL with the compiler's
  * log. */
-int sl_adjoint_set_form(sl_ctx* ctx, int32_t form);
+int sl_adjoint_set_form(sl_ctx* ctx, int32_t form, int32_t variant);
 
 /* The specialised adjoint: the operation shapes it was generated with (one
- * forward and one reverse function each), the registers per thread of the
- * variant in use (the fastest when timed; see sl_problem_adjoint_source) and
- * the compile time of its variants in milliseconds (0 before it was needed,
- * -1 if its compile failed); any pointer may be NULL. */
-int sl_adjoint_kernel_info(sl_ctx* ctx, int32_t* shapes, int32_t* regs, double* compile_ms);
+ * forward and one reverse function each), the variant in use (the fastest
+ * when timed, the first when fixed; see sl_problem_adjoint_source; -1 before
+ * it was built) and its registers per thread, and the compile time of its
+ * variants in milliseconds (0 before it was needed, -1 if its compile
+ * failed); any pointer may be NULL. */
+int sl_adjoint_kernel_info(sl_ctx* ctx, int32_t* shapes, int32_t* variant, int32_t* regs, double* compile_ms);
 
 /* The specialised adjoint's CUDA C++ source for a problem (no device
  * needed), one of its SL_ADJOINT_VARIANTS variants (0: 4 blocks per SM, 1: 8,

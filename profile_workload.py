@@ -1,7 +1,8 @@
 """A short, fixed workload for ncu captures of the library's kernels.
 
     python profile_workload.py [--workload cfg2|cfg5] [--iterations 2] [--chains C]
-        [--lprob 0.5] [--adjoint 0] [--adjoint-form F] [--graph] [--lod-kernel K] [--ls-specialised]
+        [--lprob 0.5] [--adjoint 0] [--adjoint-form F] [--adjoint-variant V] [--graph] [--lod-kernel K]
+        [--ls-specialised]
 
 cfg2 is the 120-member, 2000-SNP pedigree (10 chains by default); cfg5 the
 400-member, 10,000-SNP pedigree (32 chains by default).  It runs `iterations`
@@ -12,7 +13,8 @@ chain (the first scoring also times the LOD kernel candidates unless
 --lod-kernel forces one of SL_LOD_KERNEL_*; --ls-specialised runs the
 L-sampler compiled for the pedigree), and, with --adjoint G, the trait-peel
 adjoint of G graphs under the dominant model (0.01, 0.8, 0.9), q = 1e-3, in
-the form --adjoint-form fixes (SL_ADJOINT_*; 0: chosen by timing).  It prints
+the form --adjoint-form fixes (SL_ADJOINT_*; 0: chosen by timing; for the
+compiled form, --adjoint-variant picks its variant).  It prints
 the per-kernel-class event times of the sampling part and the adjoint's time.
 """
 from __future__ import annotations
@@ -45,6 +47,7 @@ def main(argv=None):
     ap.add_argument("--lprob", type=float, default=0.5)
     ap.add_argument("--adjoint", type=int, default=0)
     ap.add_argument("--adjoint-form", type=int, default=0)
+    ap.add_argument("--adjoint-variant", type=int, default=0)
     ap.add_argument("--seed", type=int, default=5)
     ap.add_argument("--graph", action="store_true")
     ap.add_argument("--lod-kernel", type=int, default=api.SL_LOD_KERNEL_AUTO)
@@ -80,14 +83,14 @@ def main(argv=None):
         with api.Context(api.Problem.from_arrays(dd, with_legal=False), n_chains=1,
                          lod_precision=api.SL_LOD_FP32_RESCALED, lod_flags=api.SL_LOD_ZERO_OK) as actx:
             gset = np.stack([graphs[i % C] for i in range(a.adjoint)])
-            actx.adjoint_set_form(a.adjoint_form)
+            actx.adjoint_set_form(a.adjoint_form, a.adjoint_variant)
             t = time.perf_counter()
             grad, pt = actx.trait_backward(gset)
             dt = time.perf_counter() - t
             print("adjoint", grad.shape, float(np.abs(grad).max()), pt)
             print(f"adjoint: {dt:.3f} s wall for the first call (compiles and timing included); form and timed "
-                  f"launches (warp, thread, specialised ms): {actx.adjoint_info()}; specialised (shapes, registers, "
-                  f"compile ms): {actx.adjoint_kernel_info()}")
+                  f"launches (warp, thread, specialised ms): {actx.adjoint_info()}; specialised (shapes, variant, "
+                  f"registers, compile ms): {actx.adjoint_kernel_info()}")
             t = time.perf_counter()
             actx.trait_backward(gset)
             dt = time.perf_counter() - t

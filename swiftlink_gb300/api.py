@@ -25,6 +25,7 @@ SL_LS_KERNEL_GENERIC, SL_LS_KERNEL_SPECIALISED, SL_LS_KERNEL_BACKGROUND, SL_LS_K
 SL_LS_KERNEL_GENERIC32, SL_LS_KERNEL_GENERIC16, SL_LS_KERNEL_GENERIC8 = 4, 5, 6
 SL_KERNEL_LSAMPLER, SL_KERNEL_MSAMPLER, SL_KERNEL_LOD, SL_KERNEL_LOD_MERGE, SL_KERNEL_OTHER = 0, 1, 2, 3, 4
 SL_ADJOINT_WARP, SL_ADJOINT_THREAD, SL_ADJOINT_SPECIALISED = 1, 2, 3
+SL_ADJOINT_VARIANTS = 4
 
 EXPORTED = [
     "sl_create", "sl_destroy", "sl_last_error", "sl_set_descent_graphs", "sl_get_descent_graphs",
@@ -353,19 +354,22 @@ class Context:
                                           ctypes.byref(c)))
         return f.value, a.value, b.value, c.value
 
-    def adjoint_set_form(self, form: int = 0):
-        """Fix the adjoint's form (SL_ADJOINT_*), or 0 to choose by timing."""
-        self._check(lib().sl_adjoint_set_form(self.h, ctypes.c_int32(form)))
+    def adjoint_set_form(self, form: int = 0, variant: int = 0):
+        """Fix the adjoint's form (SL_ADJOINT_*; for SL_ADJOINT_SPECIALISED
+        also its variant), or 0 to choose by timing."""
+        self._check(lib().sl_adjoint_set_form(self.h, ctypes.c_int32(form), ctypes.c_int32(variant)))
 
     def adjoint_kernel_info(self):
-        """(operation shapes, registers per thread, compile ms) of the
-        specialised adjoint; compile ms 0 before it was needed, -1 if it did
-        not build."""
+        """(operation shapes, variant in use, its registers per thread,
+        compile ms of the variants) of the specialised adjoint; compile ms 0
+        before it was needed, -1 if it did not build."""
         n = ctypes.c_int32()
+        v = ctypes.c_int32()
         r = ctypes.c_int32()
         ms = ctypes.c_double()
-        self._check(lib().sl_adjoint_kernel_info(self.h, ctypes.byref(n), ctypes.byref(r), ctypes.byref(ms)))
-        return n.value, r.value, ms.value
+        self._check(lib().sl_adjoint_kernel_info(self.h, ctypes.byref(n), ctypes.byref(v), ctypes.byref(r),
+                                                 ctypes.byref(ms)))
+        return n.value, v.value, r.value, ms.value
 
     def trait_backward(self, dgs: Optional[np.ndarray] = None):
         """d log L / d (theta_L, theta_R, pen x3, frequency) at every LOD

@@ -190,6 +190,7 @@ struct sl_ctx {
     size_t adj_thr_bytes = 0;
     AdjJit adj_jit_v[kAdjJitVariants];   // the specialised form at each register budget
     int adj_jit_sel = 0;              // the variant in use (timed with the forms)
+    int adj_jit_req = 0;              // the variant a fixed SL_ADJOINT_SPECIALISED form runs
     int adj_jit_state = 0;            // 0 not tried, 1 built, -1 its compile failed
     std::string adj_jit_log;
     float* d_adjJ = nullptr;          // its arena: blocks x adj_jit_block_floats
@@ -2449,6 +2450,7 @@ static int adjoint_choose(sl_ctx* ctx, const uint32_t* graphs, int64_t words, in
             if ((rc = adjoint_jit_build(ctx))) return rc;
             if (ctx->adj_jit_state != 1)
                 return fail(ctx, SL_EINVAL, "the specialised adjoint did not build: %s", ctx->adj_jit_log.c_str());
+            ctx->adj_jit_sel = ctx->adj_jit_req;
         }
         ctx->adj_form = ctx->adj_form_req;
         return SL_OK;
@@ -2578,12 +2580,14 @@ int sl_adjoint_info(sl_ctx* ctx, int32_t* form, double* warp_ms, double* thread_
     return SL_OK;
 }
 
-int sl_adjoint_set_form(sl_ctx* ctx, int32_t form) {
+int sl_adjoint_set_form(sl_ctx* ctx, int32_t form, int32_t variant) {
     if (!ctx) return fail(ctx, SL_EINVAL, "null context");
     if (!ctx->has_adjoint)
         return fail(ctx, SL_EINVAL, "no trait-peel adjoint: the problem carries no disease model (affection is NULL) "
                                     "or an op multiplies more than 8 rfunctions");
     if (form < 0 || form > SL_ADJOINT_SPECIALISED) return fail(ctx, SL_EINVAL, "unknown adjoint form %d", form);
+    if (variant < 0 || variant >= kAdjJitVariants) return fail(ctx, SL_EINVAL, "no variant %d", variant);
+    ctx->adj_jit_req = variant;
     if (form == SL_ADJOINT_SPECIALISED && !adjoint_jit_eligible(ctx))
         return fail(ctx, SL_EINVAL, "the specialised adjoint keeps every matrix: the memory plan splits the peel "
                                     "into %d segments", ctx->adj.nseg);
@@ -2592,8 +2596,9 @@ int sl_adjoint_set_form(sl_ctx* ctx, int32_t form) {
     return SL_OK;
 }
 
-int sl_adjoint_kernel_info(sl_ctx* ctx, int32_t* shapes, int32_t* regs, double* compile_ms) {
+int sl_adjoint_kernel_info(sl_ctx* ctx, int32_t* shapes, int32_t* variant, int32_t* regs, double* compile_ms) {
     if (!ctx) return fail(ctx, SL_EINVAL, "null context");
+    if (variant) *variant = ctx->adj_jit_state == 1 ? ctx->adj_jit_sel : -1;
     const AdjJit& j = ctx->adj_jit_v[ctx->adj_jit_sel];
     double ms = 0.0;
     for (const AdjJit& v : ctx->adj_jit_v) ms += v.compile_ms;

@@ -245,25 +245,29 @@ def test_device_adjoint_400_member_pedigree_recomputes():
     np.testing.assert_allclose(pt, host_grad(d, None, 0, 0)[2:], rtol=GRAD_RTOL)
 
 
+FORMS = [(api.SL_ADJOINT_WARP, 0), (api.SL_ADJOINT_THREAD, 0)] + \
+    [(api.SL_ADJOINT_SPECIALISED, v) for v in range(api.SL_ADJOINT_VARIANTS)]
+
+
 @pytest.mark.gpu
-@pytest.mark.parametrize("form", [api.SL_ADJOINT_WARP, api.SL_ADJOINT_THREAD, api.SL_ADJOINT_SPECIALISED])
+@pytest.mark.parametrize("form,variant", FORMS)
 @pytest.mark.parametrize("model", ["recessive", "dominant"])
 @pytest.mark.parametrize("name", CASES)
-def test_each_adjoint_form_matches_host_fp64(name, model, form):
+def test_each_adjoint_form_matches_host_fp64(name, model, form, variant):
     """Each form fixed by sl_adjoint_set_form -- the warp form, the thread
-    form and the peel's adjoint compiled for the pedigree -- against the
-    FP64 host adjoint at every position of every golden graph."""
+    form and every variant of the peel's adjoint compiled for the pedigree --
+    against the FP64 host adjoint at every position of every golden graph."""
     g = load_golden(name)
     d = g if model == "recessive" else with_model(g, *DOMINANT)
     n = g["n_lod"]
     graphs = np.ascontiguousarray(g["lod_graphs"], np.int32)
     with api.Context(api.Problem.from_arrays(d), n_chains=1) as ctx:
-        ctx.adjoint_set_form(form)
+        ctx.adjoint_set_form(form, variant)
         grad, _ = ctx.trait_backward(graphs)
         assert ctx.adjoint_info()[0] == form
         if form == api.SL_ADJOINT_SPECIALISED:
-            shapes, regs, ms = ctx.adjoint_kernel_info()
-            assert shapes >= 1 and regs > 0 and ms > 0
+            shapes, used, regs, ms = ctx.adjoint_kernel_info()
+            assert shapes >= 1 and used == variant and regs > 0 and ms > 0
     positions = [(l, o) for l in range(g["M"] - 1) for o in range(n)]
     for b in range(graphs.shape[0]):
         want = host_all(d, graphs[b], positions)
