@@ -714,8 +714,7 @@ def adjoint_rate(device, G=1000, chunk=250):
                                "specialised": round(spec_ms, 3),
                                "tasks": 65536, "selection": "timed on the first call's first tasks"},
             "specialised": {"shapes": shapes, "registers": regs, "compile_ms": round(compile_ms, 1),
-                            "variant": {0: "4 blocks per SM", 1: "8 blocks per SM", 2: "4 blocks per SM, L2 prefetch",
-                                        3: "8 blocks per SM, L2 prefetch"}.get(variant, str(variant))},
+                            "variant": {0: "4 blocks per SM", 1: "8 blocks per SM"}.get(variant, str(variant))},
             "model": "dominant (0.01, 0.8, 0.9), q = 1e-3",
             "path": "sl_trait_backward: host graphs in, d log L / d (theta_L, theta_R, penetrances, q) out"}
 

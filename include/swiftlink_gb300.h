@@ -419,14 +419,13 @@ int sl_adjoint_set_form(sl_ctx* ctx, int32_t form, int32_t variant);
 int sl_adjoint_kernel_info(sl_ctx* ctx, int32_t* shapes, int32_t* variant, int32_t* regs, double* compile_ms);
 
 /* The specialised adjoint's CUDA C++ source for a problem (no device
- * needed), one of its SL_ADJOINT_VARIANTS variants (0: 4 blocks per SM, 1: 8,
- * 2 and 3 the same with L2 prefetches of each next operation's arena lines):
- * up to cap - 1 bytes and a terminating zero into buf (buf may be NULL with
- * cap 0), its length into *len and its operation shapes into *shapes; with
- * compile != 0 it is also compiled with NVRTC for sm_103a (milliseconds into
- * *compile_ms; SL_EINVAL with the compiler's log when it fails).  Any output
- * pointer may be NULL. */
-#define SL_ADJOINT_VARIANTS 4
+ * needed), one of its SL_ADJOINT_VARIANTS variants (0: compiled for 4 blocks
+ * of 128 threads per SM, 1: for 8): up to cap - 1 bytes and a terminating
+ * zero into buf (buf may be NULL with cap 0), its length into *len and its
+ * operation shapes into *shapes; with compile != 0 it is also compiled with
+ * NVRTC for sm_103a (milliseconds into *compile_ms; SL_EINVAL with the
+ * compiler's log when it fails).  Any output pointer may be NULL. */
+#define SL_ADJOINT_VARIANTS 2
 int sl_problem_adjoint_source(const sl_problem_desc* problem, int32_t variant, int32_t compile, char* buf,
                               int64_t cap, int64_t* len, int32_t* shapes, double* compile_ms);
 

@@ -25,7 +25,7 @@ SL_LS_KERNEL_GENERIC, SL_LS_KERNEL_SPECIALISED, SL_LS_KERNEL_BACKGROUND, SL_LS_K
 SL_LS_KERNEL_GENERIC32, SL_LS_KERNEL_GENERIC16, SL_LS_KERNEL_GENERIC8 = 4, 5, 6
 SL_KERNEL_LSAMPLER, SL_KERNEL_MSAMPLER, SL_KERNEL_LOD, SL_KERNEL_LOD_MERGE, SL_KERNEL_OTHER = 0, 1, 2, 3, 4
 SL_ADJOINT_WARP, SL_ADJOINT_THREAD, SL_ADJOINT_SPECIALISED = 1, 2, 3
-SL_ADJOINT_VARIANTS = 4
+SL_ADJOINT_VARIANTS = 2
 
 EXPORTED = [
     "sl_create", "sl_destroy", "sl_last_error", "sl_set_descent_graphs", "sl_get_descent_graphs",

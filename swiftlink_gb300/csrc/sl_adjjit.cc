@@ -511,7 +511,6 @@ std::string adj_jit_source(const AdjJitIn& in, int* shapes_out, int* half_out) {
     emitf(s, "#define HB %lld\n", (long long)half * kAdjJitThreads);
     s += "struct G6 { float l, r, p0, p1, p2, q; };\n";
     s += kPow2;
-    s += "__device__ __forceinline__ void pfl2(const float* p) { asm volatile(\"prefetch.global.L2 [%0];\" :: \"l\"(p)); }\n";
     for (size_t i = 0; i < uniq.size(); ++i) {
         emit_forward(s, uniq[i], (int)i);
         emit_reverse(s, uniq[i], (int)i);
@@ -557,22 +556,7 @@ std::string adj_jit_source(const AdjJitIn& in, int* shapes_out, int* half_out) {
         a += ", th, an, th2, an2";
         return a;
     };
-    // with prefetch: before each op, the lines the op after it reads are
-    // asked into L2 (its previous rfunctions' matrices; in the reverse, also
-    // its cells' adjoints), one 128-byte line per warp and arena slot
-    auto prefetch = [&](int k, bool reverse) {
-        if (!in.prefetch || k < 0 || k >= K) return;
-        if (reverse)
-            emitf(s, "    for (int q = 0; q < %d; ++q) pfl2(Ab + HB + %d + q * %d);\n", 1 << (2 * in.ops[k].c),
-                  aoff[k] * kAdjJitThreads, kAdjJitThreads);
-        for (const Prev& p : shapes[k].prev)
-            emitf(s, "    for (int q = 0; q < %d; ++q) pfl2(Ab + %d + q * %d);\n", 1 << (2 * p.c),
-                  aoff[p.op] * kAdjJitThreads, kAdjJitThreads);
-    };
-    for (int k = 0; k < K; ++k) {
-        prefetch(k + 1, false);
-        emitf(s, "    F%d(%s);\n", sid[k], args(k, false).c_str());
-    }
+    for (int k = 0; k < K; ++k) emitf(s, "    F%d(%s);\n", sid[k], args(k, false).c_str());
     emitf(s, "    const float root = Ab[%d];\n", aoff[K - 1] * kAdjJitThreads);
     emitf(s,
           "    if (!(root > 0.0f)) {\n"
@@ -583,7 +567,6 @@ std::string adj_jit_source(const AdjJitIn& in, int* shapes_out, int* half_out) {
     emitf(s, "    Ab[HB + %d] = 1.0f / root;\n", aoff[K - 1] * kAdjJitThreads);
     s += "    double g0 = 0.0, g1 = 0.0, g2 = 0.0, g3 = 0.0, g4 = 0.0, g5 = 0.0;\n";
     for (int k = K - 1; k >= 0; --k) {
-        prefetch(k - 1, true);
         emitf(s,
               "    { const G6 r = R%d(%s); g0 += (double)r.l; g1 += (double)r.r; g2 += (double)r.p0; g3 += (double)r.p1; "
               "g4 += (double)r.p2; g5 += (double)r.q; }\n",

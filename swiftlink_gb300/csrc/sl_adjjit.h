@@ -18,16 +18,13 @@ struct AdjJitIn {
     const int32_t* od;
     int F, M, n, W;
     int min_blocks;          // resident blocks of kAdjJitThreads per SM the kernel is compiled for
-    bool prefetch;           // ask each next op's arena lines into L2 before the current op
 };
 
 constexpr int kAdjJitThreads = 128;   // threads per block of the generated kernel
 // the variants compiled and timed: 4 blocks per SM (128 registers a thread)
-// or 8 (64 registers, more spills, twice the tasks in flight), each without
-// and with L2 prefetches of the next op's lines
-constexpr int kAdjJitVariants = 4;
-constexpr int kAdjJitMinBlocks[kAdjJitVariants] = {4, 8, 4, 8};
-constexpr bool kAdjJitPrefetch[kAdjJitVariants] = {false, false, true, true};
+// or 8 (64 registers, more spills, twice the tasks in flight)
+constexpr int kAdjJitVariants = 2;
+constexpr int kAdjJitMinBlocks[kAdjJitVariants] = {4, 8};
 
 struct AdjJit {
     void* lib = nullptr;     // cudaLibrary_t

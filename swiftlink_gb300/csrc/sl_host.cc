@@ -2388,7 +2388,6 @@ static int adjoint_jit_build(sl_ctx* ctx) {
     in.W = ctx->P.W;
     for (int v = 0; v < kAdjJitVariants; ++v) {
         in.min_blocks = kAdjJitMinBlocks[v];
-        in.prefetch = kAdjJitPrefetch[v];
         std::string log;
         if (adj_jit_compile(in, &ctx->adj_jit_v[v], &log)) {
             for (AdjJit& j : ctx->adj_jit_v) adj_jit_release(&j);
@@ -2642,7 +2641,6 @@ int sl_problem_adjoint_source(const sl_problem_desc* d, int32_t variant, int32_t
     in.n = d->lod_per_interval;
     in.W = (2 * (d->n_members - d->n_founders) + 31) / 32;
     in.min_blocks = kAdjJitMinBlocks[variant];
-    in.prefetch = kAdjJitPrefetch[variant];
     int ns = 0, half = 0;
     const std::string src = adj_jit_source(in, &ns, &half);
     if (len) *len = (int64_t)src.size();
