@@ -522,6 +522,7 @@ def run_ours(args):
     # underflows at every position of this pedigree, as the reference's does)
     lod_pos_s = timed_lod(ctx, stream, flush, C, npos, reps=5)
     lsel, ljit_ms = ctx.lod_kernel_info()
+    ls_lanes, ls_t = ctx.ls_tuning()
     pctx = api.Context(prob, n_chains=1, lod_precision=api.SL_LOD_FP64_RESCALED, device=local,
                        lod_flags=api.SL_LOD_ZERO_OK)
     pctx.set_graphs(graphs[:1])
@@ -604,8 +605,10 @@ def run_ours(args):
                "lod_positions_per_s": lod_pos_s * world,
                "lod_kernel": {"selected": int(lsel), "specialised_compile_ms": round(ljit_ms, 1),
                               "selection": "timed at the first scoring (SL_LOD_KERNEL_AUTO)"},
-               "ls_kernel": {"selected": "lsampler_kernel<float> (compact rfunctions)",
-                             "selection": "SL_LS_KERNEL_GENERIC: 32 or 16 lanes per (chain, locus) task, "
+               "ls_kernel": {"selected": "lsampler_kernel<float> (compact rfunctions)", "lanes": ls_lanes,
+                             "timed_half_sweep_ms": {"32": round(ls_t[0], 3), "16": round(ls_t[1], 3),
+                                                     "8": round(ls_t[2], 3)},
+                             "selection": "SL_LS_KERNEL_GENERIC: 32, 16 or 8 lanes per (chain, locus) task, "
                                           "timed before the first sweep"},
                "plain": {"steps_per_s": plain_steps_s * world, "lod_positions_per_s": plain_lod_pos_s * world,
                          "form": "one chain per launch, exact FP64 samplers, FP64 LOD peel with rescaling",

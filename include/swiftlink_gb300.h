@@ -447,6 +447,15 @@ int sl_lod_kernel_info(sl_ctx* ctx, int32_t* kernel, double* compile_ms);
  * sl_last_error).  A background compile that has ended is taken up here. */
 int sl_ls_kernel_info(sl_ctx* ctx, int32_t* kernel, double* compile_ms);
 
+/* The L-sampler autotuner's outcome: the lanes per (chain, locus) task of the
+ * generic kernel in use (32, 16 or 8; 0 when the specialised kernel runs) and
+ * the timed half-sweep of each candidate in milliseconds, times_ms[0..3] =
+ * 32, 16 and 8 lanes and the specialised kernel (0 for a candidate not timed,
+ * and for all of them before the first L-sampler work or when a pedigree of
+ * the same size class on this device was timed first).  Either pointer may
+ * be NULL. */
+int sl_ls_tuning(sl_ctx* ctx, int32_t* lanes, double* times_ms);
+
 /*
  * A peel sequence for a pedigree (members founders first, mother/father -1 for
  * founders), in the form sl_problem_desc takes (replaces PeelSequenceGenerator::

@@ -37,7 +37,7 @@ EXPORTED = [
     "sl_problem_trait_backward_eval", "sl_lod_kernel_info", "sl_ls_kernel_info", "sl_set_temperatures", "sl_mc3_stats",
     "sl_chain_loglik", "sl_peel_sequence", "sl_batch_create", "sl_batch_run", "sl_batch_destroy",
     "sl_sequential_imputation", "sl_sequential_imputation_run", "sl_adjoint_memory", "sl_adjoint_info",
-    "sl_adjoint_set_form", "sl_adjoint_kernel_info", "sl_problem_adjoint_source",
+    "sl_adjoint_set_form", "sl_adjoint_kernel_info", "sl_problem_adjoint_source", "sl_ls_tuning",
 ]
 
 
@@ -316,6 +316,15 @@ class Context:
 
     def lod_reset(self):
         self._check(lib().sl_lod_reset(self.h))
+
+    def ls_tuning(self):
+        """(lanes per task of the generic L-sampler in use, 0 for the
+        specialised one; the autotuner's timed half-sweeps in ms for 32, 16
+        and 8 lanes and the specialised kernel, 0 where not timed)."""
+        lanes = ctypes.c_int32()
+        t = (ctypes.c_double * 4)()
+        self._check(lib().sl_ls_tuning(self.h, ctypes.byref(lanes), t))
+        return lanes.value, list(t)
 
     def ls_kernel_info(self):
         """(SL_LS_KERNEL_GENERIC or SL_LS_KERNEL_SPECIALISED in use, milliseconds spent compiling it;

@@ -2335,6 +2335,19 @@ int sl_ls_kernel_info(sl_ctx* ctx, int32_t* kernel, double* compile_ms) {
     return SL_OK;
 }
 
+int sl_ls_tuning(sl_ctx* ctx, int32_t* lanes, double* times_ms) {
+    if (!ctx) return fail(ctx, SL_EINVAL, "null context");
+    ls_adopt(ctx);
+    if (lanes) *lanes = ctx->ls_choice == LS_JIT ? 0 : ls_lanes(ctx->ls_choice);
+    if (times_ms) {
+        times_ms[0] = ctx->ls_tune_ms[LS_GEN32];
+        times_ms[1] = ctx->ls_tune_ms[LS_GEN16];
+        times_ms[2] = ctx->ls_tune_ms[LS_GEN8];
+        times_ms[3] = ctx->ls_tune_ms[LS_JIT];
+    }
+    return SL_OK;
+}
+
 int sl_lod_kernel_info(sl_ctx* ctx, int32_t* kernel, double* compile_ms) {
     if (!ctx) return fail(ctx, SL_EINVAL, "null context");
     if (kernel) *kernel = ctx->lod_precision == SL_LOD_FP32_RESCALED ? ctx->lod_kernel_sel : SL_LOD_KERNEL_INTERP;
