@@ -354,27 +354,40 @@ def lm_choices(C, it0, it1, seed, lprob):
     return (philox.uniform(seed, hi, 0) < lprob).sum(axis=0)
 
 
-def issue_estimate(C, it0, it1, seed, lprob, n_meioses, sm_mhz, sms, seconds, counts):
+def issue_estimate(C, it0, it1, seed, lprob, n_meioses, sm_mhz, sms, seconds, counts, lanes=None, shares=None):
     """SM issue utilisation of timed run-graph launches: the warp instructions
     of the L- and M-sweeps they ran (each chain's L/M choice replayed with the
     same Philox draws; instructions per unit from ncu counts of the same
-    workload: one chain's L half-sweep, one chain's meiosis step in the
-    founder-allele-graph and filter kernels) over the SMs' issue rate (4
-    schedulers per SM, one warp instruction per cycle each, at the SM clock
-    sampled during the launches).  The scoring launches are left out."""
-    need = ("l_half_sweep_per_chain", "fag_per_meiosis_step", "scan_per_meiosis_step")
+    workload: one chain's L half-sweep with the lane group in use, one chain's
+    meiosis step in the founder-allele-graph and filter kernels) over the SMs'
+    issue rate (4 schedulers per SM, one warp instruction per cycle each, at
+    the SM clock sampled during the launches).  The scoring launches are left
+    out.  With `shares` (each class's share of a profiled pass's kernel time)
+    each class's instructions are also set against its share of the time."""
+    need = ("fag_per_meiosis_step", "scan_per_meiosis_step")
     if not counts or any(counts.get(k) is None for k in need) or not sm_mhz or not sms or seconds <= 0:
+        return None
+    per_half = counts.get("l_half_sweep_per_chain")
+    if per_half is None:
+        per_half = (counts.get("l_half_sweep_per_chain_by_lanes") or {}).get(str(lanes))
+    if per_half is None:
         return None
     n_l = int(lm_choices(C, it0, it1, seed, lprob).sum())
     n_m = C * (it1 - it0) - n_l
-    per_l = 2 * counts["l_half_sweep_per_chain"]
+    per_l = 2 * per_half
     per_m = (n_meioses + 1) * counts["fag_per_meiosis_step"] + n_meioses * counts["scan_per_meiosis_step"]
     inst = n_l * per_l + n_m * per_m
     peak = sms * 4 * sm_mhz * 1e6
-    return {"bound": "issue", "achieved": inst / seconds / 1e9, "peak": peak / 1e9, "unit": "G warp-inst/s",
-            "frac": inst / seconds / peak, "l_sweeps": n_l, "m_sweeps": n_m,
-            "warp_inst_per_l_sweep": per_l, "warp_inst_per_m_sweep": per_m,
-            "source": counts.get("source", "ncu smsp__inst_executed.sum")}
+    out = {"bound": "issue", "achieved": inst / seconds / 1e9, "peak": peak / 1e9, "unit": "G warp-inst/s",
+           "frac": inst / seconds / peak, "l_sweeps": n_l, "m_sweeps": n_m, "lsampler_lanes": lanes,
+           "warp_inst_per_l_sweep": per_l, "warp_inst_per_m_sweep": per_m,
+           "source": counts.get("source", "ncu smsp__inst_executed.sum")}
+    if shares and shares.get("l") and shares.get("m"):
+        out["frac_l_sweeps"] = n_l * per_l / (shares["l"] * seconds * peak)
+        out["frac_m_sweeps"] = n_m * per_m / (shares["m"] * seconds * peak)
+        out["class_fractions"] = "each class's instructions over its share of a profiled pass's kernel time " \
+                                 "(the classes overlap in the timed run: approximate)"
+    return out
 
 
 def timed_lod(ctx, stream, flush, G, npos, reps):
@@ -511,9 +524,11 @@ def run_ours(args):
                         "small by construction; the issue estimate below is the binding bound",
                 "kernel_share_profiled_pass": {names[k]: round(v[0] / tot, 4) for k, v in kern.items()}}
     try:
+        ktot = max(1e-9, kern[0][0] + kern[1][0])
         roofline["issue"] = issue_estimate(C, it0, it0 + K * S, seed, LPROB, nm, (clk or {}).get("sm_mhz"),
                                            torch.cuda.get_device_properties(dev).multi_processor_count,
-                                           sum(step_ms) / 1e3, cnt.get("issue_cfg5"))
+                                           sum(step_ms) / 1e3, cnt.get("issue_cfg5"), ctx.ls_tuning()[0],
+                                           {"l": kern[0][0] / ktot, "m": kern[1][0] / ktot})
     except Exception as exc:   # an estimate only: never lose the bench line over it
         roofline["issue"] = {"error": str(exc)[:200]}
 

@@ -2414,7 +2414,18 @@ static int adjoint_jit_build(sl_ctx* ctx) {
     return SL_OK;
 }
 
-static bool adjoint_jit_eligible(const sl_ctx* ctx) { return ctx->adj.nseg == 1; }
+// The specialised form keeps every rfunction, in global memory: it runs
+// under a plan that keeps everything, and under the default budget (which
+// bounds the shared-memory forms) whenever one block's arena slice per SM fits
+// its 4 GiB; a budget the caller set rules it out when the plan splits.
+static bool adjoint_jit_eligible(const sl_ctx* ctx) {
+    if (ctx->adj.nseg == 1) return true;
+    if (ctx->adj_budget != 0) return false;
+    int64_t half = 0;
+    for (const OpDev& op : ctx->adj_ops) half += int64_t(1) << (2 * op.c);
+    const int64_t per = adj_jit_block_floats((int)half, ctx->P.K) * (int64_t)sizeof(float);
+    return per * ctx->sms <= (int64_t(4) << 30);
+}
 
 // The specialised form's arena: the blocks that stay resident on every SM
 // (fewer for fewer tasks), each with its slice, within 4 GiB.
@@ -2601,8 +2612,8 @@ int sl_adjoint_set_form(sl_ctx* ctx, int32_t form, int32_t variant) {
     if (variant < 0 || variant >= kAdjJitVariants) return fail(ctx, SL_EINVAL, "no variant %d", variant);
     ctx->adj_jit_req = variant;
     if (form == SL_ADJOINT_SPECIALISED && !adjoint_jit_eligible(ctx))
-        return fail(ctx, SL_EINVAL, "the specialised adjoint keeps every matrix: the memory plan splits the peel "
-                                    "into %d segments", ctx->adj.nseg);
+        return fail(ctx, SL_EINVAL, "the specialised adjoint keeps every matrix: the memory budget set splits the "
+                                    "peel into %d segments", ctx->adj.nseg);
     ctx->adj_form_req = form;
     ctx->adj_form = 0;
     return SL_OK;

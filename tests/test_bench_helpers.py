@@ -40,6 +40,24 @@ def test_issue_estimate_counts_every_chain_iteration():
     assert bench.issue_estimate(C, it0, it1, bench.SEED, bench.LPROB, 184, 2070.0, 152, 1.0, {}) is None
 
 
+def test_issue_estimate_takes_the_lane_group_in_use():
+    """The L-sampler's count is picked by the lane group the autotuner kept;
+    a lane group without a count gives no estimate; with the classes' time
+    shares each class's fraction uses its share of the time."""
+    C, it0, it1 = 10, 500, 700
+    counts = {"l_half_sweep_per_chain_by_lanes": {"32": 4e5, "8": 1e5}, "fag_per_meiosis_step": 2e3,
+              "scan_per_meiosis_step": 1e3}
+    r8 = bench.issue_estimate(C, it0, it1, bench.SEED, bench.LPROB, 184, 2070.0, 152, 1.0, counts, 8)
+    r32 = bench.issue_estimate(C, it0, it1, bench.SEED, bench.LPROB, 184, 2070.0, 152, 1.0, counts, 32)
+    assert r8["warp_inst_per_l_sweep"] == 2e5 and r32["warp_inst_per_l_sweep"] == 8e5
+    assert bench.issue_estimate(C, it0, it1, bench.SEED, bench.LPROB, 184, 2070.0, 152, 1.0, counts, 16) is None
+    r = bench.issue_estimate(C, it0, it1, bench.SEED, bench.LPROB, 184, 2070.0, 152, 1.0, counts, 8,
+                             {"l": 0.25, "m": 0.75})
+    peak = 152 * 4 * 2070.0e6
+    assert abs(r["frac_l_sweeps"] - r["l_sweeps"] * 2e5 / (0.25 * peak)) < 1e-12
+    assert abs(r["frac_m_sweeps"] - r["m_sweeps"] * r["warp_inst_per_m_sweep"] / (0.75 * peak)) < 1e-12
+
+
 def test_per_iteration_cost_mixes_sweeps_and_scoring():
     t = {"lsweep_s": 2.0, "msweep_s": 6.0, "score_s": 100.0}
     assert abs(bench.per_iteration_s(t, 0.5) - (4.0 + 1.0)) < 1e-12
