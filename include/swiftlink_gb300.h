@@ -368,7 +368,8 @@ int sl_lod_score_device_graphs_noalloc(sl_ctx* ctx, int32_t n_graphs, const uint
  * or the peel and its reverse written out for this pedigree and compiled
  * with NVRTC at the first call, in SL_ADJOINT_VARIANTS variants (one thread
  * per position, every rfunction in a global arena of up to 4 GiB; under the
- * default memory budget, or a budget whose plan keeps every rfunction).  The
+ * default memory budget, or a budget whose plan keeps every rfunction, for
+ * peels whose cutsets have at most 4 members).  The
  * first call with graphs times the forms on its first tasks and keeps the
  * fastest (sl_adjoint_info), unless sl_adjoint_set_form fixed one; the first
  * two follow the memory plan of sl_adjoint_memory (kept, or recomputed when
@@ -404,10 +405,10 @@ int sl_adjoint_info(sl_ctx* ctx, int32_t* form, double* warp_ms, double* thread_
 /* Fix the adjoint's form for the following calls (0: choose by timing, the
  * default), and for SL_ADJOINT_SPECIALISED its variant (0 to
  * SL_ADJOINT_VARIANTS - 1, see sl_problem_adjoint_source; ignored by the
- * other forms).  SL_ADJOINT_SPECIALISED needs the default memory budget or a
- * budget whose plan keeps every rfunction (sl_adjoint_memory: one segment),
- * else SL_EINVAL; a later budget whose plan splits the peel returns the
- * choice to timing.  If its NVRTC compile
+ * other forms).  SL_ADJOINT_SPECIALISED needs cutsets of at most 4 members
+ * and the default memory budget or a budget whose plan keeps every rfunction
+ * (sl_adjoint_memory: one segment), else SL_EINVAL; a later budget whose plan
+ * splits the peel returns the choice to timing.  If its NVRTC compile
  * fails, the next sl_trait_backward returns SL_EINVAL with the compiler's
  * log. */
 int sl_adjoint_set_form(sl_ctx* ctx, int32_t form, int32_t variant);

@@ -1379,6 +1379,7 @@ int sl_create(const sl_problem_desc* d, const sl_options* opt, sl_ctx** out) {
             return s <= 1 ? 0 : (s == 2 ? 1 : 2);
         };
         int most = 1;
+        std::vector<int> per_locus(M);
         for (int l = 0; l < M; ++l) {
             const uint8_t* lg = ctx->legal.data() + (size_t)l * N;
             int tot = 0;
@@ -1387,11 +1388,24 @@ int sl_create(const sl_problem_desc* d, const sl_options* opt, sl_ctx** out) {
                 for (int q = 0; q < ops[k].c; ++q) b += rank_bits(lg[od[ops[k].cut_at + q]] & 15);
                 tot += 1 << b;
             }
+            per_locus[l] = tot;
             most = std::max(most, tot);
         }
         if (most > 65535)   // the tasks' offsets are 16-bit (and such an arena would not fit shared memory)
             return bail(fail(nullptr, SL_EINVAL, "L-sampler needs %d rfunction cells at one locus", most));
         P.ls_arena = most;
+        // a task's shared memory holds the cells of 98% of the loci whole (in
+        // steps of 32); the few loci that need more put their last rfunctions'
+        // cells in the task's slice of a global spill buffer.  Not worth it
+        // when it saves less than an eighth of the arena.
+        std::sort(per_locus.begin(), per_locus.end());
+        int cap = per_locus[(size_t)((M - 1) * 0.98)];
+        cap = (cap + 31) / 32 * 32;
+        P.ls_cap = (cap < most && most - cap >= most / 8) ? cap : most;
+        P.ls_spill_cells = most - P.ls_cap;
+        P.ls_spill_slots = 0;
+        P.ls_spill_chains = 0;
+        P.ls_spill = nullptr;
     }
     P.max_child = max_child;
     P.fag_bytes = 0;
@@ -1477,6 +1491,23 @@ int sl_create(const sl_problem_desc* d, const sl_options* opt, sl_ctx** out) {
     const int lod_blocks = std::max(1, (int)std::min<size_t>(16, per_sm / (ctx->lod_wpb * lodw + 1024)));
     ctx->ls_grid = ctx->sms * ls_blocks;
     ctx->lod_grid = ctx->sms * lod_blocks;
+    if (P.ls_spill_cells > 0) {
+        // per chain, one slice per task slot of the largest L-sampler grid:
+        // ls_grid blocks of up to max(ls_wpb, 4) tasks (the lane groups pack 1,
+        // 2 or 4 tasks per warp)
+        P.ls_spill_slots = (int64_t)ctx->ls_grid * std::max(ctx->ls_wpb, 4);
+        P.ls_spill_chains = ctx->n_chains;
+        const size_t n = (size_t)P.ls_spill_chains * P.ls_spill_slots * P.ls_spill_cells;
+        if (P.ls_fast) {
+            float* sp = nullptr;
+            if ((rc = dev_alloc(ctx, &sp, n))) return bail(rc);
+            P.ls_spill = sp;
+        } else {
+            double* sp = nullptr;
+            if ((rc = dev_alloc(ctx, &sp, n))) return bail(rc);
+            P.ls_spill = sp;
+        }
+    }
     // founder-allele-graph block: the size that keeps the most threads resident
     // per SM (a chain-by-locus grid then fits in as few waves as possible)
     ctx->ms_threads = 0;
@@ -2417,8 +2448,15 @@ static int adjoint_jit_build(sl_ctx* ctx) {
 // The specialised form keeps every rfunction, in global memory: it runs
 // under a plan that keeps everything, and under the default budget (which
 // bounds the shared-memory forms) whenever one block's arena slice per SM fits
-// its 4 GiB; a budget the caller set rules it out when the plan splits.
+// its 4 GiB; a budget the caller set rules it out when the plan splits.  Its
+// functions write out every cell and term of an operation, so a cutset of
+// more than kAdjJitMaxCut members (1,024 cells and more) would make a function
+// too large to compile in reasonable time: such peels keep the other forms.
+static constexpr int kAdjJitMaxCut = 4;
+
 static bool adjoint_jit_eligible(const sl_ctx* ctx) {
+    for (const OpDev& op : ctx->adj_ops)
+        if (op.c > kAdjJitMaxCut) return false;
     if (ctx->adj.nseg == 1) return true;
     if (ctx->adj_budget != 0) return false;
     int64_t half = 0;
@@ -2612,8 +2650,9 @@ int sl_adjoint_set_form(sl_ctx* ctx, int32_t form, int32_t variant) {
     if (variant < 0 || variant >= kAdjJitVariants) return fail(ctx, SL_EINVAL, "no variant %d", variant);
     ctx->adj_jit_req = variant;
     if (form == SL_ADJOINT_SPECIALISED && !adjoint_jit_eligible(ctx))
-        return fail(ctx, SL_EINVAL, "the specialised adjoint keeps every matrix: the memory budget set splits the "
-                                    "peel into %d segments", ctx->adj.nseg);
+        return fail(ctx, SL_EINVAL, "the specialised adjoint is not built for this peel: it keeps every matrix (the "
+                                    "memory budget set splits the peel into %d segments) and takes cutsets of at "
+                                    "most %d members", ctx->adj.nseg, kAdjJitMaxCut);
     ctx->adj_form_req = form;
     ctx->adj_form = 0;
     return SL_OK;

@@ -31,6 +31,11 @@ struct ProblemDev {
     int32_t arena;                       // sum over ops of 4^c
     int32_t ls_arena;                    // the L-sampler's compact rfunctions: the largest, over loci, sum over
                                          // ops of their cells in legal states (sl_kernels.cu, ls_locus)
+    int32_t ls_cap;                      // the part of them a task keeps in shared memory (<= ls_arena)
+    int32_t ls_spill_cells;              // ls_arena - ls_cap: cells per task slot in the global spill buffer
+    int64_t ls_spill_slots;              // task slots the spill buffer holds per chain
+    int32_t ls_spill_chains;             // chains it has slots for
+    void* ls_spill;                      // [chains][slots][ls_spill_cells] of the L-sampler's type, or null
     int32_t max_child;                   // max children of an op (>= 1)
     int32_t fag_bytes;                   // shared bytes one FAG evaluation needs
     double marker_trans;                 // log(0.5) * 2 * Nnf (descent_graph.cc:22)

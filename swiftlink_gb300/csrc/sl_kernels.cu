@@ -207,11 +207,27 @@ struct LsCell {
     int ext, rk, bits, bad;
 };
 
+// A task's compact rfunctions: the first `cap` cells in the task's shared
+// memory, the rest (at the few loci whose rfunctions need more) in its slice
+// of a global spill buffer.  Sizing the shared part for nearly every locus
+// rather than the largest keeps more tasks resident on an SM.
+template <typename T>
+struct LsArena {
+    T* sh;
+    T* gl;
+    int cap;
+    __device__ __forceinline__ T ld(int o) const { return o < cap ? sh[o] : gl[o - cap]; }
+    __device__ __forceinline__ void st(int o, T v) const {
+        if (o < cap) sh[o] = v;
+        else gl[o - cap] = v;
+    }
+};
+
 // One presum entry (cell, peel state v) in the reference's product order
 // (sampler_rfunction.cc:190-287, rfunction.cc:116-142); a previous rfunction
 // is read at its compact index, or as zero where the dense matrix held zero.
 template <typename T>
-__device__ T ls_term(const OpDev& op, const int32_t* opd, const T* Am, const uint16_t* off, const T* dist,
+__device__ T ls_term(const OpDev& op, const int32_t* opd, const LsArena<T>& Am, const uint16_t* off, const T* dist,
                      const LsCell& x, int v, T tv) {
     using A = Ls<T>;
     const int ext = x.ext;
@@ -232,7 +248,7 @@ __device__ T ls_term(const OpDev& op, const int32_t* opd, const T* Am, const uin
             sh += (x.bits >> (2 * pos)) & 3;
             bad |= (x.bad >> pos) & 1;
         }
-        tmp = A::mul(tmp, bad ? T(0) : Am[off[po[j]] + idx]);
+        tmp = A::mul(tmp, bad ? T(0) : Am.ld(off[po[j]] + idx));
         pd += 2 + pc;
     }
     if (op.type == PARENT) {
@@ -280,7 +296,7 @@ __device__ __forceinline__ int state_of_rank(int mask, int r) {   // the r-th al
 __host__ __device__ __forceinline__ size_t al16(size_t x) { return (x + 15) & ~(size_t)15; }
 template <typename T>
 __host__ __device__ __forceinline__ size_t ls_draws_at(const ProblemDev& P) {
-    return al16((size_t)P.ls_arena * sizeof(T) + (size_t)P.max_child * 16 * sizeof(T) + (size_t)P.N);
+    return al16((size_t)P.ls_cap * sizeof(T) + (size_t)P.max_child * 16 * sizeof(T) + (size_t)P.N);
 }
 template <typename T>
 __host__ __device__ __forceinline__ size_t ls_gcol_at(const ProblemDev& P) {
@@ -301,6 +317,16 @@ __host__ __device__ __forceinline__ size_t ls_off_at(const ProblemDev& P) {
 template <typename T>
 __host__ __device__ __forceinline__ size_t ls_warp_bytes(const ProblemDev& P) {
     return al16(ls_off_at<T>(P) + 2 * ((size_t)P.K + 1));   // 16-bit offsets: the arena holds < 65,536 cells
+}
+
+// Task slot s's part of the spill buffer of chain `chain` (null when no
+// locus spills, or past the buffer's slots).  Every chain has its own slots:
+// the run graph launches the chains' sweeps concurrently; a launch over
+// several chains runs its tasks slot by slot in the first chain's slots.
+template <typename T>
+__device__ __forceinline__ T* ls_spill_slice(const ProblemDev& P, int chain, int64_t s) {
+    if (P.ls_spill_cells <= 0 || s >= P.ls_spill_slots || chain < 0 || chain >= P.ls_spill_chains) return nullptr;
+    return (T*)P.ls_spill + ((size_t)chain * P.ls_spill_slots + s) * P.ls_spill_cells;
 }
 
 // Block-shared copies of the peel's operations and their lists: every lane
@@ -337,12 +363,12 @@ __device__ __forceinline__ void ls_stage_tables(const ProblemDev& P, unsigned ch
 template <typename T, int G>
 __device__ int ls_locus(const ProblemDev& P, const OpDev* ops, const int32_t* opd, uint32_t* dg, int cr, int chain,
                         int l, bool hasL, bool hasR, const Draws& draws, int64_t unit, int64_t base,
-                        unsigned char* wsmem, int lane, int* status, double* logroot) {
+                        unsigned char* wsmem, T* spill, int lane, int* status, double* logroot) {
     using Ar = Ls<T>;
     const Lanes<G> L;
     constexpr bool kRescale = sizeof(T) == 4;   // FP32: each rfunction scaled to a maximum of about 1
-    T* A = (T*)wsmem;
-    T* dist = A + P.ls_arena;
+    const LsArena<T> A{(T*)wsmem, spill, P.ls_cap};
+    T* dist = A.sh + P.ls_cap;
     int8_t* assign = (int8_t*)(dist + 16 * P.max_child);
     uint16_t* off = (uint16_t*)(wsmem + ls_off_at<T>(P));
     uint32_t* colC = dg + ((size_t)chain * P.M + l) * P.W;
@@ -405,7 +431,8 @@ __device__ int ls_locus(const ProblemDev& P, const OpDev* ops, const int32_t* op
         }
         if (lane == G - 1) off[P.K] = (uint16_t)incl;
         L.sync();
-        if (L.shfl(incl, G - 1) > P.ls_arena) {   // cannot happen: the arena holds the most any locus needs
+        if (L.shfl(incl, G - 1) > P.ls_arena || (spill == nullptr && L.shfl(incl, G - 1) > P.ls_cap)) {
+            // cannot happen: the arena (shared part and spill) holds the most any locus needs
             if (lane == 0) set_status(status, ST_ILLEGAL_DG);
             return -1;
         }
@@ -429,7 +456,7 @@ __device__ int ls_locus(const ProblemDev& P, const OpDev* ops, const int32_t* op
         bits |= rank_bits(mp) << (2 * op.c);
         const int ncell = 1 << B;
         const T* trait = pri + 4 * (gcol[op.peel] & 3);
-        T* out = A + off[k];
+        const int ob = off[k];
         T mx = T(0);
         // one (cell, state) term per lane, four lanes per cell; the cell's
         // total adds its terms in state order from zero, as the reference's
@@ -465,7 +492,7 @@ __device__ int ls_locus(const ProblemDev& P, const OpDev* ops, const int32_t* op
             const T t2 = L.shfl(term, grp + 2), t3 = L.shfl(term, grp + 3);
             if (v == 0 && it0 + lane < nitem) {
                 const T total = Ar::add(Ar::add(Ar::add(Ar::add(T(0), t0), t1), t2), t3);
-                out[cell] = total;
+                A.st(ob + cell, total);
                 mx = total > mx ? total : mx;
             }
         }
@@ -482,12 +509,13 @@ __device__ int ls_locus(const ProblemDev& P, const OpDev* ops, const int32_t* op
                 const int ex = ilogbf((float)mx);
                 scale += ex;
                 const float f = scalbnf(1.0f, -ex);
-                for (int cell = lane; cell < ncell; cell += G) out[cell] = (T)((float)out[cell] * f);
+                L.sync();   // the cells other lanes of the group wrote (some maybe in the global spill)
+                for (int cell = lane; cell < ncell; cell += G) A.st(ob + cell, (T)((float)A.ld(ob + cell) * f));
             }
         }
         L.sync();
     }
-    const T root = A[off[P.K - 1]];
+    const T root = A.ld(off[P.K - 1]);
     if (root == T(0)) {
         if (lane == 0) set_status(status, ST_ZERO_LIK);
         L.sync();
@@ -618,13 +646,18 @@ __global__ void __launch_bounds__(128) lsampler_kernel(ProblemDev P, uint32_t* d
     ls_stage_tables(P, smem, ops, opd);
     __syncthreads();
     unsigned char* wsmem = smem + ls_tables_bytes(P) + (size_t)slot * ls_warp_bytes<T>(P);
+    T* spill = ls_spill_slice<T>(P, first, (int64_t)blockIdx.x * tpb + slot);
+    if (P.ls_spill_cells > 0 && !spill) {   // the launch has more task slots than the spill buffer: never run past it
+        if (lane == 0) set_status(status, ST_ILLEGAL_DG);
+        return;
+    }
     const int64_t ntask = (int64_t)nchain * nloci;
     for (int64_t t = (int64_t)blockIdx.x * tpb + slot; t < ntask; t += (int64_t)gridDim.x * tpb) {
         const int cr = (int)(t / nloci);
         if (sel && sel[cr] != want) continue;
         const int l = loci[t % nloci];
-        ls_locus<T, G>(P, ops, opd, dg, cr, first + cr, l, l > 0, l < P.M - 1, draws, l, 0, wsmem, lane, status,
-                       nullptr);
+        ls_locus<T, G>(P, ops, opd, dg, cr, first + cr, l, l > 0, l < P.M - 1, draws, l, 0, wsmem, spill, lane,
+                       status, nullptr);
     }
 }
 
@@ -648,6 +681,11 @@ __global__ void __launch_bounds__(128) si_kernel(ProblemDev P, uint32_t* dg, int
     ls_stage_tables(P, smem, ops, opd);
     __syncthreads();
     unsigned char* wsmem = smem + ls_tables_bytes(P) + (size_t)warp * ls_warp_bytes<T>(P);
+    T* spill = ls_spill_slice<T>(P, first, (int64_t)blockIdx.x * wpb + warp);
+    if (P.ls_spill_cells > 0 && !spill) {
+        if (lane == 0) set_status(status, ST_ILLEGAL_DG);
+        return;
+    }
     for (int t = blockIdx.x * wpb + warp; t < nchain * npass; t += gridDim.x * wpb) {
         const int cr = t % nchain, q = t / nchain;
         const int chain = first + cr, M = P.M, start = starts[t];
@@ -662,8 +700,8 @@ __global__ void __launch_bounds__(128) si_kernel(ProblemDev P, uint32_t* dg, int
             const bool hasL = v > start && l > 0;
             const bool hasR = v > 0 && v <= start && l < M - 1;
             double lr = 0.0;
-            const int used = ls_locus<T, 32>(P, ops, opd, dgq, cr, chain, l, hasL, hasR, dq, unit, base, wsmem, lane,
-                                         status, &lr);
+            const int used = ls_locus<T, 32>(P, ops, opd, dgq, cr, chain, l, hasL, hasR, dq, unit, base, wsmem,
+                                             spill, lane, status, &lr);
             if (used < 0) {
                 ok = false;
                 break;

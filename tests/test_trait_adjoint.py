@@ -223,30 +223,30 @@ def test_device_adjoint_large_pedigree(budget):
 def test_device_adjoint_400_member_pedigree_recomputes():
     """The 400-member, 10,000-SNP pedigree under the dominant model: its
     dense rfunctions and adjoints (about 92 KB per task) exceed the default
-    budget, so the default plan splits the peel into segments and the
-    interpreted forms recompute (the plan needs less than half the dense
-    footprint), while the compiled form keeps every rfunction in its global
-    arena; each of the thread form and the compiled form, on the starting
-    graph at sampled positions, against the host FP64 adjoint (which rescales
-    too: the plain peel underflows here)."""
+    budget, so the default plan splits the peel into segments and
+    recomputes; the device adjoint of the starting graph at sampled positions
+    against the host FP64 adjoint (which rescales too: the plain peel
+    underflows here); the plan needs less than half the dense footprint.
+    Its cutsets of five members rule out the compiled form."""
     from swiftlink_gb300 import pedigree, synth
     g = pedigree.problem_from_workload(synth.make_workload(5))
     d = with_model(g, *DOMINANT)
     n = g["n_lod"]
     dg = np.ascontiguousarray(g["dg0"], np.int32)
-    positions = [(l, o) for l in sample_loci(g["M"], 5) for o in range(n)]
-    want = host_all(d, dg, positions)
     with api.Context(api.Problem.from_arrays(d), n_chains=1) as ctx:
         seg, used = ctx.adjoint_memory(0)
         dense = 8 * sum(4 ** len(c) for c in g["op_cutset"])   # every matrix and its adjoint, FP32
         assert seg > 1 and used < dense // 2, (seg, used, dense)
-        for form in (api.SL_ADJOINT_THREAD, api.SL_ADJOINT_SPECIALISED):
-            ctx.adjoint_set_form(form)
-            grad, pt = ctx.trait_backward(dg[None])
-            got = np.array([grad[0, l, o] for l, o in positions])
-            for k in range(6):
-                assert rel_err(got[:, k], want[:, k]) <= GRAD_RTOL, (form, k, rel_err(got[:, k], want[:, k]))
-            np.testing.assert_allclose(pt, host_grad(d, None, 0, 0)[2:], rtol=GRAD_RTOL)
+        with pytest.raises(api.SwiftLinkError):
+            ctx.adjoint_set_form(api.SL_ADJOINT_SPECIALISED)
+        grad, pt = ctx.trait_backward(dg[None])
+        assert ctx.adjoint_info()[0] in (api.SL_ADJOINT_WARP, api.SL_ADJOINT_THREAD)
+    positions = [(l, o) for l in sample_loci(g["M"], 5) for o in range(n)]
+    want = host_all(d, dg, positions)
+    got = np.array([grad[0, l, o] for l, o in positions])
+    for k in range(6):
+        assert rel_err(got[:, k], want[:, k]) <= GRAD_RTOL, (k, rel_err(got[:, k], want[:, k]))
+    np.testing.assert_allclose(pt, host_grad(d, None, 0, 0)[2:], rtol=GRAD_RTOL)
 
 
 FORMS = [(api.SL_ADJOINT_WARP, 0), (api.SL_ADJOINT_THREAD, 0)] + \
