@@ -114,24 +114,17 @@ def host_kernel(src, tmp_path, tag):
     return ctypes.CDLL(so)
 
 
-@pytest.mark.skipif(shutil.which("g++") is None, reason="needs a host C++ compiler")
-@pytest.mark.parametrize("model", ["recessive", "dominant"])
-@pytest.mark.parametrize("name", CASES)
-def test_generated_adjoint_matches_host_fp64(name, model, tmp_path):
-    """Every position of the first golden graph, two blocks of threads (so
-    each thread's arena column holds several tasks one after another)."""
-    g = load_golden(name)
-    d = g if model == "recessive" else with_model(g, *DOMINANT)
+def run_host(d, graph, ntask, tmp_path, tag):
+    """The generated kernel of problem d over the first ntask positions of
+    graph, run on the host; returns its gradients [ntask][6]."""
     prob = api.Problem.from_arrays(d)
     desc = prob.desc()
     src, shapes, _ = source(desc)
     assert shapes >= 1
-    lib = host_kernel(src, str(tmp_path), f"{name}_{model}")
+    lib = host_kernel(src, str(tmp_path), tag)
     half = int(re.search(r"#define HB (\d+)", src).group(1)) // THREADS
-    N, F, M, n, K = int(g["N"]), int(g["F"]), int(g["M"]), int(g["n_lod"]), int(g["K"])
-    graph = np.ascontiguousarray(g["lod_graphs"][:1], np.int32)
-    pk = np.ascontiguousarray(pack(graph, N, F, M))
-    ntask = (M - 1) * n
+    N, F, M, K = int(d["N"]), int(d["F"]), int(d["M"]), len(d["op_cutset"])
+    pk = np.ascontiguousarray(pack(graph[None], N, F, M))
     blocks = 2
     grad = np.zeros((ntask, 6))
     status = np.zeros(1, np.int32)
@@ -147,14 +140,50 @@ def test_generated_adjoint_matches_host_fp64(name, model, tmp_path):
     run(blocks, P(pk), pk.shape[1] * pk.shape[2], 0, ntask, P(grad), P(status), P(partial), P(arena), P(dprob),
         P(dgrad), 0)
     assert status[0] == 0
+    return grad
+
+
+def host_fp64(d, graph, ntask):
+    desc = api.Problem.from_arrays(d).desc()
+    n = int(d["n_lod"])
     want = np.zeros((ntask, 6))
     hb = api.lib().sl_problem_trait_backward_eval
     for u in range(ntask):
         l, o = divmod(u, n)
-        assert hb(ctypes.byref(desc), P(graph[0]), l, o, P(want[u])) == 0
+        assert hb(ctypes.byref(desc), graph.ctypes.data_as(ctypes.c_void_p), l, o,
+                  want[u].ctypes.data_as(ctypes.c_void_p)) == 0
+    return want
+
+
+def assert_close(grad, want):
     for k in range(6):
         err = np.linalg.norm(grad[:, k] - want[:, k]) / max(np.linalg.norm(want[:, k]), 1e-300)
         assert err <= GRAD_RTOL, (k, err)
+
+
+@pytest.mark.skipif(shutil.which("g++") is None, reason="needs a host C++ compiler")
+@pytest.mark.parametrize("model", ["recessive", "dominant"])
+@pytest.mark.parametrize("name", CASES)
+def test_generated_adjoint_matches_host_fp64(name, model, tmp_path):
+    """Every position of the first golden graph, two blocks of threads (so
+    each thread's arena column holds several tasks one after another)."""
+    g = load_golden(name)
+    d = g if model == "recessive" else with_model(g, *DOMINANT)
+    graph = np.ascontiguousarray(g["lod_graphs"][0], np.int32)
+    ntask = (int(g["M"]) - 1) * int(g["n_lod"])
+    assert_close(run_host(d, graph, ntask, tmp_path, f"{name}_{model}"), host_fp64(d, graph, ntask))
+
+
+@pytest.mark.skipif(shutil.which("g++") is None, reason="needs a host C++ compiler")
+def test_generated_adjoint_large_pedigree_matches_host_fp64(tmp_path):
+    """The 120-member, 2000-SNP pedigree under the dominant model (27
+    operation shapes, cutsets of up to four members, parent peels with
+    several children): its starting graph's first 60 positions."""
+    from swiftlink_gb300.workloads import load_problem
+    g = load_problem("cfg2")
+    d = with_model(g, *DOMINANT)
+    graph = np.ascontiguousarray(g["dg0"], np.int32)
+    assert_close(run_host(d, graph, 60, tmp_path, "cfg2"), host_fp64(d, graph, 60))
 
 
 @pytest.mark.parametrize("variant", range(api.SL_ADJOINT_VARIANTS))
