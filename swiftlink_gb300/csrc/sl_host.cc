@@ -32,6 +32,7 @@ namespace sl {
 // kernels (sl_kernels.cu)
 size_t lsampler_smem_per_warp(const ProblemDev& P);
 size_t lsampler_smem_shared(const ProblemDev& P);
+int lsampler_resident_tasks(const ProblemDev& P, int wpb);
 cudaError_t launch_lsampler(const ProblemDev& P, uint32_t* dg, int first, int nchain, const int32_t* loci,
                             int nloci, const double* u, int64_t ucs, int64_t uls, uint64_t seed, uint64_t iter,
                             const uint8_t* sel, int want, int* status, cudaStream_t s, int grid_cap, int wpb,
@@ -1373,6 +1374,7 @@ int sl_create(const sl_problem_desc* d, const sl_options* opt, sl_ctx** out) {
     // the L-sampler's compact rfunctions (ls_locus, sl_kernels.cu): at a
     // locus, op k's cells number 2^(the sum of its members' rank bits); the
     // warp's arena holds the most any locus needs
+    int ls_cap_try = 0;
     {
         auto rank_bits = [](int mask) {
             const int s = __builtin_popcount(mask);
@@ -1401,8 +1403,9 @@ int sl_create(const sl_problem_desc* d, const sl_options* opt, sl_ctx** out) {
         std::sort(per_locus.begin(), per_locus.end());
         int cap = per_locus[(size_t)((M - 1) * 0.98)];
         cap = (cap + 31) / 32 * 32;
-        P.ls_cap = (cap < most && most - cap >= most / 8) ? cap : most;
-        P.ls_spill_cells = most - P.ls_cap;
+        ls_cap_try = (cap < most && most - cap >= most / 8) ? cap : most;
+        P.ls_cap = most;
+        P.ls_spill_cells = 0;
         P.ls_spill_slots = 0;
         P.ls_spill_chains = 0;
         P.ls_spill = nullptr;
@@ -1479,7 +1482,20 @@ int sl_create(const sl_problem_desc* d, const sl_options* opt, sl_ctx** out) {
     P.n_lvl = (int32_t)lvl_off.size() - 1;
 
     // ---- launch shapes from the shared-memory footprint of one task
-    const size_t lsw = lsampler_smem_per_warp(P), lst = lsampler_smem_shared(P);
+    const size_t lst = lsampler_smem_shared(P);
+    if (ls_cap_try < P.ls_arena) {
+        // the split arena only where it keeps a tenth more tasks resident (where
+        // registers, not shared memory, bound the residency it would only cost)
+        auto wpb_for = [&]() {
+            return (int)std::max<size_t>(1, std::min<size_t>(4, (kSmemBudget - lst) / lsampler_smem_per_warp(P)));
+        };
+        const int whole = lsampler_resident_tasks(P, wpb_for());
+        P.ls_cap = ls_cap_try;
+        const int split = lsampler_resident_tasks(P, wpb_for());
+        if (split * 10 < whole * 11) P.ls_cap = P.ls_arena;
+        P.ls_spill_cells = P.ls_arena - P.ls_cap;
+    }
+    const size_t lsw = lsampler_smem_per_warp(P);
     const size_t lodw = (size_t)arena * (ctx->lod_precision == SL_LOD_FP32_RESCALED ? 4 : 8);
     if (lst + lsw > kSmemBudget || lodw > kSmemBudget)
         return bail(fail(nullptr, SL_EINVAL, "peel sequence needs %zu bytes per task, above the shared-memory budget",

@@ -3208,6 +3208,38 @@ static cudaError_t launch_lsampler_g(const ProblemDev& P, uint32_t* dg, int firs
     return cudaGetLastError();
 }
 
+// The most L-sampler tasks an SM keeps resident, over the three lane groups,
+// for blocks of wpb warps' worth of tasks (launch_lsampler's shapes): the
+// occupancy of each kernel with its shared memory and registers.
+template <typename T, int G>
+static int ls_resident_g(const ProblemDev& P, int wpb) {
+    const int tpb = wpb * (32 / G);
+    const size_t smem = ls_tables_bytes(P) + (size_t)tpb * ls_warp_bytes<T>(P);
+    if (ensure_smem((const void*)lsampler_kernel<T, G>, smem) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    int blocks = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, (const void*)lsampler_kernel<T, G>, wpb * 32, smem) !=
+        cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return blocks * tpb;
+}
+
+template <typename T>
+static int ls_resident_t(const ProblemDev& P, int wpb) {
+    const int a = ls_resident_g<T, 32>(P, wpb);
+    const int b = ls_resident_g<T, 16>(P, wpb > 1 ? wpb / 2 : 1);
+    const int c = ls_resident_g<T, 8>(P, wpb > 3 ? wpb / 4 : 1);
+    return std::max(a, std::max(b, c));
+}
+
+int lsampler_resident_tasks(const ProblemDev& P, int wpb) {
+    return P.ls_fast ? ls_resident_t<float>(P, wpb) : ls_resident_t<double>(P, wpb);
+}
+
 // lanes = 32, 16 or 8 lanes per (chain, locus) task; all draw the same graphs.
 cudaError_t launch_lsampler(const ProblemDev& P, uint32_t* dg, int first, int nchain, const int32_t* loci, int nloci,
                             const double* u, int64_t ucs, int64_t uls, uint64_t seed, uint64_t iter,
