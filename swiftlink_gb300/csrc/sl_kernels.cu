@@ -1,10 +1,11 @@
 // sm_103a kernels for the SwiftLink MCMC hot path.
 //
 // Samplers (one chain's descent graph per chain, bit-packed [chain][M][W]):
-//  * lsampler_kernel<T>   -- L-sampler, one warp per (chain, locus): T=double
-//                            with the reference's operation order (bit-exact
-//                            decisions), T=float the batched form.  The form
-//                            compiled per pedigree lives in sl_lsjit.cc.
+//  * lsampler_kernel<T,G> -- L-sampler, one group of G = 32, 16 or 8 lanes per
+//                            (chain, locus): T=double with the reference's
+//                            operation order (bit-exact decisions), T=float
+//                            the batched form.  The form compiled per
+//                            pedigree lives in sl_lsjit.cc.
 //  * si_kernel<T>, si_select_kernel -- sequential imputation passes (one-sided
 //                            L-steps from a start locus) and the best pass.
 //  * fag_kernel           -- M-sampler likelihoods, thread per (chain, locus):
@@ -23,7 +24,10 @@
 //                            and carries the exponent.
 //  * lod_prog_kernel      -- the FP32 rescaled peel as a slot-program
 //                            interpreter (specialised forms: sl_jit.cc).
-//  * trait_adjoint_kernel -- the hand-written adjoint of the rescaled peel.
+//  * trait_adjoint_kernel, trait_adjoint_thr_kernel -- the hand-written
+//                            adjoint of the rescaled peel, a warp or a thread
+//                            per task (the form compiled per pedigree lives
+//                            in sl_adjjit.cc).
 //  * lod_merge_kernel, chain_merge_kernel -- FP64 log-sum accumulation.
 // Run graph: run_init / chain_iter / chain_advance kernels drive each chain's
 // WHILE and SWITCH nodes; choose / shuffle / set_key draw the iteration's
