@@ -421,6 +421,16 @@ int sl_adjoint_set_form(sl_ctx* ctx, int32_t form, int32_t variant);
  * failed); any pointer may be NULL. */
 int sl_adjoint_kernel_info(sl_ctx* ctx, int32_t* shapes, int32_t* variant, int32_t* regs, double* compile_ms);
 
+/* The batched LOD scorer specialised to a problem (the kernel sl_create
+ * compiles for an SL_LOD_FP32_RESCALED context), as CUDA C++ source (no
+ * device needed): values in registers (shared = 0) or in a per-thread
+ * shared-memory arena (shared = 1), `threads` per block (a multiple of 32),
+ * lod_flags as sl_options' (SL_LOD_ZERO_OK).  Up to cap - 1 bytes and a
+ * terminating zero into buf (buf may be NULL with cap 0), its length into
+ * *len and the program's float slots into *slots; either may be NULL. */
+int sl_problem_lod_source(const sl_problem_desc* problem, int32_t shared, int32_t threads, int32_t lod_flags,
+                          char* buf, int64_t cap, int64_t* len, int32_t* slots);
+
 /* The specialised adjoint's CUDA C++ source for a problem (no device
  * needed), one of its SL_ADJOINT_VARIANTS variants (0: compiled for 4 blocks
  * of 128 threads per SM, 1: for 8): up to cap - 1 bytes and a terminating

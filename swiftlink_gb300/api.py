@@ -38,6 +38,7 @@ EXPORTED = [
     "sl_chain_loglik", "sl_peel_sequence", "sl_batch_create", "sl_batch_run", "sl_batch_destroy",
     "sl_sequential_imputation", "sl_sequential_imputation_run", "sl_adjoint_memory", "sl_adjoint_info",
     "sl_adjoint_set_form", "sl_adjoint_kernel_info", "sl_problem_adjoint_source", "sl_ls_tuning",
+    "sl_problem_lod_source",
 ]
 
 

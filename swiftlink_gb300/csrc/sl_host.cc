@@ -2701,6 +2701,33 @@ int sl_problem_trait_backward_eval(const sl_problem_desc* d, const int32_t* dg, 
     return host_backward(d, prog, dg, locus, offset, grad, nullptr);
 }
 
+int sl_problem_lod_source(const sl_problem_desc* d, int32_t shared, int32_t threads, int32_t lod_flags, char* buf,
+                          int64_t cap, int64_t* len, int32_t* slots) {
+    int rc = check_desc(d);
+    if (rc) return rc;
+    if (cap < 0 || (cap > 0 && !buf)) return fail(nullptr, SL_EINVAL, "bad buffer");
+    if (threads < 32 || threads > 1024 || threads % 32) return fail(nullptr, SL_EINVAL, "bad threads per block %d", threads);
+    std::vector<OpDev> ops;
+    std::vector<int32_t> od;
+    int arena = 0, max_child = 1;
+    if ((rc = build_ops(d, ops, od, arena, max_child))) return rc;
+    LodProgram prog;
+    compile_lod_program(d, ops, od, prog);
+    const int N = d->n_members, F = d->n_founders;
+    const JitProgramIn in{prog.words.data(), prog.words.size(), prog.consts.data(), F, d->n_markers,
+                          d->lod_per_interval, (2 * (N - F) + 31) / 32, N - F, prog.slots,
+                          std::log(0.5) * (2 * (N - F)), (lod_flags & SL_LOD_ZERO_OK) ? 1 : 0};
+    const std::string src = jit_lod_source(in, threads, shared != 0);
+    if (len) *len = (int64_t)src.size();
+    if (slots) *slots = prog.slots;
+    if (buf && cap > 0) {
+        const size_t n = std::min<size_t>(src.size(), (size_t)cap - 1);
+        std::memcpy(buf, src.data(), n);
+        buf[n] = 0;
+    }
+    return SL_OK;
+}
+
 int sl_problem_adjoint_source(const sl_problem_desc* d, int32_t variant, int32_t compile, char* buf, int64_t cap,
                               int64_t* len, int32_t* shapes, double* compile_ms) {
     int rc = check_desc(d);

@@ -29,6 +29,7 @@ inline double __longlong_as_double(long long i) {
     std::memcpy(&d, &i, 8);
     return d;
 }
+inline int __popc(unsigned x) { return __builtin_popcount(x); }
 inline int atomicCAS(int* p, int c, int v) {
     const int o = *p;
     if (o == c) *p = v;
