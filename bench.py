@@ -390,7 +390,10 @@ def issue_estimate(C, it0, it1, seed, lprob, n_meioses, sm_mhz, sms, seconds, co
     return out
 
 
-def timed_lod(ctx, stream, flush, G, npos, reps):
+def timed_lod(ctx, stream, flush, G, npos, reps, allmax=None):
+    """Positions/s of one scoring of the context's chains (reps timed
+    scorings, L2 flushed before each), the time the slowest rank's when
+    allmax reduces over ranks."""
     import torch
     ctx.lod_score_chains()
     ctx.synchronize()
@@ -404,6 +407,8 @@ def timed_lod(ctx, stream, flush, G, npos, reps):
             evs[i][1].record(stream)
     ctx.synchronize()
     t = sum(a.elapsed_time(b) for a, b in evs) / 1e3
+    if allmax is not None:
+        t = allmax(t)
     return reps * G * npos / t
 
 
@@ -535,14 +540,14 @@ def run_ours(args):
     # ---------------- LOD positions/s: batched (all chains' graphs per launch, FP32-rescaled)
     # against plain (one graph per launch, FP64 with rescaling: the plain FP64 peel
     # underflows at every position of this pedigree, as the reference's does)
-    lod_pos_s = timed_lod(ctx, stream, flush, C, npos, reps=5)
+    lod_pos_s = timed_lod(ctx, stream, flush, C, npos, reps=5, allmax=allmax)
     lsel, ljit_ms = ctx.lod_kernel_info()
     ls_lanes, ls_t = ctx.ls_tuning()
     pctx = api.Context(prob, n_chains=1, lod_precision=api.SL_LOD_FP64_RESCALED, device=local,
                        lod_flags=api.SL_LOD_ZERO_OK)
     pctx.set_graphs(graphs[:1])
     pstream = torch.cuda.ExternalStream(pctx.stream_handle())
-    plain_lod_pos_s = timed_lod(pctx, pstream, flush, 1, npos, reps=3)
+    plain_lod_pos_s = timed_lod(pctx, pstream, flush, 1, npos, reps=3, allmax=allmax)
 
     # ---------------- FP32 error: one scoring of the chains' graphs in FP32 against FP64 with rescaling
     ctx.lod_reset()
@@ -580,7 +585,7 @@ def run_ours(args):
         with torch.cuda.stream(xstream):
             evx[i][1].record(xstream)
     xctx.synchronize()
-    plain_steps_s = Kx / (sum(a.elapsed_time(b) for a, b in evx) / 1e3)
+    plain_steps_s = Kx / allmax(sum(a.elapsed_time(b) for a, b in evx) / 1e3)
     xctx.close()
 
     # ---------------- end to end through the public API with host buffers: every step
