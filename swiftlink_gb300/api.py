@@ -205,6 +205,7 @@ class Problem:
             s.disease_freq = self.freq
             for i in range(3):
                 s.penetrance[i] = self.penetrance[i]
+        s._arrays = k   # the descriptor's pointers stay valid while it lives, even past this Problem
         return s
 
 
