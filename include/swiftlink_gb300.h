@@ -427,9 +427,12 @@ int sl_adjoint_kernel_info(sl_ctx* ctx, int32_t* shapes, int32_t* variant, int32
  * shared-memory arena (shared = 1), `threads` per block (a multiple of 32),
  * lod_flags as sl_options' (SL_LOD_ZERO_OK).  Up to cap - 1 bytes and a
  * terminating zero into buf (buf may be NULL with cap 0), its length into
- * *len and the program's float slots into *slots; either may be NULL. */
+ * *len and the program's float slots into *slots; with compile != 0 it is
+ * also compiled with NVRTC for sm_103a (milliseconds into *compile_ms;
+ * SL_EINVAL with the compiler's log when it fails).  Any output pointer may
+ * be NULL. */
 int sl_problem_lod_source(const sl_problem_desc* problem, int32_t shared, int32_t threads, int32_t lod_flags,
-                          char* buf, int64_t cap, int64_t* len, int32_t* slots);
+                          int32_t compile, char* buf, int64_t cap, int64_t* len, int32_t* slots, double* compile_ms);
 
 /* The specialised adjoint's CUDA C++ source for a problem (no device
  * needed), one of its SL_ADJOINT_VARIANTS variants (0: compiled for 4 blocks

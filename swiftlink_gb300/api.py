@@ -94,6 +94,13 @@ def lib():
         L.sl_launch_count.argtypes = [_vp]
         L.sl_destroy.argtypes = [_vp]
         L.sl_destroy.restype = None
+        P = ctypes.POINTER
+        L.sl_problem_adjoint_source.argtypes = [P(ProblemDesc), ctypes.c_int32, ctypes.c_int32, ctypes.c_char_p,
+                                                ctypes.c_int64, P(ctypes.c_int64), P(ctypes.c_int32),
+                                                P(ctypes.c_double)]
+        L.sl_problem_lod_source.argtypes = [P(ProblemDesc), ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                            ctypes.c_int32, ctypes.c_char_p, ctypes.c_int64, P(ctypes.c_int64),
+                                            P(ctypes.c_int32), P(ctypes.c_double)]
         _lib = L
     return _lib
 

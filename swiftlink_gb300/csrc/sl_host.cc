@@ -2701,8 +2701,8 @@ int sl_problem_trait_backward_eval(const sl_problem_desc* d, const int32_t* dg, 
     return host_backward(d, prog, dg, locus, offset, grad, nullptr);
 }
 
-int sl_problem_lod_source(const sl_problem_desc* d, int32_t shared, int32_t threads, int32_t lod_flags, char* buf,
-                          int64_t cap, int64_t* len, int32_t* slots) {
+int sl_problem_lod_source(const sl_problem_desc* d, int32_t shared, int32_t threads, int32_t lod_flags,
+                          int32_t compile, char* buf, int64_t cap, int64_t* len, int32_t* slots, double* compile_ms) {
     int rc = check_desc(d);
     if (rc) return rc;
     if (cap < 0 || (cap > 0 && !buf)) return fail(nullptr, SL_EINVAL, "bad buffer");
@@ -2724,6 +2724,13 @@ int sl_problem_lod_source(const sl_problem_desc* d, int32_t shared, int32_t thre
         const size_t n = std::min<size_t>(src.size(), (size_t)cap - 1);
         std::memcpy(buf, src.data(), n);
         buf[n] = 0;
+    }
+    if (compile) {
+        const auto t0 = std::chrono::steady_clock::now();
+        const std::shared_ptr<const JitBinary> bin = jit_binary(src, shared ? "sl_lod_jit_smem.cu" : "sl_lod_jit_reg.cu");
+        if (compile_ms)
+            *compile_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        if (bin->rc) return fail(nullptr, SL_EINVAL, "the specialised LOD scorer did not compile: %s", bin->log.c_str());
     }
     return SL_OK;
 }

@@ -167,10 +167,32 @@ std::string jit_source(const JitProgramIn& in, int threads, bool shared) {
             emitf(s, "    const float mx%d = %s;\n", k, mx.c_str());
             emitf(s, "    const int e%d = mx%d > 0.0f ? ilogbf(mx%d) - %d : 0;\n    scale += e%d;\n", k, k, k,
                   target, k);
-            for (int q = 0; q < cnt; ++q) {
-                const std::string old = ref(first + q);
-                s += def(first + q) + "ldexpf(" + old + ", -e" + std::to_string(k) + ");\n";
+            // 2^-e as a float when it is a normal number (nearly always): a product
+            // with it is exact, or rounded once where the result is subnormal, as
+            // ldexpf rounds; ldexpf only where 2^-e itself is out of range
+            emitf(s, "    const float sc%d = (e%d >= -127 && e%d <= 126) ? __int_as_float((127 - e%d) << 23) : 0.0f;\n",
+                  k, k, k, k);
+            std::vector<std::string> olds(cnt), news(cnt);
+            for (int q = 0; q < cnt; ++q) olds[q] = ref(first + q);
+            if (shared) {
+                for (int q = 0; q < cnt; ++q) news[q] = olds[q];
+            } else {
+                std::string decl = "    float ";
+                for (int q = 0; q < cnt; ++q) {
+                    const int slot = first + q;
+                    if (slot >= (int)cur.size()) cur.resize(slot + 1, -1);
+                    cur[slot] = next++;
+                    news[q] = "v" + std::to_string(cur[slot]);
+                    decl += (q ? ", " : "") + news[q];
+                }
+                s += decl + ";\n";
             }
+            emitf(s, "    if (sc%d != 0.0f) {\n", k);
+            for (int q = 0; q < cnt; ++q) emitf(s, "      %s = %s * sc%d;\n", news[q].c_str(), olds[q].c_str(), k);
+            s += "    } else {\n";
+            for (int q = 0; q < cnt; ++q)
+                emitf(s, "      %s = ldexpf(%s, -e%d);\n", news[q].c_str(), olds[q].c_str(), k);
+            s += "    }\n";
         } else {   // LI_END
             const int rs = pc[1];
             result = rs >= 0 ? ref(rs) : std::string("0.0f");

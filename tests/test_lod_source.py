@@ -59,12 +59,15 @@ extern "C" void host_run(unsigned blocks, const u32* graphs, long long gw, int G
 '''
 
 
-def lod_source(desc):
+def lod_source(desc, shared=0, compile_=False):
     f = api.lib().sl_problem_lod_source
     n = ctypes.c_int64()
-    assert f(ctypes.byref(desc), 0, THREADS, api.SL_LOD_ZERO_OK, None, 0, ctypes.byref(n), None) == 0
+    assert f(ctypes.byref(desc), shared, THREADS, api.SL_LOD_ZERO_OK, 0, None, 0, ctypes.byref(n), None, None) == 0
     buf = ctypes.create_string_buffer(n.value + 1)
-    assert f(ctypes.byref(desc), 0, THREADS, api.SL_LOD_ZERO_OK, buf, n.value + 1, None, None) == 0
+    ms = ctypes.c_double()
+    rc = f(ctypes.byref(desc), shared, THREADS, api.SL_LOD_ZERO_OK, int(compile_), buf, n.value + 1, None, None,
+           ctypes.byref(ms))
+    assert rc == 0, api.lib().sl_last_error(None)
     return buf.value.decode()
 
 
@@ -126,3 +129,13 @@ def test_generated_lod_kernel_large_pedigree(tmp_path):
     assert api.lib().sl_problem_legal_masks(ctypes.byref(desc), g["legal"].ctypes.data_as(ctypes.c_void_p)) == 0
     g["trait_prior"] = port.derive_priors(g["genotypes"], g["typed"], g["minor"])
     check_against_port(g, g["dg0"][None], tmp_path)
+
+
+@pytest.mark.parametrize("shared", [0, 1])
+def test_generated_lod_kernel_compiles_for_sm103a(shared):
+    """Both storage forms of the 30-member case through NVRTC for sm_103a (no
+    device needed)."""
+    g = load_golden("cfg1")
+    prob = api.Problem.from_arrays(g)
+    src = lod_source(prob.desc(), shared=shared, compile_=True)
+    assert "sl_lod_jit" in src and ("extern __shared__" in src) == bool(shared)
