@@ -139,3 +139,48 @@ def test_generated_lod_kernel_compiles_for_sm103a(shared):
     prob = api.Problem.from_arrays(g)
     src = lod_source(prob.desc(), shared=shared, compile_=True)
     assert "sl_lod_jit" in src and ("extern __shared__" in src) == bool(shared)
+
+
+@pytest.mark.skipif(shutil.which("g++") is None, reason="needs a host C++ compiler")
+@pytest.mark.parametrize("name", CASES)
+def test_generated_lod_kernel_forms_agree(name, tmp_path):
+    """The shared-memory form (values in a per-thread column of the block's
+    arena, immediate offsets) against the register form on the host: the
+    same operations in the same order, so the same values."""
+    g = load_golden(name)
+    prob = api.Problem.from_arrays(g)
+    N, F, M, n = int(g["N"]), int(g["F"]), int(g["M"]), int(g["n_lod"])
+    graphs = np.ascontiguousarray(g["lod_graphs"], np.int32)
+    G = graphs.shape[0]
+    pk = np.ascontiguousarray(pack(graphs, N, F, M))
+    npos = (M - 1) * n
+    theta = np.asarray(g["theta"], np.float64)
+    partial = np.asarray(g["partial"], np.float32)
+    lt, la = np.log(theta), np.log(1.0 - theta)
+    P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    out = []
+    for shared in (0, 1):
+        desc = prob.desc()
+        slots = ctypes.c_int32()
+        f = api.lib().sl_problem_lod_source
+        ln = ctypes.c_int64()
+        assert f(ctypes.byref(desc), shared, THREADS, api.SL_LOD_ZERO_OK, 0, None, 0, ctypes.byref(ln),
+                 ctypes.byref(slots), None) == 0
+        src = lod_source(desc, shared=shared)
+        # the block's shared arena as a host array: the emulated threads run one after another
+        arena = "" if not shared else "float sh[%d];\n" % (THREADS * max(1, slots.value))
+        path, so = os.path.join(tmp_path, f"lod{shared}.cc"), os.path.join(tmp_path, f"lod{shared}.so")
+        with open(path, "w") as fh:
+            fh.write('#include "cuda_host_prelude.h"\n' + arena + src.replace("extern __shared__ float sh[];", "")
+                     + DRIVER)
+        subprocess.run(["g++", "-O1", "-shared", "-fPIC", "-I", HERE, "-o", so, path], check=True)
+        lib = ctypes.CDLL(so)
+        vals = np.zeros(G * npos)
+        status = np.zeros(1, np.int32)
+        run = lib.host_run
+        run.argtypes = [ctypes.c_uint, ctypes.c_void_p, ctypes.c_longlong, ctypes.c_int, ctypes.c_void_p,
+                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+        run(1, P(pk), M * pk.shape[2], G, P(vals), P(status), P(partial), P(lt), P(la))
+        assert status[0] == 0
+        out.append(vals)
+    assert np.array_equal(out[0], out[1])
